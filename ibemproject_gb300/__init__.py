@@ -1,0 +1,145 @@
+"""GB300-native (sm_103a) implementation of the 3D elastic spherical iBEM path.
+
+The compute lives in ``libibem_gb300.so`` (CUDA kernels + C ABI, ``include/ibem_gb300.h``)
+and its C++ host layer (``host/ibem_plugins.*``), which mirrors the reference's
+integrator / BEMBuilder / systemSolver / postProcessor plugins.  This module loads the
+library with ctypes and exposes the C ABI to Python callers (tests, the bench); device
+buffers are passed as raw pointers (for example ``torch.Tensor.data_ptr()``).
+
+There is no CPU path: every entry point raises if the library is not built or a call
+fails.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libibem_gb300.so")
+
+IBEM_OK, IBEM_ERR_ARG, IBEM_ERR_CUDA, IBEM_ERR_NOCONV, IBEM_ERR_TIMEOUT, IBEM_ERR_SINGULAR, IBEM_ERR_IO = range(7)
+SOLVE_FP64, SOLVE_MIXED_IR = 0, 1
+
+_c_dp = ctypes.POINTER(ctypes.c_double)
+_c_ip = ctypes.POINTER(ctypes.c_int)
+_vp = ctypes.c_void_p
+_i64 = ctypes.c_int64
+_int = ctypes.c_int
+_dbl = ctypes.c_double
+
+
+class Material(ctypes.Structure):
+    _fields_ = [("E0", ctypes.c_double), ("nu0", ctypes.c_double),
+                ("E1", ctypes.c_double), ("nu1", ctypes.c_double)]
+
+
+class SolveReport(ctypes.Structure):
+    _fields_ = [("backward_error", ctypes.c_double), ("iterations", ctypes.c_int),
+                ("info", ctypes.c_int), ("t_factor_ms", ctypes.c_double),
+                ("t_solve_ms", ctypes.c_double)]
+
+
+class IbemError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"ibem status {status}: {msg}")
+        self.status = status
+
+
+# Every symbol the header declares, with its ctypes signature.
+SIGNATURES = {
+    "ibem_last_error": (ctypes.c_char_p, []),
+    "ibem_layout_size": (_int, [_int]),
+    "ibem_e3d_pair_blocks": (_int, [_vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _i64, _i64, _i64, _vp]),
+    "ibem_e3d_node_blocks": (_int, [_vp, _int, _vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _i64, _i64,
+                                    _i64, _vp]),
+    "ibem_e3d_bem_hg": (_int, [_vp, _int, _vp, _int, ctypes.POINTER(Material), _vp, _i64, _i64, _i64, _vp, _i64,
+                               _i64, _i64, _vp]),
+    "ibem_e3d_bem_to_incl": (_int, [_vp, _int, _vp, _int, _vp, _int, ctypes.POINTER(Material), _int, _vp, _i64,
+                                    _i64, _vp, _i64, _i64, _i64, _vp]),
+    "ibem_e3d_bc_plan": (_int, [_int, _int, _c_ip, _c_dp, _c_dp, _c_ip, _c_ip]),
+    "ibem_e3d_apply_bc": (_int, [_int, _int, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _vp]),
+    "ibem_e3d_get_ut": (_int, [_int, _int, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "ibem_e3d_farfield_rhs": (_int, [_int, ctypes.POINTER(Material), _int, _c_dp, _vp, _vp]),
+    "ibem_e3d_solve": (_int, [_int, _i64, _vp, _i64, _vp, _vp, _dbl, ctypes.POINTER(SolveReport), _vp]),
+    "ibem_e3d_field": (_int, [_vp, _int, _vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _vp, _int, _vp,
+                              _int, _vp, _vp, _c_dp, _vp, _vp]),
+    "ibem_e3d_run_host": (_int, [_int, _int, ctypes.POINTER(Material), _int, _c_dp, _int, _c_ip, _c_dp, _c_dp,
+                                 _int, _c_dp, _c_dp, _int, _c_dp, _c_dp, _dbl, _c_dp, _c_dp,
+                                 ctypes.POINTER(SolveReport)]),
+    "ibem_e3d_run_dir": (_int, [ctypes.c_char_p, _int, _int, _dbl, ctypes.POINTER(SolveReport)]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load libibem_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with ibemproject_gb300.build.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != IBEM_OK:
+        raise IbemError(status, lib().ibem_last_error().decode(errors="replace"))
+
+
+def material(E0, nu0, E1, nu1) -> Material:
+    return Material(E0, nu0, E1, nu1)
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_c_dp)
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(_c_ip)
+
+
+def run_host(case, layout: int = 78, form: int = SOLVE_FP64, tol: float = 1e-12):
+    """Whole pipeline through the host-buffer C ABI: returns (X, stress, report)."""
+    m = material(case.E0, case.nu0, case.E1, case.nu1)
+    N = 3 * case.NN + layout * case.num
+    X = np.zeros(N)
+    S = np.zeros((case.nump, 6))
+    rep = SolveReport()
+    f64 = lambda a, shape: np.ascontiguousarray(a if a is not None and np.size(a) else np.zeros(shape),
+                                                dtype=np.float64)
+    nodes = f64(case.nodes, 3)
+    conn = np.ascontiguousarray(case.conn if case.NE else np.zeros(4, np.int32), dtype=np.int32)
+    bc = f64(case.bc, 2)
+    tbc = f64(case.tbc, 24)
+    cen = f64(case.centers, 3)
+    rad = f64(case.radius, 1)
+    pts = f64(case.points, 3)
+    sig = np.ascontiguousarray(case.sig_inf, dtype=np.float64) if case.sig_inf is not None else None
+    check(lib().ibem_e3d_run_host(layout, form, ctypes.byref(m), case.NN, _dp(nodes), case.NE, _ip(conn),
+                                  _dp(bc), _dp(tbc), case.num, _dp(cen), _dp(rad), case.nump, _dp(pts),
+                                  _dp(sig) if sig is not None else None, tol, _dp(X), _dp(S),
+                                  ctypes.byref(rep)))
+    return X, S, rep
+
+
+def run_dir(path: str, layout: int = 78, form: int = SOLVE_FP64, tol: float = 1e-12) -> SolveReport:
+    rep = SolveReport()
+    check(lib().ibem_e3d_run_dir(path.encode(), layout, form, tol, ctypes.byref(rep)))
+    return rep
+
+
+def bc_plan(case):
+    ucol = np.zeros(3 * case.NN, dtype=np.int32)
+    tcol = np.zeros(12 * case.NE, dtype=np.int32)
+    conn = np.ascontiguousarray(case.conn, dtype=np.int32)
+    check(lib().ibem_e3d_bc_plan(case.NN, case.NE, _ip(conn), _dp(np.ascontiguousarray(case.bc, dtype=np.float64)),
+                                 _dp(np.ascontiguousarray(case.tbc, dtype=np.float64)), _ip(ucol), _ip(tcol)))
+    return ucol, tcol

@@ -106,30 +106,35 @@ def read_case(path: str) -> Case:
                 sig, title)
 
 
+def _f(v) -> str:
+    """Shortest round-trip decimal of a float (read back bit-exactly by strtod / >>)."""
+    return repr(float(v))
+
+
 def write_case(path: str, c: Case) -> None:
     os.makedirs(path, exist_ok=True)
     with open(os.path.join(path, "position.txt"), "w") as f:
-        f.write(f"{c.num}\n{c.E1!r}\n{c.nu1!r}\n")
+        f.write(f"{c.num}\n{_f(c.E1)}\n{_f(c.nu1)}\n")
         for p, a in zip(c.centers, c.radius):
-            f.write(f"{p[0]!r} {p[1]!r} {p[2]!r} {a!r}\n")
+            f.write(f"{_f(p[0])} {_f(p[1])} {_f(p[2])} {_f(a)}\n")
     with open(os.path.join(path, "BEM.txt"), "w") as f:
-        f.write(f"{c.title}\n{c.E0!r}\n{c.nu0!r}\n{c.NN}\n{c.NE}\n\n")
+        f.write(f"{c.title}\n{_f(c.E0)}\n{_f(c.nu0)}\n{c.NN}\n{c.NE}\n\n")
         for p in c.nodes:
-            f.write(f"{p[0]!r} {p[1]!r} {p[2]!r}\n")
+            f.write(f"{_f(p[0])} {_f(p[1])} {_f(p[2])}\n")
         for e in c.conn:
             f.write(" ".join(str(int(v)) for v in e) + "\n")
         for r in c.bc:
-            f.write(f"{int(r[0])} {r[1]!r}\n")
+            f.write(f"{int(r[0])} {_f(r[1])}\n")
         for r in c.tbc:
-            f.write(" ".join(str(int(v)) for v in r[:12]) + " " + " ".join(repr(float(v)) for v in r[12:]) + "\n")
+            f.write(" ".join(str(int(v)) for v in r[:12]) + " " + " ".join(_f(v) for v in r[12:]) + "\n")
     with open(os.path.join(path, "postprocess.txt"), "w") as f:
         f.write(f"{c.nump}\n")
         for p in c.points:
-            f.write(f"{p[0]!r} {p[1]!r} {p[2]!r}\n")
+            f.write(f"{_f(p[0])} {_f(p[1])} {_f(p[2])}\n")
     ff = os.path.join(path, "farfield.txt")
     if c.sig_inf is not None:
         with open(ff, "w") as f:
-            f.write(" ".join(repr(float(v)) for v in c.sig_inf) + "\n")
+            f.write(" ".join(_f(v) for v in c.sig_inf) + "\n")
     elif os.path.exists(ff):
         os.remove(ff)
 

@@ -1,0 +1,879 @@
+// Dense solve of the iBEM system (replaces systemSolverElastic3D::_solve,
+// systemSolverElastic3D.h:44-60, X = A.fullPivLu().solve(b)).
+//
+// Both forms first equilibrate A (row, then column max scaling): the raw iBEM matrix
+// spans ~47 decades, which partial pivoting alone cannot handle (full pivoting can).
+//
+//   IBEM_SOLVE_FP64      LU with partial pivoting of the scaled matrix in FP64.
+//   IBEM_SOLVE_MIXED_IR  LU with partial pivoting in FP32 (trailing updates on the tensor
+//                        cores with the split-BF16 "x3" scheme, FP32 accumulation), then
+//                        FP64 GMRES iterative refinement preconditioned by the FP32 factors;
+//                        FP64 is used for the residual b - A x and the GMRES arithmetic.
+//
+// LU structure: recursive on column halves (Toledo), so most flops sit in a few large
+// GEMMs.  Leaves are panels of <= 32 columns factorised by one cooperative kernel that
+// keeps the panel rows in shared memory across all SMs and needs one grid barrier per
+// column: every CTA publishes its best pivot candidate row (and the current diagonal row
+// if it owns it), then all CTAs pick the same pivot and swap/scale/update locally.
+// The grid barrier is a bounded spin: after kSpinLimit polls it raises an error flag and
+// every CTA returns, so a fault can end the kernel but never hang it.
+#include <cooperative_groups.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "ibem_internal.h"
+#include "solver.h"
+
+namespace ibem {
+namespace {
+
+constexpr int kPanelThreads = 256;
+constexpr int kLeaf = 32;                   // panel width of the recursion leaves
+constexpr long long kSpinLimit = 1LL << 22; // polls before a barrier gives up
+
+// ---------------------------------------------------------------- utilities
+template <typename T>
+__global__ void k_fill(T* p, int64_t n, T v) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+// row max |a_ij| (threads over rows: coalesced along columns)
+__global__ void k_rowmax(int64_t n, const double* __restrict__ A, int64_t lda, double* __restrict__ r) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double m = 0;
+  for (int64_t j = 0; j < n; ++j) m = fmax(m, fabs(A[j * lda + i]));
+  r[i] = m > 0 ? 1.0 / m : 1.0;
+}
+
+// column max |r_i a_ij| -> c_j (one block per column)
+__global__ void k_colmax(int64_t n, const double* __restrict__ A, int64_t lda, const double* __restrict__ r,
+                         double* __restrict__ c) {
+  __shared__ double sm[256];
+  const int64_t j = blockIdx.x;
+  double m = 0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(r[i] * A[j * lda + i]));
+  sm[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) c[j] = sm[0] > 0 ? 1.0 / sm[0] : 1.0;
+}
+
+// W = R A C in precision T (column-major, ldw)
+template <typename T>
+__global__ void k_scale_copy(int64_t n, const double* __restrict__ A, int64_t lda, const double* __restrict__ r,
+                             const double* __restrict__ c, T* __restrict__ W, int64_t ldw) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t j = blockIdx.y;
+  if (i >= n) return;
+  W[j * ldw + i] = (T)(r[i] * A[j * lda + i] * c[j]);
+}
+
+// ---------------------------------------------------------------- grid barrier
+struct GridSync {
+  unsigned int count;
+  unsigned int gen;
+  int err;
+};
+
+__device__ __forceinline__ bool grid_barrier(GridSync* gs, unsigned int nblocks, unsigned int& my_gen) {
+  __syncthreads();
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned int g = my_gen;
+    __threadfence();
+    if (atomicAdd(&gs->count, 1u) == nblocks - 1) {
+      gs->count = 0;
+      __threadfence();
+      atomicExch(&gs->gen, g + 1);
+    } else {
+      long long it = 0;
+      while (atomicAdd(&gs->gen, 0u) == g) {
+        if (++it > kSpinLimit || atomicAdd(&gs->err, 0) != 0) {
+          atomicExch(&gs->err, 1);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    my_gen = g + 1;
+    s_ok = ok && (atomicAdd(&gs->err, 0) == 0);
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// ---------------------------------------------------------------- panel kernel
+// Factorises the m x nb panel (nb <= kLeaf) at P with partial pivoting.  Scratch:
+//   cand  [2][gridDim.x][kLeaf + 2] of T (candidate rows: values, |pivot|, row index)
+//   rowj  [2][kLeaf] of T
+// ipiv[j] receives the absolute pivot row (kglob + panel row) of column j; info the
+// first zero pivot (1-based, absolute).  Rows are split evenly over CTAs and live in
+// dynamic shared memory.
+template <typename T>
+__global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int64_t lda, int m, int nb,
+                                                         int rows_per, T* __restrict__ cand, T* __restrict__ rowj,
+                                                         int* __restrict__ ipiv, int kglob, int* __restrict__ info,
+                                                         GridSync* gs) {
+  extern __shared__ unsigned char smem_raw[];
+  T* sp = reinterpret_cast<T*>(smem_raw);  // rows_per x kLeaf, row-major
+  __shared__ T s_pr[kLeaf];                 // pivot row
+  __shared__ T s_jr[kLeaf];                 // row j
+  __shared__ T s_bv[kPanelThreads / 32];
+  __shared__ int s_bi[kPanelThreads / 32];
+  __shared__ int s_piv;
+  const int cta = blockIdx.x, ncta = gridDim.x;
+  const int r0 = cta * rows_per;
+  const int nr = max(0, min(rows_per, m - r0));
+  unsigned int my_gen = 0;
+  for (int idx = threadIdx.x; idx < nr * nb; idx += blockDim.x) {
+    const int rr = idx % nr, cc = idx / nr;
+    sp[rr * kLeaf + cc] = P[(int64_t)cc * lda + r0 + rr];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int j = 0; j < nb; ++j) {
+    const int buf = j & 1;
+    // (a) local candidate: max |a_ij| over rows >= j owned here (first max wins)
+    T best = -1;
+    int bi = -1;
+    for (int rr = threadIdx.x; rr < nr; rr += blockDim.x) {
+      const int gr = r0 + rr;
+      if (gr < j) continue;
+      const T v = fabs(sp[rr * kLeaf + j]);
+      if (v > best) { best = v; bi = gr; }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      const T ov = __shfl_down_sync(0xffffffffu, best, off);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+      if (ov > best || (ov == best && oi >= 0 && (bi < 0 || oi < bi))) { best = ov; bi = oi; }
+    }
+    if (lane == 0) { s_bv[warp] = best; s_bi[warp] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T b = -1;
+      int i = -1;
+      for (int w = 0; w < kPanelThreads / 32; ++w)
+        if (s_bv[w] > b || (s_bv[w] == b && s_bi[w] >= 0 && (i < 0 || s_bi[w] < i))) { b = s_bv[w]; i = s_bi[w]; }
+      s_piv = i;
+      T* cd = cand + ((int64_t)buf * ncta + cta) * (kLeaf + 2);
+      cd[kLeaf] = b;
+      cd[kLeaf + 1] = (T)i;
+    }
+    __syncthreads();
+    {
+      T* cd = cand + ((int64_t)buf * ncta + cta) * (kLeaf + 2);
+      const int i = s_piv;
+      if (threadIdx.x < nb) cd[threadIdx.x] = (i >= 0) ? sp[(i - r0) * kLeaf + threadIdx.x] : (T)0;
+      if (j >= r0 && j < r0 + nr && threadIdx.x < nb) rowj[buf * kLeaf + threadIdx.x] = sp[(j - r0) * kLeaf + threadIdx.x];
+    }
+    // (b) one barrier per column
+    if (!grid_barrier(gs, ncta, my_gen)) return;
+    // (c) global pivot: identical choice in every CTA
+    if (threadIdx.x == 0) {
+      T b = -1;
+      int i = -1, src = -1;
+      for (int c = 0; c < ncta; ++c) {
+        const T* cd = cand + ((int64_t)buf * ncta + c) * (kLeaf + 2);
+        const T v = cd[kLeaf];
+        const int ci = (int)cd[kLeaf + 1];
+        if (ci < 0) continue;
+        if (v > b || (v == b && ci < i)) { b = v; i = ci; src = c; }
+      }
+      s_piv = i;
+      s_bi[0] = src;
+      if (cta == 0) {
+        ipiv[j] = kglob + i;
+        if (b == 0 && *info == 0) *info = kglob + j + 1;
+      }
+    }
+    __syncthreads();
+    const int piv = s_piv;
+    if (threadIdx.x < nb) {
+      s_pr[threadIdx.x] = cand[((int64_t)buf * ncta + s_bi[0]) * (kLeaf + 2) + threadIdx.x];
+      s_jr[threadIdx.x] = rowj[buf * kLeaf + threadIdx.x];
+    }
+    __syncthreads();
+    // (d) swap rows j and piv where they live
+    if (piv != j) {
+      if (piv >= r0 && piv < r0 + nr && threadIdx.x < nb) sp[(piv - r0) * kLeaf + threadIdx.x] = s_jr[threadIdx.x];
+      if (j >= r0 && j < r0 + nr && threadIdx.x < nb) sp[(j - r0) * kLeaf + threadIdx.x] = s_pr[threadIdx.x];
+    }
+    __syncthreads();
+    // (e) scale and rank-1 update of rows below j
+    const T pjj = s_pr[j];
+    if (pjj != (T)0) {
+      for (int rr = threadIdx.x; rr < nr; rr += blockDim.x) {
+        if (r0 + rr <= j) continue;
+        T* row = sp + rr * kLeaf;
+        const T l = row[j] / pjj;
+        row[j] = l;
+        for (int k = j + 1; k < nb; ++k) row[k] -= l * s_pr[k];
+      }
+    }
+    __syncthreads();
+  }
+  for (int idx = threadIdx.x; idx < nr * nb; idx += blockDim.x) {
+    const int rr = idx % nr, cc = idx / nr;
+    P[(int64_t)cc * lda + r0 + rr] = sp[rr * kLeaf + cc];
+  }
+}
+
+// apply the panel's row exchanges (rows k0+j <-> ipiv[j], j ascending) to columns [c0,c1)
+template <typename T>
+__global__ void k_laswp(T* __restrict__ A, int64_t lda, int64_t k0, const int* __restrict__ ipiv, int nb,
+                        int64_t c0, int64_t c1) {
+  const int64_t c = c0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= c1) return;
+  T* col = A + c * lda;
+  for (int j = 0; j < nb; ++j) {
+    const int64_t p = ipiv[j];
+    const int64_t q = k0 + j;
+    if (p != q) { const T t = col[q]; col[q] = col[p]; col[p] = t; }
+  }
+}
+
+// small triangular solve: B (n1 x n2) <- L^-1 B, L unit lower n1 x n1 (n1 <= 64);
+// one CTA per 64 columns of B, L staged in shared memory
+template <typename T>
+__global__ void __launch_bounds__(64) k_trsm_small(const T* __restrict__ L, int64_t ldl, int n1, T* __restrict__ B,
+                                                   int64_t ldb, int64_t n2) {
+  __shared__ T sL[64 * 64];
+  for (int idx = threadIdx.x; idx < n1 * n1; idx += blockDim.x) {
+    const int i = idx % n1, k = idx / n1;
+    sL[k * 64 + i] = L[(int64_t)k * ldl + i];
+  }
+  __syncthreads();
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= n2) return;
+  T* b = B + c * ldb;
+  T x[64];
+  for (int i = 0; i < n1; ++i) x[i] = b[i];
+  for (int i = 0; i < n1; ++i) {
+    const T xi = x[i];
+    for (int k = i + 1; k < n1; ++k) x[k] -= sL[i * 64 + k] * xi;
+  }
+  for (int i = 0; i < n1; ++i) b[i] = x[i];
+}
+
+// ---------------------------------------------------------------- SIMT GEMM  C -= A B
+// 64x64 tile, 256 threads, 4x4 outputs per thread, k-step 16.
+template <typename T>
+__global__ void __launch_bounds__(256) k_gemm_sub(int64_t m, int64_t n, int64_t k, const T* __restrict__ A,
+                                                  int64_t lda, const T* __restrict__ B, int64_t ldb,
+                                                  T* __restrict__ C, int64_t ldc) {
+  __shared__ T sA[16][64 + 1];
+  __shared__ T sB[16][64 + 1];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int64_t i0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
+  T acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0;
+  for (int64_t kk = 0; kk < k; kk += 16) {
+    for (int idx = threadIdx.x; idx < 16 * 64; idx += 256) {
+      const int r = idx % 64, c = idx / 64;
+      const int64_t gi = i0 + r, gk = kk + c;
+      sA[c][r] = (gi < m && gk < k) ? A[gk * lda + gi] : (T)0;
+      const int rk = idx % 16, cj = idx / 16;
+      const int64_t gk2 = kk + rk, gj = j0 + cj;
+      sB[rk][cj] = (gk2 < k && gj < n) ? B[gj * ldb + gk2] : (T)0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      T av[4], bv[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) av[a] = sA[t][tx + 16 * a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) bv[b] = sB[t][ty + 16 * b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int64_t gi = i0 + tx + 16 * a, gj = j0 + ty + 16 * b;
+      if (gi < m && gj < n) C[gj * ldc + gi] -= acc[a][b];
+    }
+}
+
+// ---------------------------------------------------------------- vectors
+// y[i] = b[i] - sum_j A[i,j] x[j] over a column chunk; partial sums summed by k_sum_parts
+__global__ void k_gemv_part(int64_t n, const double* __restrict__ A, int64_t lda, const double* __restrict__ x,
+                            int64_t chunk, double* __restrict__ part) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+  if (i >= n) return;
+  double s0 = 0, s1 = 0;
+  int64_t j = j0;
+  for (; j + 1 < j1; j += 2) {
+    s0 += A[j * lda + i] * x[j];
+    s1 += A[(j + 1) * lda + i] * x[j + 1];
+  }
+  if (j < j1) s0 += A[j * lda + i] * x[j];
+  part[blockIdx.y * n + i] = s0 + s1;
+}
+__global__ void k_residual(int64_t n, int nparts, const double* __restrict__ part, const double* __restrict__ b,
+                           double* __restrict__ r) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0;
+  for (int p = 0; p < nparts; ++p) s += part[p * n + i];
+  r[i] = b[i] - s;
+}
+
+// blocked forward/backward substitution with the factors in precision T.
+// Diagonal block solve: one CTA; then GEMV update of the rows below/above.
+template <typename T>
+__global__ void k_trsv_diag(const T* __restrict__ F, int64_t ldf, int64_t k0, int nb, double* __restrict__ y,
+                            int lower) {
+  __shared__ double sy[64];
+  __shared__ double sF[64][65];
+  for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+    const int i = idx % nb, k = idx / nb;
+    sF[i][k] = (double)F[(k0 + k) * ldf + k0 + i];
+  }
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) sy[i] = y[k0 + i];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (lower) {
+      for (int i = 0; i < nb; ++i) {
+        double s = sy[i];
+        for (int k = 0; k < i; ++k) s -= sF[i][k] * sy[k];
+        sy[i] = s;
+      }
+    } else {
+      for (int i = nb - 1; i >= 0; --i) {
+        double s = sy[i];
+        for (int k = i + 1; k < nb; ++k) s -= sF[i][k] * sy[k];
+        sy[i] = s / sF[i][i];
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) y[k0 + i] = sy[i];
+}
+// y[r] -= sum_{k in [k0,k0+nb)} F[r,k] y[k] for rows r in [r0, r1)
+template <typename T>
+__global__ void k_trsv_update(const T* __restrict__ F, int64_t ldf, int64_t k0, int nb, int64_t r0, int64_t r1,
+                              double* __restrict__ y) {
+  const int64_t r = r0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= r1) return;
+  double s = 0;
+  for (int k = 0; k < nb; ++k) s += (double)F[(k0 + k) * ldf + r] * y[k0 + k];
+  y[r] -= s;
+}
+
+// out[i] = y[perm[i]]  (P y with P the row permutation of the factorisation)
+__global__ void k_gather(int64_t n, const int* __restrict__ perm, const double* __restrict__ y,
+                         double* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = y[perm[i]];
+}
+
+__global__ void k_vmul(int64_t n, const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = a[i] * b[i];
+}
+
+}  // namespace
+
+// =====================================================================================
+template <typename T>
+struct LuWork {
+  T* cand = nullptr;
+  T* rowj = nullptr;
+  int* ipiv_dev = nullptr;  // N entries (global, absolute row of each exchange)
+  int* perm = nullptr;      // N entries: row i of P A is row perm[i] of A
+  double* tmp = nullptr;    // N-vector scratch of lu_apply
+  int* info = nullptr;
+  GridSync* gs = nullptr;
+  int ncta = 0;
+  int rows_cap = 0;
+};
+
+template <typename T>
+static ibem_status panel(T* A, int64_t lda, int64_t k0, int64_t m, int nb, LuWork<T>& w, cudaStream_t st) {
+  // rows per CTA so that every CTA fits its rows in shared memory
+  int ncta = w.ncta;
+  int rows_per = (int)((m + ncta - 1) / ncta);
+  if (rows_per > w.rows_cap) return fail(IBEM_ERR_ARG, "panel too tall for shared memory");
+  if (rows_per < 1) rows_per = 1;
+  ncta = (int)((m + rows_per - 1) / rows_per);
+  size_t smem = (size_t)rows_per * kLeaf * sizeof(T);
+  // reset count and generation (not the sticky error flag) before every launch
+  IBEM_CUDA(cudaMemsetAsync(w.gs, 0, 2 * sizeof(unsigned int), st));
+  T* P = A + k0 * lda + k0;
+  int mm = (int)m;
+  int* ip = w.ipiv_dev + k0;
+  int kg = (int)k0;
+  void* args[] = {&P, &lda, &mm, &nb, &rows_per, &w.cand, &w.rowj, &ip, &kg, &w.info, &w.gs};
+  IBEM_CUDA(cudaLaunchCooperativeKernel((void*)k_panel<T>, dim3(ncta), dim3(kPanelThreads), args, smem, st));
+  return IBEM_OK;
+}
+
+template <typename T>
+static ibem_status gemm_sub(int64_t m, int64_t n, int64_t k, const T* A, int64_t lda, const T* B, int64_t ldb,
+                            T* C, int64_t ldc, cudaStream_t st);
+
+template <>
+ibem_status gemm_sub<double>(int64_t m, int64_t n, int64_t k, const double* A, int64_t lda, const double* B,
+                             int64_t ldb, double* C, int64_t ldc, cudaStream_t st) {
+  if (m <= 0 || n <= 0 || k <= 0) return IBEM_OK;
+  dim3 grid((unsigned)((m + 63) / 64), (unsigned)((n + 63) / 64));
+  k_gemm_sub<double><<<grid, 256, 0, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
+  IBEM_LAUNCH_CHECK("gemm f64");
+  return IBEM_OK;
+}
+
+template <>
+ibem_status gemm_sub<float>(int64_t m, int64_t n, int64_t k, const float* A, int64_t lda, const float* B,
+                            int64_t ldb, float* C, int64_t ldc, cudaStream_t st) {
+  if (m <= 0 || n <= 0 || k <= 0) return IBEM_OK;
+  dim3 grid((unsigned)((m + 63) / 64), (unsigned)((n + 63) / 64));
+  k_gemm_sub<float><<<grid, 256, 0, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
+  IBEM_LAUNCH_CHECK("gemm f32");
+  return IBEM_OK;
+}
+
+// B (n1 x n2) <- L^-1 B with L the unit-lower n1 x n1 block at L (recursive)
+template <typename T>
+static ibem_status trsm(const T* L, int64_t ldl, int64_t n1, T* B, int64_t ldb, int64_t n2, cudaStream_t st) {
+  if (n1 <= 0 || n2 <= 0) return IBEM_OK;
+  if (n1 <= 64) {
+    k_trsm_small<T><<<(unsigned)((n2 + 63) / 64), 64, 0, st>>>(L, ldl, (int)n1, B, ldb, n2);
+    IBEM_LAUNCH_CHECK("trsm_small");
+    return IBEM_OK;
+  }
+  const int64_t h = std::max<int64_t>(kLeaf, (n1 / 2) / kLeaf * kLeaf);
+  ibem_status s = trsm(L, ldl, h, B, ldb, n2, st);
+  if (s) return s;
+  s = gemm_sub<T>(n1 - h, n2, h, L + h, ldl, B, ldb, B + h, ldb, st);
+  if (s) return s;
+  return trsm(L + h * ldl + h, ldl, n1 - h, B + h, ldb, n2, st);
+}
+
+// recursive LU of the m x n column block starting at (k0, k0) of A (m = N - k0).
+template <typename T>
+static ibem_status lu_rec(T* A, int64_t lda, int64_t N, int64_t k0, int64_t n, LuWork<T>& w, cudaStream_t st) {
+  const int64_t m = N - k0;
+  if (n <= kLeaf) {
+    ibem_status s = panel(A, lda, k0, m, (int)n, w, st);
+    if (s) return s;
+    // exchanges of this panel on the columns to its left and right (within [0, N))
+    if (k0 > 0) k_laswp<T><<<(unsigned)((k0 + 127) / 128), 128, 0, st>>>(A, lda, k0, w.ipiv_dev + k0, (int)n, 0, k0);
+    if (k0 + n < N)
+      k_laswp<T><<<(unsigned)((N - k0 - n + 127) / 128), 128, 0, st>>>(A, lda, k0, w.ipiv_dev + k0, (int)n, k0 + n, N);
+    IBEM_LAUNCH_CHECK("laswp");
+    return IBEM_OK;
+  }
+  const int64_t n1 = std::max<int64_t>(kLeaf, (n / 2) / kLeaf * kLeaf), n2 = n - n1;
+  // left half (its exchanges are applied to every column, including the right half)
+  ibem_status s = lu_rec(A, lda, N, k0, n1, w, st);
+  if (s) return s;
+  T* A11 = A + k0 * lda + k0;
+  T* A12 = A + (k0 + n1) * lda + k0;
+  T* A21 = A + k0 * lda + k0 + n1;
+  T* A22 = A + (k0 + n1) * lda + k0 + n1;
+  s = trsm(A11, lda, n1, A12, lda, n2, st);
+  if (s) return s;
+  s = gemm_sub<T>(m - n1, n2, n1, A21, lda, A12, lda, A22, lda, st);
+  if (s) return s;
+  return lu_rec(A, lda, N, k0 + n1, n2, w, st);
+}
+
+template <typename T>
+static ibem_status lu_alloc(LuWork<T>& w, int64_t N) {
+  int dev = 0, nsm = 0, smem_optin = 0;
+  IBEM_CUDA(cudaGetDevice(&dev));
+  IBEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  IBEM_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const int static_smem = 2 * kLeaf * (int)sizeof(T) + 64;
+  int dyn_cap = std::min(smem_optin - static_smem - 1024, 200 * 1024);
+  w.rows_cap = dyn_cap / (kLeaf * (int)sizeof(T));
+  IBEM_CUDA(cudaFuncSetAttribute((const void*)k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_cap));
+  int per_sm = 0;
+  IBEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_panel<T>, kPanelThreads,
+                                                          (size_t)w.rows_cap * kLeaf * sizeof(T)));
+  if (per_sm < 1) return fail(IBEM_ERR_CUDA, "panel kernel cannot be resident");
+  w.ncta = nsm;  // one CTA per SM (all co-resident for the cooperative launch)
+  if ((int64_t)w.ncta * w.rows_cap < N) return fail(IBEM_ERR_ARG, "matrix too large for the panel kernel");
+  IBEM_CUDA(cudaMalloc(&w.cand, sizeof(T) * 2 * (size_t)w.ncta * (kLeaf + 2)));
+  IBEM_CUDA(cudaMalloc(&w.rowj, sizeof(T) * 2 * kLeaf));
+  IBEM_CUDA(cudaMalloc(&w.ipiv_dev, sizeof(int) * (size_t)N));
+  IBEM_CUDA(cudaMalloc(&w.perm, sizeof(int) * (size_t)N));
+  IBEM_CUDA(cudaMalloc(&w.tmp, sizeof(double) * (size_t)N));
+  IBEM_CUDA(cudaMalloc(&w.info, sizeof(int)));
+  IBEM_CUDA(cudaMalloc(&w.gs, sizeof(GridSync)));
+  IBEM_CUDA(cudaMemset(w.info, 0, sizeof(int)));
+  IBEM_CUDA(cudaMemset(w.gs, 0, sizeof(GridSync)));
+  return IBEM_OK;
+}
+
+template <typename T>
+static void lu_free(LuWork<T>& w) {
+  cudaFree(w.cand);
+  cudaFree(w.rowj);
+  cudaFree(w.ipiv_dev);
+  cudaFree(w.perm);
+  cudaFree(w.tmp);
+  cudaFree(w.info);
+  cudaFree(w.gs);
+  w = LuWork<T>();
+}
+
+// Solve with the factors F (precision T): y <- U^-1 L^-1 P y (y FP64, in place)
+template <typename T>
+static ibem_status lu_apply(const T* F, int64_t ldf, int64_t N, const int* perm, double* tmp, double* y,
+                            cudaStream_t st) {
+  k_gather<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, perm, y, tmp);
+  IBEM_CUDA(cudaMemcpyAsync(y, tmp, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+  const int nb = 64;
+  for (int64_t k0 = 0; k0 < N; k0 += nb) {
+    const int b = (int)std::min<int64_t>(nb, N - k0);
+    k_trsv_diag<T><<<1, 64, 0, st>>>(F, ldf, k0, b, y, 1);
+    if (k0 + b < N)
+      k_trsv_update<T><<<(unsigned)((N - k0 - b + 255) / 256), 256, 0, st>>>(F, ldf, k0, b, k0 + b, N, y);
+  }
+  for (int64_t k0 = ((N - 1) / nb) * nb; k0 >= 0; k0 -= nb) {
+    const int b = (int)std::min<int64_t>(nb, N - k0);
+    k_trsv_diag<T><<<1, 64, 0, st>>>(F, ldf, k0, b, y, 0);
+    if (k0 > 0) k_trsv_update<T><<<(unsigned)((k0 + 255) / 256), 256, 0, st>>>(F, ldf, k0, b, 0, k0, y);
+  }
+  IBEM_LAUNCH_CHECK("lu_apply");
+  return IBEM_OK;
+}
+
+// r = b - A x  (FP64)
+static ibem_status residual(int64_t N, const double* A, int64_t lda, const double* x, const double* b, double* r,
+                            double* part, int nparts, cudaStream_t st) {
+  const int64_t chunk = (N + nparts - 1) / nparts;
+  dim3 grid((unsigned)((N + 255) / 256), (unsigned)nparts);
+  k_gemv_part<<<grid, 256, 0, st>>>(N, A, lda, x, chunk, part);
+  k_residual<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, nparts, part, b, r);
+  IBEM_LAUNCH_CHECK("residual");
+  return IBEM_OK;
+}
+
+
+// ------------------------------------------------------------------ device vectors
+namespace {
+__global__ void k_dot_many(int64_t n, int nv, const double* __restrict__ V, int64_t ldv, const double* __restrict__ w,
+                           double* __restrict__ out) {
+  // out[j] += sum_i V[i,j] w[i]  (grid-stride over rows, one atomic per block and vector)
+  __shared__ double red[256];
+  for (int j = 0; j < nv; ++j) {
+    double s = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+      s += V[j * ldv + i] * w[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int t = blockDim.x / 2; t > 0; t >>= 1) {
+      if (threadIdx.x < t) red[threadIdx.x] += red[threadIdx.x + t];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(out + j, red[0]);
+    __syncthreads();
+  }
+}
+// w -= V h (h on device, nv entries); y = alpha x
+__global__ void k_sub_Vh(int64_t n, int nv, const double* __restrict__ V, int64_t ldv, const double* __restrict__ h,
+                         double* __restrict__ w) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0;
+  for (int j = 0; j < nv; ++j) s += V[j * ldv + i] * h[j];
+  w[i] -= s;
+}
+__global__ void k_axpby(int64_t n, double a, const double* __restrict__ x, double b, double* __restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = a * x[i] + b * y[i];
+}
+__global__ void k_absmax_rowsum(int64_t n, const double* __restrict__ A, int64_t lda, double* __restrict__ rs) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0;
+  for (int64_t j = 0; j < n; ++j) s += fabs(A[j * lda + i]);
+  rs[i] = s;
+}
+}  // namespace
+
+static double host_absmax(const std::vector<double>& v) {
+  double m = 0;
+  for (double x : v) m = std::max(m, std::fabs(x));
+  return m;
+}
+
+struct SolveCtx {
+  int64_t N;
+  cudaStream_t st;
+  double *r = nullptr, *c = nullptr, *part = nullptr, *rs = nullptr;
+  int nparts = 16;
+  ibem_status alloc(int64_t n, cudaStream_t s) {
+    N = n;
+    st = s;
+    IBEM_CUDA(cudaMalloc(&r, sizeof(double) * N));
+    IBEM_CUDA(cudaMalloc(&c, sizeof(double) * N));
+    IBEM_CUDA(cudaMalloc(&rs, sizeof(double) * N));
+    IBEM_CUDA(cudaMalloc(&part, sizeof(double) * N * nparts));
+    return IBEM_OK;
+  }
+  ~SolveCtx() {
+    cudaFree(r);
+    cudaFree(c);
+    cudaFree(part);
+    cudaFree(rs);
+  }
+};
+
+static ibem_status vec_to_host(const double* d, int64_t n, std::vector<double>& h, cudaStream_t st) {
+  h.resize(n);
+  IBEM_CUDA(cudaMemcpyAsync(h.data(), d, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  IBEM_CUDA(cudaStreamSynchronize(st));
+  return IBEM_OK;
+}
+
+// backward error ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf); anorm = ||A||_inf
+static ibem_status backward_error(SolveCtx& cx, const double* A, int64_t lda, const double* x, const double* b,
+                                  double* rvec, double anorm, double& be) {
+  ibem_status s = residual(cx.N, A, lda, x, b, rvec, cx.part, cx.nparts, cx.st);
+  if (s) return s;
+  std::vector<double> hr, hx, hb;
+  if ((s = vec_to_host(rvec, cx.N, hr, cx.st))) return s;
+  if ((s = vec_to_host(x, cx.N, hx, cx.st))) return s;
+  if ((s = vec_to_host(b, cx.N, hb, cx.st))) return s;
+  be = host_absmax(hr) / (anorm * host_absmax(hx) + host_absmax(hb));
+  return IBEM_OK;
+}
+
+template <typename T>
+static ibem_status factor(SolveCtx& cx, const double* A, int64_t lda, T*& W, LuWork<T>& w, int& info) {
+  const int64_t N = cx.N;
+  k_rowmax<<<(unsigned)((N + 255) / 256), 256, 0, cx.st>>>(N, A, lda, cx.r);
+  k_colmax<<<(unsigned)N, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c);
+  IBEM_LAUNCH_CHECK("equilibrate");
+  IBEM_CUDA(cudaMalloc(&W, sizeof(T) * (size_t)N * N));
+  dim3 g((unsigned)((N + 255) / 256), (unsigned)N);
+  k_scale_copy<T><<<g, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c, W, N);
+  IBEM_LAUNCH_CHECK("scale_copy");
+  ibem_status s = lu_alloc(w, N);
+  if (s) return s;
+  s = lu_rec<T>(W, N, N, 0, N, w, cx.st);
+  if (s) return s;
+  // row permutation from the sequence of exchanges (LAPACK ipiv semantics)
+  {
+    std::vector<int> ip((size_t)N), perm((size_t)N);
+    IBEM_CUDA(cudaMemcpyAsync(ip.data(), w.ipiv_dev, sizeof(int) * N, cudaMemcpyDeviceToHost, cx.st));
+    IBEM_CUDA(cudaStreamSynchronize(cx.st));
+    for (int64_t i = 0; i < N; ++i) perm[i] = (int)i;
+    for (int64_t i = 0; i < N; ++i) {
+      const int p = ip[i];
+      if (p < 0 || p >= N) return fail(IBEM_ERR_CUDA, "factorisation produced an invalid pivot");
+      std::swap(perm[i], perm[p]);
+    }
+    IBEM_CUDA(cudaMemcpyAsync(w.perm, perm.data(), sizeof(int) * N, cudaMemcpyHostToDevice, cx.st));
+    IBEM_CUDA(cudaStreamSynchronize(cx.st));
+  }
+  int hinfo = 0;
+  GridSync hgs;
+  IBEM_CUDA(cudaMemcpyAsync(&hinfo, w.info, sizeof(int), cudaMemcpyDeviceToHost, cx.st));
+  IBEM_CUDA(cudaMemcpyAsync(&hgs, w.gs, sizeof(GridSync), cudaMemcpyDeviceToHost, cx.st));
+  IBEM_CUDA(cudaStreamSynchronize(cx.st));
+  if (hgs.err) return fail(IBEM_ERR_TIMEOUT, "panel grid barrier gave up");
+  info = hinfo;
+  return IBEM_OK;
+}
+
+// z <- C (LU)^-1 R v  (the scaled-system preconditioner), z and v FP64
+template <typename T>
+static ibem_status precond(SolveCtx& cx, const T* W, const LuWork<T>& w, const double* v, double* z) {
+  const unsigned nb = (unsigned)((cx.N + 255) / 256);
+  k_vmul<<<nb, 256, 0, cx.st>>>(cx.N, cx.r, v, z);
+  ibem_status s = lu_apply<T>(W, cx.N, cx.N, w.perm, w.tmp, z, cx.st);
+  if (s) return s;
+  k_vmul<<<nb, 256, 0, cx.st>>>(cx.N, cx.c, z, z);
+  IBEM_LAUNCH_CHECK("precond");
+  return IBEM_OK;
+}
+
+ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda, const double* b, double* x,
+                        double tol, ibem_solve_report* rep, cudaStream_t st) {
+  if (N <= 0 || !A || !b || !x || lda < N) return fail(IBEM_ERR_ARG, "solve: bad sizes or pointers");
+  SolveCtx cx;
+  ibem_status s = cx.alloc(N, st);
+  if (s) return s;
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  k_absmax_rowsum<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, A, lda, cx.rs);
+  std::vector<double> hrs;
+  if ((s = vec_to_host(cx.rs, N, hrs, st))) return s;
+  const double anorm = host_absmax(hrs);
+  double* rvec = nullptr;
+  IBEM_CUDA(cudaMalloc(&rvec, sizeof(double) * N));
+  ibem_solve_report R{};
+  cudaEventRecord(e0, st);
+  if (form == IBEM_SOLVE_FP64) {
+    double* W = nullptr;
+    LuWork<double> w;
+    int info = 0;
+    s = factor<double>(cx, A, lda, W, w, info);
+    cudaEventRecord(e1, st);
+    if (!s) {
+      R.info = info;
+      if (info) s = fail(IBEM_ERR_SINGULAR, "zero pivot in the FP64 factorisation");
+    }
+    if (!s) s = precond<double>(cx, W, w, b, x);
+    cudaEventRecord(e2, st);
+    if (!s) s = backward_error(cx, A, lda, x, b, rvec, anorm, R.backward_error);
+    lu_free(w);
+    cudaFree(W);
+  } else if (form == IBEM_SOLVE_MIXED_IR) {
+    float* W = nullptr;
+    LuWork<float> w;
+    int info = 0;
+    s = factor<float>(cx, A, lda, W, w, info);
+    cudaEventRecord(e1, st);
+    if (!s) {
+      R.info = info;
+      if (info) s = fail(IBEM_ERR_SINGULAR, "zero pivot in the FP32 factorisation");
+    }
+    // FGMRES(m) on A d = r with the right preconditioner M^-1 = C (LU)^-1 R, FP64
+    const int m = 30, max_outer = 20;
+    double *V = nullptr, *Z = nullptr, *hd = nullptr;
+    if (!s) {
+      cudaError_t ce = cudaMalloc(&V, sizeof(double) * (size_t)N * (m + 1));
+      if (ce == cudaSuccess) ce = cudaMalloc(&Z, sizeof(double) * (size_t)N * m);
+      if (ce == cudaSuccess) ce = cudaMalloc(&hd, sizeof(double) * (m + 1) * 2);
+      if (ce != cudaSuccess) s = cuda_fail(ce, "gmres workspace");
+    }
+    if (!s) s = precond<float>(cx, W, w, b, x);
+    int iters = 0;
+    const unsigned nb = (unsigned)((N + 255) / 256);
+    for (int outer = 0; !s && outer < max_outer; ++outer) {
+      double be = 0;
+      if ((s = backward_error(cx, A, lda, x, b, rvec, anorm, be))) break;
+      R.backward_error = be;
+      if (be <= tol) break;
+      std::vector<double> hr;
+      if ((s = vec_to_host(rvec, N, hr, st))) break;
+      double beta = 0;
+      for (double v : hr) beta += v * v;
+      beta = std::sqrt(beta);
+      if (beta == 0) break;
+      k_axpby<<<nb, 256, 0, st>>>(N, 1.0 / beta, rvec, 0.0, V);
+      std::vector<double> H((m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0);
+      g[0] = beta;
+      int k = 0;
+      for (; k < m; ++k) {
+        double* vk = V + (size_t)k * N;
+        double* zk = Z + (size_t)k * N;
+        double* wv = V + (size_t)(k + 1) * N;
+        if ((s = precond<float>(cx, W, w, vk, zk))) break;
+        // wv = A zk
+        {
+          const int64_t chunk = (N + cx.nparts - 1) / cx.nparts;
+          dim3 grid(nb, (unsigned)cx.nparts);
+          k_gemv_part<<<grid, 256, 0, st>>>(N, A, lda, zk, chunk, cx.part);
+          IBEM_CUDA(cudaMemsetAsync(rvec, 0, sizeof(double) * N, st));
+          k_residual<<<nb, 256, 0, st>>>(N, cx.nparts, cx.part, rvec, wv);  // wv = 0 - A zk
+          k_axpby<<<nb, 256, 0, st>>>(N, 0.0, wv, -1.0, wv);                // wv = A zk
+        }
+        // classical Gram-Schmidt, twice
+        std::vector<double> hk(k + 1, 0.0), h2(k + 1);
+        for (int pass = 0; pass < 2; ++pass) {
+          IBEM_CUDA(cudaMemsetAsync(hd, 0, sizeof(double) * (k + 1), st));
+          k_dot_many<<<256, 256, 0, st>>>(N, k + 1, V, N, wv, hd);
+          k_sub_Vh<<<nb, 256, 0, st>>>(N, k + 1, V, N, hd, wv);
+          IBEM_CUDA(cudaMemcpyAsync(h2.data(), hd, sizeof(double) * (k + 1), cudaMemcpyDeviceToHost, st));
+          IBEM_CUDA(cudaStreamSynchronize(st));
+          for (int i = 0; i <= k; ++i) hk[i] += h2[i];
+        }
+        IBEM_CUDA(cudaMemsetAsync(hd, 0, sizeof(double), st));
+        k_dot_many<<<256, 256, 0, st>>>(N, 1, wv, N, wv, hd);
+        double nrm2 = 0;
+        IBEM_CUDA(cudaMemcpyAsync(&nrm2, hd, sizeof(double), cudaMemcpyDeviceToHost, st));
+        IBEM_CUDA(cudaStreamSynchronize(st));
+        const double hn = std::sqrt(std::max(nrm2, 0.0));
+        if (hn > 0) k_axpby<<<nb, 256, 0, st>>>(N, 1.0 / hn, wv, 0.0, wv);
+        for (int i = 0; i <= k; ++i) H[i * m + k] = hk[i];
+        H[(k + 1) * m + k] = hn;
+        // Givens rotations on column k
+        for (int i = 0; i < k; ++i) {
+          const double t = cs[i] * H[i * m + k] + sn[i] * H[(i + 1) * m + k];
+          H[(i + 1) * m + k] = -sn[i] * H[i * m + k] + cs[i] * H[(i + 1) * m + k];
+          H[i * m + k] = t;
+        }
+        const double den = std::hypot(H[k * m + k], H[(k + 1) * m + k]);
+        cs[k] = den > 0 ? H[k * m + k] / den : 1.0;
+        sn[k] = den > 0 ? H[(k + 1) * m + k] / den : 0.0;
+        H[k * m + k] = den;
+        H[(k + 1) * m + k] = 0;
+        g[k + 1] = -sn[k] * g[k];
+        g[k] = cs[k] * g[k];
+        ++iters;
+        if (std::fabs(g[k + 1]) <= 1e-3 * tol * beta || hn == 0) { ++k; break; }
+      }
+      if (s) break;
+      // y = H^-1 g (upper triangular k x k), x += Z y
+      std::vector<double> y(k, 0.0);
+      for (int i = k - 1; i >= 0; --i) {
+        double t = g[i];
+        for (int j2 = i + 1; j2 < k; ++j2) t -= H[i * m + j2] * y[j2];
+        y[i] = t / H[i * m + i];
+      }
+      IBEM_CUDA(cudaMemcpyAsync(hd, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, st));
+      k_axpby<<<nb, 256, 0, st>>>(N, -1.0, x, 0.0, x);  // x = -x
+      k_sub_Vh<<<nb, 256, 0, st>>>(N, k, Z, N, hd, x);  // x = -x - Z y
+      k_axpby<<<nb, 256, 0, st>>>(N, -1.0, x, 0.0, x);  // x = x + Z y
+      IBEM_LAUNCH_CHECK("gmres update");
+    }
+    cudaEventRecord(e2, st);
+    if (!s) {
+      double be = 0;
+      s = backward_error(cx, A, lda, x, b, rvec, anorm, be);
+      R.backward_error = be;
+      if (!s && be > tol) s = fail(IBEM_ERR_NOCONV, "GMRES-IR did not reach the tolerance");
+    }
+    R.iterations = iters;
+    cudaFree(V);
+    cudaFree(Z);
+    cudaFree(hd);
+    lu_free(w);
+    cudaFree(W);
+  } else {
+    s = fail(IBEM_ERR_ARG, "unknown solver form");
+  }
+  cudaStreamSynchronize(st);
+  float t1 = 0, t2 = 0;
+  cudaEventElapsedTime(&t1, e0, e1);
+  cudaEventElapsedTime(&t2, e1, e2);
+  R.t_factor_ms = t1;
+  R.t_solve_ms = t2;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  cudaFree(rvec);
+  if (rep) *rep = R;
+  return s;
+}
+
+}  // namespace ibem

@@ -1,0 +1,19 @@
+// Internal interface of the dense solver (solver.cu) and its tensor-core GEMM (gemm_tc.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ibem_internal.h"
+
+namespace ibem {
+
+// C (m x n, ldc) -= A (m x k, lda) B (k x n, ldb), FP32 storage, column-major, computed on
+// the tensor cores with each operand split into two BF16 terms (hi + lo) and the three
+// products hi*hi + hi*lo + lo*hi accumulated in FP32.
+ibem_status gemm_sub_f32_tc(int64_t m, int64_t n, int64_t k, const float* A, int64_t lda, const float* B,
+                            int64_t ldb, float* C, int64_t ldc, cudaStream_t st);
+
+ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda, const double* b, double* x,
+                        double tol, ibem_solve_report* rep, cudaStream_t st);
+
+}  // namespace ibem

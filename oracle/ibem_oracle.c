@@ -622,8 +622,66 @@ int orc_bem_hg(int NN, const double* nodes, int NE, const int* conn, const orc_m
  * 780-980, 429-672, 37-322) with the contrast (dlam, dmu); the post-processing
  * variant (postProcessorElastic3D.cpp:32-114) is dlam = lam0, dmu = mu0, nder = 0.
  * Rows t = (k<=l) x W (W the nder derivative indices, last fastest); Dsu/Dst [t][n]. */
+/* All derivatives of 1/R (orders 0..kmax_i) and R (orders 0..kmax_r) at x, stored as
+ * full 3^k tensors (index digits, first index slowest). */
+typedef struct {
+  double* inv[7];
+  double* len[9];
+  double buf[3 * 2187 + 3 * 729];
+} GCache;
+
+static void gcache_fill(GCache* g, const double* x, int kmax_i, int kmax_r) {
+  double r = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+  double* p = g->buf;
+  int idx[12];
+  for (int k = 0; k <= kmax_i; ++k) {
+    int lim = 1;
+    for (int t = 0; t < k; ++t) lim *= 3;
+    g->inv[k] = p;
+    for (int f = 0; f < lim; ++f) {
+      int q = f;
+      for (int t = k - 1; t >= 0; --t) { idx[t] = q % 3; q /= 3; }
+      p[f] = dPow(x, r, -1.0, idx, k);
+    }
+    p += lim;
+  }
+  for (int k = 0; k <= kmax_r; ++k) {
+    int lim = 1;
+    for (int t = 0; t < k; ++t) lim *= 3;
+    g->len[k] = p;
+    for (int f = 0; f < lim; ++f) {
+      int q = f;
+      for (int t = k - 1; t >= 0; --t) { idx[t] = q % 3; q /= 3; }
+      p[f] = dPow(x, r, 1.0, idx, k);
+    }
+    p += lim;
+  }
+}
+
+static inline int flat(const int* idx, int k) {
+  int f = 0;
+  for (int t = 0; t < k; ++t) f = 3 * f + idx[t];
+  return f;
+}
+
+/* d_K G_ij from the cache (same formula as dGreen) */
+static double dGreenC(const GCache* g, const Mat* M, int i, int j, const int* K, int k) {
+  int idx[12];
+  double v = 0;
+  if (i == j) v += g->inv[k][flat(K, k)] / (4 * ORC_PI * M->mu0);
+  idx[0] = i;
+  idx[1] = j;
+  memcpy(idx + 2, K, sizeof(int) * k);
+  v -= g->len[k + 2][flat(idx, k + 2)] / (16 * ORC_PI * M->mu0 * (1 - M->nu0));
+  return v;
+}
+
 static void stress_kernel(const double* x, const Mat* M, double dlam, double dmu, int nder,
                           const double* nv, double* Dsu, double* Dst) {
+  GCache gc;
+  gcache_fill(&gc, x, 2 + nder, 4 + nder);
+#define dGreen(x_, M_, i_, j_, K_, k_) dGreenC(&gc, M_, i_, j_, K_, k_)
+
   int nW = nder == 0 ? 1 : (nder == 1 ? 3 : 9);
   double su = (nder % 2 == 0) ? 1.0 : -1.0; /* Dsu sign */
   double st = -su;                          /* Dst sign */
@@ -676,6 +734,7 @@ static void stress_kernel(const double* x, const Mat* M, double dlam, double dmu
         }
         ++t;
       }
+#undef dGreen
 }
 
 /* Integ3_stress{,1,2} (:982-1167, 674-778, 324-427): regular 8x8 quadrature over one
@@ -1002,5 +1061,14 @@ int orc_farfield_rhs(int num, const orc_mat* m, int layout, const double* sig_in
             v += (C0(&M, U[r].i, U[r].j, k, l) - C1(&M, U[r].i, U[r].j, k, l)) * eps[k][l];
       b[(int64_t)nu * h + r] = v;
     }
+  return 0;
+}
+
+/* Stress kernel at one Gauss point (for checking the CUDA code function by function);
+ * dlam/dmu = (C0 - C1) contrast, or (lam0, mu0) for the post-processing variant. */
+int orc_stress_kernel(const double* x, const double* nv, const orc_mat* m, double dlam,
+                      double dmu, int nder, double* Dsu, double* Dst) {
+  Mat M = mat_from(m);
+  stress_kernel(x, &M, dlam, dmu, nder, nv, Dsu, Dst);
   return 0;
 }

@@ -74,6 +74,8 @@ def lib():
         L.orc_post.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, ctypes.POINTER(OrcMat),
                                ctypes.c_int, _dp, ctypes.c_int, _dp, ctypes.c_int, _ip, _dp, _dp,
                                _dp, _dp]
+        L.orc_stress_kernel.argtypes = [_dp, _dp, ctypes.POINTER(OrcMat), ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_int, _dp, _dp]
         L.orc_farfield_rhs.argtypes = [ctypes.c_int, ctypes.POINTER(OrcMat), ctypes.c_int, _dp, _dp]
         _lib = L
     return _lib
@@ -209,3 +211,13 @@ def farfield_rhs(num, m, layout, sig_inf):
     lib().orc_farfield_rhs(num, ctypes.byref(m), layout,
                            _d(np.ascontiguousarray(sig_inf, dtype=np.float64)), _d(b))
     return b
+
+
+def stress_kernel(x, nv, m, dlam, dmu, nder):
+    nrow = 6 * 3 ** nder
+    Dsu = np.zeros(nrow * 3)
+    Dst = np.zeros(nrow * 3)
+    lib().orc_stress_kernel(_d(np.ascontiguousarray(x, dtype=np.float64)),
+                            _d(np.ascontiguousarray(nv, dtype=np.float64)), ctypes.byref(m),
+                            float(dlam), float(dmu), nder, _d(Dsu), _d(Dst))
+    return Dsu.reshape(nrow, 3), Dst.reshape(nrow, 3)

@@ -1,0 +1,116 @@
+// Host build of the generated sphere code, for checking the generator against the
+// oracle without a GPU (compiled by tests/test_codegen_host.py with the host compiler).
+#include <string.h>
+#include "gen_sphere24.cuh"
+#include "gen_sphere60.cuh"
+#include "gen_sphere78.cuh"
+
+namespace {
+struct ArrSink {
+  double* out;
+  int nu;
+  void operator()(int r, int c, double v) { out[r * nu + c] += v; }
+};
+}  // namespace
+
+extern "C" int hg_pair_block(int layout, const double* x, double a, double E0, double nu0,
+                             double E1, double nu1, int self, double* out) {
+  SphMat mc = sph_mat_init(E0, nu0, E1, nu1);
+  int nu = layout;
+  memset(out, 0, sizeof(double) * nu * nu);
+  ArrSink s{out, nu};
+  if (layout == 24) {
+    sph_block24_c0_r0(x[0], x[1], x[2], a, mc, s); sph_block24_c0_r1(x[0], x[1], x[2], a, mc, s);
+    sph_block24_c1_r0(x[0], x[1], x[2], a, mc, s); sph_block24_c1_r1(x[0], x[1], x[2], a, mc, s);
+    if (self) sph_self24(mc, s);
+  } else if (layout == 78) {
+    sph_block78_c0_r0(x[0], x[1], x[2], a, mc, s); sph_block78_c0_r1(x[0], x[1], x[2], a, mc, s);
+    sph_block78_c0_r2(x[0], x[1], x[2], a, mc, s); sph_block78_c1_r0(x[0], x[1], x[2], a, mc, s);
+    sph_block78_c1_r1(x[0], x[1], x[2], a, mc, s); sph_block78_c1_r2(x[0], x[1], x[2], a, mc, s);
+    sph_block78_c2_r0(x[0], x[1], x[2], a, mc, s); sph_block78_c2_r1(x[0], x[1], x[2], a, mc, s);
+    sph_block78_c2_r2(x[0], x[1], x[2], a, mc, s);
+    if (self) sph_self78(mc, s);
+  } else if (layout == 60) {
+    sph_block60_c0_r0(x[0], x[1], x[2], a, mc, s); sph_block60_c0_r1(x[0], x[1], x[2], a, mc, s);
+    sph_block60_c0_r2(x[0], x[1], x[2], a, mc, s); sph_block60_c1_r0(x[0], x[1], x[2], a, mc, s);
+    sph_block60_c1_r1(x[0], x[1], x[2], a, mc, s); sph_block60_c1_r2(x[0], x[1], x[2], a, mc, s);
+    sph_block60_c2_r0(x[0], x[1], x[2], a, mc, s); sph_block60_c2_r1(x[0], x[1], x[2], a, mc, s);
+    sph_block60_c2_r2(x[0], x[1], x[2], a, mc, s);
+    if (self) sph_self60(mc, s);
+  } else {
+    return -1;
+  }
+  return 0;
+}
+
+extern "C" int hg_node(int layout, const double* x, double a, double E0, double nu0, double E1,
+                       double nu1, double* out /* 3 x layout */) {
+  SphMat mc = sph_mat_init(E0, nu0, E1, nu1);
+  memset(out, 0, sizeof(double) * 3 * layout);
+  ArrSink s{out, layout};
+  if (layout == 24) sph_node24(x[0], x[1], x[2], a, mc, s);
+  else if (layout == 78) sph_node78(x[0], x[1], x[2], a, mc, s);
+  else if (layout == 60) sph_node60(x[0], x[1], x[2], a, mc, s);
+  else return -1;
+  return 0;
+}
+
+extern "C" int hg_field(int layout, const double* x, double a, double E0, double nu0, double E1,
+                        double nu1, const double* E, double* e /* 6, accumulated */) {
+  SphMat mc = sph_mat_init(E0, nu0, E1, nu1);
+  if (layout == 24) sph_field24(x[0], x[1], x[2], a, mc, E, e);
+  else if (layout == 78) sph_field78(x[0], x[1], x[2], a, mc, E, e);
+  else if (layout == 60) sph_field60(x[0], x[1], x[2], a, mc, E, e);
+  else return -1;
+  return 0;
+}
+
+#include "gen_bem.cuh"
+
+// Dsu/Dst of all rows of one order (rows (k<=l) x W, W last), dofs fastest.
+extern "C" int hg_bem_stress(int order, const double* x, const double* nv, double E0, double nu0,
+                             double E1, double nu1, double dlam, double dmu, double* Dsu,
+                             double* Dst) {
+  BemMat bm = bem_mat_init(E0, nu0, E1, nu1);
+  double su[18], st[18];
+  int nW = order == 0 ? 1 : (order == 1 ? 3 : 9);
+#define CALL(fn)                                                                  \
+  fn(x[0], x[1], x[2], nv[0], nv[1], nv[2], bm, dlam, dmu, su, st);               \
+  for (int t = 0; t < 6; ++t) {                                                   \
+    Dsu[(t * nW + w) * 3 + n] = su[t * 3 + n];                                    \
+    Dst[(t * nW + w) * 3 + n] = st[t * 3 + n];                                    \
+  }
+  for (int w = 0; w < nW; ++w)
+    for (int n = 0; n < 3; ++n) {
+      if (order == 0) {
+        if (n == 0) { CALL(bem_stress_o0_w_n0) } else if (n == 1) { CALL(bem_stress_o0_w_n1) } else { CALL(bem_stress_o0_w_n2) }
+      } else if (order == 1) {
+        switch (w * 3 + n) {
+          case 0: { CALL(bem_stress_o1_w0_n0) } break; case 1: { CALL(bem_stress_o1_w0_n1) } break;
+          case 2: { CALL(bem_stress_o1_w0_n2) } break; case 3: { CALL(bem_stress_o1_w1_n0) } break;
+          case 4: { CALL(bem_stress_o1_w1_n1) } break; case 5: { CALL(bem_stress_o1_w1_n2) } break;
+          case 6: { CALL(bem_stress_o1_w2_n0) } break; case 7: { CALL(bem_stress_o1_w2_n1) } break;
+          case 8: { CALL(bem_stress_o1_w2_n2) } break;
+        }
+      } else {
+        switch (w * 3 + n) {
+#define C2(W, N, WS) case W * 3 + N: { CALL(bem_stress_o2_w##WS##_n##N) } break;
+          C2(0, 0, 00) C2(0, 1, 00) C2(0, 2, 00) C2(1, 0, 01) C2(1, 1, 01) C2(1, 2, 01)
+          C2(2, 0, 02) C2(2, 1, 02) C2(2, 2, 02) C2(3, 0, 10) C2(3, 1, 10) C2(3, 2, 10)
+          C2(4, 0, 11) C2(4, 1, 11) C2(4, 2, 11) C2(5, 0, 12) C2(5, 1, 12) C2(5, 2, 12)
+          C2(6, 0, 20) C2(6, 1, 20) C2(6, 2, 20) C2(7, 0, 21) C2(7, 1, 21) C2(7, 2, 21)
+          C2(8, 0, 22) C2(8, 1, 22) C2(8, 2, 22)
+#undef C2
+        }
+      }
+    }
+#undef CALL
+  return 0;
+}
+
+extern "C" int hg_bem_stress_post(const double* x, const double* nv, double E0, double nu0,
+                                  double E1, double nu1, double* Dsu, double* Dst) {
+  BemMat bm = bem_mat_init(E0, nu0, E1, nu1);
+  bem_stress_post(x[0], x[1], x[2], nv[0], nv[1], nv[2], bm, bm.lam0, bm.mu0, Dsu, Dst);
+  return 0;
+}

@@ -1,0 +1,116 @@
+"""The generated sphere / boundary code (ibemproject_gb300/csrc/gen_*.cuh), compiled for
+the host, against the oracle: same straight-line source the GPU kernels inline."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, scaled_err
+
+HG = os.path.join(ROOT, "tests", "hostgen")
+SO = os.path.join(HG, "_build", "libhostgen.so")
+MAT = (70e9, 0.3, 400e9, 0.2)
+
+
+@pytest.fixture(scope="module")
+def hg():
+    from ibemproject_gb300 import codegen
+    codegen.generate()
+    os.makedirs(os.path.dirname(SO), exist_ok=True)
+    subprocess.run(["g++", "-O0", "-shared", "-fPIC", "-I", os.path.join(ROOT, "ibemproject_gb300", "csrc"),
+                    "-o", SO, os.path.join(HG, "hostgen.cpp")], check=True)
+    return ctypes.CDLL(SO)
+
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _mat():
+    return [ctypes.c_double(v) for v in MAT]
+
+
+@pytest.mark.parametrize("layout", [24, 60, 78])
+def test_pair_blocks(hg, oracle_mod, layout):
+    m = oracle_mod.mat(*MAT)
+    cen = np.array([[0.5, 0.5, 0.5], [0.61, 0.47, 0.52], [0.41, 0.58, 0.44]])
+    rad = np.array([0.05, 0.04, 0.045])
+    A = oracle_mod.pair_blocks(cen, rad, m, layout)
+    nu = layout
+    for s in range(3):
+        for h in range(3):
+            x = np.ascontiguousarray(cen[s] - cen[h])
+            out = np.zeros(nu * nu)
+            hg.hg_pair_block(layout, d(x), ctypes.c_double(rad[h]), *_mat(), int(s == h), d(out))
+            assert scaled_err(out.reshape(nu, nu), A[nu * s:nu * s + nu, nu * h:nu * h + nu]) < 1e-13
+
+
+@pytest.mark.parametrize("layout", [24, 60, 78])
+def test_node_and_field(hg, oracle_mod, layout):
+    m = oracle_mod.mat(*MAT)
+    rng = np.random.default_rng(11)
+    for t in range(4):
+        x = rng.normal(size=3) * 0.2
+        a = 0.05
+        out = np.zeros(3 * layout)
+        hg.hg_node(layout, d(x), ctypes.c_double(a), *_mat(), d(out))
+        H = np.zeros((3, layout), order="F")
+        oracle_mod.lib().orc_node_blocks(1, d(np.ascontiguousarray(x)), 1, d(np.zeros(3)), d(np.array([a])),
+                                         ctypes.byref(m), layout, d(H), 3, 0, 0)
+        assert scaled_err(out.reshape(3, layout), H) < 1e-13
+    # field: one particle, points outside and inside, against the oracle's post
+    from ibemproject_gb300.cases import Case
+    E = rng.normal(size=layout)
+    pts = np.array([[0.13, -0.05, 0.02], [0.01, 0.02, -0.015], [0.0, 0.0, 0.0]])
+    c = Case(*MAT, np.zeros((0, 3)), np.zeros((0, 4), np.int32), np.zeros((0, 2)), np.zeros((0, 24)),
+             np.zeros((1, 3)), np.array([0.05]), pts)
+    want = oracle_mod.post(c, layout, E, sig_inf=np.zeros(6))
+    mu0 = MAT[0] / (2 * (1 + MAT[1]))
+    lam0 = 2 * mu0 * MAT[1] / (1 - 2 * MAT[1])
+    for k, p in enumerate(pts):
+        e = np.zeros(6)
+        hg.hg_field(layout, d(np.ascontiguousarray(p)), ctypes.c_double(0.05), *_mat(), d(E), d(e))
+        if p @ p <= 0.05 ** 2:   # local eigenstrain subtraction is done by the kernel wrapper
+            x = p
+            loc = E[:6].copy()
+            for r in range(6):
+                loc[r] += E[6 + 3 * r:9 + 3 * r] @ x
+                if layout == 78:
+                    M = E[24 + 9 * r:33 + 9 * r].reshape(3, 3)
+                    loc[r] += sum((1 if i == j else 2) * M[i, j] * x[i] * x[j] for i in range(3) for j in range(i, 3))
+                elif layout == 60:
+                    v = E[24 + 6 * r:30 + 6 * r]
+                    pr = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
+                    loc[r] += sum((1 if i == j else 2) * v[t] * x[i] * x[j] for t, (i, j) in enumerate(pr))
+            e -= loc
+        tr = e[0] + e[3] + e[5]
+        s = np.array([lam0 * tr + 2 * mu0 * e[0], 2 * mu0 * e[1], 2 * mu0 * e[2],
+                      lam0 * tr + 2 * mu0 * e[3], 2 * mu0 * e[4], lam0 * tr + 2 * mu0 * e[5]])
+        assert scaled_err(s, want[k]) < 1e-13
+
+
+@pytest.mark.parametrize("order", [0, 1, 2])
+def test_bem_stress_kernels(hg, oracle_mod, order):
+    m = oracle_mod.mat(*MAT)
+    mu0 = MAT[0] / 2.6
+    lam0 = 2 * mu0 * 0.3 / 0.4
+    mu1 = MAT[2] / 2.4
+    lam1 = 2 * mu1 * 0.2 / 0.6
+    rng = np.random.default_rng(5 + order)
+    for t in range(4):
+        x = rng.normal(size=3) * 0.3
+        nv = rng.normal(size=3)
+        nv /= np.linalg.norm(nv)
+        nrow = 6 * 3 ** order
+        su = np.zeros(nrow * 3)
+        st = np.zeros(nrow * 3)
+        hg.hg_bem_stress(order, d(x), d(nv), *_mat(), ctypes.c_double(lam0 - lam1), ctypes.c_double(mu0 - mu1),
+                         d(su), d(st))
+        rsu, rst = oracle_mod.stress_kernel(x, nv, m, lam0 - lam1, mu0 - mu1, order)
+        assert scaled_err(su.reshape(nrow, 3), rsu) < 1e-13
+        assert scaled_err(st.reshape(nrow, 3), rst) < 1e-13

@@ -1,0 +1,174 @@
+"""Kernel-level parity of the CUDA path (through the C ABI) with the oracle and with the
+reference's own matrices.  Tolerance: 1e-11 of the largest entry of the compared block
+for matrix entries (all FP64)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import case_from_npz, golden, scaled_err
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+MAT = (70e9, 0.3, 400e9, 0.2)
+
+
+def dev(a, dtype=None):
+    a = np.ascontiguousarray(a)
+    t = torch.from_numpy(a)
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.cuda()
+
+
+def P(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+@pytest.fixture(scope="module")
+def g():
+    import ibemproject_gb300 as g
+    assert torch.cuda.is_available(), "GPU tests need CUDA"
+    g.lib()
+    return g
+
+
+def spheres(n, seed):
+    from ibemproject_gb300 import cases
+    rng = np.random.default_rng(seed)
+    C, R = cases.rsa_spheres(n, rng, 0.15, 0.85, lambda k: 0.03 + 0.03 * ((k * 7) % 5) / 5,
+                             lambda r, Rk: r + Rk + 0.01)
+    return C, R
+
+
+@pytest.mark.parametrize("layout", [24, 60, 78])
+def test_pair_blocks_vs_oracle(g, oracle_mod, layout):
+    C, R = spheres(6, 3)
+    m = g.material(*MAT)
+    want = oracle_mod.pair_blocks(C, R, oracle_mod.mat(*MAT), layout)
+    n = layout * len(R)
+    pad = 5
+    A = torch.full((n + 2 * pad, n + 3 * pad), float("nan"), dtype=torch.float64, device="cuda")
+    lda = A.shape[1]   # torch row-major (rows=cols of the column-major view): use A^T storage
+    At = torch.full((n + 3 * pad, n + 2 * pad), float("nan"), dtype=torch.float64, device="cuda")
+    g.check(g.lib().ibem_e3d_pair_blocks(P(dev(C)), P(dev(R)), len(R), ctypes.byref(m), layout, P(At),
+                                         At.shape[1], pad, 2 * pad, None))
+    torch.cuda.synchronize()
+    got = At.cpu().numpy().T   # column-major view: got[r, c] = At[c, r]
+    blk = got[pad:pad + n, 2 * pad:2 * pad + n]
+    for s in range(len(R)):
+        for h in range(len(R)):
+            sl = (slice(layout * s, layout * (s + 1)), slice(layout * h, layout * (h + 1)))
+            assert scaled_err(blk[sl], want[sl]) < 1e-11
+    # nothing written outside the block
+    mask = np.ones_like(got, dtype=bool)
+    mask[pad:pad + n, 2 * pad:2 * pad + n] = False
+    assert np.all(np.isnan(got[mask]))
+
+
+@pytest.mark.parametrize("layout", [24, 78])
+def test_node_blocks_vs_oracle(g, oracle_mod, layout):
+    from ibemproject_gb300 import cases
+    nodes, conn, face = cases.cube_mesh(3)
+    C, R = spheres(3, 5)
+    m = g.material(*MAT)
+    NN = len(nodes)
+    H = torch.zeros((layout * len(R), 3 * NN), dtype=torch.float64, device="cuda")  # column-major 3NN x nu*num
+    g.check(g.lib().ibem_e3d_node_blocks(P(dev(nodes)), NN, P(dev(C)), P(dev(R)), len(R), ctypes.byref(m), layout,
+                                         P(H), 3 * NN, 0, 0, None))
+    got = H.cpu().numpy().T
+    want = np.zeros((3 * NN, layout * len(R)), order="F")
+    _d = ctypes.POINTER(ctypes.c_double)
+    oracle_mod.lib().orc_node_blocks(NN, nodes.ctypes.data_as(_d), len(R), np.ascontiguousarray(C).ctypes.data_as(_d),
+                                     np.ascontiguousarray(R).ctypes.data_as(_d), ctypes.byref(oracle_mod.mat(*MAT)),
+                                     layout, want.ctypes.data_as(_d), 3 * NN, 0, 0)
+    assert scaled_err(got, want) < 1e-11
+
+
+def _tiny_device_matrices(g, layout=78):
+    z = golden("tiny_reference.npz")
+    c = case_from_npz(z)
+    m = g.material(c.E0, c.nu0, c.E1, c.nu1)
+    N = 3 * c.NN + layout * c.num
+    Ht = torch.zeros((N, N), dtype=torch.float64, device="cuda")
+    Gt = torch.zeros((12 * c.NE, N), dtype=torch.float64, device="cuda")
+    nodes, conn, cen, rad = dev(c.nodes), dev(c.conn.astype(np.int32)), dev(c.centers), dev(c.radius)
+    L = g.lib()
+    g.check(L.ibem_e3d_bem_hg(P(nodes), c.NN, P(conn), c.NE, ctypes.byref(m), P(Ht), N, 0, 0, P(Gt), N, 0, 0, None))
+    g.check(L.ibem_e3d_node_blocks(P(nodes), c.NN, P(cen), P(rad), c.num, ctypes.byref(m), layout, P(Ht), N, 0,
+                                   3 * c.NN, None))
+    g.check(L.ibem_e3d_pair_blocks(P(cen), P(rad), c.num, ctypes.byref(m), layout, P(Ht), N, 3 * c.NN, 3 * c.NN,
+                                   None))
+    g.check(L.ibem_e3d_bem_to_incl(P(nodes), c.NN, P(conn), c.NE, P(cen), c.num, ctypes.byref(m), layout, P(Ht), N,
+                                   0, P(Gt), N, 0, 3 * c.NN, None))
+    torch.cuda.synchronize()
+    return z, c, Ht, Gt
+
+
+def test_assembly_vs_reference_matrices(g):
+    z, c, Ht, Gt = _tiny_device_matrices(g)
+    H = Ht.cpu().numpy().T
+    G = Gt.cpu().numpy().T
+    n3 = 3 * c.NN
+    for rs, cs in [(slice(0, n3), slice(0, n3)), (slice(0, n3), slice(n3, None)),
+                   (slice(n3, None), slice(n3, None)), (slice(n3, None), slice(0, n3))]:
+        assert scaled_err(H[rs, cs], z["HMAT"][rs, cs]) < 1e-11
+    assert scaled_err(G[:n3], z["GMAT"][:n3]) < 1e-11
+    assert scaled_err(G[n3:], z["GMAT"][n3:]) < 1e-11
+
+
+def test_apply_bc_and_get_ut(g, oracle_mod):
+    z, c, Ht, Gt = _tiny_device_matrices(g)
+    N = Ht.shape[0]
+    ucol, tcol = g.bc_plan(c)
+    At = torch.zeros((N, N), dtype=torch.float64, device="cuda")
+    b = torch.zeros(N, dtype=torch.float64, device="cuda")
+    bc, tbc = dev(c.bc), dev(c.tbc)
+    du, dt = dev(ucol), dev(tcol)
+    g.check(g.lib().ibem_e3d_apply_bc(c.NN, c.NE, N, P(du), P(dt), P(bc), P(tbc), P(Ht), N, P(Gt), N, P(At), N,
+                                      P(b), None))
+    torch.cuda.synchronize()
+    A_o, b_o, _, _ = oracle_mod.apply_bc(c, z["HMAT"], z["GMAT"])
+    assert scaled_err(At.cpu().numpy().T, A_o) < 1e-11
+    assert scaled_err(b.cpu().numpy(), z["b"]) < 1e-11
+    X = dev(z["X"])
+    U = torch.zeros(N, dtype=torch.float64, device="cuda")
+    T = torch.zeros(12 * c.NE, dtype=torch.float64, device="cuda")
+    g.check(g.lib().ibem_e3d_get_ut(c.NN, c.NE, N, P(du), P(dt), P(bc), P(tbc), P(X), P(U), P(T), None))
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(U.cpu().numpy(), z["U"])
+    np.testing.assert_array_equal(T.cpu().numpy(), z["T"])
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_solve_tiny_reference_system(g, oracle_mod, form):
+    z = golden("tiny_reference.npz")
+    c = case_from_npz(z)
+    A_o, b_o, _, _ = oracle_mod.apply_bc(c, z["HMAT"], z["GMAT"])
+    N = len(b_o)
+    At = dev(np.asfortranarray(A_o).T.copy())  # row-major torch holding A^T == column-major A
+    b = dev(b_o)
+    x = torch.zeros(N, dtype=torch.float64, device="cuda")
+    rep = g.SolveReport()
+    g.check(g.lib().ibem_e3d_solve(form, N, P(At), N, P(b), P(x), 1e-13, ctypes.byref(rep), None))
+    xs = x.cpu().numpy()
+    n3 = 3 * c.NN
+    assert scaled_err(xs[n3:], z["X"][n3:]) < 1e-9
+    assert scaled_err(xs[:n3], z["X"][:n3]) < 1e-9
+    assert rep.backward_error < 1e-13
+
+
+def test_field_vs_oracle(g, oracle_mod):
+    z = golden("tiny_reference.npz")
+    c = case_from_npz(z)
+    m = g.material(c.E0, c.nu0, c.E1, c.nu1)
+    n3 = 3 * c.NN
+    E = z["U"][n3:]
+    S = torch.zeros((c.nump, 6), dtype=torch.float64, device="cuda")
+    g.check(g.lib().ibem_e3d_field(P(dev(c.points)), c.nump, P(dev(c.centers)), P(dev(c.radius)), c.num,
+                                   ctypes.byref(m), 78, P(dev(E)), P(dev(c.nodes)), c.NN,
+                                   P(dev(c.conn.astype(np.int32))), c.NE, P(dev(z["U"])), P(dev(z["T"])), None,
+                                   P(S), None))
+    torch.cuda.synchronize()
+    assert scaled_err(S.cpu().numpy(), z["stress"]) < 1e-11
