@@ -1,0 +1,324 @@
+#!/usr/bin/env python
+"""Benchmark of the 3D spherical iBEM hot path on GB300.
+
+Workload (one "step" = one time-to-solution of one microstructure): 2,000 spheres,
+radius U[0.8, 1.2] x 0.012, random sequential addition with a surface gap >= 0.1 r,
+volume fraction ~15%, matrix E = 70 GPa / nu = 0.3, particles E = 400 GPa / nu = 0.2,
+linear Taylor eigenstrain (24 unknowns per sphere, N = 48,000), remote uniaxial stress
+sigma33 = 1, stresses on a cell-centred 64^3 grid (262,144 points).  Seeded synthetic
+inputs (no dataset is involved).
+
+A step = sphere-pair assembly (FP64) + far-field right-hand side + solve in the chosen
+form (FP32 LU with split-BF16 tensor-core updates + FP64 GMRES-IR to a scaled backward
+error <= tol) + stresses at all grid points (FP64).  `value` is seconds per solution with
+inputs resident in HBM; `e2e` is the same through ibem_e3d_run_host with host buffers
+(inputs copied in and X / stresses copied out inside the timed region).  The plain FP64
+form is timed once on the same microstructure and its relative difference reported.
+
+--impl reference times the CPU restatement of the reference's algorithm (the oracle,
+OpenMP over all host cores) on bounded samples of the same workload, extrapolated to it.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time-to-solution at 1e-8 rel. error: chosen form vs plain FP64, 1xGB300"
+WORKLOAD = "2000 spheres r~U[0.8,1.2]*0.012, vf 15%, linear eigenstrain (N=48000), far-field sigma33=1, 64^3 grid"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--num", type=int, default=2000)
+    ap.add_argument("--grid", type=int, default=64)
+    ap.add_argument("--tol", type=float, default=1e-12)
+    ap.add_argument("--no-plain", action="store_true", help="skip the one plain-FP64 comparison solve")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline sampling")
+    return ap.parse_args()
+
+
+def make_case(num, grid, seed):
+    from ibemproject_gb300 import cases
+    return cases.farfield_case(num=num, r0=0.012, vf=0.15, grid=grid, seed=seed)
+
+
+# ------------------------------------------------------------------ CPU baseline (oracle)
+def cpu_baseline(case, budget_s=20.0):
+    """Oracle (CPU restatement, OpenMP) on bounded samples of the workload, extrapolated:
+    assembly ~ num^2 pairs, dense solve ~ N^3, field sums ~ points x num."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    m = oracle.mat(case.E0, case.nu0, case.E1, case.nu1)
+    num, N, nump = case.num, 24 * case.num, case.nump
+    per = budget_s / 3.0
+    # assembly sample: a growing prefix of the spheres until ~per seconds
+    ns, ta = 40, 0.0
+    while True:
+        t = time.perf_counter()
+        oracle.pair_blocks(case.centers[:ns], case.radius[:ns], m, 24)
+        ta = time.perf_counter() - t
+        if ta > per / 4 or ns >= num:
+            break
+        ns = min(num, int(ns * 1.6))
+    t_asm = ta * (num / ns) ** 2
+    # solve sample: full-pivot LU (the reference's fullPivLu algorithm) of a sub-system
+    nsub = max(10, min(num, int(ns)))
+    A = oracle.pair_blocks(case.centers[:nsub], case.radius[:nsub], m, 24)
+    b = oracle.farfield_rhs(nsub, m, 24, case.sig_inf)
+    while True:
+        t = time.perf_counter()
+        oracle.solve_fullpiv(A, b)
+        tsol = time.perf_counter() - t
+        if tsol > per / 4 or nsub * 2 > num:
+            break
+        nsub = int(nsub * 1.5)
+        A = oracle.pair_blocks(case.centers[:nsub], case.radius[:nsub], m, 24)
+        b = oracle.farfield_rhs(nsub, m, 24, case.sig_inf)
+    t_sol = tsol * (N / (24 * nsub)) ** 3
+    # field sample: points against all spheres
+    E = np.zeros(N)
+    E[0::24] = 1e-12
+    npts = 8
+    while True:
+        idx = np.linspace(0, nump - 1, npts).astype(int)
+        t = time.perf_counter()
+        oracle.post(case, 24, E, sig_inf=case.sig_inf, points=case.points[idx])
+        tf = time.perf_counter() - t
+        if tf > per / 4 or npts >= nump:
+            break
+        npts = min(nump, npts * 2)
+    t_fld = tf * nump / npts
+    total = t_asm + t_sol + t_fld
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {
+        "value": total, "unit": "s", "cores": cores, "kind": "port",
+        "sample": (f"oracle (CPU restatement) timed on {ns} of {num} spheres' pair blocks (x (num/{ns})^2), "
+                   f"full-pivot LU at N={24 * nsub} (x (N/{24 * nsub})^3), field sums at {npts} of {nump} "
+                   f"points over all spheres (x {nump}/{npts}); extrapolated"),
+        "stages_s": {"assembly": t_asm, "solve": t_sol, "field": t_fld},
+    }
+
+
+# ------------------------------------------------------------------ clocks
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=open(self.path, "w"),
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for ln in open(self.path):
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ ours
+def run_ours(args, rank, world):
+    import torch
+    import ibemproject_gb300 as g
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    L = g.lib()
+    case = make_case(args.num, args.grid, 2024 + rank)   # replicas: one realisation per rank
+    N, num, nump = 24 * case.num, case.num, case.nump
+    m = g.material(case.E0, case.nu0, case.E1, case.nu1)
+    cen = torch.from_numpy(np.ascontiguousarray(case.centers)).to(dev)
+    rad = torch.from_numpy(np.ascontiguousarray(case.radius)).to(dev)
+    pts = torch.from_numpy(np.ascontiguousarray(case.points)).to(dev)
+    A = torch.empty((N, N), dtype=torch.float64, device=dev)   # column-major N x N (square)
+    b = torch.empty(N, dtype=torch.float64, device=dev)
+    x = torch.empty(N, dtype=torch.float64, device=dev)
+    S = torch.empty((nump, 6), dtype=torch.float64, device=dev)
+    sig = np.ascontiguousarray(case.sig_inf)
+    sigp = sig.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    rep = g.SolveReport()
+    stage_ms = {"assembly": [], "solve": [], "field": []}
+
+    def step(form=g.SOLVE_MIXED_IR, xo=x, So=S):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record(stream)
+        g.check(L.ibem_e3d_pair_blocks(P(cen), P(rad), num, ctypes.byref(m), 24, P(A), N, 0, 0, sp))
+        g.check(L.ibem_e3d_farfield_rhs(num, ctypes.byref(m), 24, sigp, P(b), sp))
+        ev[1].record(stream)
+        g.check(L.ibem_e3d_solve(form, N, P(A), N, P(b), P(xo), args.tol, ctypes.byref(rep), sp))
+        ev[2].record(stream)
+        g.check(L.ibem_e3d_field(P(pts), nump, P(cen), P(rad), num, ctypes.byref(m), 24, P(xo), None, 0, None, 0,
+                                 None, None, sigp, P(So), sp))
+        ev[3].record(stream)
+        return ev
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    clocks = Clocks(dev.index if "CUDA_VISIBLE_DEVICES" not in os.environ else dev.index)
+    clocks.start()
+    launches0 = L.ibem_kernel_launches()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record(stream)
+    evs = []
+    for _ in range(args.steps):
+        evs.append(step())
+    t1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    launches = L.ibem_kernel_launches() - launches0
+    ck = clocks.stop()
+    ms = t0.elapsed_time(t1) / args.steps
+    for ev in evs:
+        stage_ms["assembly"].append(ev[0].elapsed_time(ev[1]))
+        stage_ms["solve"].append(ev[1].elapsed_time(ev[2]))
+        stage_ms["field"].append(ev[2].elapsed_time(ev[3]))
+    rep_mixed = (rep.backward_error, rep.iterations, rep.t_factor_ms, rep.t_solve_ms)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # plain FP64 form once on the same microstructure, and the difference to it
+    plain = None
+    if not args.no_plain and rank == 0:
+        x64 = torch.empty(N, dtype=torch.float64, device=dev)
+        S64 = torch.empty((nump, 6), dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        ev = step(g.SOLVE_FP64, x64, S64)
+        torch.cuda.synchronize()
+        plain_ms = ev[0].elapsed_time(ev[3])
+        ex = float((x - x64).abs().max() / x64.abs().max())
+        es = float((S - S64).abs().max() / S64.abs().max())
+        plain = {"time_to_solution_s": plain_ms / 1e3, "factor_ms": rep.t_factor_ms, "solve_ms": rep.t_solve_ms,
+                 "backward_error": rep.backward_error, "mixed_rel_err_eigenstrain": ex,
+                 "mixed_rel_err_stress": es}
+        del x64, S64
+
+    # end to end through the host-buffer C ABI (copies inside the timed region)
+    e2e = None
+    if rank == 0 and args.e2e_steps > 0:
+        del A
+        torch.cuda.empty_cache()
+        t = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            g.run_host(case, layout=24, form=g.SOLVE_MIXED_IR, tol=args.tol)
+        e2e_s = (time.perf_counter() - t) / args.e2e_steps
+        h2d = case.centers.nbytes + case.radius.nbytes + case.points.nbytes + 48
+        d2h = 8 * N + 8 * 6 * nump
+        e2e = {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+    return case, ms, stage_ms, rep_mixed, plain, e2e, ck, launches
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        case = make_case(args.num, args.grid, 2024)
+        vals = []
+        for _ in range(max(1, args.steps)):
+            cb = cpu_baseline(case, budget_s=args.cpu_budget / max(1, args.steps))
+            vals.append(cb["value"])
+        v = statistics.median(vals)
+        cb["value"] = v
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": 0, "ms_per_step": v * 1e3, "higher_is_better": False,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD, "layout": 24, "N": 24 * case.num, "points": case.nump,
+                           "l2": "not applicable (CPU)"},
+                "cpu_baseline": cb, "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0,
+                                            "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    case, ms, stage_ms, rep_mixed, plain, e2e, ck, launches = run_ours(args, rank, world)
+    if rank == 0:
+        cb = cpu_baseline(case, budget_s=args.cpu_budget) if world == 1 else None
+        N = 24 * case.num
+        med = {k: statistics.median(v) for k, v in stage_ms.items()}
+        line = {
+            "metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32/bf16x3",
+            "data": "synthetic (seeded RSA microstructure)",
+            "config": {"workload": WORKLOAD, "layout": 24, "N": N, "points": case.nump, "form": "mixed_ir",
+                       "tol_scaled_backward_error": args.tol,
+                       "l2": "inputs larger than L2 (A is 18.4 GB FP64)", "parallelism": f"replicas x{world}"},
+            "stages_ms": med,
+            "solve": {"backward_error": rep_mixed[0], "gmres_iterations": rep_mixed[1],
+                      "factor_ms": rep_mixed[2], "refine_ms": rep_mixed[3]},
+            "plain_fp64": plain,
+            "e2e": e2e,
+            "clocks": ck,
+            "gpu_launches": int(launches),
+            "cpu_baseline": cb,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -51,6 +51,7 @@ class IbemError(RuntimeError):
 SIGNATURES = {
     "ibem_last_error": (ctypes.c_char_p, []),
     "ibem_layout_size": (_int, [_int]),
+    "ibem_kernel_launches": (ctypes.c_longlong, []),
     "ibem_e3d_pair_blocks": (_int, [_vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _i64, _i64, _i64, _vp]),
     "ibem_e3d_node_blocks": (_int, [_vp, _int, _vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _i64, _i64,
                                     _i64, _vp]),

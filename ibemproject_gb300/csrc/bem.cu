@@ -355,8 +355,8 @@ ibem_status bem_hg(const double* nodes, int NN, const int* conn, int NE, const i
   kc.ct = 1.0 / (8 * IBEM_PI * (1 - m.nu0));
   kc.c3 = 1 - 2 * m.nu0;
   dim3 grid((NN + 127) / 128, NE);
-  bem_hg_kernel<<<grid, 128, 0, st>>>(nodes, NN, conn, kc, Hb, ldh, Gb, ldg);
-  bem_diag_kernel<<<(3 * NN + 127) / 128, 128, 0, st>>>(NN, Hb, ldh);
+  ::ibem::count_launch(), bem_hg_kernel<<<grid, 128, 0, st>>>(nodes, NN, conn, kc, Hb, ldh, Gb, ldg);
+  ::ibem::count_launch(), bem_diag_kernel<<<(3 * NN + 127) / 128, 128, 0, st>>>(NN, Hb, ldh);
   IBEM_LAUNCH_CHECK("bem_hg");
   return IBEM_OK;
 }
@@ -370,10 +370,10 @@ ibem_status bem_to_incl(const double* nodes, int NN, const int* conn, int NE, co
   double* Gb = G + gcol0 * ldg + row0;
   const int compact = layout == 60;
   dim3 g0((num + 127) / 128, NE, 3), g1((num + 127) / 128, NE, 9), g2((num + 127) / 128, NE, 27);
-  bem_incl_kernel<0><<<g0, 128, 0, st>>>(nodes, NN, conn, cen, num, bm, layout, compact, Hb, ldh, Gb, ldg);
-  bem_incl_kernel<1><<<g1, 128, 0, st>>>(nodes, NN, conn, cen, num, bm, layout, compact, Hb, ldh, Gb, ldg);
+  ::ibem::count_launch(), bem_incl_kernel<0><<<g0, 128, 0, st>>>(nodes, NN, conn, cen, num, bm, layout, compact, Hb, ldh, Gb, ldg);
+  ::ibem::count_launch(), bem_incl_kernel<1><<<g1, 128, 0, st>>>(nodes, NN, conn, cen, num, bm, layout, compact, Hb, ldh, Gb, ldg);
   if (layout != 24)
-    bem_incl_kernel<2><<<g2, 128, 0, st>>>(nodes, NN, conn, cen, num, bm, layout, compact, Hb, ldh, Gb, ldg);
+    ::ibem::count_launch(), bem_incl_kernel<2><<<g2, 128, 0, st>>>(nodes, NN, conn, cen, num, bm, layout, compact, Hb, ldh, Gb, ldg);
   IBEM_LAUNCH_CHECK("bem_to_incl");
   return IBEM_OK;
 }
@@ -382,7 +382,7 @@ ibem_status bem_post(const double* pts, int nump, const double* nodes, int NN, c
                      int NE, const ibem_material& m, const double* U, const double* T,
                      double* stress, cudaStream_t st) {
   BemMat bm = bem_mat_init(m.E0, m.nu0, m.E1, m.nu1);
-  bem_post_kernel<<<(nump + 127) / 128, 128, 0, st>>>(pts, nump, nodes, NN, conn, NE, bm, U, T, stress);
+  ::ibem::count_launch(), bem_post_kernel<<<(nump + 127) / 128, 128, 0, st>>>(pts, nump, nodes, NN, conn, NE, bm, U, T, stress);
   IBEM_LAUNCH_CHECK("bem_post");
   return IBEM_OK;
 }

@@ -1,6 +1,7 @@
 // extern "C" entry points of libibem_gb300.so (declared in include/ibem_gb300.h).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -12,6 +13,12 @@
 namespace ibem {
 
 static thread_local std::string g_last_error;
+static std::atomic<long long> g_launches{0};
+
+int count_launch() {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return 0;
+}
 
 ibem_status fail(ibem_status st, const std::string& msg) {
   g_last_error = msg;
@@ -106,6 +113,8 @@ using namespace ibem;
 extern "C" {
 
 const char* ibem_last_error(void) { return g_last_error.c_str(); }
+
+long long ibem_kernel_launches(void) { return g_launches.load(); }
 
 int ibem_layout_size(int layout) { return valid_layout(layout) ? layout : -1; }
 
@@ -208,12 +217,12 @@ ibem_status ibem_e3d_apply_bc(int NN, int NE, int64_t N, const int* ucol_dev, co
   cudaStream_t st = as_stream(stream);
   IBEM_CUDA(cudaMemset2DAsync(A_dev, lda * sizeof(double), 0, N * sizeof(double), n3, st));
   const unsigned gx = (unsigned)((N + 255) / 256);
-  k_bc_ucols<<<dim3(gx, n3), 256, 0, st>>>(N, n3, ucol_dev, H_dev, ldh, A_dev, lda);
+  ::ibem::count_launch(), k_bc_ucols<<<dim3(gx, n3), 256, 0, st>>>(N, n3, ucol_dev, H_dev, ldh, A_dev, lda);
   for (int k0 = 0; k0 < nt; k0 += 65535) {
     const int cnt = std::min(65535, nt - k0);
-    k_bc_tcols<<<dim3(gx, cnt), 256, 0, st>>>(N, cnt, tcol_dev + k0, G_dev + (int64_t)k0 * ldg, ldg, A_dev, lda);
+    ::ibem::count_launch(), k_bc_tcols<<<dim3(gx, cnt), 256, 0, st>>>(N, cnt, tcol_dev + k0, G_dev + (int64_t)k0 * ldg, ldg, A_dev, lda);
   }
-  k_bc_rhs<<<gx, 256, 0, st>>>(N, n3, nt, bc_dev, tbc_dev, H_dev, ldh, G_dev, ldg, b_dev);
+  ::ibem::count_launch(), k_bc_rhs<<<gx, 256, 0, st>>>(N, n3, nt, bc_dev, tbc_dev, H_dev, ldh, G_dev, ldg, b_dev);
   if (N > n3)
     IBEM_CUDA(cudaMemcpy2DAsync(A_dev + (int64_t)n3 * lda, lda * sizeof(double), H_dev + (int64_t)n3 * ldh,
                                 ldh * sizeof(double), N * sizeof(double), N - n3, cudaMemcpyDeviceToDevice, st));
@@ -226,7 +235,7 @@ ibem_status ibem_e3d_get_ut(int NN, int NE, int64_t N, const int* ucol_dev, cons
                             double* U_dev, double* T_dev, void* stream) {
   if (NN < 0 || NE < 0 || N < 3 * (int64_t)NN) return fail(IBEM_ERR_ARG, "get_ut: bad sizes");
   const int64_t n = std::max<int64_t>(N, 12 * (int64_t)NE);
-  k_get_ut<<<(unsigned)((n + 255) / 256), 256, 0, as_stream(stream)>>>(3 * NN, N, 12 * NE, ucol_dev, tcol_dev,
+  ::ibem::count_launch(), k_get_ut<<<(unsigned)((n + 255) / 256), 256, 0, as_stream(stream)>>>(3 * NN, N, 12 * NE, ucol_dev, tcol_dev,
                                                                        bc_dev, tbc_dev, X_dev, U_dev, T_dev);
   IBEM_LAUNCH_CHECK("get_ut");
   return IBEM_OK;
@@ -252,7 +261,7 @@ ibem_status ibem_e3d_farfield_rhs(int num, const ibem_material* mat, int layout,
     for (int j = i; j < 3; ++j, ++r) f.v[r] = (l0 - l1) * etr * (i == j) + 2 * (mu0 - mu1) * eps[i][j];
   if (num == 0) return IBEM_OK;
   const int64_t n = (int64_t)num * layout;
-  k_farfield<<<(unsigned)((n + 255) / 256), 256, 0, as_stream(stream)>>>(num, layout, f, b_dev);
+  ::ibem::count_launch(), k_farfield<<<(unsigned)((n + 255) / 256), 256, 0, as_stream(stream)>>>(num, layout, f, b_dev);
   IBEM_LAUNCH_CHECK("farfield_rhs");
   return IBEM_OK;
 }
@@ -278,7 +287,7 @@ ibem_status ibem_e3d_field(const double* points_dev, int nump, const double* cen
   } else {
     FarRhs f;
     for (int i = 0; i < 6; ++i) f.v[i] = sig_inf ? sig_inf[i] : 0.0;
-    k_fill6<<<(unsigned)(((int64_t)nump * 6 + 255) / 256), 256, 0, st>>>(nump, f, stress_dev);
+    ::ibem::count_launch(), k_fill6<<<(unsigned)(((int64_t)nump * 6 + 255) / 256), 256, 0, st>>>(nump, f, stress_dev);
     IBEM_LAUNCH_CHECK("field init");
   }
   if (num == 0) return IBEM_OK;

@@ -26,6 +26,10 @@ ibem_status cuda_fail(cudaError_t e, const char* where);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Counts kernel launches of this library (read through ibem_kernel_launches); every
+// launch site is written `::ibem::count_launch(), kernel<<<...>>>(...)`.
+int count_launch();
+
 // ---- sphere kernels (sphere24.cu / sphere60.cu / sphere78.cu) ----
 struct SphLaunch {
   const double* cen;

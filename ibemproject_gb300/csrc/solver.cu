@@ -425,6 +425,7 @@ static ibem_status panel(T* A, int64_t lda, int64_t k0, int64_t m, int nb, LuWor
   int* ip = w.ipiv_dev + k0;
   int kg = (int)k0;
   void* args[] = {&P, &lda, &mm, &nb, &rows_per, &w.cand, &w.rowj, &ip, &kg, &w.info, &w.gs};
+  count_launch();
   IBEM_CUDA(cudaLaunchCooperativeKernel((void*)k_panel<T>, dim3(ncta), dim3(kPanelThreads), args, smem, st));
   return IBEM_OK;
 }
@@ -438,7 +439,7 @@ ibem_status gemm_sub<double>(int64_t m, int64_t n, int64_t k, const double* A, i
                              int64_t ldb, double* C, int64_t ldc, cudaStream_t st) {
   if (m <= 0 || n <= 0 || k <= 0) return IBEM_OK;
   dim3 grid((unsigned)((m + 63) / 64), (unsigned)((n + 63) / 64));
-  k_gemm_sub<double><<<grid, 256, 0, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
+  ::ibem::count_launch(), k_gemm_sub<double><<<grid, 256, 0, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
   IBEM_LAUNCH_CHECK("gemm f64");
   return IBEM_OK;
 }
@@ -448,7 +449,7 @@ ibem_status gemm_sub<float>(int64_t m, int64_t n, int64_t k, const float* A, int
                             int64_t ldb, float* C, int64_t ldc, cudaStream_t st) {
   if (m <= 0 || n <= 0 || k <= 0) return IBEM_OK;
   dim3 grid((unsigned)((m + 63) / 64), (unsigned)((n + 63) / 64));
-  k_gemm_sub<float><<<grid, 256, 0, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
+  ::ibem::count_launch(), k_gemm_sub<float><<<grid, 256, 0, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
   IBEM_LAUNCH_CHECK("gemm f32");
   return IBEM_OK;
 }
@@ -458,7 +459,7 @@ template <typename T>
 static ibem_status trsm(const T* L, int64_t ldl, int64_t n1, T* B, int64_t ldb, int64_t n2, cudaStream_t st) {
   if (n1 <= 0 || n2 <= 0) return IBEM_OK;
   if (n1 <= 64) {
-    k_trsm_small<T><<<(unsigned)((n2 + 63) / 64), 64, 0, st>>>(L, ldl, (int)n1, B, ldb, n2);
+    ::ibem::count_launch(), k_trsm_small<T><<<(unsigned)((n2 + 63) / 64), 64, 0, st>>>(L, ldl, (int)n1, B, ldb, n2);
     IBEM_LAUNCH_CHECK("trsm_small");
     return IBEM_OK;
   }
@@ -478,9 +479,9 @@ static ibem_status lu_rec(T* A, int64_t lda, int64_t N, int64_t k0, int64_t n, L
     ibem_status s = panel(A, lda, k0, m, (int)n, w, st);
     if (s) return s;
     // exchanges of this panel on the columns to its left and right (within [0, N))
-    if (k0 > 0) k_laswp<T><<<(unsigned)((k0 + 127) / 128), 128, 0, st>>>(A, lda, k0, w.ipiv_dev + k0, (int)n, 0, k0);
+    if (k0 > 0) ::ibem::count_launch(), k_laswp<T><<<(unsigned)((k0 + 127) / 128), 128, 0, st>>>(A, lda, k0, w.ipiv_dev + k0, (int)n, 0, k0);
     if (k0 + n < N)
-      k_laswp<T><<<(unsigned)((N - k0 - n + 127) / 128), 128, 0, st>>>(A, lda, k0, w.ipiv_dev + k0, (int)n, k0 + n, N);
+      ::ibem::count_launch(), k_laswp<T><<<(unsigned)((N - k0 - n + 127) / 128), 128, 0, st>>>(A, lda, k0, w.ipiv_dev + k0, (int)n, k0 + n, N);
     IBEM_LAUNCH_CHECK("laswp");
     return IBEM_OK;
   }
@@ -543,19 +544,19 @@ static void lu_free(LuWork<T>& w) {
 template <typename T>
 static ibem_status lu_apply(const T* F, int64_t ldf, int64_t N, const int* perm, double* tmp, double* y,
                             cudaStream_t st) {
-  k_gather<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, perm, y, tmp);
+  ::ibem::count_launch(), k_gather<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, perm, y, tmp);
   IBEM_CUDA(cudaMemcpyAsync(y, tmp, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
   const int nb = 64;
   for (int64_t k0 = 0; k0 < N; k0 += nb) {
     const int b = (int)std::min<int64_t>(nb, N - k0);
-    k_trsv_diag<T><<<1, 64, 0, st>>>(F, ldf, k0, b, y, 1);
+    ::ibem::count_launch(), k_trsv_diag<T><<<1, 64, 0, st>>>(F, ldf, k0, b, y, 1);
     if (k0 + b < N)
-      k_trsv_update<T><<<(unsigned)((N - k0 - b + 255) / 256), 256, 0, st>>>(F, ldf, k0, b, k0 + b, N, y);
+      ::ibem::count_launch(), k_trsv_update<T><<<(unsigned)((N - k0 - b + 255) / 256), 256, 0, st>>>(F, ldf, k0, b, k0 + b, N, y);
   }
   for (int64_t k0 = ((N - 1) / nb) * nb; k0 >= 0; k0 -= nb) {
     const int b = (int)std::min<int64_t>(nb, N - k0);
-    k_trsv_diag<T><<<1, 64, 0, st>>>(F, ldf, k0, b, y, 0);
-    if (k0 > 0) k_trsv_update<T><<<(unsigned)((k0 + 255) / 256), 256, 0, st>>>(F, ldf, k0, b, 0, k0, y);
+    ::ibem::count_launch(), k_trsv_diag<T><<<1, 64, 0, st>>>(F, ldf, k0, b, y, 0);
+    if (k0 > 0) ::ibem::count_launch(), k_trsv_update<T><<<(unsigned)((k0 + 255) / 256), 256, 0, st>>>(F, ldf, k0, b, 0, k0, y);
   }
   IBEM_LAUNCH_CHECK("lu_apply");
   return IBEM_OK;
@@ -566,8 +567,8 @@ static ibem_status residual(int64_t N, const double* A, int64_t lda, const doubl
                             double* part, int nparts, cudaStream_t st) {
   const int64_t chunk = (N + nparts - 1) / nparts;
   dim3 grid((unsigned)((N + 255) / 256), (unsigned)nparts);
-  k_gemv_part<<<grid, 256, 0, st>>>(N, A, lda, x, chunk, part);
-  k_residual<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, nparts, part, b, r);
+  ::ibem::count_launch(), k_gemv_part<<<grid, 256, 0, st>>>(N, A, lda, x, chunk, part);
+  ::ibem::count_launch(), k_residual<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, nparts, part, b, r);
   IBEM_LAUNCH_CHECK("residual");
   return IBEM_OK;
 }
@@ -606,13 +607,6 @@ __global__ void k_axpby(int64_t n, double a, const double* __restrict__ x, doubl
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) y[i] = a * x[i] + b * y[i];
 }
-__global__ void k_absmax_rowsum(int64_t n, const double* __restrict__ A, int64_t lda, double* __restrict__ rs) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double s = 0;
-  for (int64_t j = 0; j < n; ++j) s += fabs(A[j * lda + i]);
-  rs[i] = s;
-}
 }  // namespace
 
 static double host_absmax(const std::vector<double>& v) {
@@ -650,28 +644,63 @@ static ibem_status vec_to_host(const double* d, int64_t n, std::vector<double>& 
   return IBEM_OK;
 }
 
-// backward error ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf); anorm = ||A||_inf
-static ibem_status backward_error(SolveCtx& cx, const double* A, int64_t lda, const double* x, const double* b,
-                                  double* rvec, double anorm, double& be) {
-  ibem_status s = residual(cx.N, A, lda, x, b, rvec, cx.part, cx.nparts, cx.st);
+namespace {
+// row sums of |R A C| (the inf-norm of the equilibrated matrix)
+__global__ void k_scaled_rowsum(int64_t n, const double* __restrict__ A, int64_t lda, const double* __restrict__ r,
+                                const double* __restrict__ c, double* __restrict__ rs) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0;
+  for (int64_t j = 0; j < n; ++j) s += fabs(A[j * lda + i]) * c[j];
+  rs[i] = s * r[i];
+}
+// y = r .* (A (c .* v)) via the partial-sum GEMV; tmp is an N-vector
+__global__ void k_scale_rows_of_parts(int64_t n, int nparts, const double* __restrict__ part,
+                                      const double* __restrict__ r, double* __restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0;
+  for (int p = 0; p < nparts; ++p) s += part[p * n + i];
+  y[i] = r[i] * s;
+}
+}  // namespace
+
+// y = As v with As = R A C (FP64; tmp is N-vector scratch)
+static ibem_status scaled_matvec(SolveCtx& cx, const double* A, int64_t lda, const double* v, double* tmp,
+                                 double* y) {
+  const int64_t N = cx.N;
+  const unsigned nb = (unsigned)((N + 255) / 256);
+  ::ibem::count_launch(), k_vmul<<<nb, 256, 0, cx.st>>>(N, cx.c, v, tmp);
+  const int64_t chunk = (N + cx.nparts - 1) / cx.nparts;
+  ::ibem::count_launch(), k_gemv_part<<<dim3(nb, (unsigned)cx.nparts), 256, 0, cx.st>>>(N, A, lda, tmp, chunk, cx.part);
+  ::ibem::count_launch(), k_scale_rows_of_parts<<<nb, 256, 0, cx.st>>>(N, cx.nparts, cx.part, cx.r, y);
+  IBEM_LAUNCH_CHECK("scaled_matvec");
+  return IBEM_OK;
+}
+
+// scaled backward error of ys for As ys = bs: ||bs - As ys|| / (||As|| ||ys|| + ||bs||)  (inf-norms)
+static ibem_status scaled_backward_error(SolveCtx& cx, const double* A, int64_t lda, const double* ys,
+                                         const double* bs, double* rvec, double* tmp, double as_norm, double& be) {
+  ibem_status s = scaled_matvec(cx, A, lda, ys, tmp, rvec);
   if (s) return s;
-  std::vector<double> hr, hx, hb;
+  ::ibem::count_launch(), k_axpby<<<(unsigned)((cx.N + 255) / 256), 256, 0, cx.st>>>(cx.N, 1.0, bs, -1.0, rvec);  // rvec = bs - As ys
+  std::vector<double> hr, hy, hb;
   if ((s = vec_to_host(rvec, cx.N, hr, cx.st))) return s;
-  if ((s = vec_to_host(x, cx.N, hx, cx.st))) return s;
-  if ((s = vec_to_host(b, cx.N, hb, cx.st))) return s;
-  be = host_absmax(hr) / (anorm * host_absmax(hx) + host_absmax(hb));
+  if ((s = vec_to_host(ys, cx.N, hy, cx.st))) return s;
+  if ((s = vec_to_host(bs, cx.N, hb, cx.st))) return s;
+  be = host_absmax(hr) / (as_norm * host_absmax(hy) + host_absmax(hb));
   return IBEM_OK;
 }
 
 template <typename T>
 static ibem_status factor(SolveCtx& cx, const double* A, int64_t lda, T*& W, LuWork<T>& w, int& info) {
   const int64_t N = cx.N;
-  k_rowmax<<<(unsigned)((N + 255) / 256), 256, 0, cx.st>>>(N, A, lda, cx.r);
-  k_colmax<<<(unsigned)N, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c);
+  ::ibem::count_launch(), k_rowmax<<<(unsigned)((N + 255) / 256), 256, 0, cx.st>>>(N, A, lda, cx.r);
+  ::ibem::count_launch(), k_colmax<<<(unsigned)N, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c);
   IBEM_LAUNCH_CHECK("equilibrate");
   IBEM_CUDA(cudaMalloc(&W, sizeof(T) * (size_t)N * N));
   dim3 g((unsigned)((N + 255) / 256), (unsigned)N);
-  k_scale_copy<T><<<g, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c, W, N);
+  ::ibem::count_launch(), k_scale_copy<T><<<g, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c, W, N);
   IBEM_LAUNCH_CHECK("scale_copy");
   ibem_status s = lu_alloc(w, N);
   if (s) return s;
@@ -701,62 +730,62 @@ static ibem_status factor(SolveCtx& cx, const double* A, int64_t lda, T*& W, LuW
   return IBEM_OK;
 }
 
-// z <- C (LU)^-1 R v  (the scaled-system preconditioner), z and v FP64
-template <typename T>
-static ibem_status precond(SolveCtx& cx, const T* W, const LuWork<T>& w, const double* v, double* z) {
-  const unsigned nb = (unsigned)((cx.N + 255) / 256);
-  k_vmul<<<nb, 256, 0, cx.st>>>(cx.N, cx.r, v, z);
-  ibem_status s = lu_apply<T>(W, cx.N, cx.N, w.perm, w.tmp, z, cx.st);
-  if (s) return s;
-  k_vmul<<<nb, 256, 0, cx.st>>>(cx.N, cx.c, z, z);
-  IBEM_LAUNCH_CHECK("precond");
-  return IBEM_OK;
-}
-
 ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda, const double* b, double* x,
                         double tol, ibem_solve_report* rep, cudaStream_t st) {
   if (N <= 0 || !A || !b || !x || lda < N) return fail(IBEM_ERR_ARG, "solve: bad sizes or pointers");
+  if (form != IBEM_SOLVE_FP64 && form != IBEM_SOLVE_MIXED_IR) return fail(IBEM_ERR_ARG, "unknown solver form");
   SolveCtx cx;
   ibem_status s = cx.alloc(N, st);
   if (s) return s;
+  // Everything below works on the equilibrated system  As ys = bs,  As = R A C,
+  // bs = R b, x = C ys: errors are measured row-relative, so the small boundary rows of
+  // the iBEM matrix weigh as much as the inclusion rows.
+  double *bs = nullptr, *ys = nullptr, *rvec = nullptr, *tmp = nullptr;
+  IBEM_CUDA(cudaMalloc(&bs, sizeof(double) * N));
+  IBEM_CUDA(cudaMalloc(&ys, sizeof(double) * N));
+  IBEM_CUDA(cudaMalloc(&rvec, sizeof(double) * N));
+  IBEM_CUDA(cudaMalloc(&tmp, sizeof(double) * N));
   cudaEvent_t e0, e1, e2;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventCreate(&e2);
-  k_absmax_rowsum<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, A, lda, cx.rs);
-  std::vector<double> hrs;
-  if ((s = vec_to_host(cx.rs, N, hrs, st))) return s;
-  const double anorm = host_absmax(hrs);
-  double* rvec = nullptr;
-  IBEM_CUDA(cudaMalloc(&rvec, sizeof(double) * N));
   ibem_solve_report R{};
+  const unsigned nb = (unsigned)((N + 255) / 256);
   cudaEventRecord(e0, st);
+  double as_norm = 0;
+  auto finish_norm = [&]() -> ibem_status {
+    ::ibem::count_launch(), k_scaled_rowsum<<<nb, 256, 0, st>>>(N, A, lda, cx.r, cx.c, cx.rs);
+    IBEM_LAUNCH_CHECK("scaled_rowsum");
+    std::vector<double> h;
+    ibem_status q = vec_to_host(cx.rs, N, h, st);
+    as_norm = host_absmax(h);
+    return q;
+  };
   if (form == IBEM_SOLVE_FP64) {
     double* W = nullptr;
     LuWork<double> w;
     int info = 0;
     s = factor<double>(cx, A, lda, W, w, info);
     cudaEventRecord(e1, st);
+    if (!s && info) { R.info = info; s = fail(IBEM_ERR_SINGULAR, "zero pivot in the FP64 factorisation"); }
     if (!s) {
-      R.info = info;
-      if (info) s = fail(IBEM_ERR_SINGULAR, "zero pivot in the FP64 factorisation");
+      ::ibem::count_launch(), k_vmul<<<nb, 256, 0, st>>>(N, cx.r, b, bs);
+      IBEM_CUDA(cudaMemcpyAsync(ys, bs, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+      s = lu_apply<double>(W, N, N, w.perm, w.tmp, ys, st);
     }
-    if (!s) s = precond<double>(cx, W, w, b, x);
     cudaEventRecord(e2, st);
-    if (!s) s = backward_error(cx, A, lda, x, b, rvec, anorm, R.backward_error);
+    if (!s) s = finish_norm();
+    if (!s) s = scaled_backward_error(cx, A, lda, ys, bs, rvec, tmp, as_norm, R.backward_error);
     lu_free(w);
     cudaFree(W);
-  } else if (form == IBEM_SOLVE_MIXED_IR) {
+  } else {
     float* W = nullptr;
     LuWork<float> w;
     int info = 0;
     s = factor<float>(cx, A, lda, W, w, info);
     cudaEventRecord(e1, st);
-    if (!s) {
-      R.info = info;
-      if (info) s = fail(IBEM_ERR_SINGULAR, "zero pivot in the FP32 factorisation");
-    }
-    // FGMRES(m) on A d = r with the right preconditioner M^-1 = C (LU)^-1 R, FP64
+    if (!s && info) { R.info = info; s = fail(IBEM_ERR_SINGULAR, "zero pivot in the FP32 factorisation"); }
+    // GMRES(m) on As d = rs, right-preconditioned by the FP32 factors of As, all in FP64
     const int m = 30, max_outer = 20;
     double *V = nullptr, *Z = nullptr, *hd = nullptr;
     if (!s) {
@@ -765,21 +794,27 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
       if (ce == cudaSuccess) ce = cudaMalloc(&hd, sizeof(double) * (m + 1) * 2);
       if (ce != cudaSuccess) s = cuda_fail(ce, "gmres workspace");
     }
-    if (!s) s = precond<float>(cx, W, w, b, x);
+    if (!s) {
+      ::ibem::count_launch(), k_vmul<<<nb, 256, 0, st>>>(N, cx.r, b, bs);
+      IBEM_CUDA(cudaMemcpyAsync(ys, bs, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+      s = lu_apply<float>(W, N, N, w.perm, w.tmp, ys, st);
+    }
+    if (!s) s = finish_norm();
     int iters = 0;
-    const unsigned nb = (unsigned)((N + 255) / 256);
     for (int outer = 0; !s && outer < max_outer; ++outer) {
       double be = 0;
-      if ((s = backward_error(cx, A, lda, x, b, rvec, anorm, be))) break;
+      if ((s = scaled_backward_error(cx, A, lda, ys, bs, rvec, tmp, as_norm, be))) break;
       R.backward_error = be;
       if (be <= tol) break;
-      std::vector<double> hr;
-      if ((s = vec_to_host(rvec, N, hr, st))) break;
-      double beta = 0;
-      for (double v : hr) beta += v * v;
-      beta = std::sqrt(beta);
+      // rvec holds rs = bs - As ys
+      IBEM_CUDA(cudaMemsetAsync(hd, 0, sizeof(double), st));
+      ::ibem::count_launch(), k_dot_many<<<256, 256, 0, st>>>(N, 1, rvec, N, rvec, hd);
+      double b2 = 0;
+      IBEM_CUDA(cudaMemcpyAsync(&b2, hd, sizeof(double), cudaMemcpyDeviceToHost, st));
+      IBEM_CUDA(cudaStreamSynchronize(st));
+      const double beta = std::sqrt(std::max(b2, 0.0));
       if (beta == 0) break;
-      k_axpby<<<nb, 256, 0, st>>>(N, 1.0 / beta, rvec, 0.0, V);
+      ::ibem::count_launch(), k_axpby<<<nb, 256, 0, st>>>(N, 1.0 / beta, rvec, 0.0, V);
       std::vector<double> H((m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0);
       g[0] = beta;
       int k = 0;
@@ -787,37 +822,29 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
         double* vk = V + (size_t)k * N;
         double* zk = Z + (size_t)k * N;
         double* wv = V + (size_t)(k + 1) * N;
-        if ((s = precond<float>(cx, W, w, vk, zk))) break;
-        // wv = A zk
-        {
-          const int64_t chunk = (N + cx.nparts - 1) / cx.nparts;
-          dim3 grid(nb, (unsigned)cx.nparts);
-          k_gemv_part<<<grid, 256, 0, st>>>(N, A, lda, zk, chunk, cx.part);
-          IBEM_CUDA(cudaMemsetAsync(rvec, 0, sizeof(double) * N, st));
-          k_residual<<<nb, 256, 0, st>>>(N, cx.nparts, cx.part, rvec, wv);  // wv = 0 - A zk
-          k_axpby<<<nb, 256, 0, st>>>(N, 0.0, wv, -1.0, wv);                // wv = A zk
-        }
+        IBEM_CUDA(cudaMemcpyAsync(zk, vk, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        if ((s = lu_apply<float>(W, N, N, w.perm, w.tmp, zk, st))) break;
+        if ((s = scaled_matvec(cx, A, lda, zk, tmp, wv))) break;
         // classical Gram-Schmidt, twice
         std::vector<double> hk(k + 1, 0.0), h2(k + 1);
         for (int pass = 0; pass < 2; ++pass) {
           IBEM_CUDA(cudaMemsetAsync(hd, 0, sizeof(double) * (k + 1), st));
-          k_dot_many<<<256, 256, 0, st>>>(N, k + 1, V, N, wv, hd);
-          k_sub_Vh<<<nb, 256, 0, st>>>(N, k + 1, V, N, hd, wv);
+          ::ibem::count_launch(), k_dot_many<<<256, 256, 0, st>>>(N, k + 1, V, N, wv, hd);
+          ::ibem::count_launch(), k_sub_Vh<<<nb, 256, 0, st>>>(N, k + 1, V, N, hd, wv);
           IBEM_CUDA(cudaMemcpyAsync(h2.data(), hd, sizeof(double) * (k + 1), cudaMemcpyDeviceToHost, st));
           IBEM_CUDA(cudaStreamSynchronize(st));
           for (int i = 0; i <= k; ++i) hk[i] += h2[i];
         }
         IBEM_CUDA(cudaMemsetAsync(hd, 0, sizeof(double), st));
-        k_dot_many<<<256, 256, 0, st>>>(N, 1, wv, N, wv, hd);
+        ::ibem::count_launch(), k_dot_many<<<256, 256, 0, st>>>(N, 1, wv, N, wv, hd);
         double nrm2 = 0;
         IBEM_CUDA(cudaMemcpyAsync(&nrm2, hd, sizeof(double), cudaMemcpyDeviceToHost, st));
         IBEM_CUDA(cudaStreamSynchronize(st));
         const double hn = std::sqrt(std::max(nrm2, 0.0));
-        if (hn > 0) k_axpby<<<nb, 256, 0, st>>>(N, 1.0 / hn, wv, 0.0, wv);
+        if (hn > 0) ::ibem::count_launch(), k_axpby<<<nb, 256, 0, st>>>(N, 1.0 / hn, wv, 0.0, wv);
         for (int i = 0; i <= k; ++i) H[i * m + k] = hk[i];
         H[(k + 1) * m + k] = hn;
-        // Givens rotations on column k
-        for (int i = 0; i < k; ++i) {
+        for (int i = 0; i < k; ++i) {  // previous Givens rotations
           const double t = cs[i] * H[i * m + k] + sn[i] * H[(i + 1) * m + k];
           H[(i + 1) * m + k] = -sn[i] * H[i * m + k] + cs[i] * H[(i + 1) * m + k];
           H[i * m + k] = t;
@@ -830,26 +857,26 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
         g[k + 1] = -sn[k] * g[k];
         g[k] = cs[k] * g[k];
         ++iters;
-        if (std::fabs(g[k + 1]) <= 1e-3 * tol * beta || hn == 0) { ++k; break; }
+        // stop the inner cycle once the scaled residual estimate is well below tol
+        if (std::fabs(g[k + 1]) <= 1e-2 * tol * (as_norm + 1.0) || hn == 0) { ++k; break; }
       }
       if (s) break;
-      // y = H^-1 g (upper triangular k x k), x += Z y
-      std::vector<double> y(k, 0.0);
+      std::vector<double> yv(k, 0.0);
       for (int i = k - 1; i >= 0; --i) {
         double t = g[i];
-        for (int j2 = i + 1; j2 < k; ++j2) t -= H[i * m + j2] * y[j2];
-        y[i] = t / H[i * m + i];
+        for (int j2 = i + 1; j2 < k; ++j2) t -= H[i * m + j2] * yv[j2];
+        yv[i] = t / H[i * m + i];
       }
-      IBEM_CUDA(cudaMemcpyAsync(hd, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, st));
-      k_axpby<<<nb, 256, 0, st>>>(N, -1.0, x, 0.0, x);  // x = -x
-      k_sub_Vh<<<nb, 256, 0, st>>>(N, k, Z, N, hd, x);  // x = -x - Z y
-      k_axpby<<<nb, 256, 0, st>>>(N, -1.0, x, 0.0, x);  // x = x + Z y
+      IBEM_CUDA(cudaMemcpyAsync(hd, yv.data(), sizeof(double) * k, cudaMemcpyHostToDevice, st));
+      ::ibem::count_launch(), k_axpby<<<nb, 256, 0, st>>>(N, -1.0, ys, 0.0, ys);  // ys = -ys
+      ::ibem::count_launch(), k_sub_Vh<<<nb, 256, 0, st>>>(N, k, Z, N, hd, ys);    // ys = -ys - Z y
+      ::ibem::count_launch(), k_axpby<<<nb, 256, 0, st>>>(N, -1.0, ys, 0.0, ys);  // ys = ys + Z y
       IBEM_LAUNCH_CHECK("gmres update");
     }
     cudaEventRecord(e2, st);
     if (!s) {
       double be = 0;
-      s = backward_error(cx, A, lda, x, b, rvec, anorm, be);
+      s = scaled_backward_error(cx, A, lda, ys, bs, rvec, tmp, as_norm, be);
       R.backward_error = be;
       if (!s && be > tol) s = fail(IBEM_ERR_NOCONV, "GMRES-IR did not reach the tolerance");
     }
@@ -859,9 +886,8 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
     cudaFree(hd);
     lu_free(w);
     cudaFree(W);
-  } else {
-    s = fail(IBEM_ERR_ARG, "unknown solver form");
   }
+  if (!s) ::ibem::count_launch(), k_vmul<<<nb, 256, 0, st>>>(N, cx.c, ys, x);  // x = C ys
   cudaStreamSynchronize(st);
   float t1 = 0, t2 = 0;
   cudaEventElapsedTime(&t1, e0, e1);
@@ -871,7 +897,10 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaEventDestroy(e2);
+  cudaFree(bs);
+  cudaFree(ys);
   cudaFree(rvec);
+  cudaFree(tmp);
   if (rep) *rep = R;
   return s;
 }

@@ -17,11 +17,11 @@ ibem_status launch_pair24(const SphLaunch& p, double* A, int64_t lda, int64_t ro
   SphMat mc = sph_mat_init(p.E0, p.nu0, p.E1, p.nu1);
   double* base = A + col0 * lda + row0;
   dim3 grid((p.num + kPairThreads - 1) / kPairThreads, p.num);
-  pair24_c0_r0<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
-  pair24_c0_r1<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
-  pair24_c1_r0<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
-  pair24_c1_r1<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
-  self24<<<(p.num + 127) / 128, 128, 0, st>>>(p.num, mc, base, lda);
+  ::ibem::count_launch(), pair24_c0_r0<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
+  ::ibem::count_launch(), pair24_c0_r1<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
+  ::ibem::count_launch(), pair24_c1_r0<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
+  ::ibem::count_launch(), pair24_c1_r1<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
+  ::ibem::count_launch(), self24<<<(p.num + 127) / 128, 128, 0, st>>>(p.num, mc, base, lda);
   IBEM_LAUNCH_CHECK("pair24");
   return IBEM_OK;
 }
@@ -30,7 +30,7 @@ ibem_status launch_node24(const SphLaunch& p, const double* nodes, int NN, doubl
                           int64_t row0, int64_t col0, cudaStream_t st) {
   SphMat mc = sph_mat_init(p.E0, p.nu0, p.E1, p.nu1);
   dim3 grid((NN + kPairThreads - 1) / kPairThreads, p.num);
-  node24<<<grid, kPairThreads, 0, st>>>(nodes, NN, p.cen, p.rad, mc, H + col0 * ldh + row0, ldh);
+  ::ibem::count_launch(), node24<<<grid, kPairThreads, 0, st>>>(nodes, NN, p.cen, p.rad, mc, H + col0 * ldh + row0, ldh);
   IBEM_LAUNCH_CHECK("node24");
   return IBEM_OK;
 }
@@ -38,7 +38,7 @@ ibem_status launch_node24(const SphLaunch& p, const double* nodes, int NN, doubl
 ibem_status launch_field24(const SphLaunch& p, const double* pts, int nump, const double* E,
                            double* stress, cudaStream_t st) {
   SphMat mc = sph_mat_init(p.E0, p.nu0, p.E1, p.nu1);
-  field24<<<(nump + kFieldThreads - 1) / kFieldThreads, kFieldThreads, 0, st>>>(
+  ::ibem::count_launch(), field24<<<(nump + kFieldThreads - 1) / kFieldThreads, kFieldThreads, 0, st>>>(
       pts, nump, p.cen, p.rad, p.num, mc, E, stress);
   IBEM_LAUNCH_CHECK("field24");
   return IBEM_OK;

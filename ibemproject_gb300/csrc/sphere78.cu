@@ -20,16 +20,16 @@ ibem_status launch_pair78(const SphLaunch& p, double* A, int64_t lda, int64_t ro
   SphMat mc = sph_mat_init(p.E0, p.nu0, p.E1, p.nu1);
   double* base = A + col0 * lda + row0;
   dim3 grid((p.num + kPairThreads - 1) / kPairThreads, p.num);
-  pair78_c0_r0<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
-  pair78_c0_r1<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
-  pair78_c0_r2<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
-  pair78_c1_r0<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
-  pair78_c1_r1<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
-  pair78_c1_r2<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
-  pair78_c2_r0<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
-  pair78_c2_r1<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
-  pair78_c2_r2<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
-  self78<<<(p.num + 127) / 128, 128, 0, st>>>(p.num, mc, base, lda);
+  ::ibem::count_launch(), pair78_c0_r0<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
+  ::ibem::count_launch(), pair78_c0_r1<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
+  ::ibem::count_launch(), pair78_c0_r2<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
+  ::ibem::count_launch(), pair78_c1_r0<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
+  ::ibem::count_launch(), pair78_c1_r1<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
+  ::ibem::count_launch(), pair78_c1_r2<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
+  ::ibem::count_launch(), pair78_c2_r0<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
+  ::ibem::count_launch(), pair78_c2_r1<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
+  ::ibem::count_launch(), pair78_c2_r2<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
+  ::ibem::count_launch(), self78<<<(p.num + 127) / 128, 128, 0, st>>>(p.num, mc, base, lda);
   IBEM_LAUNCH_CHECK("pair78");
   return IBEM_OK;
 }
@@ -38,7 +38,7 @@ ibem_status launch_node78(const SphLaunch& p, const double* nodes, int NN, doubl
                           int64_t row0, int64_t col0, cudaStream_t st) {
   SphMat mc = sph_mat_init(p.E0, p.nu0, p.E1, p.nu1);
   dim3 grid((NN + kPairThreads - 1) / kPairThreads, p.num);
-  node78<<<grid, kPairThreads, 0, st>>>(nodes, NN, p.cen, p.rad, mc, H + col0 * ldh + row0, ldh);
+  ::ibem::count_launch(), node78<<<grid, kPairThreads, 0, st>>>(nodes, NN, p.cen, p.rad, mc, H + col0 * ldh + row0, ldh);
   IBEM_LAUNCH_CHECK("node78");
   return IBEM_OK;
 }
@@ -46,7 +46,7 @@ ibem_status launch_node78(const SphLaunch& p, const double* nodes, int NN, doubl
 ibem_status launch_field78(const SphLaunch& p, const double* pts, int nump, const double* E,
                            double* stress, cudaStream_t st) {
   SphMat mc = sph_mat_init(p.E0, p.nu0, p.E1, p.nu1);
-  field78<<<(nump + kFieldThreads - 1) / kFieldThreads, kFieldThreads, 0, st>>>(
+  ::ibem::count_launch(), field78<<<(nump + kFieldThreads - 1) / kFieldThreads, kFieldThreads, 0, st>>>(
       pts, nump, p.cen, p.rad, p.num, mc, E, stress);
   IBEM_LAUNCH_CHECK("field78");
   return IBEM_OK;

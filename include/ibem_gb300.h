@@ -47,6 +47,9 @@ typedef struct {
 /* Message of the last failing call on this host thread. */
 const char* ibem_last_error(void);
 
+/* Number of kernels this library has launched since it was loaded (all threads). */
+long long ibem_kernel_launches(void);
+
 /* Number of unknowns per particle of a layout (24, 60, 78), or -1. */
 int ibem_layout_size(int layout);
 
@@ -127,7 +130,9 @@ typedef enum {
 } ibem_solver_form;
 
 typedef struct {
-  double backward_error;   /* ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) */
+  /* backward error of the equilibrated system As ys = bs (As = R A C, bs = R b, x = C ys,
+   * R and C the row/column max scalings): ||bs - As ys|| / (||As|| ||ys|| + ||bs||), inf-norms */
+  double backward_error;
   int iterations;          /* refinement / GMRES iterations (0 for FP64) */
   int info;                /* 0, or the first zero pivot (1-based) */
   double t_factor_ms, t_solve_ms;

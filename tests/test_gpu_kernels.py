@@ -49,10 +49,10 @@ def test_pair_blocks_vs_oracle(g, oracle_mod, layout):
     want = oracle_mod.pair_blocks(C, R, oracle_mod.mat(*MAT), layout)
     n = layout * len(R)
     pad = 5
-    A = torch.full((n + 2 * pad, n + 3 * pad), float("nan"), dtype=torch.float64, device="cuda")
-    lda = A.shape[1]   # torch row-major (rows=cols of the column-major view): use A^T storage
+    # torch is row-major: a (cols x rows) tensor is the column-major (rows x cols) matrix
     At = torch.full((n + 3 * pad, n + 2 * pad), float("nan"), dtype=torch.float64, device="cuda")
-    g.check(g.lib().ibem_e3d_pair_blocks(P(dev(C)), P(dev(R)), len(R), ctypes.byref(m), layout, P(At),
+    dC, dR = dev(C), dev(R)   # keep the device copies alive until the kernel has run
+    g.check(g.lib().ibem_e3d_pair_blocks(P(dC), P(dR), len(R), ctypes.byref(m), layout, P(At),
                                          At.shape[1], pad, 2 * pad, None))
     torch.cuda.synchronize()
     got = At.cpu().numpy().T   # column-major view: got[r, c] = At[c, r]
@@ -75,8 +75,10 @@ def test_node_blocks_vs_oracle(g, oracle_mod, layout):
     m = g.material(*MAT)
     NN = len(nodes)
     H = torch.zeros((layout * len(R), 3 * NN), dtype=torch.float64, device="cuda")  # column-major 3NN x nu*num
-    g.check(g.lib().ibem_e3d_node_blocks(P(dev(nodes)), NN, P(dev(C)), P(dev(R)), len(R), ctypes.byref(m), layout,
+    dn, dC, dR = dev(nodes), dev(C), dev(R)
+    g.check(g.lib().ibem_e3d_node_blocks(P(dn), NN, P(dC), P(dR), len(R), ctypes.byref(m), layout,
                                          P(H), 3 * NN, 0, 0, None))
+    torch.cuda.synchronize()
     got = H.cpu().numpy().T
     want = np.zeros((3 * NN, layout * len(R)), order="F")
     _d = ctypes.POINTER(ctypes.c_double)
@@ -103,6 +105,7 @@ def _tiny_device_matrices(g, layout=78):
     g.check(L.ibem_e3d_bem_to_incl(P(nodes), c.NN, P(conn), c.NE, P(cen), c.num, ctypes.byref(m), layout, P(Ht), N,
                                    0, P(Gt), N, 0, 3 * c.NN, None))
     torch.cuda.synchronize()
+    del nodes, conn, cen, rad
     return z, c, Ht, Gt
 
 
@@ -166,9 +169,10 @@ def test_field_vs_oracle(g, oracle_mod):
     n3 = 3 * c.NN
     E = z["U"][n3:]
     S = torch.zeros((c.nump, 6), dtype=torch.float64, device="cuda")
-    g.check(g.lib().ibem_e3d_field(P(dev(c.points)), c.nump, P(dev(c.centers)), P(dev(c.radius)), c.num,
-                                   ctypes.byref(m), 78, P(dev(E)), P(dev(c.nodes)), c.NN,
-                                   P(dev(c.conn.astype(np.int32))), c.NE, P(dev(z["U"])), P(dev(z["T"])), None,
-                                   P(S), None))
+    keep = [dev(c.points), dev(c.centers), dev(c.radius), dev(E), dev(c.nodes), dev(c.conn.astype(np.int32)),
+            dev(z["U"]), dev(z["T"])]
+    pts, cen, rad, dE, nodes, conn, dU, dT = keep
+    g.check(g.lib().ibem_e3d_field(P(pts), c.nump, P(cen), P(rad), c.num, ctypes.byref(m), 78, P(dE), P(nodes),
+                                   c.NN, P(conn), c.NE, P(dU), P(dT), None, P(S), None))
     torch.cuda.synchronize()
     assert scaled_err(S.cpu().numpy(), z["stress"]) < 1e-11
