@@ -272,6 +272,11 @@ ibem_status ibem_e3d_solve(ibem_solver_form form, int64_t N, double* A_dev, int6
   return solve_dense(form, N, A_dev, lda, b_dev, x_dev, tol, report, as_stream(stream));
 }
 
+ibem_status ibem_e3d_solve_noalloc(int64_t N, const double* A_dev, int64_t lda, const double* b_dev,
+                                   double* x_dev, ibem_solve_report* report, void* stream) {
+  return solve_fp64_noalloc(N, A_dev, lda, b_dev, x_dev, report, as_stream(stream));
+}
+
 ibem_status ibem_e3d_field(const double* points_dev, int nump, const double* centers_dev,
                            const double* radius_dev, int num, const ibem_material* mat,
                            int layout, const double* E_dev, const double* nodes_dev, int NN,

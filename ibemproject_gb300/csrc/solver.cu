@@ -23,6 +23,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <mutex>
 #include <vector>
 
 #include "ibem_internal.h"
@@ -903,6 +905,187 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
   cudaFree(tmp);
   if (rep) *rep = R;
   return s;
+}
+
+
+// ===================================================================================
+// Allocation-free FP64 solve for small systems (no counterpart in the reference).
+//
+// For callers that must not allocate device memory: applications whose device memory is
+// owned by a host framework (a caching allocator or a fixed budget reserved up front),
+// where a raw cudaMalloc can fail or fragment that budget, and latency-critical loops,
+// where cudaMalloc/cudaFree may synchronise the device.  The caller passes A, b and x;
+// every other buffer of the solve (the factor copy, scalings, pivots, permutation, the
+// panel kernel's candidate rows and grid barrier, residual scratch) lives in one
+// file-scope static __device__ array of kNoAllocBytes, so N is limited to kNoAllocMaxN.
+// The array is held by every GPU that loads the library until the process exits.
+// Its device address is looked up once per device, on that device's first call
+// (cudaGetSymbolAddress); make that first call before any stream capture.  All calls
+// share the array and it keeps the last call's contents: calls that overlap on the GPU
+// (other host threads, other streams) race and must be serialised by the caller.
+// ===================================================================================
+namespace {
+constexpr int64_t kNoAllocMaxN = 1024;
+constexpr int kNoAllocMaxCta = 256;   // panel kernel CTAs (>= SMs of one GPU)
+constexpr int kNoAllocParts = 16;
+constexpr size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+constexpr size_t kNaW = 0;                                                           // N x N factor copy
+constexpr size_t kNaVec = align256(sizeof(double) * kNoAllocMaxN * kNoAllocMaxN);    // 6 N-vectors
+constexpr size_t kNaPerm = kNaVec + 6 * align256(sizeof(double) * kNoAllocMaxN);     // perm, ipiv
+constexpr size_t kNaCand = kNaPerm + 2 * align256(sizeof(int) * kNoAllocMaxN);
+constexpr size_t kNaRowj = kNaCand + align256(sizeof(double) * 2 * kNoAllocMaxCta * (kLeaf + 2));
+constexpr size_t kNaGs = kNaRowj + align256(sizeof(double) * 2 * kLeaf);
+constexpr size_t kNaInfo = kNaGs + align256(sizeof(GridSync));
+constexpr size_t kNaPart = kNaInfo + align256(sizeof(int));
+constexpr size_t kNaRed = kNaPart + align256(sizeof(double) * kNoAllocParts * kNoAllocMaxN);
+constexpr size_t kNoAllocBytes = kNaRed + align256(sizeof(double) * 4);
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_base[kNoAllocMaxDevices] = {};
+int g_noalloc_ncta[kNoAllocMaxDevices] = {};
+int g_noalloc_rows_cap[kNoAllocMaxDevices] = {};
+
+// row exchanges (LAPACK ipiv) -> gather permutation, one thread (N <= kNoAllocMaxN)
+__global__ void k_ipiv_to_perm(int64_t n, const int* __restrict__ ipiv, int* __restrict__ perm) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  for (int64_t i = 0; i < n; ++i) perm[i] = (int)i;
+  for (int64_t i = 0; i < n; ++i) {
+    int p = ipiv[i];
+    if (p < 0 || p >= n) p = (int)i;  // never index outside (a bad pivot shows in info)
+    const int t = perm[i];
+    perm[i] = perm[p];
+    perm[p] = t;
+  }
+}
+
+// out[0..3] = max|a|, max|b|, max|c|, max|d| over n entries (one block)
+__global__ void k_absmax4(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
+                          const double* __restrict__ c, const double* __restrict__ d, double* __restrict__ out) {
+  __shared__ double red[4][256];
+  double m[4] = {0, 0, 0, 0};
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    m[0] = fmax(m[0], fabs(a[i]));
+    m[1] = fmax(m[1], fabs(b[i]));
+    m[2] = fmax(m[2], fabs(c[i]));
+    m[3] = fmax(m[3], fabs(d[i]));
+  }
+  for (int q = 0; q < 4; ++q) red[q][threadIdx.x] = m[q];
+  __syncthreads();
+  for (int t = blockDim.x / 2; t > 0; t >>= 1) {
+    if (threadIdx.x < t)
+      for (int q = 0; q < 4; ++q) red[q][threadIdx.x] = fmax(red[q][threadIdx.x], red[q][threadIdx.x + t]);
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) out[threadIdx.x] = red[threadIdx.x][0];
+}
+}  // namespace
+
+static ibem_status noalloc_setup(int dev, unsigned char** base, int* ncta, int* rows_cap) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(IBEM_ERR_ARG, "solve_noalloc: device index out of range");
+  if (!g_noalloc_base[dev]) {
+    void* p = nullptr;
+    IBEM_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    int nsm = 0, smem_optin = 0;
+    IBEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    IBEM_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (nsm > kNoAllocMaxCta) return fail(IBEM_ERR_ARG, "solve_noalloc: more SMs than the static panel scratch holds");
+    const int static_smem = 2 * kLeaf * (int)sizeof(double) + 64;
+    const int dyn_cap = std::min(smem_optin - static_smem - 1024, 200 * 1024);
+    IBEM_CUDA(cudaFuncSetAttribute((const void*)k_panel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   dyn_cap));
+    int per_sm = 0;
+    const int cap = dyn_cap / (kLeaf * (int)sizeof(double));
+    IBEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_panel<double>, kPanelThreads,
+                                                            (size_t)cap * kLeaf * sizeof(double)));
+    if (per_sm < 1) return fail(IBEM_ERR_CUDA, "solve_noalloc: panel kernel cannot be resident");
+    g_noalloc_ncta[dev] = nsm;
+    g_noalloc_rows_cap[dev] = cap;
+    g_noalloc_base[dev] = static_cast<unsigned char*>(p);
+  }
+  *base = g_noalloc_base[dev];
+  *ncta = g_noalloc_ncta[dev];
+  *rows_cap = g_noalloc_rows_cap[dev];
+  return IBEM_OK;
+}
+
+ibem_status solve_fp64_noalloc(int64_t N, const double* A, int64_t lda, const double* b, double* x,
+                               ibem_solve_report* rep, cudaStream_t st) {
+  if (N <= 0 || N > kNoAllocMaxN) {
+    char buf[128];
+    std::snprintf(buf, sizeof buf, "solve_noalloc: N = %lld outside 1..%lld (the static workspace limit)",
+                  (long long)N, (long long)kNoAllocMaxN);
+    return fail(IBEM_ERR_ARG, buf);
+  }
+  if (!A || !b || !x || lda < N) return fail(IBEM_ERR_ARG, "solve_noalloc: bad pointers or lda");
+  int dev = 0;
+  IBEM_CUDA(cudaGetDevice(&dev));
+  unsigned char* base = nullptr;
+  int ncta = 0, rows_cap = 0;
+  ibem_status s = noalloc_setup(dev, &base, &ncta, &rows_cap);
+  if (s) return s;
+  double* W = reinterpret_cast<double*>(base + kNaW);
+  double* vec[6];
+  for (int i = 0; i < 6; ++i) vec[i] = reinterpret_cast<double*>(base + kNaVec + i * align256(sizeof(double) * kNoAllocMaxN));
+  double *r = vec[0], *c = vec[1], *bs = vec[2], *ys = vec[3], *tmp = vec[4], *rv = vec[5];
+  int* perm = reinterpret_cast<int*>(base + kNaPerm);
+  int* ipiv = reinterpret_cast<int*>(base + kNaPerm + align256(sizeof(int) * kNoAllocMaxN));
+  GridSync* gs = reinterpret_cast<GridSync*>(base + kNaGs);
+  int* info = reinterpret_cast<int*>(base + kNaInfo);
+  double* part = reinterpret_cast<double*>(base + kNaPart);
+  double* red = reinterpret_cast<double*>(base + kNaRed);
+  // the previous call's contents are still there: clear what must start at zero
+  IBEM_CUDA(cudaMemsetAsync(gs, 0, sizeof(GridSync), st));
+  IBEM_CUDA(cudaMemsetAsync(info, 0, sizeof(int), st));
+  const unsigned nb = (unsigned)((N + 255) / 256);
+  ::ibem::count_launch(), k_rowmax<<<nb, 256, 0, st>>>(N, A, lda, r);
+  ::ibem::count_launch(), k_colmax<<<(unsigned)N, 256, 0, st>>>(N, A, lda, r, c);
+  ::ibem::count_launch(), k_scale_copy<double><<<dim3(nb, (unsigned)N), 256, 0, st>>>(N, A, lda, r, c, W, N);
+  IBEM_LAUNCH_CHECK("solve_noalloc: equilibrate");
+  LuWork<double> w;
+  w.cand = reinterpret_cast<double*>(base + kNaCand);
+  w.rowj = reinterpret_cast<double*>(base + kNaRowj);
+  w.ipiv_dev = ipiv;
+  w.perm = perm;
+  w.tmp = tmp;
+  w.info = info;
+  w.gs = gs;
+  w.ncta = ncta;
+  w.rows_cap = rows_cap;
+  if ((s = lu_rec<double>(W, N, N, 0, N, w, st))) return s;
+  ::ibem::count_launch(), k_ipiv_to_perm<<<1, 1, 0, st>>>(N, ipiv, perm);
+  ::ibem::count_launch(), k_vmul<<<nb, 256, 0, st>>>(N, r, b, bs);
+  IBEM_CUDA(cudaMemcpyAsync(ys, bs, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+  if ((s = lu_apply<double>(W, N, N, perm, tmp, ys, st))) return s;
+  ::ibem::count_launch(), k_vmul<<<nb, 256, 0, st>>>(N, c, ys, x);
+  // scaled backward error, reduced on the device
+  ::ibem::count_launch(), k_vmul<<<nb, 256, 0, st>>>(N, c, ys, tmp);
+  const int64_t chunk = (N + kNoAllocParts - 1) / kNoAllocParts;
+  ::ibem::count_launch(), k_gemv_part<<<dim3(nb, kNoAllocParts), 256, 0, st>>>(N, A, lda, tmp, chunk, part);
+  ::ibem::count_launch(), k_scale_rows_of_parts<<<nb, 256, 0, st>>>(N, kNoAllocParts, part, r, rv);
+  ::ibem::count_launch(), k_axpby<<<nb, 256, 0, st>>>(N, 1.0, bs, -1.0, rv);
+  ::ibem::count_launch(), k_scaled_rowsum<<<nb, 256, 0, st>>>(N, A, lda, r, c, tmp);
+  ::ibem::count_launch(), k_absmax4<<<1, 256, 0, st>>>(N, rv, ys, bs, tmp, red);
+  IBEM_LAUNCH_CHECK("solve_noalloc");
+  double h[4] = {0, 0, 0, 0};
+  int hinfo = 0;
+  GridSync hgs{};
+  IBEM_CUDA(cudaMemcpyAsync(h, red, sizeof h, cudaMemcpyDeviceToHost, st));
+  IBEM_CUDA(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
+  IBEM_CUDA(cudaMemcpyAsync(&hgs, gs, sizeof(GridSync), cudaMemcpyDeviceToHost, st));
+  IBEM_CUDA(cudaStreamSynchronize(st));
+  if (rep) {
+    ibem_solve_report R{};
+    R.backward_error = h[0] / (h[3] * h[1] + h[2]);
+    R.info = hinfo;
+    *rep = R;
+  }
+  if (hgs.err) return fail(IBEM_ERR_TIMEOUT, "solve_noalloc: panel grid barrier gave up");
+  if (hinfo) return fail(IBEM_ERR_SINGULAR, "solve_noalloc: zero pivot");
+  return IBEM_OK;
 }
 
 }  // namespace ibem

@@ -16,4 +16,8 @@ ibem_status gemm_sub_f32_tc(int64_t m, int64_t n, int64_t k, const float* A, int
 ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda, const double* b, double* x,
                         double tol, ibem_solve_report* rep, cudaStream_t st);
 
+// Allocation-free FP64 solve for N <= 1024 (workspace in a static device array).
+ibem_status solve_fp64_noalloc(int64_t N, const double* A, int64_t lda, const double* b, double* x,
+                               ibem_solve_report* rep, cudaStream_t st);
+
 }  // namespace ibem

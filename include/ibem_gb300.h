@@ -146,6 +146,21 @@ ibem_status ibem_e3d_solve(ibem_solver_form form, int64_t N, double* A_dev, int6
                            const double* b_dev, double* x_dev, double tol,
                            ibem_solve_report* report, void* stream);
 
+/* The plain FP64 solve of ibem_e3d_solve for callers that may not allocate device
+ * memory; it has no counterpart in the reference.  Meant for code whose device memory
+ * belongs to a host framework (a caching allocator or a budget reserved up front, where a
+ * raw cudaMalloc can fail or fragment that budget) and for latency-critical loops, where
+ * cudaMalloc/cudaFree can stall the device.  The caller owns A_dev (left intact), b_dev
+ * and x_dev; the rest of the workspace is one static device array of about 9 MB inside
+ * the library, held by every GPU that loads it until the process exits, which limits N
+ * to 1024 (larger N returns IBEM_ERR_ARG).  The first call on a device looks the array's
+ * address up (setup), so make it before any stream capture.  Every call reuses the same
+ * array: calls that overlap on the GPU (from several host threads or streams) race and
+ * must be serialised by the caller.  Synchronous; report gets the scaled backward error
+ * and info as for ibem_e3d_solve (timings are left 0). */
+ibem_status ibem_e3d_solve_noalloc(int64_t N, const double* A_dev, int64_t lda, const double* b_dev,
+                                   double* x_dev, ibem_solve_report* report, void* stream);
+
 /* ---- postProcessor (postProcessorElastic3D.cpp) -------------------------- */
 
 /* Stress at sample points: replaces postProcessorElastic3D::getFlux

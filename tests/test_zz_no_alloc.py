@@ -1,0 +1,67 @@
+"""ibem_e3d_solve_noalloc: the allocation-free FP64 solve, for callers whose device memory
+belongs to a host framework (a caching allocator or a reserved budget) or who cannot
+afford cudaMalloc/cudaFree stalls in a latency-critical loop.
+
+It is checked through the C ABI against ibem_e3d_solve (plain FP64 form) on two calls in
+a row with different systems, so the second call must clear and reuse the static
+workspace the first one left behind.  Tolerance: 1e-9 of the largest entry, as for the
+eigenstrain coefficients in the other GPU tests.  This file is collected last so that a
+run stopping at the first failure has already run every other test."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import case_from_npz, golden, scaled_err
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _systems(oracle_mod):
+    from ibemproject_gb300 import cases
+    z = golden("tiny_reference.npz")
+    c = case_from_npz(z)
+    A1, b1, _, _ = oracle_mod.apply_bc(c, z["HMAT"], z["GMAT"])          # bounded cube, N = 234
+    f = cases.farfield_case(num=30, r0=0.05, vf=0.1, grid=0, seed=4)
+    m = f.orc_mat()
+    A2 = oracle_mod.pair_blocks(f.centers, f.radius, m, 24)               # 30 spheres, N = 720
+    b2 = oracle_mod.farfield_rhs(f.num, m, 24, f.sig_inf)
+    return [(np.asfortranarray(A1), b1), (np.asfortranarray(A2), b2)]
+
+
+def _solve(g, fn, A, b):
+    N = len(b)
+    At = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()   # row-major A^T == column-major A
+    bt = torch.from_numpy(np.ascontiguousarray(b)).cuda()
+    xt = torch.zeros(N, dtype=torch.float64, device="cuda")
+    rep = g.SolveReport()
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    if fn == "noalloc":
+        st = g.lib().ibem_e3d_solve_noalloc(N, P(At), N, P(bt), P(xt), ctypes.byref(rep), None)
+    else:
+        st = g.lib().ibem_e3d_solve(g.SOLVE_FP64, N, P(At), N, P(bt), P(xt), 1e-12, ctypes.byref(rep), None)
+    g.check(st)
+    torch.cuda.synchronize()
+    # A is left intact by both entry points
+    assert torch.equal(At.cpu(), torch.from_numpy(np.ascontiguousarray(A.T)))
+    return xt.cpu().numpy(), rep
+
+
+def test_noalloc_solve_matches_allocating_solve_twice(oracle_mod):
+    import ibemproject_gb300 as g
+    g.lib()
+    for A, b in _systems(oracle_mod):          # two calls in a row on different systems
+        x_ref, _ = _solve(g, "alloc", A, b)
+        x_na, rep = _solve(g, "noalloc", A, b)
+        assert scaled_err(x_na, x_ref) < 1e-9
+        assert rep.info == 0 and rep.backward_error < 1e-13
+
+
+def test_noalloc_rejects_sizes_beyond_its_workspace():
+    import ibemproject_gb300 as g
+    big = 1025
+    st = g.lib().ibem_e3d_solve_noalloc(big, ctypes.c_void_p(1), big, ctypes.c_void_p(1), ctypes.c_void_p(1),
+                                        None, None)
+    assert st == g.IBEM_ERR_ARG
+    assert b"1024" in g.lib().ibem_last_error()
