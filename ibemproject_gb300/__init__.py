@@ -64,6 +64,7 @@ SIGNATURES = {
     "ibem_e3d_get_ut": (_int, [_int, _int, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "ibem_e3d_farfield_rhs": (_int, [_int, ctypes.POINTER(Material), _int, _c_dp, _vp, _vp]),
     "ibem_e3d_solve": (_int, [_int, _i64, _vp, _i64, _vp, _vp, _dbl, ctypes.POINTER(SolveReport), _vp]),
+    "ibem_gemm_sub_f32": (_int, [_i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp]),
     "ibem_e3d_solve_noalloc": (_int, [_i64, _vp, _i64, _vp, _vp, ctypes.POINTER(SolveReport), _vp]),
     "ibem_e3d_field": (_int, [_vp, _int, _vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _vp, _int, _vp,
                               _int, _vp, _vp, _c_dp, _vp, _vp]),

@@ -272,6 +272,33 @@ ibem_status ibem_e3d_solve(ibem_solver_form form, int64_t N, double* A_dev, int6
   return solve_dense(form, N, A_dev, lda, b_dev, x_dev, tol, report, as_stream(stream));
 }
 
+ibem_status ibem_gemm_sub_f32(int64_t m, int64_t n, int64_t k, const float* A_dev, int64_t lda,
+                              const float* B_dev, int64_t ldb, float* C_dev, int64_t ldc, void* stream) {
+  if (m < 0 || n < 0 || k < 0 || lda < m || ldb < k || ldc < m) return fail(IBEM_ERR_ARG, "gemm_sub_f32: bad sizes");
+  if (m == 0 || n == 0 || k == 0) return IBEM_OK;
+  cudaStream_t st = as_stream(stream);
+  const size_t ws_bytes = gemm_tc_workspace_bytes(m, n);
+  void* ws = nullptr;
+  int* err = nullptr;
+  IBEM_CUDA(cudaMalloc(&ws, ws_bytes));
+  cudaError_t ce = cudaMalloc(&err, sizeof(int));
+  if (ce != cudaSuccess) { cudaFree(ws); return cuda_fail(ce, "gemm_sub_f32"); }
+  ibem_status s = IBEM_OK;
+  ce = cudaMemsetAsync(err, 0, sizeof(int), st);
+  if (ce != cudaSuccess) s = cuda_fail(ce, "gemm_sub_f32");
+  if (!s) s = gemm_sub_f32_tc(m, n, k, A_dev, lda, B_dev, ldb, C_dev, ldc, ws, ws_bytes, err, st);
+  int herr = 0;
+  if (!s) {
+    ce = cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) s = cuda_fail(ce, "gemm_sub_f32");
+    else if (herr) s = fail(IBEM_ERR_TIMEOUT, "gemm_sub_f32: a device-side wait gave up");
+  }
+  cudaFree(ws);
+  cudaFree(err);
+  return s;
+}
+
 ibem_status ibem_e3d_solve_noalloc(int64_t N, const double* A_dev, int64_t lda, const double* b_dev,
                                    double* x_dev, ibem_solve_report* report, void* stream) {
   return solve_fp64_noalloc(N, A_dev, lda, b_dev, x_dev, report, as_stream(stream));

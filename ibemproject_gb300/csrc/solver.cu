@@ -409,6 +409,9 @@ struct LuWork {
   GridSync* gs = nullptr;
   int ncta = 0;
   int rows_cap = 0;
+  void* gemm_ws = nullptr;   // BF16 split workspace of the tensor-core GEMM (FP32 LU only)
+  size_t gemm_ws_bytes = 0;
+  int* gemm_err = nullptr;   // raised by the tensor-core GEMM's bounded waits
 };
 
 template <typename T>
@@ -434,11 +437,12 @@ static ibem_status panel(T* A, int64_t lda, int64_t k0, int64_t m, int nb, LuWor
 
 template <typename T>
 static ibem_status gemm_sub(int64_t m, int64_t n, int64_t k, const T* A, int64_t lda, const T* B, int64_t ldb,
-                            T* C, int64_t ldc, cudaStream_t st);
+                            T* C, int64_t ldc, LuWork<T>& w, cudaStream_t st);
 
 template <>
 ibem_status gemm_sub<double>(int64_t m, int64_t n, int64_t k, const double* A, int64_t lda, const double* B,
-                             int64_t ldb, double* C, int64_t ldc, cudaStream_t st) {
+                             int64_t ldb, double* C, int64_t ldc, LuWork<double>& w, cudaStream_t st) {
+  (void)w;
   if (m <= 0 || n <= 0 || k <= 0) return IBEM_OK;
   dim3 grid((unsigned)((m + 63) / 64), (unsigned)((n + 63) / 64));
   ::ibem::count_launch(), k_gemm_sub<double><<<grid, 256, 0, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
@@ -448,8 +452,11 @@ ibem_status gemm_sub<double>(int64_t m, int64_t n, int64_t k, const double* A, i
 
 template <>
 ibem_status gemm_sub<float>(int64_t m, int64_t n, int64_t k, const float* A, int64_t lda, const float* B,
-                            int64_t ldb, float* C, int64_t ldc, cudaStream_t st) {
+                            int64_t ldb, float* C, int64_t ldc, LuWork<float>& w, cudaStream_t st) {
   if (m <= 0 || n <= 0 || k <= 0) return IBEM_OK;
+  // tensor cores for every update large enough to fill 128 x 256 tiles; small ones on CUDA cores
+  if (w.gemm_ws && m >= 128 && n >= 128 && k >= 32)
+    return gemm_sub_f32_tc(m, n, k, A, lda, B, ldb, C, ldc, w.gemm_ws, w.gemm_ws_bytes, w.gemm_err, st);
   dim3 grid((unsigned)((m + 63) / 64), (unsigned)((n + 63) / 64));
   ::ibem::count_launch(), k_gemm_sub<float><<<grid, 256, 0, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
   IBEM_LAUNCH_CHECK("gemm f32");
@@ -458,7 +465,8 @@ ibem_status gemm_sub<float>(int64_t m, int64_t n, int64_t k, const float* A, int
 
 // B (n1 x n2) <- L^-1 B with L the unit-lower n1 x n1 block at L (recursive)
 template <typename T>
-static ibem_status trsm(const T* L, int64_t ldl, int64_t n1, T* B, int64_t ldb, int64_t n2, cudaStream_t st) {
+static ibem_status trsm(const T* L, int64_t ldl, int64_t n1, T* B, int64_t ldb, int64_t n2, LuWork<T>& w,
+                        cudaStream_t st) {
   if (n1 <= 0 || n2 <= 0) return IBEM_OK;
   if (n1 <= 64) {
     ::ibem::count_launch(), k_trsm_small<T><<<(unsigned)((n2 + 63) / 64), 64, 0, st>>>(L, ldl, (int)n1, B, ldb, n2);
@@ -466,11 +474,11 @@ static ibem_status trsm(const T* L, int64_t ldl, int64_t n1, T* B, int64_t ldb, 
     return IBEM_OK;
   }
   const int64_t h = std::max<int64_t>(kLeaf, (n1 / 2) / kLeaf * kLeaf);
-  ibem_status s = trsm(L, ldl, h, B, ldb, n2, st);
+  ibem_status s = trsm(L, ldl, h, B, ldb, n2, w, st);
   if (s) return s;
-  s = gemm_sub<T>(n1 - h, n2, h, L + h, ldl, B, ldb, B + h, ldb, st);
+  s = gemm_sub<T>(n1 - h, n2, h, L + h, ldl, B, ldb, B + h, ldb, w, st);
   if (s) return s;
-  return trsm(L + h * ldl + h, ldl, n1 - h, B + h, ldb, n2, st);
+  return trsm(L + h * ldl + h, ldl, n1 - h, B + h, ldb, n2, w, st);
 }
 
 // recursive LU of the m x n column block starting at (k0, k0) of A (m = N - k0).
@@ -495,9 +503,9 @@ static ibem_status lu_rec(T* A, int64_t lda, int64_t N, int64_t k0, int64_t n, L
   T* A12 = A + (k0 + n1) * lda + k0;
   T* A21 = A + k0 * lda + k0 + n1;
   T* A22 = A + (k0 + n1) * lda + k0 + n1;
-  s = trsm(A11, lda, n1, A12, lda, n2, st);
+  s = trsm(A11, lda, n1, A12, lda, n2, w, st);
   if (s) return s;
-  s = gemm_sub<T>(m - n1, n2, n1, A21, lda, A12, lda, A22, lda, st);
+  s = gemm_sub<T>(m - n1, n2, n1, A21, lda, A12, lda, A22, lda, w, st);
   if (s) return s;
   return lu_rec(A, lda, N, k0 + n1, n2, w, st);
 }
@@ -527,6 +535,12 @@ static ibem_status lu_alloc(LuWork<T>& w, int64_t N) {
   IBEM_CUDA(cudaMalloc(&w.gs, sizeof(GridSync)));
   IBEM_CUDA(cudaMemset(w.info, 0, sizeof(int)));
   IBEM_CUDA(cudaMemset(w.gs, 0, sizeof(GridSync)));
+  if (sizeof(T) == sizeof(float)) {
+    w.gemm_ws_bytes = gemm_tc_workspace_bytes(N, N / 2 + 2 * kLeaf);
+    IBEM_CUDA(cudaMalloc(&w.gemm_ws, w.gemm_ws_bytes));
+    IBEM_CUDA(cudaMalloc(&w.gemm_err, sizeof(int)));
+    IBEM_CUDA(cudaMemset(w.gemm_err, 0, sizeof(int)));
+  }
   return IBEM_OK;
 }
 
@@ -539,6 +553,8 @@ static void lu_free(LuWork<T>& w) {
   cudaFree(w.tmp);
   cudaFree(w.info);
   cudaFree(w.gs);
+  cudaFree(w.gemm_ws);
+  cudaFree(w.gemm_err);
   w = LuWork<T>();
 }
 
@@ -722,12 +738,14 @@ static ibem_status factor(SolveCtx& cx, const double* A, int64_t lda, T*& W, LuW
     IBEM_CUDA(cudaMemcpyAsync(w.perm, perm.data(), sizeof(int) * N, cudaMemcpyHostToDevice, cx.st));
     IBEM_CUDA(cudaStreamSynchronize(cx.st));
   }
-  int hinfo = 0;
+  int hinfo = 0, herr = 0;
   GridSync hgs;
   IBEM_CUDA(cudaMemcpyAsync(&hinfo, w.info, sizeof(int), cudaMemcpyDeviceToHost, cx.st));
   IBEM_CUDA(cudaMemcpyAsync(&hgs, w.gs, sizeof(GridSync), cudaMemcpyDeviceToHost, cx.st));
+  if (w.gemm_err) IBEM_CUDA(cudaMemcpyAsync(&herr, w.gemm_err, sizeof(int), cudaMemcpyDeviceToHost, cx.st));
   IBEM_CUDA(cudaStreamSynchronize(cx.st));
   if (hgs.err) return fail(IBEM_ERR_TIMEOUT, "panel grid barrier gave up");
+  if (herr) return fail(IBEM_ERR_TIMEOUT, "tensor-core GEMM wait gave up");
   info = hinfo;
   return IBEM_OK;
 }

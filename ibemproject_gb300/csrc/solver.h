@@ -10,8 +10,12 @@ namespace ibem {
 // C (m x n, ldc) -= A (m x k, lda) B (k x n, ldb), FP32 storage, column-major, computed on
 // the tensor cores with each operand split into two BF16 terms (hi + lo) and the three
 // products hi*hi + hi*lo + lo*hi accumulated in FP32.
+// `ws` is scratch of at least gemm_tc_workspace_bytes(max m, max n) bytes (the BF16 splits);
+// `err` a device int raised if a bounded device-side wait gave up.
 ibem_status gemm_sub_f32_tc(int64_t m, int64_t n, int64_t k, const float* A, int64_t lda, const float* B,
-                            int64_t ldb, float* C, int64_t ldc, cudaStream_t st);
+                            int64_t ldb, float* C, int64_t ldc, void* ws, size_t ws_bytes, int* err,
+                            cudaStream_t st);
+size_t gemm_tc_workspace_bytes(int64_t max_m, int64_t max_n);
 
 ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda, const double* b, double* x,
                         double tol, ibem_solve_report* rep, cudaStream_t st);

@@ -146,6 +146,14 @@ ibem_status ibem_e3d_solve(ibem_solver_form form, int64_t N, double* A_dev, int6
                            const double* b_dev, double* x_dev, double tol,
                            ibem_solve_report* report, void* stream);
 
+/* The trailing-update primitive of the mixed-precision factorisation, exposed for
+ * testing and reuse: C (m x n) -= A (m x k) B (k x n), FP32 column-major storage,
+ * computed on the tcgen05 tensor cores with each operand split into two BF16 terms
+ * (hi*hi + hi*lo + lo*hi, FP32 accumulation).  Allocates its scratch; synchronous.
+ * No reference counterpart (the reference's LU is Eigen's, on the CPU). */
+ibem_status ibem_gemm_sub_f32(int64_t m, int64_t n, int64_t k, const float* A_dev, int64_t lda,
+                              const float* B_dev, int64_t ldb, float* C_dev, int64_t ldc, void* stream);
+
 /* The plain FP64 solve of ibem_e3d_solve for callers that may not allocate device
  * memory; it has no counterpart in the reference.  Meant for code whose device memory
  * belongs to a host framework (a caching allocator or a budget reserved up front, where a

@@ -176,3 +176,21 @@ def test_field_vs_oracle(g, oracle_mod):
                                    c.NN, P(conn), c.NE, P(dU), P(dT), None, P(S), None))
     torch.cuda.synchronize()
     assert scaled_err(S.cpu().numpy(), z["stress"]) < 1e-11
+
+
+@pytest.mark.parametrize("m,n,k", [(256, 256, 64), (300, 520, 200), (1024, 768, 1000), (129, 257, 33)])
+def test_tensor_core_gemm(g, m, n, k):
+    """C -= A B on the tcgen05 tensor cores with split-BF16 operands: close to FP32 (the
+    dropped lo*lo term is ~2^-16 relative per product; tolerance 2e-5 of max|A||B| k)."""
+    gen = torch.Generator(device="cpu").manual_seed(m + n + k)
+    A = torch.randn(k, m, generator=gen, dtype=torch.float32).cuda()   # column-major m x k (lda = m)
+    B = torch.randn(n, k, generator=gen, dtype=torch.float32).cuda()   # column-major k x n (ldb = k)
+    C = torch.randn(n, m, generator=gen, dtype=torch.float32).cuda()   # column-major m x n (ldc = m)
+    want = C.double() - (A.double().T @ B.double().T).T
+    g.check(g.lib().ibem_gemm_sub_f32(m, n, k, P(A), m, P(B), k, P(C), m, None))
+    torch.cuda.synchronize()
+    err = (C.double() - want).abs().max().item()
+    scale = (A.abs().max() * B.abs().max()).item() * k
+    assert err < 2e-5 * scale, (err, scale)
+    # and much better than a plain BF16 product would be
+    assert err < 1e-4 * (A.double().T @ B.double().T).abs().max().item()
