@@ -117,6 +117,34 @@ def cpu_baseline(case, budget_s=20.0):
     }
 
 
+# ------------------------------------------------------------------ roofline
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops_sustained", 1700.0), "measured"
+    return 6800.0, 1700.0, "fallback"
+
+
+def roofline(prof):
+    """Roofline of the tensor-core GEMM (the trailing updates of the factorisation):
+    achieved = algorithmic flops (2 m n k per launch, the FP32 GEMM's work; split-BF16 issues
+    3 MMAs per product on top of that) / its event-timed duration, against the measured
+    sustained dense BF16 rate."""
+    hbm, tf, src = measured_peaks()
+    g = prof.get("gemm_tc")
+    if not g or g["ms"] <= 0:
+        return None
+    achieved = g["flops"] / (g["ms"] * 1e-3) / 1e12
+    return {"kernel": "k_umma_bf16x3 (gemm_tc)", "bound": "tensor", "achieved": achieved, "peak": tf,
+            "unit": "TFLOP/s", "frac": achieved / tf, "peak_source": f"{src} bf16_tflops_sustained",
+            "launches": g["launches"], "avg_launch_ms": g["ms"] / max(1, g["launches"]),
+            "flops_per_launch": g["flops"] / max(1, g["launches"]),
+            "tensor_flops_issued_per_launch": 3 * g["flops"] / max(1, g["launches"]),
+            "traffic": None}
+
+
 # ------------------------------------------------------------------ clocks
 class Clocks:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -208,8 +236,9 @@ def run_ours(args, rank, world):
         step()
     torch.cuda.synchronize()
     barrier()
-    clocks = Clocks(dev.index if "CUDA_VISIBLE_DEVICES" not in os.environ else dev.index)
+    clocks = Clocks(dev.index)
     clocks.start()
+    L.ibem_prof_enable(1)   # per-phase CUDA events on the launching stream, timed region only
     launches0 = L.ibem_kernel_launches()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
@@ -223,6 +252,8 @@ def run_ours(args, rank, world):
     barrier()
     launches = L.ibem_kernel_launches() - launches0
     ck = clocks.stop()
+    prof = g.prof_report()
+    L.ibem_prof_enable(0)
     ms = t0.elapsed_time(t1) / args.steps
     for ev in evs:
         stage_ms["assembly"].append(ev[0].elapsed_time(ev[1]))
@@ -262,7 +293,7 @@ def run_ours(args, rank, world):
         h2d = case.centers.nbytes + case.radius.nbytes + case.points.nbytes + 48
         d2h = 8 * N + 8 * 6 * nump
         e2e = {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
-    return case, ms, stage_ms, rep_mixed, plain, e2e, ck, launches
+    return case, ms, stage_ms, rep_mixed, plain, e2e, ck, launches, prof
 
 
 def main():
@@ -292,7 +323,7 @@ def main():
     import torch
     if world > 1:
         torch.distributed.init_process_group("nccl")
-    case, ms, stage_ms, rep_mixed, plain, e2e, ck, launches = run_ours(args, rank, world)
+    case, ms, stage_ms, rep_mixed, plain, e2e, ck, launches, prof = run_ours(args, rank, world)
     if rank == 0:
         cb = cpu_baseline(case, budget_s=args.cpu_budget) if world == 1 else None
         N = 24 * case.num
@@ -312,6 +343,9 @@ def main():
             "e2e": e2e,
             "clocks": ck,
             "gpu_launches": int(launches),
+            "profile_ms_per_step": {k: {"launches": v["launches"] / args.steps, "ms": v["ms"] / args.steps}
+                                    for k, v in prof.items()},
+            "roofline": roofline(prof),
             "cpu_baseline": cb,
         }
         print(json.dumps(line))

@@ -52,6 +52,8 @@ SIGNATURES = {
     "ibem_last_error": (ctypes.c_char_p, []),
     "ibem_layout_size": (_int, [_int]),
     "ibem_kernel_launches": (ctypes.c_longlong, []),
+    "ibem_prof_enable": (None, [_int]),
+    "ibem_prof_report": (_int, [ctypes.c_char_p, _int]),
     "ibem_e3d_pair_blocks": (_int, [_vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _i64, _i64, _i64, _vp]),
     "ibem_e3d_node_blocks": (_int, [_vp, _int, _vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _i64, _i64,
                                     _i64, _vp]),
@@ -146,3 +148,11 @@ def bc_plan(case):
     check(lib().ibem_e3d_bc_plan(case.NN, case.NE, _ip(conn), _dp(np.ascontiguousarray(case.bc, dtype=np.float64)),
                                  _dp(np.ascontiguousarray(case.tbc, dtype=np.float64)), _ip(ucol), _ip(tcol)))
     return ucol, tcol
+
+
+def prof_report() -> dict:
+    """Phase timings recorded since the last ibem_prof_enable (see include/ibem_gb300.h)."""
+    import json
+    buf = ctypes.create_string_buffer(1 << 16)
+    lib().ibem_prof_report(buf, len(buf))
+    return json.loads(buf.value.decode())

@@ -25,6 +25,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "prof.h"
 #include "solver.h"
 
 namespace ibem {
@@ -311,11 +312,14 @@ ibem_status gemm_sub_f32_tc(int64_t m, int64_t n, int64_t k, const float* A, int
     __nv_bfloat16* alo = ahi + (size_t)m * kp;
     __nv_bfloat16* bhi = alo + (size_t)m * kp;
     __nv_bfloat16* blo = bhi + (size_t)n * kp;
+    {
+      ProfScope psplit(PROF_GEMM_SPLIT, st);
     ::ibem::count_launch(), k_split_a<<<dim3((unsigned)((m + 31) / 32), (unsigned)(kp / 32)), dim3(32, 8), 0, st>>>(
         m, kc, A + k0 * lda, lda, kp, ahi, alo);
     ::ibem::count_launch(), k_split_b<<<dim3((unsigned)((kp + 255) / 256), (unsigned)n), 256, 0, st>>>(
         kc, n, B + k0, ldb, kp, bhi, blo);
-    IBEM_LAUNCH_CHECK("gemm_tc split");
+      IBEM_LAUNCH_CHECK("gemm_tc split");
+    }
     alignas(64) CUtensorMap maps[4];
     ibem_status s;
     if ((s = encode_map(&maps[0], ahi, m, kc, kp, BM))) return s;
@@ -323,6 +327,7 @@ ibem_status gemm_sub_f32_tc(int64_t m, int64_t n, int64_t k, const float* A, int
     if ((s = encode_map(&maps[2], bhi, n, kc, kp, BN))) return s;
     if ((s = encode_map(&maps[3], blo, n, kc, kp, BN))) return s;
     dim3 grid((unsigned)((m + BM - 1) / BM), (unsigned)((n + BN - 1) / BN));
+    ProfScope ps(PROF_GEMM_TC, st, 2.0 * m * n * kc);
     ::ibem::count_launch(), k_umma_bf16x3<<<grid, 128, SMEM_BYTES, st>>>(maps[0], maps[1], maps[2], maps[3], C,
                                                                            ldc, (int)m, (int)n, (int)(kp / BK), err);
     IBEM_LAUNCH_CHECK("gemm_tc");

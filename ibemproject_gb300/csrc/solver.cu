@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "ibem_internal.h"
+#include "prof.h"
 #include "solver.h"
 
 namespace ibem {
@@ -430,6 +431,7 @@ static ibem_status panel(T* A, int64_t lda, int64_t k0, int64_t m, int nb, LuWor
   int* ip = w.ipiv_dev + k0;
   int kg = (int)k0;
   void* args[] = {&P, &lda, &mm, &nb, &rows_per, &w.cand, &w.rowj, &ip, &kg, &w.info, &w.gs};
+  ProfScope ps(PROF_PANEL, st);
   count_launch();
   IBEM_CUDA(cudaLaunchCooperativeKernel((void*)k_panel<T>, dim3(ncta), dim3(kPanelThreads), args, smem, st));
   return IBEM_OK;
@@ -444,6 +446,7 @@ ibem_status gemm_sub<double>(int64_t m, int64_t n, int64_t k, const double* A, i
                              int64_t ldb, double* C, int64_t ldc, LuWork<double>& w, cudaStream_t st) {
   (void)w;
   if (m <= 0 || n <= 0 || k <= 0) return IBEM_OK;
+  ProfScope ps(PROF_GEMM_SIMT, st, 2.0 * m * n * k);
   dim3 grid((unsigned)((m + 63) / 64), (unsigned)((n + 63) / 64));
   ::ibem::count_launch(), k_gemm_sub<double><<<grid, 256, 0, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
   IBEM_LAUNCH_CHECK("gemm f64");
@@ -457,6 +460,7 @@ ibem_status gemm_sub<float>(int64_t m, int64_t n, int64_t k, const float* A, int
   // tensor cores for every update large enough to fill 128 x 256 tiles; small ones on CUDA cores
   if (w.gemm_ws && m >= 128 && n >= 128 && k >= 32)
     return gemm_sub_f32_tc(m, n, k, A, lda, B, ldb, C, ldc, w.gemm_ws, w.gemm_ws_bytes, w.gemm_err, st);
+  ProfScope ps(PROF_GEMM_SIMT, st, 2.0 * m * n * k);
   dim3 grid((unsigned)((m + 63) / 64), (unsigned)((n + 63) / 64));
   ::ibem::count_launch(), k_gemm_sub<float><<<grid, 256, 0, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
   IBEM_LAUNCH_CHECK("gemm f32");
@@ -469,6 +473,7 @@ static ibem_status trsm(const T* L, int64_t ldl, int64_t n1, T* B, int64_t ldb, 
                         cudaStream_t st) {
   if (n1 <= 0 || n2 <= 0) return IBEM_OK;
   if (n1 <= 64) {
+    ProfScope ps(PROF_TRSM_SMALL, st);
     ::ibem::count_launch(), k_trsm_small<T><<<(unsigned)((n2 + 63) / 64), 64, 0, st>>>(L, ldl, (int)n1, B, ldb, n2);
     IBEM_LAUNCH_CHECK("trsm_small");
     return IBEM_OK;
@@ -489,6 +494,7 @@ static ibem_status lu_rec(T* A, int64_t lda, int64_t N, int64_t k0, int64_t n, L
     ibem_status s = panel(A, lda, k0, m, (int)n, w, st);
     if (s) return s;
     // exchanges of this panel on the columns to its left and right (within [0, N))
+    ProfScope ps(PROF_LASWP, st);
     if (k0 > 0) ::ibem::count_launch(), k_laswp<T><<<(unsigned)((k0 + 127) / 128), 128, 0, st>>>(A, lda, k0, w.ipiv_dev + k0, (int)n, 0, k0);
     if (k0 + n < N)
       ::ibem::count_launch(), k_laswp<T><<<(unsigned)((N - k0 - n + 127) / 128), 128, 0, st>>>(A, lda, k0, w.ipiv_dev + k0, (int)n, k0 + n, N);
@@ -562,6 +568,7 @@ static void lu_free(LuWork<T>& w) {
 template <typename T>
 static ibem_status lu_apply(const T* F, int64_t ldf, int64_t N, const int* perm, double* tmp, double* y,
                             cudaStream_t st) {
+  ProfScope ps(PROF_TRSV, st, 2.0 * N * N);
   ::ibem::count_launch(), k_gather<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, perm, y, tmp);
   IBEM_CUDA(cudaMemcpyAsync(y, tmp, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
   const int nb = 64;
@@ -687,6 +694,7 @@ __global__ void k_scale_rows_of_parts(int64_t n, int nparts, const double* __res
 static ibem_status scaled_matvec(SolveCtx& cx, const double* A, int64_t lda, const double* v, double* tmp,
                                  double* y) {
   const int64_t N = cx.N;
+  ProfScope ps(PROF_MATVEC, cx.st, 2.0 * N * N);
   const unsigned nb = (unsigned)((N + 255) / 256);
   ::ibem::count_launch(), k_vmul<<<nb, 256, 0, cx.st>>>(N, cx.c, v, tmp);
   const int64_t chunk = (N + cx.nparts - 1) / cx.nparts;
@@ -713,6 +721,7 @@ static ibem_status scaled_backward_error(SolveCtx& cx, const double* A, int64_t 
 template <typename T>
 static ibem_status factor(SolveCtx& cx, const double* A, int64_t lda, T*& W, LuWork<T>& w, int& info) {
   const int64_t N = cx.N;
+  ProfScope ps(PROF_EQUIL, cx.st);
   ::ibem::count_launch(), k_rowmax<<<(unsigned)((N + 255) / 256), 256, 0, cx.st>>>(N, A, lda, cx.r);
   ::ibem::count_launch(), k_colmax<<<(unsigned)N, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c);
   IBEM_LAUNCH_CHECK("equilibrate");

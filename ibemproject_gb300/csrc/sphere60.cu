@@ -1,5 +1,6 @@
 // Sphere kernels for the 60-unknown layout (eigenstrain orders 0, 1 and 2, order 2 stored for p <= q ).
 #include "gen_sphere60.cuh"
+#include "prof.h"
 #include "sphere_kernels.cuh"
 
 #define IBEM_PAIRS_60(C) \
@@ -18,6 +19,7 @@ namespace ibem {
 ibem_status launch_pair60(const SphLaunch& p, double* A, int64_t lda, int64_t row0, int64_t col0,
                           cudaStream_t st) {
   SphMat mc = sph_mat_init(p.E0, p.nu0, p.E1, p.nu1);
+  ProfScope ps(PROF_PAIR, st);
   double* base = A + col0 * lda + row0;
   dim3 grid((p.num + kPairThreads - 1) / kPairThreads, p.num);
   ::ibem::count_launch(), pair60_c0_r0<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
@@ -46,6 +48,7 @@ ibem_status launch_node60(const SphLaunch& p, const double* nodes, int NN, doubl
 ibem_status launch_field60(const SphLaunch& p, const double* pts, int nump, const double* E,
                            double* stress, cudaStream_t st) {
   SphMat mc = sph_mat_init(p.E0, p.nu0, p.E1, p.nu1);
+  ProfScope ps(PROF_FIELD, st);
   ::ibem::count_launch(), field60<<<(nump + kFieldThreads - 1) / kFieldThreads, kFieldThreads, 0, st>>>(
       pts, nump, p.cen, p.rad, p.num, mc, E, stress);
   IBEM_LAUNCH_CHECK("field60");

@@ -50,6 +50,14 @@ const char* ibem_last_error(void);
 /* Number of kernels this library has launched since it was loaded (all threads). */
 long long ibem_kernel_launches(void);
 
+/* Phase profiler: with profiling on, CUDA events are recorded on the launching stream around
+ * each phase (pair blocks, field sums, panels, row exchanges, tensor-core GEMMs, ...);
+ * ibem_prof_enable(1) also clears what was recorded.  ibem_prof_report writes a JSON object
+ * {"phase": {"launches", "ms", "flops"}} into buf (synchronising the events) and returns its
+ * length.  Instrumentation for measurement; no reference counterpart. */
+void ibem_prof_enable(int on);
+int ibem_prof_report(char* buf, int cap);
+
 /* Number of unknowns per particle of a layout (24, 60, 78), or -1. */
 int ibem_layout_size(int layout);
 
