@@ -87,6 +87,12 @@ struct GridSync {
   int err;
 };
 
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 __device__ __forceinline__ bool grid_barrier(GridSync* gs, unsigned int nblocks, unsigned int& my_gen) {
   __syncthreads();
   __shared__ int s_ok;
@@ -100,8 +106,8 @@ __device__ __forceinline__ bool grid_barrier(GridSync* gs, unsigned int nblocks,
       atomicExch(&gs->gen, g + 1);
     } else {
       long long it = 0;
-      while (atomicAdd(&gs->gen, 0u) == g) {
-        if (++it > kSpinLimit || atomicAdd(&gs->err, 0) != 0) {
+      while (ld_acquire(&gs->gen) == g) {
+        if (++it > kSpinLimit || *reinterpret_cast<volatile int*>(&gs->err) != 0) {
           atomicExch(&gs->err, 1);
           ok = 0;
           break;
@@ -134,7 +140,8 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int6
   __shared__ T s_jr[kLeaf];                 // row j
   __shared__ T s_bv[kPanelThreads / 32];
   __shared__ int s_bi[kPanelThreads / 32];
-  __shared__ int s_piv;
+  __shared__ int s_src[kPanelThreads / 32];
+  __shared__ int s_piv, s_sel;
   const int cta = blockIdx.x, ncta = gridDim.x;
   const int r0 = cta * rows_per;
   const int nr = max(0, min(rows_per, m - r0));
@@ -182,28 +189,46 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int6
     }
     // (b) one barrier per column
     if (!grid_barrier(gs, ncta, my_gen)) return;
-    // (c) global pivot: identical choice in every CTA
-    if (threadIdx.x == 0) {
-      T b = -1;
-      int i = -1, src = -1;
-      for (int c = 0; c < ncta; ++c) {
-        const T* cd = cand + ((int64_t)buf * ncta + c) * (kLeaf + 2);
-        const T v = cd[kLeaf];
-        const int ci = (int)cd[kLeaf + 1];
-        if (ci < 0) continue;
-        if (v > b || (v == b && ci < i)) { b = v; i = ci; src = c; }
+    // (c) global pivot, identical in every CTA: parallel argmax over the CTA candidates
+    //     (largest |a|, ties to the smallest row; CTAs without a candidate never win)
+    {
+      T v = -1;
+      int ci = -1, src = -1;
+      if (threadIdx.x < ncta) {
+        const T* cd = cand + ((int64_t)buf * ncta + threadIdx.x) * (kLeaf + 2);
+        ci = (int)cd[kLeaf + 1];
+        v = ci >= 0 ? cd[kLeaf] : (T)-1;
+        src = threadIdx.x;
       }
-      s_piv = i;
-      s_bi[0] = src;
-      if (cta == 0) {
-        ipiv[j] = kglob + i;
-        if (b == 0 && *info == 0) *info = kglob + j + 1;
+      for (int off = 16; off > 0; off >>= 1) {
+        const T ov = __shfl_down_sync(0xffffffffu, v, off);
+        const int oi = __shfl_down_sync(0xffffffffu, ci, off);
+        const int os = __shfl_down_sync(0xffffffffu, src, off);
+        if (oi >= 0 && (ci < 0 || ov > v || (ov == v && oi < ci))) { v = ov; ci = oi; src = os; }
+      }
+      if (lane == 0) { s_bv[warp] = v; s_bi[warp] = ci; s_src[warp] = src; }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        T b = -1;
+        int i = -1, sr = -1;
+        for (int w = 0; w < kPanelThreads / 32; ++w)
+          if (s_bi[w] >= 0 && (i < 0 || s_bv[w] > b || (s_bv[w] == b && s_bi[w] < i))) {
+            b = s_bv[w];
+            i = s_bi[w];
+            sr = s_src[w];
+          }
+        s_piv = i;
+        s_sel = sr;
+        if (cta == 0) {
+          ipiv[j] = kglob + i;
+          if (b == 0 && *info == 0) *info = kglob + j + 1;
+        }
       }
     }
     __syncthreads();
     const int piv = s_piv;
     if (threadIdx.x < nb) {
-      s_pr[threadIdx.x] = cand[((int64_t)buf * ncta + s_bi[0]) * (kLeaf + 2) + threadIdx.x];
+      s_pr[threadIdx.x] = cand[((int64_t)buf * ncta + s_sel) * (kLeaf + 2) + threadIdx.x];
       s_jr[threadIdx.x] = rowj[buf * kLeaf + threadIdx.x];
     }
     __syncthreads();
@@ -247,26 +272,34 @@ __global__ void k_laswp(T* __restrict__ A, int64_t lda, int64_t k0, const int* _
 }
 
 // small triangular solve: B (n1 x n2) <- L^-1 B, L unit lower n1 x n1 (n1 <= 64);
-// one CTA per 64 columns of B, L staged in shared memory
+// one CTA per 64 columns of B, L and the B columns staged in shared memory, one thread
+// per column
 template <typename T>
 __global__ void __launch_bounds__(64) k_trsm_small(const T* __restrict__ L, int64_t ldl, int n1, T* __restrict__ B,
                                                    int64_t ldb, int64_t n2) {
-  __shared__ T sL[64 * 64];
+  extern __shared__ unsigned char trsm_smem[];
+  T* sL = reinterpret_cast<T*>(trsm_smem);  // [k][i] = L(i, k), 64 x 65
+  T* sB = sL + 64 * 65;                      // [i][c] = B(i, c0 + c), 64 x 65
+  const int64_t c0 = blockIdx.x * (int64_t)64;
   for (int idx = threadIdx.x; idx < n1 * n1; idx += blockDim.x) {
     const int i = idx % n1, k = idx / n1;
-    sL[k * 64 + i] = L[(int64_t)k * ldl + i];
+    sL[k * 65 + i] = L[(int64_t)k * ldl + i];
+  }
+  for (int idx = threadIdx.x; idx < n1 * 64; idx += blockDim.x) {
+    const int i = idx % n1, c = idx / n1;
+    sB[i * 65 + c] = (c0 + c < n2) ? B[(c0 + c) * ldb + i] : (T)0;
   }
   __syncthreads();
-  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= n2) return;
-  T* b = B + c * ldb;
-  T x[64];
-  for (int i = 0; i < n1; ++i) x[i] = b[i];
+  const int c = threadIdx.x;
   for (int i = 0; i < n1; ++i) {
-    const T xi = x[i];
-    for (int k = i + 1; k < n1; ++k) x[k] -= sL[i * 64 + k] * xi;
+    const T xi = sB[i * 65 + c];
+    for (int k = i + 1; k < n1; ++k) sB[k * 65 + c] -= sL[i * 65 + k] * xi;
   }
-  for (int i = 0; i < n1; ++i) b[i] = x[i];
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < n1 * 64; idx += blockDim.x) {
+    const int i = idx % n1, cc = idx / n1;
+    if (c0 + cc < n2) B[(c0 + cc) * ldb + i] = sB[i * 65 + cc];
+  }
 }
 
 // ---------------------------------------------------------------- SIMT GEMM  C -= A B
@@ -342,46 +375,60 @@ __global__ void k_residual(int64_t n, int nparts, const double* __restrict__ par
   r[i] = b[i] - s;
 }
 
-// blocked forward/backward substitution with the factors in precision T.
-// Diagonal block solve: one CTA; then GEMV update of the rows below/above.
-template <typename T>
-__global__ void k_trsv_diag(const T* __restrict__ F, int64_t ldf, int64_t k0, int nb, double* __restrict__ y,
-                            int lower) {
-  __shared__ double sy[64];
-  __shared__ double sF[64][65];
+// Blocked substitution with the factors in precision T (vectors FP64), one launch per
+// kTrsvB-row block.  Every CTA loads the diagonal block and the block's right-hand side,
+// solves the small triangle in shared memory (the same arithmetic in every CTA), CTA 0
+// stores the solved block to `out`, and each CTA applies the block column to its share of
+// the remaining rows of `y`.  `y` rows of the block are only read and other rows only
+// written within a launch, so CTAs never race.
+constexpr int kTrsvB = 128;
+template <typename T, bool LOWER>
+__global__ void __launch_bounds__(256) k_trsv_block(const T* __restrict__ F, int64_t ldf, int64_t N, int64_t k0,
+                                                    int nb, double* __restrict__ y, double* __restrict__ out) {
+  extern __shared__ unsigned char trsv_smem[];
+  T* sF = reinterpret_cast<T*>(trsv_smem);  // [c][r] = F(k0 + r, k0 + c), kTrsvB x (kTrsvB + 1)
+  double* sy = reinterpret_cast<double*>(trsv_smem + sizeof(T) * kTrsvB * (kTrsvB + 1) + 16);
   for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
-    const int i = idx % nb, k = idx / nb;
-    sF[i][k] = (double)F[(k0 + k) * ldf + k0 + i];
+    const int r = idx % nb, c = idx / nb;
+    sF[c * (kTrsvB + 1) + r] = F[(k0 + c) * ldf + k0 + r];
   }
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) sy[i] = y[k0 + i];
+  for (int r = threadIdx.x; r < nb; r += blockDim.x) sy[r] = y[k0 + r];
   __syncthreads();
-  if (threadIdx.x == 0) {
-    if (lower) {
-      for (int i = 0; i < nb; ++i) {
-        double s = sy[i];
-        for (int k = 0; k < i; ++k) s -= sF[i][k] * sy[k];
-        sy[i] = s;
-      }
-    } else {
-      for (int i = nb - 1; i >= 0; --i) {
-        double s = sy[i];
-        for (int k = i + 1; k < nb; ++k) s -= sF[i][k] * sy[k];
-        sy[i] = s / sF[i][i];
-      }
+  const int t = threadIdx.x;
+  if (LOWER) {
+    for (int j = 0; j < nb; ++j) {
+      if (t > j && t < nb) sy[t] -= (double)sF[j * (kTrsvB + 1) + t] * sy[j];
+      __syncthreads();
+    }
+  } else {
+    for (int j = nb - 1; j >= 0; --j) {
+      if (t == j) sy[j] /= (double)sF[j * (kTrsvB + 1) + j];
+      __syncthreads();
+      if (t < j) sy[t] -= (double)sF[j * (kTrsvB + 1) + t] * sy[j];
+      __syncthreads();
     }
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) y[k0 + i] = sy[i];
-}
-// y[r] -= sum_{k in [k0,k0+nb)} F[r,k] y[k] for rows r in [r0, r1)
-template <typename T>
-__global__ void k_trsv_update(const T* __restrict__ F, int64_t ldf, int64_t k0, int nb, int64_t r0, int64_t r1,
-                              double* __restrict__ y) {
+  if (blockIdx.x == 0)
+    for (int r = threadIdx.x; r < nb; r += blockDim.x) out[k0 + r] = sy[r];
+  const int64_t r0 = LOWER ? k0 + nb : 0, r1 = LOWER ? N : k0;
   const int64_t r = r0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= r1) return;
-  double s = 0;
-  for (int k = 0; k < nb; ++k) s += (double)F[(k0 + k) * ldf + r] * y[k0 + k];
-  y[r] -= s;
+  if (r < r1) {
+    double acc = 0;
+    for (int c = 0; c < nb; ++c) acc += (double)F[(k0 + c) * ldf + r] * sy[c];
+    y[r] -= acc;
+  }
+}
+
+template <typename T>
+cudaError_t set_solver_smem_attrs() {
+  cudaError_t e = cudaFuncSetAttribute((const void*)k_trsm_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(2 * 64 * 65 * sizeof(T)));
+  const int tb = (int)(sizeof(T) * kTrsvB * (kTrsvB + 1) + 16 + sizeof(double) * kTrsvB);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute((const void*)k_trsv_block<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute((const void*)k_trsv_block<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb);
+  return e;
 }
 
 // out[i] = y[perm[i]]  (P y with P the row permutation of the factorisation)
@@ -474,7 +521,8 @@ static ibem_status trsm(const T* L, int64_t ldl, int64_t n1, T* B, int64_t ldb, 
   if (n1 <= 0 || n2 <= 0) return IBEM_OK;
   if (n1 <= 64) {
     ProfScope ps(PROF_TRSM_SMALL, st);
-    ::ibem::count_launch(), k_trsm_small<T><<<(unsigned)((n2 + 63) / 64), 64, 0, st>>>(L, ldl, (int)n1, B, ldb, n2);
+    ::ibem::count_launch(), k_trsm_small<T><<<(unsigned)((n2 + 63) / 64), 64, 2 * 64 * 65 * sizeof(T), st>>>(
+        L, ldl, (int)n1, B, ldb, n2);
     IBEM_LAUNCH_CHECK("trsm_small");
     return IBEM_OK;
   }
@@ -526,11 +574,13 @@ static ibem_status lu_alloc(LuWork<T>& w, int64_t N) {
   int dyn_cap = std::min(smem_optin - static_smem - 1024, 200 * 1024);
   w.rows_cap = dyn_cap / (kLeaf * (int)sizeof(T));
   IBEM_CUDA(cudaFuncSetAttribute((const void*)k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_cap));
+  IBEM_CUDA(set_solver_smem_attrs<T>());
   int per_sm = 0;
   IBEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_panel<T>, kPanelThreads,
                                                           (size_t)w.rows_cap * kLeaf * sizeof(T)));
   if (per_sm < 1) return fail(IBEM_ERR_CUDA, "panel kernel cannot be resident");
-  w.ncta = nsm;  // one CTA per SM (all co-resident for the cooperative launch)
+  w.ncta = std::min(nsm, kPanelThreads);  // one CTA per SM (co-resident for the cooperative launch);
+                                          // the candidate argmax uses one thread per CTA
   if ((int64_t)w.ncta * w.rows_cap < N) return fail(IBEM_ERR_ARG, "matrix too large for the panel kernel");
   IBEM_CUDA(cudaMalloc(&w.cand, sizeof(T) * 2 * (size_t)w.ncta * (kLeaf + 2)));
   IBEM_CUDA(cudaMalloc(&w.rowj, sizeof(T) * 2 * kLeaf));
@@ -564,25 +614,27 @@ static void lu_free(LuWork<T>& w) {
   w = LuWork<T>();
 }
 
-// Solve with the factors F (precision T): y <- U^-1 L^-1 P y (y FP64, in place)
+// Solve with the factors F (precision T): y <- U^-1 L^-1 P y (y FP64, in place; tmp N-vector)
 template <typename T>
 static ibem_status lu_apply(const T* F, int64_t ldf, int64_t N, const int* perm, double* tmp, double* y,
                             cudaStream_t st) {
   ProfScope ps(PROF_TRSV, st, 2.0 * N * N);
   ::ibem::count_launch(), k_gather<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, perm, y, tmp);
+  const size_t smem = sizeof(T) * kTrsvB * (kTrsvB + 1) + 16 + sizeof(double) * kTrsvB;
+  // forward: unit lower, right-hand side and updates in tmp, solved blocks to y
+  for (int64_t k0 = 0; k0 < N; k0 += kTrsvB) {
+    const int b = (int)std::min<int64_t>(kTrsvB, N - k0);
+    const int64_t rows = N - k0 - b;
+    const unsigned grid = (unsigned)std::max<int64_t>(1, (rows + 255) / 256);
+    ::ibem::count_launch(), k_trsv_block<T, true><<<grid, 256, smem, st>>>(F, ldf, N, k0, b, tmp, y);
+  }
+  // backward: upper, right-hand side and updates in y, solved blocks to tmp
+  for (int64_t k0 = ((N - 1) / kTrsvB) * kTrsvB; k0 >= 0; k0 -= kTrsvB) {
+    const int b = (int)std::min<int64_t>(kTrsvB, N - k0);
+    const unsigned grid = (unsigned)std::max<int64_t>(1, (k0 + 255) / 256);
+    ::ibem::count_launch(), k_trsv_block<T, false><<<grid, 256, smem, st>>>(F, ldf, N, k0, b, y, tmp);
+  }
   IBEM_CUDA(cudaMemcpyAsync(y, tmp, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
-  const int nb = 64;
-  for (int64_t k0 = 0; k0 < N; k0 += nb) {
-    const int b = (int)std::min<int64_t>(nb, N - k0);
-    ::ibem::count_launch(), k_trsv_diag<T><<<1, 64, 0, st>>>(F, ldf, k0, b, y, 1);
-    if (k0 + b < N)
-      ::ibem::count_launch(), k_trsv_update<T><<<(unsigned)((N - k0 - b + 255) / 256), 256, 0, st>>>(F, ldf, k0, b, k0 + b, N, y);
-  }
-  for (int64_t k0 = ((N - 1) / nb) * nb; k0 >= 0; k0 -= nb) {
-    const int b = (int)std::min<int64_t>(nb, N - k0);
-    ::ibem::count_launch(), k_trsv_diag<T><<<1, 64, 0, st>>>(F, ldf, k0, b, y, 0);
-    if (k0 > 0) ::ibem::count_launch(), k_trsv_update<T><<<(unsigned)((k0 + 255) / 256), 256, 0, st>>>(F, ldf, k0, b, 0, k0, y);
-  }
   IBEM_LAUNCH_CHECK("lu_apply");
   return IBEM_OK;
 }
@@ -721,14 +773,15 @@ static ibem_status scaled_backward_error(SolveCtx& cx, const double* A, int64_t 
 template <typename T>
 static ibem_status factor(SolveCtx& cx, const double* A, int64_t lda, T*& W, LuWork<T>& w, int& info) {
   const int64_t N = cx.N;
-  ProfScope ps(PROF_EQUIL, cx.st);
-  ::ibem::count_launch(), k_rowmax<<<(unsigned)((N + 255) / 256), 256, 0, cx.st>>>(N, A, lda, cx.r);
-  ::ibem::count_launch(), k_colmax<<<(unsigned)N, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c);
-  IBEM_LAUNCH_CHECK("equilibrate");
   IBEM_CUDA(cudaMalloc(&W, sizeof(T) * (size_t)N * N));
-  dim3 g((unsigned)((N + 255) / 256), (unsigned)N);
-  ::ibem::count_launch(), k_scale_copy<T><<<g, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c, W, N);
-  IBEM_LAUNCH_CHECK("scale_copy");
+  {
+    ProfScope ps(PROF_EQUIL, cx.st);
+    ::ibem::count_launch(), k_rowmax<<<(unsigned)((N + 255) / 256), 256, 0, cx.st>>>(N, A, lda, cx.r);
+    ::ibem::count_launch(), k_colmax<<<(unsigned)N, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c);
+    dim3 g((unsigned)((N + 255) / 256), (unsigned)N);
+    ::ibem::count_launch(), k_scale_copy<T><<<g, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c, W, N);
+    IBEM_LAUNCH_CHECK("equilibrate");
+  }
   ibem_status s = lu_alloc(w, N);
   if (s) return s;
   s = lu_rec<T>(W, N, N, 0, N, w, cx.st);
@@ -1024,12 +1077,13 @@ static ibem_status noalloc_setup(int dev, unsigned char** base, int* ncta, int* 
     const int dyn_cap = std::min(smem_optin - static_smem - 1024, 200 * 1024);
     IBEM_CUDA(cudaFuncSetAttribute((const void*)k_panel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    dyn_cap));
+    IBEM_CUDA(set_solver_smem_attrs<double>());
     int per_sm = 0;
     const int cap = dyn_cap / (kLeaf * (int)sizeof(double));
     IBEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_panel<double>, kPanelThreads,
                                                             (size_t)cap * kLeaf * sizeof(double)));
     if (per_sm < 1) return fail(IBEM_ERR_CUDA, "solve_noalloc: panel kernel cannot be resident");
-    g_noalloc_ncta[dev] = nsm;
+    g_noalloc_ncta[dev] = std::min(nsm, kPanelThreads);
     g_noalloc_rows_cap[dev] = cap;
     g_noalloc_base[dev] = static_cast<unsigned char*>(p);
   }
