@@ -1,0 +1,115 @@
+// Strain at a field point from one sphere with a linear Taylor eigenstrain (24 unknowns),
+// contracted with the eigenstrain before any tensor is formed.
+//
+// postProcessorElastic3D.cpp:407-470 forms e_ij = sum_cols D_ijmn(..)·map·E_col with the
+// Eshelby-type tensors of integratorElastic3DHelper.cpp:2394-2442 (D_40, D_50).  Writing
+// E_mn (order 0) and F_mnp (order 1) as full tensors symmetric in (m, n) absorbs map[m][n],
+// and every derivative of the sphere potentials is a radial pattern:
+//   d_ij F = F2 x_i x_j + F1 d_ij,   d_ijk F = F3 x_i x_j x_k + F2 (d_ij x_k + 2 more),
+//   d_ijkl F = F4 xxxx + F3 (6 d xx) + F2 (3 d d),   Fk = k-th derivative of F in u = |x|^2/2.
+// With psi = Psi0, phi = V0, psi_p = a^2 x_p Q, phi_p = a^2 x_p V1 the contraction gives
+//   e_ij = c { T(Psi, E)_ij - 2 nu trE phi_,ij - 2 (1-nu) [M_ij + M_ji]
+//            + a^2 [ T(Q, E')_ij + 2 (Q3 (v.x) x_i x_j + Q2 (v_i x_j + v_j x_i + d_ij v.x))
+//                    + Q3 (s_i x_j + s_j x_i) + Q2 (g_i x_j + g_j x_i + 2 (G^j x)_i + 2 (G^i x)_j) ]
+//            - 2 nu a^2 [ (w.x)(V1'' x_i x_j + V1' d_ij) + V1' (w_i x_j + w_j x_i) ]
+//            - 2 (1-nu) a^2 [ P_ij + P_ji ] },   c = 1 / (8 pi (1 - nu))
+// with T(G, E)_ij = G4 q x_i x_j + G3 (d_ij q + 2 (Ex)_i x_j + 2 x_i (Ex)_j + trE x_i x_j)
+//                   + G2 (d_ij trE + 2 E_ij),  q = x.E.x,
+//      M_ij = Phi2 (Ex)_i x_j + Phi1 E_ij,  E'_mn = sum_p F_mnp x_p,  v_n = sum_m F_mnm,
+//      w_p = sum_m F_mmp,  G^i_mn = F_mni,  s_i = x.G^i.x,  g_i = tr G^i,
+//      P_ij = V1'' (E'x)_i x_j + V1' (E'_ij + v_i x_j + (G^j x)_i).
+// Inside the sphere (lambda = 0) the u-derivatives of J vanish, exactly as the reference.
+#pragma once
+#include "gen_sphere_common.cuh"
+
+IBEM_HD IBEM_INLINE void sph_field24_contracted(const double x0, const double x1, const double x2, const double a,
+                                                const SphMat& mc, const double* __restrict__ Eu,
+                                                double* __restrict__ e) {
+  const double x[3] = {x0, x1, x2};
+  const double a2 = a * a;
+  const double u = 0.5 * (x0 * x0 + x1 * x1 + x2 * x2);
+  const double lam = 2.0 * u - a2;
+  const double ext = lam > 0.0 ? 1.0 : 0.0;
+  const double rho2 = lam > 0.0 ? a2 + lam : a2;
+  // J_m = 4 pi a^3 / ((2m+1) rho^(2m+1)), m = 1..4
+  const double irho2 = 1.0 / rho2;
+  const double j0 = 4.0 * IBEM_PI * a * a2 / sqrt(rho2);
+  const double J1 = j0 * irho2 / 3.0, J2 = j0 * irho2 * irho2 / 5.0;
+  const double J3 = j0 * irho2 * irho2 * irho2 / 7.0, J4 = j0 * irho2 * irho2 * irho2 * irho2 / 9.0;
+  const double J5 = J4 * irho2 * (9.0 / 11.0);
+  // u-derivative ladders: V_n^(k) = -J_{n+1}^(k-1), J_m^(k) = (-1)^k (2m+3)..(2m+2k+1) J_{m+k} (outside)
+  const double V0_1 = -J1, V0_2 = 5.0 * ext * J2, V0_3 = -35.0 * ext * J3;
+  const double V1_1 = -J2, V1_2 = 7.0 * ext * J3, V1_3 = -63.0 * ext * J4;
+  const double V2_1 = -J3, V2_2 = 9.0 * ext * J4, V2_3 = -99.0 * ext * J5;
+  const double Ps2 = V0_1 - a2 * V1_1, Ps3 = V0_2 - a2 * V1_2, Ps4 = V0_3 - a2 * V1_3;  // Psi0''..''''
+  const double Q2 = V1_1 - a2 * V2_1, Q3 = V1_2 - a2 * V2_2, Q4 = V1_3 - a2 * V2_3;    // Q''..''''
+  const double Ph1 = V0_1, Ph2 = V0_2;                                                // phi', phi''
+  // eigenstrain tensors (symmetric in the first two indices)
+  double E[3][3], F[3][3][3];
+  {
+    const int pi[6] = {0, 0, 0, 1, 1, 2}, pj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      E[pi[t]][pj[t]] = E[pj[t]][pi[t]] = Eu[t];
+#pragma unroll
+      for (int p = 0; p < 3; ++p) F[pi[t]][pj[t]][p] = F[pj[t]][pi[t]][p] = Eu[6 + 3 * t + p];
+    }
+  }
+  // order 0 invariants
+  double Ex[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) Ex[i] = E[i][0] * x0 + E[i][1] * x1 + E[i][2] * x2;
+  const double q = Ex[0] * x0 + Ex[1] * x1 + Ex[2] * x2;
+  const double tE = E[0][0] + E[1][1] + E[2][2];
+  // order 1 invariants
+  double Ep[3][3], v[3], w[3], Gx[3][3], s[3], g[3];  // Gx[i][j] = (G^i x)_j
+#pragma unroll
+  for (int m = 0; m < 3; ++m)
+#pragma unroll
+    for (int n = 0; n < 3; ++n) Ep[m][n] = F[m][n][0] * x0 + F[m][n][1] * x1 + F[m][n][2] * x2;
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    v[n] = F[0][n][0] + F[1][n][1] + F[2][n][2];
+    w[n] = F[0][0][n] + F[1][1][n] + F[2][2][n];
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Gx[i][j] = F[j][0][i] * x0 + F[j][1][i] * x1 + F[j][2][i] * x2;
+    s[i] = Gx[i][0] * x0 + Gx[i][1] * x1 + Gx[i][2] * x2;
+    g[i] = F[0][0][i] + F[1][1][i] + F[2][2][i];
+  }
+  double Epx[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) Epx[i] = Ep[i][0] * x0 + Ep[i][1] * x1 + Ep[i][2] * x2;
+  const double qp = Epx[0] * x0 + Epx[1] * x1 + Epx[2] * x2;
+  const double tEp = Ep[0][0] + Ep[1][1] + Ep[2][2];
+  const double vx = v[0] * x0 + v[1] * x1 + v[2] * x2;
+  const double wx = w[0] * x0 + w[1] * x1 + w[2] * x2;
+  const double nu2 = mc.tn2, nu1m = mc.tn1;  // 2 nu, 1 - nu
+  const int pi[6] = {0, 0, 0, 1, 1, 2}, pj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    const int i = pi[t], j = pj[t];
+    const double d = i == j ? 1.0 : 0.0;
+    const double xx = x[i] * x[j];
+    // order 0
+    const double T0 = Ps4 * q * xx + Ps3 * (d * q + 2.0 * (Ex[i] * x[j] + x[i] * Ex[j]) + tE * xx) +
+                      Ps2 * (d * tE + 2.0 * E[i][j]);
+    const double phij = Ph2 * xx + Ph1 * d;
+    const double Mij = Ph2 * Ex[i] * x[j] + Ph1 * E[i][j];
+    const double Mji = Ph2 * Ex[j] * x[i] + Ph1 * E[j][i];
+    double r0 = T0 - nu2 * tE * phij - 2.0 * nu1m * (Mij + Mji);
+    // order 1
+    const double T1 = Q4 * qp * xx + Q3 * (d * qp + 2.0 * (Epx[i] * x[j] + x[i] * Epx[j]) + tEp * xx) +
+                      Q2 * (d * tEp + 2.0 * Ep[i][j]);
+    const double A1 = T1 + 2.0 * (Q3 * vx * xx + Q2 * (v[i] * x[j] + v[j] * x[i] + d * vx)) +
+                      Q3 * (s[i] * x[j] + s[j] * x[i]) +
+                      Q2 * (g[i] * x[j] + g[j] * x[i] + 2.0 * Gx[j][i] + 2.0 * Gx[i][j]);
+    const double B1 = wx * (V1_2 * xx + V1_1 * d) + V1_1 * (w[i] * x[j] + w[j] * x[i]);
+    const double Pij = V1_2 * Epx[i] * x[j] + V1_1 * (Ep[i][j] + v[i] * x[j] + Gx[j][i]);
+    const double Pji = V1_2 * Epx[j] * x[i] + V1_1 * (Ep[j][i] + v[j] * x[i] + Gx[i][j]);
+    r0 += a2 * (A1 - nu2 * B1 - 2.0 * nu1m * (Pij + Pji));
+    e[t] += mc.kd * r0;
+  }
+}

@@ -200,6 +200,7 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int6
         v = ci >= 0 ? cd[kLeaf] : (T)-1;
         src = threadIdx.x;
       }
+      if (threadIdx.x < nb) s_jr[threadIdx.x] = rowj[buf * kLeaf + threadIdx.x];  // row j, same round trip
       for (int off = 16; off > 0; off >>= 1) {
         const T ov = __shfl_down_sync(0xffffffffu, v, off);
         const int oi = __shfl_down_sync(0xffffffffu, ci, off);
@@ -227,10 +228,7 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int6
     }
     __syncthreads();
     const int piv = s_piv;
-    if (threadIdx.x < nb) {
-      s_pr[threadIdx.x] = cand[((int64_t)buf * ncta + s_sel) * (kLeaf + 2) + threadIdx.x];
-      s_jr[threadIdx.x] = rowj[buf * kLeaf + threadIdx.x];
-    }
+    if (threadIdx.x < nb) s_pr[threadIdx.x] = cand[((int64_t)buf * ncta + s_sel) * (kLeaf + 2) + threadIdx.x];
     __syncthreads();
     // (d) swap rows j and piv where they live
     if (piv != j) {
@@ -257,17 +255,19 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int6
   }
 }
 
-// apply the panel's row exchanges (rows k0+j <-> ipiv[j], j ascending) to columns [c0,c1)
+// apply the panel's row exchanges (rows k0+j <-> ipiv[j], j ascending) to every column
+// outside the panel [k0, k0+nb): thread t takes column t (t < k0) or t + nb
 template <typename T>
 __global__ void k_laswp(T* __restrict__ A, int64_t lda, int64_t k0, const int* __restrict__ ipiv, int nb,
-                        int64_t c0, int64_t c1) {
-  const int64_t c = c0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= c1) return;
+                        int64_t ncols) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= ncols) return;
+  const int64_t c = t < k0 ? t : t + nb;
   T* col = A + c * lda;
   for (int j = 0; j < nb; ++j) {
     const int64_t p = ipiv[j];
     const int64_t q = k0 + j;
-    if (p != q) { const T t = col[q]; col[q] = col[p]; col[p] = t; }
+    if (p != q) { const T tv = col[q]; col[q] = col[p]; col[p] = tv; }
   }
 }
 
@@ -300,6 +300,31 @@ __global__ void __launch_bounds__(64) k_trsm_small(const T* __restrict__ L, int6
     const int i = idx % n1, cc = idx / n1;
     if (c0 + cc < n2) B[(c0 + cc) * ldb + i] = sB[i * 65 + cc];
   }
+}
+
+// Same solve with the triangle size fixed at compile time: the column lives in registers,
+// the loops are fully unrolled (no dependent shared-memory round trips).
+template <typename T, int NB>
+__global__ void __launch_bounds__(128) k_trsm_small_fixed(const T* __restrict__ L, int64_t ldl, T* __restrict__ B,
+                                                          int64_t ldb, int64_t n2) {
+  __shared__ T sL[NB * NB];  // [i][k] = L(k, i) for k > i
+  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+    const int k = idx % NB, i = idx / NB;
+    sL[i * NB + k] = L[(int64_t)i * ldl + k];
+  }
+  __syncthreads();
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= n2) return;
+  T* b = B + c * ldb;
+  T x[NB];
+#pragma unroll
+  for (int i = 0; i < NB; ++i) x[i] = b[i];
+#pragma unroll
+  for (int i = 0; i < NB; ++i)
+#pragma unroll
+    for (int k = i + 1; k < NB; ++k) x[k] -= sL[i * NB + k] * x[i];
+#pragma unroll
+  for (int i = 0; i < NB; ++i) b[i] = x[i];
 }
 
 // ---------------------------------------------------------------- SIMT GEMM  C -= A B
@@ -392,30 +417,69 @@ __global__ void __launch_bounds__(256) k_trsv_block(const T* __restrict__ F, int
     const int r = idx % nb, c = idx / nb;
     sF[c * (kTrsvB + 1) + r] = F[(k0 + c) * ldf + k0 + r];
   }
-  for (int r = threadIdx.x; r < nb; r += blockDim.x) sy[r] = y[k0 + r];
   __syncthreads();
-  const int t = threadIdx.x;
-  if (LOWER) {
-    for (int j = 0; j < nb; ++j) {
-      if (t > j && t < nb) sy[t] -= (double)sF[j * (kTrsvB + 1) + t] * sy[j];
-      __syncthreads();
+  if (threadIdx.x < 32) {
+    // the small triangle in one warp: lane owns rows lane, lane+32, lane+64, lane+96;
+    // the solved value of row j is broadcast with a shuffle (no block barriers)
+    const int lane = threadIdx.x;
+    double v[kTrsvB / 32];
+#pragma unroll
+    for (int q = 0; q < kTrsvB / 32; ++q) {
+      const int r = lane + 32 * q;
+      v[q] = r < nb ? y[k0 + r] : 0.0;
     }
-  } else {
-    for (int j = nb - 1; j >= 0; --j) {
-      if (t == j) sy[j] /= (double)sF[j * (kTrsvB + 1) + j];
-      __syncthreads();
-      if (t < j) sy[t] -= (double)sF[j * (kTrsvB + 1) + t] * sy[j];
-      __syncthreads();
+    if (LOWER) {
+#pragma unroll
+      for (int q = 0; q < kTrsvB / 32; ++q)
+        for (int jj = 0; jj < 32; ++jj) {
+          const int j = 32 * q + jj;
+          if (j >= nb) break;
+          const double xj = __shfl_sync(0xffffffffu, v[q], jj);
+#pragma unroll
+          for (int q2 = 0; q2 < kTrsvB / 32; ++q2) {
+            const int r = lane + 32 * q2;
+            if (r > j && r < nb) v[q2] -= (double)sF[j * (kTrsvB + 1) + r] * xj;
+          }
+        }
+    } else {
+#pragma unroll
+      for (int q = kTrsvB / 32 - 1; q >= 0; --q)
+        for (int jj = 31; jj >= 0; --jj) {
+          const int j = 32 * q + jj;
+          if (j >= nb) continue;
+          if (lane == jj) v[q] /= (double)sF[j * (kTrsvB + 1) + j];
+          const double xj = __shfl_sync(0xffffffffu, v[q], jj);
+#pragma unroll
+          for (int q2 = 0; q2 < kTrsvB / 32; ++q2) {
+            const int r = lane + 32 * q2;
+            if (r < j) v[q2] -= (double)sF[j * (kTrsvB + 1) + r] * xj;
+          }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < kTrsvB / 32; ++q) {
+      const int r = lane + 32 * q;
+      if (r < nb) sy[r] = v[q];
     }
   }
+  __syncthreads();
   if (blockIdx.x == 0)
     for (int r = threadIdx.x; r < nb; r += blockDim.x) out[k0 + r] = sy[r];
+  // block column applied to this CTA's rows: 4 independent partial sums keep loads in flight
   const int64_t r0 = LOWER ? k0 + nb : 0, r1 = LOWER ? N : k0;
   const int64_t r = r0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r < r1) {
-    double acc = 0;
-    for (int c = 0; c < nb; ++c) acc += (double)F[(k0 + c) * ldf + r] * sy[c];
-    y[r] -= acc;
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    const T* col = F + k0 * ldf + r;
+    int c = 0;
+    for (; c + 3 < nb; c += 4) {
+      a0 += (double)col[(int64_t)c * ldf] * sy[c];
+      a1 += (double)col[(int64_t)(c + 1) * ldf] * sy[c + 1];
+      a2 += (double)col[(int64_t)(c + 2) * ldf] * sy[c + 2];
+      a3 += (double)col[(int64_t)(c + 3) * ldf] * sy[c + 3];
+    }
+    for (; c < nb; ++c) a0 += (double)col[(int64_t)c * ldf] * sy[c];
+    y[r] -= (a0 + a1) + (a2 + a3);
   }
 }
 
@@ -521,8 +585,13 @@ static ibem_status trsm(const T* L, int64_t ldl, int64_t n1, T* B, int64_t ldb, 
   if (n1 <= 0 || n2 <= 0) return IBEM_OK;
   if (n1 <= 64) {
     ProfScope ps(PROF_TRSM_SMALL, st);
-    ::ibem::count_launch(), k_trsm_small<T><<<(unsigned)((n2 + 63) / 64), 64, 2 * 64 * 65 * sizeof(T), st>>>(
-        L, ldl, (int)n1, B, ldb, n2);
+    if (n1 == 32)
+      ::ibem::count_launch(), k_trsm_small_fixed<T, 32><<<(unsigned)((n2 + 127) / 128), 128, 0, st>>>(L, ldl, B, ldb, n2);
+    else if (n1 == 64 && sizeof(T) == sizeof(float))
+      ::ibem::count_launch(), k_trsm_small_fixed<T, 64><<<(unsigned)((n2 + 127) / 128), 128, 0, st>>>(L, ldl, B, ldb, n2);
+    else
+      ::ibem::count_launch(), k_trsm_small<T><<<(unsigned)((n2 + 63) / 64), 64, 2 * 64 * 65 * sizeof(T), st>>>(
+          L, ldl, (int)n1, B, ldb, n2);
     IBEM_LAUNCH_CHECK("trsm_small");
     return IBEM_OK;
   }
@@ -543,9 +612,10 @@ static ibem_status lu_rec(T* A, int64_t lda, int64_t N, int64_t k0, int64_t n, L
     if (s) return s;
     // exchanges of this panel on the columns to its left and right (within [0, N))
     ProfScope ps(PROF_LASWP, st);
-    if (k0 > 0) ::ibem::count_launch(), k_laswp<T><<<(unsigned)((k0 + 127) / 128), 128, 0, st>>>(A, lda, k0, w.ipiv_dev + k0, (int)n, 0, k0);
-    if (k0 + n < N)
-      ::ibem::count_launch(), k_laswp<T><<<(unsigned)((N - k0 - n + 127) / 128), 128, 0, st>>>(A, lda, k0, w.ipiv_dev + k0, (int)n, k0 + n, N);
+    const int64_t ncols = N - n;  // every column outside the panel
+    if (ncols > 0)
+      ::ibem::count_launch(), k_laswp<T><<<(unsigned)((ncols + 127) / 128), 128, 0, st>>>(A, lda, k0, w.ipiv_dev + k0,
+                                                                                           (int)n, ncols);
     IBEM_LAUNCH_CHECK("laswp");
     return IBEM_OK;
   }

@@ -1,4 +1,5 @@
 // Sphere kernels for the 24-unknown layout (eigenstrain orders 0 and 1).
+#include "field_contract.cuh"
 #include "gen_sphere24.cuh"
 #include "prof.h"
 #include "sphere_kernels.cuh"
@@ -9,7 +10,7 @@ IBEM_PAIR_KERNEL(pair24_c1_r0, sph_block24_c1_r0, 24)
 IBEM_PAIR_KERNEL(pair24_c1_r1, sph_block24_c1_r1, 24)
 IBEM_SELF_KERNEL(self24, sph_self24, 24)
 IBEM_NODE_KERNEL(node24, sph_node24, 24)
-IBEM_FIELD_KERNEL(field24, sph_field24, 24)
+IBEM_FIELD_KERNEL(field24, sph_field24_contracted, 24)
 
 namespace ibem {
 

@@ -114,3 +114,12 @@ extern "C" int hg_bem_stress_post(const double* x, const double* nv, double E0, 
   bem_stress_post(x[0], x[1], x[2], nv[0], nv[1], nv[2], bm, bm.lam0, bm.mu0, Dsu, Dst);
   return 0;
 }
+
+#include "field_contract.cuh"
+
+extern "C" int hg_field24c(const double* x, double a, double E0, double nu0, double E1, double nu1,
+                           const double* E, double* e) {
+  SphMat mc = sph_mat_init(E0, nu0, E1, nu1);
+  sph_field24_contracted(x[0], x[1], x[2], a, mc, E, e);
+  return 0;
+}
