@@ -18,6 +18,9 @@
 //      M_ij = Phi2 (Ex)_i x_j + Phi1 E_ij,  E'_mn = sum_p F_mnp x_p,  v_n = sum_m F_mnm,
 //      w_p = sum_m F_mmp,  G^i_mn = F_mni,  s_i = x.G^i.x,  g_i = tr G^i,
 //      P_ij = V1'' (E'x)_i x_j + V1' (E'_ij + v_i x_j + (G^j x)_i).
+// Collecting like terms, per (point, sphere) pair:
+//   e_ij / c = A x_i x_j + B d_ij + W_i x_j + W_j x_i + C0 E_ij + C1 E'_ij + C2 ((G^i x)_j + (G^j x)_i)
+// with scalar A, B, C0..C2 and vector W computed once (about 260 FP64 operations per pair).
 // Inside the sphere (lambda = 0) the u-derivatives of J vanish, exactly as the reference.
 #pragma once
 #include "gen_sphere_common.cuh"
@@ -27,23 +30,29 @@ IBEM_HD IBEM_INLINE void sph_field24_contracted(const double x0, const double x1
                                                 double* __restrict__ e) {
   const double x[3] = {x0, x1, x2};
   const double a2 = a * a;
-  const double u = 0.5 * (x0 * x0 + x1 * x1 + x2 * x2);
-  const double lam = 2.0 * u - a2;
+  const double r2 = x0 * x0 + x1 * x1 + x2 * x2;
+  const double lam = r2 - a2;
   const double ext = lam > 0.0 ? 1.0 : 0.0;
   const double rho2 = lam > 0.0 ? a2 + lam : a2;
-  // J_m = 4 pi a^3 / ((2m+1) rho^(2m+1)), m = 1..4
-  const double irho2 = 1.0 / rho2;
-  const double j0 = 4.0 * IBEM_PI * a * a2 / sqrt(rho2);
-  const double J1 = j0 * irho2 / 3.0, J2 = j0 * irho2 * irho2 / 5.0;
-  const double J3 = j0 * irho2 * irho2 * irho2 / 7.0, J4 = j0 * irho2 * irho2 * irho2 * irho2 / 9.0;
-  const double J5 = J4 * irho2 * (9.0 / 11.0);
+  // J_m = 4 pi a^3 / ((2m+1) rho^(2m+1)), m = 1..5
+#ifdef __CUDA_ARCH__
+  const double ir = rsqrt(rho2);
+#else
+  const double ir = 1.0 / sqrt(rho2);
+#endif
+  const double irho2 = ir * ir;
+  const double j0 = 4.0 * IBEM_PI * a * a2 * ir;
+  const double p1 = j0 * irho2, p2 = p1 * irho2, p3 = p2 * irho2, p4 = p3 * irho2, p5 = p4 * irho2;
+  const double J1 = p1 * (1.0 / 3.0), J2 = p2 * (1.0 / 5.0), J3 = p3 * (1.0 / 7.0), J4 = p4 * (1.0 / 9.0),
+               J5 = p5 * (1.0 / 11.0);
   // u-derivative ladders: V_n^(k) = -J_{n+1}^(k-1), J_m^(k) = (-1)^k (2m+3)..(2m+2k+1) J_{m+k} (outside)
   const double V0_1 = -J1, V0_2 = 5.0 * ext * J2, V0_3 = -35.0 * ext * J3;
   const double V1_1 = -J2, V1_2 = 7.0 * ext * J3, V1_3 = -63.0 * ext * J4;
   const double V2_1 = -J3, V2_2 = 9.0 * ext * J4, V2_3 = -99.0 * ext * J5;
-  const double Ps2 = V0_1 - a2 * V1_1, Ps3 = V0_2 - a2 * V1_2, Ps4 = V0_3 - a2 * V1_3;  // Psi0''..''''
-  const double Q2 = V1_1 - a2 * V2_1, Q3 = V1_2 - a2 * V2_2, Q4 = V1_3 - a2 * V2_3;    // Q''..''''
-  const double Ph1 = V0_1, Ph2 = V0_2;                                                // phi', phi''
+  // 2nd..4th u-derivatives of Psi0 and Q; 1st and 2nd of phi = V0
+  const double Ps2 = V0_1 - a2 * V1_1, Ps3 = V0_2 - a2 * V1_2, Ps4 = V0_3 - a2 * V1_3;
+  const double Q2 = V1_1 - a2 * V2_1, Q3 = V1_2 - a2 * V2_2, Q4 = V1_3 - a2 * V2_3;
+  const double Ph1 = V0_1, Ph2 = V0_2;
   // eigenstrain tensors (symmetric in the first two indices)
   double E[3][3], F[3][3][3];
   {
@@ -55,22 +64,18 @@ IBEM_HD IBEM_INLINE void sph_field24_contracted(const double x0, const double x1
       for (int p = 0; p < 3; ++p) F[pi[t]][pj[t]][p] = F[pj[t]][pi[t]][p] = Eu[6 + 3 * t + p];
     }
   }
-  // order 0 invariants
-  double Ex[3];
+  double Ex[3], Ep[3][3], Epx[3], v[3], w[3], Gx[3][3], s[3], g[3];  // Gx[i][j] = (G^i x)_j
 #pragma unroll
   for (int i = 0; i < 3; ++i) Ex[i] = E[i][0] * x0 + E[i][1] * x1 + E[i][2] * x2;
-  const double q = Ex[0] * x0 + Ex[1] * x1 + Ex[2] * x2;
-  const double tE = E[0][0] + E[1][1] + E[2][2];
-  // order 1 invariants
-  double Ep[3][3], v[3], w[3], Gx[3][3], s[3], g[3];  // Gx[i][j] = (G^i x)_j
 #pragma unroll
   for (int m = 0; m < 3; ++m)
 #pragma unroll
-    for (int n = 0; n < 3; ++n) Ep[m][n] = F[m][n][0] * x0 + F[m][n][1] * x1 + F[m][n][2] * x2;
+    for (int n = m; n < 3; ++n) Ep[m][n] = Ep[n][m] = F[m][n][0] * x0 + F[m][n][1] * x1 + F[m][n][2] * x2;
 #pragma unroll
   for (int n = 0; n < 3; ++n) {
     v[n] = F[0][n][0] + F[1][n][1] + F[2][n][2];
     w[n] = F[0][0][n] + F[1][1][n] + F[2][2][n];
+    Epx[n] = Ep[n][0] * x0 + Ep[n][1] * x1 + Ep[n][2] * x2;
   }
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
@@ -79,37 +84,30 @@ IBEM_HD IBEM_INLINE void sph_field24_contracted(const double x0, const double x1
     s[i] = Gx[i][0] * x0 + Gx[i][1] * x1 + Gx[i][2] * x2;
     g[i] = F[0][0][i] + F[1][1][i] + F[2][2][i];
   }
-  double Epx[3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) Epx[i] = Ep[i][0] * x0 + Ep[i][1] * x1 + Ep[i][2] * x2;
+  const double q = Ex[0] * x0 + Ex[1] * x1 + Ex[2] * x2;
+  const double tE = E[0][0] + E[1][1] + E[2][2];
   const double qp = Epx[0] * x0 + Epx[1] * x1 + Epx[2] * x2;
   const double tEp = Ep[0][0] + Ep[1][1] + Ep[2][2];
   const double vx = v[0] * x0 + v[1] * x1 + v[2] * x2;
   const double wx = w[0] * x0 + w[1] * x1 + w[2] * x2;
   const double nu2 = mc.tn2, nu1m = mc.tn1;  // 2 nu, 1 - nu
+  const double A = Ps4 * q + Ps3 * tE - nu2 * tE * Ph2 + a2 * (Q4 * qp + Q3 * (tEp + 2.0 * vx) - nu2 * wx * V1_2);
+  const double B = Ps3 * q + Ps2 * tE - nu2 * tE * Ph1 + a2 * (Q3 * qp + Q2 * (tEp + 2.0 * vx) - nu2 * wx * V1_1);
+  const double cE = 2.0 * Ps3 - 2.0 * nu1m * Ph2;
+  const double cEp = a2 * (2.0 * Q3 - 2.0 * nu1m * V1_2), cv = a2 * (2.0 * Q2 - 2.0 * nu1m * V1_1);
+  const double cs = a2 * Q3, cg = a2 * Q2, cw = -a2 * nu2 * V1_1;
+  double W[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) W[i] = cE * Ex[i] + cEp * Epx[i] + cv * v[i] + cs * s[i] + cg * g[i] + cw * w[i];
+  const double C0 = 2.0 * Ps2 - 4.0 * nu1m * Ph1;
+  const double C1 = a2 * (2.0 * Q2 - 4.0 * nu1m * V1_1);
+  const double C2 = a2 * (2.0 * Q2 - 2.0 * nu1m * V1_1);
   const int pi[6] = {0, 0, 0, 1, 1, 2}, pj[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
   for (int t = 0; t < 6; ++t) {
     const int i = pi[t], j = pj[t];
-    const double d = i == j ? 1.0 : 0.0;
-    const double xx = x[i] * x[j];
-    // order 0
-    const double T0 = Ps4 * q * xx + Ps3 * (d * q + 2.0 * (Ex[i] * x[j] + x[i] * Ex[j]) + tE * xx) +
-                      Ps2 * (d * tE + 2.0 * E[i][j]);
-    const double phij = Ph2 * xx + Ph1 * d;
-    const double Mij = Ph2 * Ex[i] * x[j] + Ph1 * E[i][j];
-    const double Mji = Ph2 * Ex[j] * x[i] + Ph1 * E[j][i];
-    double r0 = T0 - nu2 * tE * phij - 2.0 * nu1m * (Mij + Mji);
-    // order 1
-    const double T1 = Q4 * qp * xx + Q3 * (d * qp + 2.0 * (Epx[i] * x[j] + x[i] * Epx[j]) + tEp * xx) +
-                      Q2 * (d * tEp + 2.0 * Ep[i][j]);
-    const double A1 = T1 + 2.0 * (Q3 * vx * xx + Q2 * (v[i] * x[j] + v[j] * x[i] + d * vx)) +
-                      Q3 * (s[i] * x[j] + s[j] * x[i]) +
-                      Q2 * (g[i] * x[j] + g[j] * x[i] + 2.0 * Gx[j][i] + 2.0 * Gx[i][j]);
-    const double B1 = wx * (V1_2 * xx + V1_1 * d) + V1_1 * (w[i] * x[j] + w[j] * x[i]);
-    const double Pij = V1_2 * Epx[i] * x[j] + V1_1 * (Ep[i][j] + v[i] * x[j] + Gx[j][i]);
-    const double Pji = V1_2 * Epx[j] * x[i] + V1_1 * (Ep[j][i] + v[j] * x[i] + Gx[i][j]);
-    r0 += a2 * (A1 - nu2 * B1 - 2.0 * nu1m * (Pij + Pji));
-    e[t] += mc.kd * r0;
+    double r = A * x[i] * x[j] + W[i] * x[j] + W[j] * x[i] + C0 * E[i][j] + C1 * Ep[i][j] + C2 * (Gx[i][j] + Gx[j][i]);
+    if (i == j) r += B;
+    e[t] += mc.kd * r;
   }
 }

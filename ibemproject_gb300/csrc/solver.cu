@@ -80,60 +80,41 @@ __global__ void k_scale_copy(int64_t n, const double* __restrict__ A, int64_t ld
   W[j * ldw + i] = (T)(r[i] * A[j * lda + i] * c[j]);
 }
 
-// ---------------------------------------------------------------- grid barrier
+// ---------------------------------------------------------------- panel error flag
+// Sticky error flag shared by the CTAs of the panel kernel: set when a spin gives up.
 struct GridSync {
-  unsigned int count;
-  unsigned int gen;
   int err;
 };
 
-__device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
-  unsigned int v;
+// ---------------------------------------------------------------- panel kernel
+// Factorises the m x nb panel (nb <= kLeaf) at P with partial pivoting.  Rows are split
+// evenly over the CTAs and live in dynamic shared memory.  Per column j, every CTA writes
+// one record in rec[j & 1][cta] = {|best|, its global row, that row's values and, in the
+// CTA that owns row j, row j's values} and adds 1 to the arrival counter cnt[j & 1]; one
+// thread per CTA waits (bounded) until the counter reaches base[j & 1] + (j / 2 + 1) * ncta,
+// the value after every CTA of this launch has arrived for column j.  The counters only
+// grow; the host passes the bases they had at launch.  Every CTA then reads all records
+// (L2 loads), picks the same pivot (largest |a|, ties to the smallest row), swaps and
+// updates its own rows.  Double buffering by column parity is enough: a CTA overwrites a
+// record two columns later only after every CTA has arrived for the next column, which
+// each does only after reading the current records.
+// ipiv[j] receives the absolute pivot row of column j; info the first zero pivot.
+constexpr int kRec = 2 * kLeaf + 4;  // record length in elements of T
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-
-__device__ __forceinline__ bool grid_barrier(GridSync* gs, unsigned int nblocks, unsigned int& my_gen) {
-  __syncthreads();
-  __shared__ int s_ok;
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    const unsigned int g = my_gen;
-    __threadfence();
-    if (atomicAdd(&gs->count, 1u) == nblocks - 1) {
-      gs->count = 0;
-      __threadfence();
-      atomicExch(&gs->gen, g + 1);
-    } else {
-      long long it = 0;
-      while (ld_acquire(&gs->gen) == g) {
-        if (++it > kSpinLimit || *reinterpret_cast<volatile int*>(&gs->err) != 0) {
-          atomicExch(&gs->err, 1);
-          ok = 0;
-          break;
-        }
-      }
-    }
-    __threadfence();
-    my_gen = g + 1;
-    s_ok = ok && (atomicAdd(&gs->err, 0) == 0);
-  }
-  __syncthreads();
-  return s_ok != 0;
+__device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// ---------------------------------------------------------------- panel kernel
-// Factorises the m x nb panel (nb <= kLeaf) at P with partial pivoting.  Scratch:
-//   cand  [2][gridDim.x][kLeaf + 2] of T (candidate rows: values, |pivot|, row index)
-//   rowj  [2][kLeaf] of T
-// ipiv[j] receives the absolute pivot row (kglob + panel row) of column j; info the
-// first zero pivot (1-based, absolute).  Rows are split evenly over CTAs and live in
-// dynamic shared memory.
 template <typename T>
 __global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int64_t lda, int m, int nb,
-                                                         int rows_per, T* __restrict__ cand, T* __restrict__ rowj,
-                                                         int* __restrict__ ipiv, int kglob, int* __restrict__ info,
-                                                         GridSync* gs) {
+                                                         int rows_per, T* rec, unsigned* cnt, unsigned base0,
+                                                         unsigned base1, int* __restrict__ ipiv, int kglob,
+                                                         int* __restrict__ info, GridSync* gs) {
   extern __shared__ unsigned char smem_raw[];
   T* sp = reinterpret_cast<T*>(smem_raw);  // rows_per x kLeaf, row-major
   __shared__ T s_pr[kLeaf];                 // pivot row
@@ -141,15 +122,15 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int6
   __shared__ T s_bv[kPanelThreads / 32];
   __shared__ int s_bi[kPanelThreads / 32];
   __shared__ int s_src[kPanelThreads / 32];
-  __shared__ int s_piv, s_sel;
+  __shared__ int s_piv, s_sel, s_fail;
   const int cta = blockIdx.x, ncta = gridDim.x;
   const int r0 = cta * rows_per;
   const int nr = max(0, min(rows_per, m - r0));
-  unsigned int my_gen = 0;
   for (int idx = threadIdx.x; idx < nr * nb; idx += blockDim.x) {
     const int rr = idx % nr, cc = idx / nr;
     sp[rr * kLeaf + cc] = P[(int64_t)cc * lda + r0 + rr];
   }
+  if (threadIdx.x == 0) s_fail = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int j = 0; j < nb; ++j) {
@@ -176,67 +157,84 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int6
       for (int w = 0; w < kPanelThreads / 32; ++w)
         if (s_bv[w] > b || (s_bv[w] == b && s_bi[w] >= 0 && (i < 0 || s_bi[w] < i))) { b = s_bv[w]; i = s_bi[w]; }
       s_piv = i;
-      T* cd = cand + ((int64_t)buf * ncta + cta) * (kLeaf + 2);
-      cd[kLeaf] = b;
-      cd[kLeaf + 1] = (T)i;
+      T* rc = rec + ((int64_t)buf * ncta + cta) * kRec;
+      rc[0] = b;
+      rc[1] = (T)i;
     }
     __syncthreads();
     {
-      T* cd = cand + ((int64_t)buf * ncta + cta) * (kLeaf + 2);
+      T* rc = rec + ((int64_t)buf * ncta + cta) * kRec;
       const int i = s_piv;
-      if (threadIdx.x < nb) cd[threadIdx.x] = (i >= 0) ? sp[(i - r0) * kLeaf + threadIdx.x] : (T)0;
-      if (j >= r0 && j < r0 + nr && threadIdx.x < nb) rowj[buf * kLeaf + threadIdx.x] = sp[(j - r0) * kLeaf + threadIdx.x];
+      if (threadIdx.x < nb) {
+        rc[4 + threadIdx.x] = (i >= 0) ? sp[(i - r0) * kLeaf + threadIdx.x] : (T)0;
+        if (j >= r0 && j < r0 + nr) rc[4 + kLeaf + threadIdx.x] = sp[(j - r0) * kLeaf + threadIdx.x];
+      }
+      __threadfence();
     }
-    // (b) one barrier per column
-    if (!grid_barrier(gs, ncta, my_gen)) return;
-    // (c) global pivot, identical in every CTA: parallel argmax over the CTA candidates
-    //     (largest |a|, ties to the smallest row; CTAs without a candidate never win)
-    {
-      T v = -1;
-      int ci = -1, src = -1;
-      if (threadIdx.x < ncta) {
-        const T* cd = cand + ((int64_t)buf * ncta + threadIdx.x) * (kLeaf + 2);
-        ci = (int)cd[kLeaf + 1];
-        v = ci >= 0 ? cd[kLeaf] : (T)-1;
-        src = threadIdx.x;
-      }
-      if (threadIdx.x < nb) s_jr[threadIdx.x] = rowj[buf * kLeaf + threadIdx.x];  // row j, same round trip
-      for (int off = 16; off > 0; off >>= 1) {
-        const T ov = __shfl_down_sync(0xffffffffu, v, off);
-        const int oi = __shfl_down_sync(0xffffffffu, ci, off);
-        const int os = __shfl_down_sync(0xffffffffu, src, off);
-        if (oi >= 0 && (ci < 0 || ov > v || (ov == v && oi < ci))) { v = ov; ci = oi; src = os; }
-      }
-      if (lane == 0) { s_bv[warp] = v; s_bi[warp] = ci; s_src[warp] = src; }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        T b = -1;
-        int i = -1, sr = -1;
-        for (int w = 0; w < kPanelThreads / 32; ++w)
-          if (s_bi[w] >= 0 && (i < 0 || s_bv[w] > b || (s_bv[w] == b && s_bi[w] < i))) {
-            b = s_bv[w];
-            i = s_bi[w];
-            sr = s_src[w];
-          }
-        s_piv = i;
-        s_sel = sr;
-        if (cta == 0) {
-          ipiv[j] = kglob + i;
-          if (b == 0 && *info == 0) *info = kglob + j + 1;
+    __syncthreads();
+    // (b) arrive, wait for every CTA, then read all records and pick the pivot in parallel
+    if (threadIdx.x == 0) {
+      red_release_add_u32(cnt + buf, 1u);
+      const unsigned target = (buf ? base1 : base0) + (unsigned)(j / 2 + 1) * (unsigned)ncta;
+      long long it = 0;
+      while ((int)(ld_acquire_u32(cnt + buf) - target) < 0) {
+        if (++it > kSpinLimit || *reinterpret_cast<volatile int*>(&gs->err) != 0) {
+          atomicExch(&gs->err, 1);
+          s_fail = 1;
+          break;
         }
       }
     }
     __syncthreads();
-    const int piv = s_piv;
-    if (threadIdx.x < nb) s_pr[threadIdx.x] = cand[((int64_t)buf * ncta + s_sel) * (kLeaf + 2) + threadIdx.x];
+    if (s_fail) return;  // uniform: read after the barrier by every thread
+    T v = -1;
+    int ci = -1, src = -1;
+    if (threadIdx.x < ncta) {
+      const T* rc = rec + ((int64_t)buf * ncta + threadIdx.x) * kRec;
+      ci = (int)__ldcg(rc + 1);
+      v = ci >= 0 ? __ldcg(rc) : (T)-1;
+      src = threadIdx.x;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      const T ov = __shfl_down_sync(0xffffffffu, v, off);
+      const int oi = __shfl_down_sync(0xffffffffu, ci, off);
+      const int os = __shfl_down_sync(0xffffffffu, src, off);
+      if (oi >= 0 && (ci < 0 || ov > v || (ov == v && oi < ci))) { v = ov; ci = oi; src = os; }
+    }
+    if (lane == 0) { s_bv[warp] = v; s_bi[warp] = ci; s_src[warp] = src; }
     __syncthreads();
-    // (d) swap rows j and piv where they live
+    if (threadIdx.x == 0) {
+      T b = -1;
+      int i = -1, sr = -1;
+      for (int w = 0; w < kPanelThreads / 32; ++w)
+        if (s_bi[w] >= 0 && (i < 0 || s_bv[w] > b || (s_bv[w] == b && s_bi[w] < i))) {
+          b = s_bv[w];
+          i = s_bi[w];
+          sr = s_src[w];
+        }
+      s_piv = i;
+      s_sel = sr;
+      if (cta == 0) {
+        ipiv[j] = kglob + i;
+        if (b == 0 && *info == 0) *info = kglob + j + 1;
+      }
+    }
+    __syncthreads();
+    const int piv = s_piv;
+    if (threadIdx.x < nb) {
+      // pivot row from the winning record, row j from its owner's record
+      const int owner = j / rows_per;
+      s_pr[threadIdx.x] = __ldcg(rec + ((int64_t)buf * ncta + s_sel) * kRec + 4 + threadIdx.x);
+      s_jr[threadIdx.x] = __ldcg(rec + ((int64_t)buf * ncta + owner) * kRec + 4 + kLeaf + threadIdx.x);
+    }
+    __syncthreads();
+    // (c) swap rows j and piv where they live
     if (piv != j) {
       if (piv >= r0 && piv < r0 + nr && threadIdx.x < nb) sp[(piv - r0) * kLeaf + threadIdx.x] = s_jr[threadIdx.x];
       if (j >= r0 && j < r0 + nr && threadIdx.x < nb) sp[(j - r0) * kLeaf + threadIdx.x] = s_pr[threadIdx.x];
     }
     __syncthreads();
-    // (e) scale and rank-1 update of rows below j
+    // (d) scale and rank-1 update of rows below j
     const T pjj = s_pr[j];
     if (pjj != (T)0) {
       for (int rr = threadIdx.x; rr < nr; rr += blockDim.x) {
@@ -412,7 +410,8 @@ __global__ void __launch_bounds__(256) k_trsv_block(const T* __restrict__ F, int
                                                     int nb, double* __restrict__ y, double* __restrict__ out) {
   extern __shared__ unsigned char trsv_smem[];
   T* sF = reinterpret_cast<T*>(trsv_smem);  // [c][r] = F(k0 + r, k0 + c), kTrsvB x (kTrsvB + 1)
-  double* sy = reinterpret_cast<double*>(trsv_smem + sizeof(T) * kTrsvB * (kTrsvB + 1) + 16);
+  // arithmetic in T: FP32 factors give an FP32 solve (the preconditioner of the mixed form)
+  T* sy = reinterpret_cast<T*>(trsv_smem + sizeof(T) * kTrsvB * (kTrsvB + 1) + 16);
   for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
     const int r = idx % nb, c = idx / nb;
     sF[c * (kTrsvB + 1) + r] = F[(k0 + c) * ldf + k0 + r];
@@ -422,11 +421,11 @@ __global__ void __launch_bounds__(256) k_trsv_block(const T* __restrict__ F, int
     // the small triangle in one warp: lane owns rows lane, lane+32, lane+64, lane+96;
     // the solved value of row j is broadcast with a shuffle (no block barriers)
     const int lane = threadIdx.x;
-    double v[kTrsvB / 32];
+    T v[kTrsvB / 32];
 #pragma unroll
     for (int q = 0; q < kTrsvB / 32; ++q) {
       const int r = lane + 32 * q;
-      v[q] = r < nb ? y[k0 + r] : 0.0;
+      v[q] = r < nb ? (T)y[k0 + r] : (T)0;
     }
     if (LOWER) {
 #pragma unroll
@@ -434,11 +433,11 @@ __global__ void __launch_bounds__(256) k_trsv_block(const T* __restrict__ F, int
         for (int jj = 0; jj < 32; ++jj) {
           const int j = 32 * q + jj;
           if (j >= nb) break;
-          const double xj = __shfl_sync(0xffffffffu, v[q], jj);
+          const T xj = __shfl_sync(0xffffffffu, v[q], jj);
 #pragma unroll
           for (int q2 = 0; q2 < kTrsvB / 32; ++q2) {
             const int r = lane + 32 * q2;
-            if (r > j && r < nb) v[q2] -= (double)sF[j * (kTrsvB + 1) + r] * xj;
+            if (r > j && r < nb) v[q2] -= sF[j * (kTrsvB + 1) + r] * xj;
           }
         }
     } else {
@@ -447,12 +446,12 @@ __global__ void __launch_bounds__(256) k_trsv_block(const T* __restrict__ F, int
         for (int jj = 31; jj >= 0; --jj) {
           const int j = 32 * q + jj;
           if (j >= nb) continue;
-          if (lane == jj) v[q] /= (double)sF[j * (kTrsvB + 1) + j];
-          const double xj = __shfl_sync(0xffffffffu, v[q], jj);
+          if (lane == jj) v[q] /= sF[j * (kTrsvB + 1) + j];
+          const T xj = __shfl_sync(0xffffffffu, v[q], jj);
 #pragma unroll
           for (int q2 = 0; q2 < kTrsvB / 32; ++q2) {
             const int r = lane + 32 * q2;
-            if (r < j) v[q2] -= (double)sF[j * (kTrsvB + 1) + r] * xj;
+            if (r < j) v[q2] -= sF[j * (kTrsvB + 1) + r] * xj;
           }
         }
     }
@@ -464,22 +463,22 @@ __global__ void __launch_bounds__(256) k_trsv_block(const T* __restrict__ F, int
   }
   __syncthreads();
   if (blockIdx.x == 0)
-    for (int r = threadIdx.x; r < nb; r += blockDim.x) out[k0 + r] = sy[r];
+    for (int r = threadIdx.x; r < nb; r += blockDim.x) out[k0 + r] = (double)sy[r];
   // block column applied to this CTA's rows: 4 independent partial sums keep loads in flight
   const int64_t r0 = LOWER ? k0 + nb : 0, r1 = LOWER ? N : k0;
   const int64_t r = r0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r < r1) {
-    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
     const T* col = F + k0 * ldf + r;
     int c = 0;
     for (; c + 3 < nb; c += 4) {
-      a0 += (double)col[(int64_t)c * ldf] * sy[c];
-      a1 += (double)col[(int64_t)(c + 1) * ldf] * sy[c + 1];
-      a2 += (double)col[(int64_t)(c + 2) * ldf] * sy[c + 2];
-      a3 += (double)col[(int64_t)(c + 3) * ldf] * sy[c + 3];
+      a0 += col[(int64_t)c * ldf] * sy[c];
+      a1 += col[(int64_t)(c + 1) * ldf] * sy[c + 1];
+      a2 += col[(int64_t)(c + 2) * ldf] * sy[c + 2];
+      a3 += col[(int64_t)(c + 3) * ldf] * sy[c + 3];
     }
-    for (; c < nb; ++c) a0 += (double)col[(int64_t)c * ldf] * sy[c];
-    y[r] -= (a0 + a1) + (a2 + a3);
+    for (; c < nb; ++c) a0 += col[(int64_t)c * ldf] * sy[c];
+    y[r] -= (double)((a0 + a1) + (a2 + a3));
   }
 }
 
@@ -512,8 +511,9 @@ __global__ void k_vmul(int64_t n, const double* __restrict__ a, const double* __
 // =====================================================================================
 template <typename T>
 struct LuWork {
-  T* cand = nullptr;
-  T* rowj = nullptr;
+  T* cand = nullptr;         // panel records [2][ncta][kRec]
+  unsigned* cnt = nullptr;   // panel arrival counters [2] (only grow)
+  unsigned arrived[2] = {0, 0};  // host copy of the counters' values after the last launch
   int* ipiv_dev = nullptr;  // N entries (global, absolute row of each exchange)
   int* perm = nullptr;      // N entries: row i of P A is row perm[i] of A
   double* tmp = nullptr;    // N-vector scratch of lu_apply
@@ -535,16 +535,17 @@ static ibem_status panel(T* A, int64_t lda, int64_t k0, int64_t m, int nb, LuWor
   if (rows_per < 1) rows_per = 1;
   ncta = (int)((m + rows_per - 1) / rows_per);
   size_t smem = (size_t)rows_per * kLeaf * sizeof(T);
-  // reset count and generation (not the sticky error flag) before every launch
-  IBEM_CUDA(cudaMemsetAsync(w.gs, 0, 2 * sizeof(unsigned int), st));
   T* P = A + k0 * lda + k0;
   int mm = (int)m;
   int* ip = w.ipiv_dev + k0;
   int kg = (int)k0;
-  void* args[] = {&P, &lda, &mm, &nb, &rows_per, &w.cand, &w.rowj, &ip, &kg, &w.info, &w.gs};
+  unsigned b0 = w.arrived[0], b1 = w.arrived[1];
+  void* args[] = {&P, &lda, &mm, &nb, &rows_per, &w.cand, &w.cnt, &b0, &b1, &ip, &kg, &w.info, &w.gs};
   ProfScope ps(PROF_PANEL, st);
   count_launch();
   IBEM_CUDA(cudaLaunchCooperativeKernel((void*)k_panel<T>, dim3(ncta), dim3(kPanelThreads), args, smem, st));
+  w.arrived[0] += (unsigned)ncta * (unsigned)((nb + 1) / 2);
+  w.arrived[1] += (unsigned)ncta * (unsigned)(nb / 2);
   return IBEM_OK;
 }
 
@@ -652,8 +653,9 @@ static ibem_status lu_alloc(LuWork<T>& w, int64_t N) {
   w.ncta = std::min(nsm, kPanelThreads);  // one CTA per SM (co-resident for the cooperative launch);
                                           // the candidate argmax uses one thread per CTA
   if ((int64_t)w.ncta * w.rows_cap < N) return fail(IBEM_ERR_ARG, "matrix too large for the panel kernel");
-  IBEM_CUDA(cudaMalloc(&w.cand, sizeof(T) * 2 * (size_t)w.ncta * (kLeaf + 2)));
-  IBEM_CUDA(cudaMalloc(&w.rowj, sizeof(T) * 2 * kLeaf));
+  IBEM_CUDA(cudaMalloc(&w.cand, sizeof(T) * 2 * (size_t)w.ncta * kRec));
+  IBEM_CUDA(cudaMalloc(&w.cnt, sizeof(unsigned) * 2));
+  IBEM_CUDA(cudaMemset(w.cnt, 0, sizeof(unsigned) * 2));
   IBEM_CUDA(cudaMalloc(&w.ipiv_dev, sizeof(int) * (size_t)N));
   IBEM_CUDA(cudaMalloc(&w.perm, sizeof(int) * (size_t)N));
   IBEM_CUDA(cudaMalloc(&w.tmp, sizeof(double) * (size_t)N));
@@ -673,7 +675,7 @@ static ibem_status lu_alloc(LuWork<T>& w, int64_t N) {
 template <typename T>
 static void lu_free(LuWork<T>& w) {
   cudaFree(w.cand);
-  cudaFree(w.rowj);
+  cudaFree(w.cnt);
   cudaFree(w.ipiv_dev);
   cudaFree(w.perm);
   cudaFree(w.tmp);
@@ -1083,8 +1085,8 @@ constexpr size_t kNaW = 0;                                                      
 constexpr size_t kNaVec = align256(sizeof(double) * kNoAllocMaxN * kNoAllocMaxN);    // 6 N-vectors
 constexpr size_t kNaPerm = kNaVec + 6 * align256(sizeof(double) * kNoAllocMaxN);     // perm, ipiv
 constexpr size_t kNaCand = kNaPerm + 2 * align256(sizeof(int) * kNoAllocMaxN);
-constexpr size_t kNaRowj = kNaCand + align256(sizeof(double) * 2 * kNoAllocMaxCta * (kLeaf + 2));
-constexpr size_t kNaGs = kNaRowj + align256(sizeof(double) * 2 * kLeaf);
+constexpr size_t kNaSeq = kNaCand + align256(sizeof(double) * 2 * kNoAllocMaxCta * kRec);  // panel records
+constexpr size_t kNaGs = kNaSeq + align256(sizeof(unsigned) * 2);                            // panel counters
 constexpr size_t kNaInfo = kNaGs + align256(sizeof(GridSync));
 constexpr size_t kNaPart = kNaInfo + align256(sizeof(int));
 constexpr size_t kNaRed = kNaPart + align256(sizeof(double) * kNoAllocParts * kNoAllocMaxN);
@@ -1191,6 +1193,8 @@ ibem_status solve_fp64_noalloc(int64_t N, const double* A, int64_t lda, const do
   // the previous call's contents are still there: clear what must start at zero
   IBEM_CUDA(cudaMemsetAsync(gs, 0, sizeof(GridSync), st));
   IBEM_CUDA(cudaMemsetAsync(info, 0, sizeof(int), st));
+  unsigned* cntf = reinterpret_cast<unsigned*>(base + kNaSeq);
+  IBEM_CUDA(cudaMemsetAsync(cntf, 0, sizeof(unsigned) * 2, st));
   const unsigned nb = (unsigned)((N + 255) / 256);
   ::ibem::count_launch(), k_rowmax<<<nb, 256, 0, st>>>(N, A, lda, r);
   ::ibem::count_launch(), k_colmax<<<(unsigned)N, 256, 0, st>>>(N, A, lda, r, c);
@@ -1198,7 +1202,7 @@ ibem_status solve_fp64_noalloc(int64_t N, const double* A, int64_t lda, const do
   IBEM_LAUNCH_CHECK("solve_noalloc: equilibrate");
   LuWork<double> w;
   w.cand = reinterpret_cast<double*>(base + kNaCand);
-  w.rowj = reinterpret_cast<double*>(base + kNaRowj);
+  w.cnt = cntf;
   w.ipiv_dev = ipiv;
   w.perm = perm;
   w.tmp = tmp;

@@ -1,0 +1,109 @@
+"""Kernel micro-benchmarks of the dense solver, timed with CUDA events on the launching stream.
+
+  python -m ibemproject_gb300.kernel_bench --gemm 8192,8192,8192 --gemm 24000,24000,8192
+  python -m ibemproject_gb300.kernel_bench --lu 16800 --form mixed
+
+--gemm M,N,K   C -= A B in FP32 through ibem_gemm_sub_f32 (split-BF16 x3 tcgen05 kernel).
+               Reports the tensor-core kernel alone (algorithmic 2 M N K flops over its
+               event time) and the BF16 split kernels.
+--lu N         ibem_e3d_solve of a random, diagonally dominant N x N system with the
+               per-phase profile (panel, row exchanges, TRSM, GEMM, triangular solves).
+
+One JSON line per case.  The operands are larger than L2 for M, N, K >= 4096; between
+repetitions a 256 MB buffer is written to flush L2.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+
+import torch
+
+from . import lib, check, prof_report, SolveReport, SOLVE_FP64, SOLVE_MIXED_IR
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def bench_gemm(m, n, k, reps, dev):
+    L = lib()
+    g = torch.Generator(device="cpu").manual_seed(7)
+    A = torch.randn((k, m), generator=g).to(dev).t()        # column-major m x k
+    B = torch.randn((n, k), generator=g).to(dev).t()        # column-major k x n
+    C0 = torch.randn((n, m), generator=g).to(dev).t()       # column-major m x n
+    C = C0.clone()
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(st.cuda_stream)
+    check(L.ibem_gemm_sub_f32(m, n, k, _p(A), m, _p(B), k, _p(C), m, sp))   # warm-up
+    torch.cuda.synchronize()
+    L.ibem_prof_enable(1)
+    for _ in range(reps):
+        flush.fill_(1.0)
+        check(L.ibem_gemm_sub_f32(m, n, k, _p(A), m, _p(B), k, _p(C), m, sp))
+    torch.cuda.synchronize()
+    prof = prof_report()
+    L.ibem_prof_enable(0)
+    tc, sp_ = prof.get("gemm_tc", {}), prof.get("gemm_split", {})
+    ms = tc.get("ms", 0.0) / reps
+    # accuracy of one product against an FP64 reference on a 256-column slice
+    C.copy_(C0)
+    check(L.ibem_gemm_sub_f32(m, n, k, _p(A), m, _p(B), k, _p(C), m, sp))
+    nc = min(n, 256)
+    ref = C0[:, :nc].double() - A.double() @ B[:, :nc].double()
+    err = float((C[:, :nc].double() - ref).abs().max() / ref.abs().max())
+    return {"kernel": "k_umma_bf16x3", "m": m, "n": n, "k": k, "reps": reps, "ms": ms,
+            "tflops_algorithmic": 2.0 * m * n * k / (ms * 1e-3) / 1e12 if ms > 0 else None,
+            "tflops_tensor_issued": 6.0 * m * n * k / (ms * 1e-3) / 1e12 if ms > 0 else None,
+            "split_ms": sp_.get("ms", 0.0) / reps, "rel_err_vs_fp64": err}
+
+
+def bench_lu(n, form, reps, dev):
+    L = lib()
+    g = torch.Generator(device="cpu").manual_seed(11)
+    A0 = torch.rand((n, n), generator=g, dtype=torch.float64).to(dev)
+    A0 += torch.diag(torch.full((n,), float(n) / 4, dtype=torch.float64, device=dev))
+    b = torch.rand(n, generator=g, dtype=torch.float64).to(dev)
+    x = torch.empty_like(b)
+    st = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(st.cuda_stream)
+    rep = SolveReport()
+    f = SOLVE_MIXED_IR if form == "mixed" else SOLVE_FP64
+    check(L.ibem_e3d_solve(f, n, _p(A0), n, _p(b), _p(x), 1e-12, ctypes.byref(rep), sp))
+    torch.cuda.synchronize()
+    L.ibem_prof_enable(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        check(L.ibem_e3d_solve(f, n, _p(A0), n, _p(b), _p(x), 1e-12, ctypes.byref(rep), sp))
+    e1.record(st)
+    torch.cuda.synchronize()
+    prof = prof_report()
+    L.ibem_prof_enable(0)
+    return {"kernel": "dense solve", "n": n, "form": form, "reps": reps, "ms": e0.elapsed_time(e1) / reps,
+            "backward_error": rep.backward_error, "iterations": rep.iterations,
+            "phases_ms": {k: round(v["ms"] / reps, 3) for k, v in prof.items()},
+            "phase_launches": {k: v["launches"] / reps for k, v in prof.items()}}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gemm", action="append", default=[], help="M,N,K")
+    ap.add_argument("--lu", type=int, action="append", default=[])
+    ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--reps", type=int, default=3)
+    a = ap.parse_args(argv)
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    for s in a.gemm:
+        m, n, k = (int(v) for v in s.split(","))
+        print(json.dumps(bench_gemm(m, n, k, a.reps, dev)), flush=True)
+    for n in a.lu:
+        print(json.dumps(bench_lu(n, a.form, a.reps, dev)), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
