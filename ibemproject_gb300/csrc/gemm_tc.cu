@@ -7,9 +7,11 @@
 // tensor-core MMAs per product.
 //
 // Kernel structure (one CTA per 128 x 256 output tile, 128 threads):
-//   warp 0, lane 0   TMA producer: 2-stage ring of {A_hi, A_lo (128 x 64), B_hi, B_lo (256 x 64)}
-//                    K-major BF16 tiles, 128-byte swizzle, completion on an mbarrier
-//   warp 1, lane 0   MMA issuer: per 64-wide K block, 4 x 3 tcgen05.mma.kind::f16 (M=128,
+//   warp 0, lane 0   TMA producer: 4-stage ring of {A_hi, A_lo (128 x 32), B_hi, B_lo (256 x 32)}
+//                    K-major BF16 tiles, 64-byte swizzle, completion on an mbarrier (three
+//                    48 KB stages in flight while the fourth is consumed: the loads are
+//                    latency-bound, so bytes in flight set the rate)
+//   warp 1, lane 0   MMA issuer: per 32-wide K block, 2 x 3 tcgen05.mma.kind::f16 (M=128,
 //                    N=256, K=16) into a 128 x 256 FP32 accumulator in TMEM; tcgen05.commit
 //                    releases the stage and, at the end, signals the epilogue
 //   all 4 warps      epilogue: tcgen05.ld 32x32b (warp w reads TMEM lanes 32w..32w+31 = rows),
@@ -31,10 +33,11 @@
 namespace ibem {
 namespace {
 
-constexpr int BM = 128, BN = 256, BK = 64, STAGES = 2;
-constexpr int A_TILE = BM * BK * 2;                 // 16 KB
-constexpr int B_TILE = BN * BK * 2;                 // 32 KB
-constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;  // 96 KB
+constexpr int BM = 128, BN = 256, BK = 32, STAGES = 4;
+constexpr int A_TILE = BM * BK * 2;                 // 8 KB
+constexpr int B_TILE = BN * BK * 2;                 // 16 KB
+constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;  // 48 KB
+constexpr int GROUP_M = 16;                         // tile order: groups of 16 row tiles, columns inner
 constexpr int TMEM_COLS = 256;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr long long kWaitLimit = 1LL << 22;
@@ -111,14 +114,15 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1)
       : "memory");
 }
-// UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+// UMMA shared-memory descriptor: K-major, 64-byte swizzle (rows of BK = 32 BF16), 8-row
+// groups 512 B apart
 __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address (16-byte units)
   d |= (uint64_t)1 << 16;                     // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;           // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)(512 >> 4) << 32;            // stride byte offset: 8 rows x 64 B
   d |= (uint64_t)1 << 46;                     // descriptor version for tcgen05
-  d |= (uint64_t)2 << 61;                     // SWIZZLE_128B
+  d |= (uint64_t)4 << 61;                     // SWIZZLE_64B
   return d;
 }
 // instruction descriptor: kind::f16, D = F32, A = B = BF16, both K-major, M = 128, N = 256
@@ -162,7 +166,17 @@ __global__ void __launch_bounds__(128, 1) k_umma_bf16x3(const __grid_constant__ 
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES), accum = smem_u32(bars + 2 * STAGES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  // grouped tile order: consecutive CTAs sweep the column tiles of GROUP_M row tiles, so
+  // the CTAs resident at once share A and B panels in L2
+  int tm, tn;
+  {
+    const int tiles_m = (m + BM - 1) / BM, tiles_n = (n + BN - 1) / BN;
+    const int b = blockIdx.x, per_group = GROUP_M * tiles_n;
+    const int first = (b / per_group) * GROUP_M, gsz = min(GROUP_M, tiles_m - first);
+    tm = first + (b % per_group) % gsz;
+    tn = (b % per_group) / gsz;
+  }
+  const int m0 = tm * BM, n0 = tn * BN;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -185,7 +199,7 @@ __global__ void __launch_bounds__(128, 1) k_umma_bf16x3(const __grid_constant__ 
 
   if (warp == 0 && lane == 0) {
     // ---- TMA producer
-    int issued[STAGES] = {0, 0};
+    int issued[STAGES] = {};
     for (int kb = 0; kb < kblocks; ++kb) {
       const int s = kb % STAGES;
       if (kb >= STAGES && !mbar_wait(empty0 + 8 * s, (uint32_t)((kb / STAGES - 1) & 1), err)) break;
@@ -213,7 +227,7 @@ __global__ void __launch_bounds__(128, 1) k_umma_bf16x3(const __grid_constant__ 
       const uint32_t bhi = smem_u32(st + 2 * A_TILE), blo = smem_u32(st + 2 * A_TILE + B_TILE);
 #pragma unroll
       for (int kk = 0; kk < BK / 16; ++kk) {
-        const uint32_t off = kk * 32;  // 16 BF16 = 32 bytes along K inside the swizzle atom
+        const uint32_t off = kk * 32;  // 16 BF16 = 32 bytes along K inside the 64-byte row
         umma(tmem, umma_desc(ahi + off), umma_desc(bhi + off), (kb | kk) != 0);
         umma(tmem, umma_desc(ahi + off), umma_desc(blo + off), 1u);
         umma(tmem, umma_desc(alo + off), umma_desc(bhi + off), 1u);
@@ -223,6 +237,17 @@ __global__ void __launch_bounds__(128, 1) k_umma_bf16x3(const __grid_constant__ 
     }
     if (done) umma_commit(accum);  // arrives when every MMA issued above has completed
     else mbar_arrive(accum);
+  } else if (warp >= 2) {
+    // ---- idle warps: bring the C tile into L2 while the MMAs run (one 128-byte line per
+    // 32 rows and column; warp 2 takes row groups 0 and 2, warp 3 groups 1 and 3)
+    for (int rg = warp - 2; rg < 4; rg += 2) {
+      const int rbase = m0 + 32 * rg;
+      if (rbase >= m) break;
+      for (int c = lane; c < BN; c += 32) {
+        const int col = n0 + c;
+        if (col < n) asm volatile("prefetch.global.L2 [%0];" ::"l"(C + (int64_t)col * ldc + rbase));
+      }
+    }
   }
   __syncwarp();
 
@@ -233,6 +258,15 @@ __global__ void __launch_bounds__(128, 1) k_umma_bf16x3(const __grid_constant__ 
   if (ok) {
     const int row = m0 + 32 * warp + lane;
     for (int c0 = 0; c0 < BN; c0 += 32) {
+      // the 32 loads of C go out before any store, so they overlap each other and the TMEM read
+      float cv[32];
+      if (row < m) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int col = n0 + c0 + j;
+          cv[j] = col < n ? C[(int64_t)col * ldc + row] : 0.0f;
+        }
+      }
       uint32_t r[32];
       const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
       IBEM_TMEM_LD32(taddr, r);
@@ -241,7 +275,7 @@ __global__ void __launch_bounds__(128, 1) k_umma_bf16x3(const __grid_constant__ 
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
           const int col = n0 + c0 + j;
-          if (col < n) C[(int64_t)col * ldc + row] -= __uint_as_float(r[j]);
+          if (col < n) C[(int64_t)col * ldc + row] = cv[j] - __uint_as_float(r[j]);
         }
       }
     }
@@ -275,7 +309,7 @@ ibem_status encode_map(CUtensorMap* map, const __nv_bfloat16* ptr, int64_t rows,
   const cuuint32_t box[2] = {BK, box_rows};
   const cuuint32_t estr[2] = {1, 1};
   CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(ptr), dims, strides,
-                        box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(IBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed");
   return IBEM_OK;
@@ -326,7 +360,7 @@ ibem_status gemm_sub_f32_tc(int64_t m, int64_t n, int64_t k, const float* A, int
     if ((s = encode_map(&maps[1], alo, m, kc, kp, BM))) return s;
     if ((s = encode_map(&maps[2], bhi, n, kc, kp, BN))) return s;
     if ((s = encode_map(&maps[3], blo, n, kc, kp, BN))) return s;
-    dim3 grid((unsigned)((m + BM - 1) / BM), (unsigned)((n + BN - 1) / BN));
+    dim3 grid((unsigned)(((m + BM - 1) / BM) * ((n + BN - 1) / BN)));
     ProfScope ps(PROF_GEMM_TC, st, 2.0 * m * n * kc);
     ::ibem::count_launch(), k_umma_bf16x3<<<grid, 128, SMEM_BYTES, st>>>(maps[0], maps[1], maps[2], maps[3], C,
                                                                            ldc, (int)m, (int)n, (int)(kp / BK), err);

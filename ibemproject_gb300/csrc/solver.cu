@@ -36,6 +36,7 @@ namespace {
 
 constexpr int kPanelThreads = 256;
 constexpr int kLeaf = 32;                   // panel width of the recursion leaves
+constexpr int kLdS = kLeaf + 1;             // shared-memory row stride of panel rows (no bank conflicts)
 constexpr long long kSpinLimit = 1LL << 22; // polls before a barrier gives up
 
 // ---------------------------------------------------------------- utilities
@@ -87,170 +88,330 @@ struct GridSync {
 };
 
 // ---------------------------------------------------------------- panel kernel
-// Factorises the m x nb panel (nb <= kLeaf) at P with partial pivoting.  Rows are split
-// evenly over the CTAs and live in dynamic shared memory.  Per column j, every CTA writes
-// one record in rec[j & 1][cta] = {|best|, its global row, that row's values and, in the
-// CTA that owns row j, row j's values} and adds 1 to the arrival counter cnt[j & 1]; one
-// thread per CTA waits (bounded) until the counter reaches base[j & 1] + (j / 2 + 1) * ncta,
-// the value after every CTA of this launch has arrived for column j.  The counters only
-// grow; the host passes the bases they had at launch.  Every CTA then reads all records
-// (L2 loads), picks the same pivot (largest |a|, ties to the smallest row), swaps and
-// updates its own rows.  Double buffering by column parity is enough: a CTA overwrites a
-// record two columns later only after every CTA has arrived for the next column, which
-// each does only after reading the current records.
-// ipiv[j] receives the absolute pivot row of column j; info the first zero pivot.
-constexpr int kRec = 2 * kLeaf + 4;  // record length in elements of T
+// Factorises the m x nb panel (nb <= kLeaf) at P with tournament pivoting (communication-
+// avoiding LU, Grigori-Demmel-Xiang): rows are split evenly over the CTAs and staged in
+// shared memory.
+//  1. Every CTA runs partial-pivoting elimination on its own rows and publishes the
+//     original values of the (up to nb) rows it picked as pivots: cand[cta], flag f0[cta].
+//  2. The leader of every group of F consecutive CTAs waits for its members, runs the same
+//     elimination on their candidates and publishes its nb winners: lcand[g], flag f1[g].
+//  3. CTA 0 waits for every group, eliminates their winners and so fixes the nb pivot rows
+//     and the factored top block (L11 below the diagonal, U11 on and above it).  It turns
+//     the pivot order into LAPACK row exchanges (ipiv) and a short list of the rows >= nb
+//     that receive one of the original top rows, and releases the broadcast flag fb.
+//  4. Every CTA writes its rows of the factored panel: the top rows from the broadcast, the
+//     others as L = A_row U11^-1 from the row's original values (its own or, for a row
+//     that received one of the top rows, that row's original values from the broadcast).
+// Each wait is one polling thread, bounded by kSpinLimit; a wait that gives up sets the
+// sticky gs->err and the CTA returns.  Flags hold the tag of the launch (unique and
+// increasing within a factorisation), so they are never cleared between launches.
+// Ties in the pivot search go to the smallest row, so the result is deterministic.
+constexpr int kCaluMinRows = 256;   // fewest rows a CTA takes before fewer CTAs are used
 
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+__device__ __forceinline__ int ld_acquire_s32(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
-  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void st_release_s32(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int64_t lda, int m, int nb,
-                                                         int rows_per, T* rec, unsigned* cnt, unsigned base0,
-                                                         unsigned base1, int* __restrict__ ipiv, int kglob,
-                                                         int* __restrict__ info, GridSync* gs) {
-  extern __shared__ unsigned char smem_raw[];
-  T* sp = reinterpret_cast<T*>(smem_raw);  // rows_per x kLeaf, row-major
-  __shared__ T s_pr[kLeaf];                 // pivot row
-  __shared__ T s_jr[kLeaf];                 // row j
+struct CaluBufs {
+  T* cand;     // [ncta][kLeaf][kLeaf] original values of each CTA's pivot rows (row-major)
+  int* cidx;   // [ncta][kLeaf] their panel rows (-1: none)
+  T* lcand;    // [groups][kLeaf][kLeaf] group winners
+  int* lidx;   // [groups][kLeaf]
+  T* top;      // [kLeaf][kLeaf] factored top block
+  T* orig;     // [kLeaf][kLeaf] original values of the panel's first nb rows
+  int* meta;   // [0, kLeaf) ipiv (panel-local), [kLeaf, 2 kLeaf) displaced rows,
+               // [2 kLeaf, 3 kLeaf) their source rows, [3 kLeaf] count
+  int* flags;  // [0, kCaluMaxCta) f0, [kCaluMaxCta, 2 kCaluMaxCta) f1, [2 kCaluMaxCta] fb
+};
+constexpr int kCaluMaxCta = 256;
+
+// (v, i) beats (bv, bi): larger |a|, ties to the smaller row; i < 0 is "no candidate"
+template <typename T>
+__device__ __forceinline__ bool calu_better(T v, int i, T bv, int bi) {
+  return i >= 0 && (bi < 0 || v > bv || (v == bv && i < bi));
+}
+
+template <typename T>
+__device__ __forceinline__ void calu_warp_argmax(T& v, int& i) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const T ov = __shfl_down_sync(0xffffffffu, v, off);
+    const int oi = __shfl_down_sync(0xffffffffu, i, off);
+    if (calu_better(ov, oi, v, i)) { v = ov; i = oi; }
+  }
+}
+
+constexpr int kPanelRmax = 4;  // rows per thread at most (1024 rows per elimination)
+
+// Partial-pivoting elimination of the rows held in registers: thread t holds rows
+// q = t + kPanelThreads i (i < R) in a[i][*]; live[i] marks rows that exist and are not yet
+// pivots.  Picks k pivots: s_sel[j] = q of pivot j (-1 when the rows ran out) and
+// s_top[j][*] = that row as it stood at step j (multipliers left of j, U from j on).
+// Two CTA barriers per column; every thread folds the warp winners in the same order, so
+// all agree on the pivot.
+template <typename T, int R>
+__device__ __forceinline__ void calu_elim(T (&a)[R][kLeaf], bool (&live)[R], int k, T* s_top, int* s_sel, T* s_bv,
+                                          int* s_bq) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int nw = kPanelThreads / 32;
+  bool more = true;  // uniform: rows remain for the next pivot
+#pragma unroll
+  for (int j = 0; j < kLeaf; ++j) {
+    if (j < k && more) {
+      T bv = -1;
+      int bq = -1;
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const int q = tid + kPanelThreads * i;
+        const T v = fabs(a[i][j]);
+        if (live[i] && calu_better(v, q, bv, bq)) { bv = v; bq = q; }
+      }
+      calu_warp_argmax(bv, bq);
+      if (lane == 0) { s_bv[warp] = bv; s_bq[warp] = bq; }
+      __syncthreads();
+      bv = s_bv[0];
+      bq = s_bq[0];
+#pragma unroll
+      for (int w = 1; w < nw; ++w)
+        if (calu_better(s_bv[w], s_bq[w], bv, bq)) { bv = s_bv[w]; bq = s_bq[w]; }
+      if (bq < 0) {
+        more = false;
+        if (tid == 0)
+          for (int jj = j; jj < k; ++jj) s_sel[jj] = -1;
+      } else {
+        // the owner publishes the pivot row (per-element predicates keep a[][] in registers)
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          const bool mine = bq == tid + kPanelThreads * i;
+#pragma unroll
+          for (int c = 0; c < kLeaf; ++c)
+            if (mine) s_top[j * kLdS + c] = a[i][c];
+          if (mine) { live[i] = false; s_sel[j] = bq; }
+        }
+        __syncthreads();
+        const T piv = s_top[j * kLdS + j];
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          const T l = (live[i] && piv != (T)0) ? a[i][j] / piv : (T)0;
+          if (live[i]) a[i][j] = l;
+#pragma unroll
+          for (int c = j + 1; c < kLeaf; ++c) a[i][c] -= l * s_top[j * kLdS + c];
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// one polling thread per flag: threads t < n wait for flags[t] == tag (bounded)
+__device__ __forceinline__ void calu_wait(const int* flags, int n, int tag, GridSync* gs, int* s_fail) {
+  if ((int)threadIdx.x < n) {
+    long long it = 0;
+    while (ld_acquire_s32(flags + threadIdx.x) != tag) {
+      if (++it > kSpinLimit || *reinterpret_cast<volatile int*>(&gs->err) != 0) {
+        atomicExch(&gs->err, 1);
+        *s_fail = 1;
+        break;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int64_t lda, int m, int nb, int rows_per,
+                                                         int F, CaluBufs<T> cb, int tag, int* __restrict__ ipiv,
+                                                         int kglob, int* __restrict__ info, GridSync* gs) {
+  __shared__ T s_top[kLeaf * kLdS];  // pivot rows of the current elimination; U11 in step 4
   __shared__ T s_bv[kPanelThreads / 32];
-  __shared__ int s_bi[kPanelThreads / 32];
-  __shared__ int s_src[kPanelThreads / 32];
-  __shared__ int s_piv, s_sel, s_fail;
-  const int cta = blockIdx.x, ncta = gridDim.x;
+  __shared__ int s_bq[kPanelThreads / 32];
+  __shared__ int s_sel[kLeaf];
+  __shared__ int s_meta[3 * kLeaf + 1];
+  __shared__ int s_work[3 * kLeaf];
+  __shared__ int s_fail;
+  const int cta = blockIdx.x, ncta = gridDim.x, tid = threadIdx.x;
+  const int G = (ncta + F - 1) / F;
   const int r0 = cta * rows_per;
   const int nr = max(0, min(rows_per, m - r0));
-  for (int idx = threadIdx.x; idx < nr * nb; idx += blockDim.x) {
-    const int rr = idx % nr, cc = idx / nr;
-    sp[rr * kLeaf + cc] = P[(int64_t)cc * lda + r0 + rr];
+  int* f0 = cb.flags;
+  int* f1 = cb.flags + kCaluMaxCta;
+  int* fb = cb.flags + 2 * kCaluMaxCta;
+  if (tid == 0) s_fail = 0;
+  T a[R][kLeaf];
+  bool live[R];
+  // ---- 1. local elimination of this CTA's rows
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int q = tid + kPanelThreads * i;
+    live[i] = q < nr;
+#pragma unroll
+    for (int c = 0; c < kLeaf; ++c) a[i][c] = (live[i] && c < nb) ? P[(int64_t)c * lda + r0 + q] : (T)0;
   }
-  if (threadIdx.x == 0) s_fail = 0;
+  const int kl = min(nr, nb);
+  calu_elim<T, R>(a, live, kl, s_top, s_sel, s_bv, s_bq);
+  {
+    T* cv = cb.cand + (size_t)cta * kLeaf * kLeaf;
+    for (int idx = tid; idx < kLeaf * nb; idx += kPanelThreads) {
+      const int i = idx / nb, c = idx % nb;
+      if (i < kl) cv[i * kLeaf + c] = P[(int64_t)c * lda + r0 + s_sel[i]];
+    }
+    if (tid < kLeaf) cb.cidx[cta * kLeaf + tid] = tid < kl ? r0 + s_sel[tid] : -1;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release_s32(f0 + cta, tag);
+  }
+  // ---- 2. group leaders: nb winners among the members' candidates
+  if (cta % F == 0) {
+    const int g = cta / F, gsz = min(F, ncta - cta);
+    calu_wait(f0 + cta, gsz, tag, gs, &s_fail);
+    if (s_fail) return;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int q = tid + kPanelThreads * i;
+      const int slot = cta * kLeaf + q;  // member cta + q / kLeaf, candidate q % kLeaf
+      live[i] = q < gsz * kLeaf && __ldcg(cb.cidx + slot) >= 0;
+#pragma unroll
+      for (int c = 0; c < kLeaf; ++c) a[i][c] = (live[i] && c < nb) ? __ldcg(cb.cand + (size_t)slot * kLeaf + c) : (T)0;
+    }
+    calu_elim<T, R>(a, live, nb, s_top, s_sel, s_bv, s_bq);
+    T* lv = cb.lcand + (size_t)g * kLeaf * kLeaf;
+    for (int idx = tid; idx < kLeaf * nb; idx += kPanelThreads) {
+      const int j = idx / nb, c = idx % nb;
+      const int q = s_sel[j];
+      if (q >= 0) lv[j * kLeaf + c] = __ldcg(cb.cand + (size_t)(cta * kLeaf + q) * kLeaf + c);
+    }
+    if (tid < kLeaf) {
+      const int q = tid < nb ? s_sel[tid] : -1;
+      cb.lidx[g * kLeaf + tid] = q >= 0 ? __ldcg(cb.cidx + cta * kLeaf + q) : -1;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release_s32(f1 + g, tag);
+  }
+  // ---- 3. root: the nb pivots, the factored top block and the row exchanges
+  if (cta == 0) {
+    calu_wait(f1, G, tag, gs, &s_fail);
+    if (s_fail) return;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int q = tid + kPanelThreads * i;
+      live[i] = q < G * kLeaf && __ldcg(cb.lidx + q) >= 0;
+#pragma unroll
+      for (int c = 0; c < kLeaf; ++c) a[i][c] = (live[i] && c < nb) ? __ldcg(cb.lcand + (size_t)q * kLeaf + c) : (T)0;
+    }
+    calu_elim<T, R>(a, live, nb, s_top, s_sel, s_bv, s_bq);
+    for (int idx = tid; idx < nb * nb; idx += kPanelThreads) {
+      const int j = idx / nb, c = idx % nb;
+      cb.top[j * kLeaf + c] = s_top[j * kLdS + c];
+      cb.orig[j * kLeaf + c] = P[(int64_t)c * lda + j];
+    }
+    if (tid == 0) {
+      // pivot order -> sequential row exchanges; track where the original top rows go
+      int* loc = s_work;  // shared scratch: thread 0 only
+      int* content = s_work + kLeaf;
+      int* slot = s_work + 2 * kLeaf;
+      for (int s = 0; s < nb; ++s) { loc[s] = s; content[s] = s; slot[s] = -1; }
+      int nd = 0;
+      for (int j = 0; j < nb; ++j) {
+        const int w = __ldcg(cb.lidx + s_sel[j]);
+        if (s_top[j * kLdS + j] == (T)0 && *info == 0) *info = kglob + j + 1;
+        const int p = w < nb ? loc[w] : w;
+        s_meta[j] = p;
+        const int c = content[j];
+        if (p != j) {
+          if (p < nb) {
+            content[p] = c;
+            loc[c] = p;
+          } else {
+            const int sl = w >= nb ? nd++ : slot[w];
+            s_meta[kLeaf + sl] = p;
+            s_meta[2 * kLeaf + sl] = c;
+            slot[c] = sl;
+            loc[c] = p;
+          }
+          content[j] = w;
+          if (w < nb) loc[w] = j;
+        }
+        ipiv[j] = kglob + p;
+      }
+      s_meta[3 * kLeaf] = nd;
+    }
+    __syncthreads();
+    for (int i = tid; i < 3 * kLeaf + 1; i += kPanelThreads) cb.meta[i] = s_meta[i];
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release_s32(fb, tag);
+  }
+  // ---- 4. every CTA: its rows of the factored panel
+  calu_wait(fb, 1, tag, gs, &s_fail);
+  if (s_fail) return;
+  for (int idx = tid; idx < nb * nb; idx += kPanelThreads) {
+    const int i = idx / nb, c = idx % nb;
+    s_top[i * kLdS + c] = __ldcg(cb.top + i * kLeaf + c);
+  }
+  if (tid < 3 * kLeaf + 1) s_meta[tid] = __ldcg(cb.meta + tid);
   __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int j = 0; j < nb; ++j) {
-    const int buf = j & 1;
-    // (a) local candidate: max |a_ij| over rows >= j owned here (first max wins)
-    T best = -1;
-    int bi = -1;
-    for (int rr = threadIdx.x; rr < nr; rr += blockDim.x) {
-      const int gr = r0 + rr;
-      if (gr < j) continue;
-      const T v = fabs(sp[rr * kLeaf + j]);
-      if (v > best) { best = v; bi = gr; }
+  const int nd = s_meta[3 * kLeaf];
+  for (int rr = tid; rr < nr; rr += kPanelThreads) {
+    const int r = r0 + rr;
+    if (r < nb) {
+#pragma unroll
+      for (int c = 0; c < kLeaf; ++c)
+        if (c < nb) P[(int64_t)c * lda + r] = __ldcg(cb.top + r * kLeaf + c);
+      continue;
     }
-    for (int off = 16; off > 0; off >>= 1) {
-      const T ov = __shfl_down_sync(0xffffffffu, best, off);
-      const int oi = __shfl_down_sync(0xffffffffu, bi, off);
-      if (ov > best || (ov == best && oi >= 0 && (bi < 0 || oi < bi))) { best = ov; bi = oi; }
-    }
-    if (lane == 0) { s_bv[warp] = best; s_bi[warp] = bi; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      T b = -1;
-      int i = -1;
-      for (int w = 0; w < kPanelThreads / 32; ++w)
-        if (s_bv[w] > b || (s_bv[w] == b && s_bi[w] >= 0 && (i < 0 || s_bi[w] < i))) { b = s_bv[w]; i = s_bi[w]; }
-      s_piv = i;
-      T* rc = rec + ((int64_t)buf * ncta + cta) * kRec;
-      rc[0] = b;
-      rc[1] = (T)i;
-    }
-    __syncthreads();
-    {
-      T* rc = rec + ((int64_t)buf * ncta + cta) * kRec;
-      const int i = s_piv;
-      if (threadIdx.x < nb) {
-        rc[4 + threadIdx.x] = (i >= 0) ? sp[(i - r0) * kLeaf + threadIdx.x] : (T)0;
-        if (j >= r0 && j < r0 + nr) rc[4 + kLeaf + threadIdx.x] = sp[(j - r0) * kLeaf + threadIdx.x];
-      }
-      __threadfence();
-    }
-    __syncthreads();
-    // (b) arrive, wait for every CTA, then read all records and pick the pivot in parallel
-    if (threadIdx.x == 0) {
-      red_release_add_u32(cnt + buf, 1u);
-      const unsigned target = (buf ? base1 : base0) + (unsigned)(j / 2 + 1) * (unsigned)ncta;
-      long long it = 0;
-      while ((int)(ld_acquire_u32(cnt + buf) - target) < 0) {
-        if (++it > kSpinLimit || *reinterpret_cast<volatile int*>(&gs->err) != 0) {
-          atomicExch(&gs->err, 1);
-          s_fail = 1;
-          break;
-        }
+    int src = -1;
+    for (int t = 0; t < nd; ++t)
+      if (s_meta[kLeaf + t] == r) src = s_meta[2 * kLeaf + t];
+    T x[kLeaf];
+#pragma unroll
+    for (int c = 0; c < kLeaf; ++c)
+      x[c] = c < nb ? (src < 0 ? P[(int64_t)c * lda + r] : __ldcg(cb.orig + src * kLeaf + c)) : (T)0;
+    // x U11 = original row  ->  x <- row U11^-1, column by column
+#pragma unroll
+    for (int k = 0; k < kLeaf; ++k) {
+      if (k < nb) {
+        T s = x[k];
+#pragma unroll
+        for (int i = 0; i < k; ++i) s -= x[i] * s_top[i * kLdS + k];
+        const T ukk = s_top[k * kLdS + k];
+        x[k] = ukk != (T)0 ? s / ukk : (T)0;
       }
     }
-    __syncthreads();
-    if (s_fail) return;  // uniform: read after the barrier by every thread
-    T v = -1;
-    int ci = -1, src = -1;
-    if (threadIdx.x < ncta) {
-      const T* rc = rec + ((int64_t)buf * ncta + threadIdx.x) * kRec;
-      ci = (int)__ldcg(rc + 1);
-      v = ci >= 0 ? __ldcg(rc) : (T)-1;
-      src = threadIdx.x;
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-      const T ov = __shfl_down_sync(0xffffffffu, v, off);
-      const int oi = __shfl_down_sync(0xffffffffu, ci, off);
-      const int os = __shfl_down_sync(0xffffffffu, src, off);
-      if (oi >= 0 && (ci < 0 || ov > v || (ov == v && oi < ci))) { v = ov; ci = oi; src = os; }
-    }
-    if (lane == 0) { s_bv[warp] = v; s_bi[warp] = ci; s_src[warp] = src; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      T b = -1;
-      int i = -1, sr = -1;
-      for (int w = 0; w < kPanelThreads / 32; ++w)
-        if (s_bi[w] >= 0 && (i < 0 || s_bv[w] > b || (s_bv[w] == b && s_bi[w] < i))) {
-          b = s_bv[w];
-          i = s_bi[w];
-          sr = s_src[w];
-        }
-      s_piv = i;
-      s_sel = sr;
-      if (cta == 0) {
-        ipiv[j] = kglob + i;
-        if (b == 0 && *info == 0) *info = kglob + j + 1;
-      }
-    }
-    __syncthreads();
-    const int piv = s_piv;
-    if (threadIdx.x < nb) {
-      // pivot row from the winning record, row j from its owner's record
-      const int owner = j / rows_per;
-      s_pr[threadIdx.x] = __ldcg(rec + ((int64_t)buf * ncta + s_sel) * kRec + 4 + threadIdx.x);
-      s_jr[threadIdx.x] = __ldcg(rec + ((int64_t)buf * ncta + owner) * kRec + 4 + kLeaf + threadIdx.x);
-    }
-    __syncthreads();
-    // (c) swap rows j and piv where they live
-    if (piv != j) {
-      if (piv >= r0 && piv < r0 + nr && threadIdx.x < nb) sp[(piv - r0) * kLeaf + threadIdx.x] = s_jr[threadIdx.x];
-      if (j >= r0 && j < r0 + nr && threadIdx.x < nb) sp[(j - r0) * kLeaf + threadIdx.x] = s_pr[threadIdx.x];
-    }
-    __syncthreads();
-    // (d) scale and rank-1 update of rows below j
-    const T pjj = s_pr[j];
-    if (pjj != (T)0) {
-      for (int rr = threadIdx.x; rr < nr; rr += blockDim.x) {
-        if (r0 + rr <= j) continue;
-        T* row = sp + rr * kLeaf;
-        const T l = row[j] / pjj;
-        row[j] = l;
-        for (int k = j + 1; k < nb; ++k) row[k] -= l * s_pr[k];
-      }
-    }
-    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < kLeaf; ++c)
+      if (c < nb) P[(int64_t)c * lda + r] = x[c];
   }
-  for (int idx = threadIdx.x; idx < nr * nb; idx += blockDim.x) {
-    const int rr = idx % nr, cc = idx / nr;
-    P[(int64_t)cc * lda + r0 + rr] = sp[rr * kLeaf + cc];
-  }
+}
+
+constexpr size_t calu_a256(size_t v) { return (v + 255) / 256 * 256; }
+// bytes of the panel kernel's buffers for up to ncta CTAs
+template <typename T>
+constexpr size_t calu_bytes(int ncta) {
+  return 2 * calu_a256(sizeof(T) * (size_t)ncta * kLeaf * kLeaf) + 2 * calu_a256(sizeof(int) * (size_t)ncta * kLeaf) +
+         2 * calu_a256(sizeof(T) * kLeaf * kLeaf) + calu_a256(sizeof(int) * (3 * kLeaf + 1)) +
+         calu_a256(sizeof(int) * (2 * kCaluMaxCta + 1));
+}
+template <typename T>
+CaluBufs<T> calu_carve(unsigned char* base, int ncta) {
+  CaluBufs<T> b;
+  size_t o = 0;
+  auto take = [&](size_t bytes) { unsigned char* q = base + o; o += calu_a256(bytes); return q; };
+  b.cand = reinterpret_cast<T*>(take(sizeof(T) * (size_t)ncta * kLeaf * kLeaf));
+  b.lcand = reinterpret_cast<T*>(take(sizeof(T) * (size_t)ncta * kLeaf * kLeaf));
+  b.cidx = reinterpret_cast<int*>(take(sizeof(int) * (size_t)ncta * kLeaf));
+  b.lidx = reinterpret_cast<int*>(take(sizeof(int) * (size_t)ncta * kLeaf));
+  b.top = reinterpret_cast<T*>(take(sizeof(T) * kLeaf * kLeaf));
+  b.orig = reinterpret_cast<T*>(take(sizeof(T) * kLeaf * kLeaf));
+  b.meta = reinterpret_cast<int*>(take(sizeof(int) * (3 * kLeaf + 1)));
+  b.flags = reinterpret_cast<int*>(take(sizeof(int) * (2 * kCaluMaxCta + 1)));
+  return b;
 }
 
 // apply the panel's row exchanges (rows k0+j <-> ipiv[j], j ascending) to every column
@@ -398,99 +559,210 @@ __global__ void k_residual(int64_t n, int nparts, const double* __restrict__ par
   r[i] = b[i] - s;
 }
 
-// Blocked substitution with the factors in precision T (vectors FP64), one launch per
-// kTrsvB-row block.  Every CTA loads the diagonal block and the block's right-hand side,
-// solves the small triangle in shared memory (the same arithmetic in every CTA), CTA 0
-// stores the solved block to `out`, and each CTA applies the block column to its share of
-// the remaining rows of `y`.  `y` rows of the block are only read and other rows only
-// written within a launch, so CTAs never race.
+// ---------------------------------------------------------------- triangular solves
+// Substitution with the factors in precision T (vectors FP64), blocks of kTrsvB rows.
+// After the factorisation, k_trsv_inv writes the inverse of every diagonal block of L
+// (unit lower) and U (upper) to dinv.  One cooperative launch of k_trsv_persist then solves
+// the whole triangle: CTA c takes blocks c, c + G, c + 2G, ... in dependency order and,
+// for block i, accumulates F_ij x_j over the solved blocks j (waiting on flags[j] == tag,
+// bounded), forms r_i = rhs_i - sum, applies the inverse diagonal block (x_i = D_i^-1 r_i),
+// stores x_i and releases flags[i] = tag.  Tags grow by one per launch, so the flags are
+// never cleared.  Deadlock-free because all CTAs are co-resident and every CTA meets its
+// blocks in increasing dependency order.
 constexpr int kTrsvB = 128;
-template <typename T, bool LOWER>
-__global__ void __launch_bounds__(256) k_trsv_block(const T* __restrict__ F, int64_t ldf, int64_t N, int64_t k0,
-                                                    int nb, double* __restrict__ y, double* __restrict__ out) {
-  extern __shared__ unsigned char trsv_smem[];
-  T* sF = reinterpret_cast<T*>(trsv_smem);  // [c][r] = F(k0 + r, k0 + c), kTrsvB x (kTrsvB + 1)
-  // arithmetic in T: FP32 factors give an FP32 solve (the preconditioner of the mixed form)
-  T* sy = reinterpret_cast<T*>(trsv_smem + sizeof(T) * kTrsvB * (kTrsvB + 1) + 16);
-  for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
-    const int r = idx % nb, c = idx / nb;
-    sF[c * (kTrsvB + 1) + r] = F[(k0 + c) * ldf + k0 + r];
+constexpr int kTrsvThreads = 256;   // 8 warps: warp w covers columns 16w..16w+15 of a tile
+
+// inverse of the diagonal block blockIdx.x of L (blockIdx.y = 0, unit lower) or U (= 1),
+// column-major kTrsvB x kTrsvB with explicit zeros; rows/columns past N are identity
+template <typename T>
+__global__ void __launch_bounds__(kTrsvB) k_trsv_inv(const T* __restrict__ F, int64_t ldf, int64_t N,
+                                                     T* __restrict__ dinv) {
+  extern __shared__ unsigned char inv_smem[];
+  T* X = reinterpret_cast<T*>(inv_smem);          // X[c * (kTrsvB + 1) + r]
+  T* tcol = X + kTrsvB * (kTrsvB + 1);            // kTrsvB scratch
+  const int blk = blockIdx.x, upper = blockIdx.y;
+  const int64_t k0 = (int64_t)blk * kTrsvB;
+  const int nb = (int)(N - k0 < kTrsvB ? N - k0 : kTrsvB);
+  const int r = threadIdx.x;
+  for (int c = 0; c < kTrsvB; ++c) {
+    T v;
+    if (r < nb && c < nb) v = F[(k0 + c) * ldf + k0 + r];
+    else v = (r == c) ? (T)1 : (T)0;
+    if (!upper && r <= c) v = (r == c) ? (T)1 : (T)0;   // unit lower: ignore U's part
+    if (upper && r > c) v = 0;                           // upper: ignore L's part
+    X[c * (kTrsvB + 1) + r] = v;
   }
   __syncthreads();
-  if (threadIdx.x < 32) {
-    // the small triangle in one warp: lane owns rows lane, lane+32, lane+64, lane+96;
-    // the solved value of row j is broadcast with a shuffle (no block barriers)
-    const int lane = threadIdx.x;
-    T v[kTrsvB / 32];
-#pragma unroll
-    for (int q = 0; q < kTrsvB / 32; ++q) {
-      const int r = lane + 32 * q;
-      v[q] = r < nb ? (T)y[k0 + r] : (T)0;
+  if (!upper) {
+    // right to left: X[r][j] = -(L[r][j] + sum_{j<k<r} X[r][k] L[k][j]),  r > j
+    for (int j = kTrsvB - 2; j >= 0; --j) {
+      T t = 0;
+      if (r > j) {
+        t = X[j * (kTrsvB + 1) + r];
+        for (int k = j + 1; k < r; ++k) t += X[k * (kTrsvB + 1) + r] * X[j * (kTrsvB + 1) + k];
+      }
+      __syncthreads();
+      if (r > j) X[j * (kTrsvB + 1) + r] = -t;
+      __syncthreads();
     }
-    if (LOWER) {
-#pragma unroll
-      for (int q = 0; q < kTrsvB / 32; ++q)
-        for (int jj = 0; jj < 32; ++jj) {
-          const int j = 32 * q + jj;
-          if (j >= nb) break;
-          const T xj = __shfl_sync(0xffffffffu, v[q], jj);
-#pragma unroll
-          for (int q2 = 0; q2 < kTrsvB / 32; ++q2) {
-            const int r = lane + 32 * q2;
-            if (r > j && r < nb) v[q2] -= sF[j * (kTrsvB + 1) + r] * xj;
-          }
-        }
+  } else {
+    // left to right: X[j][j] = 1 / U[j][j];  X[r][j] = -X[j][j] sum_{r<=k<j} X[r][k] U[k][j],  r < j
+    for (int j = 0; j < kTrsvB; ++j) {
+      const T djj = (T)1 / X[j * (kTrsvB + 1) + j];
+      T t = 0;
+      if (r < j)
+        for (int k = r; k < j; ++k) t += X[k * (kTrsvB + 1) + r] * X[j * (kTrsvB + 1) + k];
+      tcol[r] = t;
+      __syncthreads();
+      if (r < j) X[j * (kTrsvB + 1) + r] = -djj * tcol[r];
+      if (r == j) X[j * (kTrsvB + 1) + j] = djj;
+      __syncthreads();
+    }
+  }
+  T* out = dinv + (size_t)(2 * blk + upper) * kTrsvB * kTrsvB;
+  for (int c = 0; c < kTrsvB; ++c) out[c * kTrsvB + r] = X[c * (kTrsvB + 1) + r];
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// rows 4 * lane .. 4 * lane + 3 of column c of a tile starting at row i0 (nbi valid rows)
+template <typename T, bool VEC>
+__device__ __forceinline__ void trsv_load4(const T* col, int lane, int nbi, T v[4]) {
+  const int r = 4 * lane;
+  if (VEC && r + 3 < nbi) {
+    if (sizeof(T) == 4) {
+      const float4 q = __ldg(reinterpret_cast<const float4*>(col + r));
+      v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
     } else {
+      const double2 q0 = __ldg(reinterpret_cast<const double2*>(col + r));
+      const double2 q1 = __ldg(reinterpret_cast<const double2*>(col + r + 2));
+      v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
+    }
+  } else {
 #pragma unroll
-      for (int q = kTrsvB / 32 - 1; q >= 0; --q)
-        for (int jj = 31; jj >= 0; --jj) {
-          const int j = 32 * q + jj;
-          if (j >= nb) continue;
-          if (lane == jj) v[q] /= sF[j * (kTrsvB + 1) + j];
-          const T xj = __shfl_sync(0xffffffffu, v[q], jj);
+    for (int q = 0; q < 4; ++q) v[q] = (r + q < nbi) ? col[r + q] : (T)0;
+  }
+}
+
+template <typename T, bool LOWER, bool VEC>
+__global__ void __launch_bounds__(kTrsvThreads) k_trsv_persist(const T* __restrict__ F, int64_t ldf, int64_t N,
+                                                               int nblk, const T* __restrict__ dinv,
+                                                               const double* __restrict__ rhs, double* x,
+                                                               int* flags, int tag, GridSync* gs) {
+  extern __shared__ __align__(16) unsigned char ps_smem[];
+  T* sD = reinterpret_cast<T*>(ps_smem);                 // inverse diagonal block, kTrsvB^2
+  T* s_red = sD + kTrsvB * kTrsvB;                       // [8][kTrsvB] partial sums
+  __shared__ T s_x[kTrsvB];
+  __shared__ T s_r[kTrsvB];
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) s_fail = 0;
+  for (int t = blockIdx.x; t < nblk; t += gridDim.x) {
+    const int bi = LOWER ? t : nblk - 1 - t;
+    const int64_t i0 = (int64_t)bi * kTrsvB;
+    const int nbi = (int)(N - i0 < kTrsvB ? N - i0 : kTrsvB);
+    // stage D_i^-1 in shared memory while the tiles stream
+    {
+      const char* g = reinterpret_cast<const char*>(dinv + (size_t)(2 * bi + (LOWER ? 0 : 1)) * kTrsvB * kTrsvB);
+      char* sm = reinterpret_cast<char*>(sD);
+      for (int o = tid * 16; o < (int)(sizeof(T) * kTrsvB * kTrsvB); o += kTrsvThreads * 16) cp_async16(sm + o, g + o);
+    }
+    T acc[4] = {0, 0, 0, 0};
+    const int ntiles = LOWER ? bi : nblk - 1 - bi;
+    for (int s = 0; s < ntiles; ++s) {
+      const int bj = LOWER ? s : nblk - 1 - s;
+      const int64_t j0 = (int64_t)bj * kTrsvB;
+      const int nbj = (int)(N - j0 < kTrsvB ? N - j0 : kTrsvB);
+      // the tile does not depend on x_j: issue its loads first
+      T v[16][4];
 #pragma unroll
-          for (int q2 = 0; q2 < kTrsvB / 32; ++q2) {
-            const int r = lane + 32 * q2;
-            if (r < j) v[q2] -= sF[j * (kTrsvB + 1) + r] * xj;
+      for (int cc = 0; cc < 16; ++cc) {
+        const int c = warp * 16 + cc;
+        if (c < nbj) trsv_load4<T, VEC>(F + (j0 + c) * ldf + i0, lane, nbi, v[cc]);
+        else v[cc][0] = v[cc][1] = v[cc][2] = v[cc][3] = 0;
+      }
+      if (tid == 0) {
+        long long it = 0;
+        while (ld_acquire_s32(flags + bj) != tag) {
+          if (++it > kSpinLimit || *reinterpret_cast<volatile int*>(&gs->err) != 0) {
+            atomicExch(&gs->err, 1);
+            s_fail = 1;
+            break;
           }
         }
+      }
+      __syncthreads();
+      if (s_fail) { cp_async_wait_all(); return; }
+      if (tid < kTrsvB) s_x[tid] = tid < nbj ? (T)__ldcg(x + j0 + tid) : (T)0;
+      __syncthreads();
+#pragma unroll
+      for (int cc = 0; cc < 16; ++cc) {
+        const T xc = s_x[warp * 16 + cc];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[q] += v[cc][q] * xc;
+      }
+    }
+    // r_i = rhs_i - sum over the eight warps
+#pragma unroll
+    for (int q = 0; q < 4; ++q) s_red[warp * kTrsvB + 4 * lane + q] = acc[q];
+    cp_async_wait_all();
+    __syncthreads();
+    if (tid < kTrsvB) {
+      T sum = 0;
+#pragma unroll
+      for (int w = 0; w < kTrsvThreads / 32; ++w) sum += s_red[w * kTrsvB + tid];
+      s_r[tid] = tid < nbi ? (T)rhs[i0 + tid] - sum : (T)0;
+    }
+    __syncthreads();
+    // x_i = D_i^-1 r_i
+    T acc2[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int cc = 0; cc < 16; ++cc) {
+      const int c = warp * 16 + cc;
+      const T rc = s_r[c];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc2[q] += sD[c * kTrsvB + 4 * lane + q] * rc;
     }
 #pragma unroll
-    for (int q = 0; q < kTrsvB / 32; ++q) {
-      const int r = lane + 32 * q;
-      if (r < nb) sy[r] = v[q];
+    for (int q = 0; q < 4; ++q) s_red[warp * kTrsvB + 4 * lane + q] = acc2[q];
+    __syncthreads();
+    if (tid < nbi) {
+      T sum = 0;
+#pragma unroll
+      for (int w = 0; w < kTrsvThreads / 32; ++w) sum += s_red[w * kTrsvB + tid];
+      x[i0 + tid] = (double)sum;
     }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release_s32(flags + bi, tag);
   }
-  __syncthreads();
-  if (blockIdx.x == 0)
-    for (int r = threadIdx.x; r < nb; r += blockDim.x) out[k0 + r] = (double)sy[r];
-  // block column applied to this CTA's rows: 4 independent partial sums keep loads in flight
-  const int64_t r0 = LOWER ? k0 + nb : 0, r1 = LOWER ? N : k0;
-  const int64_t r = r0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r < r1) {
-    T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-    const T* col = F + k0 * ldf + r;
-    int c = 0;
-    for (; c + 3 < nb; c += 4) {
-      a0 += col[(int64_t)c * ldf] * sy[c];
-      a1 += col[(int64_t)(c + 1) * ldf] * sy[c + 1];
-      a2 += col[(int64_t)(c + 2) * ldf] * sy[c + 2];
-      a3 += col[(int64_t)(c + 3) * ldf] * sy[c + 3];
-    }
-    for (; c < nb; ++c) a0 += col[(int64_t)c * ldf] * sy[c];
-    y[r] -= (double)((a0 + a1) + (a2 + a3));
-  }
+}
+
+template <typename T>
+size_t trsv_persist_smem() {
+  return sizeof(T) * kTrsvB * kTrsvB + sizeof(T) * 8 * kTrsvB;
 }
 
 template <typename T>
 cudaError_t set_solver_smem_attrs() {
   cudaError_t e = cudaFuncSetAttribute((const void*)k_trsm_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(2 * 64 * 65 * sizeof(T)));
-  const int tb = (int)(sizeof(T) * kTrsvB * (kTrsvB + 1) + 16 + sizeof(double) * kTrsvB);
+  const int inv = (int)(sizeof(T) * (kTrsvB * (kTrsvB + 1) + kTrsvB));
+  const int ps = (int)trsv_persist_smem<T>();
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute((const void*)k_trsv_block<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb);
+    e = cudaFuncSetAttribute((const void*)k_trsv_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, inv);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute((const void*)k_trsv_block<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb);
+    e = cudaFuncSetAttribute((const void*)k_trsv_persist<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute((const void*)k_trsv_persist<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute((const void*)k_trsv_persist<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute((const void*)k_trsv_persist<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps);
   return e;
 }
 
@@ -511,16 +783,18 @@ __global__ void k_vmul(int64_t n, const double* __restrict__ a, const double* __
 // =====================================================================================
 template <typename T>
 struct LuWork {
-  T* cand = nullptr;         // panel records [2][ncta][kRec]
-  unsigned* cnt = nullptr;   // panel arrival counters [2] (only grow)
-  unsigned arrived[2] = {0, 0};  // host copy of the counters' values after the last launch
+  CaluBufs<T> cb{};          // buffers of the panel kernel (one allocation at cb_mem)
+  void* cb_mem = nullptr;
   int* ipiv_dev = nullptr;  // N entries (global, absolute row of each exchange)
   int* perm = nullptr;      // N entries: row i of P A is row perm[i] of A
   double* tmp = nullptr;    // N-vector scratch of lu_apply
   int* info = nullptr;
   GridSync* gs = nullptr;
   int ncta = 0;
-  int rows_cap = 0;
+  T* dinv = nullptr;         // inverses of the diagonal blocks of L and U, [nblk][2][kTrsvB^2]
+  int* tflags = nullptr;     // per-block release flags of the triangular solves
+  int ttag = 0;              // tag of the last triangular-solve launch
+  int trsv_grid = 0;         // co-resident CTAs of the persistent triangular solve
   void* gemm_ws = nullptr;   // BF16 split workspace of the tensor-core GEMM (FP32 LU only)
   size_t gemm_ws_bytes = 0;
   int* gemm_err = nullptr;   // raised by the tensor-core GEMM's bounded waits
@@ -528,24 +802,29 @@ struct LuWork {
 
 template <typename T>
 static ibem_status panel(T* A, int64_t lda, int64_t k0, int64_t m, int nb, LuWork<T>& w, cudaStream_t st) {
-  // rows per CTA so that every CTA fits its rows in shared memory
-  int ncta = w.ncta;
+  // CTAs: at most one per SM, at least kCaluMinRows rows each; the tree's fan-in F ~ sqrt
+  int ncta = (int)std::max<int64_t>(1, std::min<int64_t>(w.ncta, (m + kCaluMinRows - 1) / kCaluMinRows));
   int rows_per = (int)((m + ncta - 1) / ncta);
-  if (rows_per > w.rows_cap) return fail(IBEM_ERR_ARG, "panel too tall for shared memory");
-  if (rows_per < 1) rows_per = 1;
   ncta = (int)((m + rows_per - 1) / rows_per);
-  size_t smem = (size_t)rows_per * kLeaf * sizeof(T);
+  int F = 1;
+  while (F * F < ncta) ++F;
+  const int G = (ncta + F - 1) / F;
+  // rows of the largest elimination (own rows, a group's or the root's candidates)
+  const int rows = std::max(rows_per, std::max(F, G) * kLeaf);
+  if (rows > kPanelThreads * kPanelRmax || ncta > kCaluMaxCta)
+    return fail(IBEM_ERR_ARG, "panel too tall for the panel kernel");
+  const void* fn = rows <= kPanelThreads       ? (const void*)k_panel<T, 1>
+                   : rows <= 2 * kPanelThreads ? (const void*)k_panel<T, 2>
+                                               : (const void*)k_panel<T, 4>;
   T* P = A + k0 * lda + k0;
   int mm = (int)m;
   int* ip = w.ipiv_dev + k0;
   int kg = (int)k0;
-  unsigned b0 = w.arrived[0], b1 = w.arrived[1];
-  void* args[] = {&P, &lda, &mm, &nb, &rows_per, &w.cand, &w.cnt, &b0, &b1, &ip, &kg, &w.info, &w.gs};
+  int tag = (int)k0 + 1;   // unique within the factorisation; the flags start at zero
+  void* args[] = {&P, &lda, &mm, &nb, &rows_per, &F, &w.cb, &tag, &ip, &kg, &w.info, &w.gs};
   ProfScope ps(PROF_PANEL, st);
   count_launch();
-  IBEM_CUDA(cudaLaunchCooperativeKernel((void*)k_panel<T>, dim3(ncta), dim3(kPanelThreads), args, smem, st));
-  w.arrived[0] += (unsigned)ncta * (unsigned)((nb + 1) / 2);
-  w.arrived[1] += (unsigned)ncta * (unsigned)(nb / 2);
+  IBEM_CUDA(cudaLaunchCooperativeKernel(fn, dim3(ncta), dim3(kPanelThreads), args, 0, st));
   return IBEM_OK;
 }
 
@@ -637,30 +916,34 @@ static ibem_status lu_rec(T* A, int64_t lda, int64_t N, int64_t k0, int64_t n, L
 
 template <typename T>
 static ibem_status lu_alloc(LuWork<T>& w, int64_t N) {
-  int dev = 0, nsm = 0, smem_optin = 0;
+  int dev = 0, nsm = 0;
   IBEM_CUDA(cudaGetDevice(&dev));
   IBEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  IBEM_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  const int static_smem = 2 * kLeaf * (int)sizeof(T) + 64;
-  int dyn_cap = std::min(smem_optin - static_smem - 1024, 200 * 1024);
-  w.rows_cap = dyn_cap / (kLeaf * (int)sizeof(T));
-  IBEM_CUDA(cudaFuncSetAttribute((const void*)k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_cap));
   IBEM_CUDA(set_solver_smem_attrs<T>());
   int per_sm = 0;
-  IBEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_panel<T>, kPanelThreads,
-                                                          (size_t)w.rows_cap * kLeaf * sizeof(T)));
+  IBEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_panel<T, kPanelRmax>, kPanelThreads, 0));
   if (per_sm < 1) return fail(IBEM_ERR_CUDA, "panel kernel cannot be resident");
-  w.ncta = std::min(nsm, kPanelThreads);  // one CTA per SM (co-resident for the cooperative launch);
-                                          // the candidate argmax uses one thread per CTA
-  if ((int64_t)w.ncta * w.rows_cap < N) return fail(IBEM_ERR_ARG, "matrix too large for the panel kernel");
-  IBEM_CUDA(cudaMalloc(&w.cand, sizeof(T) * 2 * (size_t)w.ncta * kRec));
-  IBEM_CUDA(cudaMalloc(&w.cnt, sizeof(unsigned) * 2));
-  IBEM_CUDA(cudaMemset(w.cnt, 0, sizeof(unsigned) * 2));
+  w.ncta = std::min(nsm, kCaluMaxCta);  // at most one CTA per SM (co-resident for the cooperative launch)
+  if ((int64_t)w.ncta * kPanelThreads * kPanelRmax < N) return fail(IBEM_ERR_ARG, "matrix too large for the panel kernel");
+  IBEM_CUDA(cudaMalloc(&w.cb_mem, calu_bytes<T>(w.ncta)));
+  IBEM_CUDA(cudaMemset(w.cb_mem, 0, calu_bytes<T>(w.ncta)));
+  w.cb = calu_carve<T>(static_cast<unsigned char*>(w.cb_mem), w.ncta);
   IBEM_CUDA(cudaMalloc(&w.ipiv_dev, sizeof(int) * (size_t)N));
   IBEM_CUDA(cudaMalloc(&w.perm, sizeof(int) * (size_t)N));
   IBEM_CUDA(cudaMalloc(&w.tmp, sizeof(double) * (size_t)N));
   IBEM_CUDA(cudaMalloc(&w.info, sizeof(int)));
   IBEM_CUDA(cudaMalloc(&w.gs, sizeof(GridSync)));
+  {
+    const int64_t nblk = (N + kTrsvB - 1) / kTrsvB;
+    IBEM_CUDA(cudaMalloc(&w.dinv, sizeof(T) * 2 * (size_t)nblk * kTrsvB * kTrsvB));
+    IBEM_CUDA(cudaMalloc(&w.tflags, sizeof(int) * (size_t)nblk));
+    IBEM_CUDA(cudaMemset(w.tflags, 0, sizeof(int) * (size_t)nblk));
+    int per = 0;
+    IBEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_trsv_persist<T, true, true>, kTrsvThreads,
+                                                            trsv_persist_smem<T>()));
+    if (per < 1) return fail(IBEM_ERR_CUDA, "triangular-solve kernel cannot be resident");
+    w.trsv_grid = per * nsm;
+  }
   IBEM_CUDA(cudaMemset(w.info, 0, sizeof(int)));
   IBEM_CUDA(cudaMemset(w.gs, 0, sizeof(GridSync)));
   if (sizeof(T) == sizeof(float)) {
@@ -674,40 +957,64 @@ static ibem_status lu_alloc(LuWork<T>& w, int64_t N) {
 
 template <typename T>
 static void lu_free(LuWork<T>& w) {
-  cudaFree(w.cand);
-  cudaFree(w.cnt);
+  cudaFree(w.cb_mem);
   cudaFree(w.ipiv_dev);
   cudaFree(w.perm);
   cudaFree(w.tmp);
   cudaFree(w.info);
   cudaFree(w.gs);
+  cudaFree(w.dinv);
+  cudaFree(w.tflags);
   cudaFree(w.gemm_ws);
   cudaFree(w.gemm_err);
   w = LuWork<T>();
 }
 
-// Solve with the factors F (precision T): y <- U^-1 L^-1 P y (y FP64, in place; tmp N-vector)
+// Inverses of the diagonal blocks of the factors (after the factorisation, before any solve)
 template <typename T>
-static ibem_status lu_apply(const T* F, int64_t ldf, int64_t N, const int* perm, double* tmp, double* y,
-                            cudaStream_t st) {
+static ibem_status trsv_prepare(const T* F, int64_t ldf, int64_t N, LuWork<T>& w, cudaStream_t st) {
+  const unsigned nblk = (unsigned)((N + kTrsvB - 1) / kTrsvB);
+  ProfScope ps(PROF_TRSV, st);
+  const size_t smem = sizeof(T) * (kTrsvB * (kTrsvB + 1) + kTrsvB);
+  ::ibem::count_launch(), k_trsv_inv<T><<<dim3(nblk, 2), kTrsvB, smem, st>>>(F, ldf, N, w.dinv);
+  IBEM_LAUNCH_CHECK("trsv_prepare");
+  return IBEM_OK;
+}
+
+template <typename T, bool LOWER>
+static ibem_status trsv_launch(const T* F, int64_t ldf, int64_t N, LuWork<T>& w, const double* rhs, double* xo,
+                               cudaStream_t st) {
+  int nblk = (int)((N + kTrsvB - 1) / kTrsvB);
+  const bool vec = (ldf % (int64_t)(16 / sizeof(T)) == 0) && (reinterpret_cast<uintptr_t>(F) % 16 == 0);
+  const unsigned grid = (unsigned)std::min(nblk, w.trsv_grid);
+  int tag = ++w.ttag;
+  void* args[] = {&F, &ldf, &N, &nblk, &w.dinv, &rhs, &xo, &w.tflags, &tag, &w.gs};
+  const void* fn = vec ? (const void*)k_trsv_persist<T, LOWER, true> : (const void*)k_trsv_persist<T, LOWER, false>;
+  ::ibem::count_launch();
+  IBEM_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kTrsvThreads), args, trsv_persist_smem<T>(), st));
+  return IBEM_OK;
+}
+
+// Solve with the factors F (precision T): y <- U^-1 L^-1 P y (y FP64, in place; w.tmp N-vector).
+// A wait that gave up sets the sticky flag w.gs->err, read by the caller (sticky_err).
+template <typename T>
+static ibem_status lu_apply(const T* F, int64_t ldf, int64_t N, LuWork<T>& w, double* y, cudaStream_t st) {
   ProfScope ps(PROF_TRSV, st, 2.0 * N * N);
-  ::ibem::count_launch(), k_gather<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, perm, y, tmp);
-  const size_t smem = sizeof(T) * kTrsvB * (kTrsvB + 1) + 16 + sizeof(double) * kTrsvB;
-  // forward: unit lower, right-hand side and updates in tmp, solved blocks to y
-  for (int64_t k0 = 0; k0 < N; k0 += kTrsvB) {
-    const int b = (int)std::min<int64_t>(kTrsvB, N - k0);
-    const int64_t rows = N - k0 - b;
-    const unsigned grid = (unsigned)std::max<int64_t>(1, (rows + 255) / 256);
-    ::ibem::count_launch(), k_trsv_block<T, true><<<grid, 256, smem, st>>>(F, ldf, N, k0, b, tmp, y);
-  }
-  // backward: upper, right-hand side and updates in y, solved blocks to tmp
-  for (int64_t k0 = ((N - 1) / kTrsvB) * kTrsvB; k0 >= 0; k0 -= kTrsvB) {
-    const int b = (int)std::min<int64_t>(kTrsvB, N - k0);
-    const unsigned grid = (unsigned)std::max<int64_t>(1, (k0 + 255) / 256);
-    ::ibem::count_launch(), k_trsv_block<T, false><<<grid, 256, smem, st>>>(F, ldf, N, k0, b, y, tmp);
-  }
-  IBEM_CUDA(cudaMemcpyAsync(y, tmp, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+  ::ibem::count_launch(), k_gather<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, w.perm, y, w.tmp);
+  ibem_status s = trsv_launch<T, true>(F, ldf, N, w, w.tmp, y, st);    // forward: L z = P y
+  if (!s) s = trsv_launch<T, false>(F, ldf, N, w, y, w.tmp, st);      // backward: U x = z
+  if (s) return s;
+  IBEM_CUDA(cudaMemcpyAsync(y, w.tmp, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
   IBEM_LAUNCH_CHECK("lu_apply");
+  return IBEM_OK;
+}
+
+template <typename T>
+static ibem_status sticky_err(const LuWork<T>& w, cudaStream_t st) {
+  GridSync hgs{};
+  IBEM_CUDA(cudaMemcpyAsync(&hgs, w.gs, sizeof(GridSync), cudaMemcpyDeviceToHost, st));
+  IBEM_CUDA(cudaStreamSynchronize(st));
+  if (hgs.err) return fail(IBEM_ERR_TIMEOUT, "a bounded wait of the panel or triangular-solve kernel gave up");
   return IBEM_OK;
 }
 
@@ -857,6 +1164,7 @@ static ibem_status factor(SolveCtx& cx, const double* A, int64_t lda, T*& W, LuW
   ibem_status s = lu_alloc(w, N);
   if (s) return s;
   s = lu_rec<T>(W, N, N, 0, N, w, cx.st);
+  if (!s) s = trsv_prepare<T>(W, N, N, w, cx.st);
   if (s) return s;
   // row permutation from the sequence of exchanges (LAPACK ipiv semantics)
   {
@@ -878,7 +1186,7 @@ static ibem_status factor(SolveCtx& cx, const double* A, int64_t lda, T*& W, LuW
   IBEM_CUDA(cudaMemcpyAsync(&hgs, w.gs, sizeof(GridSync), cudaMemcpyDeviceToHost, cx.st));
   if (w.gemm_err) IBEM_CUDA(cudaMemcpyAsync(&herr, w.gemm_err, sizeof(int), cudaMemcpyDeviceToHost, cx.st));
   IBEM_CUDA(cudaStreamSynchronize(cx.st));
-  if (hgs.err) return fail(IBEM_ERR_TIMEOUT, "panel grid barrier gave up");
+  if (hgs.err) return fail(IBEM_ERR_TIMEOUT, "a bounded wait of the panel kernel gave up");
   if (herr) return fail(IBEM_ERR_TIMEOUT, "tensor-core GEMM wait gave up");
   info = hinfo;
   return IBEM_OK;
@@ -925,7 +1233,8 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
     if (!s) {
       ::ibem::count_launch(), k_vmul<<<nb, 256, 0, st>>>(N, cx.r, b, bs);
       IBEM_CUDA(cudaMemcpyAsync(ys, bs, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
-      s = lu_apply<double>(W, N, N, w.perm, w.tmp, ys, st);
+      s = lu_apply<double>(W, N, N, w, ys, st);
+      if (!s) s = sticky_err(w, st);
     }
     cudaEventRecord(e2, st);
     if (!s) s = finish_norm();
@@ -951,11 +1260,12 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
     if (!s) {
       ::ibem::count_launch(), k_vmul<<<nb, 256, 0, st>>>(N, cx.r, b, bs);
       IBEM_CUDA(cudaMemcpyAsync(ys, bs, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
-      s = lu_apply<float>(W, N, N, w.perm, w.tmp, ys, st);
+      s = lu_apply<float>(W, N, N, w, ys, st);
     }
     if (!s) s = finish_norm();
     int iters = 0;
     for (int outer = 0; !s && outer < max_outer; ++outer) {
+      if ((s = sticky_err(w, st))) break;
       double be = 0;
       if ((s = scaled_backward_error(cx, A, lda, ys, bs, rvec, tmp, as_norm, be))) break;
       R.backward_error = be;
@@ -977,7 +1287,7 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
         double* zk = Z + (size_t)k * N;
         double* wv = V + (size_t)(k + 1) * N;
         IBEM_CUDA(cudaMemcpyAsync(zk, vk, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
-        if ((s = lu_apply<float>(W, N, N, w.perm, w.tmp, zk, st))) break;
+        if ((s = lu_apply<float>(W, N, N, w, zk, st))) break;
         if ((s = scaled_matvec(cx, A, lda, zk, tmp, wv))) break;
         // classical Gram-Schmidt, twice
         std::vector<double> hk(k + 1, 0.0), h2(k + 1);
@@ -1028,6 +1338,7 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
       IBEM_LAUNCH_CHECK("gmres update");
     }
     cudaEventRecord(e2, st);
+    if (!s) s = sticky_err(w, st);
     if (!s) {
       double be = 0;
       s = scaled_backward_error(cx, A, lda, ys, bs, rvec, tmp, as_norm, be);
@@ -1078,19 +1389,21 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
 // ===================================================================================
 namespace {
 constexpr int64_t kNoAllocMaxN = 1024;
-constexpr int kNoAllocMaxCta = 256;   // panel kernel CTAs (>= SMs of one GPU)
 constexpr int kNoAllocParts = 16;
 constexpr size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 constexpr size_t kNaW = 0;                                                           // N x N factor copy
 constexpr size_t kNaVec = align256(sizeof(double) * kNoAllocMaxN * kNoAllocMaxN);    // 6 N-vectors
 constexpr size_t kNaPerm = kNaVec + 6 * align256(sizeof(double) * kNoAllocMaxN);     // perm, ipiv
 constexpr size_t kNaCand = kNaPerm + 2 * align256(sizeof(int) * kNoAllocMaxN);
-constexpr size_t kNaSeq = kNaCand + align256(sizeof(double) * 2 * kNoAllocMaxCta * kRec);  // panel records
-constexpr size_t kNaGs = kNaSeq + align256(sizeof(unsigned) * 2);                            // panel counters
+constexpr int kNoAllocCaluCta = (int)((kNoAllocMaxN + kCaluMinRows - 1) / kCaluMinRows);  // panel CTAs at most
+constexpr size_t kNaGs = kNaCand + calu_bytes<double>(kNoAllocCaluCta);                    // panel buffers
 constexpr size_t kNaInfo = kNaGs + align256(sizeof(GridSync));
 constexpr size_t kNaPart = kNaInfo + align256(sizeof(int));
 constexpr size_t kNaRed = kNaPart + align256(sizeof(double) * kNoAllocParts * kNoAllocMaxN);
-constexpr size_t kNoAllocBytes = kNaRed + align256(sizeof(double) * 4);
+constexpr int kNoAllocBlk = (int)((kNoAllocMaxN + kTrsvB - 1) / kTrsvB);                   // triangular-solve blocks
+constexpr size_t kNaDinv = kNaRed + align256(sizeof(double) * 4);
+constexpr size_t kNaTflags = kNaDinv + align256(sizeof(double) * 2 * kNoAllocBlk * kTrsvB * kTrsvB);
+constexpr size_t kNoAllocBytes = kNaTflags + align256(sizeof(int) * kNoAllocBlk);
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -1098,7 +1411,7 @@ constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
 unsigned char* g_noalloc_base[kNoAllocMaxDevices] = {};
 int g_noalloc_ncta[kNoAllocMaxDevices] = {};
-int g_noalloc_rows_cap[kNoAllocMaxDevices] = {};
+int g_noalloc_trsv_grid[kNoAllocMaxDevices] = {};
 
 // row exchanges (LAPACK ipiv) -> gather permutation, one thread (N <= kNoAllocMaxN)
 __global__ void k_ipiv_to_perm(int64_t n, const int* __restrict__ ipiv, int* __restrict__ perm) {
@@ -1135,33 +1448,29 @@ __global__ void k_absmax4(int64_t n, const double* __restrict__ a, const double*
 }
 }  // namespace
 
-static ibem_status noalloc_setup(int dev, unsigned char** base, int* ncta, int* rows_cap) {
+static ibem_status noalloc_setup(int dev, unsigned char** base, int* ncta, int* trsv_grid) {
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(IBEM_ERR_ARG, "solve_noalloc: device index out of range");
   if (!g_noalloc_base[dev]) {
     void* p = nullptr;
     IBEM_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    int nsm = 0, smem_optin = 0;
+    int nsm = 0;
     IBEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    IBEM_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    if (nsm > kNoAllocMaxCta) return fail(IBEM_ERR_ARG, "solve_noalloc: more SMs than the static panel scratch holds");
-    const int static_smem = 2 * kLeaf * (int)sizeof(double) + 64;
-    const int dyn_cap = std::min(smem_optin - static_smem - 1024, 200 * 1024);
-    IBEM_CUDA(cudaFuncSetAttribute((const void*)k_panel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   dyn_cap));
     IBEM_CUDA(set_solver_smem_attrs<double>());
     int per_sm = 0;
-    const int cap = dyn_cap / (kLeaf * (int)sizeof(double));
-    IBEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_panel<double>, kPanelThreads,
-                                                            (size_t)cap * kLeaf * sizeof(double)));
+    IBEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_panel<double, kPanelRmax>, kPanelThreads, 0));
     if (per_sm < 1) return fail(IBEM_ERR_CUDA, "solve_noalloc: panel kernel cannot be resident");
-    g_noalloc_ncta[dev] = std::min(nsm, kPanelThreads);
-    g_noalloc_rows_cap[dev] = cap;
+    int per_tr = 0;
+    IBEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_tr, k_trsv_persist<double, true, true>, kTrsvThreads,
+                                                            trsv_persist_smem<double>()));
+    if (per_tr < 1) return fail(IBEM_ERR_CUDA, "solve_noalloc: triangular-solve kernel cannot be resident");
+    g_noalloc_trsv_grid[dev] = per_tr * nsm;
+    g_noalloc_ncta[dev] = std::min(nsm, kCaluMaxCta);
     g_noalloc_base[dev] = static_cast<unsigned char*>(p);
   }
   *base = g_noalloc_base[dev];
   *ncta = g_noalloc_ncta[dev];
-  *rows_cap = g_noalloc_rows_cap[dev];
+  *trsv_grid = g_noalloc_trsv_grid[dev];
   return IBEM_OK;
 }
 
@@ -1177,8 +1486,8 @@ ibem_status solve_fp64_noalloc(int64_t N, const double* A, int64_t lda, const do
   int dev = 0;
   IBEM_CUDA(cudaGetDevice(&dev));
   unsigned char* base = nullptr;
-  int ncta = 0, rows_cap = 0;
-  ibem_status s = noalloc_setup(dev, &base, &ncta, &rows_cap);
+  int ncta = 0, trsv_grid = 0;
+  ibem_status s = noalloc_setup(dev, &base, &ncta, &trsv_grid);
   if (s) return s;
   double* W = reinterpret_cast<double*>(base + kNaW);
   double* vec[6];
@@ -1193,28 +1502,30 @@ ibem_status solve_fp64_noalloc(int64_t N, const double* A, int64_t lda, const do
   // the previous call's contents are still there: clear what must start at zero
   IBEM_CUDA(cudaMemsetAsync(gs, 0, sizeof(GridSync), st));
   IBEM_CUDA(cudaMemsetAsync(info, 0, sizeof(int), st));
-  unsigned* cntf = reinterpret_cast<unsigned*>(base + kNaSeq);
-  IBEM_CUDA(cudaMemsetAsync(cntf, 0, sizeof(unsigned) * 2, st));
+  IBEM_CUDA(cudaMemsetAsync(base + kNaCand, 0, calu_bytes<double>(kNoAllocCaluCta), st));
   const unsigned nb = (unsigned)((N + 255) / 256);
   ::ibem::count_launch(), k_rowmax<<<nb, 256, 0, st>>>(N, A, lda, r);
   ::ibem::count_launch(), k_colmax<<<(unsigned)N, 256, 0, st>>>(N, A, lda, r, c);
   ::ibem::count_launch(), k_scale_copy<double><<<dim3(nb, (unsigned)N), 256, 0, st>>>(N, A, lda, r, c, W, N);
   IBEM_LAUNCH_CHECK("solve_noalloc: equilibrate");
   LuWork<double> w;
-  w.cand = reinterpret_cast<double*>(base + kNaCand);
-  w.cnt = cntf;
+  w.cb = calu_carve<double>(base + kNaCand, kNoAllocCaluCta);
   w.ipiv_dev = ipiv;
   w.perm = perm;
   w.tmp = tmp;
   w.info = info;
   w.gs = gs;
-  w.ncta = ncta;
-  w.rows_cap = rows_cap;
+  w.ncta = std::min(ncta, kNoAllocCaluCta);
+  w.dinv = reinterpret_cast<double*>(base + kNaDinv);
+  w.tflags = reinterpret_cast<int*>(base + kNaTflags);
+  w.trsv_grid = trsv_grid;
+  IBEM_CUDA(cudaMemsetAsync(w.tflags, 0, sizeof(int) * kNoAllocBlk, st));
   if ((s = lu_rec<double>(W, N, N, 0, N, w, st))) return s;
+  if ((s = trsv_prepare<double>(W, N, N, w, st))) return s;
   ::ibem::count_launch(), k_ipiv_to_perm<<<1, 1, 0, st>>>(N, ipiv, perm);
   ::ibem::count_launch(), k_vmul<<<nb, 256, 0, st>>>(N, r, b, bs);
   IBEM_CUDA(cudaMemcpyAsync(ys, bs, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
-  if ((s = lu_apply<double>(W, N, N, perm, tmp, ys, st))) return s;
+  if ((s = lu_apply<double>(W, N, N, w, ys, st))) return s;
   ::ibem::count_launch(), k_vmul<<<nb, 256, 0, st>>>(N, c, ys, x);
   // scaled backward error, reduced on the device
   ::ibem::count_launch(), k_vmul<<<nb, 256, 0, st>>>(N, c, ys, tmp);
@@ -1238,7 +1549,7 @@ ibem_status solve_fp64_noalloc(int64_t N, const double* A, int64_t lda, const do
     R.info = hinfo;
     *rep = R;
   }
-  if (hgs.err) return fail(IBEM_ERR_TIMEOUT, "solve_noalloc: panel grid barrier gave up");
+  if (hgs.err) return fail(IBEM_ERR_TIMEOUT, "solve_noalloc: a bounded wait of the panel or triangular-solve kernel gave up");
   if (hinfo) return fail(IBEM_ERR_SINGULAR, "solve_noalloc: zero pivot");
   return IBEM_OK;
 }

@@ -167,7 +167,7 @@ ibem_status ibem_gemm_sub_f32(int64_t m, int64_t n, int64_t k, const float* A_de
  * belongs to a host framework (a caching allocator or a budget reserved up front, where a
  * raw cudaMalloc can fail or fragment that budget) and for latency-critical loops, where
  * cudaMalloc/cudaFree can stall the device.  The caller owns A_dev (left intact), b_dev
- * and x_dev; the rest of the workspace is one static device array of about 9 MB inside
+ * and x_dev; the rest of the workspace is one static device array of about 11 MB inside
  * the library, held by every GPU that loads it until the process exits, which limits N
  * to 1024 (larger N returns IBEM_ERR_ARG).  The first call on a device looks the array's
  * address up (setup), so make it before any stream capture.  Every call reuses the same
