@@ -10,7 +10,7 @@ inputs (no dataset is involved).
 
 A step = sphere-pair assembly (FP64) + far-field right-hand side + solve in the chosen
 form (FP32 LU with split-BF16 tensor-core updates + FP64 GMRES-IR to a scaled backward
-error <= tol) + stresses at all grid points (FP64).  `value` is seconds per solution with
+error <= tol) + stresses at all grid points (double-float sphere sums, ~48 bits).  `value` is seconds per solution with
 inputs resident in HBM; `e2e` is the same through ibem_e3d_run_host with host buffers
 (inputs copied in and X / stresses copied out inside the timed region).  The plain FP64
 form is timed once on the same microstructure and its relative difference reported.
@@ -223,8 +223,8 @@ def run_ours(args, rank, world):
         ev[1].record(stream)
         g.check(L.ibem_e3d_solve(form, N, P(A), N, P(b), P(xo), args.tol, ctypes.byref(rep), sp))
         ev[2].record(stream)
-        g.check(L.ibem_e3d_field(P(pts), nump, P(cen), P(rad), num, ctypes.byref(m), 24, P(xo), None, 0, None, 0,
-                                 None, None, sigp, P(So), sp))
+        g.check(L.ibem_e3d_field_form(form, P(pts), nump, P(cen), P(rad), num, ctypes.byref(m), 24, P(xo), None, 0,
+                                      None, 0, None, None, sigp, P(So), sp))
         ev[3].record(stream)
         return ev
 

@@ -304,13 +304,14 @@ ibem_status ibem_e3d_solve_noalloc(int64_t N, const double* A_dev, int64_t lda, 
   return solve_fp64_noalloc(N, A_dev, lda, b_dev, x_dev, report, as_stream(stream));
 }
 
-ibem_status ibem_e3d_field(const double* points_dev, int nump, const double* centers_dev,
-                           const double* radius_dev, int num, const ibem_material* mat,
-                           int layout, const double* E_dev, const double* nodes_dev, int NN,
-                           const int* conn_dev, int NE, const double* U_dev,
-                           const double* T_dev, const double* sig_inf, double* stress_dev,
-                           void* stream) {
+ibem_status ibem_e3d_field_form(ibem_solver_form form, const double* points_dev, int nump,
+                                const double* centers_dev, const double* radius_dev, int num,
+                                const ibem_material* mat, int layout, const double* E_dev,
+                                const double* nodes_dev, int NN, const int* conn_dev, int NE,
+                                const double* U_dev, const double* T_dev, const double* sig_inf,
+                                double* stress_dev, void* stream) {
   if (!mat || !valid_layout(layout) || nump < 0 || num < 0) return fail(IBEM_ERR_ARG, "field: bad arguments");
+  if (form != IBEM_SOLVE_FP64 && form != IBEM_SOLVE_MIXED_IR) return fail(IBEM_ERR_ARG, "field: unknown form");
   if (nump == 0) return IBEM_OK;
   cudaStream_t st = as_stream(stream);
   if (NE > 0) {
@@ -324,9 +325,21 @@ ibem_status ibem_e3d_field(const double* points_dev, int nump, const double* cen
   }
   if (num == 0) return IBEM_OK;
   SphLaunch p = sph(centers_dev, radius_dev, num, mat);
-  if (layout == 24) return launch_field24(p, points_dev, nump, E_dev, stress_dev, st);
+  if (layout == 24)
+    return form == IBEM_SOLVE_MIXED_IR ? launch_field24_df(p, points_dev, nump, E_dev, stress_dev, st)
+                                       : launch_field24(p, points_dev, nump, E_dev, stress_dev, st);
   if (layout == 60) return launch_field60(p, points_dev, nump, E_dev, stress_dev, st);
   return launch_field78(p, points_dev, nump, E_dev, stress_dev, st);
+}
+
+ibem_status ibem_e3d_field(const double* points_dev, int nump, const double* centers_dev,
+                           const double* radius_dev, int num, const ibem_material* mat,
+                           int layout, const double* E_dev, const double* nodes_dev, int NN,
+                           const int* conn_dev, int NE, const double* U_dev,
+                           const double* T_dev, const double* sig_inf, double* stress_dev,
+                           void* stream) {
+  return ibem_e3d_field_form(IBEM_SOLVE_FP64, points_dev, nump, centers_dev, radius_dev, num, mat, layout, E_dev,
+                             nodes_dev, NN, conn_dev, NE, U_dev, T_dev, sig_inf, stress_dev, stream);
 }
 
 }  // extern "C"

@@ -111,3 +111,127 @@ IBEM_HD IBEM_INLINE void sph_field24_contracted(const double x0, const double x1
     e[t] += mc.kd * r;
   }
 }
+
+// ----------------------------------------------------------------------------------------
+// The same contraction in double-float arithmetic (dfloat.cuh), for the mixed-precision
+// form.  The strain of an inclusion depends on x / a only: with x' = x / a, a' = 1 and the
+// order-1 eigenstrain scaled to F' = a F, every term above is unchanged (E' = F'.x' = F.x,
+// and the coefficients of each power of x scale with the matching power of a), so the sums
+// run on O(1) quantities that stay well inside the FP32 exponent range for any sphere size.
+#include "dfloat.cuh"
+
+namespace ibem {
+
+// per-sphere constants of the double-float sum (scaled coordinates)
+struct SphDF {
+  dfloat c[3];   // centre
+  dfloat ia;     // 1 / a
+  dfloat E[6];   // order-0 eigenstrain, storage order of the 24 unknowns
+  dfloat F[18];  // a * order-1 eigenstrain, F[3 t + p] for the symmetric pair t and p
+  dfloat v[3];   // v_n = sum_m F_mnm
+  dfloat w[3];   // w_p = sum_m F_mmp (also the trace vector g of the derivation)
+  dfloat tE;     // trace of E
+};
+
+IBEM_HD inline SphDF sph_df_make(const double* cen, double a, const double* Eu) {
+  SphDF s;
+  const double ia = 1.0 / a;
+  for (int i = 0; i < 3; ++i) s.c[i] = df_make(cen[i]);
+  s.ia = df_make(ia);
+  const int pi[6] = {0, 0, 0, 1, 1, 2}, pj[6] = {0, 1, 2, 1, 2, 2};
+  double F[3][3][3];
+  for (int t = 0; t < 6; ++t) {
+    s.E[t] = df_make(Eu[t]);
+    for (int p = 0; p < 3; ++p) {
+      F[pi[t]][pj[t]][p] = F[pj[t]][pi[t]][p] = a * Eu[6 + 3 * t + p];
+      s.F[3 * t + p] = df_make(a * Eu[6 + 3 * t + p]);
+    }
+  }
+  for (int n = 0; n < 3; ++n) {
+    s.v[n] = df_make(F[0][n][0] + F[1][n][1] + F[2][n][2]);
+    s.w[n] = df_make(F[0][0][n] + F[1][1][n] + F[2][2][n]);
+  }
+  s.tE = df_make(Eu[0] + Eu[3] + Eu[5]);
+  return s;
+}
+
+// e[6] += strain / c at the point (px, py, pz) (double-float, point already converted);
+// returns whether the point lies inside or on the sphere.  The caller multiplies by
+// c = 1 / (8 pi (1 - nu)) once, after the sum.
+IBEM_HD IBEM_INLINE bool sph_field24_df(const dfloat* p, const SphDF& sp, dfloat tn1, dfloat tn2, dfloat* e) {
+  dfloat x[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) x[i] = (p[i] - sp.c[i]) * sp.ia;
+  const dfloat r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+  const bool ext = r2.hi > 1.0f || (r2.hi == 1.0f && r2.lo > 0.0f);
+  const float fe = ext ? 1.0f : 0.0f;
+  const dfloat rho2 = ext ? r2 : dfloat{1.0f, 0.0f};
+  // ir = rho2^-1/2: FP32 estimate, one double-float Newton step
+  float y0;
+#ifdef __CUDA_ARCH__
+  y0 = rsqrtf(rho2.hi);
+#else
+  y0 = 1.0f / std::sqrt(rho2.hi);
+#endif
+  const dfloat yd{y0, 0.0f};
+  const dfloat t = dfloat{1.0f, 0.0f} - rho2 * (yd * yd);
+  const dfloat ir = yd + yd * (t * 0.5f);
+  const dfloat irho2 = ir * ir;
+  const dfloat four_pi = df_make(4.0 * IBEM_PI);
+  const dfloat j0 = four_pi * ir;
+  const dfloat p1 = j0 * irho2, p2 = p1 * irho2, p3 = p2 * irho2, p4 = p3 * irho2, p5 = p4 * irho2;
+  const dfloat J1 = p1 * df_make(1.0 / 3.0), J2 = p2 * df_make(1.0 / 5.0), J3 = p3 * df_make(1.0 / 7.0),
+               J4 = p4 * df_make(1.0 / 9.0), J5 = p5 * df_make(1.0 / 11.0);
+  const dfloat V0_1 = -J1, V0_2 = J2 * (5.0f * fe), V0_3 = J3 * (-35.0f * fe);
+  const dfloat V1_1 = -J2, V1_2 = J3 * (7.0f * fe), V1_3 = J4 * (-63.0f * fe);
+  const dfloat V2_1 = -J3, V2_2 = J4 * (9.0f * fe), V2_3 = J5 * (-99.0f * fe);
+  const dfloat Ps2 = V0_1 - V1_1, Ps3 = V0_2 - V1_2, Ps4 = V0_3 - V1_3;
+  const dfloat Q2 = V1_1 - V2_1, Q3 = V1_2 - V2_2, Q4 = V1_3 - V2_3;
+  const dfloat Ph1 = V0_1, Ph2 = V0_2;
+  // E x, E' = F'.x (symmetric), E' x, G^i x, s_i = x.G^i.x
+  const int ti[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};  // (m, n) -> symmetric pair
+  dfloat Ex[3], Ep[6], Epx[3], Gx[3][3], s[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) Ex[i] = sp.E[ti[i][0]] * x[0] + sp.E[ti[i][1]] * x[1] + sp.E[ti[i][2]] * x[2];
+#pragma unroll
+  for (int t = 0; t < 6; ++t) Ep[t] = sp.F[3 * t] * x[0] + sp.F[3 * t + 1] * x[1] + sp.F[3 * t + 2] * x[2];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) Epx[n] = Ep[ti[n][0]] * x[0] + Ep[ti[n][1]] * x[1] + Ep[ti[n][2]] * x[2];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      Gx[i][j] = sp.F[3 * ti[j][0] + i] * x[0] + sp.F[3 * ti[j][1] + i] * x[1] + sp.F[3 * ti[j][2] + i] * x[2];
+    s[i] = Gx[i][0] * x[0] + Gx[i][1] * x[1] + Gx[i][2] * x[2];
+  }
+  const dfloat q = Ex[0] * x[0] + Ex[1] * x[1] + Ex[2] * x[2];
+  const dfloat qp = Epx[0] * x[0] + Epx[1] * x[1] + Epx[2] * x[2];
+  const dfloat tEp = Ep[0] + Ep[3] + Ep[5];
+  const dfloat vx = sp.v[0] * x[0] + sp.v[1] * x[1] + sp.v[2] * x[2];
+  const dfloat wx = sp.w[0] * x[0] + sp.w[1] * x[1] + sp.w[2] * x[2];
+  const dfloat tE = sp.tE;
+  const dfloat tv = tEp + vx * 2.0f;
+  const dfloat A = Ps4 * q + Ps3 * tE - tE * Ph2 * tn2 + (Q4 * qp + Q3 * tv - wx * V1_2 * tn2);
+  const dfloat B = Ps3 * q + Ps2 * tE - tE * Ph1 * tn2 + (Q3 * qp + Q2 * tv - wx * V1_1 * tn2);
+  const dfloat tn1x2 = tn1 * 2.0f, tn1x4 = tn1 * 4.0f;
+  const dfloat cE = Ps3 * 2.0f - Ph2 * tn1x2;
+  const dfloat cEp = Q3 * 2.0f - V1_2 * tn1x2, cv = Q2 * 2.0f - V1_1 * tn1x2;
+  const dfloat cs = Q3, cgw = Q2 - V1_1 * tn2;  // g == w: the two terms share a coefficient
+  dfloat W[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) W[i] = cE * Ex[i] + cEp * Epx[i] + cv * sp.v[i] + cs * s[i] + cgw * sp.w[i];
+  const dfloat C0 = Ps2 * 2.0f - Ph1 * tn1x4;
+  const dfloat C1 = Q2 * 2.0f - V1_1 * tn1x4;
+  const dfloat C2 = Q2 * 2.0f - V1_1 * tn1x2;
+  const int pi[6] = {0, 0, 0, 1, 1, 2}, pj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    const int i = pi[t], j = pj[t];
+    dfloat r = A * x[i] * x[j] + W[i] * x[j] + W[j] * x[i] + C0 * sp.E[t] + C1 * Ep[t] + C2 * (Gx[i][j] + Gx[j][i]);
+    if (i == j) r += B;
+    e[t] += r;
+  }
+  return !ext;
+}
+
+}  // namespace ibem

@@ -46,6 +46,8 @@ ibem_status launch_node78(const SphLaunch& p, const double* nodes, int NN, doubl
 // particle part of the stress at points; sbase (nump x 6) holds the boundary or
 // remote stress on entry and the total stress on exit
 ibem_status launch_field24(const SphLaunch& p, const double* pts, int nump, const double* E, double* stress, cudaStream_t st);
+ibem_status launch_field24_df(const SphLaunch& p, const double* pts, int nump, const double* E, double* stress,
+                              cudaStream_t st);
 ibem_status launch_field60(const SphLaunch& p, const double* pts, int nump, const double* E, double* stress, cudaStream_t st);
 ibem_status launch_field78(const SphLaunch& p, const double* pts, int nump, const double* E, double* stress, cudaStream_t st);
 

@@ -105,7 +105,7 @@ struct GridSync {
 // Each wait is one polling thread, bounded by kSpinLimit; a wait that gives up sets the
 // sticky gs->err and the CTA returns.  Flags hold the tag of the launch (unique and
 // increasing within a factorisation), so they are never cleared between launches.
-// Ties in the pivot search go to the smallest row, so the result is deterministic.
+// Pivots: largest |a| to 14 bits, ties to the smallest row, so the result is deterministic.
 constexpr int kCaluMinRows = 256;   // fewest rows a CTA takes before fewer CTAs are used
 
 __device__ __forceinline__ int ld_acquire_s32(const int* p) {
@@ -131,78 +131,80 @@ struct CaluBufs {
 };
 constexpr int kCaluMaxCta = 256;
 
-// (v, i) beats (bv, bi): larger |a|, ties to the smaller row; i < 0 is "no candidate"
-template <typename T>
-__device__ __forceinline__ bool calu_better(T v, int i, T bv, int bi) {
-  return i >= 0 && (bi < 0 || v > bv || (v == bv && i < bi));
-}
-
-template <typename T>
-__device__ __forceinline__ void calu_warp_argmax(T& v, int& i) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const T ov = __shfl_down_sync(0xffffffffu, v, off);
-    const int oi = __shfl_down_sync(0xffffffffu, i, off);
-    if (calu_better(ov, oi, v, i)) { v = ov; i = oi; }
-  }
-}
-
 constexpr int kPanelRmax = 4;  // rows per thread at most (1024 rows per elimination)
 
 // Partial-pivoting elimination of the rows held in registers: thread t holds rows
 // q = t + kPanelThreads i (i < R) in a[i][*]; live[i] marks rows that exist and are not yet
 // pivots.  Picks k pivots: s_sel[j] = q of pivot j (-1 when the rows ran out) and
 // s_top[j][*] = that row as it stood at step j (multipliers left of j, U from j on).
-// Two CTA barriers per column; every thread folds the warp winners in the same order, so
-// all agree on the pivot.
+// Before step j every live row is stored rotated by j: a[c] = column (c + j) mod kLeaf, so
+// column j is a[0], the columns still to update are a[1 .. kLeaf-1-j] and the multipliers
+// of steps 0 .. j-1 sit in a[kLeaf-j .. kLeaf-1].  One step rotates by one more (update and
+// shift fused), which keeps every register index static while the column loop stays
+// rolled (small code: the loop runs from the instruction cache).  The pivot's reciprocal
+// scales the column, as LAPACK's getf2 does.  Two CTA barriers per column; every thread
+// folds the warp winners in the same order, so all agree on the pivot.
+__device__ __forceinline__ float calu_rcp(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double calu_rcp(double x) { return __drcp_rn(x); }
+
+// Pivot search key of row q (< 1024) with |a| = av: the top 22 bits of the FP32 |a| above
+// the inverted row index, so one unsigned max picks the largest |a| (to 14 bits, about
+// 6e-5 relative) with ties to the smallest row; 0 is "no row".
+__device__ __forceinline__ unsigned calu_key(float av, int q) {
+  return (((__float_as_uint(av) >> 9) + 1u) << 10) | (unsigned)(1023 - q);
+}
+
 template <typename T, int R>
-__device__ __forceinline__ void calu_elim(T (&a)[R][kLeaf], bool (&live)[R], int k, T* s_top, int* s_sel, T* s_bv,
-                                          int* s_bq) {
+__device__ __forceinline__ void calu_elim(T (&a)[R][kLeaf], bool (&live)[R], int k, T* s_top, T* s_pr, int* s_sel,
+                                          unsigned* s_key) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int nw = kPanelThreads / 32;
-  bool more = true;  // uniform: rows remain for the next pivot
+#pragma unroll 1
+  for (int j = 0; j < k; ++j) {
+    unsigned key = 0;
 #pragma unroll
-  for (int j = 0; j < kLeaf; ++j) {
-    if (j < k && more) {
-      T bv = -1;
-      int bq = -1;
+    for (int i = 0; i < R; ++i)
+      if (live[i]) key = max(key, calu_key((float)fabs(a[i][0]), tid + kPanelThreads * i));
+    key = __reduce_max_sync(0xffffffffu, key);
+    if (lane == 0) s_key[warp] = key;
+    __syncthreads();
 #pragma unroll
-      for (int i = 0; i < R; ++i) {
-        const int q = tid + kPanelThreads * i;
-        const T v = fabs(a[i][j]);
-        if (live[i] && calu_better(v, q, bv, bq)) { bv = v; bq = q; }
+    for (int w = 0; w < nw; ++w) key = max(key, s_key[w]);
+    if (key == 0) {  // uniform: no rows left for this and later pivots
+      if (tid == 0)
+        for (int jj = j; jj < k; ++jj) s_sel[jj] = -1;
+      break;
+    }
+    const int bq = 1023 - (int)(key & 1023u);
+    // the owner thread alone publishes the pivot row: un-rotated into s_top[j] (the
+    // factored block) and rotated into s_pr (the update's operand, static offsets, zero
+    // where a[] holds multipliers)
+    if (tid == bq % kPanelThreads) {
+      const int oi = bq / kPanelThreads;
+#pragma unroll
+      for (int c = 0; c < kLeaf; ++c) {
+        T v = a[0][c];
+#pragma unroll
+        for (int i = 1; i < R; ++i) v = oi == i ? a[i][c] : v;  // selects, not an indexed read
+        s_top[j * kLdS + ((c + j) & (kLeaf - 1))] = v;
+        s_pr[c] = (c + j < kLeaf) ? v : (T)0;
       }
-      calu_warp_argmax(bv, bq);
-      if (lane == 0) { s_bv[warp] = bv; s_bq[warp] = bq; }
-      __syncthreads();
-      bv = s_bv[0];
-      bq = s_bq[0];
 #pragma unroll
-      for (int w = 1; w < nw; ++w)
-        if (calu_better(s_bv[w], s_bq[w], bv, bq)) { bv = s_bv[w]; bq = s_bq[w]; }
-      if (bq < 0) {
-        more = false;
-        if (tid == 0)
-          for (int jj = j; jj < k; ++jj) s_sel[jj] = -1;
-      } else {
-        // the owner publishes the pivot row (per-element predicates keep a[][] in registers)
+      for (int i = 0; i < R; ++i) live[i] = live[i] && oi != i;
+      s_sel[j] = bq;
+    }
+    __syncthreads();
+    T pr[kLeaf];
 #pragma unroll
-        for (int i = 0; i < R; ++i) {
-          const bool mine = bq == tid + kPanelThreads * i;
+    for (int c = 0; c < kLeaf; ++c) pr[c] = s_pr[c];
+    const T rp = pr[0] != (T)0 ? calu_rcp(pr[0]) : (T)0;
 #pragma unroll
-          for (int c = 0; c < kLeaf; ++c)
-            if (mine) s_top[j * kLdS + c] = a[i][c];
-          if (mine) { live[i] = false; s_sel[j] = bq; }
-        }
-        __syncthreads();
-        const T piv = s_top[j * kLdS + j];
+    for (int i = 0; i < R; ++i) {
+      if (live[i]) {
+        const T l = a[i][0] * rp;
 #pragma unroll
-        for (int i = 0; i < R; ++i) {
-          const T l = (live[i] && piv != (T)0) ? a[i][j] / piv : (T)0;
-          if (live[i]) a[i][j] = l;
-#pragma unroll
-          for (int c = j + 1; c < kLeaf; ++c) a[i][c] -= l * s_top[j * kLdS + c];
-        }
+        for (int c = 1; c < kLeaf; ++c) a[i][c - 1] = a[i][c] - l * pr[c];
+        a[i][kLeaf - 1] = l;
       }
     }
   }
@@ -225,15 +227,16 @@ __device__ __forceinline__ void calu_wait(const int* flags, int n, int tag, Grid
 }
 
 template <typename T, int R>
-__global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int64_t lda, int m, int nb, int rows_per,
+__global__ void __launch_bounds__(kPanelThreads, 1) k_panel(T* __restrict__ P, int64_t lda, int m, int nb, int rows_per,
                                                          int F, CaluBufs<T> cb, int tag, int* __restrict__ ipiv,
                                                          int kglob, int* __restrict__ info, GridSync* gs) {
-  __shared__ T s_top[kLeaf * kLdS];  // pivot rows of the current elimination; U11 in step 4
-  __shared__ T s_bv[kPanelThreads / 32];
-  __shared__ int s_bq[kPanelThreads / 32];
+  __shared__ T s_top[kLeaf * kLdS];                // pivot rows of the current elimination
+  __shared__ __align__(16) T s_pr[kLeaf * kLeaf];  // rotated pivot row; in step 4 the rotated rows of U11
+  __shared__ __align__(16) unsigned s_key[kPanelThreads / 32];
   __shared__ int s_sel[kLeaf];
   __shared__ int s_meta[3 * kLeaf + 1];
   __shared__ int s_work[3 * kLeaf];
+  __shared__ T s_rinv[kLeaf];
   __shared__ int s_fail;
   const int cta = blockIdx.x, ncta = gridDim.x, tid = threadIdx.x;
   const int G = (ncta + F - 1) / F;
@@ -254,7 +257,7 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int6
     for (int c = 0; c < kLeaf; ++c) a[i][c] = (live[i] && c < nb) ? P[(int64_t)c * lda + r0 + q] : (T)0;
   }
   const int kl = min(nr, nb);
-  calu_elim<T, R>(a, live, kl, s_top, s_sel, s_bv, s_bq);
+  calu_elim<T, R>(a, live, kl, s_top, s_pr, s_sel, s_key);
   {
     T* cv = cb.cand + (size_t)cta * kLeaf * kLeaf;
     for (int idx = tid; idx < kLeaf * nb; idx += kPanelThreads) {
@@ -279,7 +282,7 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int6
 #pragma unroll
       for (int c = 0; c < kLeaf; ++c) a[i][c] = (live[i] && c < nb) ? __ldcg(cb.cand + (size_t)slot * kLeaf + c) : (T)0;
     }
-    calu_elim<T, R>(a, live, nb, s_top, s_sel, s_bv, s_bq);
+    calu_elim<T, R>(a, live, nb, s_top, s_pr, s_sel, s_key);
     T* lv = cb.lcand + (size_t)g * kLeaf * kLeaf;
     for (int idx = tid; idx < kLeaf * nb; idx += kPanelThreads) {
       const int j = idx / nb, c = idx % nb;
@@ -305,7 +308,7 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int6
 #pragma unroll
       for (int c = 0; c < kLeaf; ++c) a[i][c] = (live[i] && c < nb) ? __ldcg(cb.lcand + (size_t)q * kLeaf + c) : (T)0;
     }
-    calu_elim<T, R>(a, live, nb, s_top, s_sel, s_bv, s_bq);
+    calu_elim<T, R>(a, live, nb, s_top, s_pr, s_sel, s_key);
     for (int idx = tid; idx < nb * nb; idx += kPanelThreads) {
       const int j = idx / nb, c = idx % nb;
       cb.top[j * kLeaf + c] = s_top[j * kLdS + c];
@@ -351,11 +354,15 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int6
   // ---- 4. every CTA: its rows of the factored panel
   calu_wait(fb, 1, tag, gs, &s_fail);
   if (s_fail) return;
-  for (int idx = tid; idx < nb * nb; idx += kPanelThreads) {
-    const int i = idx / nb, c = idx % nb;
-    s_top[i * kLdS + c] = __ldcg(cb.top + i * kLeaf + c);
+  for (int idx = tid; idx < kLeaf * kLeaf; idx += kPanelThreads) {
+    const int i = idx / kLeaf, c = idx % kLeaf;  // s_pr[i][c] = U11[i][i + c], zero past the block
+    s_pr[idx] = (i < nb && i + c < nb) ? __ldcg(cb.top + i * kLeaf + i + c) : (T)0;
   }
   if (tid < 3 * kLeaf + 1) s_meta[tid] = __ldcg(cb.meta + tid);
+  if (tid < nb) {
+    const T u = __ldcg(cb.top + tid * kLeaf + tid);
+    s_rinv[tid] = u != (T)0 ? calu_rcp(u) : (T)0;
+  }
   __syncthreads();
   const int nd = s_meta[3 * kLeaf];
   for (int rr = tid; rr < nr; rr += kPanelThreads) {
@@ -373,20 +380,22 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(T* __restrict__ P, int6
 #pragma unroll
     for (int c = 0; c < kLeaf; ++c)
       x[c] = c < nb ? (src < 0 ? P[(int64_t)c * lda + r] : __ldcg(cb.orig + src * kLeaf + c)) : (T)0;
-    // x U11 = original row  ->  x <- row U11^-1, column by column
+    // x U11 = original row, right-looking with the same rotation as the elimination:
+    // before step kk, x[c] holds column (c + kk) mod kLeaf; the solved value enters at the end
+#pragma unroll 1
+    for (int kk = 0; kk < nb; ++kk) {
+      const T xk = x[0] * s_rinv[kk];
+      const T* ur = s_pr + kk * kLeaf;  // U11[kk][kk + c], zero past the block
 #pragma unroll
-    for (int k = 0; k < kLeaf; ++k) {
-      if (k < nb) {
-        T s = x[k];
-#pragma unroll
-        for (int i = 0; i < k; ++i) s -= x[i] * s_top[i * kLdS + k];
-        const T ukk = s_top[k * kLdS + k];
-        x[k] = ukk != (T)0 ? s / ukk : (T)0;
-      }
+      for (int c = 1; c < kLeaf; ++c) x[c - 1] = x[c] - xk * ur[c];
+      x[kLeaf - 1] = xk;
     }
+    // after nb steps column c sits in x[(c - nb) mod kLeaf]
 #pragma unroll
-    for (int c = 0; c < kLeaf; ++c)
-      if (c < nb) P[(int64_t)c * lda + r] = x[c];
+    for (int c = 0; c < kLeaf; ++c) {
+      const int col = (c + nb) & (kLeaf - 1);
+      if (col < nb) P[(int64_t)col * lda + r] = x[c];
+    }
   }
 }
 

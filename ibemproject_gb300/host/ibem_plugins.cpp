@@ -238,8 +238,9 @@ void postProcessorElastic3D_gb300::getFlux(Config& c_) {
   const ibem_material m = c.material();
   c.stress.alloc(6 * (size_t)c.nump);
   const double* E = c.U.p + 3 * (int64_t)c.NN;
-  check(ibem_e3d_field(c.d_pts.p, c.nump, c.d_cen.p, c.d_rad.p, c.num, &m, c.layout, E, c.d_nodes.p, c.NN, c.d_conn.p,
-                       c.NE, c.U.p, c.T.p, c.sig_inf.empty() ? nullptr : c.sig_inf.data(), c.stress.p, c.stream),
+  check(ibem_e3d_field_form(c.form, c.d_pts.p, c.nump, c.d_cen.p, c.d_rad.p, c.num, &m, c.layout, E, c.d_nodes.p,
+                            c.NN, c.d_conn.p, c.NE, c.U.p, c.T.p, c.sig_inf.empty() ? nullptr : c.sig_inf.data(),
+                            c.stress.p, c.stream),
         "getFlux");
   c.stress.download(c.s_pt, c.stream);
   if (!write_file) return;

@@ -192,6 +192,19 @@ ibem_status ibem_e3d_field(const double* points_dev, int nump, const double* cen
                            const double* T_dev, const double* sig_inf, double* stress_dev,
                            void* stream);
 
+/* ibem_e3d_field with a precision choice (no counterpart in the reference, which has one
+ * precision).  IBEM_SOLVE_FP64 is ibem_e3d_field.  IBEM_SOLVE_MIXED_IR runs the sphere
+ * sums of the 24-unknown layout in double-float arithmetic (pairs of FP32 numbers, about
+ * 48 significant bits; agrees with the FP64 sums to ~1e-12 of the strain), which GB300
+ * executes several times faster than FP64; the 60/78 layouts and the boundary part stay
+ * FP64.  ibem_e3d_run_host / ibem_e3d_run_dir use the form given to them here too. */
+ibem_status ibem_e3d_field_form(ibem_solver_form form, const double* points_dev, int nump,
+                                const double* centers_dev, const double* radius_dev, int num,
+                                const ibem_material* mat, int layout, const double* E_dev,
+                                const double* nodes_dev, int NN, const int* conn_dev, int NE,
+                                const double* U_dev, const double* T_dev, const double* sig_inf,
+                                double* stress_dev, void* stream);
+
 /* ---- whole pipeline on host buffers --------------------------------------- */
 
 /* One call per input case with host arrays, for FFI callers: assembly, ApplyBC,

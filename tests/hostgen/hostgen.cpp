@@ -123,3 +123,16 @@ extern "C" int hg_field24c(const double* x, double a, double E0, double nu0, dou
   sph_field24_contracted(x[0], x[1], x[2], a, mc, E, e);
   return 0;
 }
+
+// the double-float form of the same contraction: point p, sphere centre cen, radius a;
+// returns the strain (times the material constant) in e
+extern "C" int hg_field24df(const double* p, const double* cen, double a, double E0, double nu0, double E1,
+                            double nu1, const double* E, double* e) {
+  SphMat mc = sph_mat_init(E0, nu0, E1, nu1);
+  const ibem::SphDF sp = ibem::sph_df_make(cen, a, E);
+  const ibem::dfloat pd[3] = {ibem::df_make(p[0]), ibem::df_make(p[1]), ibem::df_make(p[2])};
+  ibem::dfloat acc[6] = {};
+  ibem::sph_field24_df(pd, sp, ibem::df_make(mc.tn1), ibem::df_make(mc.tn2), acc);
+  for (int t = 0; t < 6; ++t) e[t] = mc.kd * ibem::df_double(acc[t]);
+  return 0;
+}

@@ -194,3 +194,32 @@ def test_tensor_core_gemm(g, m, n, k):
     assert err < 2e-5 * scale, (err, scale)
     # and much better than a plain BF16 product would be
     assert err < 1e-4 * (A.double().T @ B.double().T).abs().max().item()
+
+
+@pytest.mark.gpu
+def test_field_double_float_vs_fp64_and_oracle(g, oracle_mod):
+    """Stresses of the 24-unknown layout: the FP64 sums match the oracle to 1e-11 and the
+    double-float sums of the mixed form (ibem_e3d_field_form) to 1e-10 (scaled), with
+    points inside, near and far from the spheres."""
+    from ibemproject_gb300 import cases
+    c = cases.farfield_case(num=60, r0=0.05, vf=0.15, grid=10, seed=3)
+    rng = np.random.default_rng(4)
+    E = rng.normal(size=(c.num, 24)) * 1e-3
+    E[:, 6:] /= 0.05   # order-1 eigenstrain per unit length
+    E = E.ravel()
+    m = g.material(c.E0, c.nu0, c.E1, c.nu1)
+    sig = np.ascontiguousarray(c.sig_inf, dtype=np.float64)
+    sigp = sig.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    keep = [dev(c.points), dev(c.centers), dev(c.radius), dev(E)]
+    pts, cen, rad, dE = keep
+    out = {}
+    for form in (g.SOLVE_FP64, g.SOLVE_MIXED_IR):
+        S = torch.zeros((c.nump, 6), dtype=torch.float64, device="cuda")
+        g.check(g.lib().ibem_e3d_field_form(form, P(pts), c.nump, P(cen), P(rad), c.num, ctypes.byref(m), 24, P(dE),
+                                            None, 0, None, 0, None, None, sigp, P(S), None))
+        torch.cuda.synchronize()
+        out[form] = S.cpu().numpy()
+    ref = oracle_mod.post(c, 24, E, sig_inf=c.sig_inf)
+    assert scaled_err(out[g.SOLVE_FP64], ref) < 1e-11
+    assert scaled_err(out[g.SOLVE_MIXED_IR], ref) < 1e-10
+    assert scaled_err(out[g.SOLVE_MIXED_IR], out[g.SOLVE_FP64]) < 1e-10
