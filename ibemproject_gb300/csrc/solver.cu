@@ -126,10 +126,12 @@ struct CaluBufs {
   T* top;      // [kLeaf][kLeaf] factored top block
   T* orig;     // [kLeaf][kLeaf] original values of the panel's first nb rows
   int* meta;   // [0, kLeaf) ipiv (panel-local), [kLeaf, 2 kLeaf) displaced rows,
-               // [2 kLeaf, 3 kLeaf) their source rows, [3 kLeaf] count
+               // [2 kLeaf, 3 kLeaf) their source rows, [3 kLeaf] count,
+               // [3 kLeaf + 1, 4 kLeaf + 1) the pivot rows in order (panel-local; a record)
   int* flags;  // [0, kCaluMaxCta) f0, [kCaluMaxCta, 2 kCaluMaxCta) f1, [2 kCaluMaxCta] fb
 };
 constexpr int kCaluMaxCta = 256;
+constexpr int kMetaLen = 4 * kLeaf + 1;
 
 constexpr int kPanelRmax = 4;  // rows per thread at most (1024 rows per elimination)
 
@@ -234,7 +236,7 @@ __global__ void __launch_bounds__(kPanelThreads, 1) k_panel(T* __restrict__ P, i
   __shared__ __align__(16) T s_pr[kLeaf * kLeaf];  // rotated pivot row; in step 4 the rotated rows of U11
   __shared__ __align__(16) unsigned s_key[kPanelThreads / 32];
   __shared__ int s_sel[kLeaf];
-  __shared__ int s_meta[3 * kLeaf + 1];
+  __shared__ int s_meta[kMetaLen];
   __shared__ int s_work[3 * kLeaf];
   __shared__ T s_rinv[kLeaf];
   __shared__ int s_fail;
@@ -326,6 +328,7 @@ __global__ void __launch_bounds__(kPanelThreads, 1) k_panel(T* __restrict__ P, i
         if (s_top[j * kLdS + j] == (T)0 && *info == 0) *info = kglob + j + 1;
         const int p = w < nb ? loc[w] : w;
         s_meta[j] = p;
+        s_meta[3 * kLeaf + 1 + j] = w;
         const int c = content[j];
         if (p != j) {
           if (p < nb) {
@@ -346,7 +349,7 @@ __global__ void __launch_bounds__(kPanelThreads, 1) k_panel(T* __restrict__ P, i
       s_meta[3 * kLeaf] = nd;
     }
     __syncthreads();
-    for (int i = tid; i < 3 * kLeaf + 1; i += kPanelThreads) cb.meta[i] = s_meta[i];
+    for (int i = tid; i < kMetaLen; i += kPanelThreads) cb.meta[i] = s_meta[i];
     __threadfence();
     __syncthreads();
     if (tid == 0) st_release_s32(fb, tag);
@@ -358,7 +361,7 @@ __global__ void __launch_bounds__(kPanelThreads, 1) k_panel(T* __restrict__ P, i
     const int i = idx / kLeaf, c = idx % kLeaf;  // s_pr[i][c] = U11[i][i + c], zero past the block
     s_pr[idx] = (i < nb && i + c < nb) ? __ldcg(cb.top + i * kLeaf + i + c) : (T)0;
   }
-  if (tid < 3 * kLeaf + 1) s_meta[tid] = __ldcg(cb.meta + tid);
+  if (tid < kMetaLen) s_meta[tid] = __ldcg(cb.meta + tid);
   if (tid < nb) {
     const T u = __ldcg(cb.top + tid * kLeaf + tid);
     s_rinv[tid] = u != (T)0 ? calu_rcp(u) : (T)0;
@@ -404,7 +407,7 @@ constexpr size_t calu_a256(size_t v) { return (v + 255) / 256 * 256; }
 template <typename T>
 constexpr size_t calu_bytes(int ncta) {
   return 2 * calu_a256(sizeof(T) * (size_t)ncta * kLeaf * kLeaf) + 2 * calu_a256(sizeof(int) * (size_t)ncta * kLeaf) +
-         2 * calu_a256(sizeof(T) * kLeaf * kLeaf) + calu_a256(sizeof(int) * (3 * kLeaf + 1)) +
+         2 * calu_a256(sizeof(T) * kLeaf * kLeaf) + calu_a256(sizeof(int) * kMetaLen) +
          calu_a256(sizeof(int) * (2 * kCaluMaxCta + 1));
 }
 template <typename T>
@@ -418,7 +421,7 @@ CaluBufs<T> calu_carve(unsigned char* base, int ncta) {
   b.lidx = reinterpret_cast<int*>(take(sizeof(int) * (size_t)ncta * kLeaf));
   b.top = reinterpret_cast<T*>(take(sizeof(T) * kLeaf * kLeaf));
   b.orig = reinterpret_cast<T*>(take(sizeof(T) * kLeaf * kLeaf));
-  b.meta = reinterpret_cast<int*>(take(sizeof(int) * (3 * kLeaf + 1)));
+  b.meta = reinterpret_cast<int*>(take(sizeof(int) * kMetaLen));
   b.flags = reinterpret_cast<int*>(take(sizeof(int) * (2 * kCaluMaxCta + 1)));
   return b;
 }
@@ -470,29 +473,56 @@ __global__ void __launch_bounds__(64) k_trsm_small(const T* __restrict__ L, int6
   }
 }
 
-// Same solve with the triangle size fixed at compile time: the column lives in registers,
-// the loops are fully unrolled (no dependent shared-memory round trips).
+// Same solve with the triangle size fixed at compile time: 128 columns per CTA are staged
+// through shared memory with coalesced loads and stores, each thread solves one column in
+// registers with fully unrolled loops.
+constexpr int kTrsmCols = 128;
 template <typename T, int NB>
-__global__ void __launch_bounds__(128) k_trsm_small_fixed(const T* __restrict__ L, int64_t ldl, T* __restrict__ B,
-                                                          int64_t ldb, int64_t n2) {
-  __shared__ T sL[NB * NB];  // [i][k] = L(k, i) for k > i
-  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+__global__ void __launch_bounds__(kTrsmCols) k_trsm_small_fixed(const T* __restrict__ L, int64_t ldl,
+                                                                T* __restrict__ B, int64_t ldb, int64_t n2) {
+  extern __shared__ __align__(16) unsigned char trsm_smem[];
+  T* sL = reinterpret_cast<T*>(trsm_smem);   // [i][k] = L(k, i) for k > i
+  T* sB = sL + NB * NB;                      // [r][cc], stride kTrsmCols + 1
+  const int64_t c0 = blockIdx.x * (int64_t)kTrsmCols;
+  for (int idx = threadIdx.x; idx < NB * NB; idx += kTrsmCols) {
     const int k = idx % NB, i = idx / NB;
     sL[i * NB + k] = L[(int64_t)i * ldl + k];
   }
+  // loads in batches of 16 per thread, each batch issued before its shared-memory stores
+#pragma unroll 1
+  for (int q0 = 0; q0 < NB; q0 += 16) {
+    T v[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int idx = threadIdx.x + (q0 + q) * kTrsmCols, r = idx % NB, cc = idx / NB;
+      v[q] = c0 + cc < n2 ? B[(c0 + cc) * ldb + r] : (T)0;
+    }
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int idx = threadIdx.x + (q0 + q) * kTrsmCols, r = idx % NB, cc = idx / NB;
+      sB[r * (kTrsmCols + 1) + cc] = v[q];
+    }
+  }
   __syncthreads();
-  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= n2) return;
-  T* b = B + c * ldb;
   T x[NB];
 #pragma unroll
-  for (int i = 0; i < NB; ++i) x[i] = b[i];
+  for (int i = 0; i < NB; ++i) x[i] = sB[i * (kTrsmCols + 1) + threadIdx.x];
 #pragma unroll
   for (int i = 0; i < NB; ++i)
 #pragma unroll
     for (int k = i + 1; k < NB; ++k) x[k] -= sL[i * NB + k] * x[i];
 #pragma unroll
-  for (int i = 0; i < NB; ++i) b[i] = x[i];
+  for (int i = 0; i < NB; ++i) sB[i * (kTrsmCols + 1) + threadIdx.x] = x[i];
+  __syncthreads();
+#pragma unroll 4
+  for (int q = 0; q < NB; ++q) {
+    const int idx = threadIdx.x + q * kTrsmCols, r = idx % NB, cc = idx / NB;
+    if (c0 + cc < n2) B[(c0 + cc) * ldb + r] = sB[r * (kTrsmCols + 1) + cc];
+  }
+}
+template <typename T, int NB>
+constexpr size_t trsm_fixed_smem() {
+  return sizeof(T) * (NB * NB + NB * (kTrsmCols + 1));
 }
 
 // ---------------------------------------------------------------- SIMT GEMM  C -= A B
@@ -534,13 +564,83 @@ __global__ void __launch_bounds__(256) k_gemm_sub(int64_t m, int64_t n, int64_t 
     }
     __syncthreads();
   }
+  // all sixteen loads of C before any store: independent, so they overlap
+  T cv[4][4];
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
       const int64_t gi = i0 + tx + 16 * a, gj = j0 + ty + 16 * b;
-      if (gi < m && gj < n) C[gj * ldc + gi] -= acc[a][b];
+      cv[a][b] = (gi < m && gj < n) ? C[gj * ldc + gi] : (T)0;
     }
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int64_t gi = i0 + tx + 16 * a, gj = j0 + ty + 16 * b;
+      if (gi < m && gj < n) C[gj * ldc + gi] = cv[a][b] - acc[a][b];
+    }
+}
+
+// Small-k variant (k <= kSmallK): the whole A (64 x k) and B (k x 64) panels are staged in
+// shared memory with one barrier, instead of k / 16 load-barrier-compute rounds; this is
+// the shape of every SIMT update in the recursive factorisation (k = 32 .. 96).
+constexpr int kSmallK = 128;
+template <typename T>
+__global__ void __launch_bounds__(256) k_gemm_sub_smallk(int64_t m, int64_t n, int k, const T* __restrict__ A,
+                                                         int64_t lda, const T* __restrict__ B, int64_t ldb,
+                                                         T* __restrict__ C, int64_t ldc) {
+  extern __shared__ __align__(16) unsigned char gs_smem[];
+  T* sA = reinterpret_cast<T*>(gs_smem);  // [kk][r], stride 65
+  T* sB = sA + kSmallK * 65;              // [kk][c], stride 65
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int64_t i0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
+#pragma unroll 8
+  for (int idx = threadIdx.x; idx < 64 * k; idx += 256) {
+    const int r = idx % 64, kk = idx / 64;
+    const int64_t gi = i0 + r;
+    sA[kk * 65 + r] = gi < m ? A[kk * lda + gi] : (T)0;
+    const int rk = idx % k, cj = idx / k;
+    const int64_t gj = j0 + cj;
+    sB[rk * 65 + cj] = gj < n ? B[gj * ldb + rk] : (T)0;
+  }
+  __syncthreads();
+  T acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0;
+#pragma unroll 4
+  for (int t = 0; t < k; ++t) {
+    T av[4], bv[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) av[a] = sA[t * 65 + tx + 16 * a];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) bv[b] = sB[t * 65 + ty + 16 * b];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
+  }
+  T cv[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int64_t gi = i0 + tx + 16 * a, gj = j0 + ty + 16 * b;
+      cv[a][b] = (gi < m && gj < n) ? C[gj * ldc + gi] : (T)0;
+    }
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int64_t gi = i0 + tx + 16 * a, gj = j0 + ty + 16 * b;
+      if (gi < m && gj < n) C[gj * ldc + gi] = cv[a][b] - acc[a][b];
+    }
+}
+template <typename T>
+constexpr size_t gemm_smallk_smem() {
+  return sizeof(T) * 2 * kSmallK * 65;
 }
 
 // ---------------------------------------------------------------- vectors
@@ -760,6 +860,15 @@ template <typename T>
 cudaError_t set_solver_smem_attrs() {
   cudaError_t e = cudaFuncSetAttribute((const void*)k_trsm_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(2 * 64 * 65 * sizeof(T)));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute((const void*)k_gemm_sub_smallk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)gemm_smallk_smem<T>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute((const void*)k_trsm_small_fixed<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)trsm_fixed_smem<T, 32>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute((const void*)k_trsm_small_fixed<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)trsm_fixed_smem<T, 64>());
   const int inv = (int)(sizeof(T) * (kTrsvB * (kTrsvB + 1) + kTrsvB));
   const int ps = (int)trsv_persist_smem<T>();
   if (e == cudaSuccess)
@@ -848,7 +957,11 @@ ibem_status gemm_sub<double>(int64_t m, int64_t n, int64_t k, const double* A, i
   if (m <= 0 || n <= 0 || k <= 0) return IBEM_OK;
   ProfScope ps(PROF_GEMM_SIMT, st, 2.0 * m * n * k);
   dim3 grid((unsigned)((m + 63) / 64), (unsigned)((n + 63) / 64));
-  ::ibem::count_launch(), k_gemm_sub<double><<<grid, 256, 0, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
+  if (k <= kSmallK)
+    ::ibem::count_launch(), k_gemm_sub_smallk<double><<<grid, 256, gemm_smallk_smem<double>(), st>>>(m, n, (int)k, A, lda, B,
+                                                                                         ldb, C, ldc);
+  else
+    ::ibem::count_launch(), k_gemm_sub<double><<<grid, 256, 0, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
   IBEM_LAUNCH_CHECK("gemm f64");
   return IBEM_OK;
 }
@@ -862,7 +975,11 @@ ibem_status gemm_sub<float>(int64_t m, int64_t n, int64_t k, const float* A, int
     return gemm_sub_f32_tc(m, n, k, A, lda, B, ldb, C, ldc, w.gemm_ws, w.gemm_ws_bytes, w.gemm_err, st);
   ProfScope ps(PROF_GEMM_SIMT, st, 2.0 * m * n * k);
   dim3 grid((unsigned)((m + 63) / 64), (unsigned)((n + 63) / 64));
-  ::ibem::count_launch(), k_gemm_sub<float><<<grid, 256, 0, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
+  if (k <= kSmallK)
+    ::ibem::count_launch(), k_gemm_sub_smallk<float><<<grid, 256, gemm_smallk_smem<float>(), st>>>(m, n, (int)k, A, lda, B,
+                                                                                         ldb, C, ldc);
+  else
+    ::ibem::count_launch(), k_gemm_sub<float><<<grid, 256, 0, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
   IBEM_LAUNCH_CHECK("gemm f32");
   return IBEM_OK;
 }
@@ -875,9 +992,11 @@ static ibem_status trsm(const T* L, int64_t ldl, int64_t n1, T* B, int64_t ldb, 
   if (n1 <= 64) {
     ProfScope ps(PROF_TRSM_SMALL, st);
     if (n1 == 32)
-      ::ibem::count_launch(), k_trsm_small_fixed<T, 32><<<(unsigned)((n2 + 127) / 128), 128, 0, st>>>(L, ldl, B, ldb, n2);
+      ::ibem::count_launch(), k_trsm_small_fixed<T, 32><<<(unsigned)((n2 + kTrsmCols - 1) / kTrsmCols), kTrsmCols,
+                                                          trsm_fixed_smem<T, 32>(), st>>>(L, ldl, B, ldb, n2);
     else if (n1 == 64 && sizeof(T) == sizeof(float))
-      ::ibem::count_launch(), k_trsm_small_fixed<T, 64><<<(unsigned)((n2 + 127) / 128), 128, 0, st>>>(L, ldl, B, ldb, n2);
+      ::ibem::count_launch(), k_trsm_small_fixed<T, 64><<<(unsigned)((n2 + kTrsmCols - 1) / kTrsmCols), kTrsmCols,
+                                                          trsm_fixed_smem<T, 64>(), st>>>(L, ldl, B, ldb, n2);
     else
       ::ibem::count_launch(), k_trsm_small<T><<<(unsigned)((n2 + 63) / 64), 64, 2 * 64 * 65 * sizeof(T), st>>>(
           L, ldl, (int)n1, B, ldb, n2);
