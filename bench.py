@@ -127,11 +127,17 @@ def measured_peaks():
     return 6800.0, 1700.0, "fallback"
 
 
+# DRAM bytes (read + write) per launch of k_umma_bf16x3 over every launch of this workload,
+# from one ncu capture of the bench command (profiles/k_umma_bf16x3_bench2000_traffic.md)
+UMMA_TRAFFIC_BYTES_PER_LAUNCH = 242.7e6
+
+
 def roofline(prof):
-    """Roofline of the tensor-core GEMM (the trailing updates of the factorisation):
-    achieved = algorithmic flops (2 m n k per launch, the FP32 GEMM's work; split-BF16 issues
-    3 MMAs per product on top of that) / its event-timed duration, against the measured
-    sustained dense BF16 rate."""
+    """Roofline of the tensor-core GEMM (the trailing updates of the factorisation, the
+    largest kernel of the step): achieved = algorithmic flops (2 m n k per launch, the FP32
+    GEMM's work) / its event-timed duration, against the measured sustained dense BF16 rate.
+    The split-BF16 scheme issues 3 BF16 MMAs per product, so frac_of_issued (3x) is the
+    fraction of the tensor pipe's rate actually used."""
     hbm, tf, src = measured_peaks()
     g = prof.get("gemm_tc")
     if not g or g["ms"] <= 0:
@@ -142,7 +148,9 @@ def roofline(prof):
             "launches": g["launches"], "avg_launch_ms": g["ms"] / max(1, g["launches"]),
             "flops_per_launch": g["flops"] / max(1, g["launches"]),
             "tensor_flops_issued_per_launch": 3 * g["flops"] / max(1, g["launches"]),
-            "traffic": None}
+            "frac_of_issued": 3 * achieved / tf,
+            "traffic": UMMA_TRAFFIC_BYTES_PER_LAUNCH, "traffic_unit": "bytes per launch (ncu dram read+write)",
+            "traffic_source": "profiles/k_umma_bf16x3_bench2000_traffic.md"}
 
 
 # ------------------------------------------------------------------ clocks
@@ -188,6 +196,19 @@ class Clocks:
         reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ replicas
+def job_seconds_per_solution(ms_local, world, device=None):
+    """Whole-job seconds per solution of N replicas: every rank solved one realisation in
+    its own timed steps; the job's time is the slowest rank's, and N solutions came out of
+    it (weak scaling).  Single process: ms_local / 1e3."""
+    if world <= 1:
+        return ms_local / 1e3
+    import torch
+    t = torch.tensor([float(ms_local)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item()) / 1e3 / world
 
 
 # ------------------------------------------------------------------ ours
@@ -264,10 +285,7 @@ def run_ours(args, rank, world):
         stage_ms["solve"].append(ev[1].elapsed_time(ev[2]))
         stage_ms["field"].append(ev[2].elapsed_time(ev[3]))
     rep_mixed = (rep.backward_error, rep.iterations, rep.t_factor_ms, rep.t_solve_ms)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = job_seconds_per_solution(ms, world, dev) * 1e3
 
     # plain FP64 form once on the same microstructure, and the difference to it
     plain = None
