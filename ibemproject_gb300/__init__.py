@@ -41,6 +41,25 @@ class SolveReport(ctypes.Structure):
                 ("t_solve_ms", ctypes.c_double)]
 
 
+class Batch(ctypes.Structure):
+    _fields_ = [("nseg", ctypes.c_int), ("seg_begin", ctypes.POINTER(ctypes.c_int)),
+                ("centers_dev", ctypes.c_void_p), ("radius_dev", ctypes.c_void_p),
+                ("mats", ctypes.POINTER(Material))]
+
+
+class MfOptions(ctypes.Structure):
+    _fields_ = [("restart", ctypes.c_int), ("max_cycles", ctypes.c_int), ("max_outer", ctypes.c_int),
+                ("tol", ctypes.c_double), ("inner_tol", ctypes.c_double)]
+
+
+class MfReport(ctypes.Structure):
+    _fields_ = [("rel_residual", ctypes.c_double), ("outer", ctypes.c_int), ("inner", ctypes.c_int),
+                ("t_setup_ms", ctypes.c_double), ("t_solve_ms", ctypes.c_double)]
+
+
+PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1
+
+
 class IbemError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"ibem status {status}: {msg}")
@@ -76,6 +95,20 @@ SIGNATURES = {
                                  _int, _c_dp, _c_dp, _int, _c_dp, _c_dp, _dbl, _c_dp, _c_dp,
                                  ctypes.POINTER(SolveReport)]),
     "ibem_e3d_run_dir": (_int, [ctypes.c_char_p, _int, _int, _dbl, ctypes.POINTER(SolveReport)]),
+    "ibem_e3d_mf_matvec": (_int, [ctypes.POINTER(Batch), _int, _vp, _vp, _vp]),
+    "ibem_e3d_mf_solve": (_int, [ctypes.POINTER(Batch), _vp, _vp, _int, _vp, ctypes.POINTER(MfOptions),
+                                 ctypes.POINTER(MfReport), _vp]),
+    "ibem_e3d_batch_farfield_rhs": (_int, [ctypes.POINTER(Batch), _c_dp, _vp, _vp]),
+    "ibem_e3d_effective_modulus": (_int, [ctypes.POINTER(Batch), _vp, _c_dp, _c_dp, _c_dp, _c_dp, _vp]),
+    "ibem_gnn_param_count": (_i64, []),
+    "ibem_gnn_init_params": (_int, [_vp, ctypes.c_uint64, _vp]),
+    "ibem_gnn_prepare": (_int, [ctypes.POINTER(Batch), _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "ibem_gnn_loss_grad": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _c_dp, _vp, _vp]),
+    "ibem_gnn_edge_weights": (_int, [_int, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "ibem_gnn_adamw": (_int, [_i64, _vp, _vp, _vp, _vp, _int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                              ctypes.c_float, ctypes.c_float, _vp]),
+    "ibem_gnn_train": (_int, [ctypes.POINTER(Batch), _int, _vp, _vp, _vp, _int, ctypes.c_float, ctypes.c_float,
+                              _c_dp, _vp]),
 }
 
 _lib = None

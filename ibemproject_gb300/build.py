@@ -18,7 +18,8 @@ LIB = os.path.join(HERE, "libibem_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = [
     "csrc/sphere24.cu", "csrc/sphere60.cu", "csrc/sphere78.cu", "csrc/bem.cu",
-    "csrc/solver.cu", "csrc/gemm_tc.cu", "csrc/capi.cu", "csrc/prof.cu", "host/ibem_plugins.cpp",
+    "csrc/solver.cu", "csrc/gemm_tc.cu", "csrc/capi.cu", "csrc/prof.cu", "csrc/mf.cu", "csrc/gnn.cu",
+    "host/ibem_plugins.cpp",
 ]
 
 

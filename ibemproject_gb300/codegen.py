@@ -34,6 +34,7 @@ from __future__ import annotations
 import itertools
 import math
 import os
+import re
 from collections import OrderedDict
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -649,6 +650,47 @@ IBEM_HD inline SphMat sph_mat_init(double E0, double nu0, double E1, double nu1)
 """
 
 
+_F32_LIT = re.compile(r"(?<![\w.])(\d+\.\d*(?:[eE][+-]?\d+)?)(?![\w.])")
+
+F32_HEAD = """// GENERATED by ibemproject_gb300/codegen.py -- do not edit by hand.
+// FP32 variant of the layout-24 sphere blocks for the matrix-free solver, which calls
+// them in coordinates scaled by the source radius (a = 1), so that every intermediate is
+// O(1) in single precision.  Same derivation as gen_sphere24.cuh.
+#pragma once
+#include "gen_sphere_common.cuh"
+
+// Dimensionless material constants of the FP32 blocks (sph_matf_init: SphMat / mu0).
+struct SphMatF {
+  float kmu, klam, tn1, tn2;  // as SphMat, contrast terms divided by mu0
+  float lam0, mu0;            // C0 / mu0 (self term): lam0 / mu0 and 1
+};
+
+IBEM_HD inline SphMatF sph_matf_init(const SphMat& m) {
+  SphMatF f;
+  const double s = 1.0 / m.mu0;
+  f.kmu = (float)(m.kmu * s);
+  f.klam = (float)(m.klam * s);
+  f.tn1 = (float)m.tn1;
+  f.tn2 = (float)m.tn2;
+  f.lam0 = (float)(m.lam0 * s);
+  f.mu0 = 1.0f;
+  return f;
+}
+"""
+
+
+def to_f32(src: str, old_name: str, new_name: str) -> str:
+    """Single-precision copy of a generated block function: the same straight-line
+    arithmetic with float operands and literals."""
+    out = src.replace(old_name + "(", new_name + "(")
+    out = out.replace("const SphMat& mc", "const SphMatF& mc")
+    out = out.replace("const double", "const float").replace("double Jv[", "float Jv[")
+    out = out.replace("double pw", "float pw")
+    out = out.replace("sqrt(", "sqrtf(").replace("IBEM_PI", "3.14159265358979f")
+    out = _F32_LIT.sub(lambda m: m.group(1) + "f", out)
+    return out
+
+
 def generate(out_dir: str | None = None) -> dict:
     out_dir = out_dir or os.path.join(HERE, "csrc")
     files = {}
@@ -665,6 +707,13 @@ def generate(out_dir: str | None = None) -> dict:
     parts.append(gen_node_function("sph_node24", 24))
     parts.append(gen_self_function("sph_self24", 24))
     files["gen_sphere24.cuh"] = "\n\n".join(parts) + "\n"
+    fparts = [F32_HEAD]
+    for co in range(2):
+        for ro in range(2):
+            nm = f"sph_block24_c{co}_r{ro}"
+            fparts.append(to_f32(parts[1 + 2 * co + ro], nm, nm.replace("block24", "block24f")))
+    fparts.append(to_f32(gen_self_function("sph_self24", 24), "sph_self24", "sph_self24f"))
+    files["gen_sphere24_f32.cuh"] = "\n\n".join(fparts) + "\n"
     for lay in (78, 60):
         U = units(lay)
         parts = [FILE_HEAD]

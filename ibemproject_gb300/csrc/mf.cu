@@ -1,0 +1,926 @@
+// Matrix-free solves of the layout-24 sphere systems, one realisation or a batch of them.
+//
+// The pair blocks that ibem_e3d_pair_blocks stores (integratorElastic3D.cpp:341-567,
+// orders 0 and 1) are evaluated inside the products instead:
+//   k_mf_apply_f32  As x in FP32 on the scaled system (mf.h), the GMRES operator;
+//   k_mf_apply_f64  A x in FP64, physical units, the refinement residual b - A x.
+// One thread per target particle s, 128 consecutive targets of one realisation per CTA;
+// the CTA's source particles h (a slice of the realisation, gridDim.y slices) are staged
+// through shared memory in chunks with their coefficients, and every thread sums the
+// products of the generated 24 x 24 blocks with them in registers (the generated code
+// calls the sink with constant indices, so the sums stay in registers).  Slices add
+// their partial sums atomically.
+//
+// Solver: FP64 iterative refinement x += Dc d; each correction d solves As d = Dr r with a
+// restarted FP32 GMRES right-preconditioned by a block-diagonal P (block-Jacobi or learned),
+// all realisations of a batch in lock step (per-realisation Arnoldi: segmented dot
+// products, Hessenberg updates and Givens rotations on the device, one thread per
+// realisation), stopping each realisation on its own residual estimate.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gen_sphere24.cuh"
+#include "mf.h"
+#include "prof.h"
+
+namespace ibem {
+namespace {
+
+constexpr int kMfThreads = 128;
+constexpr int kMfChunk = 32;
+
+// sink of a generated block: acc[r] += v * x[c] (r, c compile-time constants after inlining)
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+template <class T>
+struct MvSink {
+  T (&acc)[kMfNu];
+  const T* __restrict__ xs;
+  __device__ __forceinline__ void operator()(int r, int c, T v) const { acc[r] = fma_t(v, xs[c], acc[r]); }
+};
+
+__global__ void __launch_bounds__(kMfThreads)
+    k_mf_apply_f32(const MfTile* __restrict__ tiles, const int* __restrict__ seg_begin,
+                   const float4* __restrict__ gh, const float4* __restrict__ gl,
+                   const SphMatF* __restrict__ mats, const float* __restrict__ x, float* __restrict__ y) {
+  __shared__ float4 sgh[kMfChunk], sgl[kMfChunk];
+  __shared__ float sx[kMfChunk * kMfNu];
+  const MfTile t = tiles[blockIdx.x];
+  const int hb0 = seg_begin[t.seg], he0 = seg_begin[t.seg + 1];
+  const int per = (he0 - hb0 + gridDim.y - 1) / gridDim.y;
+  const int hb = hb0 + blockIdx.y * per, he = min(he0, hb + per);
+  if (hb >= he) return;
+  const int s = t.s0 + threadIdx.x;
+  const bool act = threadIdx.x < t.ns;
+  const SphMatF mc = mats[t.seg];
+  const float4 ph = act ? gh[s] : make_float4(0.f, 0.f, 0.f, 1.f);
+  const float4 pl = act ? gl[s] : make_float4(0.f, 0.f, 0.f, 1.f);
+  float acc[kMfNu];
+#pragma unroll
+  for (int r = 0; r < kMfNu; ++r) acc[r] = 0.f;
+  for (int h0 = hb; h0 < he; h0 += kMfChunk) {
+    const int nh = min(kMfChunk, he - h0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nh; i += blockDim.x) {
+      sgh[i] = gh[h0 + i];
+      sgl[i] = gl[h0 + i];
+    }
+    for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x) sx[i] = x[(int64_t)kMfNu * h0 + i];
+    __syncthreads();
+    if (!act) continue;
+    for (int hh = 0; hh < nh; ++hh) {
+      const float4 qh = sgh[hh], ql = sgl[hh];
+      const float ia = ql.w;
+      // offset from the source centre in units of its radius (hi/lo parts keep ~48 bits)
+      const float x0 = ((ph.x - qh.x) + (pl.x - ql.x)) * ia;
+      const float x1 = ((ph.y - qh.y) + (pl.y - ql.y)) * ia;
+      const float x2 = ((ph.z - qh.z) + (pl.z - ql.z)) * ia;
+      const float* xs = sx + kMfNu * hh;
+      MvSink<float> s0{acc, xs};
+      sph_block24f_c0_r0(x0, x1, x2, 1.f, mc, s0);
+      sph_block24f_c1_r0(x0, x1, x2, 1.f, mc, s0);
+      float t1[kMfNu];
+#pragma unroll
+      for (int r = 6; r < kMfNu; ++r) t1[r] = 0.f;
+      MvSink<float> s1{t1, xs};
+      sph_block24f_c0_r1(x0, x1, x2, 1.f, mc, s1);
+      sph_block24f_c1_r1(x0, x1, x2, 1.f, mc, s1);
+      const float ratio = ph.w * ia;  // a_s / a_h on rows of order 1
+#pragma unroll
+      for (int r = 6; r < kMfNu; ++r) acc[r] = fmaf(ratio, t1[r], acc[r]);
+      if (h0 + hh == s) sph_self24f(mc, s0);
+    }
+  }
+  if (!act) return;
+  float* o = y + (int64_t)kMfNu * s;
+#pragma unroll
+  for (int r = 0; r < kMfNu; ++r) atomicAdd(o + r, acc[r]);
+}
+
+__global__ void __launch_bounds__(kMfThreads)
+    k_mf_apply_f64(const MfTile* __restrict__ tiles, const int* __restrict__ seg_begin,
+                   const double* __restrict__ cen, const double* __restrict__ rad,
+                   const SphMat* __restrict__ mats, const double* __restrict__ x, double* __restrict__ y) {
+  __shared__ double sc[kMfChunk * 4];
+  __shared__ double sx[kMfChunk * kMfNu];
+  const MfTile t = tiles[blockIdx.x];
+  const int hb0 = seg_begin[t.seg], he0 = seg_begin[t.seg + 1];
+  const int per = (he0 - hb0 + gridDim.y - 1) / gridDim.y;
+  const int hb = hb0 + blockIdx.y * per, he = min(he0, hb + per);
+  if (hb >= he) return;
+  const int s = t.s0 + threadIdx.x;
+  const bool act = threadIdx.x < t.ns;
+  const SphMat mc = mats[t.seg];
+  double p0 = 0, p1 = 0, p2 = 0;
+  if (act) {
+    p0 = cen[3 * (int64_t)s];
+    p1 = cen[3 * (int64_t)s + 1];
+    p2 = cen[3 * (int64_t)s + 2];
+  }
+  double acc[kMfNu];
+#pragma unroll
+  for (int r = 0; r < kMfNu; ++r) acc[r] = 0.0;
+  for (int h0 = hb; h0 < he; h0 += kMfChunk) {
+    const int nh = min(kMfChunk, he - h0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nh; i += blockDim.x) {
+      sc[4 * i] = cen[3 * (int64_t)(h0 + i)];
+      sc[4 * i + 1] = cen[3 * (int64_t)(h0 + i) + 1];
+      sc[4 * i + 2] = cen[3 * (int64_t)(h0 + i) + 2];
+      sc[4 * i + 3] = rad[h0 + i];
+    }
+    for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x) sx[i] = x[(int64_t)kMfNu * h0 + i];
+    __syncthreads();
+    if (!act) continue;
+    for (int hh = 0; hh < nh; ++hh) {
+      const double x0 = p0 - sc[4 * hh], x1 = p1 - sc[4 * hh + 1], x2 = p2 - sc[4 * hh + 2];
+      const double a = sc[4 * hh + 3];
+      MvSink<double> sk{acc, sx + kMfNu * hh};
+      sph_block24_c0_r0(x0, x1, x2, a, mc, sk);
+      sph_block24_c1_r0(x0, x1, x2, a, mc, sk);
+      sph_block24_c0_r1(x0, x1, x2, a, mc, sk);
+      sph_block24_c1_r1(x0, x1, x2, a, mc, sk);
+      if (h0 + hh == s) sph_self24(mc, sk);
+    }
+  }
+  if (!act) return;
+  double* o = y + (int64_t)kMfNu * s;
+#pragma unroll
+  for (int r = 0; r < kMfNu; ++r) atomicAdd(o + r, acc[r]);
+}
+
+// Geometry in the FP32 layout, scalings, segment of every particle.
+__global__ void k_mf_prep(int num, const double* __restrict__ cen, const double* __restrict__ rad,
+                          const int* __restrict__ seg_of, const SphMat* __restrict__ mats, float4* __restrict__ gh,
+                          float4* __restrict__ gl, double* __restrict__ dr, double* __restrict__ dc) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= num) return;
+  float hi[3], lo[3];
+  for (int k = 0; k < 3; ++k) {
+    const double c = cen[3 * (int64_t)p + k];
+    hi[k] = (float)c;
+    lo[k] = (float)(c - (double)hi[k]);
+  }
+  const double a = rad[p];
+  gh[p] = make_float4(hi[0], hi[1], hi[2], (float)a);
+  gl[p] = make_float4(lo[0], lo[1], lo[2], (float)(1.0 / a));
+  const double imu = 1.0 / mats[seg_of[p]].mu0;
+  for (int r = 0; r < kMfNu; ++r) {
+    dr[(int64_t)kMfNu * p + r] = (r >= 6 ? a : 1.0) * imu;
+    dc[(int64_t)kMfNu * p + r] = r >= 6 ? 1.0 / a : 1.0;
+  }
+}
+
+// Scaled diagonal block As[p,p] (FP64, x = 0, unit sphere, moduli / mu0) inverted by
+// Gauss-Jordan with partial pivoting; one CTA of 32 threads per particle.
+__global__ void __launch_bounds__(32) k_block_jacobi(const int* __restrict__ seg_of, const SphMat* __restrict__ mats,
+                                                     float* __restrict__ P) {
+  __shared__ double M[kMfNu][2 * kMfNu + 1];
+  const int p = blockIdx.x;
+  const int t = threadIdx.x;
+  for (int i = t; i < kMfNu * 2 * kMfNu; i += 32) {
+    const int r = i / (2 * kMfNu), c = i % (2 * kMfNu);
+    M[r][c] = (c >= kMfNu && c - kMfNu == r) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  if (t == 0) {
+    SphMat mc = mats[seg_of[p]];
+    const double s = 1.0 / mc.mu0;
+    mc.kmu *= s;
+    mc.klam *= s;
+    mc.lam0 *= s;
+    mc.mu0 = 1.0;
+    struct Put {
+      double (*M)[2 * kMfNu + 1];
+      __device__ void operator()(int r, int c, double v) const { M[r][c] += v; }
+    } put{M};
+    sph_block24_c0_r0(0.0, 0.0, 0.0, 1.0, mc, put);
+    sph_block24_c1_r0(0.0, 0.0, 0.0, 1.0, mc, put);
+    sph_block24_c0_r1(0.0, 0.0, 0.0, 1.0, mc, put);
+    sph_block24_c1_r1(0.0, 0.0, 0.0, 1.0, mc, put);
+    sph_self24(mc, put);
+  }
+  __syncthreads();
+  __shared__ int piv;
+  __shared__ double f[kMfNu];
+  for (int k = 0; k < kMfNu; ++k) {
+    if (t == 0) {
+      int best = k;
+      for (int r = k + 1; r < kMfNu; ++r)
+        if (fabs(M[r][k]) > fabs(M[best][k])) best = r;
+      piv = best;
+    }
+    __syncthreads();
+    const int pr = piv;
+    if (pr != k)
+      for (int c = t; c < 2 * kMfNu; c += 32) {
+        const double v = M[k][c];
+        M[k][c] = M[pr][c];
+        M[pr][c] = v;
+      }
+    __syncthreads();
+    const double d = M[k][k];
+    const double id = d != 0.0 ? 1.0 / d : 0.0;
+    __syncthreads();
+    for (int c = t; c < 2 * kMfNu; c += 32) M[k][c] *= id;
+    if (t < kMfNu) f[t] = M[t][k];  // column k of the other rows (row k is being scaled, unused)
+    __syncthreads();
+    for (int i = t; i < kMfNu * 2 * kMfNu; i += 32) {
+      const int r = i / (2 * kMfNu), c = i % (2 * kMfNu);
+      if (r != k) M[r][c] -= f[r] * M[k][c];
+    }
+    __syncthreads();
+  }
+  float* o = P + (int64_t)kMfNu * kMfNu * p;
+  for (int i = t; i < kMfNu * kMfNu; i += 32) o[i] = (float)M[i / kMfNu][kMfNu + i % kMfNu];
+}
+
+// z[p] = P[p] v[p] (24 x 24 row-major blocks); one thread per row
+__global__ void k_bdiag_apply(int num, const float* __restrict__ P, const float* __restrict__ v, float* __restrict__ z) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)num * kMfNu) return;
+  const int64_t p = t / kMfNu;
+  const float4* row = reinterpret_cast<const float4*>(P + t * kMfNu);
+  const float4* vv = reinterpret_cast<const float4*>(v + p * kMfNu);
+  float s = 0.f;
+#pragma unroll
+  for (int c = 0; c < kMfNu / 4; ++c) {
+    const float4 a = row[c], b = vv[c];
+    s = fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, fmaf(a.w, b.w, s))));
+  }
+  z[t] = s;
+}
+
+// out[seg * ldo + j] += sum over the segment's rows of V_j[row] * w[row], j < nv.
+// grid (nseg, splits); a CTA of 256 threads holds up to 8 rows per thread in registers.
+constexpr int kDotRows = 8, kDotThreads = 256;
+template <class TV>
+__global__ void __launch_bounds__(kDotThreads)
+    k_seg_dots(const int* __restrict__ seg_begin, int nv, const TV* __restrict__ V, int64_t ldv,
+               const TV* __restrict__ w, double* __restrict__ out, int ldo) {
+  const int seg = blockIdx.x;
+  const int64_t r0 = (int64_t)kMfNu * seg_begin[seg], r1 = (int64_t)kMfNu * seg_begin[seg + 1];
+  const int64_t base = r0 + (int64_t)blockIdx.y * kDotThreads * kDotRows;
+  if (base >= r1) return;
+  TV wr[kDotRows];
+#pragma unroll
+  for (int i = 0; i < kDotRows; ++i) {
+    const int64_t r = base + threadIdx.x + (int64_t)i * kDotThreads;
+    wr[i] = r < r1 ? w[r] : TV(0);
+  }
+  __shared__ double red[kDotThreads / 32];
+  for (int j = 0; j < nv; ++j) {
+    const TV* vj = V + (int64_t)j * ldv;
+    double s = 0;
+#pragma unroll
+    for (int i = 0; i < kDotRows; ++i) {
+      const int64_t r = base + threadIdx.x + (int64_t)i * kDotThreads;
+      if (r < r1) s += (double)vj[r] * (double)wr[i];
+    }
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tot = 0;
+      for (int k = 0; k < kDotThreads / 32; ++k) tot += red[k];
+      atomicAdd(out + (int64_t)seg * ldo + j, tot);
+    }
+    __syncthreads();
+  }
+}
+
+// w[row] -= sum_j h[seg(row) * ldh + j] V_j[row]
+__global__ void k_seg_sub(int64_t N, const int* __restrict__ seg_of, int nv, const float* __restrict__ V, int64_t ldv,
+                          const double* __restrict__ h, int ldh, float* __restrict__ w) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= N) return;
+  const double* hs = h + (int64_t)seg_of[r / kMfNu] * ldh;
+  float s = w[r];
+  for (int j = 0; j < nv; ++j) s -= (float)hs[j] * V[(int64_t)j * ldv + r];
+  w[r] = s;
+}
+
+// y[row] (+)= scale[seg(row)] * x[row] (FP32 <- FP64 / FP32)
+template <class TX, class TY>
+__global__ void k_seg_scale(int64_t N, const int* __restrict__ seg_of, const double* __restrict__ scale,
+                            const TX* __restrict__ x, TY* __restrict__ y, int add) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= N) return;
+  const double v = scale[seg_of[r / kMfNu]] * (double)x[r];
+  y[r] = add ? (TY)((double)y[r] + v) : (TY)v;
+}
+
+// Per-realisation Arnoldi bookkeeping after step k (one thread per realisation):
+// H(:,k) = d1 + d2 (two Gram-Schmidt passes), H(k+1,k) = sqrt(n2), previous Givens
+// rotations, the new one, g; inv = 1 / H(k+1,k) for normalising the new basis vector.
+struct Krylov {
+  double* H;      // nseg x (m+1) x m, row-major per realisation
+  double* g;      // nseg x (m+1)
+  double* cs;     // nseg x m
+  double* sn;
+  double* beta;   // nseg
+  double* inv;    // nseg
+  int* kc;        // nseg: Arnoldi columns accepted in this cycle
+  int* active;    // nseg: 1 while the cycle continues for the realisation
+  double* d1;     // nseg x (m+1) dot products, pass 1
+  double* d2;     // pass 2
+  double* n2;     // nseg
+  double* yv;     // nseg x m
+  double* thr;    // nseg: |g| target of the current GMRES solve (inner_tol * first beta)
+  int* nsteps;    // nseg: Arnoldi steps taken while active (reported)
+  int* nactive;   // 1
+};
+
+__global__ void k_arnoldi_update(int nseg, int m, int k, Krylov K) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  if (!K.active[s]) {
+    K.inv[s] = 0.0;
+    return;
+  }
+  double* H = K.H + (int64_t)s * (m + 1) * m;
+  double* g = K.g + (int64_t)s * (m + 1);
+  double* cs = K.cs + (int64_t)s * m;
+  double* sn = K.sn + (int64_t)s * m;
+  for (int i = 0; i <= k; ++i) H[i * m + k] = K.d1[(int64_t)s * (m + 1) + i] + K.d2[(int64_t)s * (m + 1) + i];
+  // ||w|| after the two Gram-Schmidt passes
+  const double hn = sqrt(fmax(K.n2[s], 0.0));
+  H[(k + 1) * m + k] = hn;
+  for (int i = 0; i < k; ++i) {
+    const double a = H[i * m + k], b = H[(i + 1) * m + k];
+    H[i * m + k] = cs[i] * a + sn[i] * b;
+    H[(i + 1) * m + k] = -sn[i] * a + cs[i] * b;
+  }
+  const double a = H[k * m + k], b = H[(k + 1) * m + k];
+  const double den = hypot(a, b);
+  cs[k] = den > 0 ? a / den : 1.0;
+  sn[k] = den > 0 ? b / den : 0.0;
+  H[k * m + k] = den;
+  H[(k + 1) * m + k] = 0.0;
+  g[k + 1] = -sn[k] * g[k];
+  g[k] = cs[k] * g[k];
+  K.kc[s] = k + 1;
+  K.nsteps[s] += 1;
+  K.inv[s] = hn > 0 ? 1.0 / hn : 0.0;
+  if (fabs(g[k + 1]) <= K.thr[s] || hn == 0.0 || k + 1 == m) {
+    K.active[s] = 0;
+    K.inv[s] = 0.0;
+  } else {
+    atomicAdd(K.nactive, 1);
+  }
+}
+
+// y = H(0:kc, 0:kc)^-1 g(0:kc) per realisation (zeros beyond kc)
+__global__ void k_hess_solve(int nseg, int m, Krylov K) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const double* H = K.H + (int64_t)s * (m + 1) * m;
+  const double* g = K.g + (int64_t)s * (m + 1);
+  double* y = K.yv + (int64_t)s * m;
+  const int kc = K.kc[s];
+  for (int i = m - 1; i >= kc; --i) y[i] = 0.0;
+  for (int i = kc - 1; i >= 0; --i) {
+    double t = g[i];
+    for (int j = i + 1; j < kc; ++j) t -= H[i * m + j] * y[j];
+    y[i] = H[i * m + i] != 0.0 ? t / H[i * m + i] : 0.0;
+  }
+}
+
+// start of a GMRES cycle: beta = sqrt(n2), g = (beta, 0, ...); on the first cycle of a
+// solve thr = inner_tol * beta; active while beta > thr and the realisation is not done
+__global__ void k_cycle_start(int nseg, int m, Krylov K, const int* __restrict__ done, int first, double inner_tol) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const double b = sqrt(fmax(K.n2[s], 0.0));
+  K.beta[s] = b;
+  if (first) K.thr[s] = inner_tol * b;
+  double* g = K.g + (int64_t)s * (m + 1);
+  for (int i = 0; i <= m; ++i) g[i] = 0.0;
+  g[0] = b;
+  const int a = (b > K.thr[s] && b > 0.0 && !done[s]) ? 1 : 0;
+  K.active[s] = a;
+  K.kc[s] = 0;
+  K.inv[s] = a ? 1.0 / b : 0.0;
+  if (a) atomicAdd(K.nactive, 1);
+}
+
+// x[row] += sum_j y[seg][j] V_j[row]
+__global__ void k_seg_combine(int64_t N, const int* __restrict__ seg_of, int nv, const float* __restrict__ V,
+                              int64_t ldv, const double* __restrict__ y, int ldy, float* __restrict__ x) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= N) return;
+  const double* ys = y + (int64_t)seg_of[r / kMfNu] * ldy;
+  double s = 0;
+  for (int j = 0; j < nv; ++j) s += ys[j] * (double)V[(int64_t)j * ldv + r];
+  x[r] += (float)s;
+}
+
+template <class T>
+__global__ void k_fill(T* p, int64_t n, T v) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+__global__ void k_mul(int64_t n, const double* __restrict__ a, const double* __restrict__ x, double* __restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = a[i] * x[i];
+}
+__global__ void k_div_to_f32(int64_t n, const double* __restrict__ x, const double* __restrict__ d, float* __restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = (float)(x[i] / d[i]);
+}
+__global__ void k_f32_div(int64_t n, const float* __restrict__ x, const double* __restrict__ d, double* __restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = (double)x[i] / d[i];
+}
+// rs = dr * (b - y)
+__global__ void k_resid(int64_t n, const double* __restrict__ dr, const double* __restrict__ b,
+                        const double* __restrict__ y, double* __restrict__ rs) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) rs[i] = dr[i] * (b[i] - y[i]);
+}
+__global__ void k_to_f32(int64_t n, const double* __restrict__ x, float* __restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = (float)x[i];
+}
+// y += x (FP32)
+__global__ void k_add_f32(int64_t n, const float* __restrict__ x, float* __restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] += x[i];
+}
+// xs += d (FP64 += FP32)
+__global__ void k_acc_f32(int64_t n, const float* __restrict__ d, double* __restrict__ xs) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) xs[i] += (double)d[i];
+}
+// out = a - b (FP32)
+__global__ void k_sub_f32(int64_t n, const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a[i] - b[i];
+}
+// mean order-0 eigenstrain weighted by volume: out[seg*6 + r] += V_p E_p[r]
+__global__ void k_vol_eigen(int num, const int* __restrict__ seg_of, const double* __restrict__ rad,
+                            const double* __restrict__ x, double* __restrict__ out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= num) return;
+  const double a = rad[p];
+  const double vp = 4.0 / 3.0 * 3.141592653589793 * a * a * a;
+  for (int r = 0; r < 6; ++r) atomicAdd(out + 6 * seg_of[p] + r, vp * x[(int64_t)kMfNu * p + r]);
+}
+
+inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+// ------------------------------------------------------------------ batch set-up
+ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st) {
+  if (in.nseg <= 0 || !in.seg_begin || !in.centers_dev || !in.radius_dev || !in.mats)
+    return fail(IBEM_ERR_ARG, "mf: bad batch");
+  b.nseg = in.nseg;
+  b.seg_begin_h.assign(in.seg_begin, in.seg_begin + in.nseg + 1);
+  b.mats_h.assign(in.mats, in.mats + in.nseg);
+  if (b.seg_begin_h[0] != 0) return fail(IBEM_ERR_ARG, "mf: seg_begin[0] must be 0");
+  b.max_seg = 0;
+  for (int s = 0; s < in.nseg; ++s) {
+    const int n = b.seg_begin_h[s + 1] - b.seg_begin_h[s];
+    if (n < 1) return fail(IBEM_ERR_ARG, "mf: every realisation needs at least one particle");
+    b.max_seg = std::max(b.max_seg, n);
+  }
+  b.num = b.seg_begin_h[in.nseg];
+  b.N = (int64_t)kMfNu * b.num;
+  b.cen = in.centers_dev;
+  b.rad = in.radius_dev;
+  std::vector<int> seg_of(b.num);
+  std::vector<MfTile> tiles;
+  for (int s = 0; s < in.nseg; ++s) {
+    for (int p = b.seg_begin_h[s]; p < b.seg_begin_h[s + 1]; ++p) seg_of[p] = s;
+    for (int p = b.seg_begin_h[s]; p < b.seg_begin_h[s + 1]; p += kMfThreads)
+      tiles.push_back({s, p, std::min(kMfThreads, b.seg_begin_h[s + 1] - p), 0});
+  }
+  b.ntiles = (int)tiles.size();
+  // slices of the source range: about 4 CTAs per SM in total, at least 32 sources per slice
+  const int want = 152 * 4;
+  b.hsplit = std::max(1, std::min((want + b.ntiles - 1) / b.ntiles, (b.max_seg + 31) / 32));
+  std::vector<SphMat> md(in.nseg);
+  std::vector<SphMatF> mf(in.nseg);
+  for (int s = 0; s < in.nseg; ++s) {
+    const ibem_material& m = in.mats[s];
+    md[s] = sph_mat_init(m.E0, m.nu0, m.E1, m.nu1);
+    mf[s] = sph_matf_init(md[s]);
+  }
+  IBEM_CUDA(cudaMalloc(&b.seg_begin, sizeof(int) * (in.nseg + 1)));
+  IBEM_CUDA(cudaMalloc(&b.seg_of, sizeof(int) * b.num));
+  IBEM_CUDA(cudaMalloc(&b.gh, sizeof(float4) * b.num));
+  IBEM_CUDA(cudaMalloc(&b.gl, sizeof(float4) * b.num));
+  IBEM_CUDA(cudaMalloc(&b.matd, sizeof(SphMat) * in.nseg));
+  IBEM_CUDA(cudaMalloc(&b.matf, sizeof(SphMatF) * in.nseg));
+  IBEM_CUDA(cudaMalloc(&b.dr, sizeof(double) * b.N));
+  IBEM_CUDA(cudaMalloc(&b.dc, sizeof(double) * b.N));
+  IBEM_CUDA(cudaMalloc(&b.tiles, sizeof(MfTile) * b.ntiles));
+  IBEM_CUDA(cudaMemcpyAsync(b.seg_begin, b.seg_begin_h.data(), sizeof(int) * (in.nseg + 1), cudaMemcpyHostToDevice, st));
+  IBEM_CUDA(cudaMemcpyAsync(b.seg_of, seg_of.data(), sizeof(int) * b.num, cudaMemcpyHostToDevice, st));
+  IBEM_CUDA(cudaMemcpyAsync(b.matd, md.data(), sizeof(SphMat) * in.nseg, cudaMemcpyHostToDevice, st));
+  IBEM_CUDA(cudaMemcpyAsync(b.matf, mf.data(), sizeof(SphMatF) * in.nseg, cudaMemcpyHostToDevice, st));
+  IBEM_CUDA(cudaMemcpyAsync(b.tiles, tiles.data(), sizeof(MfTile) * b.ntiles, cudaMemcpyHostToDevice, st));
+  ::ibem::count_launch(), k_mf_prep<<<nblk(b.num), 256, 0, st>>>(b.num, b.cen, b.rad, b.seg_of, b.matd, b.gh, b.gl,
+                                                                 b.dr, b.dc);
+  IBEM_LAUNCH_CHECK("mf prep");
+  // the host vectors above must outlive the copies
+  IBEM_CUDA(cudaStreamSynchronize(st));
+  return IBEM_OK;
+}
+
+void mf_batch_free(MfBatch& b) {
+  cudaFree(b.seg_begin);
+  cudaFree(b.seg_of);
+  cudaFree(b.gh);
+  cudaFree(b.gl);
+  cudaFree(b.matd);
+  cudaFree(b.matf);
+  cudaFree(b.dr);
+  cudaFree(b.dc);
+  cudaFree(b.tiles);
+  b = MfBatch();
+}
+
+ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_t st) {
+  ProfScope ps(PROF_MATVEC, st);
+  IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(float) * b.N, st));
+  ::ibem::count_launch(), k_mf_apply_f32<<<dim3(b.ntiles, b.hsplit), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, b.gh,
+                                                                                         b.gl, b.matf, x, y);
+  IBEM_LAUNCH_CHECK("mf apply f32");
+  return IBEM_OK;
+}
+
+ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st) {
+  ProfScope ps(PROF_PAIR, st);
+  IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
+  ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, b.cen,
+                                                                                         b.rad, b.matd, x, y);
+  IBEM_LAUNCH_CHECK("mf apply f64");
+  return IBEM_OK;
+}
+
+ibem_status mf_block_jacobi(const MfBatch& b, float* P, cudaStream_t st) {
+  ::ibem::count_launch(), k_block_jacobi<<<b.num, 32, 0, st>>>(b.seg_of, b.matd, P);
+  IBEM_LAUNCH_CHECK("block jacobi");
+  return IBEM_OK;
+}
+
+
+// ------------------------------------------------------------------ solver
+namespace {
+
+struct MfSolver {
+  const MfBatch& b;
+  cudaStream_t st;
+  int m;
+  int64_t N;
+  float* V = nullptr;    // (m+1) x N Krylov basis
+  float* z = nullptr;    // N
+  float* w = nullptr;    // N
+  float* d = nullptr;    // N   correction of the current refinement step
+  float* rin = nullptr;  // N   right-hand side of the current GMRES solve
+  float* r32 = nullptr;  // N   residual of a restarted cycle
+  int* done = nullptr;   // nseg
+  Krylov K{};
+  void* kmem = nullptr;
+  int splits = 1;
+  MfSolver(const MfBatch& bb, cudaStream_t s, int mm) : b(bb), st(s), m(mm), N(bb.N) {
+    splits = (int)((kMfNu * (int64_t)b.max_seg + kDotThreads * kDotRows - 1) / (kDotThreads * kDotRows));
+  }
+  ~MfSolver() {
+    cudaFree(V);
+    cudaFree(z);
+    cudaFree(w);
+    cudaFree(d);
+    cudaFree(rin);
+    cudaFree(r32);
+    cudaFree(done);
+    cudaFree(kmem);
+  }
+  ibem_status alloc() {
+    IBEM_CUDA(cudaMalloc(&V, sizeof(float) * N * (m + 1)));
+    IBEM_CUDA(cudaMalloc(&z, sizeof(float) * N));
+    IBEM_CUDA(cudaMalloc(&w, sizeof(float) * N));
+    IBEM_CUDA(cudaMalloc(&d, sizeof(float) * N));
+    IBEM_CUDA(cudaMalloc(&rin, sizeof(float) * N));
+    IBEM_CUDA(cudaMalloc(&r32, sizeof(float) * N));
+    IBEM_CUDA(cudaMalloc(&done, sizeof(int) * b.nseg));
+    const size_t S = b.nseg;
+    const size_t nd = S * ((size_t)(m + 1) * m + (m + 1) + 2 * (size_t)m + 4 + 2 * (size_t)(m + 1) + m);
+    IBEM_CUDA(cudaMalloc(&kmem, nd * sizeof(double) + sizeof(int) * (3 * S + 1)));
+    double* p = (double*)kmem;
+    K.H = p; p += S * (m + 1) * m;
+    K.g = p; p += S * (m + 1);
+    K.cs = p; p += S * m;
+    K.sn = p; p += S * m;
+    K.beta = p; p += S;
+    K.inv = p; p += S;
+    K.n2 = p; p += S;
+    K.thr = p; p += S;
+    K.d1 = p; p += S * (m + 1);
+    K.d2 = p; p += S * (m + 1);
+    K.yv = p; p += S * m;
+    int* ip = (int*)p;
+    K.kc = ip; ip += S;
+    K.active = ip; ip += S;
+    K.nsteps = ip; ip += S;
+    K.nactive = ip;
+    IBEM_CUDA(cudaMemsetAsync(kmem, 0, nd * sizeof(double) + sizeof(int) * (3 * S + 1), st));
+    return IBEM_OK;
+  }
+  template <class T>
+  ibem_status seg_norm2(const T* v, double* n2) {
+    IBEM_CUDA(cudaMemsetAsync(n2, 0, sizeof(double) * b.nseg, st));
+    ::ibem::count_launch(), k_seg_dots<T><<<dim3(b.nseg, splits), kDotThreads, 0, st>>>(b.seg_begin, 1, v, 0, v, n2, 1);
+    IBEM_LAUNCH_CHECK("seg norm");
+    return IBEM_OK;
+  }
+  int read_nactive(ibem_status& s) {
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, K.nactive, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) s = cuda_fail(e, "gmres: read active count");
+    return h;
+  }
+  // FP32 GMRES(m) with restarts on As d = rin, right-preconditioned by P; d overwritten.
+  // Realisations flagged in `done` take no step.  Stops each realisation once
+  // ||rin - As d|| <= inner_tol ||rin|| (Arnoldi estimate).
+  ibem_status gmres(const float* P, int max_cycles, double inner_tol) {
+    const int S = b.nseg;
+    ibem_status s = IBEM_OK;
+    IBEM_CUDA(cudaMemsetAsync(d, 0, sizeof(float) * N, st));
+    for (int cyc = 0; cyc < max_cycles && !s; ++cyc) {
+      const float* r = rin;
+      if (cyc > 0) {  // residual of the restarted cycle, rin - As d
+        if ((s = mf_apply_f32(b, d, w, st))) break;
+        ::ibem::count_launch(), k_sub_f32<<<nblk(N), 256, 0, st>>>(N, rin, w, r32);
+        r = r32;
+      }
+      if ((s = seg_norm2(r, K.n2))) break;
+      IBEM_CUDA(cudaMemsetAsync(K.nactive, 0, sizeof(int), st));
+      ::ibem::count_launch(), k_cycle_start<<<nblk(S, 128), 128, 0, st>>>(S, m, K, done, cyc == 0, inner_tol);
+      ::ibem::count_launch(), k_seg_scale<float, float><<<nblk(N), 256, 0, st>>>(N, b.seg_of, K.inv, r, V, 0);
+      IBEM_LAUNCH_CHECK("gmres cycle start");
+      const int na = read_nactive(s);
+      if (s || na == 0) break;
+      int k = 0;
+      while (k < m) {
+        float* vk = V + (int64_t)k * N;
+        float* wv = V + (int64_t)(k + 1) * N;
+        ::ibem::count_launch(), k_bdiag_apply<<<nblk(N), 256, 0, st>>>(b.num, P, vk, z);
+        if ((s = mf_apply_f32(b, z, wv, st))) break;
+        {
+          ProfScope pg(PROF_GMRES_OTHER, st);
+          IBEM_CUDA(cudaMemsetAsync(K.d1, 0, sizeof(double) * 2 * (size_t)S * (m + 1), st));
+          ::ibem::count_launch(), k_seg_dots<float><<<dim3(S, splits), kDotThreads, 0, st>>>(b.seg_begin, k + 1, V, N, wv, K.d1, m + 1);
+          ::ibem::count_launch(), k_seg_sub<<<nblk(N), 256, 0, st>>>(N, b.seg_of, k + 1, V, N, K.d1, m + 1, wv);
+          ::ibem::count_launch(), k_seg_dots<float><<<dim3(S, splits), kDotThreads, 0, st>>>(b.seg_begin, k + 1, V, N, wv, K.d2, m + 1);
+          ::ibem::count_launch(), k_seg_sub<<<nblk(N), 256, 0, st>>>(N, b.seg_of, k + 1, V, N, K.d2, m + 1, wv);
+          if ((s = seg_norm2(wv, K.n2))) break;
+          IBEM_CUDA(cudaMemsetAsync(K.nactive, 0, sizeof(int), st));
+          ::ibem::count_launch(), k_arnoldi_update<<<nblk(S, 128), 128, 0, st>>>(S, m, k, K);
+          ::ibem::count_launch(), k_seg_scale<float, float><<<nblk(N), 256, 0, st>>>(N, b.seg_of, K.inv, wv, wv, 0);
+          IBEM_LAUNCH_CHECK("arnoldi step");
+        }
+        ++k;
+        if (read_nactive(s) == 0 || s) break;
+      }
+      if (s) break;
+      // d += P V y
+      ::ibem::count_launch(), k_hess_solve<<<nblk(S, 128), 128, 0, st>>>(S, m, K);
+      IBEM_CUDA(cudaMemsetAsync(w, 0, sizeof(float) * N, st));
+      ::ibem::count_launch(), k_seg_combine<<<nblk(N), 256, 0, st>>>(N, b.seg_of, k, V, N, K.yv, m, w);
+      ::ibem::count_launch(), k_bdiag_apply<<<nblk(N), 256, 0, st>>>(b.num, P, w, z);
+      ::ibem::count_launch(), k_add_f32<<<nblk(N), 256, 0, st>>>(N, z, d);
+      IBEM_LAUNCH_CHECK("gmres update");
+    }
+    return s;
+  }
+};
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const float* P, const ibem_mf_options& o,
+                     ibem_mf_report* rep, cudaStream_t st) {
+  const auto t0 = std::chrono::steady_clock::now();
+  const int S = b.nseg;
+  const int64_t N = b.N;
+  MfSolver g(b, st, o.restart);
+  ibem_status s = g.alloc();
+  double *xs = nullptr, *rs = nullptr, *y = nullptr, *bn2 = nullptr;
+  if (!s) {
+    cudaError_t e = cudaMalloc(&xs, sizeof(double) * N);
+    if (e == cudaSuccess) e = cudaMalloc(&rs, sizeof(double) * N);
+    if (e == cudaSuccess) e = cudaMalloc(&y, sizeof(double) * N);
+    if (e == cudaSuccess) e = cudaMalloc(&bn2, sizeof(double) * 2 * S);
+    if (e != cudaSuccess) s = cuda_fail(e, "mf solve workspace");
+  }
+  std::vector<double> hb(S), hr(S);
+  std::vector<int> hdone(S, 0), outer_of(S, 0);
+  if (!s) {
+    cudaMemsetAsync(xs, 0, sizeof(double) * N, st);
+    ::ibem::count_launch(), k_mul<<<nblk(N), 256, 0, st>>>(N, b.dr, bvec, rs);  // rs = Dr b (x = 0)
+    s = g.seg_norm2(rs, bn2);
+    if (!s) {
+      cudaMemcpyAsync(hb.data(), bn2, sizeof(double) * S, cudaMemcpyDeviceToHost, st);
+      const cudaError_t e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) s = cuda_fail(e, "mf solve: rhs norms");
+    }
+  }
+  int outer = 0;
+  while (!s) {
+    if (outer > 0) {
+      s = g.seg_norm2(rs, bn2 + S);
+      if (s) break;
+      cudaMemcpyAsync(hr.data(), bn2 + S, sizeof(double) * S, cudaMemcpyDeviceToHost, st);
+      const cudaError_t e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) { s = cuda_fail(e, "mf solve: residual norms"); break; }
+    } else {
+      hr = hb;
+    }
+    bool all = true;
+    for (int i = 0; i < S; ++i) {
+      const double rel = hb[i] > 0 ? std::sqrt(hr[i] / hb[i]) : 0.0;
+      rep[i].rel_residual = rel;
+      hdone[i] = rel <= o.tol ? 1 : 0;
+      all = all && hdone[i];
+    }
+    if (all || outer >= o.max_outer) break;
+    for (int i = 0; i < S; ++i)
+      if (!hdone[i]) outer_of[i] = outer + 1;
+    cudaMemcpyAsync(g.done, hdone.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st);
+    // FP32 correction of the scaled system, then the FP64 residual of the new iterate
+    ::ibem::count_launch(), k_to_f32<<<nblk(N), 256, 0, st>>>(N, rs, g.rin);
+    if ((s = g.gmres(P, o.max_cycles, o.inner_tol))) break;
+    ::ibem::count_launch(), k_acc_f32<<<nblk(N), 256, 0, st>>>(N, g.d, xs);
+    ::ibem::count_launch(), k_mul<<<nblk(N), 256, 0, st>>>(N, b.dc, xs, x);
+    if ((s = mf_apply_f64(b, x, y, st))) break;
+    ::ibem::count_launch(), k_resid<<<nblk(N), 256, 0, st>>>(N, b.dr, bvec, y, rs);
+    IBEM_LAUNCH_CHECK("mf refinement");
+    ++outer;
+  }
+  if (!s) {
+    ::ibem::count_launch(), k_mul<<<nblk(N), 256, 0, st>>>(N, b.dc, xs, x);
+    std::vector<int> steps(S);
+    cudaMemcpyAsync(steps.data(), g.K.nsteps, sizeof(int) * S, cudaMemcpyDeviceToHost, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) s = cuda_fail(e, "mf solve: finish");
+    for (int i = 0; i < S; ++i) {
+      rep[i].outer = outer_of[i];
+      rep[i].inner = steps[i];
+      rep[i].t_solve_ms = ms_since(t0);
+    }
+    for (int i = 0; i < S && !s; ++i)
+      if (!(rep[i].rel_residual <= o.tol)) s = fail(IBEM_ERR_NOCONV, "mf solve: a realisation missed the tolerance");
+  }
+  cudaFree(xs);
+  cudaFree(rs);
+  cudaFree(y);
+  cudaFree(bn2);
+  return s;
+}
+
+}  // namespace ibem
+
+// ------------------------------------------------------------------ C ABI
+using namespace ibem;
+
+extern "C" ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int precision, const double* x_dev,
+                                          double* y_dev, void* stream) {
+  if (!batch || !x_dev || !y_dev || (precision != 32 && precision != 64))
+    return fail(IBEM_ERR_ARG, "mf_matvec: bad arguments");
+  cudaStream_t st = as_stream(stream);
+  MfBatch b;
+  ibem_status s = mf_batch_init(b, *batch, st);
+  if (!s) {
+    if (precision == 64) {
+      s = mf_apply_f64(b, x_dev, y_dev, st);
+    } else {
+      float *xf = nullptr, *yf = nullptr;
+      cudaError_t e = cudaMalloc(&xf, sizeof(float) * b.N);
+      if (e == cudaSuccess) e = cudaMalloc(&yf, sizeof(float) * b.N);
+      if (e != cudaSuccess) s = cuda_fail(e, "mf_matvec workspace");
+      if (!s) {
+        ::ibem::count_launch(), k_div_to_f32<<<nblk(b.N), 256, 0, st>>>(b.N, x_dev, b.dc, xf);  // xs = x / Dc
+        s = mf_apply_f32(b, xf, yf, st);
+        if (!s) ::ibem::count_launch(), k_f32_div<<<nblk(b.N), 256, 0, st>>>(b.N, yf, b.dr, y_dev);  // y = ys / Dr
+      }
+      if (!s) {
+        const cudaError_t e2 = cudaStreamSynchronize(st);
+        if (e2 != cudaSuccess) s = cuda_fail(e2, "mf_matvec");
+      }
+      cudaFree(xf);
+      cudaFree(yf);
+    }
+  }
+  if (!s) {
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) s = cuda_fail(e, "mf_matvec");
+  }
+  mf_batch_free(b);
+  return s;
+}
+
+namespace ibem {
+ibem_status mf_learned_blocks(const MfBatch& b, const float* params, float* P, cudaStream_t st);
+}
+
+extern "C" ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const double* b_dev, double* x_dev,
+                                         ibem_precond pc, const float* gnn_params_dev, const ibem_mf_options* opt,
+                                         ibem_mf_report* reports, void* stream) {
+  if (!batch || !b_dev || !x_dev || !reports) return fail(IBEM_ERR_ARG, "mf_solve: bad arguments");
+  if (pc != IBEM_PRECOND_BLOCK_JACOBI && pc != IBEM_PRECOND_LEARNED) return fail(IBEM_ERR_ARG, "mf_solve: preconditioner");
+  if (pc == IBEM_PRECOND_LEARNED && !gnn_params_dev) return fail(IBEM_ERR_ARG, "mf_solve: learned form needs parameters");
+  ibem_mf_options o{};
+  if (opt) o = *opt;
+  if (o.restart <= 0) o.restart = 50;
+  if (o.max_cycles <= 0) o.max_cycles = 20;
+  if (o.max_outer <= 0) o.max_outer = 8;
+  if (o.tol <= 0) o.tol = 1e-10;
+  if (o.inner_tol <= 0) o.inner_tol = 1e-5;
+  if (o.restart > 200) return fail(IBEM_ERR_ARG, "mf_solve: restart > 200");
+  cudaStream_t st = as_stream(stream);
+  const auto t0 = std::chrono::steady_clock::now();
+  MfBatch b;
+  ibem_status s = mf_batch_init(b, *batch, st);
+  float* P = nullptr;
+  if (!s) {
+    const cudaError_t e = cudaMalloc(&P, sizeof(float) * kMfNu * kMfNu * (size_t)b.num);
+    if (e != cudaSuccess) s = cuda_fail(e, "mf_solve: preconditioner blocks");
+  }
+  if (!s) s = mf_block_jacobi(b, P, st);
+  if (!s && pc == IBEM_PRECOND_LEARNED) s = mf_learned_blocks(b, gnn_params_dev, P, st);
+  if (!s) {
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) s = cuda_fail(e, "mf_solve: set-up");
+  }
+  const double tset = ms_since(t0);
+  for (int i = 0; i < batch->nseg; ++i) reports[i] = ibem_mf_report{};
+  if (!s) s = mf_solve(b, b_dev, x_dev, P, o, reports, st);
+  for (int i = 0; i < batch->nseg; ++i) reports[i].t_setup_ms = tset;
+  cudaFree(P);
+  mf_batch_free(b);
+  return s;
+}
+
+extern "C" ibem_status ibem_e3d_batch_farfield_rhs(const ibem_e3d_batch* batch, const double* sig_inf, double* b_dev,
+                                                   void* stream) {
+  if (!batch || !batch->seg_begin || !batch->mats || !sig_inf || !b_dev)
+    return fail(IBEM_ERR_ARG, "batch_farfield_rhs: bad arguments");
+  for (int s = 0; s < batch->nseg; ++s) {
+    const int p0 = batch->seg_begin[s], n = batch->seg_begin[s + 1] - p0;
+    const ibem_status r = ibem_e3d_farfield_rhs(n, &batch->mats[s], 24, sig_inf, b_dev + (int64_t)kMfNu * p0, stream);
+    if (r) return r;
+  }
+  return IBEM_OK;
+}
+
+extern "C" ibem_status ibem_e3d_effective_modulus(const ibem_e3d_batch* batch, const double* x_dev,
+                                                  const double* volume, const double* sig_inf, double* mean_strain,
+                                                  double* e_eff, void* stream) {
+  if (!batch || !x_dev || !volume || !sig_inf || !e_eff) return fail(IBEM_ERR_ARG, "effective_modulus: bad arguments");
+  cudaStream_t st = as_stream(stream);
+  MfBatch b;
+  ibem_status s = mf_batch_init(b, *batch, st);
+  double* acc = nullptr;
+  const int S = batch->nseg;
+  std::vector<double> h(6 * (size_t)S);
+  if (!s) {
+    cudaError_t e = cudaMalloc(&acc, sizeof(double) * 6 * S);
+    if (e == cudaSuccess) e = cudaMemsetAsync(acc, 0, sizeof(double) * 6 * S, st);
+    if (e != cudaSuccess) s = cuda_fail(e, "effective_modulus");
+  }
+  if (!s) {
+    ::ibem::count_launch(), k_vol_eigen<<<nblk(b.num), 256, 0, st>>>(b.num, b.seg_of, b.rad, x_dev, acc);
+    cudaMemcpyAsync(h.data(), acc, sizeof(double) * 6 * S, cudaMemcpyDeviceToHost, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) s = cuda_fail(e, "effective_modulus");
+  }
+  if (!s) {
+    for (int i = 0; i < S; ++i) {
+      const ibem_material& m = batch->mats[i];
+      const double tr = sig_inf[0] + sig_inf[3] + sig_inf[5];
+      double eps[6];
+      for (int r = 0; r < 6; ++r) {
+        const bool diag = (r == 0 || r == 3 || r == 5);
+        eps[r] = ((1 + m.nu0) * sig_inf[r] - (diag ? m.nu0 * tr : 0.0)) / m.E0 + h[6 * i + r] / volume[i];
+      }
+      if (mean_strain)
+        for (int r = 0; r < 6; ++r) mean_strain[6 * i + r] = eps[r];
+      e_eff[i] = eps[5] != 0 ? sig_inf[5] / eps[5] : 0.0;
+    }
+  }
+  cudaFree(acc);
+  mf_batch_free(b);
+  return s;
+}

@@ -1,0 +1,79 @@
+// Internal interface of the matrix-free solver (mf.cu) and the learned preconditioner
+// (gnn.cu): the sphere system of layout 24 is never stored; its 24 x 24 pair blocks are
+// evaluated on the fly inside the products.
+//
+// Batches: the particles of several independent realisations (segments) are concatenated;
+// particle p belongs to segment seg_of[p] and interacts only with particles of that
+// segment.  Unknowns of particle p are rows 24p .. 24p + 23 (E_ij | E_ijk, as layout 24).
+//
+// Scaled system.  With a_p the radius of particle p, mu0 the matrix shear modulus of the
+// segment, rho_r = 1 for rows of order 1 (r >= 6) and sigma_c = 1 for columns of order 1,
+//   As = Dr A Dc,   Dr = diag(a_s^rho_r / mu0),   Dc = diag(a_h^-sigma_c),
+// so that As[(s,r),(h,c)] = (a_s / a_h)^rho_r * B(x / a_h; 1)_rc / mu0 with B the pair block
+// of a unit sphere: every entry is O(1) whatever the radii and moduli, which is what the
+// FP32 products need.  x = Dc xs and bs = Dr b.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "gen_sphere_common.cuh"
+#include "gen_sphere24_f32.cuh"
+#include "ibem_internal.h"
+
+namespace ibem {
+
+constexpr int kMfNu = 24;   // unknowns per particle of the matrix-free path
+constexpr int kKnn = 16;    // neighbours per particle of the learned preconditioner
+
+struct MfTile {
+  int seg, s0, ns, pad;     // one CTA's target particles s0 .. s0 + ns - 1 of segment seg
+};
+
+struct MfBatch {
+  int nseg = 0, num = 0, max_seg = 0;
+  int64_t N = 0;
+  std::vector<int> seg_begin_h;
+  std::vector<ibem_material> mats_h;
+  int* seg_begin = nullptr;   // nseg + 1
+  int* seg_of = nullptr;      // num
+  const double* cen = nullptr;  // caller's, num x 3
+  const double* rad = nullptr;  // caller's, num
+  float4* gh = nullptr;       // centre (high float parts), radius
+  float4* gl = nullptr;       // centre (low float parts), 1 / radius
+  SphMat* matd = nullptr;     // per segment, physical units
+  SphMatF* matf = nullptr;    // per segment, divided by mu0
+  double* dr = nullptr;       // N: row scaling
+  double* dc = nullptr;       // N: column scaling
+  MfTile* tiles = nullptr;
+  int ntiles = 0, hsplit = 1;
+};
+
+ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st);
+void mf_batch_free(MfBatch& b);
+
+// y = As x (FP32, scaled system); y is overwritten
+ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_t st);
+// y = A x (FP64, physical units); y is overwritten
+ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st);
+// P[p] = inverse of the scaled diagonal block As[p, p] (24 x 24, row-major, FP32)
+ibem_status mf_block_jacobi(const MfBatch& b, float* P, cudaStream_t st);
+
+// ---- learned preconditioner (gnn.cu) ----
+constexpr int kGnnHidden = 64, kGnnLayers = 3, kGnnNodeF = 10, kGnnEdgeF = 7;
+int64_t gnn_param_count();
+// k nearest neighbours within each segment (by centre distance, ties to the lower index);
+// nbr[p * kKnn + j] = neighbour index or -1
+ibem_status gnn_knn(const MfBatch& b, int* nbr, cudaStream_t st);
+ibem_status gnn_features(const MfBatch& b, const int* nbr, float* xn, float* ef, cudaStream_t st);
+// Edge corrections T_e = B_i As_ij B_j As_ji B_i for every edge e = (i <- j):
+//   P[i] += w_e T_e  when w != nullptr (P holds B on entry),
+//   u[q][e] = T_e r_q[i] for q < nrhs when r != nullptr.
+ibem_status gnn_edge_corrections(const MfBatch& b, const int* nbr, const float* B, const float* w, float* P,
+                                 int nrhs, const float* r, float* u, cudaStream_t st);
+// Edge weights of the network (forward only); w has num * kKnn entries
+ibem_status gnn_forward_weights(int num, const int* nbr, const float* xn, const float* ef, const float* params,
+                                float* w, cudaStream_t st);
+
+}  // namespace ibem

@@ -177,6 +177,124 @@ ibem_status ibem_gemm_sub_f32(int64_t m, int64_t n, int64_t k, const float* A_de
 ibem_status ibem_e3d_solve_noalloc(int64_t N, const double* A_dev, int64_t lda, const double* b_dev,
                                    double* x_dev, ibem_solve_report* report, void* stream);
 
+/* ---- matrix-free solves, batches of realisations (layout 24) --------------- */
+
+/* Several independent microstructures ("realisations", "segments") whose particles are
+ * concatenated: particles seg_begin[s] .. seg_begin[s+1]-1 form realisation s and interact
+ * only with each other; unknowns of particle p are entries 24p .. 24p+23 of b and x (the
+ * layout-24 order of a single-realisation system).  No reference counterpart: the
+ * reference solves one microstructure per run (systemSolverElastic3D.h:44-60) with
+ * the matrix stored. */
+typedef struct {
+  int nseg;
+  const int* seg_begin;          /* host, nseg + 1 offsets, seg_begin[0] = 0 */
+  const double* centers_dev;     /* seg_begin[nseg] x 3, row-major */
+  const double* radius_dev;      /* seg_begin[nseg] */
+  const ibem_material* mats;     /* host, one per realisation */
+} ibem_e3d_batch;
+
+typedef enum {
+  IBEM_PRECOND_BLOCK_JACOBI = 0, /* inverse of each particle's own 24 x 24 block */
+  IBEM_PRECOND_LEARNED = 1       /* block-Jacobi + GNN-weighted neighbour corrections */
+} ibem_precond;
+
+typedef struct {
+  int restart;        /* Krylov basis size of the FP32 GMRES (0 = 50) */
+  int max_cycles;     /* GMRES restarts per refinement step (0 = 20) */
+  int max_outer;      /* FP64 refinement steps (0 = 8) */
+  double tol;         /* target rel_residual (0 = 1e-10) */
+  double inner_tol;   /* residual reduction asked of each FP32 GMRES solve (0 = 1e-5) */
+} ibem_mf_options;
+
+typedef struct {
+  double rel_residual;   /* ||Dr (b - A x)||_2 / ||Dr b||_2, FP64, Dr the row scaling
+                          * a_s^order / mu0 that makes every entry O(1) */
+  int outer;             /* FP64 residual evaluations / refinement steps */
+  int inner;             /* Arnoldi steps (FP32 matrix-free products) */
+  double t_setup_ms, t_solve_ms;
+} ibem_mf_report;
+
+/* y = A x for the sphere systems of a batch (the matrix ibem_e3d_pair_blocks would
+ * assemble for each realisation, layout 24), without storing A: every 24 x 24 pair block is
+ * evaluated inside the product.  precision 64: FP64 in physical units; precision 32: the
+ * FP32 product of the scaled system (x and y are converted on the way in and out), about
+ * 1e-6 relative.  x_dev, y_dev: 24 * seg_begin[nseg] doubles. */
+ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int precision, const double* x_dev,
+                               double* y_dev, void* stream);
+
+/* Solve A x = b for every realisation of a batch without storing A (a form of
+ * systemSolverElastic3D::solve, systemSolverElastic3D.h:44-60, for boundary-free far-field
+ * cases): FP64 iterative refinement whose residuals are FP64 matrix-free products, each
+ * correction an FP32 restarted GMRES on the scaled system with matrix-free FP32 products,
+ * right-preconditioned block-diagonally (`pc`; IBEM_PRECOND_LEARNED needs gnn_params_dev
+ * from ibem_gnn_train).  reports: host array of nseg.  Workspace is allocated internally.
+ * Synchronous.  IBEM_ERR_NOCONV if a realisation misses opt->tol. */
+ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const double* b_dev, double* x_dev,
+                              ibem_precond pc, const float* gnn_params_dev,
+                              const ibem_mf_options* opt, ibem_mf_report* reports, void* stream);
+
+/* Far-field right-hand sides of a batch (ibem_e3d_farfield_rhs per realisation, layout 24). */
+ibem_status ibem_e3d_batch_farfield_rhs(const ibem_e3d_batch* batch, const double* sig_inf,
+                                        double* b_dev, void* stream);
+
+/* Effective response of each realisation under the remote stress sig_inf (host, xx xy xz yy
+ * yz zz) from its solution x: mean strain <e> = C0^-1 : sig_inf + sum_p (V_p / volume) E_p
+ * (the eigenstrain's order-0 part, whose volume average over a sphere is E_p), written to
+ * mean_strain (host nseg x 6, may be NULL), and E_eff = sig_inf[5] / <e_33> to e_eff (host
+ * nseg).  volume: host nseg, each realisation's cell volume.  Synchronous. */
+ibem_status ibem_e3d_effective_modulus(const ibem_e3d_batch* batch, const double* x_dev,
+                                       const double* volume, const double* sig_inf,
+                                       double* mean_strain, double* e_eff, void* stream);
+
+/* ---- learned preconditioner (no reference counterpart) --------------------- */
+/* A message-passing network over each particle's 16 nearest neighbours predicts one
+ * weight w_e per edge e = (i <- j); the preconditioner block of particle i is
+ *   P_i = B_i + sum_e w_e T_e,   T_e = B_i As_ij B_j As_ji B_i,
+ * B the block-Jacobi inverse and As the scaled pair blocks (the leading term of the
+ * diagonal block of As^-1 coming from neighbour j).  Inputs: node features (dim 10: semi-
+ * axes / radius, orientation quaternion, E1/(10 E0), nu0, nu1) and edge features (dim 7:
+ * offset / a_i, distance / a_i, a_j / a_i, gap / a_i, (2 a_i / distance)^3).  Network:
+ * h = relu(W_in x + b); 3 layers of m_e = relu(W_m [h_i, h_j, f_e] + b),
+ * h_i += relu(W_u [h_i, mean_e m_e] + b); w_e = W_o2 relu(W_o1 [h_i, h_j, f_e] + b) + b_o2.
+ * Parameters: one flat FP32 array of ibem_gnn_param_count() values (W row-major
+ * in x out, each followed by its bias, in the order above). */
+int64_t ibem_gnn_param_count(void);
+
+/* Seeded initialisation (uniform +-1/sqrt(fan_in), output layer zero: P = block-Jacobi). */
+ibem_status ibem_gnn_init_params(float* params_dev, uint64_t seed, void* stream);
+
+/* Graph, features and training projections of a batch.  nbr_dev: num*16 ints (-1 when a
+ * realisation has fewer than 17 particles); node_feat_dev num*10; edge_feat_dev num*16*7.
+ * With nrhs > 0 pairs (r_hat, e_hat) of the scaled system (e_hat = As^-1 r_hat, FP64,
+ * nrhs x N each), z_dev (nrhs x N) = B r - e and u_dev (nrhs x num*16 x 24) = T_e r_i, both
+ * divided by sqrt(sum ||e||^2), so that the training loss is
+ *   L = sum_q sum_i || z_qi + sum_e w_e u_qe ||^2  (relative squared error of P r vs e). */
+ibem_status ibem_gnn_prepare(const ibem_e3d_batch* batch, int nrhs, const double* r_hat_dev,
+                             const double* e_hat_dev, int* nbr_dev, float* node_feat_dev,
+                             float* edge_feat_dev, float* z_dev, float* u_dev, void* stream);
+
+/* Loss L (host) and its gradient with respect to the parameters (grad_dev, overwritten). */
+ibem_status ibem_gnn_loss_grad(int num, const int* nbr_dev, const float* node_feat_dev,
+                               const float* edge_feat_dev, int nrhs, const float* z_dev,
+                               const float* u_dev, const float* params_dev, double* loss,
+                               float* grad_dev, void* stream);
+
+/* Edge weights w (num*16) of the network (forward pass only). */
+ibem_status ibem_gnn_edge_weights(int num, const int* nbr_dev, const float* node_feat_dev,
+                                  const float* edge_feat_dev, const float* params_dev, float* w_dev,
+                                  void* stream);
+
+/* One AdamW step (decoupled weight decay, bias-corrected moments; step counts from 1). */
+ibem_status ibem_gnn_adamw(int64_t n, float* params_dev, const float* grad_dev, float* m_dev,
+                           float* v_dev, int step, float lr, float beta1, float beta2, float eps,
+                           float weight_decay, void* stream);
+
+/* Full-batch training: prepare, then `steps` AdamW steps (betas 0.9/0.999, eps 1e-8);
+ * loss_hist (host, steps + 1) gets the loss before every step and after the last.  Synchronous. */
+ibem_status ibem_gnn_train(const ibem_e3d_batch* batch, int nrhs, const double* r_hat_dev,
+                           const double* e_hat_dev, float* params_dev, int steps, float lr,
+                           float weight_decay, double* loss_hist, void* stream);
+
 /* ---- postProcessor (postProcessorElastic3D.cpp) -------------------------- */
 
 /* Stress at sample points: replaces postProcessorElastic3D::getFlux

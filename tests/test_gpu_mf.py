@@ -1,0 +1,225 @@
+"""Matrix-free solves, batches of realisations and the learned preconditioner on the GPU,
+through the C ABI (ibem_e3d_mf_*, ibem_gnn_*).
+
+Checks: the on-the-fly products against the matrix that ibem_e3d_pair_blocks assembles
+(itself pinned to the oracle elsewhere): FP64 to 1e-12, FP32 to 2e-5 in the scaled norm;
+matrix-free solutions against the plain FP64 LU solve to 1e-8 (relative, eigenstrain
+coefficients); the graph, features and training projections against numpy restatements;
+the network's loss and gradient against the float64 autograd oracle (oracle/gnn_oracle.py)
+to 1e-4; AdamW against the oracle's step; the trained network against block-Jacobi on
+held-out microstructures; effective moduli against the dilute Eshelby solution."""
+import numpy as np
+import pytest
+
+from conftest import scaled_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def B():
+    import ibemproject_gb300 as g
+    g.lib()
+    from ibemproject_gb300 import batch
+    return batch
+
+
+def small_cases(nums, seed=0, vf=0.15, contrast=None):
+    from ibemproject_gb300 import cases
+    out = []
+    for k, n in enumerate(nums):
+        E1 = 400e9 if contrast is None else 70e9 * contrast[k]
+        out.append(cases.farfield_case(num=n, r0=0.012, vf=vf, grid=0, seed=seed + k, E1=E1))
+    return out
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_mf_matvec_matches_assembled_matrix(B):
+    import torch
+    cs = small_cases([40, 23], seed=11, contrast=[5.7, 12.0])
+    bt = B.DeviceBatch(cs)
+    rng = np.random.default_rng(3)
+    dr, dc = bt.scalings()
+    xs = rng.standard_normal(bt.N)
+    x = torch.from_numpy(xs * dc).cuda()   # O(1) in the scaled unknowns
+    y64 = B.matvec(bt, x, 64).cpu().numpy()
+    y32 = B.matvec(bt, x, 32).cpu().numpy()
+    for s, c in enumerate(cs):
+        rows = bt.seg_rows(s)
+        A = B.dense_system(c).cpu().numpy().T   # row-major view of the column-major storage
+        ref = A @ x.cpu().numpy()[rows]
+        assert scaled_err(y64[rows], ref) < 1e-12
+        assert rel(dr[rows] * y32[rows], dr[rows] * ref) < 2e-5
+
+
+def test_block_jacobi_solve_matches_dense_lu(B):
+    cs = small_cases([120, 45], seed=5, contrast=[5.7, 15.0])
+    bt = B.DeviceBatch(cs)
+    sig = np.array([0, 0, 0, 0, 0, 1.0])
+    b = B.farfield_rhs(bt, sig)
+    x, reps = B.solve(bt, b, B.PRECOND_BLOCK_JACOBI, tol=1e-11)
+    x = x.cpu().numpy()
+    for s, c in enumerate(cs):
+        rows = bt.seg_rows(s)
+        xr = B.dense_solve(c, b[rows]).cpu().numpy()
+        assert scaled_err(x[rows], xr) < 1e-8
+        assert reps[s].rel_residual <= 1e-11
+        assert reps[s].outer >= 1 and reps[s].inner >= 1
+
+
+def test_gnn_graph_features_and_projections(B):
+    import torch
+    cs = small_cases([30, 14], seed=21, contrast=[5.7, 3.0])   # second has < 17 particles
+    bt = B.DeviceBatch(cs)
+    r, e = B.training_pairs(bt, nrhs=2, seed=4)
+    pr = B.prepare(bt, r, e)
+    nbr = pr["nbr"].cpu().numpy().reshape(bt.num, B.KNN)
+    xn = pr["xn"].cpu().numpy().reshape(bt.num, B.NODE_FEATS)
+    ef = pr["ef"].cpu().numpy().reshape(bt.num, B.KNN, B.EDGE_FEATS)
+    C, R = bt.centers_host, bt.radius_host
+    dr, dc = bt.scalings()
+    rn, en = r.cpu().numpy(), e.cpu().numpy()
+    k = 1.0 / np.sqrt((en ** 2).sum())
+    z = pr["z"].cpu().numpy()[:2 * bt.N].reshape(2, bt.N)
+    u = pr["u"].cpu().numpy()[:2 * bt.num * B.KNN * 24].reshape(2, bt.num * B.KNN, 24)
+    for s, c in enumerate(cs):
+        p0, p1 = int(bt.seg_begin[s]), int(bt.seg_begin[s + 1])
+        A = B.dense_system(c).cpu().numpy().T
+        rows = bt.seg_rows(s)
+        As = dr[rows, None] * A * dc[None, rows]
+        blk = lambda i, j: As[24 * i:24 * i + 24, 24 * j:24 * j + 24]
+        Binv = [np.linalg.inv(blk(i, i)) for i in range(c.num)]
+        for i in range(c.num):
+            p = p0 + i
+            d2 = ((C[p0:p1] - C[p]) ** 2).sum(axis=1)
+            order = [p0 + j for j in np.lexsort((np.arange(c.num), d2)) if p0 + j != p][:B.KNN]
+            want = np.full(B.KNN, -1)
+            want[:len(order)] = order
+            np.testing.assert_array_equal(nbr[p], want)
+            assert np.allclose(xn[p], [1, 1, 1, 1, 0, 0, 0, c.E1 / (10 * c.E0), c.nu0, c.nu1], rtol=1e-6)
+            # z = (B r - e) k
+            for q in range(2):
+                zr = (Binv[i] @ rn[q, 24 * p:24 * p + 24] - en[q, 24 * p:24 * p + 24]) * k
+                assert np.abs(z[q, 24 * p:24 * p + 24] - zr).max() <= 1e-4 * np.abs(zr).max() + 1e-7
+            for slot, j in enumerate(nbr[p]):
+                eidx = p * B.KNN + slot
+                if j < 0:
+                    assert np.all(ef[p, slot] == 0) and np.all(u[:, eidx] == 0)
+                    continue
+                d = (C[j] - C[p]) / R[p]
+                dist = np.linalg.norm(d)
+                fe = [*d, dist, R[j] / R[p], dist - 1 - R[j] / R[p], (2 / dist) ** 3]
+                np.testing.assert_allclose(ef[p, slot], fe, rtol=1e-5, atol=1e-6)
+                jj = j - p0
+                T = Binv[i] @ blk(i, jj) @ Binv[jj] @ blk(jj, i) @ Binv[i]
+                for q in range(2):
+                    ur = T @ rn[q, 24 * p:24 * p + 24] * k
+                    assert np.abs(u[q, eidx] - ur).max() <= 2e-4 * np.abs(ur).max() + 1e-9
+
+
+def _random_problem(B, seed=0):
+    cs = small_cases([26, 18], seed=31 + seed, contrast=[5.7, 9.0])
+    bt = B.DeviceBatch(cs)
+    r, e = B.training_pairs(bt, nrhs=2, seed=seed)
+    return bt, B.prepare(bt, r, e)
+
+
+def test_gnn_loss_and_gradient_match_oracle(B):
+    import torch
+    import gnn_oracle as go
+    bt, pr = _random_problem(B)
+    rng = np.random.default_rng(7)
+    p = B.init_params(seed=3).cpu().numpy().astype(np.float64)
+    n_out = go.H + 1
+    p[-n_out:] = rng.uniform(-0.3, 0.3, n_out)   # a non-zero output layer: every block gets gradient
+    pt = torch.from_numpy(p.astype(np.float32)).cuda()
+    L, g = B.loss_grad(pr, bt.num, pt)
+    g = g.cpu().numpy()
+    nrhs = pr["nrhs"]
+    Lo, go_ = go.loss_and_grad(pt.cpu().numpy().astype(np.float64), pr["nbr"].cpu().numpy(),
+                               pr["xn"].cpu().numpy(), pr["ef"].cpu().numpy(),
+                               pr["z"].cpu().numpy()[:nrhs * bt.N].astype(np.float64),
+                               pr["u"].cpu().numpy()[:nrhs * bt.num * B.KNN * 24].astype(np.float64))
+    assert abs(L - Lo) <= 1e-4 * abs(Lo)
+    assert np.abs(g - go_).max() <= 1e-4 * np.abs(go_).max()
+    # weights of the forward pass alone
+    w = B.edge_weights(pr, bt.num, pt).cpu().numpy()
+    wo = go.forward(torch.from_numpy(pt.cpu().numpy().astype(np.float64)), pr["nbr"].cpu(),
+                    pr["xn"].cpu().double().reshape(-1, go.NODE_F), pr["ef"].cpu().double()).numpy()
+    assert np.abs(w - wo).max() <= 1e-4 * max(1.0, np.abs(wo).max())
+
+
+def test_adamw_matches_oracle(B):
+    import torch
+    import gnn_oracle as go
+    rng = np.random.default_rng(9)
+    n = 1000
+    p0, gr = rng.standard_normal(n), rng.standard_normal(n)
+    P = torch.from_numpy(p0.astype(np.float32)).cuda()
+    M = torch.zeros(n, device="cuda")
+    V = torch.zeros(n, device="cuda")
+    p, m, v = p0.astype(np.float32).astype(np.float64), np.zeros(n), np.zeros(n)
+    for step in (1, 2, 3):
+        G = torch.from_numpy((gr * step).astype(np.float32)).cuda()
+        B.adamw(P, G, M, V, step, 1e-2, weight_decay=0.01)
+        p, m, v = go.adamw_step(p, (gr * step).astype(np.float32).astype(np.float64), m, v, step, 1e-2,
+                                weight_decay=0.01)
+    np.testing.assert_allclose(P.cpu().numpy(), p, rtol=1e-5, atol=1e-6)
+
+
+def test_learned_preconditioner_beats_block_jacobi(B):
+    """Train on 8 microstructures, then solve 3 held-out ones with both preconditioners."""
+    import torch
+    train_cs = small_cases([90, 120, 100, 80, 110, 95, 130, 85], seed=100, vf=0.25)
+    bt = B.DeviceBatch(train_cs)
+    r, e = B.training_pairs(bt, nrhs=3, seed=1)
+    params = B.init_params(seed=0)
+    hist = B.train(bt, r, e, params, steps=300, lr=3e-3)
+    assert hist[-1] < 0.9 * hist[0]
+    test_cs = small_cases([150, 140, 160], seed=500, vf=0.25)
+    tb = B.DeviceBatch(test_cs)
+    b = B.farfield_rhs(tb, np.array([0, 0, 0, 0, 0, 1.0]))
+    x0, r0 = B.solve(tb, b, B.PRECOND_BLOCK_JACOBI, tol=1e-10)
+    x1, r1 = B.solve(tb, b, B.PRECOND_LEARNED, params=params, tol=1e-10)
+    it0 = sum(x.inner for x in r0)
+    it1 = sum(x.inner for x in r1)
+    assert it1 < it0, (it0, it1)
+    x0, x1 = x0.cpu().numpy(), x1.cpu().numpy()
+    for s, c in enumerate(test_cs):
+        rows = tb.seg_rows(s)
+        xr = B.dense_solve(c, b[rows]).cpu().numpy()
+        assert scaled_err(x1[rows], xr) < 1e-8
+        assert scaled_err(x0[rows], xr) < 1e-8
+
+
+def test_effective_modulus_single_sphere_matches_eshelby(B):
+    """One sphere: the eigenstrain is uniform and Eshelby's; <e33> = e0_33 + f e*_33."""
+    from ibemproject_gb300 import cases
+    c = cases.farfield_case(num=1, r0=0.05, vf=0.01, grid=0, seed=1)
+    bt = B.DeviceBatch([c])
+    sig = np.array([0, 0, 0, 0, 0, 1e6])
+    b = B.farfield_rhs(bt, sig)
+    x, _ = B.solve(bt, b, B.PRECOND_BLOCK_JACOBI, tol=1e-12)
+    V = 4 / 3 * np.pi * c.radius[0] ** 3 / 0.01
+    Eeff, eps = B.effective_modulus(bt, x, sig, volume=[V])
+    # Eshelby: C1 (e0 + S e*) = C0 (e0 + S e* - e*), isotropic S of a sphere (Voigt-free 3x3x3x3)
+    nu0, E0, E1, nu1 = c.nu0, c.E0, c.E1, c.nu1
+    I = np.eye(3)
+    def iso(E, nu):
+        lam, mu = E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))
+        return lam * np.einsum("ij,kl->ijkl", I, I) + mu * (np.einsum("ik,jl->ijkl", I, I) + np.einsum("il,jk->ijkl", I, I))
+    a1 = (5 * nu0 - 1) / (15 * (1 - nu0))
+    a2 = (4 - 5 * nu0) / (15 * (1 - nu0))
+    S = a1 * np.einsum("ij,kl->ijkl", I, I) + a2 * (np.einsum("ik,jl->ijkl", I, I) + np.einsum("il,jk->ijkl", I, I))
+    C0, C1 = iso(E0, nu0), iso(E1, nu1)
+    e0 = ((1 + nu0) * np.diag([0, 0, sig[5]]) - nu0 * sig[5] * I) / E0
+    M = (np.tensordot(C1 - C0, S, 2) + C0).reshape(9, 9)
+    rhs = -np.tensordot(C1 - C0, e0, 2).reshape(9)
+    estar = np.linalg.lstsq(M, rhs, rcond=None)[0].reshape(3, 3)   # minimum norm: the symmetric solution
+    f = 4 / 3 * np.pi * c.radius[0] ** 3 / V
+    e33 = e0[2, 2] + f * estar[2, 2]
+    assert abs(eps[0, 5] - e33) <= 1e-9 * abs(e33)
+    assert abs(Eeff[0] - sig[5] / e33) <= 1e-9 * abs(sig[5] / e33)
