@@ -57,7 +57,7 @@ class MfReport(ctypes.Structure):
                 ("t_setup_ms", ctypes.c_double), ("t_solve_ms", ctypes.c_double)]
 
 
-PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1
+PRECOND_BLOCK_JACOBI, PRECOND_LEARNED, PRECOND_NEUMANN = 0, 1, 2
 
 
 class IbemError(RuntimeError):

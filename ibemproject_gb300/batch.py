@@ -18,7 +18,7 @@ import ctypes
 import numpy as np
 
 from . import (Batch, IbemError, Material, MfOptions, MfReport, PRECOND_BLOCK_JACOBI, PRECOND_LEARNED,
-               SOLVE_FP64, SolveReport, check, lib)
+               PRECOND_NEUMANN, SOLVE_FP64, SolveReport, check, lib)
 
 NU = 24
 KNN = 16
@@ -194,7 +194,7 @@ def prepare(batch: DeviceBatch, r_hat=None, e_hat=None):
         "xn": torch.empty(batch.num * NODE_FEATS, dtype=torch.float32, device=dev),
         "ef": torch.empty(E * EDGE_FEATS, dtype=torch.float32, device=dev),
         "z": torch.empty(max(nrhs, 1) * batch.N, dtype=torch.float32, device=dev),
-        "u": torch.empty(max(nrhs, 1) * E * NU, dtype=torch.float32, device=dev),
+        "u": torch.empty(max(nrhs, 1) * E * 2 * NU, dtype=torch.float32, device=dev),
         "nrhs": nrhs,
     }
     check(lib().ibem_gnn_prepare(batch.ref(), nrhs, _ptr(r_hat) if nrhs else None, _ptr(e_hat) if nrhs else None,
@@ -216,8 +216,9 @@ def loss_grad(prep: dict, num: int, params):
 
 
 def edge_weights(prep: dict, num: int, params):
+    """(w_e, alpha_e) of every edge, num*16 x 2 flattened."""
     import torch
-    w = torch.empty(num * KNN, dtype=torch.float32, device=params.device)
+    w = torch.empty(num * KNN * 2, dtype=torch.float32, device=params.device)
     check(lib().ibem_gnn_edge_weights(num, _ptr(prep["nbr"]), _ptr(prep["xn"]), _ptr(prep["ef"]), _ptr(params),
                                       _ptr(w), None))
     torch.cuda.synchronize()
@@ -241,4 +242,4 @@ def train(batch: DeviceBatch, r_hat, e_hat, params, steps: int, lr: float = 2e-3
 
 __all__ = ["DeviceBatch", "farfield_rhs", "matvec", "solve", "effective_modulus", "dense_system", "dense_solve",
            "training_pairs", "param_count", "init_params", "prepare", "loss_grad", "edge_weights", "adamw", "train",
-           "PRECOND_BLOCK_JACOBI", "PRECOND_LEARNED", "IbemError"]
+           "PRECOND_BLOCK_JACOBI", "PRECOND_LEARNED", "PRECOND_NEUMANN", "IbemError"]

@@ -1,20 +1,24 @@
-// Learned block preconditioner of the matrix-free solver (no reference counterpart).
+// Learned neighbour-coupled preconditioner of the matrix-free solver (no reference
+// counterpart).
 //
-// For every particle i the preconditioner block is P_i = B_i + sum_e w_e T_e over its 16
-// nearest neighbours j (edges e = (i <- j)), B the block-Jacobi inverse and
-//   T_e = B_i As_ij B_j As_ji B_i,
-// the neighbour's leading contribution to the diagonal block of As^-1 (Neumann series of
-// As = D + O: (As^-1)_ii = B_i + sum_j B_i O_ij B_j O_ji B_i + ...).  A message-passing
-// network predicts the weights w_e from the local geometry (w = 1 is the truncated
-// series, w = 0 block-Jacobi; the trained weights absorb the higher-order terms).
+// With B_i the block-Jacobi inverses and As = D + O split into its diagonal and
+// off-diagonal blocks, the Neumann series As^-1 = B - B O B + B O B O B - ... gives, on the
+// graph of each particle's 16 nearest neighbours j (edges e = (i <- j)),
+//   C_e = -B_i As_ij B_j           (first-order term of (As^-1)_ij)
+//   T_e =  B_i As_ij B_j As_ji B_i  (second-order term of (As^-1)_ii from neighbour j).
+// The preconditioner is block-sparse on that graph:
+//   (P v)_i = (B_i + sum_e w_e T_e) v_i + sum_e alpha_e C_e v_j,
+// with two weights per edge predicted by a message-passing network from the local geometry
+// (w = alpha = 0: block-Jacobi; w = alpha = 1: the truncated series; trained weights absorb
+// the higher-order terms and the neighbours left out).
 //
 // Kernels: k_knn (brute force within a realisation), k_features, k_edge_corr (one CTA of
 // 64 threads per edge: four threads evaluate the two FP32 pair blocks into shared memory,
 // all 64 form the four 24 x 24 products), the network's dense layers as one tiled FP32 GEMM
 // kernel (k_gemm, 64 x 64 tiles, optional transposes, bias, ReLU, atomic split-K for the
 // weight gradients) with gather / scatter / mean kernels around it, the loss and its
-// gradient with respect to w (k_loss), and AdamW (k_adamw).  Training runs these in a
-// host loop (gnn_train) on one batch of realisations.
+// gradient with respect to the edge weights (k_loss), and AdamW (k_adamw).  Training runs
+// these in a host loop (ibem_gnn_train) on one batch of realisations.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -48,8 +52,8 @@ struct Layout {
     }
     w_o1 = take((int64_t)kEin * kH);
     b_o1 = take(kH);
-    w_o2 = take(kH);
-    b_o2 = take(1);
+    w_o2 = take((int64_t)kH * kGnnOut);
+    b_o2 = take(kGnnOut);
     total = o;
   }
 };
@@ -138,31 +142,32 @@ struct SmemSink {
   __device__ __forceinline__ void operator()(int r, int c, float v) const { M[r * kMfNu + c] = v * scale; }
 };
 
-// C = A B for 24 x 24 row-major matrices in shared memory, 64 threads
-__device__ __forceinline__ void mm24(const float* A, const float* B, float* C) {
+// C = sc * A B for 24 x 24 row-major matrices in shared memory
+__device__ __forceinline__ void mm24(const float* A, const float* B, float* C, float sc) {
   for (int e = threadIdx.x; e < kMfNu * kMfNu; e += blockDim.x) {
     const int r = e / kMfNu, c = e % kMfNu;
     float s = 0.f;
 #pragma unroll
     for (int k = 0; k < kMfNu; ++k) s = fmaf(A[r * kMfNu + k], B[k * kMfNu + c], s);
-    C[e] = s;
+    C[e] = sc * s;
   }
 }
 
 __global__ void __launch_bounds__(64)
     k_edge_corr(int num, const int* __restrict__ nbr, const int* __restrict__ seg_of, const SphMatF* __restrict__ mats,
                 const double* __restrict__ cen, const double* __restrict__ rad, const float* __restrict__ B,
-                const float* __restrict__ w, float* __restrict__ P, int nrhs, const float* __restrict__ rq,
-                int64_t N, float* __restrict__ u) {
+                const float* __restrict__ wa, float* __restrict__ D, float* __restrict__ Q, int nrhs,
+                const float* __restrict__ rq, int64_t N, float* __restrict__ u) {
   __shared__ float Aij[kMfNu * kMfNu], Aji[kMfNu * kMfNu], Bi[kMfNu * kMfNu], Bj[kMfNu * kMfNu];
   __shared__ float T1[kMfNu * kMfNu], T2[kMfNu * kMfNu];
   const int64_t e = blockIdx.x;
+  const int64_t E = (int64_t)num * kKnn;
   const int i = (int)(e / kKnn);
   const int j = nbr[e];
   if (j < 0) {  // no neighbour in this slot
     if (u)
-      for (int q = 0; q < nrhs; ++q)
-        for (int r = threadIdx.x; r < kMfNu; r += blockDim.x) u[((int64_t)q * num * kKnn + e) * kMfNu + r] = 0.f;
+      for (int t = threadIdx.x; t < nrhs * 2 * kMfNu; t += blockDim.x)
+        u[((int64_t)(t / (2 * kMfNu)) * E + e) * 2 * kMfNu + t % (2 * kMfNu)] = 0.f;
     return;
   }
   const float* bi = B + (int64_t)kMfNu * kMfNu * i;
@@ -191,27 +196,33 @@ __global__ void __launch_bounds__(64)
     }
   }
   __syncthreads();
-  mm24(Aji, Bi, T1);
+  mm24(Aji, Bi, T1, 1.f);    // As_ji B_i
+  mm24(Aij, Bj, T2, 1.f);    // As_ij B_j
   __syncthreads();
-  mm24(Bj, T1, T2);
+  mm24(Bi, T2, Aij, -1.f);   // C = -B_i As_ij B_j        (As_ij no longer needed)
   __syncthreads();
-  mm24(Aij, T2, T1);
+  mm24(Aij, T1, T2, -1.f);   // T = -C As_ji B_i
   __syncthreads();
-  mm24(Bi, T1, T2);  // T_e
-  __syncthreads();
-  if (P && w) {
-    const float we = w[e];
-    float* pi = P + (int64_t)kMfNu * kMfNu * i;
-    for (int k = threadIdx.x; k < kMfNu * kMfNu; k += blockDim.x) atomicAdd(pi + k, we * T2[k]);
+  if (wa) {
+    const float we = wa[2 * e], ae = wa[2 * e + 1];
+    if (D) {
+      float* di = D + (int64_t)kMfNu * kMfNu * i;
+      for (int k = threadIdx.x; k < kMfNu * kMfNu; k += blockDim.x) atomicAdd(di + k, we * T2[k]);
+    }
+    if (Q) {
+      float* qe = Q + (int64_t)kMfNu * kMfNu * e;
+      for (int k = threadIdx.x; k < kMfNu * kMfNu; k += blockDim.x) qe[k] = ae * Aij[k];
+    }
   }
   if (u && rq) {
-    for (int t = threadIdx.x; t < nrhs * kMfNu; t += blockDim.x) {
-      const int q = t / kMfNu, r = t % kMfNu;
-      const float* rv = rq + (int64_t)q * N + (int64_t)kMfNu * i;
+    for (int t = threadIdx.x; t < nrhs * 2 * kMfNu; t += blockDim.x) {
+      const int q = t / (2 * kMfNu), part = (t / kMfNu) & 1, r = t % kMfNu;
+      const float* rv = rq + (int64_t)q * N + (int64_t)kMfNu * (part ? j : i);
+      const float* M = part ? Aij : T2;
       float s = 0.f;
 #pragma unroll
-      for (int c = 0; c < kMfNu; ++c) s = fmaf(T2[r * kMfNu + c], rv[c], s);
-      u[((int64_t)q * num * kKnn + e) * kMfNu + r] = s;
+      for (int c = 0; c < kMfNu; ++c) s = fmaf(M[r * kMfNu + c], rv[c], s);
+      u[((int64_t)q * E + e) * 2 * kMfNu + part * kMfNu + r] = s;
     }
   }
 }
@@ -395,69 +406,89 @@ __global__ void k_add_left(int num, const float* __restrict__ dHn, const float* 
   if (t >= (int64_t)num * kH) return;
   dH[t] = dHn[t] + dUin[(t / kH) * kUin + t % kH];
 }
-// w[e] = O1[e] . w_o2 + b_o2 (0 for a missing neighbour)
+// out[e][k] = O1[e] . w_o2[:, k] + b_o2[k] (0 for a missing neighbour)
 __global__ void k_out(int64_t E, const int* __restrict__ nbr, const float* __restrict__ O1, const float* __restrict__ w2,
                       const float* __restrict__ b2, float* __restrict__ w) {
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= E) return;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= E * kGnnOut) return;
+  const int64_t e = t / kGnnOut;
+  const int k = (int)(t % kGnnOut);
   if (nbr[e] < 0) {
-    w[e] = 0.f;
+    w[t] = 0.f;
     return;
   }
-  float s = b2[0];
-  for (int c = 0; c < kH; ++c) s = fmaf(O1[e * kH + c], w2[c], s);
-  w[e] = s;
+  float s = b2[k];
+  for (int c = 0; c < kH; ++c) s = fmaf(O1[e * kH + c], w2[c * kGnnOut + k], s);
+  w[t] = s;
 }
-// dO1[e] = dw[e] * w_o2 * (O1 > 0)
+// dO1[e][c] = sum_k dout[e][k] w_o2[c][k] * (O1 > 0)
 __global__ void k_out_bwd(int64_t E, const float* __restrict__ O1, const float* __restrict__ w2,
                           const float* __restrict__ dw, float* __restrict__ dO1) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= E * kH) return;
-  const float o = O1[t];
-  dO1[t] = o > 0.f ? dw[t / kH] * w2[t % kH] : 0.f;
+  const int64_t e = t / kH;
+  const int c = (int)(t % kH);
+  float d = 0.f;
+  for (int k = 0; k < kGnnOut; ++k) d = fmaf(dw[e * kGnnOut + k], w2[c * kGnnOut + k], d);
+  dO1[t] = O1[t] > 0.f ? d : 0.f;
 }
 
-// Loss L = sum_q sum_i ||z_qi + sum_e w_e u_qe||^2 and dL/dw_e; one warp per particle
-__global__ void k_loss(int num, int nrhs, const int* __restrict__ nbr, const float* __restrict__ w,
+// Loss L = sum_q sum_i ||z_qi + sum_e (w_e u_qe + alpha_e v_qe)||^2 and its gradient with
+// respect to (w_e, alpha_e); one warp per particle, lanes over the 24 rows
+__global__ void k_loss(int num, int nrhs, const int* __restrict__ nbr, const float* __restrict__ wa,
                        const float* __restrict__ z, const float* __restrict__ u, double* __restrict__ loss,
                        float* __restrict__ dw) {
   const int i = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
   if (i >= num) return;
   const int64_t E = (int64_t)num * kKnn;
-  float we[kKnn];
+  float we[kKnn], ae[kKnn], gw[kKnn], ga[kKnn];
 #pragma unroll
-  for (int k = 0; k < kKnn; ++k) we[k] = nbr[(int64_t)i * kKnn + k] >= 0 ? w[(int64_t)i * kKnn + k] : 0.f;
-  float g[kKnn];
-#pragma unroll
-  for (int k = 0; k < kKnn; ++k) g[k] = 0.f;
+  for (int k = 0; k < kKnn; ++k) {
+    const bool v = nbr[(int64_t)i * kKnn + k] >= 0;
+    we[k] = v ? wa[2 * ((int64_t)i * kKnn + k)] : 0.f;
+    ae[k] = v ? wa[2 * ((int64_t)i * kKnn + k) + 1] : 0.f;
+    gw[k] = ga[k] = 0.f;
+  }
   double ls = 0;
   for (int q = 0; q < nrhs; ++q) {
     float qv = 0.f;
-    float uk[kKnn];
+    float uk[kKnn], vk[kKnn];
     if (lane < kMfNu) {
       qv = z[(int64_t)q * num * kMfNu + (int64_t)i * kMfNu + lane];
 #pragma unroll
       for (int k = 0; k < kKnn; ++k) {
-        uk[k] = u[((int64_t)q * E + (int64_t)i * kKnn + k) * kMfNu + lane];
-        qv = fmaf(we[k], uk[k], qv);
+        const float* ue = u + ((int64_t)q * E + (int64_t)i * kKnn + k) * 2 * kMfNu;
+        uk[k] = ue[lane];
+        vk[k] = ue[kMfNu + lane];
+        qv = fmaf(we[k], uk[k], fmaf(ae[k], vk[k], qv));
       }
     } else {
 #pragma unroll
-      for (int k = 0; k < kKnn; ++k) uk[k] = 0.f;
+      for (int k = 0; k < kKnn; ++k) uk[k] = vk[k] = 0.f;
     }
     ls += (double)qv * qv;
 #pragma unroll
-    for (int k = 0; k < kKnn; ++k) g[k] = fmaf(2.f * qv, uk[k], g[k]);
+    for (int k = 0; k < kKnn; ++k) {
+      gw[k] = fmaf(2.f * qv, uk[k], gw[k]);
+      ga[k] = fmaf(2.f * qv, vk[k], ga[k]);
+    }
   }
 #pragma unroll
   for (int k = 0; k < kKnn; ++k)
-    for (int o = 16; o; o >>= 1) g[k] += __shfl_xor_sync(0xffffffffu, g[k], o);
+    for (int o = 16; o; o >>= 1) {
+      gw[k] += __shfl_xor_sync(0xffffffffu, gw[k], o);
+      ga[k] += __shfl_xor_sync(0xffffffffu, ga[k], o);
+    }
   for (int o = 16; o; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
   if (lane == 0) {
     atomicAdd(loss, ls);
 #pragma unroll
-    for (int k = 0; k < kKnn; ++k) dw[(int64_t)i * kKnn + k] = nbr[(int64_t)i * kKnn + k] >= 0 ? g[k] : 0.f;
+    for (int k = 0; k < kKnn; ++k) {
+      const bool v = nbr[(int64_t)i * kKnn + k] >= 0;
+      dw[2 * ((int64_t)i * kKnn + k)] = v ? gw[k] : 0.f;
+      dw[2 * ((int64_t)i * kKnn + k) + 1] = v ? ga[k] : 0.f;
+    }
   }
 }
 
@@ -504,9 +535,9 @@ struct Net {
     }
     if (!s) s = buf(Oin, E * kEin);
     if (!s) s = buf(O1, E * kH);
-    if (!s) s = buf(w, E);
+    if (!s) s = buf(w, E * kGnnOut);
     if (backward) {
-      if (!s) s = buf(dw, E);
+      if (!s) s = buf(dw, E * kGnnOut);
       if (!s) s = buf(dO1, E * kH);
       if (!s) s = buf(dEin, E * kEin);
       if (!s) s = buf(dH, (int64_t)num * kH);
@@ -545,15 +576,15 @@ struct Net {
     }
     ::ibem::count_launch(), k_gather_edges<<<nb(E * kEin), 256, 0, st>>>(E, nbr, H[kGnnLayers], ef, Oin);
     gemm((int)E, kH, kEin, Oin, kEin, P + L.w_o1, kH, O1, kH, P + L.b_o1, 1);
-    ::ibem::count_launch(), k_out<<<nb(E), 256, 0, st>>>(E, nbr, O1, P + L.w_o2, P + L.b_o2, w);
+    ::ibem::count_launch(), k_out<<<nb(E * kGnnOut), 256, 0, st>>>(E, nbr, O1, P + L.w_o2, P + L.b_o2, w);
     IBEM_LAUNCH_CHECK("gnn forward");
     return IBEM_OK;
   }
   // gradient of the parameters from dw (set by the loss); G zeroed here
   ibem_status backward(const int* nbr, const float* xn, const float* P, float* G) {
     IBEM_CUDA(cudaMemsetAsync(G, 0, sizeof(float) * L.total, st));
-    // w = O1 w_o2 + b_o2 (dw is 0 on missing neighbours)
-    gemm_dw((int)E, 1, kH, O1, dw, G + L.w_o2, G + L.b_o2);
+    // out = O1 w_o2 + b_o2 (dw is 0 on missing neighbours)
+    gemm_dw((int)E, kGnnOut, kH, O1, dw, G + L.w_o2, G + L.b_o2);
     ::ibem::count_launch(), k_out_bwd<<<nb(E * kH), 256, 0, st>>>(E, O1, P + L.w_o2, dw, dO1);
     gemm_dw((int)E, kH, kEin, Oin, dO1, G + L.w_o1, G + L.b_o1);
     gemm_dx((int)E, kH, kEin, dO1, P + L.w_o1, dEin);
@@ -631,43 +662,53 @@ ibem_status gnn_features(const MfBatch& b, const int* nbr, float* xn, float* ef,
   return IBEM_OK;
 }
 
-ibem_status gnn_edge_corrections(const MfBatch& b, const int* nbr, const float* B, const float* w, float* P, int nrhs,
-                                 const float* r, float* u, cudaStream_t st) {
+ibem_status gnn_edge_corrections(const MfBatch& b, const int* nbr, const float* B, const float* wa, float* D, float* Q,
+                                 int nrhs, const float* r, float* u, cudaStream_t st) {
   const int64_t E = (int64_t)b.num * kKnn;
-  ::ibem::count_launch(), k_edge_corr<<<(unsigned)E, 64, 0, st>>>(b.num, nbr, b.seg_of, b.matf, b.cen, b.rad, B, w, P,
-                                                                  nrhs, r, b.N, u);
+  ::ibem::count_launch(), k_edge_corr<<<(unsigned)E, 64, 0, st>>>(b.num, nbr, b.seg_of, b.matf, b.cen, b.rad, B, wa, D,
+                                                                  Q, nrhs, r, b.N, u);
   IBEM_LAUNCH_CHECK("edge corrections");
   return IBEM_OK;
 }
 
 ibem_status gnn_forward_weights(int num, const int* nbr, const float* xn, const float* ef, const float* params, float* w,
-                                cudaStream_t st) {
+                                cudaStream_t st) {  // w: num * kKnn x kGnnOut
   Net net;
   net.num = num;
   net.E = (int64_t)num * kKnn;
   net.st = st;
   ibem_status s = net.alloc(false);
   if (!s) s = net.forward(nbr, xn, ef, params);
-  if (!s) IBEM_CUDA(cudaMemcpyAsync(w, net.w, sizeof(float) * net.E, cudaMemcpyDeviceToDevice, st));
+  if (!s) IBEM_CUDA(cudaMemcpyAsync(w, net.w, sizeof(float) * net.E * kGnnOut, cudaMemcpyDeviceToDevice, st));
   if (!s) IBEM_CUDA(cudaStreamSynchronize(st));
   return s;
 }
 
-// P (block-Jacobi on entry) += sum_e w_e T_e with the network's weights
-ibem_status mf_learned_blocks(const MfBatch& b, const float* params, float* P, cudaStream_t st) {
+__global__ void k_fill1(int64_t n, float* __restrict__ p) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 1.f;
+}
+
+ibem_status mf_neighbour_precond(const MfBatch& b, const float* params, MfPrecond& pc, cudaStream_t st) {
   Prepared pr;
   const int64_t E = (int64_t)b.num * kKnn;
-  ibem_status s = pr.buf(pr.nbr, E);
-  if (!s) s = pr.buf(pr.xn, (int64_t)b.num * kGnnNodeF);
-  if (!s) s = pr.buf(pr.ef, E * kGnnEdgeF);
-  float* w = nullptr;
-  if (!s) s = pr.buf(w, E);
+  IBEM_CUDA(cudaMalloc(&pc.nbr, sizeof(int) * E));
+  IBEM_CUDA(cudaMalloc(&pc.Q, sizeof(float) * E * kMfNu * kMfNu));
+  pr.nbr = pc.nbr;
+  float* wa = nullptr;
+  ibem_status s = pr.buf(wa, E * kGnnOut);
   if (!s) s = pr.buf(pr.B, (int64_t)b.num * kMfNu * kMfNu);
-  if (!s) s = gnn_knn(b, pr.nbr, st);
-  if (!s) s = gnn_features(b, pr.nbr, pr.xn, pr.ef, st);
-  if (!s) s = gnn_forward_weights(b.num, pr.nbr, pr.xn, pr.ef, params, w, st);
-  if (!s) IBEM_CUDA(cudaMemcpyAsync(pr.B, P, sizeof(float) * b.num * kMfNu * kMfNu, cudaMemcpyDeviceToDevice, st));
-  if (!s) s = gnn_edge_corrections(b, pr.nbr, pr.B, w, P, 0, nullptr, nullptr, st);
+  if (!s) s = gnn_knn(b, pc.nbr, st);
+  if (!s && params) {
+    if (!s) s = pr.buf(pr.xn, (int64_t)b.num * kGnnNodeF);
+    if (!s) s = pr.buf(pr.ef, E * kGnnEdgeF);
+    if (!s) s = gnn_features(b, pc.nbr, pr.xn, pr.ef, st);
+    if (!s) s = gnn_forward_weights(b.num, pc.nbr, pr.xn, pr.ef, params, wa, st);
+  } else if (!s) {
+    ::ibem::count_launch(), k_fill1<<<nb(E * kGnnOut), 256, 0, st>>>(E * kGnnOut, wa);
+  }
+  if (!s) IBEM_CUDA(cudaMemcpyAsync(pr.B, pc.D, sizeof(float) * b.num * kMfNu * kMfNu, cudaMemcpyDeviceToDevice, st));
+  if (!s) s = gnn_edge_corrections(b, pc.nbr, pr.B, wa, pc.D, pc.Q, 0, nullptr, nullptr, st);
   if (!s) IBEM_CUDA(cudaStreamSynchronize(st));
   return s;
 }
@@ -686,7 +727,7 @@ ibem_status prepare(const MfBatch& b, int nrhs, const double* r, const double* e
   if (!s && !pr.xn) s = pr.buf(pr.xn, (int64_t)b.num * kGnnNodeF);
   if (!s && !pr.ef) s = pr.buf(pr.ef, E * kGnnEdgeF);
   if (!s && nrhs > 0 && !pr.z) s = pr.buf(pr.z, (int64_t)nrhs * b.N);
-  if (!s && nrhs > 0 && !pr.u) s = pr.buf(pr.u, (int64_t)nrhs * E * kMfNu);
+  if (!s && nrhs > 0 && !pr.u) s = pr.buf(pr.u, (int64_t)nrhs * E * 2 * kMfNu);
   if (!s) s = pr.buf(pr.B, (int64_t)b.num * kMfNu * kMfNu);
   if (!s) s = gnn_knn(b, pr.nbr, st);
   if (!s) s = gnn_features(b, pr.nbr, pr.xn, pr.ef, st);
@@ -704,7 +745,7 @@ ibem_status prepare(const MfBatch& b, int nrhs, const double* r, const double* e
         ::ibem::count_launch(), k_sample_z<<<nb(b.N), 256, 0, st>>>(b.num, pr.B, r + (int64_t)q * b.N, e + (int64_t)q * b.N,
                                                                      sc, pr.z + (int64_t)q * b.N, rf + (int64_t)q * b.N);
       IBEM_LAUNCH_CHECK("gnn samples");
-      s = gnn_edge_corrections(b, pr.nbr, pr.B, nullptr, nullptr, nrhs, rf, pr.u, st);
+      s = gnn_edge_corrections(b, pr.nbr, pr.B, nullptr, nullptr, nullptr, nrhs, rf, pr.u, st);
     }
   }
   if (!s) IBEM_CUDA(cudaStreamSynchronize(st));

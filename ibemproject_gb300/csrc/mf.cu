@@ -240,18 +240,31 @@ __global__ void __launch_bounds__(32) k_block_jacobi(const int* __restrict__ seg
   for (int i = t; i < kMfNu * kMfNu; i += 32) o[i] = (float)M[i / kMfNu][kMfNu + i % kMfNu];
 }
 
-// z[p] = P[p] v[p] (24 x 24 row-major blocks); one thread per row
-__global__ void k_bdiag_apply(int num, const float* __restrict__ P, const float* __restrict__ v, float* __restrict__ z) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= (int64_t)num * kMfNu) return;
-  const int64_t p = t / kMfNu;
-  const float4* row = reinterpret_cast<const float4*>(P + t * kMfNu);
-  const float4* vv = reinterpret_cast<const float4*>(v + p * kMfNu);
+// z = P v for the block-sparse preconditioner: z_p = D_p v_p + sum_slot Q_(p,slot) v_nbr;
+// one thread per row (24 x 24 row-major blocks, float4 loads)
+__device__ __forceinline__ float dot24(const float* __restrict__ a, const float* __restrict__ b) {
+  const float4* x = reinterpret_cast<const float4*>(a);
+  const float4* y = reinterpret_cast<const float4*>(b);
   float s = 0.f;
 #pragma unroll
   for (int c = 0; c < kMfNu / 4; ++c) {
-    const float4 a = row[c], b = vv[c];
-    s = fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, fmaf(a.w, b.w, s))));
+    const float4 u = x[c], v = y[c];
+    s = fmaf(u.x, v.x, fmaf(u.y, v.y, fmaf(u.z, v.z, fmaf(u.w, v.w, s))));
+  }
+  return s;
+}
+__global__ void k_precond_apply(int num, const float* __restrict__ D, const float* __restrict__ Q,
+                                const int* __restrict__ nbr, const float* __restrict__ v, float* __restrict__ z) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)num * kMfNu) return;
+  const int64_t p = t / kMfNu;
+  const int r = (int)(t % kMfNu);
+  float s = dot24(D + t * kMfNu, v + p * kMfNu);
+  if (Q) {
+    for (int k = 0; k < kKnn; ++k) {
+      const int j = nbr[p * kKnn + k];
+      if (j >= 0) s += dot24(Q + ((p * kKnn + k) * kMfNu + r) * kMfNu, v + (int64_t)j * kMfNu);
+    }
   }
   z[t] = s;
 }
@@ -651,7 +664,7 @@ struct MfSolver {
   // FP32 GMRES(m) with restarts on As d = rin, right-preconditioned by P; d overwritten.
   // Realisations flagged in `done` take no step.  Stops each realisation once
   // ||rin - As d|| <= inner_tol ||rin|| (Arnoldi estimate).
-  ibem_status gmres(const float* P, int max_cycles, double inner_tol) {
+  ibem_status gmres(const MfPrecond& P, int max_cycles, double inner_tol) {
     const int S = b.nseg;
     ibem_status s = IBEM_OK;
     IBEM_CUDA(cudaMemsetAsync(d, 0, sizeof(float) * N, st));
@@ -673,7 +686,7 @@ struct MfSolver {
       while (k < m) {
         float* vk = V + (int64_t)k * N;
         float* wv = V + (int64_t)(k + 1) * N;
-        ::ibem::count_launch(), k_bdiag_apply<<<nblk(N), 256, 0, st>>>(b.num, P, vk, z);
+        ::ibem::count_launch(), k_precond_apply<<<nblk(N), 256, 0, st>>>(b.num, P.D, P.Q, P.nbr, vk, z);
         if ((s = mf_apply_f32(b, z, wv, st))) break;
         {
           ProfScope pg(PROF_GMRES_OTHER, st);
@@ -696,7 +709,7 @@ struct MfSolver {
       ::ibem::count_launch(), k_hess_solve<<<nblk(S, 128), 128, 0, st>>>(S, m, K);
       IBEM_CUDA(cudaMemsetAsync(w, 0, sizeof(float) * N, st));
       ::ibem::count_launch(), k_seg_combine<<<nblk(N), 256, 0, st>>>(N, b.seg_of, k, V, N, K.yv, m, w);
-      ::ibem::count_launch(), k_bdiag_apply<<<nblk(N), 256, 0, st>>>(b.num, P, w, z);
+      ::ibem::count_launch(), k_precond_apply<<<nblk(N), 256, 0, st>>>(b.num, P.D, P.Q, P.nbr, w, z);
       ::ibem::count_launch(), k_add_f32<<<nblk(N), 256, 0, st>>>(N, z, d);
       IBEM_LAUNCH_CHECK("gmres update");
     }
@@ -710,7 +723,7 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 
 }  // namespace
 
-ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const float* P, const ibem_mf_options& o,
+ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPrecond& P, const ibem_mf_options& o,
                      ibem_mf_report* rep, cudaStream_t st) {
   const auto t0 = std::chrono::steady_clock::now();
   const int S = b.nseg;
@@ -831,15 +844,12 @@ extern "C" ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int preci
   return s;
 }
 
-namespace ibem {
-ibem_status mf_learned_blocks(const MfBatch& b, const float* params, float* P, cudaStream_t st);
-}
-
 extern "C" ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const double* b_dev, double* x_dev,
                                          ibem_precond pc, const float* gnn_params_dev, const ibem_mf_options* opt,
                                          ibem_mf_report* reports, void* stream) {
   if (!batch || !b_dev || !x_dev || !reports) return fail(IBEM_ERR_ARG, "mf_solve: bad arguments");
-  if (pc != IBEM_PRECOND_BLOCK_JACOBI && pc != IBEM_PRECOND_LEARNED) return fail(IBEM_ERR_ARG, "mf_solve: preconditioner");
+  if (pc != IBEM_PRECOND_BLOCK_JACOBI && pc != IBEM_PRECOND_LEARNED && pc != IBEM_PRECOND_NEUMANN)
+    return fail(IBEM_ERR_ARG, "mf_solve: preconditioner");
   if (pc == IBEM_PRECOND_LEARNED && !gnn_params_dev) return fail(IBEM_ERR_ARG, "mf_solve: learned form needs parameters");
   ibem_mf_options o{};
   if (opt) o = *opt;
@@ -853,13 +863,14 @@ extern "C" ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const doub
   const auto t0 = std::chrono::steady_clock::now();
   MfBatch b;
   ibem_status s = mf_batch_init(b, *batch, st);
-  float* P = nullptr;
+  MfPrecond P;
   if (!s) {
-    const cudaError_t e = cudaMalloc(&P, sizeof(float) * kMfNu * kMfNu * (size_t)b.num);
+    const cudaError_t e = cudaMalloc(&P.D, sizeof(float) * kMfNu * kMfNu * (size_t)b.num);
     if (e != cudaSuccess) s = cuda_fail(e, "mf_solve: preconditioner blocks");
   }
-  if (!s) s = mf_block_jacobi(b, P, st);
-  if (!s && pc == IBEM_PRECOND_LEARNED) s = mf_learned_blocks(b, gnn_params_dev, P, st);
+  if (!s) s = mf_block_jacobi(b, P.D, st);
+  if (!s && pc != IBEM_PRECOND_BLOCK_JACOBI)
+    s = mf_neighbour_precond(b, pc == IBEM_PRECOND_LEARNED ? gnn_params_dev : nullptr, P, st);
   if (!s) {
     const cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) s = cuda_fail(e, "mf_solve: set-up");
@@ -868,7 +879,9 @@ extern "C" ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const doub
   for (int i = 0; i < batch->nseg; ++i) reports[i] = ibem_mf_report{};
   if (!s) s = mf_solve(b, b_dev, x_dev, P, o, reports, st);
   for (int i = 0; i < batch->nseg; ++i) reports[i].t_setup_ms = tset;
-  cudaFree(P);
+  cudaFree(P.D);
+  cudaFree(P.Q);
+  cudaFree(P.nbr);
   mf_batch_free(b);
   return s;
 }

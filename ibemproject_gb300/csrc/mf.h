@@ -55,25 +55,39 @@ void mf_batch_free(MfBatch& b);
 
 // y = As x (FP32, scaled system); y is overwritten
 ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_t st);
+
+// Block-sparse preconditioner on the k-nearest-neighbour graph:
+//   (P v)_i = D_i v_i + sum_slot Q_(i,slot) v_nbr(i,slot)
+struct MfPrecond {
+  float* D = nullptr;    // num x 24 x 24 diagonal blocks (row-major)
+  float* Q = nullptr;    // num*kKnn x 24 x 24 off-diagonal blocks, or nullptr (block-diagonal)
+  int* nbr = nullptr;    // num*kKnn neighbour indices (-1: empty slot)
+};
 // y = A x (FP64, physical units); y is overwritten
 ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st);
 // P[p] = inverse of the scaled diagonal block As[p, p] (24 x 24, row-major, FP32)
 ibem_status mf_block_jacobi(const MfBatch& b, float* P, cudaStream_t st);
 
 // ---- learned preconditioner (gnn.cu) ----
-constexpr int kGnnHidden = 64, kGnnLayers = 3, kGnnNodeF = 10, kGnnEdgeF = 7;
+constexpr int kGnnHidden = 64, kGnnLayers = 3, kGnnNodeF = 10, kGnnEdgeF = 7, kGnnOut = 2;
 int64_t gnn_param_count();
 // k nearest neighbours within each segment (by centre distance, ties to the lower index);
 // nbr[p * kKnn + j] = neighbour index or -1
 ibem_status gnn_knn(const MfBatch& b, int* nbr, cudaStream_t st);
 ibem_status gnn_features(const MfBatch& b, const int* nbr, float* xn, float* ef, cudaStream_t st);
-// Edge corrections T_e = B_i As_ij B_j As_ji B_i for every edge e = (i <- j):
-//   P[i] += w_e T_e  when w != nullptr (P holds B on entry),
-//   u[q][e] = T_e r_q[i] for q < nrhs when r != nullptr.
-ibem_status gnn_edge_corrections(const MfBatch& b, const int* nbr, const float* B, const float* w, float* P,
-                                 int nrhs, const float* r, float* u, cudaStream_t st);
-// Edge weights of the network (forward only); w has num * kKnn entries
+// Neumann blocks of every edge e = (i <- j), B the block-Jacobi inverses:
+//   C_e = -B_i As_ij B_j          (first-order term of (As^-1)_ij)
+//   T_e =  B_i As_ij B_j As_ji B_i (second-order term of (As^-1)_ii)
+// With weights wa (num*kKnn x 2: w_e, alpha_e): D[i] += w_e T_e (D holds B on entry) and
+// Q[e] = alpha_e C_e.  With samples r (nrhs x N): u[q][e] = (T_e r_qi, C_e r_qj).
+ibem_status gnn_edge_corrections(const MfBatch& b, const int* nbr, const float* B, const float* wa, float* D,
+                                 float* Q, int nrhs, const float* r, float* u, cudaStream_t st);
+// Edge outputs (w_e, alpha_e) of the network (forward only): num * kKnn x 2
 ibem_status gnn_forward_weights(int num, const int* nbr, const float* xn, const float* ef, const float* params,
-                                float* w, cudaStream_t st);
+                                float* wa, cudaStream_t st);
+// The neighbour-coupled preconditioner of a batch: block-Jacobi plus the Neumann blocks
+// weighted by the network (params) or all weighted 1 (params == nullptr).  D must hold
+// the block-Jacobi inverses; Q and nbr are allocated here (freed by the caller).
+ibem_status mf_neighbour_precond(const MfBatch& b, const float* params, MfPrecond& pc, cudaStream_t st);
 
 }  // namespace ibem

@@ -195,7 +195,8 @@ typedef struct {
 
 typedef enum {
   IBEM_PRECOND_BLOCK_JACOBI = 0, /* inverse of each particle's own 24 x 24 block */
-  IBEM_PRECOND_LEARNED = 1       /* block-Jacobi + GNN-weighted neighbour corrections */
+  IBEM_PRECOND_LEARNED = 1,      /* block-Jacobi + GNN-weighted Neumann blocks on the kNN graph */
+  IBEM_PRECOND_NEUMANN = 2       /* the same blocks with every weight 1 (no network) */
 } ibem_precond;
 
 typedef struct {
@@ -247,28 +248,33 @@ ibem_status ibem_e3d_effective_modulus(const ibem_e3d_batch* batch, const double
                                        double* mean_strain, double* e_eff, void* stream);
 
 /* ---- learned preconditioner (no reference counterpart) --------------------- */
-/* A message-passing network over each particle's 16 nearest neighbours predicts one
- * weight w_e per edge e = (i <- j); the preconditioner block of particle i is
- *   P_i = B_i + sum_e w_e T_e,   T_e = B_i As_ij B_j As_ji B_i,
- * B the block-Jacobi inverse and As the scaled pair blocks (the leading term of the
- * diagonal block of As^-1 coming from neighbour j).  Inputs: node features (dim 10: semi-
- * axes / radius, orientation quaternion, E1/(10 E0), nu0, nu1) and edge features (dim 7:
- * offset / a_i, distance / a_i, a_j / a_i, gap / a_i, (2 a_i / distance)^3).  Network:
- * h = relu(W_in x + b); 3 layers of m_e = relu(W_m [h_i, h_j, f_e] + b),
- * h_i += relu(W_u [h_i, mean_e m_e] + b); w_e = W_o2 relu(W_o1 [h_i, h_j, f_e] + b) + b_o2.
+/* On the graph of each particle's 16 nearest neighbours (edges e = (i <- j)), with B the
+ * block-Jacobi inverses and As the scaled pair blocks, the Neumann series of As^-1 gives
+ *   C_e = -B_i As_ij B_j            (first-order term of (As^-1)_ij)
+ *   T_e =  B_i As_ij B_j As_ji B_i   (second-order term of (As^-1)_ii from j).
+ * The preconditioner is block-sparse on that graph:
+ *   (P v)_i = (B_i + sum_e w_e T_e) v_i + sum_e alpha_e C_e v_j,
+ * and a message-passing network predicts the two weights (w_e, alpha_e) of every edge.
+ * Inputs: node features (dim 10: semi-axes / radius, orientation quaternion, E1/(10 E0),
+ * nu0, nu1) and edge features (dim 7: offset / a_i, distance / a_i, a_j / a_i, gap / a_i,
+ * (2 a_i / distance)^3).  Network: h = relu(W_in x + b); 3 layers of
+ * m_e = relu(W_m [h_i, h_j, f_e] + b), h_i += relu(W_u [h_i, mean_e m_e] + b);
+ * (w_e, alpha_e) = W_o2 relu(W_o1 [h_i, h_j, f_e] + b) + b_o2.  Hidden width 64.
  * Parameters: one flat FP32 array of ibem_gnn_param_count() values (W row-major
- * in x out, each followed by its bias, in the order above). */
+ * fan-in x fan-out, each followed by its bias, in the order above). */
 int64_t ibem_gnn_param_count(void);
 
-/* Seeded initialisation (uniform +-1/sqrt(fan_in), output layer zero: P = block-Jacobi). */
+/* Seeded initialisation (uniform +-1/sqrt(fan_in); output layer zero, so that the untrained
+ * network gives w = alpha = 0, i.e. block-Jacobi). */
 ibem_status ibem_gnn_init_params(float* params_dev, uint64_t seed, void* stream);
 
 /* Graph, features and training projections of a batch.  nbr_dev: num*16 ints (-1 when a
  * realisation has fewer than 17 particles); node_feat_dev num*10; edge_feat_dev num*16*7.
  * With nrhs > 0 pairs (r_hat, e_hat) of the scaled system (e_hat = As^-1 r_hat, FP64,
- * nrhs x N each), z_dev (nrhs x N) = B r - e and u_dev (nrhs x num*16 x 24) = T_e r_i, both
- * divided by sqrt(sum ||e||^2), so that the training loss is
- *   L = sum_q sum_i || z_qi + sum_e w_e u_qe ||^2  (relative squared error of P r vs e). */
+ * nrhs x N each): z_dev (nrhs x N) = B r - e, and u_dev (nrhs x num*16 x 2 x 24) holds
+ * (T_e r_i, C_e r_j) for every edge, all divided by sqrt(sum ||e||^2), so that the
+ * training loss is the relative squared error of P r against e:
+ *   L = sum_q sum_i || z_qi + sum_e (w_e u_qe0 + alpha_e u_qe1) ||^2. */
 ibem_status ibem_gnn_prepare(const ibem_e3d_batch* batch, int nrhs, const double* r_hat_dev,
                              const double* e_hat_dev, int* nbr_dev, float* node_feat_dev,
                              float* edge_feat_dev, float* z_dev, float* u_dev, void* stream);
@@ -279,7 +285,7 @@ ibem_status ibem_gnn_loss_grad(int num, const int* nbr_dev, const float* node_fe
                                const float* u_dev, const float* params_dev, double* loss,
                                float* grad_dev, void* stream);
 
-/* Edge weights w (num*16) of the network (forward pass only). */
+/* Edge weights (w_e, alpha_e) of the network, num*16 x 2 (forward pass only). */
 ibem_status ibem_gnn_edge_weights(int num, const int* nbr_dev, const float* node_feat_dev,
                                   const float* edge_feat_dev, const float* params_dev, float* w_dev,
                                   void* stream);

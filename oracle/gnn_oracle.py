@@ -10,17 +10,17 @@ ibem_gnn_param_count in include/ibem_gb300.h:
     for 3 layers:
         m_e = relu([h_i, h_j, f_e] W_m + b_m)                   edge e = (i <- j), f_e (7)
         h_i = h_i + relu([h_i, mean_e m_e] W_u + b_u)
-    w_e = relu([h_i, h_j, f_e] W_o1 + b_o1) . w_o2 + b_o2
-    L   = sum_q sum_i || z_qi + sum_e w_e u_qe ||^2
+    (w_e, alpha_e) = relu([h_i, h_j, f_e] W_o1 + b_o1) W_o2 + b_o2
+    L   = sum_q sum_i || z_qi + sum_e (w_e u_qe0 + alpha_e u_qe1) ||^2
 
-Missing neighbours (index -1) are left out of the mean and get w_e = 0.  Parameters are one
+Missing neighbours (index -1) are left out of the mean and get w_e = alpha_e = 0.  Parameters are one
 flat vector, every W row-major (fan-in x fan-out) followed by its bias, in the order above.
 """
 from __future__ import annotations
 
 import numpy as np
 
-H, LAYERS, KNN, NODE_F, EDGE_F, NU = 64, 3, 16, 10, 7, 24
+H, LAYERS, KNN, NODE_F, EDGE_F, NU, OUT = 64, 3, 16, 10, 7, 24, 2
 EIN = 2 * H + EDGE_F
 UIN = 2 * H
 
@@ -30,7 +30,7 @@ def layout():
     out = [("w_in", (NODE_F, H)), ("b_in", (H,))]
     for l in range(LAYERS):
         out += [(f"w_m{l}", (EIN, H)), (f"b_m{l}", (H,)), (f"w_u{l}", (UIN, H)), (f"b_u{l}", (H,))]
-    out += [("w_o1", (EIN, H)), ("b_o1", (H,)), ("w_o2", (H,)), ("b_o2", (1,))]
+    out += [("w_o1", (EIN, H)), ("b_o1", (H,)), ("w_o2", (H, OUT)), ("b_o2", (OUT,))]
     return out
 
 
@@ -48,7 +48,7 @@ def unpack(p):
 
 
 def forward(p, nbr, xn, ef):
-    """Edge weights w (num * 16) for parameters p (torch float64 vector)."""
+    """Edge weights (num * 16, 2) for parameters p (torch float64 vector)."""
     import torch
     P = unpack(p)
     num = xn.shape[0]
@@ -71,15 +71,15 @@ def forward(p, nbr, xn, ef):
         h = h + torch.relu(torch.cat([h, agg], dim=1) @ P[f"w_u{l}"] + P[f"b_u{l}"])
     o1 = torch.relu(edge_in(h) @ P["w_o1"] + P["b_o1"])
     w = o1 @ P["w_o2"] + P["b_o2"]
-    return (w * valid.to(p.dtype)).reshape(-1)
+    return (w * valid.unsqueeze(2).to(p.dtype)).reshape(-1, OUT)
 
 
 def loss(p, nbr, xn, ef, z, u):
-    """z: (nrhs, num, 24); u: (nrhs, num*16, 24)."""
+    """z: (nrhs, num, 24); u: (nrhs, num*16, 2, 24)."""
     w = forward(p, nbr, xn, ef)
     num = xn.shape[0]
     nrhs = z.shape[0]
-    corr = (w.reshape(1, num, KNN, 1) * u.reshape(nrhs, num, KNN, NU)).sum(2)
+    corr = (w.reshape(1, num, KNN, OUT, 1) * u.reshape(nrhs, num, KNN, OUT, NU)).sum((2, 3))
     return ((z + corr) ** 2).sum()
 
 
@@ -91,7 +91,7 @@ def loss_and_grad(p_np, nbr_np, xn_np, ef_np, z_np, u_np):
     p = t(p_np).requires_grad_(True)
     nrhs = z_np.size // (num * NU)
     L = loss(p, torch.from_numpy(np.asarray(nbr_np)), t(xn_np).reshape(num, NODE_F), t(ef_np),
-             t(z_np).reshape(nrhs, num, NU), t(u_np).reshape(nrhs, num * KNN, NU))
+             t(z_np).reshape(nrhs, num, NU), t(u_np).reshape(nrhs, num * KNN, OUT, NU))
     L.backward()
     return float(L.detach()), p.grad.numpy().copy()
 

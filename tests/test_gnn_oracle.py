@@ -17,7 +17,7 @@ def small_graph(num=12, nrhs=2, seed=0):
     xn = rng.standard_normal((num, go.NODE_F))
     ef = rng.standard_normal((num * go.KNN, go.EDGE_F)) * (nbr.reshape(-1, 1) >= 0)
     z = rng.standard_normal((nrhs, num, go.NU))
-    u = rng.standard_normal((nrhs, num * go.KNN, go.NU)) * 0.3
+    u = rng.standard_normal((nrhs, num * go.KNN, go.OUT, go.NU)) * 0.3
     p = rng.uniform(-0.2, 0.2, go.param_count())
     return p, nbr.ravel(), xn.ravel(), ef.ravel(), z.ravel(), u.ravel()
 
@@ -28,7 +28,7 @@ def test_oracle_gradient_matches_finite_differences():
     rng = np.random.default_rng(1)
     idx = rng.choice(p.size, 40, replace=False)
     # include the output layer and a first-layer weight
-    idx = np.concatenate([idx, [p.size - 1, p.size - 2, 0]])
+    idx = np.concatenate([idx, [p.size - 1, p.size - 2, p.size - 3, 0]])
     h = 1e-6
     for i in idx:
         pp, pm = p.copy(), p.copy()
@@ -45,6 +45,7 @@ def test_missing_neighbours_get_zero_weight():
                    torch.from_numpy(ef)).numpy()
     assert np.all(w[nbr < 0] == 0)
     assert np.any(w[nbr >= 0] != 0)
+    assert w.shape == (nbr.size, go.OUT)
 
 
 def test_oracle_adamw_matches_torch():

@@ -84,7 +84,7 @@ def test_gnn_graph_features_and_projections(B):
     rn, en = r.cpu().numpy(), e.cpu().numpy()
     k = 1.0 / np.sqrt((en ** 2).sum())
     z = pr["z"].cpu().numpy()[:2 * bt.N].reshape(2, bt.N)
-    u = pr["u"].cpu().numpy()[:2 * bt.num * B.KNN * 24].reshape(2, bt.num * B.KNN, 24)
+    u = pr["u"].cpu().numpy()[:2 * bt.num * B.KNN * 48].reshape(2, bt.num * B.KNN, 2, 24)
     for s, c in enumerate(cs):
         p0, p1 = int(bt.seg_begin[s]), int(bt.seg_begin[s + 1])
         A = B.dense_system(c).cpu().numpy().T
@@ -114,10 +114,13 @@ def test_gnn_graph_features_and_projections(B):
                 fe = [*d, dist, R[j] / R[p], dist - 1 - R[j] / R[p], (2 / dist) ** 3]
                 np.testing.assert_allclose(ef[p, slot], fe, rtol=1e-5, atol=1e-6)
                 jj = j - p0
-                T = Binv[i] @ blk(i, jj) @ Binv[jj] @ blk(jj, i) @ Binv[i]
+                Cn = -Binv[i] @ blk(i, jj) @ Binv[jj]
+                T = -Cn @ blk(jj, i) @ Binv[i]
                 for q in range(2):
                     ur = T @ rn[q, 24 * p:24 * p + 24] * k
-                    assert np.abs(u[q, eidx] - ur).max() <= 2e-4 * np.abs(ur).max() + 1e-9
+                    vr = Cn @ rn[q, 24 * j:24 * j + 24] * k
+                    assert np.abs(u[q, eidx, 0] - ur).max() <= 2e-4 * np.abs(ur).max() + 1e-9
+                    assert np.abs(u[q, eidx, 1] - vr).max() <= 2e-4 * np.abs(vr).max() + 1e-9
 
 
 def _random_problem(B, seed=0):
@@ -133,7 +136,7 @@ def test_gnn_loss_and_gradient_match_oracle(B):
     bt, pr = _random_problem(B)
     rng = np.random.default_rng(7)
     p = B.init_params(seed=3).cpu().numpy().astype(np.float64)
-    n_out = go.H + 1
+    n_out = go.H * go.OUT + go.OUT
     p[-n_out:] = rng.uniform(-0.3, 0.3, n_out)   # a non-zero output layer: every block gets gradient
     pt = torch.from_numpy(p.astype(np.float32)).cuda()
     L, g = B.loss_grad(pr, bt.num, pt)
@@ -142,11 +145,11 @@ def test_gnn_loss_and_gradient_match_oracle(B):
     Lo, go_ = go.loss_and_grad(pt.cpu().numpy().astype(np.float64), pr["nbr"].cpu().numpy(),
                                pr["xn"].cpu().numpy(), pr["ef"].cpu().numpy(),
                                pr["z"].cpu().numpy()[:nrhs * bt.N].astype(np.float64),
-                               pr["u"].cpu().numpy()[:nrhs * bt.num * B.KNN * 24].astype(np.float64))
+                               pr["u"].cpu().numpy()[:nrhs * bt.num * B.KNN * 48].astype(np.float64))
     assert abs(L - Lo) <= 1e-4 * abs(Lo)
     assert np.abs(g - go_).max() <= 1e-4 * np.abs(go_).max()
     # weights of the forward pass alone
-    w = B.edge_weights(pr, bt.num, pt).cpu().numpy()
+    w = B.edge_weights(pr, bt.num, pt).cpu().numpy().reshape(-1, go.OUT)
     wo = go.forward(torch.from_numpy(pt.cpu().numpy().astype(np.float64)), pr["nbr"].cpu(),
                     pr["xn"].cpu().double().reshape(-1, go.NODE_F), pr["ef"].cpu().double()).numpy()
     assert np.abs(w - wo).max() <= 1e-4 * max(1.0, np.abs(wo).max())
@@ -173,20 +176,22 @@ def test_adamw_matches_oracle(B):
 def test_learned_preconditioner_beats_block_jacobi(B):
     """Train on 8 microstructures, then solve 3 held-out ones with both preconditioners."""
     import torch
-    train_cs = small_cases([90, 120, 100, 80, 110, 95, 130, 85], seed=100, vf=0.25)
+    train_cs = small_cases([90, 120, 100, 80, 110, 95, 130, 85], seed=100, vf=0.2)
     bt = B.DeviceBatch(train_cs)
     r, e = B.training_pairs(bt, nrhs=3, seed=1)
     params = B.init_params(seed=0)
     hist = B.train(bt, r, e, params, steps=300, lr=3e-3)
-    assert hist[-1] < 0.9 * hist[0]
-    test_cs = small_cases([150, 140, 160], seed=500, vf=0.25)
+    assert hist[-1] < 0.5 * hist[0]
+    test_cs = small_cases([150, 140, 160], seed=500, vf=0.2)
     tb = B.DeviceBatch(test_cs)
     b = B.farfield_rhs(tb, np.array([0, 0, 0, 0, 0, 1.0]))
     x0, r0 = B.solve(tb, b, B.PRECOND_BLOCK_JACOBI, tol=1e-10)
     x1, r1 = B.solve(tb, b, B.PRECOND_LEARNED, params=params, tol=1e-10)
-    it0 = sum(x.inner for x in r0)
-    it1 = sum(x.inner for x in r1)
-    assert it1 < it0, (it0, it1)
+    _, r2 = B.solve(tb, b, B.PRECOND_NEUMANN, tol=1e-10)
+    it0, it1, it2 = (sum(x.inner for x in r) for r in (r0, r1, r2))
+    print(f"training loss {hist[0]:.4f} -> {hist[-1]:.4f}; Arnoldi steps: block-Jacobi {it0}, "
+          f"learned {it1}, Neumann weights 1 {it2}")
+    assert it1 < 0.8 * it0, (it0, it1)
     x0, x1 = x0.cpu().numpy(), x1.cpu().numpy()
     for s, c in enumerate(test_cs):
         rows = tb.seg_rows(s)
