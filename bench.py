@@ -8,12 +8,20 @@ linear Taylor eigenstrain (24 unknowns per sphere, N = 48,000), remote uniaxial 
 sigma33 = 1, stresses on a cell-centred 64^3 grid (262,144 points).  Seeded synthetic
 inputs (no dataset is involved).
 
-A step = sphere-pair assembly (FP64) + far-field right-hand side + solve in the chosen
-form (FP32 LU with split-BF16 tensor-core updates + FP64 GMRES-IR to a scaled backward
-error <= tol) + stresses at all grid points (double-float sphere sums, ~48 bits).  `value` is seconds per solution with
-inputs resident in HBM; `e2e` is the same through ibem_e3d_run_host with host buffers
-(inputs copied in and X / stresses copied out inside the timed region).  The plain FP64
-form is timed once on the same microstructure and its relative difference reported.
+A step = far-field right-hand side + solve + stresses at all grid points (double-float
+sphere sums, ~48 bits).  The chosen form (default, --form learned_gmres) solves without
+storing the matrix: FP32 restarted GMRES on the scaled system with on-the-fly pair-block
+products, right-preconditioned by block-Jacobi plus GNN-weighted Neumann blocks on the
+16-nearest-neighbour graph, inside FP64 iterative refinement whose residuals are FP64
+on-the-fly products (stop: relative residual <= 1e-10).  The network is trained before
+the timed region on small microstructures of the same distribution (its time is
+reported).  --form mixed_ir times the dense path instead: FP64 pair assembly, FP32 LU with
+split-BF16 tensor-core updates and FP64 GMRES-IR.  Both dense forms (mixed and plain FP64)
+are also run once on the same microstructure and the chosen form's difference to the
+plain FP64 solution is reported.  `value` is seconds per solution with inputs resident in
+HBM; `e2e` is the same through the host-buffer C ABI (ibem_e3d_run_host_mf, or
+ibem_e3d_run_host for mixed_ir) with inputs copied in and X / stresses copied out inside
+the timed region.
 
 --impl reference times the CPU restatement of the reference's algorithm (the oracle,
 OpenMP over all host cores) on bounded samples of the same workload, extrapolated to it.
@@ -51,6 +59,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the one plain-FP64 comparison solve")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline sampling")
+    ap.add_argument("--form", default="learned_gmres", choices=["learned_gmres", "mixed_ir"])
+    ap.add_argument("--train-steps", type=int, default=300)
     return ap.parse_args()
 
 
@@ -153,6 +163,39 @@ def roofline(prof):
             "traffic_source": "profiles/k_umma_bf16x3_bench2000_traffic.md"}
 
 
+def roofline_chosen(prof, case):
+    """Roofline of the largest kernel of the matrix-free step, the double-float stress sums
+    (field24_df): FP32-pipe bound.  Algorithmic work = FP32 flops per (point, sphere) pair
+    (counted by ncu's FP32 instruction counters on a small case, FFMA counted twice) x the
+    pairs of one launch, over its event-timed duration; peak = the nominal FP32 FMA rate
+    (152 SMs x 128 lanes x 2 flops) at the measured maximum SM clock, as MEASURED_PEAKS.json
+    holds no FP32 figure."""
+    f = prof.get("field")
+    if not f or f["ms"] <= 0:
+        return None
+    mhz = 2070.0
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            mhz = json.load(fh).get("sm_max_mhz", mhz)
+    peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
+    pairs = case.nump * case.num
+    achieved = FIELD_DF_FLOPS_PER_PAIR * pairs / (f["ms"] / f["launches"] * 1e-3) / 1e12
+    return {"kernel": "field24_df (stress sums, double-float)", "bound": "fp32", "achieved": achieved,
+            "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_source": f"nominal FP32 FMA rate at sm_max_mhz {mhz:g} (no measured FP32 peak)",
+            "flops_per_pair": FIELD_DF_FLOPS_PER_PAIR, "pairs_per_launch": pairs,
+            "avg_launch_ms": f["ms"] / f["launches"], "traffic": FIELD_DF_TRAFFIC_PER_LAUNCH,
+            "traffic_source": "profiles/field24_df_bench200.md (scaled by points x spheres)"}
+
+
+# FP32 flops per (point, sphere) pair of field24_df: FADD + FMUL + 2 FFMA thread instructions
+# counted by ncu on the 200-sphere, 16^3-point case (2.776e9 flops / 819,200 pairs); the
+# kernel's DRAM bytes per full-size launch are filled in from the full-size capture
+FIELD_DF_FLOPS_PER_PAIR = 3388.0
+FIELD_DF_TRAFFIC_PER_LAUNCH = None
+
+
 # ------------------------------------------------------------------ clocks
 class Clocks:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -212,6 +255,30 @@ def job_seconds_per_solution(ms_local, world, device=None):
 
 
 # ------------------------------------------------------------------ ours
+def train_preconditioner(args, rank, dev):
+    """GNN weights of the learned preconditioner, trained on 12 microstructures of 100-150
+    spheres of the bench distribution (residual / correction pairs from the plain FP64
+    solver, 4 per microstructure).  Returns (params tensor, info dict)."""
+    from ibemproject_gb300 import batch as B
+    from ibemproject_gb300 import cases
+    t = time.perf_counter()
+    rng = np.random.default_rng(77 + rank)
+    nums = rng.integers(100, 151, size=12)
+    train = [cases.farfield_case(num=int(n), r0=0.012, vf=0.15, grid=0, seed=9000 + 31 * rank + k)
+             for k, n in enumerate(nums)]
+    bt = B.DeviceBatch(train, device=dev)
+    r, e = B.training_pairs(bt, nrhs=4, seed=5 + rank)
+    t_data = time.perf_counter() - t
+    params = B.init_params(seed=1, device=dev)
+    t = time.perf_counter()
+    hist = B.train(bt, r, e, params, steps=args.train_steps, lr=3e-3)
+    t_train = time.perf_counter() - t
+    info = {"microstructures": len(train), "spheres": int(sum(nums)), "pairs": 4 * len(train),
+            "steps": args.train_steps, "loss_first": float(hist[0]), "loss_last": float(hist[-1]),
+            "data_s": t_data, "train_s": t_train, "params": int(params.numel())}
+    return params, info
+
+
 def run_ours(args, rank, world):
     import torch
     import ibemproject_gb300 as g
@@ -224,7 +291,6 @@ def run_ours(args, rank, world):
     cen = torch.from_numpy(np.ascontiguousarray(case.centers)).to(dev)
     rad = torch.from_numpy(np.ascontiguousarray(case.radius)).to(dev)
     pts = torch.from_numpy(np.ascontiguousarray(case.points)).to(dev)
-    A = torch.empty((N, N), dtype=torch.float64, device=dev)   # column-major N x N (square)
     b = torch.empty(N, dtype=torch.float64, device=dev)
     x = torch.empty(N, dtype=torch.float64, device=dev)
     S = torch.empty((nump, 6), dtype=torch.float64, device=dev)
@@ -234,17 +300,36 @@ def run_ours(args, rank, world):
     sp = ctypes.c_void_p(stream.cuda_stream)
     P = lambda t: ctypes.c_void_p(t.data_ptr())
     rep = g.SolveReport()
-    stage_ms = {"assembly": [], "solve": [], "field": []}
+    mrep = (g.MfReport * 1)()
+    seg = np.array([0, num], dtype=np.int32)
+    mats = (g.Material * 1)(m)
+    batch = g.Batch(1, seg.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), cen.data_ptr(), rad.data_ptr(), mats)
+    opt = g.MfOptions(50, 20, 8, 1e-10, 1e-5)
+    params, train_info = (None, None)
+    if args.form == "learned_gmres":
+        params, train_info = train_preconditioner(args, rank, dev)
+    A = None
 
-    def step(form=g.SOLVE_MIXED_IR, xo=x, So=S):
+    def step(form, xo=x, So=S):
+        nonlocal A
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         ev[0].record(stream)
-        g.check(L.ibem_e3d_pair_blocks(P(cen), P(rad), num, ctypes.byref(m), 24, P(A), N, 0, 0, sp))
-        g.check(L.ibem_e3d_farfield_rhs(num, ctypes.byref(m), 24, sigp, P(b), sp))
-        ev[1].record(stream)
-        g.check(L.ibem_e3d_solve(form, N, P(A), N, P(b), P(xo), args.tol, ctypes.byref(rep), sp))
+        if form == "learned_gmres":
+            g.check(L.ibem_e3d_farfield_rhs(num, ctypes.byref(m), 24, sigp, P(b), sp))
+            ev[1].record(stream)
+            g.check(L.ibem_e3d_mf_solve(ctypes.byref(batch), P(b), P(xo), g.PRECOND_LEARNED, P(params),
+                                        ctypes.byref(opt), mrep, sp))
+        else:
+            if A is None:
+                A = torch.empty((N, N), dtype=torch.float64, device=dev)   # column-major N x N
+            f = g.SOLVE_MIXED_IR if form == "mixed_ir" else g.SOLVE_FP64
+            g.check(L.ibem_e3d_pair_blocks(P(cen), P(rad), num, ctypes.byref(m), 24, P(A), N, 0, 0, sp))
+            g.check(L.ibem_e3d_farfield_rhs(num, ctypes.byref(m), 24, sigp, P(b), sp))
+            ev[1].record(stream)
+            g.check(L.ibem_e3d_solve(f, N, P(A), N, P(b), P(xo), args.tol, ctypes.byref(rep), sp))
         ev[2].record(stream)
-        g.check(L.ibem_e3d_field_form(form, P(pts), nump, P(cen), P(rad), num, ctypes.byref(m), 24, P(xo), None, 0,
+        ff = g.SOLVE_FP64 if form == "plain_fp64" else g.SOLVE_MIXED_IR
+        g.check(L.ibem_e3d_field_form(ff, P(pts), nump, P(cen), P(rad), num, ctypes.byref(m), 24, P(xo), None, 0,
                                       None, 0, None, None, sigp, P(So), sp))
         ev[3].record(stream)
         return ev
@@ -253,8 +338,14 @@ def run_ours(args, rank, world):
         if world > 1:
             torch.distributed.barrier()
 
+    def stages(evs):
+        return {"rhs_or_assembly": statistics.median(e[0].elapsed_time(e[1]) for e in evs),
+                "solve": statistics.median(e[1].elapsed_time(e[2]) for e in evs),
+                "field": statistics.median(e[2].elapsed_time(e[3]) for e in evs)}
+
+    form = args.form
     for _ in range(args.warmup):
-        step()
+        step(form)
     torch.cuda.synchronize()
     barrier()
     clocks = Clocks(dev.index)
@@ -266,56 +357,70 @@ def run_ours(args, rank, world):
     t0.record(stream)
     evs = []
     for _ in range(args.steps):
-        evs.append(step())
+        evs.append(step(form))
     t1.record(stream)
     torch.cuda.synchronize()
     barrier()
     launches = L.ibem_kernel_launches() - launches0
     ck = clocks.stop()
     ms = t0.elapsed_time(t1) / args.steps
+    stage_ms = stages(evs)
+    solve_info = ({"rel_residual": mrep[0].rel_residual, "refinement_steps": mrep[0].outer,
+                   "arnoldi_steps": mrep[0].inner, "setup_ms": mrep[0].t_setup_ms}
+                  if form == "learned_gmres" else
+                  {"backward_error": rep.backward_error, "gmres_iterations": rep.iterations,
+                   "factor_ms": rep.t_factor_ms, "refine_ms": rep.t_solve_ms})
     # one more step with the per-phase CUDA events of the library (kept out of the timed
     # steps above, whose total they would inflate by their own records)
     L.ibem_prof_enable(1)
-    step()
+    step(form)
     torch.cuda.synchronize()
     prof = g.prof_report()
     L.ibem_prof_enable(0)
-    for ev in evs:
-        stage_ms["assembly"].append(ev[0].elapsed_time(ev[1]))
-        stage_ms["solve"].append(ev[1].elapsed_time(ev[2]))
-        stage_ms["field"].append(ev[2].elapsed_time(ev[3]))
-    rep_mixed = (rep.backward_error, rep.iterations, rep.t_factor_ms, rep.t_solve_ms)
     ms = job_seconds_per_solution(ms, world, dev) * 1e3
 
-    # plain FP64 form once on the same microstructure, and the difference to it
-    plain = None
+    # the other forms once on the same microstructure, and the chosen form's difference to
+    # the plain FP64 solution
+    others, prof_mixed = {}, None
     if not args.no_plain and rank == 0:
-        x64 = torch.empty(N, dtype=torch.float64, device=dev)
-        S64 = torch.empty((nump, 6), dtype=torch.float64, device=dev)
-        torch.cuda.synchronize()
-        ev = step(g.SOLVE_FP64, x64, S64)
-        torch.cuda.synchronize()
-        plain_ms = ev[0].elapsed_time(ev[3])
-        ex = float((x - x64).abs().max() / x64.abs().max())
-        es = float((S - S64).abs().max() / S64.abs().max())
-        plain = {"time_to_solution_s": plain_ms / 1e3, "factor_ms": rep.t_factor_ms, "solve_ms": rep.t_solve_ms,
-                 "backward_error": rep.backward_error, "mixed_rel_err_eigenstrain": ex,
-                 "mixed_rel_err_stress": es}
-        del x64, S64
+        x2 = torch.empty(N, dtype=torch.float64, device=dev)
+        S2 = torch.empty((nump, 6), dtype=torch.float64, device=dev)
+        for f in (["mixed_ir"] if form != "mixed_ir" else []) + ["plain_fp64"]:
+            if f == "mixed_ir":
+                step(f, x2, S2)   # warm-up of the dense path
+                L.ibem_prof_enable(1)
+            torch.cuda.synchronize()
+            ev = step(f, x2, S2)
+            torch.cuda.synchronize()
+            if f == "mixed_ir":
+                prof_mixed = g.prof_report()
+                L.ibem_prof_enable(0)
+            others[f] = {"time_to_solution_s": ev[0].elapsed_time(ev[3]) / 1e3, "stages_ms": stages([ev]),
+                         "factor_ms": rep.t_factor_ms, "backward_error": rep.backward_error}
+            if f == "plain_fp64":
+                others[f]["chosen_rel_err_eigenstrain"] = float((x - x2).abs().max() / x2.abs().max())
+                others[f]["chosen_rel_err_stress"] = float((S - S2).abs().max() / S2.abs().max())
+        del x2, S2
+    if form == "mixed_ir":
+        prof_mixed = prof
+    A = None
+    torch.cuda.empty_cache()
 
     # end to end through the host-buffer C ABI (copies inside the timed region)
     e2e = None
     if rank == 0 and args.e2e_steps > 0:
-        del A
-        torch.cuda.empty_cache()
+        hp = params.cpu().numpy() if params is not None else None
+        run = (lambda: g.run_host_mf(case, g.PRECOND_LEARNED, hp)) if form == "learned_gmres" else \
+              (lambda: g.run_host(case, layout=24, form=g.SOLVE_MIXED_IR, tol=args.tol))
+        run()
         t = time.perf_counter()
         for _ in range(args.e2e_steps):
-            g.run_host(case, layout=24, form=g.SOLVE_MIXED_IR, tol=args.tol)
+            run()
         e2e_s = (time.perf_counter() - t) / args.e2e_steps
-        h2d = case.centers.nbytes + case.radius.nbytes + case.points.nbytes + 48
+        h2d = case.centers.nbytes + case.radius.nbytes + case.points.nbytes + 48 + (hp.nbytes if hp is not None else 0)
         d2h = 8 * N + 8 * 6 * nump
         e2e = {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
-    return case, ms, stage_ms, rep_mixed, plain, e2e, ck, launches, prof
+    return (case, ms, stage_ms, solve_info, others, e2e, ck, launches, prof, prof_mixed, train_info)
 
 
 def main():
@@ -345,29 +450,35 @@ def main():
     import torch
     if world > 1:
         torch.distributed.init_process_group("nccl")
-    case, ms, stage_ms, rep_mixed, plain, e2e, ck, launches, prof = run_ours(args, rank, world)
+    (case, ms, stage_ms, solve_info, others, e2e, ck, launches, prof, prof_mixed,
+     train_info) = run_ours(args, rank, world)
     if rank == 0:
         cb = cpu_baseline(case, budget_s=args.cpu_budget) if world == 1 else None
         N = 24 * case.num
-        med = {k: statistics.median(v) for k, v in stage_ms.items()}
+        learned = args.form == "learned_gmres"
         line = {
             "metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32/bf16x3",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 GMRES + f64 refinement" if learned else "f64+f32/bf16x3",
             "data": "synthetic (seeded RSA microstructure)",
-            "config": {"workload": WORKLOAD, "layout": 24, "N": N, "points": case.nump, "form": "mixed_ir",
-                       "tol_scaled_backward_error": args.tol,
-                       "l2": "inputs larger than L2 (A is 18.4 GB FP64)", "parallelism": f"replicas x{world}"},
-            "stages_ms": med,
-            "solve": {"backward_error": rep_mixed[0], "gmres_iterations": rep_mixed[1],
-                      "factor_ms": rep_mixed[2], "refine_ms": rep_mixed[3]},
-            "plain_fp64": plain,
+            "config": {"workload": WORKLOAD, "layout": 24, "N": N, "points": case.nump, "form": args.form,
+                       "tol": "relative residual 1e-10 (scaled system)" if learned else
+                              f"scaled backward error {args.tol}",
+                       "l2": ("inputs in HBM; the matrix is never stored (18.4 GB in FP64 if it were)" if learned
+                              else "inputs larger than L2 (A is 18.4 GB FP64)"),
+                       "parallelism": f"replicas x{world}"},
+            "stages_ms": stage_ms,
+            "solve": solve_info,
+            "preconditioner_training": train_info,
+            "other_forms": others,
             "e2e": e2e,
             "clocks": ck,
             "gpu_launches": int(launches),
             "profile_ms_per_step": {k: {"launches": v["launches"], "ms": v["ms"]} for k, v in prof.items()},
             "profile_note": "one extra step after the timed ones, with CUDA events around each phase",
-            "roofline": roofline(prof),
+            "roofline": roofline_chosen(prof, case) if learned else roofline(prof),
+            "roofline_tensor_gemm": roofline(prof_mixed) if prof_mixed else None,
             "cpu_baseline": cb,
         }
         print(json.dumps(line))

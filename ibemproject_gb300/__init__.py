@@ -100,6 +100,9 @@ SIGNATURES = {
                                  ctypes.POINTER(MfReport), _vp]),
     "ibem_e3d_batch_farfield_rhs": (_int, [ctypes.POINTER(Batch), _c_dp, _vp, _vp]),
     "ibem_e3d_effective_modulus": (_int, [ctypes.POINTER(Batch), _vp, _c_dp, _c_dp, _c_dp, _c_dp, _vp]),
+    "ibem_e3d_run_host_mf": (_int, [ctypes.POINTER(Material), _int, _c_dp, _c_dp, _int, _c_dp, _c_dp, _int,
+                                    ctypes.POINTER(ctypes.c_float), ctypes.POINTER(MfOptions), _c_dp, _c_dp,
+                                    ctypes.POINTER(MfReport)]),
     "ibem_gnn_param_count": (_i64, []),
     "ibem_gnn_init_params": (_int, [_vp, ctypes.c_uint64, _vp]),
     "ibem_gnn_prepare": (_int, [ctypes.POINTER(Batch), _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -167,6 +170,28 @@ def run_host(case, layout: int = 78, form: int = SOLVE_FP64, tol: float = 1e-12)
                                   _dp(bc), _dp(tbc), case.num, _dp(cen), _dp(rad), case.nump, _dp(pts),
                                   _dp(sig) if sig is not None else None, tol, _dp(X), _dp(S),
                                   ctypes.byref(rep)))
+    return X, S, rep
+
+
+def run_host_mf(case, precond: int = PRECOND_LEARNED, params=None, tol: float = 1e-10):
+    """Boundary-free far-field pipeline, matrix-free solve, through the host-buffer C ABI:
+    returns (X, stress, MfReport).  params: host float32 array (learned form)."""
+    m = material(case.E0, case.nu0, case.E1, case.nu1)
+    N = 24 * case.num
+    X = np.zeros(N)
+    S = np.zeros((case.nump, 6))
+    rep = MfReport()
+    cen = np.ascontiguousarray(case.centers, dtype=np.float64)
+    rad = np.ascontiguousarray(case.radius, dtype=np.float64)
+    pts = np.ascontiguousarray(case.points if case.nump else np.zeros((1, 3)), dtype=np.float64)
+    sig = np.ascontiguousarray(case.sig_inf, dtype=np.float64)
+    prm, hold = None, None
+    if params is not None:
+        hold = np.ascontiguousarray(params, dtype=np.float32)   # kept alive across the call
+        prm = hold.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    opt = MfOptions(0, 0, 0, tol, 0.0)
+    check(lib().ibem_e3d_run_host_mf(ctypes.byref(m), case.num, _dp(cen), _dp(rad), case.nump, _dp(pts), _dp(sig),
+                                     precond, prm, ctypes.byref(opt), _dp(X), _dp(S), ctypes.byref(rep)))
     return X, S, rep
 
 

@@ -1,15 +1,14 @@
 // Matrix-free solves of the layout-24 sphere systems, one realisation or a batch of them.
 //
 // The pair blocks that ibem_e3d_pair_blocks stores (integratorElastic3D.cpp:341-567,
-// orders 0 and 1) are evaluated inside the products instead:
+// orders 0 and 1) are never formed: their products with the coefficients are evaluated
+// as the contracted strain and its gradient (mf_contract.cuh):
 //   k_mf_apply_f32  As x in FP32 on the scaled system (mf.h), the GMRES operator;
 //   k_mf_apply_f64  A x in FP64, physical units, the refinement residual b - A x.
 // One thread per target particle s, 128 consecutive targets of one realisation per CTA;
 // the CTA's source particles h (a slice of the realisation, gridDim.y slices) are staged
 // through shared memory in chunks with their coefficients, and every thread sums the
-// products of the generated 24 x 24 blocks with them in registers (the generated code
-// calls the sink with constant indices, so the sums stay in registers).  Slices add
-// their partial sums atomically.
+// pair products in registers.  Slices add their partial sums atomically.
 //
 // Solver: FP64 iterative refinement x += Dc d; each correction d solves As d = Dr r with a
 // restarted FP32 GMRES right-preconditioned by a block-diagonal P (block-Jacobi or learned),
@@ -26,6 +25,7 @@
 
 #include "gen_sphere24.cuh"
 #include "mf.h"
+#include "mf_contract.cuh"
 #include "prof.h"
 
 namespace ibem {
@@ -81,18 +81,8 @@ __global__ void __launch_bounds__(kMfThreads)
       const float x1 = ((ph.y - qh.y) + (pl.y - ql.y)) * ia;
       const float x2 = ((ph.z - qh.z) + (pl.z - ql.z)) * ia;
       const float* xs = sx + kMfNu * hh;
+      sph_pair_apply24<float>(x0, x1, x2, 1.f, mc.kmu, mc.klam, mc.tn1, mc.tn2, xs, ph.w * ia, acc);
       MvSink<float> s0{acc, xs};
-      sph_block24f_c0_r0(x0, x1, x2, 1.f, mc, s0);
-      sph_block24f_c1_r0(x0, x1, x2, 1.f, mc, s0);
-      float t1[kMfNu];
-#pragma unroll
-      for (int r = 6; r < kMfNu; ++r) t1[r] = 0.f;
-      MvSink<float> s1{t1, xs};
-      sph_block24f_c0_r1(x0, x1, x2, 1.f, mc, s1);
-      sph_block24f_c1_r1(x0, x1, x2, 1.f, mc, s1);
-      const float ratio = ph.w * ia;  // a_s / a_h on rows of order 1
-#pragma unroll
-      for (int r = 6; r < kMfNu; ++r) acc[r] = fmaf(ratio, t1[r], acc[r]);
       if (h0 + hh == s) sph_self24f(mc, s0);
     }
   }
@@ -140,11 +130,8 @@ __global__ void __launch_bounds__(kMfThreads)
     for (int hh = 0; hh < nh; ++hh) {
       const double x0 = p0 - sc[4 * hh], x1 = p1 - sc[4 * hh + 1], x2 = p2 - sc[4 * hh + 2];
       const double a = sc[4 * hh + 3];
+      sph_pair_apply24<double>(x0, x1, x2, a, mc.kmu, mc.klam, mc.tn1, mc.tn2, sx + kMfNu * hh, 1.0, acc);
       MvSink<double> sk{acc, sx + kMfNu * hh};
-      sph_block24_c0_r0(x0, x1, x2, a, mc, sk);
-      sph_block24_c1_r0(x0, x1, x2, a, mc, sk);
-      sph_block24_c0_r1(x0, x1, x2, a, mc, sk);
-      sph_block24_c1_r1(x0, x1, x2, a, mc, sk);
       if (h0 + hh == s) sph_self24(mc, sk);
     }
   }
@@ -935,5 +922,60 @@ extern "C" ibem_status ibem_e3d_effective_modulus(const ibem_e3d_batch* batch, c
   }
   cudaFree(acc);
   mf_batch_free(b);
+  return s;
+}
+
+extern "C" ibem_status ibem_e3d_run_host_mf(const ibem_material* mat, int num, const double* centers,
+                                            const double* radius, int nump, const double* points,
+                                            const double* sig_inf, ibem_precond pc, const float* gnn_params,
+                                            const ibem_mf_options* opt, double* X, double* stress,
+                                            ibem_mf_report* report) {
+  if (!mat || num <= 0 || !centers || !radius || nump < 0 || (nump > 0 && !points) || !sig_inf || !X ||
+      (nump > 0 && !stress) || !report)
+    return fail(IBEM_ERR_ARG, "run_host_mf: bad arguments");
+  if (pc == IBEM_PRECOND_LEARNED && !gnn_params) return fail(IBEM_ERR_ARG, "run_host_mf: learned form needs parameters");
+  const int64_t N = (int64_t)kMfNu * num;
+  const int64_t np = gnn_param_count();
+  double *cen = nullptr, *rad = nullptr, *pts = nullptr, *b = nullptr, *x = nullptr, *S = nullptr;
+  float* prm = nullptr;
+  cudaStream_t st = nullptr;
+  ibem_status s = IBEM_OK;
+  {
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&cen, sizeof(double) * 3 * num);
+    if (e == cudaSuccess) e = cudaMalloc(&rad, sizeof(double) * num);
+    if (e == cudaSuccess) e = cudaMalloc(&pts, sizeof(double) * 3 * std::max(nump, 1));
+    if (e == cudaSuccess) e = cudaMalloc(&b, sizeof(double) * N);
+    if (e == cudaSuccess) e = cudaMalloc(&x, sizeof(double) * N);
+    if (e == cudaSuccess) e = cudaMalloc(&S, sizeof(double) * 6 * std::max(nump, 1));
+    if (e == cudaSuccess && gnn_params) e = cudaMalloc(&prm, sizeof(float) * np);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cen, centers, sizeof(double) * 3 * num, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rad, radius, sizeof(double) * num, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && nump > 0) e = cudaMemcpyAsync(pts, points, sizeof(double) * 3 * nump, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && gnn_params) e = cudaMemcpyAsync(prm, gnn_params, sizeof(float) * np, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) s = cuda_fail(e, "run_host_mf: set-up");
+  }
+  const int seg[2] = {0, num};
+  const ibem_e3d_batch bt{1, seg, cen, rad, mat};
+  if (!s) s = ibem_e3d_farfield_rhs(num, mat, kMfNu, sig_inf, b, st);
+  if (!s) s = ibem_e3d_mf_solve(&bt, b, x, pc, prm, opt, report, st);
+  if (!s && nump > 0)
+    s = ibem_e3d_field_form(IBEM_SOLVE_MIXED_IR, pts, nump, cen, rad, num, mat, kMfNu, x, nullptr, 0, nullptr, 0,
+                            nullptr, nullptr, sig_inf, S, st);
+  if (!s) {
+    cudaError_t e = cudaMemcpyAsync(X, x, sizeof(double) * N, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && nump > 0) e = cudaMemcpyAsync(stress, S, sizeof(double) * 6 * nump, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) s = cuda_fail(e, "run_host_mf: results");
+  }
+  if (st) cudaStreamSynchronize(st);
+  cudaFree(cen);
+  cudaFree(rad);
+  cudaFree(pts);
+  cudaFree(b);
+  cudaFree(x);
+  cudaFree(S);
+  cudaFree(prm);
+  if (st) cudaStreamDestroy(st);
   return s;
 }

@@ -247,6 +247,18 @@ ibem_status ibem_e3d_effective_modulus(const ibem_e3d_batch* batch, const double
                                        const double* volume, const double* sig_inf,
                                        double* mean_strain, double* e_eff, void* stream);
 
+/* The boundary-free far-field pipeline of one microstructure on host buffers, for FFI
+ * callers (the matrix-free counterpart of ibem_e3d_run_host, layout 24): copies in,
+ * far-field right-hand side, ibem_e3d_mf_solve with `pc` (gnn_params: host array of
+ * ibem_gnn_param_count() floats, needed for IBEM_PRECOND_LEARNED), stresses at the points
+ * (ibem_e3d_field_form, double-float sphere sums) and copies out.  X: 24*num; stress:
+ * nump x 6.  Synchronous. */
+ibem_status ibem_e3d_run_host_mf(const ibem_material* mat, int num, const double* centers,
+                                 const double* radius, int nump, const double* points,
+                                 const double* sig_inf, ibem_precond pc, const float* gnn_params,
+                                 const ibem_mf_options* opt, double* X, double* stress,
+                                 ibem_mf_report* report);
+
 /* ---- learned preconditioner (no reference counterpart) --------------------- */
 /* On the graph of each particle's 16 nearest neighbours (edges e = (i <- j)), with B the
  * block-Jacobi inverses and As the scaled pair blocks, the Neumann series of As^-1 gives

@@ -228,3 +228,18 @@ def test_effective_modulus_single_sphere_matches_eshelby(B):
     e33 = e0[2, 2] + f * estar[2, 2]
     assert abs(eps[0, 5] - e33) <= 1e-9 * abs(e33)
     assert abs(Eeff[0] - sig[5] / e33) <= 1e-9 * abs(sig[5] / e33)
+
+
+def test_host_buffer_pipeline_matches_dense_path(B):
+    """ibem_e3d_run_host_mf (copies, right-hand side, matrix-free solve, stresses) against
+    the dense host-buffer pipeline ibem_e3d_run_host in FP64 on the same far-field case."""
+    import ibemproject_gb300 as g
+    from ibemproject_gb300 import cases
+    c = cases.farfield_case(num=60, r0=0.012, vf=0.15, grid=6, seed=8)
+    Xd, Sd, _ = g.run_host(c, layout=24, form=g.SOLVE_FP64)
+    for pc, params in ((g.PRECOND_BLOCK_JACOBI, None), (g.PRECOND_NEUMANN, None),
+                       (g.PRECOND_LEARNED, B.init_params(seed=2).cpu().numpy())):
+        X, S, rep = g.run_host_mf(c, pc, params)
+        assert scaled_err(X, Xd) < 1e-8, pc
+        assert scaled_err(S, Sd) < 1e-8, pc
+        assert rep.rel_residual <= 1e-10
