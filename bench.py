@@ -186,14 +186,16 @@ def roofline_chosen(prof, case):
             "peak_source": f"nominal FP32 FMA rate at sm_max_mhz {mhz:g} (no measured FP32 peak)",
             "flops_per_pair": FIELD_DF_FLOPS_PER_PAIR, "pairs_per_launch": pairs,
             "avg_launch_ms": f["ms"] / f["launches"], "traffic": FIELD_DF_TRAFFIC_PER_LAUNCH,
-            "traffic_source": "profiles/field24_df_bench200.md (scaled by points x spheres)"}
+            "traffic_unit": "bytes per launch (ncu dram read+write)",
+            "traffic_source": "profiles/launches_bench_2000spheres_learned_step.md",
+            "flops_source": "profiles/field24_df_bench200.md"}
 
 
 # FP32 flops per (point, sphere) pair of field24_df: FADD + FMUL + 2 FFMA thread instructions
-# counted by ncu on the 200-sphere, 16^3-point case (2.776e9 flops / 819,200 pairs); the
-# kernel's DRAM bytes per full-size launch are filled in from the full-size capture
+# counted by ncu on the 200-sphere, 16^3-point case (2.776e9 flops / 819,200 pairs); DRAM
+# bytes (read + write) of its full-size launch from the launch list of one bench step
 FIELD_DF_FLOPS_PER_PAIR = 3388.0
-FIELD_DF_TRAFFIC_PER_LAUNCH = None
+FIELD_DF_TRAFFIC_PER_LAUNCH = 20.24e6
 
 
 # ------------------------------------------------------------------ clocks
@@ -356,8 +358,10 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     t0.record(stream)
     evs = []
+    torch.cuda.nvtx.range_push("timed_steps")   # lets ncu select exactly these launches
     for _ in range(args.steps):
         evs.append(step(form))
+    torch.cuda.nvtx.range_pop()
     t1.record(stream)
     torch.cuda.synchronize()
     barrier()

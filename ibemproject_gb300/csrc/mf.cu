@@ -548,7 +548,7 @@ void mf_batch_free(MfBatch& b) {
 }
 
 ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_t st) {
-  ProfScope ps(PROF_MATVEC, st);
+  ProfScope ps(PROF_MF_F32, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(float) * b.N, st));
   ::ibem::count_launch(), k_mf_apply_f32<<<dim3(b.ntiles, b.hsplit), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, b.gh,
                                                                                          b.gl, b.matf, x, y);
@@ -557,7 +557,7 @@ ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_
 }
 
 ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st) {
-  ProfScope ps(PROF_PAIR, st);
+  ProfScope ps(PROF_MF_F64, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
   ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, b.cen,
                                                                                          b.rad, b.matd, x, y);
@@ -704,15 +704,10 @@ struct MfSolver {
   }
 };
 
-double ms_since(std::chrono::steady_clock::time_point t0) {
-  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-}
-
 }  // namespace
 
 ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPrecond& P, const ibem_mf_options& o,
                      ibem_mf_report* rep, cudaStream_t st) {
-  const auto t0 = std::chrono::steady_clock::now();
   const int S = b.nseg;
   const int64_t N = b.N;
   MfSolver g(b, st, o.restart);
@@ -778,7 +773,6 @@ ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPr
     for (int i = 0; i < S; ++i) {
       rep[i].outer = outer_of[i];
       rep[i].inner = steps[i];
-      rep[i].t_solve_ms = ms_since(t0);
     }
     for (int i = 0; i < S && !s; ++i)
       if (!(rep[i].rel_residual <= o.tol)) s = fail(IBEM_ERR_NOCONV, "mf solve: a realisation missed the tolerance");
@@ -847,7 +841,9 @@ extern "C" ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const doub
   if (o.inner_tol <= 0) o.inner_tol = 1e-5;
   if (o.restart > 200) return fail(IBEM_ERR_ARG, "mf_solve: restart > 200");
   cudaStream_t st = as_stream(stream);
-  const auto t0 = std::chrono::steady_clock::now();
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  for (auto& e : ev) IBEM_CUDA(cudaEventCreate(&e));
+  IBEM_CUDA(cudaEventRecord(ev[0], st));
   MfBatch b;
   ibem_status s = mf_batch_init(b, *batch, st);
   MfPrecond P;
@@ -855,17 +851,26 @@ extern "C" ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const doub
     const cudaError_t e = cudaMalloc(&P.D, sizeof(float) * kMfNu * kMfNu * (size_t)b.num);
     if (e != cudaSuccess) s = cuda_fail(e, "mf_solve: preconditioner blocks");
   }
-  if (!s) s = mf_block_jacobi(b, P.D, st);
-  if (!s && pc != IBEM_PRECOND_BLOCK_JACOBI)
-    s = mf_neighbour_precond(b, pc == IBEM_PRECOND_LEARNED ? gnn_params_dev : nullptr, P, st);
-  if (!s) {
-    const cudaError_t e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) s = cuda_fail(e, "mf_solve: set-up");
+  {
+    ProfScope pp(PROF_PRECOND, st);
+    if (!s) s = mf_block_jacobi(b, P.D, st);
+    if (!s && pc != IBEM_PRECOND_BLOCK_JACOBI)
+      s = mf_neighbour_precond(b, pc == IBEM_PRECOND_LEARNED ? gnn_params_dev : nullptr, P, st);
   }
-  const double tset = ms_since(t0);
+  cudaEventRecord(ev[1], st);
   for (int i = 0; i < batch->nseg; ++i) reports[i] = ibem_mf_report{};
   if (!s) s = mf_solve(b, b_dev, x_dev, P, o, reports, st);
-  for (int i = 0; i < batch->nseg; ++i) reports[i].t_setup_ms = tset;
+  cudaEventRecord(ev[2], st);
+  float t_set = 0.f, t_sol = 0.f;
+  if (cudaEventSynchronize(ev[2]) == cudaSuccess) {
+    cudaEventElapsedTime(&t_set, ev[0], ev[1]);
+    cudaEventElapsedTime(&t_sol, ev[1], ev[2]);
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  for (int i = 0; i < batch->nseg; ++i) {
+    reports[i].t_setup_ms = t_set;
+    reports[i].t_solve_ms = t_sol;
+  }
   cudaFree(P.D);
   cudaFree(P.Q);
   cudaFree(P.nbr);

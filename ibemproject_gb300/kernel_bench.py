@@ -8,6 +8,9 @@
                event time) and the BF16 split kernels.
 --lu N         ibem_e3d_solve of a random, diagonally dominant N x N system with the
                per-phase profile (panel, row exchanges, TRSM, GEMM, triangular solves).
+--mf NUM       the matrix-free products (ibem_e3d_mf_matvec, FP32 scaled and FP64) on a
+               far-field microstructure of NUM spheres (bench distribution): NUM^2 pair
+               products per launch, timed by the library's phase events.
 
 One JSON line per case.  The operands are larger than L2 for M, N, K >= 4096; between
 repetitions a 256 MB buffer is written to flush L2.
@@ -88,11 +91,34 @@ def bench_lu(n, form, reps, dev):
             "phase_launches": {k: v["launches"] / reps for k, v in prof.items()}}
 
 
+def bench_mf(num, reps, dev):
+    from . import batch as B
+    from . import cases
+    c = cases.farfield_case(num=num, r0=0.012, vf=0.15, grid=0, seed=2024)
+    bt = B.DeviceBatch([c], device=dev)
+    g = torch.Generator(device="cpu").manual_seed(3)
+    x = torch.randn(bt.N, generator=g, dtype=torch.float64).to(dev)
+    out = {"kernel": "k_mf_apply", "spheres": num, "pairs": num * num, "reps": reps}
+    L = lib()
+    for prec in (32, 64):
+        B.matvec(bt, x, prec)   # warm-up
+        L.ibem_prof_enable(1)
+        for _ in range(reps):
+            B.matvec(bt, x, prec)
+        prof = prof_report()
+        L.ibem_prof_enable(0)
+        ms = prof.get(f"mf_f{prec}", {}).get("ms", 0.0) / reps
+        out[f"f{prec}_ms"] = ms
+        out[f"f{prec}_ns_per_pair"] = ms * 1e6 / (num * num) if ms > 0 else None
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gemm", action="append", default=[], help="M,N,K")
     ap.add_argument("--lu", type=int, action="append", default=[])
     ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--mf", type=int, action="append", default=[])
     ap.add_argument("--reps", type=int, default=3)
     a = ap.parse_args(argv)
     dev = torch.device("cuda", 0)
@@ -102,6 +128,8 @@ def main(argv=None):
         print(json.dumps(bench_gemm(m, n, k, a.reps, dev)), flush=True)
     for n in a.lu:
         print(json.dumps(bench_lu(n, a.form, a.reps, dev)), flush=True)
+    for n in a.mf:
+        print(json.dumps(bench_mf(n, a.reps, dev)), flush=True)
     return 0
 
 
