@@ -136,3 +136,24 @@ extern "C" int hg_field24df(const double* p, const double* cen, double a, double
   for (int t = 0; t < 6; ++t) e[t] = mc.kd * ibem::df_double(acc[t]);
   return 0;
 }
+
+#include "mf_contract.cuh"
+
+// Product of one layout-24 pair block with a coefficient vector as the matrix-free solver
+// evaluates it (contracted strain and its gradient), in FP64 or FP32.
+extern "C" int hg_pair_apply24(int fp32, const double* x, double a, double E0, double nu0, double E1,
+                               double nu1, const double* coef, double* out /* 24 */) {
+  SphMat mc = sph_mat_init(E0, nu0, E1, nu1);
+  if (fp32) {
+    float y[24] = {0}, cf[24];
+    for (int i = 0; i < 24; ++i) cf[i] = (float)coef[i];
+    ibem::sph_pair_apply24<float>((float)x[0], (float)x[1], (float)x[2], (float)a, (float)mc.kmu, (float)mc.klam,
+                                  (float)mc.tn1, (float)mc.tn2, cf, 1.0f, y);
+    for (int i = 0; i < 24; ++i) out[i] = y[i];
+  } else {
+    double y[24] = {0};
+    ibem::sph_pair_apply24<double>(x[0], x[1], x[2], a, mc.kmu, mc.klam, mc.tn1, mc.tn2, coef, 1.0, y);
+    for (int i = 0; i < 24; ++i) out[i] = y[i];
+  }
+  return 0;
+}

@@ -147,3 +147,29 @@ def test_double_float_field_matches_fp64(hg):
         hg.hg_field24c(d(x), ctypes.c_double(a), *_mat(), d(E), d(e1))
         hg.hg_field24df(d(cen + x), d(cen), ctypes.c_double(a), *_mat(), d(E), d(e2))
         assert scaled_err(e2, e1) < 2e-12, (t, a, x, e1, e2)
+
+
+@pytest.mark.parametrize("fp32", [0, 1])
+def test_pair_apply_matches_generated_block(hg, fp32):
+    """The matrix-free pair product (mf_contract.cuh: contracted strain and its analytic
+    gradient) against the generated 24 x 24 block times the same coefficients, outside and
+    inside the source sphere.  FP64 to 1e-12; FP32 (unit source radius, as the solver
+    calls it) to 2e-5 of the largest entry."""
+    rng = np.random.default_rng(5)
+    for t in range(40):
+        a = 1.0 if fp32 else 0.05 * (0.8 + 0.4 * rng.random())
+        if t < 4:
+            x = rng.normal(size=3) * 0.3 * a       # inside
+        else:
+            x = rng.normal(size=3)
+            x *= a * (1.02 + 6 * rng.random()) / np.linalg.norm(x)
+        coef = rng.normal(size=24)
+        coef[6:] /= a
+        blk = np.zeros(24 * 24)
+        hg.hg_pair_block(24, d(np.ascontiguousarray(x)), ctypes.c_double(a), *_mat(), 0, d(blk))
+        want = blk.reshape(24, 24) @ coef
+        got = np.zeros(24)
+        hg.hg_pair_apply24(fp32, d(np.ascontiguousarray(x)), ctypes.c_double(a), *_mat(), d(coef), d(got))
+        tol = 2e-5 if fp32 else 1e-12
+        assert np.abs(got[:6] - want[:6]).max() <= tol * np.abs(want[:6]).max(), (t, got[:6], want[:6])
+        assert np.abs(got[6:] - want[6:]).max() <= tol * np.abs(want[6:]).max(), (t, got[6:], want[6:])
