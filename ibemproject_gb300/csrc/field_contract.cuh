@@ -234,4 +234,86 @@ IBEM_HD IBEM_INLINE bool sph_field24_df(const dfloat* p, const SphDF& sp, dfloat
   return !ext;
 }
 
+// The same contraction in FP32 for far pairs of the mixed form's split sum: a sphere whose
+// centre lies beyond kFarRadii of its radius from every point of a warp contributes at most
+// (1/kFarRadii)^3 of a near sphere, so its FP32 rounding (a few 1e-7 of the contribution,
+// unbiased) stays near 1e-9 of the strain when summed over all far spheres.  Coordinates
+// scaled by 1/a as above; the sphere's constants are the high parts of its SphDF.
+constexpr float kFarRadii = 14.0f;
+
+IBEM_HD IBEM_INLINE void sph_field24_f32(const dfloat* p, const SphDF& sp, float tn1, float tn2, float* e) {
+  float x[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) x[i] = ((p[i].hi - sp.c[i].hi) + (p[i].lo - sp.c[i].lo)) * sp.ia.hi;
+  const float r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+  // outside by construction (far pair): rho^2 = |x|^2
+  float ir;
+#ifdef __CUDA_ARCH__
+  ir = rsqrtf(r2);
+#else
+  ir = 1.0f / std::sqrt(r2);
+#endif
+  ir = ir * (1.5f - 0.5f * r2 * ir * ir);  // one Newton step
+  const float irho2 = ir * ir;
+  const float p1 = 4.0f * 3.14159265358979f * ir * irho2, p2 = p1 * irho2, p3 = p2 * irho2, p4 = p3 * irho2,
+              p5 = p4 * irho2;
+  const float J1 = p1 * (1.0f / 3.0f), J2 = p2 * 0.2f, J3 = p3 * (1.0f / 7.0f), J4 = p4 * (1.0f / 9.0f),
+              J5 = p5 * (1.0f / 11.0f);
+  const float V0_1 = -J1, V0_2 = 5.0f * J2, V0_3 = -35.0f * J3;
+  const float V1_1 = -J2, V1_2 = 7.0f * J3, V1_3 = -63.0f * J4;
+  const float V2_1 = -J3, V2_2 = 9.0f * J4, V2_3 = -99.0f * J5;
+  const float Ps2 = V0_1 - V1_1, Ps3 = V0_2 - V1_2, Ps4 = V0_3 - V1_3;
+  const float Q2 = V1_1 - V2_1, Q3 = V1_2 - V2_2, Q4 = V1_3 - V2_3;
+  const float Ph1 = V0_1, Ph2 = V0_2;
+  const int ti[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+  float Ex[3], Ep[6], Epx[3], Gx[3][3], s[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    Ex[i] = sp.E[ti[i][0]].hi * x[0] + sp.E[ti[i][1]].hi * x[1] + sp.E[ti[i][2]].hi * x[2];
+#pragma unroll
+  for (int t = 0; t < 6; ++t) Ep[t] = sp.F[3 * t].hi * x[0] + sp.F[3 * t + 1].hi * x[1] + sp.F[3 * t + 2].hi * x[2];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) Epx[n] = Ep[ti[n][0]] * x[0] + Ep[ti[n][1]] * x[1] + Ep[ti[n][2]] * x[2];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      Gx[i][j] = sp.F[3 * ti[j][0] + i].hi * x[0] + sp.F[3 * ti[j][1] + i].hi * x[1] + sp.F[3 * ti[j][2] + i].hi * x[2];
+    s[i] = Gx[i][0] * x[0] + Gx[i][1] * x[1] + Gx[i][2] * x[2];
+  }
+  const float q = Ex[0] * x[0] + Ex[1] * x[1] + Ex[2] * x[2];
+  const float qp = Epx[0] * x[0] + Epx[1] * x[1] + Epx[2] * x[2];
+  const float tEp = Ep[0] + Ep[3] + Ep[5];
+  const float vx = sp.v[0].hi * x[0] + sp.v[1].hi * x[1] + sp.v[2].hi * x[2];
+  const float wx = sp.w[0].hi * x[0] + sp.w[1].hi * x[1] + sp.w[2].hi * x[2];
+  const float tE = sp.tE.hi;
+  const float tv = tEp + 2.0f * vx;
+  const float A = Ps4 * q + Ps3 * tE - tE * Ph2 * tn2 + (Q4 * qp + Q3 * tv - wx * V1_2 * tn2);
+  const float B = Ps3 * q + Ps2 * tE - tE * Ph1 * tn2 + (Q3 * qp + Q2 * tv - wx * V1_1 * tn2);
+  const float cE = 2.0f * Ps3 - 2.0f * tn1 * Ph2;
+  const float cEp = 2.0f * Q3 - 2.0f * tn1 * V1_2, cv = 2.0f * Q2 - 2.0f * tn1 * V1_1;
+  const float cs = Q3, cgw = Q2 - tn2 * V1_1;
+  float W[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    W[i] = cE * Ex[i] + cEp * Epx[i] + cv * sp.v[i].hi + cs * s[i] + cgw * sp.w[i].hi;
+  const float C0 = 2.0f * Ps2 - 4.0f * tn1 * Ph1;
+  const float C1 = 2.0f * Q2 - 4.0f * tn1 * V1_1;
+  const float C2 = 2.0f * Q2 - 2.0f * tn1 * V1_1;
+  const int pi[6] = {0, 0, 0, 1, 1, 2}, pj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    const int i = pi[t], j = pj[t];
+    float r = A * x[i] * x[j] + W[i] * x[j] + W[j] * x[i] + C0 * sp.E[t].hi + C1 * Ep[t] + C2 * (Gx[i][j] + Gx[j][i]);
+    if (i == j) r += B;
+    e[t] = r;
+  }
+}
+
+// a += b (double-float plus FP32, error-free sum of the high parts)
+IBEM_HD IBEM_INLINE void df_add_f(dfloat& a, float b) {
+  const dfloat s = df_two_sum(a.hi, b);
+  a = df_fast_two_sum(s.hi, s.lo + a.lo);
+}
+
 }  // namespace ibem

@@ -73,6 +73,7 @@ __global__ void __launch_bounds__(kMfThreads)
     for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x) sx[i] = x[(int64_t)kMfNu * h0 + i];
     __syncthreads();
     if (!act) continue;
+#pragma unroll 1
     for (int hh = 0; hh < nh; ++hh) {
       const float4 qh = sgh[hh], ql = sgl[hh];
       const float ia = ql.w;
@@ -127,6 +128,7 @@ __global__ void __launch_bounds__(kMfThreads)
     for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x) sx[i] = x[(int64_t)kMfNu * h0 + i];
     __syncthreads();
     if (!act) continue;
+#pragma unroll 1
     for (int hh = 0; hh < nh; ++hh) {
       const double x0 = p0 - sc[4 * hh], x1 = p1 - sc[4 * hh + 1], x2 = p2 - sc[4 * hh + 2];
       const double a = sc[4 * hh + 3];

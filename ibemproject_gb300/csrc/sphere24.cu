@@ -4,6 +4,8 @@
 #include "prof.h"
 #include "sphere_kernels.cuh"
 
+#include <cub/device/device_radix_sort.cuh>
+
 IBEM_PAIR_KERNEL(pair24_c0_r0, sph_block24_c0_r0, 24)
 IBEM_PAIR_KERNEL(pair24_c0_r1, sph_block24_c0_r1, 24)
 IBEM_PAIR_KERNEL(pair24_c1_r0, sph_block24_c1_r0, 24)
@@ -13,20 +15,26 @@ IBEM_NODE_KERNEL(node24, sph_node24, 24)
 IBEM_FIELD_KERNEL(field24, sph_field24_contracted, 24)
 
 // Field sum of the mixed form: the same contraction in double-float arithmetic
-// (field_contract.cuh).  The loading threads turn each chunk of spheres into SphDF
-// constants (scaled coordinates); every thread keeps its point and its six strain sums in
-// double-float, and the inside test, the local eigenstrain and C0 run in FP64 at the end.
+// (field_contract.cuh), split by distance.  Points are processed in Morton order (a stable
+// radix sort of 30-bit keys inside the point cloud's bounding box), so the 32 points of a
+// warp form a compact cluster; a sphere that lies beyond kFarRadii radii from all 32 of them
+// is summed in FP32 (sph_field24_f32, warp-uniform branch), every other one in double-float.
+// The loading threads turn each chunk of spheres into SphDF constants (scaled coordinates);
+// every thread keeps its six strain sums in double-float, and the inside test, the local
+// eigenstrain and C0 run in FP64 at the end.
 __global__ void __launch_bounds__(ibem::kFieldThreads)
-    field24_df(const double* __restrict__ pts, int nump, const double* __restrict__ cen,
-               const double* __restrict__ rad, int num, SphMat mc, const double* __restrict__ E,
-               double* __restrict__ stress) {
+    field24_df(const double* __restrict__ pts, const int* __restrict__ order, int nump,
+               const double* __restrict__ cen, const double* __restrict__ rad, int num, SphMat mc,
+               const double* __restrict__ E, double* __restrict__ stress) {
   __shared__ ibem::SphDF ss[ibem::kFieldChunk];
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool act = s < nump;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool act = t < nump;
+  const int s = act ? order[t] : 0;
   double p0 = 0, p1 = 0, p2 = 0;
-  if (act) { p0 = pts[3 * s]; p1 = pts[3 * s + 1]; p2 = pts[3 * s + 2]; }
+  if (act) { p0 = pts[3 * (int64_t)s]; p1 = pts[3 * (int64_t)s + 1]; p2 = pts[3 * (int64_t)s + 2]; }
   const ibem::dfloat pd[3] = {ibem::df_make(p0), ibem::df_make(p1), ibem::df_make(p2)};
   const ibem::dfloat tn1 = ibem::df_make(mc.tn1), tn2 = ibem::df_make(mc.tn2);
+  const float far2 = ibem::kFarRadii * ibem::kFarRadii;
   ibem::dfloat acc[6] = {};
   int inside = -1;
   for (int h0 = 0; h0 < num; h0 += ibem::kFieldChunk) {
@@ -35,9 +43,23 @@ __global__ void __launch_bounds__(ibem::kFieldThreads)
     for (int i = threadIdx.x; i < nh; i += blockDim.x)
       ss[i] = ibem::sph_df_make(cen + 3 * (int64_t)(h0 + i), rad[h0 + i], E + 24 * (int64_t)(h0 + i));
     __syncthreads();
-    if (act)
-      for (int hh = 0; hh < nh; ++hh)
-        if (ibem::sph_field24_df(pd, ss[hh], tn1, tn2, acc)) inside = h0 + hh;
+#pragma unroll 1
+    for (int hh = 0; hh < nh; ++hh) {
+      const ibem::SphDF& sp = ss[hh];
+      const float dx = (pd[0].hi - sp.c[0].hi) * sp.ia.hi, dy = (pd[1].hi - sp.c[1].hi) * sp.ia.hi,
+                  dz = (pd[2].hi - sp.c[2].hi) * sp.ia.hi;
+      const bool far = !act || dx * dx + dy * dy + dz * dz > far2;
+      if (__all_sync(0xffffffffu, far)) {
+        if (act) {
+          float r[6];
+          ibem::sph_field24_f32(pd, sp, tn1.hi, tn2.hi, r);
+#pragma unroll
+          for (int k = 0; k < 6; ++k) ibem::df_add_f(acc[k], r[k]);
+        }
+      } else if (act) {
+        if (ibem::sph_field24_df(pd, sp, tn1, tn2, acc)) inside = h0 + hh;
+      }
+    }
   }
   if (!act) return;
   double e[6];
@@ -55,6 +77,50 @@ __global__ void __launch_bounds__(ibem::kFieldThreads)
   o[3] += mc.lam0 * tr + 2.0 * mc.mu0 * e[3];
   o[4] += 2.0 * mc.mu0 * e[4];
   o[5] += mc.lam0 * tr + 2.0 * mc.mu0 * e[5];
+}
+
+// Bounding box of the points (FP64 min / max, atomics on the ordered integer image).
+__device__ __forceinline__ unsigned long long ord_key(double v) {
+  const unsigned long long b = __double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double ord_val(unsigned long long k) {
+  return __longlong_as_double((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k);
+}
+__global__ void k_bbox(int n, const double* __restrict__ pts, unsigned long long* __restrict__ box) {
+  unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (int k = 0; k < 3; ++k) {
+      const unsigned long long o = ord_key(pts[3 * (int64_t)i + k]);
+      lo[k] = o < lo[k] ? o : lo[k];
+      hi[k] = o > hi[k] ? o : hi[k];
+    }
+  for (int k = 0; k < 3; ++k) {
+    atomicMin(box + k, lo[k]);
+    atomicMax(box + 3 + k, hi[k]);
+  }
+}
+__device__ __forceinline__ unsigned spread3(unsigned v) {  // 10 bits -> every third bit
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000ffu;
+  v = (v | (v << 8)) & 0x0300f00fu;
+  v = (v | (v << 4)) & 0x030c30c3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+__global__ void k_morton(int n, const double* __restrict__ pts, const unsigned long long* __restrict__ box,
+                         unsigned* __restrict__ key, int* __restrict__ idx) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned q[3];
+  for (int k = 0; k < 3; ++k) {
+    const double lo = ord_val(box[k]), hi = ord_val(box[3 + k]);
+    const double span = hi > lo ? hi - lo : 1.0;
+    const double f = (pts[3 * (int64_t)i + k] - lo) / span;
+    q[k] = (unsigned)min(1023.0, max(0.0, f * 1024.0));
+  }
+  key[i] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+  idx[i] = i;
 }
 
 namespace ibem {
@@ -95,12 +161,43 @@ ibem_status launch_field24(const SphLaunch& p, const double* pts, int nump, cons
 
 ibem_status launch_field24_df(const SphLaunch& p, const double* pts, int nump, const double* E,
                               double* stress, cudaStream_t st) {
+  if (nump <= 0) return IBEM_OK;
   SphMat mc = sph_mat_init(p.E0, p.nu0, p.E1, p.nu1);
   ProfScope ps(PROF_FIELD, st);
-  ::ibem::count_launch(), field24_df<<<(nump + kFieldThreads - 1) / kFieldThreads, kFieldThreads, 0, st>>>(
-      pts, nump, p.cen, p.rad, p.num, mc, E, stress);
-  IBEM_LAUNCH_CHECK("field24_df");
-  return IBEM_OK;
+  // Morton order of the points (stream-ordered scratch: keys, indices, sort workspace)
+  const unsigned nb = (unsigned)((nump + 255) / 256);
+  size_t sort_bytes = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, (const unsigned*)nullptr, (unsigned*)nullptr,
+                                  (const int*)nullptr, (int*)nullptr, nump, 0, 30, st);
+  const size_t n4 = ((size_t)nump * 4 + 255) / 256 * 256;
+  const size_t bytes = 64 + 4 * n4 + sort_bytes;
+  char* buf = nullptr;
+  IBEM_CUDA(cudaMallocAsync((void**)&buf, bytes, st));
+  unsigned long long* box = reinterpret_cast<unsigned long long*>(buf);
+  unsigned* k0 = reinterpret_cast<unsigned*>(buf + 64);
+  unsigned* k1 = reinterpret_cast<unsigned*>(buf + 64 + n4);
+  int* i0 = reinterpret_cast<int*>(buf + 64 + 2 * n4);
+  int* i1 = reinterpret_cast<int*>(buf + 64 + 3 * n4);
+  void* tmp = buf + 64 + 4 * n4;
+  const unsigned long long init[6] = {~0ull, ~0ull, ~0ull, 0, 0, 0};
+  ibem_status s = IBEM_OK;
+  cudaError_t e = cudaMemcpyAsync(box, init, sizeof(init), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    ::ibem::count_launch(), k_bbox<<<min(nb, 1024u), 256, 0, st>>>(nump, pts, box);
+    ::ibem::count_launch(), k_morton<<<nb, 256, 0, st>>>(nump, pts, box, k0, i0);
+    e = cub::DeviceRadixSort::SortPairs(tmp, sort_bytes, k0, k1, i0, i1, nump, 0, 30, st);
+  }
+  if (e == cudaSuccess) {
+    ::ibem::count_launch(), field24_df<<<(nump + kFieldThreads - 1) / kFieldThreads, kFieldThreads, 0, st>>>(
+        pts, i1, nump, p.cen, p.rad, p.num, mc, E, stress);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) s = cuda_fail(e, "field24_df");
+  cudaFreeAsync(buf, st);
+  // the host array `init` is read by the copy above before this function returns
+  const cudaError_t e2 = cudaStreamSynchronize(st);
+  if (!s && e2 != cudaSuccess) s = cuda_fail(e2, "field24_df");
+  return s;
 }
 
 }  // namespace ibem

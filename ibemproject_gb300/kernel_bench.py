@@ -8,6 +8,8 @@
                event time) and the BF16 split kernels.
 --lu N         ibem_e3d_solve of a random, diagonally dominant N x N system with the
                per-phase profile (panel, row exchanges, TRSM, GEMM, triangular solves).
+--field NUM,G  the double-float stress sums (ibem_e3d_field_form, mixed form) of NUM spheres
+               at G^3 grid points with random coefficients: NUM * G^3 pairs per launch.
 --mf NUM       the matrix-free products (ibem_e3d_mf_matvec, FP32 scaled and FP64) on a
                far-field microstructure of NUM spheres (bench distribution): NUM^2 pair
                products per launch, timed by the library's phase events.
@@ -113,12 +115,43 @@ def bench_mf(num, reps, dev):
     return out
 
 
+def bench_field(num, grid, reps, dev):
+    import numpy as np
+    from . import Material, batch as B, cases
+    c = cases.farfield_case(num=num, r0=0.012, vf=0.15, grid=grid, seed=2024)
+    L = lib()
+    m = Material(c.E0, c.nu0, c.E1, c.nu1)
+    g = torch.Generator(device="cpu").manual_seed(5)
+    E = (torch.randn(24 * num, generator=g, dtype=torch.float64) * 1e-11).to(dev)
+    cen = torch.from_numpy(np.ascontiguousarray(c.centers)).to(dev)
+    rad = torch.from_numpy(np.ascontiguousarray(c.radius)).to(dev)
+    pts = torch.from_numpy(np.ascontiguousarray(c.points)).to(dev)
+    S = torch.empty((c.nump, 6), dtype=torch.float64, device=dev)
+    sig = np.ascontiguousarray(c.sig_inf)
+    sigp = sig.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    sp = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    run = lambda: check(L.ibem_e3d_field_form(SOLVE_MIXED_IR, _p(pts), c.nump, _p(cen), _p(rad), num, ctypes.byref(m),
+                                              24, _p(E), None, 0, None, 0, None, None, sigp, _p(S), sp))
+    run()
+    torch.cuda.synchronize()
+    L.ibem_prof_enable(1)
+    for _ in range(reps):
+        run()
+    prof = prof_report()
+    L.ibem_prof_enable(0)
+    ms = prof.get("field", {}).get("ms", 0.0) / reps
+    pairs = num * c.nump
+    return {"kernel": "field24_df", "spheres": num, "points": c.nump, "pairs": pairs, "reps": reps, "ms": ms,
+            "ns_per_pair": ms * 1e6 / pairs if ms > 0 else None}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gemm", action="append", default=[], help="M,N,K")
     ap.add_argument("--lu", type=int, action="append", default=[])
     ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--mf", type=int, action="append", default=[])
+    ap.add_argument("--field", action="append", default=[], help="NUM,GRID")
     ap.add_argument("--reps", type=int, default=3)
     a = ap.parse_args(argv)
     dev = torch.device("cuda", 0)
@@ -130,6 +163,9 @@ def main(argv=None):
         print(json.dumps(bench_lu(n, a.form, a.reps, dev)), flush=True)
     for n in a.mf:
         print(json.dumps(bench_mf(n, a.reps, dev)), flush=True)
+    for f in a.field:
+        num, grid = (int(v) for v in f.split(","))
+        print(json.dumps(bench_field(num, grid, a.reps, dev)), flush=True)
     return 0
 
 

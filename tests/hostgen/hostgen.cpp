@@ -157,3 +157,15 @@ extern "C" int hg_pair_apply24(int fp32, const double* x, double a, double E0, d
   }
   return 0;
 }
+
+// the FP32 far-pair form of the contraction (field_contract.cuh: sph_field24_f32)
+extern "C" int hg_field24f32(const double* p, const double* cen, double a, double E0, double nu0, double E1,
+                             double nu1, const double* E, double* e) {
+  SphMat mc = sph_mat_init(E0, nu0, E1, nu1);
+  const ibem::SphDF sp = ibem::sph_df_make(cen, a, E);
+  const ibem::dfloat pd[3] = {ibem::df_make(p[0]), ibem::df_make(p[1]), ibem::df_make(p[2])};
+  float r[6];
+  ibem::sph_field24_f32(pd, sp, (float)mc.tn1, (float)mc.tn2, r);
+  for (int t = 0; t < 6; ++t) e[t] = mc.kd * (double)r[t];
+  return 0;
+}

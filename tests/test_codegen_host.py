@@ -173,3 +173,24 @@ def test_pair_apply_matches_generated_block(hg, fp32):
         tol = 2e-5 if fp32 else 1e-12
         assert np.abs(got[:6] - want[:6]).max() <= tol * np.abs(want[:6]).max(), (t, got[:6], want[:6])
         assert np.abs(got[6:] - want[6:]).max() <= tol * np.abs(want[6:]).max(), (t, got[6:], want[6:])
+
+
+def test_field24_f32_far_pairs(hg):
+    """The FP32 far-pair contraction of the mixed stress sums against the FP64 contraction:
+    beyond 14 radii its relative error stays at the FP32 rounding level (< 3e-6 of the
+    largest strain component), and its size relative to a contact-distance sphere is below
+    (1/14)^3, which is what bounds its share of the summed error."""
+    rng = np.random.default_rng(21)
+    worst = 0.0
+    for t in range(200):
+        a = 0.012 * (0.8 + 0.4 * rng.random())
+        cen = rng.random(3) * 0.4
+        x = rng.normal(size=3)
+        x *= a * (14.0 + 30.0 * rng.random()) / np.linalg.norm(x)
+        E = rng.normal(size=24) * 1e-3
+        E[6:] /= a
+        e1, e2 = np.zeros(6), np.zeros(6)
+        hg.hg_field24c(d(np.ascontiguousarray(x)), ctypes.c_double(a), *_mat(), d(E), d(e1))
+        hg.hg_field24f32(d(cen + x), d(cen), ctypes.c_double(a), *_mat(), d(E), d(e2))
+        worst = max(worst, scaled_err(e2, e1))
+    assert worst < 3e-6, worst

@@ -199,8 +199,10 @@ def test_tensor_core_gemm(g, m, n, k):
 @pytest.mark.gpu
 def test_field_double_float_vs_fp64_and_oracle(g, oracle_mod):
     """Stresses of the 24-unknown layout: the FP64 sums match the oracle to 1e-11 and the
-    double-float sums of the mixed form (ibem_e3d_field_form) to 1e-10 (scaled), with
-    points inside, near and far from the spheres."""
+    split sums of the mixed form (ibem_e3d_field_form: double-float for spheres within 14
+    radii of a warp's points, FP32 beyond) to 1e-9 (scaled), with points inside, near and
+    far from the spheres.  The FP32 share is designed for ~1e-9 of the strain (random-sign
+    coefficients, as here, are its worst case); the solution target is 1e-8."""
     from ibemproject_gb300 import cases
     c = cases.farfield_case(num=60, r0=0.05, vf=0.15, grid=10, seed=3)
     rng = np.random.default_rng(4)
@@ -221,5 +223,5 @@ def test_field_double_float_vs_fp64_and_oracle(g, oracle_mod):
         out[form] = S.cpu().numpy()
     ref = oracle_mod.post(c, 24, E, sig_inf=c.sig_inf)
     assert scaled_err(out[g.SOLVE_FP64], ref) < 1e-11
-    assert scaled_err(out[g.SOLVE_MIXED_IR], ref) < 1e-10
-    assert scaled_err(out[g.SOLVE_MIXED_IR], out[g.SOLVE_FP64]) < 1e-10
+    assert scaled_err(out[g.SOLVE_MIXED_IR], ref) < 1e-9
+    assert scaled_err(out[g.SOLVE_MIXED_IR], out[g.SOLVE_FP64]) < 1e-9
