@@ -165,12 +165,12 @@ def roofline(prof):
 
 
 def roofline_chosen(prof, case):
-    """Roofline of the largest kernel of the matrix-free step, the double-float stress sums
+    """Roofline of the largest kernel of the matrix-free step, the split stress sums
     (field24_df): FP32-pipe bound.  Algorithmic work = FP32 flops per (point, sphere) pair
-    (counted by ncu's FP32 instruction counters on a small case, FFMA counted twice) x the
-    pairs of one launch, over its event-timed duration; peak = the nominal FP32 FMA rate
-    (152 SMs x 128 lanes x 2 flops) at the measured maximum SM clock, as MEASURED_PEAKS.json
-    holds no FP32 figure."""
+    of this workload (ncu's FP32 instruction counters over one full-size launch, FFMA counted
+    twice) x the pairs of one launch, over its event-timed duration; peak = the nominal FP32
+    FMA rate (152 SMs x 128 lanes x 2 flops) at the measured maximum SM clock, as
+    MEASURED_PEAKS.json holds no FP32 figure."""
     f = prof.get("field")
     if not f or f["ms"] <= 0:
         return None
@@ -182,21 +182,22 @@ def roofline_chosen(prof, case):
     peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
     pairs = case.nump * case.num
     achieved = FIELD_DF_FLOPS_PER_PAIR * pairs / (f["ms"] / f["launches"] * 1e-3) / 1e12
-    return {"kernel": "field24_df (stress sums, double-float)", "bound": "fp32", "achieved": achieved,
+    return {"kernel": "field24_df (stress sums, double-float near / FP32 far)", "bound": "fp32", "achieved": achieved,
             "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
             "peak_source": f"nominal FP32 FMA rate at sm_max_mhz {mhz:g} (no measured FP32 peak)",
             "flops_per_pair": FIELD_DF_FLOPS_PER_PAIR, "pairs_per_launch": pairs,
             "avg_launch_ms": f["ms"] / f["launches"], "traffic": FIELD_DF_TRAFFIC_PER_LAUNCH,
             "traffic_unit": "bytes per launch (ncu dram read+write)",
-            "traffic_source": "profiles/launches_bench_2000spheres_learned_step.md",
-            "flops_source": "profiles/field24_df_bench200.md"}
+            "traffic_source": "profiles/field24_df_bench2000.md",
+            "flops_source": "profiles/field24_df_bench2000.md"}
 
 
-# FP32 flops per (point, sphere) pair of field24_df: FADD + FMUL + 2 FFMA thread instructions
-# counted by ncu on the 200-sphere, 16^3-point case (2.776e9 flops / 819,200 pairs); DRAM
-# bytes (read + write) of its full-size launch from the launch list of one bench step
-FIELD_DF_FLOPS_PER_PAIR = 3388.0
-FIELD_DF_TRAFFIC_PER_LAUNCH = 20.24e6
+# FP32 flops per (point, sphere) pair of field24_df on this workload: FADD + FMUL + 2 FFMA
+# thread instructions of one full-size launch counted by ncu (4.668e11 flops / 5.243e8 pairs;
+# double-float for the ~16% of (warp, sphere) pairs within 14 radii, FP32 beyond), and its
+# DRAM bytes (read + write) per launch from the same capture
+FIELD_DF_FLOPS_PER_PAIR = 890.4
+FIELD_DF_TRAFFIC_PER_LAUNCH = 20.46e6
 
 
 # ------------------------------------------------------------------ clocks

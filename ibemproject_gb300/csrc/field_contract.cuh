@@ -131,6 +131,7 @@ struct SphDF {
   dfloat v[3];   // v_n = sum_m F_mnm
   dfloat w[3];   // w_p = sum_m F_mmp (also the trace vector g of the derivation)
   dfloat tE;     // trace of E
+  float pad[2];  // 288 bytes: 18 float4
 };
 
 IBEM_HD inline SphDF sph_df_make(const double* cen, double a, const double* Eu) {

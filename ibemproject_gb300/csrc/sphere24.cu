@@ -22,10 +22,18 @@ IBEM_FIELD_KERNEL(field24, sph_field24_contracted, 24)
 // The loading threads turn each chunk of spheres into SphDF constants (scaled coordinates);
 // every thread keeps its six strain sums in double-float, and the inside test, the local
 // eigenstrain and C0 run in FP64 at the end.
+// per-sphere double-float constants, computed once per call (FP64 arithmetic, one thread each)
+__global__ void k_sph_df(int num, const double* __restrict__ cen, const double* __restrict__ rad,
+                         const double* __restrict__ E, ibem::SphDF* __restrict__ out) {
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h < num) out[h] = ibem::sph_df_make(cen + 3 * (int64_t)h, rad[h], E + 24 * (int64_t)h);
+}
+
 __global__ void __launch_bounds__(ibem::kFieldThreads)
     field24_df(const double* __restrict__ pts, const int* __restrict__ order, int nump,
-               const double* __restrict__ cen, const double* __restrict__ rad, int num, SphMat mc,
+               const double* __restrict__ cen, const ibem::SphDF* __restrict__ sph, int num, SphMat mc,
                const double* __restrict__ E, double* __restrict__ stress) {
+  static_assert(sizeof(ibem::SphDF) == 18 * sizeof(float4), "SphDF is copied as 18 float4");
   __shared__ ibem::SphDF ss[ibem::kFieldChunk];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const bool act = t < nump;
@@ -40,8 +48,11 @@ __global__ void __launch_bounds__(ibem::kFieldThreads)
   for (int h0 = 0; h0 < num; h0 += ibem::kFieldChunk) {
     const int nh = min(ibem::kFieldChunk, num - h0);
     __syncthreads();
-    for (int i = threadIdx.x; i < nh; i += blockDim.x)
-      ss[i] = ibem::sph_df_make(cen + 3 * (int64_t)(h0 + i), rad[h0 + i], E + 24 * (int64_t)(h0 + i));
+    {
+      const float4* src = reinterpret_cast<const float4*>(sph + h0);
+      float4* dst = reinterpret_cast<float4*>(ss);
+      for (int i = threadIdx.x; i < nh * 18; i += blockDim.x) dst[i] = src[i];
+    }
     __syncthreads();
 #pragma unroll 1
     for (int hh = 0; hh < nh; ++hh) {
@@ -170,7 +181,8 @@ ibem_status launch_field24_df(const SphLaunch& p, const double* pts, int nump, c
   cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, (const unsigned*)nullptr, (unsigned*)nullptr,
                                   (const int*)nullptr, (int*)nullptr, nump, 0, 30, st);
   const size_t n4 = ((size_t)nump * 4 + 255) / 256 * 256;
-  const size_t bytes = 64 + 4 * n4 + sort_bytes;
+  const size_t nsph = ((size_t)p.num * sizeof(SphDF) + 255) / 256 * 256;
+  const size_t bytes = 64 + 4 * n4 + nsph + sort_bytes;
   char* buf = nullptr;
   IBEM_CUDA(cudaMallocAsync((void**)&buf, bytes, st));
   unsigned long long* box = reinterpret_cast<unsigned long long*>(buf);
@@ -178,18 +190,20 @@ ibem_status launch_field24_df(const SphLaunch& p, const double* pts, int nump, c
   unsigned* k1 = reinterpret_cast<unsigned*>(buf + 64 + n4);
   int* i0 = reinterpret_cast<int*>(buf + 64 + 2 * n4);
   int* i1 = reinterpret_cast<int*>(buf + 64 + 3 * n4);
-  void* tmp = buf + 64 + 4 * n4;
+  SphDF* sph = reinterpret_cast<SphDF*>(buf + 64 + 4 * n4);
+  void* tmp = buf + 64 + 4 * n4 + nsph;
   const unsigned long long init[6] = {~0ull, ~0ull, ~0ull, 0, 0, 0};
   ibem_status s = IBEM_OK;
   cudaError_t e = cudaMemcpyAsync(box, init, sizeof(init), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     ::ibem::count_launch(), k_bbox<<<min(nb, 1024u), 256, 0, st>>>(nump, pts, box);
     ::ibem::count_launch(), k_morton<<<nb, 256, 0, st>>>(nump, pts, box, k0, i0);
+    if (p.num > 0) ::ibem::count_launch(), k_sph_df<<<(p.num + 127) / 128, 128, 0, st>>>(p.num, p.cen, p.rad, E, sph);
     e = cub::DeviceRadixSort::SortPairs(tmp, sort_bytes, k0, k1, i0, i1, nump, 0, 30, st);
   }
   if (e == cudaSuccess) {
     ::ibem::count_launch(), field24_df<<<(nump + kFieldThreads - 1) / kFieldThreads, kFieldThreads, 0, st>>>(
-        pts, i1, nump, p.cen, p.rad, p.num, mc, E, stress);
+        pts, i1, nump, p.cen, sph, p.num, mc, E, stress);
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) s = cuda_fail(e, "field24_df");
