@@ -12,7 +12,7 @@
 // (w = alpha = 0: block-Jacobi; w = alpha = 1: the truncated series; trained weights absorb
 // the higher-order terms and the neighbours left out).
 //
-// Kernels: k_knn (brute force within a realisation), k_features, k_edge_corr (one CTA of
+// Kernels: k_knn (brute force within a realisation, one warp per particle), k_features, k_edge_corr (one CTA of
 // 64 threads per edge: four threads evaluate the two FP32 pair blocks into shared memory,
 // all 64 form the four 24 x 24 products), the network's dense layers as one tiled FP32 GEMM
 // kernel (k_gemm, 64 x 64 tiles, optional transposes, bias, ReLU, atomic split-K for the
@@ -60,11 +60,14 @@ struct Layout {
 
 // ---------------------------------------------------------------- graph and features
 // k nearest neighbours of p within its realisation: distance^2 in FP64, ties to the
-// lower index; kept sorted by insertion
+// lower index.  One warp per particle: every lane keeps a sorted list of the best 16 of its
+// own share of the candidates (q = first + lane, + 32, ...), then 16 rounds of a warp-wide
+// minimum over the lanes' list heads pick the result in order.
 __global__ void k_knn(int num, const int* __restrict__ seg_of, const int* __restrict__ seg_begin,
                       const double* __restrict__ cen, int* __restrict__ nbr) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= num) return;
+  const int p = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (p >= num) return;  // uniform per warp
   const int sg = seg_of[p];
   const int b0 = seg_begin[sg], b1 = seg_begin[sg + 1];
   const double px = cen[3 * (int64_t)p], py = cen[3 * (int64_t)p + 1], pz = cen[3 * (int64_t)p + 2];
@@ -75,11 +78,11 @@ __global__ void k_knn(int num, const int* __restrict__ seg_of, const int* __rest
     bd[j] = INFINITY;
     bi[j] = -1;
   }
-  for (int q = b0; q < b1; ++q) {
+  for (int q = b0 + lane; q < b1; q += 32) {
     if (q == p) continue;
     const double dx = cen[3 * (int64_t)q] - px, dy = cen[3 * (int64_t)q + 1] - py, dz = cen[3 * (int64_t)q + 2] - pz;
     const double d2 = dx * dx + dy * dy + dz * dz;
-    if (!(d2 < bd[kKnn - 1])) continue;  // q > every kept index: equal distance loses
+    if (!(d2 < bd[kKnn - 1])) continue;  // later q of this lane: an equal distance loses
     double cd = d2;
     int ci = q;
 #pragma unroll
@@ -94,8 +97,32 @@ __global__ void k_knn(int num, const int* __restrict__ seg_of, const int* __rest
       }
     }
   }
+  int mine = -1;
+#pragma unroll 1
+  for (int r = 0; r < kKnn; ++r) {
+    double wd = bd[0];
+    int wi = bi[0];
 #pragma unroll
-  for (int j = 0; j < kKnn; ++j) nbr[(int64_t)kKnn * p + j] = bi[j];
+    for (int off = 16; off; off >>= 1) {
+      const double od = __shfl_xor_sync(0xffffffffu, wd, off);
+      const int oi = __shfl_xor_sync(0xffffffffu, wi, off);
+      if (od < wd || (od == wd && (unsigned)oi < (unsigned)wi)) {
+        wd = od;
+        wi = oi;
+      }
+    }
+    if (lane == r) mine = wi;
+    if (wi >= 0 && bi[0] == wi) {  // candidates are unique across lanes: one lane pops
+#pragma unroll
+      for (int j = 0; j < kKnn - 1; ++j) {
+        bd[j] = bd[j + 1];
+        bi[j] = bi[j + 1];
+      }
+      bd[kKnn - 1] = INFINITY;
+      bi[kKnn - 1] = -1;
+    }
+  }
+  if (lane < kKnn) nbr[(int64_t)kKnn * p + lane] = mine;
 }
 
 struct MatFeat {
@@ -640,7 +667,7 @@ struct Prepared {
 int64_t gnn_param_count() { return Layout().total; }
 
 ibem_status gnn_knn(const MfBatch& b, int* nbr, cudaStream_t st) {
-  ::ibem::count_launch(), k_knn<<<nb(b.num, 128), 128, 0, st>>>(b.num, b.seg_of, b.seg_begin, b.cen, nbr);
+  ::ibem::count_launch(), k_knn<<<nb((int64_t)b.num * 32, 128), 128, 0, st>>>(b.num, b.seg_of, b.seg_begin, b.cen, nbr);
   IBEM_LAUNCH_CHECK("knn");
   return IBEM_OK;
 }
