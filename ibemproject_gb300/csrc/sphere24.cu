@@ -106,9 +106,17 @@ __global__ void k_bbox(int n, const double* __restrict__ pts, unsigned long long
       lo[k] = o < lo[k] ? o : lo[k];
       hi[k] = o > hi[k] ? o : hi[k];
     }
-  for (int k = 0; k < 3; ++k) {
-    atomicMin(box + k, lo[k]);
-    atomicMax(box + 3 + k, hi[k]);
+  for (int k = 0; k < 3; ++k) {  // warp minimum / maximum first: one atomic per warp
+    for (int off = 16; off; off >>= 1) {
+      const unsigned long long ol = __shfl_xor_sync(0xffffffffu, lo[k], off);
+      const unsigned long long oh = __shfl_xor_sync(0xffffffffu, hi[k], off);
+      lo[k] = ol < lo[k] ? ol : lo[k];
+      hi[k] = oh > hi[k] ? oh : hi[k];
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(box + k, lo[k]);
+      atomicMax(box + 3 + k, hi[k]);
+    }
   }
 }
 __device__ __forceinline__ unsigned spread3(unsigned v) {  // 10 bits -> every third bit
@@ -196,7 +204,7 @@ ibem_status launch_field24_df(const SphLaunch& p, const double* pts, int nump, c
   ibem_status s = IBEM_OK;
   cudaError_t e = cudaMemcpyAsync(box, init, sizeof(init), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
-    ::ibem::count_launch(), k_bbox<<<min(nb, 1024u), 256, 0, st>>>(nump, pts, box);
+    ::ibem::count_launch(), k_bbox<<<min(nb, 304u), 256, 0, st>>>(nump, pts, box);
     ::ibem::count_launch(), k_morton<<<nb, 256, 0, st>>>(nump, pts, box, k0, i0);
     if (p.num > 0) ::ibem::count_launch(), k_sph_df<<<(p.num + 127) / 128, 128, 0, st>>>(p.num, p.cen, p.rad, E, sph);
     e = cub::DeviceRadixSort::SortPairs(tmp, sort_bytes, k0, k1, i0, i1, nump, 0, 30, st);

@@ -10,6 +10,10 @@
                per-phase profile (panel, row exchanges, TRSM, GEMM, triangular solves).
 --field NUM,G  the double-float stress sums (ibem_e3d_field_form, mixed form) of NUM spheres
                at G^3 grid points with random coefficients: NUM * G^3 pairs per launch.
+--solve NUM    the matrix-free solve of one far-field microstructure of NUM spheres (bench
+               distribution, N = 24 NUM) with block-Jacobi, Neumann and learned
+               preconditioners (the network trained first on 12 microstructures of 100-150
+               spheres): time, Arnoldi and refinement steps, phase times.
 --mf NUM       the matrix-free products (ibem_e3d_mf_matvec, FP32 scaled and FP64) on a
                far-field microstructure of NUM spheres (bench distribution): NUM^2 pair
                products per launch, timed by the library's phase events.
@@ -145,6 +149,42 @@ def bench_field(num, grid, reps, dev):
             "ns_per_pair": ms * 1e6 / pairs if ms > 0 else None}
 
 
+def bench_solve(num, reps, dev):
+    import numpy as np
+    from . import batch as B
+    from . import cases
+    import time
+    rng = np.random.default_rng(77)
+    train = [cases.farfield_case(num=int(n), r0=0.012, vf=0.15, grid=0, seed=9000 + k)
+             for k, n in enumerate(rng.integers(100, 151, size=12))]
+    tb = B.DeviceBatch(train, device=dev)
+    r, e = B.training_pairs(tb, nrhs=4, seed=5)
+    params = B.init_params(seed=1, device=dev)
+    hist = B.train(tb, r, e, params, steps=300, lr=3e-3)
+    c = cases.farfield_case(num=num, r0=0.012, vf=0.15, grid=0, seed=2024)
+    bt = B.DeviceBatch([c], device=dev)
+    b = B.farfield_rhs(bt, np.array([0, 0, 0, 0, 0, 1.0]))
+    out = {"kernel": "matrix-free solve", "spheres": num, "N": 24 * num, "reps": reps,
+           "training_loss": [float(hist[0]), float(hist[-1])]}
+    L = lib()
+    for name, pc, pp in (("block_jacobi", B.PRECOND_BLOCK_JACOBI, None), ("neumann", B.PRECOND_NEUMANN, None),
+                         ("learned", B.PRECOND_LEARNED, params)):
+        B.solve(bt, b, pc, params=pp)   # warm-up
+        torch.cuda.synchronize()
+        L.ibem_prof_enable(1)
+        t = time.perf_counter()
+        for _ in range(reps):
+            x, rep = B.solve(bt, b, pc, params=pp)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t) / reps
+        prof = prof_report()
+        L.ibem_prof_enable(0)
+        out[name] = {"s": dt, "arnoldi_steps": rep[0].inner, "refinement_steps": rep[0].outer,
+                     "rel_residual": rep[0].rel_residual,
+                     "phases_ms": {k: round(v["ms"] / reps, 3) for k, v in prof.items()}}
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gemm", action="append", default=[], help="M,N,K")
@@ -152,6 +192,7 @@ def main(argv=None):
     ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--mf", type=int, action="append", default=[])
     ap.add_argument("--field", action="append", default=[], help="NUM,GRID")
+    ap.add_argument("--solve", type=int, action="append", default=[])
     ap.add_argument("--reps", type=int, default=3)
     a = ap.parse_args(argv)
     dev = torch.device("cuda", 0)
@@ -163,6 +204,8 @@ def main(argv=None):
         print(json.dumps(bench_lu(n, a.form, a.reps, dev)), flush=True)
     for n in a.mf:
         print(json.dumps(bench_mf(n, a.reps, dev)), flush=True)
+    for n in a.solve:
+        print(json.dumps(bench_solve(n, a.reps, dev)), flush=True)
     for f in a.field:
         num, grid = (int(v) for v in f.split(","))
         print(json.dumps(bench_field(num, grid, a.reps, dev)), flush=True)
