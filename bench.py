@@ -193,11 +193,11 @@ def roofline_chosen(prof, case):
 
 
 # FP32 flops per (point, sphere) pair of field24_df on this workload: FADD + FMUL + 2 FFMA
-# thread instructions of one full-size launch counted by ncu (4.668e11 flops / 5.243e8 pairs;
+# thread instructions of one full-size launch counted by ncu (4.660e11 flops / 5.243e8 pairs;
 # double-float for the ~16% of (warp, sphere) pairs within 14 radii, FP32 beyond), and its
 # DRAM bytes (read + write) per launch from the same capture
-FIELD_DF_FLOPS_PER_PAIR = 890.4
-FIELD_DF_TRAFFIC_PER_LAUNCH = 20.46e6
+FIELD_DF_FLOPS_PER_PAIR = 888.8
+FIELD_DF_TRAFFIC_PER_LAUNCH = 21.10e6
 
 
 # ------------------------------------------------------------------ clocks
