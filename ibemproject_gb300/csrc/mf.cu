@@ -4,7 +4,7 @@
 // orders 0 and 1) are never formed: their products with the coefficients are evaluated
 // as the contracted strain and its gradient (mf_contract.cuh):
 //   k_mf_apply_f32  As x in FP32 on the scaled system (mf.h), the GMRES operator;
-//   k_mf_apply_f64  A x in FP64, physical units, the refinement residual b - A x.
+//   k_mf_apply_f64  As x in FP64, the refinement residual Dr b - As xs.
 // One thread per target particle s, 128 consecutive targets of one realisation per CTA;
 // the CTA's source particles h (a slice of the realisation, gridDim.y slices) are staged
 // through shared memory in chunks with their coefficients, and every thread sums the
@@ -81,18 +81,23 @@ __global__ void __launch_bounds__(kMfThreads)
       const float x0 = ((ph.x - qh.x) + (pl.x - ql.x)) * ia;
       const float x1 = ((ph.y - qh.y) + (pl.y - ql.y)) * ia;
       const float x2 = ((ph.z - qh.z) + (pl.z - ql.z)) * ia;
-      const float* xs = sx + kMfNu * hh;
-      sph_pair_apply24<float>(x0, x1, x2, 1.f, mc.kmu, mc.klam, mc.tn1, mc.tn2, xs, ph.w * ia, acc);
-      MvSink<float> s0{acc, xs};
-      if (h0 + hh == s) sph_self24f(mc, s0);
+      sph_pair_apply24<float, true>(x0, x1, x2, 1.f, 0.f, 0.f, mc.tn1, mc.tn2, sx + kMfNu * hh, ph.w * ia, acc);
     }
   }
   if (!act) return;
+  float yv[kMfNu];
+  sph_pair_map24<float>(acc, mc.kmu, mc.klam, yv);
+  if (s >= hb && s < he) {  // the slice holding the target adds its self term (C0 / mu0)
+    MvSink<float> sk{yv, x + (int64_t)kMfNu * s};
+    sph_self24f(mc, sk);
+  }
   float* o = y + (int64_t)kMfNu * s;
 #pragma unroll
-  for (int r = 0; r < kMfNu; ++r) atomicAdd(o + r, acc[r]);
+  for (int r = 0; r < kMfNu; ++r) atomicAdd(o + r, yv[r]);
 }
 
+// FP64 product of the scaled system (the refinement residual): the same evaluation as the
+// FP32 kernel in double precision, offsets from FP64 centres.
 __global__ void __launch_bounds__(kMfThreads)
     k_mf_apply_f64(const MfTile* __restrict__ tiles, const int* __restrict__ seg_begin,
                    const double* __restrict__ cen, const double* __restrict__ rad,
@@ -106,12 +111,13 @@ __global__ void __launch_bounds__(kMfThreads)
   if (hb >= he) return;
   const int s = t.s0 + threadIdx.x;
   const bool act = threadIdx.x < t.ns;
-  const SphMat mc = mats[t.seg];
-  double p0 = 0, p1 = 0, p2 = 0;
+  const SphMat mc = mats[t.seg];   // moduli divided by mu0 (scaled system)
+  double p0 = 0, p1 = 0, p2 = 0, as = 1;
   if (act) {
     p0 = cen[3 * (int64_t)s];
     p1 = cen[3 * (int64_t)s + 1];
     p2 = cen[3 * (int64_t)s + 2];
+    as = rad[s];
   }
   double acc[kMfNu];
 #pragma unroll
@@ -123,24 +129,28 @@ __global__ void __launch_bounds__(kMfThreads)
       sc[4 * i] = cen[3 * (int64_t)(h0 + i)];
       sc[4 * i + 1] = cen[3 * (int64_t)(h0 + i) + 1];
       sc[4 * i + 2] = cen[3 * (int64_t)(h0 + i) + 2];
-      sc[4 * i + 3] = rad[h0 + i];
+      sc[4 * i + 3] = 1.0 / rad[h0 + i];
     }
     for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x) sx[i] = x[(int64_t)kMfNu * h0 + i];
     __syncthreads();
     if (!act) continue;
 #pragma unroll 1
     for (int hh = 0; hh < nh; ++hh) {
-      const double x0 = p0 - sc[4 * hh], x1 = p1 - sc[4 * hh + 1], x2 = p2 - sc[4 * hh + 2];
-      const double a = sc[4 * hh + 3];
-      sph_pair_apply24<double>(x0, x1, x2, a, mc.kmu, mc.klam, mc.tn1, mc.tn2, sx + kMfNu * hh, 1.0, acc);
-      MvSink<double> sk{acc, sx + kMfNu * hh};
-      if (h0 + hh == s) sph_self24(mc, sk);
+      const double ia = sc[4 * hh + 3];
+      const double x0 = (p0 - sc[4 * hh]) * ia, x1 = (p1 - sc[4 * hh + 1]) * ia, x2 = (p2 - sc[4 * hh + 2]) * ia;
+      sph_pair_apply24<double, true>(x0, x1, x2, 1.0, 0.0, 0.0, mc.tn1, mc.tn2, sx + kMfNu * hh, as * ia, acc);
     }
   }
   if (!act) return;
+  double yv[kMfNu];
+  sph_pair_map24<double>(acc, mc.kmu, mc.klam, yv);
+  if (s >= hb && s < he) {
+    MvSink<double> sk{yv, x + (int64_t)kMfNu * s};
+    sph_self24(mc, sk);
+  }
   double* o = y + (int64_t)kMfNu * s;
 #pragma unroll
-  for (int r = 0; r < kMfNu; ++r) atomicAdd(o + r, acc[r]);
+  for (int r = 0; r < kMfNu; ++r) atomicAdd(o + r, yv[r]);
 }
 
 // Geometry in the FP32 layout, scalings, segment of every particle.
@@ -439,11 +449,15 @@ __global__ void k_f32_div(int64_t n, const float* __restrict__ x, const double* 
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) y[i] = (double)x[i] / d[i];
 }
-// rs = dr * (b - y)
-__global__ void k_resid(int64_t n, const double* __restrict__ dr, const double* __restrict__ b,
-                        const double* __restrict__ y, double* __restrict__ rs) {
+// out = a - b (FP64)
+__global__ void k_sub64(int64_t n, const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) rs[i] = dr[i] * (b[i] - y[i]);
+  if (i < n) out[i] = a[i] - b[i];
+}
+// y = x / d (FP64)
+__global__ void k_div64(int64_t n, const double* __restrict__ x, const double* __restrict__ d, double* __restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = x[i] / d[i];
 }
 __global__ void k_to_f32(int64_t n, const double* __restrict__ x, float* __restrict__ y) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -507,12 +521,19 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
   // slices of the source range: about 4 CTAs per SM in total, at least 32 sources per slice
   const int want = 152 * 4;
   b.hsplit = std::max(1, std::min((want + b.ntiles - 1) / b.ntiles, (b.max_seg + 31) / 32));
-  std::vector<SphMat> md(in.nseg);
+  std::vector<SphMat> md(in.nseg), ms(in.nseg);
   std::vector<SphMatF> mf(in.nseg);
   for (int s = 0; s < in.nseg; ++s) {
     const ibem_material& m = in.mats[s];
     md[s] = sph_mat_init(m.E0, m.nu0, m.E1, m.nu1);
     mf[s] = sph_matf_init(md[s]);
+    ms[s] = md[s];  // scaled: moduli / mu0
+    const double k = 1.0 / md[s].mu0;
+    ms[s].kmu *= k;
+    ms[s].klam *= k;
+    ms[s].lam0 *= k;
+    ms[s].twomu0 *= k;
+    ms[s].mu0 = 1.0;
   }
   IBEM_CUDA(cudaMalloc(&b.seg_begin, sizeof(int) * (in.nseg + 1)));
   IBEM_CUDA(cudaMalloc(&b.seg_of, sizeof(int) * b.num));
@@ -520,6 +541,7 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
   IBEM_CUDA(cudaMalloc(&b.gl, sizeof(float4) * b.num));
   IBEM_CUDA(cudaMalloc(&b.matd, sizeof(SphMat) * in.nseg));
   IBEM_CUDA(cudaMalloc(&b.matf, sizeof(SphMatF) * in.nseg));
+  IBEM_CUDA(cudaMalloc(&b.mats, sizeof(SphMat) * in.nseg));
   IBEM_CUDA(cudaMalloc(&b.dr, sizeof(double) * b.N));
   IBEM_CUDA(cudaMalloc(&b.dc, sizeof(double) * b.N));
   IBEM_CUDA(cudaMalloc(&b.tiles, sizeof(MfTile) * b.ntiles));
@@ -527,6 +549,7 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
   IBEM_CUDA(cudaMemcpyAsync(b.seg_of, seg_of.data(), sizeof(int) * b.num, cudaMemcpyHostToDevice, st));
   IBEM_CUDA(cudaMemcpyAsync(b.matd, md.data(), sizeof(SphMat) * in.nseg, cudaMemcpyHostToDevice, st));
   IBEM_CUDA(cudaMemcpyAsync(b.matf, mf.data(), sizeof(SphMatF) * in.nseg, cudaMemcpyHostToDevice, st));
+  IBEM_CUDA(cudaMemcpyAsync(b.mats, ms.data(), sizeof(SphMat) * in.nseg, cudaMemcpyHostToDevice, st));
   IBEM_CUDA(cudaMemcpyAsync(b.tiles, tiles.data(), sizeof(MfTile) * b.ntiles, cudaMemcpyHostToDevice, st));
   ::ibem::count_launch(), k_mf_prep<<<nblk(b.num), 256, 0, st>>>(b.num, b.cen, b.rad, b.seg_of, b.matd, b.gh, b.gl,
                                                                  b.dr, b.dc);
@@ -543,6 +566,7 @@ void mf_batch_free(MfBatch& b) {
   cudaFree(b.gl);
   cudaFree(b.matd);
   cudaFree(b.matf);
+  cudaFree(b.mats);
   cudaFree(b.dr);
   cudaFree(b.dc);
   cudaFree(b.tiles);
@@ -562,7 +586,7 @@ ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStrea
   ProfScope ps(PROF_MF_F64, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
   ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, b.cen,
-                                                                                         b.rad, b.matd, x, y);
+                                                                                         b.rad, b.mats, x, y);
   IBEM_LAUNCH_CHECK("mf apply f64");
   return IBEM_OK;
 }
@@ -714,11 +738,12 @@ ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPr
   const int64_t N = b.N;
   MfSolver g(b, st, o.restart);
   ibem_status s = g.alloc();
-  double *xs = nullptr, *rs = nullptr, *y = nullptr, *bn2 = nullptr;
+  double *xs = nullptr, *rs = nullptr, *y = nullptr, *bs = nullptr, *bn2 = nullptr;
   if (!s) {
     cudaError_t e = cudaMalloc(&xs, sizeof(double) * N);
     if (e == cudaSuccess) e = cudaMalloc(&rs, sizeof(double) * N);
     if (e == cudaSuccess) e = cudaMalloc(&y, sizeof(double) * N);
+    if (e == cudaSuccess) e = cudaMalloc(&bs, sizeof(double) * N);
     if (e == cudaSuccess) e = cudaMalloc(&bn2, sizeof(double) * 2 * S);
     if (e != cudaSuccess) s = cuda_fail(e, "mf solve workspace");
   }
@@ -726,7 +751,8 @@ ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPr
   std::vector<int> hdone(S, 0), outer_of(S, 0);
   if (!s) {
     cudaMemsetAsync(xs, 0, sizeof(double) * N, st);
-    ::ibem::count_launch(), k_mul<<<nblk(N), 256, 0, st>>>(N, b.dr, bvec, rs);  // rs = Dr b (x = 0)
+    ::ibem::count_launch(), k_mul<<<nblk(N), 256, 0, st>>>(N, b.dr, bvec, bs);  // bs = Dr b
+    cudaMemcpyAsync(rs, bs, sizeof(double) * N, cudaMemcpyDeviceToDevice, st);  // rs = bs (x = 0)
     s = g.seg_norm2(rs, bn2);
     if (!s) {
       cudaMemcpyAsync(hb.data(), bn2, sizeof(double) * S, cudaMemcpyDeviceToHost, st);
@@ -760,9 +786,8 @@ ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPr
     ::ibem::count_launch(), k_to_f32<<<nblk(N), 256, 0, st>>>(N, rs, g.rin);
     if ((s = g.gmres(P, o.max_cycles, o.inner_tol))) break;
     ::ibem::count_launch(), k_acc_f32<<<nblk(N), 256, 0, st>>>(N, g.d, xs);
-    ::ibem::count_launch(), k_mul<<<nblk(N), 256, 0, st>>>(N, b.dc, xs, x);
-    if ((s = mf_apply_f64(b, x, y, st))) break;
-    ::ibem::count_launch(), k_resid<<<nblk(N), 256, 0, st>>>(N, b.dr, bvec, y, rs);
+    if ((s = mf_apply_f64(b, xs, y, st))) break;   // As xs in FP64
+    ::ibem::count_launch(), k_sub64<<<nblk(N), 256, 0, st>>>(N, bs, y, rs);  // rs = bs - As xs
     IBEM_LAUNCH_CHECK("mf refinement");
     ++outer;
   }
@@ -782,6 +807,7 @@ ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPr
   cudaFree(xs);
   cudaFree(rs);
   cudaFree(y);
+  cudaFree(bs);
   cudaFree(bn2);
   return s;
 }
@@ -800,7 +826,21 @@ extern "C" ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int preci
   ibem_status s = mf_batch_init(b, *batch, st);
   if (!s) {
     if (precision == 64) {
-      s = mf_apply_f64(b, x_dev, y_dev, st);
+      double *xs = nullptr, *ys = nullptr;
+      cudaError_t e = cudaMalloc(&xs, sizeof(double) * b.N);
+      if (e == cudaSuccess) e = cudaMalloc(&ys, sizeof(double) * b.N);
+      if (e != cudaSuccess) s = cuda_fail(e, "mf_matvec workspace");
+      if (!s) {
+        ::ibem::count_launch(), k_div64<<<nblk(b.N), 256, 0, st>>>(b.N, x_dev, b.dc, xs);  // xs = x / Dc
+        s = mf_apply_f64(b, xs, ys, st);
+        if (!s) ::ibem::count_launch(), k_div64<<<nblk(b.N), 256, 0, st>>>(b.N, ys, b.dr, y_dev);  // y = ys / Dr
+      }
+      if (!s) {
+        const cudaError_t e2 = cudaStreamSynchronize(st);
+        if (e2 != cudaSuccess) s = cuda_fail(e2, "mf_matvec");
+      }
+      cudaFree(xs);
+      cudaFree(ys);
     } else {
       float *xf = nullptr, *yf = nullptr;
       cudaError_t e = cudaMalloc(&xf, sizeof(float) * b.N);

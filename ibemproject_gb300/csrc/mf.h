@@ -44,6 +44,7 @@ struct MfBatch {
   float4* gl = nullptr;       // centre (low float parts), 1 / radius
   SphMat* matd = nullptr;     // per segment, physical units
   SphMatF* matf = nullptr;    // per segment, divided by mu0
+  SphMat* mats = nullptr;     // per segment, FP64, divided by mu0 (scaled system)
   double* dr = nullptr;       // N: row scaling
   double* dc = nullptr;       // N: column scaling
   MfTile* tiles = nullptr;
@@ -63,7 +64,7 @@ struct MfPrecond {
   float* Q = nullptr;    // num*kKnn x 24 x 24 off-diagonal blocks, or nullptr (block-diagonal)
   int* nbr = nullptr;    // num*kKnn neighbour indices (-1: empty slot)
 };
-// y = A x (FP64, physical units); y is overwritten
+// y = As x (FP64, scaled system); y is overwritten
 ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st);
 // P[p] = inverse of the scaled diagonal block As[p, p] (24 x 24, row-major, FP32)
 ibem_status mf_block_jacobi(const MfBatch& b, float* P, cudaStream_t st);

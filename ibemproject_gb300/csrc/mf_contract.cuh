@@ -40,7 +40,10 @@ IBEM_HD IBEM_INLINE double rsqrt_t(double x) {
 
 // y[24] += the pair block (target at offset x from a source of radius a) times Eu[24];
 // kmu, klam, tn1 = 1 - nu0, tn2 = 2 nu0 as in SphMat; row_scale multiplies the order-1 rows.
-template <class R>
+// With RAW, y instead accumulates the contraction itself (r_t in y[t], row_scale * d_k r_t in
+// y[6 + 3t + k]) and the caller applies the same kmu / klam map once after the sum over
+// sources (sph_pair_map24): the map is linear and the same for every source of a target.
+template <class R, bool RAW = false>
 IBEM_HD IBEM_INLINE void sph_pair_apply24(R x0, R x1, R x2, R a, R kmu, R klam, R tn1, R tn2,
                                           const R* __restrict__ Eu, R row_scale, R (&y)[24]) {
   const R x[3] = {x0, x1, x2};
@@ -149,6 +152,15 @@ IBEM_HD IBEM_INLINE void sph_pair_apply24(R x0, R x1, R x2, R a, R kmu, R klam, 
       g[t][k] = Ru * x[k] + P;
     }
   }
+  if (RAW) {
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      y[t] += r[t];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) y[6 + 3 * t + k] += row_scale * g[t][k];
+    }
+    return;
+  }
   const R tr = r[0] + r[3] + r[5];
   const R dtr[3] = {g[0][0] + g[3][0] + g[5][0], g[0][1] + g[3][1] + g[5][1], g[0][2] + g[3][2] + g[5][2]};
 #pragma unroll
@@ -157,6 +169,22 @@ IBEM_HD IBEM_INLINE void sph_pair_apply24(R x0, R x1, R x2, R a, R kmu, R klam, 
     y[t] += d ? kmu * r[t] + klam * tr : kmu * r[t];
 #pragma unroll
     for (int k = 0; k < 3; ++k) y[6 + 3 * t + k] += row_scale * (d ? kmu * g[t][k] + klam * dtr[k] : kmu * g[t][k]);
+  }
+}
+
+// y = the kmu / klam map of a raw accumulation (sph_pair_apply24<R, true>)
+template <class R>
+IBEM_HD IBEM_INLINE void sph_pair_map24(const R (&acc)[24], R kmu, R klam, R (&y)[24]) {
+  const R tr = acc[0] + acc[3] + acc[5];
+  R dtr[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) dtr[k] = acc[6 + k] + acc[6 + 9 + k] + acc[6 + 15 + k];
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    const bool d = (t == 0 || t == 3 || t == 5);
+    y[t] = d ? kmu * acc[t] + klam * tr : kmu * acc[t];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) y[6 + 3 * t + k] = d ? kmu * acc[6 + 3 * t + k] + klam * dtr[k] : kmu * acc[6 + 3 * t + k];
   }
 }
 
