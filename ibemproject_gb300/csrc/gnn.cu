@@ -544,10 +544,10 @@ struct Net {
   // backward
   float *dw, *dO1, *dEin, *dH, *dHn, *dUpd, *dUin, *dM;
   ~Net() {
-    for (void* p : mem) cudaFree(p);
+    for (void* p : mem) free_async(p, st);
   }
   ibem_status buf(float*& p, int64_t n) {
-    IBEM_CUDA(cudaMalloc(&p, sizeof(float) * std::max<int64_t>(n, 1)));
+    IBEM_CUDA(alloc_async((void**)&p, sizeof(float) * std::max<int64_t>(n, 1), st));
     mem.push_back(p);
     return IBEM_OK;
   }
@@ -648,15 +648,16 @@ ibem_status loss_grad(Net& net, const int* nbr, const float* xn, const float* ef
 }
 
 struct Prepared {
+  cudaStream_t st = nullptr;
   std::vector<void*> mem;
   int* nbr = nullptr;
   float *xn = nullptr, *ef = nullptr, *z = nullptr, *u = nullptr, *B = nullptr;
   ~Prepared() {
-    for (void* p : mem) cudaFree(p);
+    for (void* p : mem) free_async(p, st);
   }
   template <class T>
   ibem_status buf(T*& p, int64_t n) {
-    IBEM_CUDA(cudaMalloc(&p, sizeof(T) * std::max<int64_t>(n, 1)));
+    IBEM_CUDA(alloc_async((void**)&p, sizeof(T) * std::max<int64_t>(n, 1), st));
     mem.push_back(p);
     return IBEM_OK;
   }
@@ -679,11 +680,11 @@ ibem_status gnn_features(const MfBatch& b, const int* nbr, float* xn, float* ef,
     h[s] = {(float)(m.E1 / (10.0 * m.E0)), (float)m.nu0, (float)m.nu1};
   }
   MatFeat* d = nullptr;
-  IBEM_CUDA(cudaMalloc(&d, sizeof(MatFeat) * b.nseg));
+  IBEM_CUDA(alloc_async((void**)&d, sizeof(MatFeat) * b.nseg, st));
   IBEM_CUDA(cudaMemcpyAsync(d, h.data(), sizeof(MatFeat) * b.nseg, cudaMemcpyHostToDevice, st));
   ::ibem::count_launch(), k_features<<<nb((int64_t)b.num * kKnn), 256, 0, st>>>(b.num, b.seg_of, d, b.cen, b.rad, nbr, xn, ef);
-  const cudaError_t e = cudaStreamSynchronize(st);
-  cudaFree(d);
+  const cudaError_t e = cudaStreamSynchronize(st);   // the host array h is read by the copy above
+  free_async(d, st);
   if (e != cudaSuccess) return cuda_fail(e, "gnn features");
   IBEM_LAUNCH_CHECK("gnn features");
   return IBEM_OK;
@@ -707,8 +708,7 @@ ibem_status gnn_forward_weights(int num, const int* nbr, const float* xn, const 
   ibem_status s = net.alloc(false);
   if (!s) s = net.forward(nbr, xn, ef, params);
   if (!s) IBEM_CUDA(cudaMemcpyAsync(w, net.w, sizeof(float) * net.E * kGnnOut, cudaMemcpyDeviceToDevice, st));
-  if (!s) IBEM_CUDA(cudaStreamSynchronize(st));
-  return s;
+  return s;   // stream-ordered: the network's buffers are freed after the copy
 }
 
 __global__ void k_fill1(int64_t n, float* __restrict__ p) {
@@ -718,9 +718,10 @@ __global__ void k_fill1(int64_t n, float* __restrict__ p) {
 
 ibem_status mf_neighbour_precond(const MfBatch& b, const float* params, MfPrecond& pc, cudaStream_t st) {
   Prepared pr;
+  pr.st = st;
   const int64_t E = (int64_t)b.num * kKnn;
-  IBEM_CUDA(cudaMalloc(&pc.nbr, sizeof(int) * E));
-  IBEM_CUDA(cudaMalloc(&pc.Q, sizeof(float) * E * kMfNu * kMfNu));
+  IBEM_CUDA(alloc_async((void**)&pc.nbr, sizeof(int) * E, st));
+  IBEM_CUDA(alloc_async((void**)&pc.Q, sizeof(float) * E * kMfNu * kMfNu, st));
   pr.nbr = pc.nbr;
   float* wa = nullptr;
   ibem_status s = pr.buf(wa, E * kGnnOut);
@@ -736,7 +737,6 @@ ibem_status mf_neighbour_precond(const MfBatch& b, const float* params, MfPrecon
   }
   if (!s) IBEM_CUDA(cudaMemcpyAsync(pr.B, pc.D, sizeof(float) * b.num * kMfNu * kMfNu, cudaMemcpyDeviceToDevice, st));
   if (!s) s = gnn_edge_corrections(b, pc.nbr, pr.B, wa, pc.D, pc.Q, 0, nullptr, nullptr, st);
-  if (!s) IBEM_CUDA(cudaStreamSynchronize(st));
   return s;
 }
 
@@ -824,6 +824,7 @@ extern "C" ibem_status ibem_gnn_prepare(const ibem_e3d_batch* batch, int nrhs, c
   ibem_status s = mf_batch_init(b, *batch, st);
   if (!s) {
     Prepared pr;
+    pr.st = st;
     // the caller's buffers are used in place (prepare allocates only what is missing)
     s = prepare(b, nrhs, r_hat_dev, e_hat_dev, pr, nbr_dev, node_feat_dev, edge_feat_dev, z_dev, u_dev, st);
   }
@@ -886,6 +887,7 @@ extern "C" ibem_status ibem_gnn_train(const ibem_e3d_batch* batch, int nrhs, con
   if (s) return s;
   {
     Prepared pr;
+    pr.st = st;
     s = prepare(b, nrhs, r_hat_dev, e_hat_dev, pr, nullptr, nullptr, nullptr, nullptr, nullptr, st);
     Net net;
     net.num = b.num;

@@ -496,6 +496,7 @@ inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t
 ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st) {
   if (in.nseg <= 0 || !in.seg_begin || !in.centers_dev || !in.radius_dev || !in.mats)
     return fail(IBEM_ERR_ARG, "mf: bad batch");
+  b.st = st;
   b.nseg = in.nseg;
   b.seg_begin_h.assign(in.seg_begin, in.seg_begin + in.nseg + 1);
   b.mats_h.assign(in.mats, in.mats + in.nseg);
@@ -535,16 +536,16 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
     ms[s].twomu0 *= k;
     ms[s].mu0 = 1.0;
   }
-  IBEM_CUDA(cudaMalloc(&b.seg_begin, sizeof(int) * (in.nseg + 1)));
-  IBEM_CUDA(cudaMalloc(&b.seg_of, sizeof(int) * b.num));
-  IBEM_CUDA(cudaMalloc(&b.gh, sizeof(float4) * b.num));
-  IBEM_CUDA(cudaMalloc(&b.gl, sizeof(float4) * b.num));
-  IBEM_CUDA(cudaMalloc(&b.matd, sizeof(SphMat) * in.nseg));
-  IBEM_CUDA(cudaMalloc(&b.matf, sizeof(SphMatF) * in.nseg));
-  IBEM_CUDA(cudaMalloc(&b.mats, sizeof(SphMat) * in.nseg));
-  IBEM_CUDA(cudaMalloc(&b.dr, sizeof(double) * b.N));
-  IBEM_CUDA(cudaMalloc(&b.dc, sizeof(double) * b.N));
-  IBEM_CUDA(cudaMalloc(&b.tiles, sizeof(MfTile) * b.ntiles));
+  IBEM_CUDA(alloc_async((void**)&b.seg_begin, sizeof(int) * (in.nseg + 1), st));
+  IBEM_CUDA(alloc_async((void**)&b.seg_of, sizeof(int) * b.num, st));
+  IBEM_CUDA(alloc_async((void**)&b.gh, sizeof(float4) * b.num, st));
+  IBEM_CUDA(alloc_async((void**)&b.gl, sizeof(float4) * b.num, st));
+  IBEM_CUDA(alloc_async((void**)&b.matd, sizeof(SphMat) * in.nseg, st));
+  IBEM_CUDA(alloc_async((void**)&b.matf, sizeof(SphMatF) * in.nseg, st));
+  IBEM_CUDA(alloc_async((void**)&b.mats, sizeof(SphMat) * in.nseg, st));
+  IBEM_CUDA(alloc_async((void**)&b.dr, sizeof(double) * b.N, st));
+  IBEM_CUDA(alloc_async((void**)&b.dc, sizeof(double) * b.N, st));
+  IBEM_CUDA(alloc_async((void**)&b.tiles, sizeof(MfTile) * b.ntiles, st));
   IBEM_CUDA(cudaMemcpyAsync(b.seg_begin, b.seg_begin_h.data(), sizeof(int) * (in.nseg + 1), cudaMemcpyHostToDevice, st));
   IBEM_CUDA(cudaMemcpyAsync(b.seg_of, seg_of.data(), sizeof(int) * b.num, cudaMemcpyHostToDevice, st));
   IBEM_CUDA(cudaMemcpyAsync(b.matd, md.data(), sizeof(SphMat) * in.nseg, cudaMemcpyHostToDevice, st));
@@ -560,16 +561,17 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
 }
 
 void mf_batch_free(MfBatch& b) {
-  cudaFree(b.seg_begin);
-  cudaFree(b.seg_of);
-  cudaFree(b.gh);
-  cudaFree(b.gl);
-  cudaFree(b.matd);
-  cudaFree(b.matf);
-  cudaFree(b.mats);
-  cudaFree(b.dr);
-  cudaFree(b.dc);
-  cudaFree(b.tiles);
+  const cudaStream_t st = b.st;
+  free_async(b.seg_begin, st);
+  free_async(b.seg_of, st);
+  free_async(b.gh, st);
+  free_async(b.gl, st);
+  free_async(b.matd, st);
+  free_async(b.matf, st);
+  free_async(b.mats, st);
+  free_async(b.dr, st);
+  free_async(b.dc, st);
+  free_async(b.tiles, st);
   b = MfBatch();
 }
 
@@ -620,26 +622,26 @@ struct MfSolver {
     splits = (int)((kMfNu * (int64_t)b.max_seg + kDotThreads * kDotRows - 1) / (kDotThreads * kDotRows));
   }
   ~MfSolver() {
-    cudaFree(V);
-    cudaFree(z);
-    cudaFree(w);
-    cudaFree(d);
-    cudaFree(rin);
-    cudaFree(r32);
-    cudaFree(done);
-    cudaFree(kmem);
+    free_async(V, st);
+    free_async(z, st);
+    free_async(w, st);
+    free_async(d, st);
+    free_async(rin, st);
+    free_async(r32, st);
+    free_async(done, st);
+    free_async(kmem, st);
   }
   ibem_status alloc() {
-    IBEM_CUDA(cudaMalloc(&V, sizeof(float) * N * (m + 1)));
-    IBEM_CUDA(cudaMalloc(&z, sizeof(float) * N));
-    IBEM_CUDA(cudaMalloc(&w, sizeof(float) * N));
-    IBEM_CUDA(cudaMalloc(&d, sizeof(float) * N));
-    IBEM_CUDA(cudaMalloc(&rin, sizeof(float) * N));
-    IBEM_CUDA(cudaMalloc(&r32, sizeof(float) * N));
-    IBEM_CUDA(cudaMalloc(&done, sizeof(int) * b.nseg));
+    IBEM_CUDA(alloc_async((void**)&V, sizeof(float) * N * (m + 1), st));
+    IBEM_CUDA(alloc_async((void**)&z, sizeof(float) * N, st));
+    IBEM_CUDA(alloc_async((void**)&w, sizeof(float) * N, st));
+    IBEM_CUDA(alloc_async((void**)&d, sizeof(float) * N, st));
+    IBEM_CUDA(alloc_async((void**)&rin, sizeof(float) * N, st));
+    IBEM_CUDA(alloc_async((void**)&r32, sizeof(float) * N, st));
+    IBEM_CUDA(alloc_async((void**)&done, sizeof(int) * b.nseg, st));
     const size_t S = b.nseg;
     const size_t nd = S * ((size_t)(m + 1) * m + (m + 1) + 2 * (size_t)m + 4 + 2 * (size_t)(m + 1) + m);
-    IBEM_CUDA(cudaMalloc(&kmem, nd * sizeof(double) + sizeof(int) * (3 * S + 1)));
+    IBEM_CUDA(alloc_async((void**)&kmem, nd * sizeof(double) + sizeof(int) * (3 * S + 1), st));
     double* p = (double*)kmem;
     K.H = p; p += S * (m + 1) * m;
     K.g = p; p += S * (m + 1);
@@ -740,11 +742,11 @@ ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPr
   ibem_status s = g.alloc();
   double *xs = nullptr, *rs = nullptr, *y = nullptr, *bs = nullptr, *bn2 = nullptr;
   if (!s) {
-    cudaError_t e = cudaMalloc(&xs, sizeof(double) * N);
-    if (e == cudaSuccess) e = cudaMalloc(&rs, sizeof(double) * N);
-    if (e == cudaSuccess) e = cudaMalloc(&y, sizeof(double) * N);
-    if (e == cudaSuccess) e = cudaMalloc(&bs, sizeof(double) * N);
-    if (e == cudaSuccess) e = cudaMalloc(&bn2, sizeof(double) * 2 * S);
+    cudaError_t e = alloc_async((void**)&xs, sizeof(double) * N, st);
+    if (e == cudaSuccess) e = alloc_async((void**)&rs, sizeof(double) * N, st);
+    if (e == cudaSuccess) e = alloc_async((void**)&y, sizeof(double) * N, st);
+    if (e == cudaSuccess) e = alloc_async((void**)&bs, sizeof(double) * N, st);
+    if (e == cudaSuccess) e = alloc_async((void**)&bn2, sizeof(double) * 2 * S, st);
     if (e != cudaSuccess) s = cuda_fail(e, "mf solve workspace");
   }
   std::vector<double> hb(S), hr(S);
@@ -804,11 +806,11 @@ ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPr
     for (int i = 0; i < S && !s; ++i)
       if (!(rep[i].rel_residual <= o.tol)) s = fail(IBEM_ERR_NOCONV, "mf solve: a realisation missed the tolerance");
   }
-  cudaFree(xs);
-  cudaFree(rs);
-  cudaFree(y);
-  cudaFree(bs);
-  cudaFree(bn2);
+  free_async(xs, st);
+  free_async(rs, st);
+  free_async(y, st);
+  free_async(bs, st);
+  free_async(bn2, st);
   return s;
 }
 
@@ -827,8 +829,8 @@ extern "C" ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int preci
   if (!s) {
     if (precision == 64) {
       double *xs = nullptr, *ys = nullptr;
-      cudaError_t e = cudaMalloc(&xs, sizeof(double) * b.N);
-      if (e == cudaSuccess) e = cudaMalloc(&ys, sizeof(double) * b.N);
+      cudaError_t e = alloc_async((void**)&xs, sizeof(double) * b.N, st);
+      if (e == cudaSuccess) e = alloc_async((void**)&ys, sizeof(double) * b.N, st);
       if (e != cudaSuccess) s = cuda_fail(e, "mf_matvec workspace");
       if (!s) {
         ::ibem::count_launch(), k_div64<<<nblk(b.N), 256, 0, st>>>(b.N, x_dev, b.dc, xs);  // xs = x / Dc
@@ -839,12 +841,12 @@ extern "C" ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int preci
         const cudaError_t e2 = cudaStreamSynchronize(st);
         if (e2 != cudaSuccess) s = cuda_fail(e2, "mf_matvec");
       }
-      cudaFree(xs);
-      cudaFree(ys);
+      free_async(xs, st);
+      free_async(ys, st);
     } else {
       float *xf = nullptr, *yf = nullptr;
-      cudaError_t e = cudaMalloc(&xf, sizeof(float) * b.N);
-      if (e == cudaSuccess) e = cudaMalloc(&yf, sizeof(float) * b.N);
+      cudaError_t e = alloc_async((void**)&xf, sizeof(float) * b.N, st);
+      if (e == cudaSuccess) e = alloc_async((void**)&yf, sizeof(float) * b.N, st);
       if (e != cudaSuccess) s = cuda_fail(e, "mf_matvec workspace");
       if (!s) {
         ::ibem::count_launch(), k_div_to_f32<<<nblk(b.N), 256, 0, st>>>(b.N, x_dev, b.dc, xf);  // xs = x / Dc
@@ -855,8 +857,8 @@ extern "C" ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int preci
         const cudaError_t e2 = cudaStreamSynchronize(st);
         if (e2 != cudaSuccess) s = cuda_fail(e2, "mf_matvec");
       }
-      cudaFree(xf);
-      cudaFree(yf);
+      free_async(xf, st);
+      free_async(yf, st);
     }
   }
   if (!s) {
@@ -890,7 +892,7 @@ extern "C" ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const doub
   ibem_status s = mf_batch_init(b, *batch, st);
   MfPrecond P;
   if (!s) {
-    const cudaError_t e = cudaMalloc(&P.D, sizeof(float) * kMfNu * kMfNu * (size_t)b.num);
+    const cudaError_t e = alloc_async((void**)&P.D, sizeof(float) * kMfNu * kMfNu * (size_t)b.num, st);
     if (e != cudaSuccess) s = cuda_fail(e, "mf_solve: preconditioner blocks");
   }
   {
@@ -913,9 +915,9 @@ extern "C" ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const doub
     reports[i].t_setup_ms = t_set;
     reports[i].t_solve_ms = t_sol;
   }
-  cudaFree(P.D);
-  cudaFree(P.Q);
-  cudaFree(P.nbr);
+  free_async(P.D, st);
+  free_async(P.Q, st);
+  free_async(P.nbr, st);
   mf_batch_free(b);
   return s;
 }
@@ -943,7 +945,7 @@ extern "C" ibem_status ibem_e3d_effective_modulus(const ibem_e3d_batch* batch, c
   const int S = batch->nseg;
   std::vector<double> h(6 * (size_t)S);
   if (!s) {
-    cudaError_t e = cudaMalloc(&acc, sizeof(double) * 6 * S);
+    cudaError_t e = alloc_async((void**)&acc, sizeof(double) * 6 * S, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(acc, 0, sizeof(double) * 6 * S, st);
     if (e != cudaSuccess) s = cuda_fail(e, "effective_modulus");
   }
@@ -967,7 +969,7 @@ extern "C" ibem_status ibem_e3d_effective_modulus(const ibem_e3d_batch* batch, c
       e_eff[i] = eps[5] != 0 ? sig_inf[5] / eps[5] : 0.0;
     }
   }
-  cudaFree(acc);
+  free_async(acc, st);
   mf_batch_free(b);
   return s;
 }
@@ -989,13 +991,13 @@ extern "C" ibem_status ibem_e3d_run_host_mf(const ibem_material* mat, int num, c
   ibem_status s = IBEM_OK;
   {
     cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&cen, sizeof(double) * 3 * num);
-    if (e == cudaSuccess) e = cudaMalloc(&rad, sizeof(double) * num);
-    if (e == cudaSuccess) e = cudaMalloc(&pts, sizeof(double) * 3 * std::max(nump, 1));
-    if (e == cudaSuccess) e = cudaMalloc(&b, sizeof(double) * N);
-    if (e == cudaSuccess) e = cudaMalloc(&x, sizeof(double) * N);
-    if (e == cudaSuccess) e = cudaMalloc(&S, sizeof(double) * 6 * std::max(nump, 1));
-    if (e == cudaSuccess && gnn_params) e = cudaMalloc(&prm, sizeof(float) * np);
+    if (e == cudaSuccess) e = alloc_async((void**)&cen, sizeof(double) * 3 * num, st);
+    if (e == cudaSuccess) e = alloc_async((void**)&rad, sizeof(double) * num, st);
+    if (e == cudaSuccess) e = alloc_async((void**)&pts, sizeof(double) * 3 * std::max(nump, 1), st);
+    if (e == cudaSuccess) e = alloc_async((void**)&b, sizeof(double) * N, st);
+    if (e == cudaSuccess) e = alloc_async((void**)&x, sizeof(double) * N, st);
+    if (e == cudaSuccess) e = alloc_async((void**)&S, sizeof(double) * 6 * std::max(nump, 1), st);
+    if (e == cudaSuccess && gnn_params) e = alloc_async((void**)&prm, sizeof(float) * np, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(cen, centers, sizeof(double) * 3 * num, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(rad, radius, sizeof(double) * num, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && nump > 0) e = cudaMemcpyAsync(pts, points, sizeof(double) * 3 * nump, cudaMemcpyHostToDevice, st);
@@ -1016,13 +1018,13 @@ extern "C" ibem_status ibem_e3d_run_host_mf(const ibem_material* mat, int num, c
     if (e != cudaSuccess) s = cuda_fail(e, "run_host_mf: results");
   }
   if (st) cudaStreamSynchronize(st);
-  cudaFree(cen);
-  cudaFree(rad);
-  cudaFree(pts);
-  cudaFree(b);
-  cudaFree(x);
-  cudaFree(S);
-  cudaFree(prm);
+  free_async(cen, st);
+  free_async(rad, st);
+  free_async(pts, st);
+  free_async(b, st);
+  free_async(x, st);
+  free_async(S, st);
+  free_async(prm, st);
   if (st) cudaStreamDestroy(st);
   return s;
 }

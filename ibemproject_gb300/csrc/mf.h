@@ -31,7 +31,18 @@ struct MfTile {
   int seg, s0, ns, pad;     // one CTA's target particles s0 .. s0 + ns - 1 of segment seg
 };
 
+// Stream-ordered scratch: allocations and frees of the solver's temporaries are queued on
+// the call's stream (cudaMallocAsync / cudaFreeAsync), so that no call synchronises the
+// device to release memory.
+inline cudaError_t alloc_async(void** p, size_t bytes, cudaStream_t st) {
+  return cudaMallocAsync(p, bytes > 0 ? bytes : 1, st);
+}
+inline void free_async(void* p, cudaStream_t st) {
+  if (p) cudaFreeAsync(p, st);
+}
+
 struct MfBatch {
+  cudaStream_t st = nullptr;   // stream of the call that owns the batch's buffers
   int nseg = 0, num = 0, max_seg = 0;
   int64_t N = 0;
   std::vector<int> seg_begin_h;

@@ -200,9 +200,10 @@ ibem_status launch_field24_df(const SphLaunch& p, const double* pts, int nump, c
   int* i1 = reinterpret_cast<int*>(buf + 64 + 3 * n4);
   SphDF* sph = reinterpret_cast<SphDF*>(buf + 64 + 4 * n4);
   void* tmp = buf + 64 + 4 * n4 + nsph;
-  const unsigned long long init[6] = {~0ull, ~0ull, ~0ull, 0, 0, 0};
   ibem_status s = IBEM_OK;
-  cudaError_t e = cudaMemcpyAsync(box, init, sizeof(init), cudaMemcpyHostToDevice, st);
+  // box = (min, min, min, max, max, max) starts at (all ones, zeros) in the ordered-integer image
+  cudaError_t e = cudaMemsetAsync(box, 0xff, 3 * sizeof(unsigned long long), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(box + 3, 0, 3 * sizeof(unsigned long long), st);
   if (e == cudaSuccess) {
     ::ibem::count_launch(), k_bbox<<<min(nb, 304u), 256, 0, st>>>(nump, pts, box);
     ::ibem::count_launch(), k_morton<<<nb, 256, 0, st>>>(nump, pts, box, k0, i0);
@@ -216,9 +217,6 @@ ibem_status launch_field24_df(const SphLaunch& p, const double* pts, int nump, c
   }
   if (e != cudaSuccess) s = cuda_fail(e, "field24_df");
   cudaFreeAsync(buf, st);
-  // the host array `init` is read by the copy above before this function returns
-  const cudaError_t e2 = cudaStreamSynchronize(st);
-  if (!s && e2 != cudaSuccess) s = cuda_fail(e2, "field24_df");
   return s;
 }
 
