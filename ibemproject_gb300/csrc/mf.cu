@@ -10,9 +10,11 @@
 // through shared memory in chunks with their coefficients, and every thread sums the
 // pair products in registers.  Slices add their partial sums atomically.
 //
-// Solver: FP64 iterative refinement x += Dc d; each correction d solves As d = Dr r with a
-// restarted FP32 GMRES right-preconditioned by a block-diagonal P (block-Jacobi or learned),
-// all realisations of a batch in lock step (per-realisation Arnoldi: segmented dot
+// Solver: iterative refinement x += Dc d; each correction d solves As d = Dr r with a
+// restarted FP32 GMRES right-preconditioned by a block-sparse P (block-Jacobi, Neumann or
+// learned); the residual that drives the next correction is a double-float product
+// (k_mf_apply_df, ~48 bits) and the one that decides convergence the FP64 product.  All
+// realisations of a batch run in lock step (per-realisation Arnoldi: segmented dot
 // products, Hessenberg updates and Givens rotations on the device, one thread per
 // realisation), stopping each realisation on its own residual estimate.
 #include <cuda_runtime.h>
@@ -25,6 +27,7 @@
 
 #include "gen_sphere24.cuh"
 #include "mf.h"
+#include "dfnum.cuh"
 #include "mf_contract.cuh"
 #include "prof.h"
 
@@ -151,6 +154,69 @@ __global__ void __launch_bounds__(kMfThreads)
   double* o = y + (int64_t)kMfNu * s;
 #pragma unroll
   for (int r = 0; r < kMfNu; ++r) atomicAdd(o + r, yv[r]);
+}
+
+// The scaled product in double-float arithmetic (~48 bits): the residual that drives a
+// refinement step (the final residual, which decides convergence, is the FP64 kernel's).
+// Centres, inverse radii and coefficients are staged as double-float pairs.
+struct DfSink {
+  DF (&acc)[kMfNu];
+  const double* __restrict__ xs;
+  __device__ __forceinline__ void operator()(int r, int c, double v) const { acc[r] += DF(v) * DF(xs[c]); }
+};
+
+__global__ void __launch_bounds__(kMfThreads)
+    k_mf_apply_df(const MfTile* __restrict__ tiles, const int* __restrict__ seg_begin,
+                  const double* __restrict__ cen, const double* __restrict__ rad,
+                  const SphMat* __restrict__ mats, const double* __restrict__ x, double* __restrict__ y) {
+  __shared__ DF sc[kMfChunk * 4];
+  __shared__ DF sx[kMfChunk * kMfNu];
+  const MfTile t = tiles[blockIdx.x];
+  const int hb0 = seg_begin[t.seg], he0 = seg_begin[t.seg + 1];
+  const int per = (he0 - hb0 + gridDim.y - 1) / gridDim.y;
+  const int hb = hb0 + blockIdx.y * per, he = min(he0, hb + per);
+  if (hb >= he) return;
+  const int s = t.s0 + threadIdx.x;
+  const bool act = threadIdx.x < t.ns;
+  const SphMat mc = mats[t.seg];   // moduli divided by mu0 (scaled system)
+  DF p0, p1, p2, as(1.0);
+  if (act) {
+    p0 = DF(cen[3 * (int64_t)s]);
+    p1 = DF(cen[3 * (int64_t)s + 1]);
+    p2 = DF(cen[3 * (int64_t)s + 2]);
+    as = DF(rad[s]);
+  }
+  const DF tn1(mc.tn1), tn2(mc.tn2);
+  DF acc[kMfNu];
+  for (int h0 = hb; h0 < he; h0 += kMfChunk) {
+    const int nh = min(kMfChunk, he - h0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nh; i += blockDim.x) {
+      sc[4 * i] = DF(cen[3 * (int64_t)(h0 + i)]);
+      sc[4 * i + 1] = DF(cen[3 * (int64_t)(h0 + i) + 1]);
+      sc[4 * i + 2] = DF(cen[3 * (int64_t)(h0 + i) + 2]);
+      sc[4 * i + 3] = DF(1.0 / rad[h0 + i]);
+    }
+    for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x) sx[i] = DF(x[(int64_t)kMfNu * h0 + i]);
+    __syncthreads();
+    if (!act) continue;
+#pragma unroll 1
+    for (int hh = 0; hh < nh; ++hh) {
+      const DF ia = sc[4 * hh + 3];
+      const DF x0 = (p0 - sc[4 * hh]) * ia, x1 = (p1 - sc[4 * hh + 1]) * ia, x2 = (p2 - sc[4 * hh + 2]) * ia;
+      sph_pair_apply24<DF, true>(x0, x1, x2, DF(1.0), DF(), DF(), tn1, tn2, sx + kMfNu * hh, as * ia, acc);
+    }
+  }
+  if (!act) return;
+  DF yv[kMfNu];
+  sph_pair_map24<DF>(acc, DF(mc.kmu), DF(mc.klam), yv);
+  if (s >= hb && s < he) {
+    DfSink sk{yv, x + (int64_t)kMfNu * s};
+    sph_self24(mc, sk);
+  }
+  double* o = y + (int64_t)kMfNu * s;
+#pragma unroll
+  for (int r = 0; r < kMfNu; ++r) atomicAdd(o + r, df_value(yv[r]));
 }
 
 // Geometry in the FP32 layout, scalings, segment of every particle.
@@ -593,6 +659,15 @@ ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStrea
   return IBEM_OK;
 }
 
+ibem_status mf_apply_df(const MfBatch& b, const double* x, double* y, cudaStream_t st) {
+  ProfScope ps(PROF_MF_DF, st, 0.0);
+  IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
+  ::ibem::count_launch(), k_mf_apply_df<<<dim3(b.ntiles, b.hsplit), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, b.cen,
+                                                                                        b.rad, b.mats, x, y);
+  IBEM_LAUNCH_CHECK("mf apply df");
+  return IBEM_OK;
+}
+
 ibem_status mf_block_jacobi(const MfBatch& b, float* P, cudaStream_t st) {
   ::ibem::count_launch(), k_block_jacobi<<<b.num, 32, 0, st>>>(b.seg_of, b.matd, P);
   IBEM_LAUNCH_CHECK("block jacobi");
@@ -762,36 +837,64 @@ ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPr
       if (e != cudaSuccess) s = cuda_fail(e, "mf solve: rhs norms");
     }
   }
+  // rs holds the residual of the current iterate; `exact` says whether it came from the
+  // FP64 product (or x = 0).  A double-float residual drives the next correction; once it
+  // shows every realisation within tol, the FP64 residual of the same iterate decides.
+  bool exact = true;
+  auto read_rel = [&]() -> ibem_status {
+    ibem_status r = g.seg_norm2(rs, bn2 + S);
+    if (r) return r;
+    cudaMemcpyAsync(hr.data(), bn2 + S, sizeof(double) * S, cudaMemcpyDeviceToHost, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "mf solve: residual norms");
+    return IBEM_OK;
+  };
+  auto fp64_residual = [&]() -> ibem_status {
+    ibem_status r = mf_apply_f64(b, xs, y, st);   // As xs in FP64
+    if (r) return r;
+    ::ibem::count_launch(), k_sub64<<<nblk(N), 256, 0, st>>>(N, bs, y, rs);   // rs = bs - As xs
+    IBEM_LAUNCH_CHECK("mf residual");
+    exact = true;
+    return read_rel();
+  };
   int outer = 0;
+  hr = hb;
   while (!s) {
-    if (outer > 0) {
-      s = g.seg_norm2(rs, bn2 + S);
-      if (s) break;
-      cudaMemcpyAsync(hr.data(), bn2 + S, sizeof(double) * S, cudaMemcpyDeviceToHost, st);
-      const cudaError_t e = cudaStreamSynchronize(st);
-      if (e != cudaSuccess) { s = cuda_fail(e, "mf solve: residual norms"); break; }
-    } else {
-      hr = hb;
-    }
     bool all = true;
+    for (int i = 0; i < S; ++i) all = all && (hb[i] > 0 ? std::sqrt(hr[i] / hb[i]) : 0.0) <= o.tol;
+    if (!exact && (all || outer >= o.max_outer)) {
+      if ((s = fp64_residual())) break;
+      all = true;
+      for (int i = 0; i < S; ++i) all = all && (hb[i] > 0 ? std::sqrt(hr[i] / hb[i]) : 0.0) <= o.tol;
+    }
     for (int i = 0; i < S; ++i) {
       const double rel = hb[i] > 0 ? std::sqrt(hr[i] / hb[i]) : 0.0;
       rep[i].rel_residual = rel;
       hdone[i] = rel <= o.tol ? 1 : 0;
-      all = all && hdone[i];
     }
     if (all || outer >= o.max_outer) break;
     for (int i = 0; i < S; ++i)
       if (!hdone[i]) outer_of[i] = outer + 1;
     cudaMemcpyAsync(g.done, hdone.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st);
-    // FP32 correction of the scaled system, then the FP64 residual of the new iterate
+    // FP32 correction of the scaled system, then the double-float residual of the new iterate
     ::ibem::count_launch(), k_to_f32<<<nblk(N), 256, 0, st>>>(N, rs, g.rin);
     if ((s = g.gmres(P, o.max_cycles, o.inner_tol))) break;
     ::ibem::count_launch(), k_acc_f32<<<nblk(N), 256, 0, st>>>(N, g.d, xs);
-    if ((s = mf_apply_f64(b, xs, y, st))) break;   // As xs in FP64
-    ::ibem::count_launch(), k_sub64<<<nblk(N), 256, 0, st>>>(N, bs, y, rs);  // rs = bs - As xs
-    IBEM_LAUNCH_CHECK("mf refinement");
     ++outer;
+    // when every active realisation's residual times the GMRES reduction is expected to meet
+    // tol, go straight to the deciding FP64 residual; otherwise a double-float one
+    bool expect = true;
+    for (int i = 0; i < S; ++i)
+      if (!hdone[i]) expect = expect && rep[i].rel_residual * o.inner_tol <= 0.5 * o.tol;
+    if (expect) {
+      if ((s = fp64_residual())) break;
+      continue;
+    }
+    if ((s = mf_apply_df(b, xs, y, st))) break;
+    ::ibem::count_launch(), k_sub64<<<nblk(N), 256, 0, st>>>(N, bs, y, rs);
+    IBEM_LAUNCH_CHECK("mf refinement");
+    exact = false;
+    if ((s = read_rel())) break;
   }
   if (!s) {
     ::ibem::count_launch(), k_mul<<<nblk(N), 256, 0, st>>>(N, b.dc, xs, x);
@@ -821,20 +924,20 @@ using namespace ibem;
 
 extern "C" ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int precision, const double* x_dev,
                                           double* y_dev, void* stream) {
-  if (!batch || !x_dev || !y_dev || (precision != 32 && precision != 64))
+  if (!batch || !x_dev || !y_dev || (precision != 32 && precision != 48 && precision != 64))
     return fail(IBEM_ERR_ARG, "mf_matvec: bad arguments");
   cudaStream_t st = as_stream(stream);
   MfBatch b;
   ibem_status s = mf_batch_init(b, *batch, st);
   if (!s) {
-    if (precision == 64) {
+    if (precision != 32) {
       double *xs = nullptr, *ys = nullptr;
       cudaError_t e = alloc_async((void**)&xs, sizeof(double) * b.N, st);
       if (e == cudaSuccess) e = alloc_async((void**)&ys, sizeof(double) * b.N, st);
       if (e != cudaSuccess) s = cuda_fail(e, "mf_matvec workspace");
       if (!s) {
         ::ibem::count_launch(), k_div64<<<nblk(b.N), 256, 0, st>>>(b.N, x_dev, b.dc, xs);  // xs = x / Dc
-        s = mf_apply_f64(b, xs, ys, st);
+        s = precision == 64 ? mf_apply_f64(b, xs, ys, st) : mf_apply_df(b, xs, ys, st);
         if (!s) ::ibem::count_launch(), k_div64<<<nblk(b.N), 256, 0, st>>>(b.N, ys, b.dr, y_dev);  // y = ys / Dr
       }
       if (!s) {

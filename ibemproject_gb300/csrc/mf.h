@@ -77,6 +77,8 @@ struct MfPrecond {
 };
 // y = As x (FP64, scaled system); y is overwritten
 ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st);
+// y = As x in double-float arithmetic (~48 bits, FP32 pipe); y is overwritten
+ibem_status mf_apply_df(const MfBatch& b, const double* x, double* y, cudaStream_t st);
 // P[p] = inverse of the scaled diagonal block As[p, p] (24 x 24, row-major, FP32)
 ibem_status mf_block_jacobi(const MfBatch& b, float* P, cudaStream_t st);
 

@@ -14,7 +14,7 @@
                distribution, N = 24 NUM) with block-Jacobi, Neumann and learned
                preconditioners (the network trained first on 12 microstructures of 100-150
                spheres): time, Arnoldi and refinement steps, phase times.
---mf NUM       the matrix-free products (ibem_e3d_mf_matvec, FP32 scaled and FP64) on a
+--mf NUM       the matrix-free products (ibem_e3d_mf_matvec: FP32, double-float, FP64) on a
                far-field microstructure of NUM spheres (bench distribution): NUM^2 pair
                products per launch, timed by the library's phase events.
 
@@ -106,16 +106,16 @@ def bench_mf(num, reps, dev):
     x = torch.randn(bt.N, generator=g, dtype=torch.float64).to(dev)
     out = {"kernel": "k_mf_apply", "spheres": num, "pairs": num * num, "reps": reps}
     L = lib()
-    for prec in (32, 64):
+    for prec, key in ((32, "f32"), (48, "df"), (64, "f64")):
         B.matvec(bt, x, prec)   # warm-up
         L.ibem_prof_enable(1)
         for _ in range(reps):
             B.matvec(bt, x, prec)
         prof = prof_report()
         L.ibem_prof_enable(0)
-        ms = prof.get(f"mf_f{prec}", {}).get("ms", 0.0) / reps
-        out[f"f{prec}_ms"] = ms
-        out[f"f{prec}_ns_per_pair"] = ms * 1e6 / (num * num) if ms > 0 else None
+        ms = prof.get(f"mf_{key}", {}).get("ms", 0.0) / reps
+        out[f"{key}_ms"] = ms
+        out[f"{key}_ns_per_pair"] = ms * 1e6 / (num * num) if ms > 0 else None
     return out
 
 

@@ -217,18 +217,20 @@ typedef struct {
 
 /* y = A x for the sphere systems of a batch (the matrix ibem_e3d_pair_blocks would
  * assemble for each realisation, layout 24), without storing A: every 24 x 24 pair block is
- * evaluated inside the product.  precision 64: FP64 in physical units; precision 32: the
- * FP32 product of the scaled system (x and y are converted on the way in and out), about
- * 1e-6 relative.  x_dev, y_dev: 24 * seg_begin[nseg] doubles. */
+ * evaluated inside the product, on the scaled system (x and y are converted on the way in
+ * and out).  precision 64: FP64; 48: double-float (FP32 pairs, ~48 bits, several times
+ * faster on GB300); 32: FP32, about 1e-6 relative.  x_dev, y_dev: 24 * seg_begin[nseg]
+ * doubles. */
 ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int precision, const double* x_dev,
                                double* y_dev, void* stream);
 
 /* Solve A x = b for every realisation of a batch without storing A (a form of
  * systemSolverElastic3D::solve, systemSolverElastic3D.h:44-60, for boundary-free far-field
- * cases): FP64 iterative refinement whose residuals are FP64 matrix-free products, each
- * correction an FP32 restarted GMRES on the scaled system with matrix-free FP32 products,
- * right-preconditioned block-diagonally (`pc`; IBEM_PRECOND_LEARNED needs gnn_params_dev
- * from ibem_gnn_train).  reports: host array of nseg.  Workspace is allocated internally.
+ * cases): iterative refinement in which each correction is an FP32 restarted GMRES on the
+ * scaled system with matrix-free FP32 products, right-preconditioned by `pc`
+ * (IBEM_PRECOND_LEARNED needs gnn_params_dev from ibem_gnn_train); residuals that drive a
+ * correction are double-float matrix-free products and the residual that decides
+ * convergence (and rel_residual) is the FP64 matrix-free product.  reports: host array of nseg.  Workspace is allocated internally.
  * Synchronous.  IBEM_ERR_NOCONV if a realisation misses opt->tol. */
 ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const double* b_dev, double* x_dev,
                               ibem_precond pc, const float* gnn_params_dev,

@@ -2,7 +2,8 @@
 through the C ABI (ibem_e3d_mf_*, ibem_gnn_*).
 
 Checks: the on-the-fly products against the matrix that ibem_e3d_pair_blocks assembles
-(itself pinned to the oracle elsewhere): FP64 to 1e-12, FP32 to 2e-5 in the scaled norm;
+(itself pinned to the oracle elsewhere): FP64 and double-float to 1e-12, FP32 to 2e-5 in the
+scaled norm;
 matrix-free solutions against the plain FP64 LU solve to 1e-8 (relative, eigenstrain
 coefficients); the graph, features and training projections against numpy restatements;
 the network's loss and gradient against the float64 autograd oracle (oracle/gnn_oracle.py)
@@ -46,12 +47,14 @@ def test_mf_matvec_matches_assembled_matrix(B):
     xs = rng.standard_normal(bt.N)
     x = torch.from_numpy(xs * dc).cuda()   # O(1) in the scaled unknowns
     y64 = B.matvec(bt, x, 64).cpu().numpy()
+    y48 = B.matvec(bt, x, 48).cpu().numpy()
     y32 = B.matvec(bt, x, 32).cpu().numpy()
     for s, c in enumerate(cs):
         rows = bt.seg_rows(s)
         A = B.dense_system(c).cpu().numpy().T   # row-major view of the column-major storage
         ref = A @ x.cpu().numpy()[rows]
         assert scaled_err(y64[rows], ref) < 1e-12
+        assert scaled_err(y48[rows], ref) < 1e-12
         assert rel(dr[rows] * y32[rows], dr[rows] * ref) < 2e-5
 
 
