@@ -34,6 +34,7 @@ __global__ void __launch_bounds__(ibem::kFieldThreads)
                const double* __restrict__ cen, const ibem::SphDF* __restrict__ sph, int num, SphMat mc,
                const double* __restrict__ E, double* __restrict__ stress) {
   static_assert(sizeof(ibem::SphDF) == 18 * sizeof(float4), "SphDF is copied as 18 float4");
+  static_assert(ibem::kFieldChunk <= 64, "the near-sphere mask of a chunk is 64 bits");
   __shared__ ibem::SphDF ss[ibem::kFieldChunk];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const bool act = t < nump;
@@ -54,6 +55,10 @@ __global__ void __launch_bounds__(ibem::kFieldThreads)
       for (int i = threadIdx.x; i < nh * 18; i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
+    // pass 1: the spheres far from every point of the warp, in FP32; the others are noted
+    // in a warp-uniform mask and summed in double-float in pass 2, so that each pass runs
+    // one of the two code paths
+    unsigned long long near = 0;
 #pragma unroll 1
     for (int hh = 0; hh < nh; ++hh) {
       const ibem::SphDF& sp = ss[hh];
@@ -67,9 +72,15 @@ __global__ void __launch_bounds__(ibem::kFieldThreads)
 #pragma unroll
           for (int k = 0; k < 6; ++k) ibem::df_add_f(acc[k], r[k]);
         }
-      } else if (act) {
-        if (ibem::sph_field24_df(pd, sp, tn1, tn2, acc)) inside = h0 + hh;
+      } else {
+        near |= 1ull << hh;
       }
+    }
+#pragma unroll 1
+    while (near) {
+      const int hh = __ffsll((long long)near) - 1;
+      near &= near - 1;
+      if (act && ibem::sph_field24_df(pd, ss[hh], tn1, tn2, acc)) inside = h0 + hh;
     }
   }
   if (!act) return;
