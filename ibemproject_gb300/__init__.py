@@ -99,6 +99,7 @@ SIGNATURES = {
     "ibem_e3d_mf_solve": (_int, [ctypes.POINTER(Batch), _vp, _vp, _int, _vp, ctypes.POINTER(MfOptions),
                                  ctypes.POINTER(MfReport), _vp]),
     "ibem_e3d_batch_farfield_rhs": (_int, [ctypes.POINTER(Batch), _c_dp, _vp, _vp]),
+    "ibem_e3d_mf_tuning": (_int, [ctypes.POINTER(Batch), _c_ip, _c_ip, _vp]),
     "ibem_e3d_effective_modulus": (_int, [ctypes.POINTER(Batch), _vp, _c_dp, _c_dp, _c_dp, _c_dp, _vp]),
     "ibem_e3d_run_host_mf": (_int, [ctypes.POINTER(Material), _int, _c_dp, _c_dp, _int, _c_dp, _c_dp, _int,
                                     ctypes.POINTER(ctypes.c_float), ctypes.POINTER(MfOptions), _c_dp, _c_dp,

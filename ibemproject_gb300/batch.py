@@ -116,6 +116,14 @@ def solve(batch: DeviceBatch, b, precond: int = PRECOND_BLOCK_JACOBI, params=Non
     return x, list(reps)
 
 
+def tuning(batch: DeviceBatch):
+    """(source slices of the FP32 product, of the double-float / FP64 products) chosen by the
+    library's autotuner for this batch's shape."""
+    a, b = ctypes.c_int(0), ctypes.c_int(0)
+    check(lib().ibem_e3d_mf_tuning(batch.ref(), ctypes.byref(a), ctypes.byref(b), None))
+    return a.value, b.value
+
+
 def effective_modulus(batch: DeviceBatch, x, sig_inf, volume=None):
     """(E_eff per realisation, mean strain nseg x 6)."""
     volume = np.ascontiguousarray(batch.volumes() if volume is None else volume, dtype=np.float64)
@@ -240,6 +248,6 @@ def train(batch: DeviceBatch, r_hat, e_hat, params, steps: int, lr: float = 2e-3
     return hist
 
 
-__all__ = ["DeviceBatch", "farfield_rhs", "matvec", "solve", "effective_modulus", "dense_system", "dense_solve",
+__all__ = ["DeviceBatch", "farfield_rhs", "matvec", "solve", "tuning", "effective_modulus", "dense_system", "dense_solve",
            "training_pairs", "param_count", "init_params", "prepare", "loss_grad", "edge_weights", "adamw", "train",
            "PRECOND_BLOCK_JACOBI", "PRECOND_LEARNED", "PRECOND_NEUMANN", "IbemError"]

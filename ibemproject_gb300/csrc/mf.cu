@@ -21,6 +21,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <map>
+#include <mutex>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -588,6 +590,7 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
   // slices of the source range: about 4 CTAs per SM in total, at least 32 sources per slice
   const int want = 152 * 4;
   b.hsplit = std::max(1, std::min((want + b.ntiles - 1) / b.ntiles, (b.max_seg + 31) / 32));
+  b.hsplit_wide = b.hsplit;
   std::vector<SphMat> md(in.nseg), ms(in.nseg);
   std::vector<SphMatF> mf(in.nseg);
   for (int s = 0; s < in.nseg; ++s) {
@@ -641,6 +644,106 @@ void mf_batch_free(MfBatch& b) {
   b = MfBatch();
 }
 
+// ------------------------------------------------------------------ autotuner
+// The products' launch shape is (target tiles) x (source slices); the slice count trades
+// parallelism and tail effects against the atomic adds of the partial sums.  For a shape
+// class (log2 buckets of the tile count and of the largest realisation, and the number of
+// SMs) the tuner times each candidate count once with CUDA events (one launch each, inputs
+// of zeros, the same work as any input) and keeps the fastest; the table lives for the
+// process.  The FP32 kernel (128 registers) and the double-float / FP64 kernels (~255
+// registers, half the resident CTAs) are tuned separately (the double-float kernel stands
+// for both wide ones).
+namespace {
+struct TuneKey {
+  int tiles_b, seg_b, sms;
+  bool operator<(const TuneKey& o) const {
+    return tiles_b != o.tiles_b ? tiles_b < o.tiles_b : seg_b != o.seg_b ? seg_b < o.seg_b : sms < o.sms;
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<int, int>> g_tune;
+
+int log2_bucket(int v) {
+  int b = 0;
+  while ((1 << b) < v) ++b;
+  return b;
+}
+}  // namespace
+
+ibem_status mf_tune(MfBatch& b, cudaStream_t st) {
+  int dev = 0, sms = 0;
+  IBEM_CUDA(cudaGetDevice(&dev));
+  IBEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const TuneKey key{log2_bucket(b.ntiles), log2_bucket(b.max_seg), sms};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      const int cap = std::max(1, (b.max_seg + 31) / 32);
+      b.hsplit = std::min(it->second.first, cap);
+      b.hsplit_wide = std::min(it->second.second, cap);
+      return IBEM_OK;
+    }
+  }
+  // candidates: CTA totals of 1, 2, 4 and 8 per SM (and the slice count that gives one
+  // slice per 32 sources at most)
+  const int cap = std::max(1, (b.max_seg + 31) / 32);
+  std::vector<int> cand;
+  for (int per_sm : {1, 2, 4, 8}) {
+    const int h = std::max(1, std::min(cap, (sms * per_sm + b.ntiles - 1) / b.ntiles));
+    if (std::find(cand.begin(), cand.end(), h) == cand.end()) cand.push_back(h);
+  }
+  float* xf = nullptr;
+  float* yf = nullptr;
+  double* xd = nullptr;
+  double* yd = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ibem_status s = IBEM_OK;
+  {
+    cudaError_t e = alloc_async((void**)&xf, sizeof(float) * b.N, st);
+    if (e == cudaSuccess) e = alloc_async((void**)&yf, sizeof(float) * b.N, st);
+    if (e == cudaSuccess) e = alloc_async((void**)&xd, sizeof(double) * b.N, st);
+    if (e == cudaSuccess) e = alloc_async((void**)&yd, sizeof(double) * b.N, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(xf, 0, sizeof(float) * b.N, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(xd, 0, sizeof(double) * b.N, st);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) s = cuda_fail(e, "mf tune");
+  }
+  int best_f = b.hsplit, best_w = b.hsplit_wide;
+  for (int wide = 0; wide < 2 && !s; ++wide) {
+    float best_ms = 1e30f;
+    for (int h : cand) {
+      if (wide) b.hsplit_wide = h; else b.hsplit = h;
+      cudaEventRecord(e0, st);
+      s = wide ? mf_apply_df(b, xd, yd, st) : mf_apply_f32(b, xf, yf, st);
+      cudaEventRecord(e1, st);
+      if (s) break;
+      const cudaError_t e = cudaEventSynchronize(e1);
+      if (e != cudaSuccess) { s = cuda_fail(e, "mf tune"); break; }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best_ms) {
+        best_ms = ms;
+        (wide ? best_w : best_f) = h;
+      }
+    }
+  }
+  b.hsplit = best_f;
+  b.hsplit_wide = best_w;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  free_async(xf, st);
+  free_async(yf, st);
+  free_async(xd, st);
+  free_async(yd, st);
+  if (!s) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = {best_f, best_w};
+  }
+  return s;
+}
+
 ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_t st) {
   ProfScope ps(PROF_MF_F32, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(float) * b.N, st));
@@ -653,7 +756,7 @@ ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_
 ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st) {
   ProfScope ps(PROF_MF_F64, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
-  ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, b.cen,
+  ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, b.cen,
                                                                                          b.rad, b.mats, x, y);
   IBEM_LAUNCH_CHECK("mf apply f64");
   return IBEM_OK;
@@ -662,7 +765,7 @@ ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStrea
 ibem_status mf_apply_df(const MfBatch& b, const double* x, double* y, cudaStream_t st) {
   ProfScope ps(PROF_MF_DF, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
-  ::ibem::count_launch(), k_mf_apply_df<<<dim3(b.ntiles, b.hsplit), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, b.cen,
+  ::ibem::count_launch(), k_mf_apply_df<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, b.cen,
                                                                                         b.rad, b.mats, x, y);
   IBEM_LAUNCH_CHECK("mf apply df");
   return IBEM_OK;
@@ -993,6 +1096,7 @@ extern "C" ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const doub
   IBEM_CUDA(cudaEventRecord(ev[0], st));
   MfBatch b;
   ibem_status s = mf_batch_init(b, *batch, st);
+  if (!s) s = mf_tune(b, st);
   MfPrecond P;
   if (!s) {
     const cudaError_t e = alloc_async((void**)&P.D, sizeof(float) * kMfNu * kMfNu * (size_t)b.num, st);
@@ -1129,5 +1233,22 @@ extern "C" ibem_status ibem_e3d_run_host_mf(const ibem_material* mat, int num, c
   free_async(S, st);
   free_async(prm, st);
   if (st) cudaStreamDestroy(st);
+  return s;
+}
+
+extern "C" ibem_status ibem_e3d_mf_tuning(const ibem_e3d_batch* batch, int* slices_fp32, int* slices_wide,
+                                          void* stream) {
+  if (!batch || !slices_fp32 || !slices_wide) return fail(IBEM_ERR_ARG, "mf_tuning: bad arguments");
+  cudaStream_t st = as_stream(stream);
+  MfBatch b;
+  ibem_status s = mf_batch_init(b, *batch, st);
+  if (!s) s = mf_tune(b, st);
+  if (!s) {
+    *slices_fp32 = b.hsplit;
+    *slices_wide = b.hsplit_wide;
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) s = cuda_fail(e, "mf_tuning");
+  }
+  mf_batch_free(b);
   return s;
 }

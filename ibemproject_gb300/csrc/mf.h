@@ -59,10 +59,15 @@ struct MfBatch {
   double* dr = nullptr;       // N: row scaling
   double* dc = nullptr;       // N: column scaling
   MfTile* tiles = nullptr;
-  int ntiles = 0, hsplit = 1;
+  int ntiles = 0;
+  int hsplit = 1;      // source slices per target tile, FP32 product (autotuned)
+  int hsplit_wide = 1; // the same for the double-float and FP64 products (~255 registers)
 };
 
 ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st);
+// Source-slice counts of the products for this batch's shape, from the autotuner's table
+// (timed on first use of a shape class, then cached for the process).
+ibem_status mf_tune(MfBatch& b, cudaStream_t st);
 void mf_batch_free(MfBatch& b);
 
 // y = As x (FP32, scaled system); y is overwritten

@@ -236,6 +236,14 @@ ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const double* b_dev, 
                               ibem_precond pc, const float* gnn_params_dev,
                               const ibem_mf_options* opt, ibem_mf_report* reports, void* stream);
 
+/* Launch shape the autotuner picks for this batch's products: source slices per target tile
+ * of the FP32 product and of the double-float / FP64 products.  The first call for a shape
+ * class (log2 buckets of the tile count and of the largest realisation) times the
+ * candidates once; the result is cached for the process and used by ibem_e3d_mf_solve.
+ * No reference counterpart.  Synchronous. */
+ibem_status ibem_e3d_mf_tuning(const ibem_e3d_batch* batch, int* slices_fp32, int* slices_wide,
+                               void* stream);
+
 /* Far-field right-hand sides of a batch (ibem_e3d_farfield_rhs per realisation, layout 24). */
 ibem_status ibem_e3d_batch_farfield_rhs(const ibem_e3d_batch* batch, const double* sig_inf,
                                         double* b_dev, void* stream);

@@ -246,3 +246,39 @@ def test_host_buffer_pipeline_matches_dense_path(B):
         assert scaled_err(X, Xd) < 1e-8, pc
         assert scaled_err(S, Sd) < 1e-8, pc
         assert rep.rel_residual <= 1e-10
+
+
+def test_batched_edge_cases_all_preconditioners(B):
+    """Ragged batches: realisations of 1, 5, 16 and 17 spheres (empty and partly filled
+    neighbour slots) beside larger ones, two materials, every preconditioner, against the
+    plain FP64 LU of each realisation."""
+    from ibemproject_gb300 import cases
+    nums = [1, 5, 16, 17, 60, 130]
+    cs = [cases.farfield_case(num=n, r0=0.012, vf=0.12, grid=0, seed=40 + k, E1=70e9 * (3.0 + 2.0 * k))
+          for k, n in enumerate(nums)]
+    bt = B.DeviceBatch(cs)
+    b = B.farfield_rhs(bt, np.array([0.3, 0.1, 0.0, -0.2, 0.05, 1.0]))
+    params = B.init_params(seed=4)
+    refs = [B.dense_solve(c, b[bt.seg_rows(s)]).cpu().numpy() for s, c in enumerate(cs)]
+    for pc, pp in ((B.PRECOND_BLOCK_JACOBI, None), (B.PRECOND_NEUMANN, None), (B.PRECOND_LEARNED, params)):
+        x, reps = B.solve(bt, b, pc, params=pp, tol=1e-11)
+        x = x.cpu().numpy()
+        for s in range(len(cs)):
+            assert scaled_err(x[bt.seg_rows(s)], refs[s]) < 1e-8, (pc, s)
+            assert reps[s].rel_residual <= 1e-11
+
+
+def test_autotuner_picks_valid_cached_shapes(B):
+    """The launch-shape autotuner: slice counts within [1, sources / 32], the same on a
+    second call (cached per shape class), and solves with the tuned shapes stay exact."""
+    cs = small_cases([300, 45], seed=61)
+    bt = B.DeviceBatch(cs)
+    f, w = B.tuning(bt)
+    cap = max(1, (300 + 31) // 32)
+    assert 1 <= f <= cap and 1 <= w <= cap
+    assert B.tuning(bt) == (f, w)
+    b = B.farfield_rhs(bt, np.array([0, 0, 0, 0, 0, 1.0]))
+    x, reps = B.solve(bt, b, B.PRECOND_BLOCK_JACOBI, tol=1e-11)
+    rows = bt.seg_rows(0)
+    xr = B.dense_solve(cs[0], b[rows]).cpu().numpy()
+    assert scaled_err(x.cpu().numpy()[rows], xr) < 1e-8
