@@ -286,7 +286,9 @@ __global__ void __launch_bounds__(kPanelThreads, 1) k_panel(T* __restrict__ P, i
     }
     calu_elim<T, R>(a, live, nb, s_top, s_pr, s_sel, s_key);
     T* lv = cb.lcand + (size_t)g * kLeaf * kLeaf;
-    for (int idx = tid; idx < kLeaf * nb; idx += kPanelThreads) {
+    // the nb winners only: s_sel[j] for j >= nb is not set by this elimination (ragged
+    // last panel, nb < kLeaf)
+    for (int idx = tid; idx < nb * nb; idx += kPanelThreads) {
       const int j = idx / nb, c = idx % nb;
       const int q = s_sel[j];
       if (q >= 0) lv[j * kLeaf + c] = __ldcg(cb.cand + (size_t)(cta * kLeaf + q) * kLeaf + c);
