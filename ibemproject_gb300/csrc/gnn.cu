@@ -13,12 +13,14 @@
 // the higher-order terms and the neighbours left out).
 //
 // Kernels: k_knn (brute force within a realisation, one warp per particle), k_features, k_edge_corr (one CTA of
-// 64 threads per edge: four threads evaluate the two FP32 pair blocks into shared memory,
+// 64 threads per edge: eight threads evaluate the two FP32 pair blocks into shared memory,
 // all 64 form the four 24 x 24 products), the network's dense layers as one tiled FP32 GEMM
 // kernel (k_gemm, 64 x 64 tiles, optional transposes, bias, ReLU, atomic split-K for the
 // weight gradients) with gather / scatter / mean kernels around it, the loss and its
 // gradient with respect to the edge weights (k_loss), and AdamW (k_adamw).  Training runs
-// these in a host loop (ibem_gnn_train) on one batch of realisations.
+// these in a host loop (ibem_gnn_train) on one batch of realisations.  Inference (the edge
+// weights of a solve) uses a split form of the first edge layers: per-node products and
+// one fused kernel per layer (forward_fast).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -28,6 +30,7 @@
 #include <vector>
 
 #include "mf.h"
+#include "prof.h"
 
 namespace ibem {
 namespace {
@@ -169,15 +172,27 @@ struct SmemSink {
   __device__ __forceinline__ void operator()(int r, int c, float v) const { M[r * kMfNu + c] = v * scale; }
 };
 
-// C = sc * A B for 24 x 24 row-major matrices in shared memory
+// C = sc * A B for 24 x 24 row-major matrices in shared memory; 64 threads, each a 3 x 3
+// register tile (rows 3 (t / 8) .., columns 3 (t % 8) ..): 6 shared loads per 9 FMAs
 __device__ __forceinline__ void mm24(const float* A, const float* B, float* C, float sc) {
-  for (int e = threadIdx.x; e < kMfNu * kMfNu; e += blockDim.x) {
-    const int r = e / kMfNu, c = e % kMfNu;
-    float s = 0.f;
+  const int tr = 3 * (threadIdx.x >> 3), tc = 3 * (threadIdx.x & 7);
+  float acc[3][3] = {};
+#pragma unroll 4
+  for (int k = 0; k < kMfNu; ++k) {
+    float a[3], b[3];
 #pragma unroll
-    for (int k = 0; k < kMfNu; ++k) s = fmaf(A[r * kMfNu + k], B[k * kMfNu + c], s);
-    C[e] = sc * s;
+    for (int i = 0; i < 3; ++i) a[i] = A[(tr + i) * kMfNu + k];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) b[j] = B[k * kMfNu + tc + j];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
   }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) C[(tr + i) * kMfNu + tc + j] = sc * acc[i][j];
 }
 
 __global__ void __launch_bounds__(64)
@@ -203,24 +218,21 @@ __global__ void __launch_bounds__(64)
     Bi[k] = bi[k];
     Bj[k] = bj[k];
   }
-  if (threadIdx.x < 4) {
+  if (threadIdx.x < 8) {  // 8 generators: 4 sub-blocks (column order x row order) of each block
     const SphMatF mc = mats[seg_of[i]];
-    const bool ij = threadIdx.x < 2;  // As_ij: target i, source j; As_ji: target j, source i
+    const bool ij = threadIdx.x < 4;  // As_ij: target i, source j; As_ji: target j, source i
+    const int fn = threadIdx.x & 3;
     const int tgt = ij ? i : j, src = ij ? j : i;
     const double ia = 1.0 / rad[src];
     const float x0 = (float)((cen[3 * (int64_t)tgt] - cen[3 * (int64_t)src]) * ia);
     const float x1 = (float)((cen[3 * (int64_t)tgt + 1] - cen[3 * (int64_t)src + 1]) * ia);
     const float x2 = (float)((cen[3 * (int64_t)tgt + 2] - cen[3 * (int64_t)src + 2]) * ia);
     float* M = ij ? Aij : Aji;
-    if ((threadIdx.x & 1) == 0) {
-      SmemSink sk{M, 1.f};
-      sph_block24f_c0_r0(x0, x1, x2, 1.f, mc, sk);
-      sph_block24f_c1_r0(x0, x1, x2, 1.f, mc, sk);
-    } else {
-      SmemSink sk{M, (float)(rad[tgt] * ia)};
-      sph_block24f_c0_r1(x0, x1, x2, 1.f, mc, sk);
-      sph_block24f_c1_r1(x0, x1, x2, 1.f, mc, sk);
-    }
+    SmemSink sk{M, fn >= 2 ? (float)(rad[tgt] * ia) : 1.f};   // rows of order 1 carry a_tgt / a_src
+    if (fn == 0) sph_block24f_c0_r0(x0, x1, x2, 1.f, mc, sk);
+    else if (fn == 1) sph_block24f_c1_r0(x0, x1, x2, 1.f, mc, sk);
+    else if (fn == 2) sph_block24f_c0_r1(x0, x1, x2, 1.f, mc, sk);
+    else sph_block24f_c1_r1(x0, x1, x2, 1.f, mc, sk);
   }
   __syncthreads();
   mm24(Aji, Bi, T1, 1.f);    // As_ji B_i
@@ -532,6 +544,71 @@ __global__ void k_adamw(int64_t n, float* __restrict__ p, const float* __restric
   p[i] = p[i] - lr * wd * p[i] - lr * mh / (sqrtf(vh) + eps);
 }
 
+// ---------------------------------------------------------------- inference pass
+// The first layer of every edge MLP splits: [h_i, h_j, f_e] W = (H W_top)_i + (H W_mid)_j
+// + f_e W_bot, so the two 64 x 64 products run once per node (P, Q) and the edge work is a
+// 7-term dot product per channel, fused with the ReLU and the mean (messages) or with the
+// output layer (edge weights).  Same arithmetic as the training pass up to rounding.
+
+// Uin[i] = [H[i], mean over valid edges of relu(P[i] + Q[j] + f_e W_bot + b)]
+__global__ void k_msg_mean(int num, const int* __restrict__ nbr, const float* __restrict__ H,
+                           const float* __restrict__ P, const float* __restrict__ Q, const float* __restrict__ ef,
+                           const float* __restrict__ Wb, const float* __restrict__ bias, float* __restrict__ Uin) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)num * kH) return;
+  const int i = (int)(t / kH), c = (int)(t % kH);
+  float w[kGnnEdgeF];
+#pragma unroll
+  for (int k = 0; k < kGnnEdgeF; ++k) w[k] = Wb[k * kH + c];
+  const float pc = P[t] + bias[c];
+  float s = 0.f;
+  int deg = 0;
+  for (int k = 0; k < kKnn; ++k) {
+    const int64_t e = (int64_t)i * kKnn + k;
+    const int j = nbr[e];
+    if (j < 0) continue;
+    float m = pc + Q[(int64_t)j * kH + c];
+#pragma unroll
+    for (int q = 0; q < kGnnEdgeF; ++q) m = fmaf(ef[e * kGnnEdgeF + q], w[q], m);
+    s += fmaxf(m, 0.f);
+    ++deg;
+  }
+  Uin[(int64_t)i * kUin + c] = H[t];
+  Uin[(int64_t)i * kUin + kH + c] = deg ? s / deg : 0.f;
+}
+
+// w_e = relu(P[i] + Q[j] + f_e W_bot + b1) W_o2 + b_o2 (0 for a missing neighbour); one warp
+// per edge, lanes over channel pairs
+__global__ void k_edge_out(int64_t E, const int* __restrict__ nbr, const float* __restrict__ P,
+                           const float* __restrict__ Q, const float* __restrict__ ef, const float* __restrict__ Wb,
+                           const float* __restrict__ b1, const float* __restrict__ w2, const float* __restrict__ b2,
+                           float* __restrict__ out) {
+  const int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (e >= E) return;
+  const int j = nbr[e];
+  if (j < 0) {
+    if (lane < kGnnOut) out[e * kGnnOut + lane] = 0.f;
+    return;
+  }
+  const int64_t i = e / kKnn;
+  float acc[kGnnOut] = {};
+#pragma unroll
+  for (int h = 0; h < kH / 32; ++h) {
+    const int c = lane + 32 * h;
+    float m = P[i * kH + c] + Q[(int64_t)j * kH + c] + b1[c];
+#pragma unroll
+    for (int q = 0; q < kGnnEdgeF; ++q) m = fmaf(ef[e * kGnnEdgeF + q], Wb[q * kH + c], m);
+    m = fmaxf(m, 0.f);
+#pragma unroll
+    for (int k = 0; k < kGnnOut; ++k) acc[k] = fmaf(m, w2[c * kGnnOut + k], acc[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < kGnnOut; ++k)
+    for (int o = 16; o; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+  if (lane < kGnnOut) out[e * kGnnOut + lane] = (lane == 0 ? acc[0] : acc[1]) + b2[lane];
+}
+
 // ---------------------------------------------------------------- network driver
 struct Net {
   int num;
@@ -636,6 +713,54 @@ struct Net {
   }
 };
 
+// Inference pass of the network (edge weights only), with the split first layers above.
+ibem_status forward_fast(int num, const int* nbr, const float* xn, const float* ef, const float* Pm, float* w,
+                         cudaStream_t st) {
+  static_assert(kGnnOut == 2, "k_edge_out writes two outputs per edge");
+  const Layout L;
+  const int64_t E = (int64_t)num * kKnn;
+  float *H = nullptr, *H2 = nullptr, *P = nullptr, *Q = nullptr, *Uin = nullptr, *Upd = nullptr;
+  const size_t nh = sizeof(float) * (size_t)num * kH;
+  cudaError_t e = alloc_async((void**)&H, nh, st);
+  if (e == cudaSuccess) e = alloc_async((void**)&H2, nh, st);
+  if (e == cudaSuccess) e = alloc_async((void**)&P, nh, st);
+  if (e == cudaSuccess) e = alloc_async((void**)&Q, nh, st);
+  if (e == cudaSuccess) e = alloc_async((void**)&Upd, nh, st);
+  if (e == cudaSuccess) e = alloc_async((void**)&Uin, 2 * nh, st);
+  ibem_status s = e == cudaSuccess ? IBEM_OK : cuda_fail(e, "gnn forward");
+  Net g;  // launch helpers only (no buffers)
+  g.num = num;
+  g.E = E;
+  g.st = st;
+  if (!s) {
+    g.gemm(num, kH, kGnnNodeF, xn, kGnnNodeF, Pm + L.w_in, kH, H, kH, Pm + L.b_in, 1);
+    for (int l = 0; l < kGnnLayers; ++l) {
+      const float* W = Pm + L.w_m[l];
+      g.gemm(num, kH, kH, H, kH, W, kH, P, kH, nullptr, 0);                 // rows 0..63: h_i
+      g.gemm(num, kH, kH, H, kH, W + kH * kH, kH, Q, kH, nullptr, 0);       // rows 64..127: h_j
+      ::ibem::count_launch(), k_msg_mean<<<nb((int64_t)num * kH), 256, 0, st>>>(num, nbr, H, P, Q, ef, W + 2 * kH * kH,
+                                                                                Pm + L.b_m[l], Uin);
+      g.gemm(num, kH, kUin, Uin, kUin, Pm + L.w_u[l], kH, Upd, kH, Pm + L.b_u[l], 1);
+      ::ibem::count_launch(), k_add<<<nb((int64_t)num * kH), 256, 0, st>>>((int64_t)num * kH, H, Upd, H2);
+      std::swap(H, H2);
+    }
+    const float* W = Pm + L.w_o1;
+    g.gemm(num, kH, kH, H, kH, W, kH, P, kH, nullptr, 0);
+    g.gemm(num, kH, kH, H, kH, W + kH * kH, kH, Q, kH, nullptr, 0);
+    ::ibem::count_launch(), k_edge_out<<<nb(E * 32, 256), 256, 0, st>>>(E, nbr, P, Q, ef, W + 2 * kH * kH, Pm + L.b_o1,
+                                                                          Pm + L.w_o2, Pm + L.b_o2, w);
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) s = cuda_fail(le, "gnn forward");
+  }
+  free_async(H, st);
+  free_async(H2, st);
+  free_async(P, st);
+  free_async(Q, st);
+  free_async(Upd, st);
+  free_async(Uin, st);
+  return s;
+}
+
 ibem_status loss_grad(Net& net, const int* nbr, const float* xn, const float* ef, int nrhs, const float* z,
                       const float* u, const float* P, double* loss_dev, float* G) {
   ibem_status s = net.forward(nbr, xn, ef, P);
@@ -668,6 +793,7 @@ struct Prepared {
 int64_t gnn_param_count() { return Layout().total; }
 
 ibem_status gnn_knn(const MfBatch& b, int* nbr, cudaStream_t st) {
+  ProfScope ps(PROF_KNN, st);
   ::ibem::count_launch(), k_knn<<<nb((int64_t)b.num * 32, 128), 128, 0, st>>>(b.num, b.seg_of, b.seg_begin, b.cen, nbr);
   IBEM_LAUNCH_CHECK("knn");
   return IBEM_OK;
@@ -693,6 +819,7 @@ ibem_status gnn_features(const MfBatch& b, const int* nbr, float* xn, float* ef,
 ibem_status gnn_edge_corrections(const MfBatch& b, const int* nbr, const float* B, const float* wa, float* D, float* Q,
                                  int nrhs, const float* r, float* u, cudaStream_t st) {
   const int64_t E = (int64_t)b.num * kKnn;
+  ProfScope ps(PROF_EDGE, st);
   ::ibem::count_launch(), k_edge_corr<<<(unsigned)E, 64, 0, st>>>(b.num, nbr, b.seg_of, b.matf, b.cen, b.rad, B, wa, D,
                                                                   Q, nrhs, r, b.N, u);
   IBEM_LAUNCH_CHECK("edge corrections");
@@ -701,14 +828,8 @@ ibem_status gnn_edge_corrections(const MfBatch& b, const int* nbr, const float* 
 
 ibem_status gnn_forward_weights(int num, const int* nbr, const float* xn, const float* ef, const float* params, float* w,
                                 cudaStream_t st) {  // w: num * kKnn x kGnnOut
-  Net net;
-  net.num = num;
-  net.E = (int64_t)num * kKnn;
-  net.st = st;
-  ibem_status s = net.alloc(false);
-  if (!s) s = net.forward(nbr, xn, ef, params);
-  if (!s) IBEM_CUDA(cudaMemcpyAsync(w, net.w, sizeof(float) * net.E * kGnnOut, cudaMemcpyDeviceToDevice, st));
-  return s;   // stream-ordered: the network's buffers are freed after the copy
+  ProfScope ps(PROF_GNN_FWD, st);
+  return forward_fast(num, nbr, xn, ef, params, w, st);
 }
 
 __global__ void k_fill1(int64_t n, float* __restrict__ p) {

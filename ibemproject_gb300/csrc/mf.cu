@@ -51,11 +51,13 @@ struct MvSink {
 
 __global__ void __launch_bounds__(kMfThreads)
     k_mf_apply_f32(const MfTile* __restrict__ tiles, const int* __restrict__ seg_begin,
+                   const int* __restrict__ mask, int mask_on,
                    const float4* __restrict__ gh, const float4* __restrict__ gl,
                    const SphMatF* __restrict__ mats, const float* __restrict__ x, float* __restrict__ y) {
   __shared__ float4 sgh[kMfChunk], sgl[kMfChunk];
   __shared__ float sx[kMfChunk * kMfNu];
   const MfTile t = tiles[blockIdx.x];
+  if (mask && mask[t.seg] != mask_on) return;  // realisation left out of this product
   const int hb0 = seg_begin[t.seg], he0 = seg_begin[t.seg + 1];
   const int per = (he0 - hb0 + gridDim.y - 1) / gridDim.y;
   const int hb = hb0 + blockIdx.y * per, he = min(he0, hb + per);
@@ -105,11 +107,13 @@ __global__ void __launch_bounds__(kMfThreads)
 // FP32 kernel in double precision, offsets from FP64 centres.
 __global__ void __launch_bounds__(kMfThreads)
     k_mf_apply_f64(const MfTile* __restrict__ tiles, const int* __restrict__ seg_begin,
+                   const int* __restrict__ mask, int mask_on,
                    const double* __restrict__ cen, const double* __restrict__ rad,
                    const SphMat* __restrict__ mats, const double* __restrict__ x, double* __restrict__ y) {
   __shared__ double sc[kMfChunk * 4];
   __shared__ double sx[kMfChunk * kMfNu];
   const MfTile t = tiles[blockIdx.x];
+  if (mask && mask[t.seg] != mask_on) return;  // realisation left out of this product
   const int hb0 = seg_begin[t.seg], he0 = seg_begin[t.seg + 1];
   const int per = (he0 - hb0 + gridDim.y - 1) / gridDim.y;
   const int hb = hb0 + blockIdx.y * per, he = min(he0, hb + per);
@@ -169,11 +173,13 @@ struct DfSink {
 
 __global__ void __launch_bounds__(kMfThreads)
     k_mf_apply_df(const MfTile* __restrict__ tiles, const int* __restrict__ seg_begin,
+                   const int* __restrict__ mask, int mask_on,
                   const double* __restrict__ cen, const double* __restrict__ rad,
                   const SphMat* __restrict__ mats, const double* __restrict__ x, double* __restrict__ y) {
   __shared__ DF sc[kMfChunk * 4];
   __shared__ DF sx[kMfChunk * kMfNu];
   const MfTile t = tiles[blockIdx.x];
+  if (mask && mask[t.seg] != mask_on) return;  // realisation left out of this product
   const int hb0 = seg_begin[t.seg], he0 = seg_begin[t.seg + 1];
   const int per = (he0 - hb0 + gridDim.y - 1) / gridDim.y;
   const int hb = hb0 + blockIdx.y * per, he = min(he0, hb + per);
@@ -522,6 +528,12 @@ __global__ void k_sub64(int64_t n, const double* __restrict__ a, const double* _
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) out[i] = a[i] - b[i];
 }
+// out = a - b (FP64) on the rows of realisations with done == 0
+__global__ void k_sub64_masked(int64_t n, const int* __restrict__ seg_of, const int* __restrict__ done,
+                               const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n && !done[seg_of[i / kMfNu]]) out[i] = a[i] - b[i];
+}
 // y = x / d (FP64)
 __global__ void k_div64(int64_t n, const double* __restrict__ x, const double* __restrict__ d, double* __restrict__ y) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -744,29 +756,29 @@ ibem_status mf_tune(MfBatch& b, cudaStream_t st) {
   return s;
 }
 
-ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_t st) {
+ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_t st, const int* mask, int mask_on) {
   ProfScope ps(PROF_MF_F32, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(float) * b.N, st));
-  ::ibem::count_launch(), k_mf_apply_f32<<<dim3(b.ntiles, b.hsplit), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, b.gh,
-                                                                                         b.gl, b.matf, x, y);
+  ::ibem::count_launch(), k_mf_apply_f32<<<dim3(b.ntiles, b.hsplit), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, mask, mask_on,
+                                                                                         b.gh, b.gl, b.matf, x, y);
   IBEM_LAUNCH_CHECK("mf apply f32");
   return IBEM_OK;
 }
 
-ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st) {
+ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st, const int* mask, int mask_on) {
   ProfScope ps(PROF_MF_F64, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
-  ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, b.cen,
-                                                                                         b.rad, b.mats, x, y);
+  ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, mask, mask_on,
+                                                                                              b.cen, b.rad, b.mats, x, y);
   IBEM_LAUNCH_CHECK("mf apply f64");
   return IBEM_OK;
 }
 
-ibem_status mf_apply_df(const MfBatch& b, const double* x, double* y, cudaStream_t st) {
+ibem_status mf_apply_df(const MfBatch& b, const double* x, double* y, cudaStream_t st, const int* mask, int mask_on) {
   ProfScope ps(PROF_MF_DF, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
-  ::ibem::count_launch(), k_mf_apply_df<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, b.cen,
-                                                                                        b.rad, b.mats, x, y);
+  ::ibem::count_launch(), k_mf_apply_df<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, mask, mask_on,
+                                                                                             b.cen, b.rad, b.mats, x, y);
   IBEM_LAUNCH_CHECK("mf apply df");
   return IBEM_OK;
 }
@@ -864,7 +876,7 @@ struct MfSolver {
     for (int cyc = 0; cyc < max_cycles && !s; ++cyc) {
       const float* r = rin;
       if (cyc > 0) {  // residual of the restarted cycle, rin - As d
-        if ((s = mf_apply_f32(b, d, w, st))) break;
+        if ((s = mf_apply_f32(b, d, w, st, done, 0))) break;
         ::ibem::count_launch(), k_sub_f32<<<nblk(N), 256, 0, st>>>(N, rin, w, r32);
         r = r32;
       }
@@ -880,7 +892,7 @@ struct MfSolver {
         float* vk = V + (int64_t)k * N;
         float* wv = V + (int64_t)(k + 1) * N;
         ::ibem::count_launch(), k_precond_apply<<<nblk(N), 256, 0, st>>>(b.num, P.D, P.Q, P.nbr, vk, z);
-        if ((s = mf_apply_f32(b, z, wv, st))) break;
+        if ((s = mf_apply_f32(b, z, wv, st, K.active, 1))) break;   // converged realisations sit out
         {
           ProfScope pg(PROF_GMRES_OTHER, st);
           IBEM_CUDA(cudaMemsetAsync(K.d1, 0, sizeof(double) * 2 * (size_t)S * (m + 1), st));
@@ -993,8 +1005,8 @@ ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPr
       if ((s = fp64_residual())) break;
       continue;
     }
-    if ((s = mf_apply_df(b, xs, y, st))) break;
-    ::ibem::count_launch(), k_sub64<<<nblk(N), 256, 0, st>>>(N, bs, y, rs);
+    if ((s = mf_apply_df(b, xs, y, st, g.done, 0))) break;   // done realisations keep their residual
+    ::ibem::count_launch(), k_sub64_masked<<<nblk(N), 256, 0, st>>>(N, b.seg_of, g.done, bs, y, rs);
     IBEM_LAUNCH_CHECK("mf refinement");
     exact = false;
     if ((s = read_rel())) break;

@@ -70,8 +70,10 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
 ibem_status mf_tune(MfBatch& b, cudaStream_t st);
 void mf_batch_free(MfBatch& b);
 
-// y = As x (FP32, scaled system); y is overwritten
-ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_t st);
+// y = As x (FP32, scaled system); y is overwritten.  With a mask, realisation s takes part
+// only when mask[s] == mask_on (its rows of y stay zero otherwise); the same for the others.
+ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_t st, const int* mask = nullptr,
+                         int mask_on = 1);
 
 // Block-sparse preconditioner on the k-nearest-neighbour graph:
 //   (P v)_i = D_i v_i + sum_slot Q_(i,slot) v_nbr(i,slot)
@@ -81,9 +83,11 @@ struct MfPrecond {
   int* nbr = nullptr;    // num*kKnn neighbour indices (-1: empty slot)
 };
 // y = As x (FP64, scaled system); y is overwritten
-ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st);
+ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st, const int* mask = nullptr,
+                         int mask_on = 1);
 // y = As x in double-float arithmetic (~48 bits, FP32 pipe); y is overwritten
-ibem_status mf_apply_df(const MfBatch& b, const double* x, double* y, cudaStream_t st);
+ibem_status mf_apply_df(const MfBatch& b, const double* x, double* y, cudaStream_t st, const int* mask = nullptr,
+                        int mask_on = 1);
 // P[p] = inverse of the scaled diagonal block As[p, p] (24 x 24, row-major, FP32)
 ibem_status mf_block_jacobi(const MfBatch& b, float* P, cudaStream_t st);
 

@@ -14,7 +14,8 @@ namespace ibem {
 namespace {
 const char* kNames[PROF_NCAT] = {"pair_blocks", "field", "bem", "equilibrate", "panel", "laswp", "trsm_small",
                                  "gemm_tc", "gemm_split", "gemm_simt", "trsv", "matvec", "gmres_other",
-                                 "mf_f32", "mf_f64", "precond_setup", "mf_df"};
+                                 "mf_f32", "mf_f64", "precond_setup", "mf_df",
+                                 "gnn_forward", "edge_blocks", "knn"};
 std::atomic<bool> g_on{false};
 std::mutex g_mu;
 struct Rec {

@@ -9,7 +9,7 @@ namespace ibem {
 enum ProfCat {
   PROF_PAIR = 0, PROF_FIELD, PROF_BEM, PROF_EQUIL, PROF_PANEL, PROF_LASWP, PROF_TRSM_SMALL,
   PROF_GEMM_TC, PROF_GEMM_SPLIT, PROF_GEMM_SIMT, PROF_TRSV, PROF_MATVEC, PROF_GMRES_OTHER, PROF_MF_F32,
-  PROF_MF_F64, PROF_PRECOND, PROF_MF_DF, PROF_NCAT
+  PROF_MF_F64, PROF_PRECOND, PROF_MF_DF, PROF_GNN_FWD, PROF_EDGE, PROF_KNN, PROF_NCAT
 };
 
 bool prof_on();

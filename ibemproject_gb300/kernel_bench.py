@@ -14,6 +14,8 @@
                distribution, N = 24 NUM) with block-Jacobi, Neumann and learned
                preconditioners (the network trained first on 12 microstructures of 100-150
                spheres): time, Arnoldi and refinement steps, phase times.
+--batch R      the batched measurement of bench.py (R realisations of U[50, 500] spheres,
+               learned preconditioner, untrained network) with per-phase times.
 --mf NUM       the matrix-free products (ibem_e3d_mf_matvec: FP32, double-float, FP64) on a
                far-field microstructure of NUM spheres (bench distribution): NUM^2 pair
                products per launch, timed by the library's phase events.
@@ -185,6 +187,36 @@ def bench_solve(num, reps, dev):
     return out
 
 
+def bench_batch(nreal, reps, dev):
+    import numpy as np
+    from . import batch as B
+    from . import cases
+    rng = np.random.default_rng(4242)
+    nums = rng.integers(50, 501, size=nreal)
+    vfs = rng.uniform(0.10, 0.20, size=nreal)
+    con = rng.uniform(2.0, 20.0, size=nreal)
+    cs = [cases.farfield_case(num=int(n), r0=0.008, vf=float(v), grid=0, seed=7000 + k, E1=70e9 * float(c))
+          for k, (n, v, c) in enumerate(zip(nums, vfs, con))]
+    bt = B.DeviceBatch(cs, device=dev)
+    params = B.init_params(seed=1, device=dev)
+    b = B.farfield_rhs(bt, np.array([0, 0, 0, 0, 0, 1.0]))
+    B.solve(bt, b, B.PRECOND_LEARNED, params=params)   # warm-up (and tuning)
+    L = lib()
+    L.ibem_prof_enable(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        x, rep = B.solve(bt, b, B.PRECOND_LEARNED, params=params)
+    e1.record()
+    torch.cuda.synchronize()
+    prof = prof_report()
+    L.ibem_prof_enable(0)
+    return {"kernel": "batched matrix-free solve", "realisations": nreal, "spheres": int(nums.sum()),
+            "ms": e0.elapsed_time(e1) / reps, "arnoldi_steps_max": max(r.inner for r in rep),
+            "phases_ms": {k: round(v["ms"] / reps, 3) for k, v in prof.items()},
+            "phase_launches": {k: v["launches"] / reps for k, v in prof.items()}}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gemm", action="append", default=[], help="M,N,K")
@@ -193,6 +225,7 @@ def main(argv=None):
     ap.add_argument("--mf", type=int, action="append", default=[])
     ap.add_argument("--field", action="append", default=[], help="NUM,GRID")
     ap.add_argument("--solve", type=int, action="append", default=[])
+    ap.add_argument("--batch", type=int, action="append", default=[])
     ap.add_argument("--reps", type=int, default=3)
     a = ap.parse_args(argv)
     dev = torch.device("cuda", 0)
@@ -206,6 +239,8 @@ def main(argv=None):
         print(json.dumps(bench_mf(n, a.reps, dev)), flush=True)
     for n in a.solve:
         print(json.dumps(bench_solve(n, a.reps, dev)), flush=True)
+    for n in a.batch:
+        print(json.dumps(bench_batch(n, a.reps, dev)), flush=True)
     for f in a.field:
         num, grid = (int(v) for v in f.split(","))
         print(json.dumps(bench_field(num, grid, a.reps, dev)), flush=True)
