@@ -418,6 +418,7 @@ struct Krylov {
   double* n2;     // nseg
   double* yv;     // nseg x m
   double* thr;    // nseg: |g| target of the current GMRES solve (inner_tol * first beta)
+  double* est;    // nseg: latest Arnoldi estimate of the GMRES residual norm
   int* nsteps;    // nseg: Arnoldi steps taken while active (reported)
   int* nactive;   // 1
 };
@@ -452,6 +453,7 @@ __global__ void k_arnoldi_update(int nseg, int m, int k, Krylov K) {
   g[k] = cs[k] * g[k];
   K.kc[s] = k + 1;
   K.nsteps[s] += 1;
+  K.est[s] = fabs(g[k + 1]);
   K.inv[s] = hn > 0 ? 1.0 / hn : 0.0;
   if (fabs(g[k + 1]) <= K.thr[s] || hn == 0.0 || k + 1 == m) {
     K.active[s] = 0;
@@ -478,13 +480,15 @@ __global__ void k_hess_solve(int nseg, int m, Krylov K) {
 }
 
 // start of a GMRES cycle: beta = sqrt(n2), g = (beta, 0, ...); on the first cycle of a
-// solve thr = inner_tol * beta; active while beta > thr and the realisation is not done
-__global__ void k_cycle_start(int nseg, int m, Krylov K, const int* __restrict__ done, int first, double inner_tol) {
+// solve thr = inner_tol[s] * beta; active while beta > thr and the realisation is not done
+__global__ void k_cycle_start(int nseg, int m, Krylov K, const int* __restrict__ done, int first,
+                              const double* __restrict__ inner_tol) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nseg) return;
   const double b = sqrt(fmax(K.n2[s], 0.0));
   K.beta[s] = b;
-  if (first) K.thr[s] = inner_tol * b;
+  if (first) K.thr[s] = inner_tol[s] * b;
+  K.est[s] = b;
   double* g = K.g + (int64_t)s * (m + 1);
   for (int i = 0; i <= m; ++i) g[i] = 0.0;
   g[0] = b;
@@ -805,6 +809,7 @@ struct MfSolver {
   float* rin = nullptr;  // N   right-hand side of the current GMRES solve
   float* r32 = nullptr;  // N   residual of a restarted cycle
   int* done = nullptr;   // nseg
+  double* tolv = nullptr;  // nseg: residual reduction asked of this GMRES solve
   Krylov K{};
   void* kmem = nullptr;
   int splits = 1;
@@ -819,6 +824,7 @@ struct MfSolver {
     free_async(rin, st);
     free_async(r32, st);
     free_async(done, st);
+    free_async(tolv, st);
     free_async(kmem, st);
   }
   ibem_status alloc() {
@@ -829,8 +835,9 @@ struct MfSolver {
     IBEM_CUDA(alloc_async((void**)&rin, sizeof(float) * N, st));
     IBEM_CUDA(alloc_async((void**)&r32, sizeof(float) * N, st));
     IBEM_CUDA(alloc_async((void**)&done, sizeof(int) * b.nseg, st));
+    IBEM_CUDA(alloc_async((void**)&tolv, sizeof(double) * b.nseg, st));
     const size_t S = b.nseg;
-    const size_t nd = S * ((size_t)(m + 1) * m + (m + 1) + 2 * (size_t)m + 4 + 2 * (size_t)(m + 1) + m);
+    const size_t nd = S * ((size_t)(m + 1) * m + (m + 1) + 2 * (size_t)m + 5 + 2 * (size_t)(m + 1) + m);
     IBEM_CUDA(alloc_async((void**)&kmem, nd * sizeof(double) + sizeof(int) * (3 * S + 1), st));
     double* p = (double*)kmem;
     K.H = p; p += S * (m + 1) * m;
@@ -841,6 +848,7 @@ struct MfSolver {
     K.inv = p; p += S;
     K.n2 = p; p += S;
     K.thr = p; p += S;
+    K.est = p; p += S;
     K.d1 = p; p += S * (m + 1);
     K.d2 = p; p += S * (m + 1);
     K.yv = p; p += S * m;
@@ -869,7 +877,7 @@ struct MfSolver {
   // FP32 GMRES(m) with restarts on As d = rin, right-preconditioned by P; d overwritten.
   // Realisations flagged in `done` take no step.  Stops each realisation once
   // ||rin - As d|| <= inner_tol ||rin|| (Arnoldi estimate).
-  ibem_status gmres(const MfPrecond& P, int max_cycles, double inner_tol) {
+  ibem_status gmres(const MfPrecond& P, int max_cycles) {
     const int S = b.nseg;
     ibem_status s = IBEM_OK;
     IBEM_CUDA(cudaMemsetAsync(d, 0, sizeof(float) * N, st));
@@ -882,7 +890,7 @@ struct MfSolver {
       }
       if ((s = seg_norm2(r, K.n2))) break;
       IBEM_CUDA(cudaMemsetAsync(K.nactive, 0, sizeof(int), st));
-      ::ibem::count_launch(), k_cycle_start<<<nblk(S, 128), 128, 0, st>>>(S, m, K, done, cyc == 0, inner_tol);
+      ::ibem::count_launch(), k_cycle_start<<<nblk(S, 128), 128, 0, st>>>(S, m, K, done, cyc == 0, tolv);
       ::ibem::count_launch(), k_seg_scale<float, float><<<nblk(N), 256, 0, st>>>(N, b.seg_of, K.inv, r, V, 0);
       IBEM_LAUNCH_CHECK("gmres cycle start");
       const int na = read_nactive(s);
@@ -939,7 +947,7 @@ ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPr
     if (e == cudaSuccess) e = alloc_async((void**)&bn2, sizeof(double) * 2 * S, st);
     if (e != cudaSuccess) s = cuda_fail(e, "mf solve workspace");
   }
-  std::vector<double> hb(S), hr(S);
+  std::vector<double> hb(S), hr(S), htol(S);
   std::vector<int> hdone(S, 0), outer_of(S, 0);
   if (!s) {
     cudaMemsetAsync(xs, 0, sizeof(double) * N, st);
@@ -991,16 +999,34 @@ ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPr
     for (int i = 0; i < S; ++i)
       if (!hdone[i]) outer_of[i] = outer + 1;
     cudaMemcpyAsync(g.done, hdone.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st);
+    // reduction asked of each realisation's GMRES: inner_tol, or deeper when that is what
+    // brings the next residual within tol (never below the ~1e-6 the FP32 products allow)
+    for (int i = 0; i < S; ++i)
+      htol[i] = std::max(1e-6, std::min(o.inner_tol, rep[i].rel_residual > 0 ? 0.1 * o.tol / rep[i].rel_residual : o.inner_tol));
+    cudaMemcpyAsync(g.tolv, htol.data(), sizeof(double) * S, cudaMemcpyHostToDevice, st);
     // FP32 correction of the scaled system, then the double-float residual of the new iterate
     ::ibem::count_launch(), k_to_f32<<<nblk(N), 256, 0, st>>>(N, rs, g.rin);
-    if ((s = g.gmres(P, o.max_cycles, o.inner_tol))) break;
+    if ((s = g.gmres(P, o.max_cycles))) break;
     ::ibem::count_launch(), k_acc_f32<<<nblk(N), 256, 0, st>>>(N, g.d, xs);
     ++outer;
-    // when every active realisation's residual times the GMRES reduction is expected to meet
-    // tol, go straight to the deciding FP64 residual; otherwise a double-float one
+    // expected residual of every realisation still running: its previous residual times the
+    // reduction its GMRES reached (Arnoldi estimate over the first beta), but no better than
+    // the FP32 products allow (~1e-6 of the correction).  When all are expected to meet tol,
+    // go straight to the deciding FP64 residual; otherwise a double-float one.
+    std::vector<double> est(S), thr(S);
+    cudaMemcpyAsync(est.data(), g.K.est, sizeof(double) * S, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(thr.data(), g.K.thr, sizeof(double) * S, cudaMemcpyDeviceToHost, st);
+    {
+      const cudaError_t e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) { s = cuda_fail(e, "mf solve: GMRES estimates"); break; }
+    }
     bool expect = true;
-    for (int i = 0; i < S; ++i)
-      if (!hdone[i]) expect = expect && rep[i].rel_residual * o.inner_tol <= 0.5 * o.tol;
+    for (int i = 0; i < S; ++i) {
+      if (hdone[i]) continue;
+      const double beta0 = thr[i] > 0 ? thr[i] / htol[i] : 0.0;
+      const double red = beta0 > 0 ? std::max(est[i] / beta0, 1e-6) : 1.0;
+      expect = expect && rep[i].rel_residual * red <= 0.5 * o.tol;
+    }
     if (expect) {
       if ((s = fp64_residual())) break;
       continue;
