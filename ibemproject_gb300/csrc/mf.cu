@@ -249,12 +249,13 @@ __global__ void k_mf_prep(int num, const double* __restrict__ cen, const double*
   }
 }
 
-// Scaled diagonal block As[p,p] (FP64, x = 0, unit sphere, moduli / mu0) inverted by
-// Gauss-Jordan with partial pivoting; one CTA of 32 threads per particle.
-__global__ void __launch_bounds__(32) k_block_jacobi(const int* __restrict__ seg_of, const SphMat* __restrict__ mats,
-                                                     float* __restrict__ P) {
+// Scaled diagonal block (FP64, x = 0, unit sphere, moduli / mu0) inverted by Gauss-Jordan
+// with partial pivoting; one CTA of 32 threads per realisation: in the scaled system a
+// sphere's own block depends on the materials only, so every sphere of a realisation shares
+// it (k_bcast_blocks copies it to each).
+__global__ void __launch_bounds__(32) k_block_jacobi(const SphMat* __restrict__ mats, float* __restrict__ P) {
   __shared__ double M[kMfNu][2 * kMfNu + 1];
-  const int p = blockIdx.x;
+  const int p = blockIdx.x;   // realisation
   const int t = threadIdx.x;
   for (int i = t; i < kMfNu * 2 * kMfNu; i += 32) {
     const int r = i / (2 * kMfNu), c = i % (2 * kMfNu);
@@ -262,7 +263,7 @@ __global__ void __launch_bounds__(32) k_block_jacobi(const int* __restrict__ seg
   }
   __syncthreads();
   if (t == 0) {
-    SphMat mc = mats[seg_of[p]];
+    SphMat mc = mats[p];
     const double s = 1.0 / mc.mu0;
     mc.kmu *= s;
     mc.klam *= s;
@@ -311,6 +312,17 @@ __global__ void __launch_bounds__(32) k_block_jacobi(const int* __restrict__ seg
   }
   float* o = P + (int64_t)kMfNu * kMfNu * p;
   for (int i = t; i < kMfNu * kMfNu; i += 32) o[i] = (float)M[i / kMfNu][kMfNu + i % kMfNu];
+}
+
+// P[p] = Pseg[seg_of[p]] (24 x 24 blocks, float4 copies)
+__global__ void k_bcast_blocks(int num, const int* __restrict__ seg_of, const float* __restrict__ Pseg,
+                               float* __restrict__ P) {
+  constexpr int kQ = kMfNu * kMfNu / 4;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)num * kQ) return;
+  const int64_t p = t / kQ;
+  const int q = (int)(t % kQ);
+  reinterpret_cast<float4*>(P)[t] = reinterpret_cast<const float4*>(Pseg)[(int64_t)seg_of[p] * kQ + q];
 }
 
 // z = P v for the block-sparse preconditioner: z_p = D_p v_p + sum_slot Q_(p,slot) v_nbr;
@@ -788,7 +800,11 @@ ibem_status mf_apply_df(const MfBatch& b, const double* x, double* y, cudaStream
 }
 
 ibem_status mf_block_jacobi(const MfBatch& b, float* P, cudaStream_t st) {
-  ::ibem::count_launch(), k_block_jacobi<<<b.num, 32, 0, st>>>(b.seg_of, b.matd, P);
+  float* Pseg = nullptr;
+  IBEM_CUDA(alloc_async((void**)&Pseg, sizeof(float) * kMfNu * kMfNu * (size_t)b.nseg, st));
+  ::ibem::count_launch(), k_block_jacobi<<<b.nseg, 32, 0, st>>>(b.matd, Pseg);
+  ::ibem::count_launch(), k_bcast_blocks<<<nblk((int64_t)b.num * kMfNu * kMfNu / 4), 256, 0, st>>>(b.num, b.seg_of, Pseg, P);
+  free_async(Pseg, st);
   IBEM_LAUNCH_CHECK("block jacobi");
   return IBEM_OK;
 }
