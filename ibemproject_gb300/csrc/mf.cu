@@ -23,6 +23,7 @@
 #include <chrono>
 #include <map>
 #include <mutex>
+#include <thread>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -1235,6 +1236,28 @@ extern "C" ibem_status ibem_e3d_effective_modulus(const ibem_e3d_batch* batch, c
   return s;
 }
 
+namespace ibem {
+namespace {
+// Pinned host staging of ibem_e3d_run_host_mf (grown on demand, kept for the process; the
+// calls that use it are serialised by its mutex).
+std::mutex g_stage_mu;
+void* g_stage = nullptr;
+size_t g_stage_bytes = 0;
+cudaError_t stage_reserve(size_t bytes) {
+  if (bytes <= g_stage_bytes) return cudaSuccess;
+  if (g_stage) cudaFreeHost(g_stage);
+  g_stage = nullptr;
+  g_stage_bytes = 0;
+  const cudaError_t e = cudaMallocHost(&g_stage, bytes);
+  if (e == cudaSuccess) g_stage_bytes = bytes;
+  return e;
+}
+}  // namespace
+}  // namespace ibem
+
+// Host buffers in, host buffers out.  The points (needed only by the stress sums) are copied
+// into pinned staging by a helper thread and sent on a second stream while the solve runs;
+// the stresses come back through the same staging.
 extern "C" ibem_status ibem_e3d_run_host_mf(const ibem_material* mat, int num, const double* centers,
                                             const double* radius, int nump, const double* points,
                                             const double* sig_inf, ibem_precond pc, const float* gnn_params,
@@ -1244,14 +1267,20 @@ extern "C" ibem_status ibem_e3d_run_host_mf(const ibem_material* mat, int num, c
       (nump > 0 && !stress) || !report)
     return fail(IBEM_ERR_ARG, "run_host_mf: bad arguments");
   if (pc == IBEM_PRECOND_LEARNED && !gnn_params) return fail(IBEM_ERR_ARG, "run_host_mf: learned form needs parameters");
+  std::lock_guard<std::mutex> lk(g_stage_mu);
   const int64_t N = (int64_t)kMfNu * num;
   const int64_t np = gnn_param_count();
+  const size_t pts_bytes = sizeof(double) * 3 * (size_t)nump, str_bytes = sizeof(double) * 6 * (size_t)nump;
   double *cen = nullptr, *rad = nullptr, *pts = nullptr, *b = nullptr, *x = nullptr, *S = nullptr;
   float* prm = nullptr;
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr, st2 = nullptr;
+  cudaEvent_t ev = nullptr;
   ibem_status s = IBEM_OK;
   {
     cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = stage_reserve(std::max(pts_bytes, str_bytes));
     if (e == cudaSuccess) e = alloc_async((void**)&cen, sizeof(double) * 3 * num, st);
     if (e == cudaSuccess) e = alloc_async((void**)&rad, sizeof(double) * num, st);
     if (e == cudaSuccess) e = alloc_async((void**)&pts, sizeof(double) * 3 * std::max(nump, 1), st);
@@ -1261,23 +1290,44 @@ extern "C" ibem_status ibem_e3d_run_host_mf(const ibem_material* mat, int num, c
     if (e == cudaSuccess && gnn_params) e = alloc_async((void**)&prm, sizeof(float) * np, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(cen, centers, sizeof(double) * 3 * num, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(rad, radius, sizeof(double) * num, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && nump > 0) e = cudaMemcpyAsync(pts, points, sizeof(double) * 3 * nump, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && gnn_params) e = cudaMemcpyAsync(prm, gnn_params, sizeof(float) * np, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);   // pts must exist before st2 copies into it
     if (e != cudaSuccess) s = cuda_fail(e, "run_host_mf: set-up");
+  }
+  // points: host -> pinned staging (helper thread) -> device on st2, behind the solve
+  cudaError_t pts_err = cudaSuccess;
+  std::thread loader;
+  int dev = 0;
+  if (!s && nump > 0) {
+    cudaGetDevice(&dev);
+    loader = std::thread([&]() {
+      cudaSetDevice(dev);   // the caller's device, not the new thread's default
+      std::memcpy(g_stage, points, pts_bytes);
+      pts_err = cudaMemcpyAsync(pts, g_stage, pts_bytes, cudaMemcpyHostToDevice, st2);
+      if (pts_err == cudaSuccess) pts_err = cudaEventRecord(ev, st2);
+    });
   }
   const int seg[2] = {0, num};
   const ibem_e3d_batch bt{1, seg, cen, rad, mat};
   if (!s) s = ibem_e3d_farfield_rhs(num, mat, kMfNu, sig_inf, b, st);
   if (!s) s = ibem_e3d_mf_solve(&bt, b, x, pc, prm, opt, report, st);
+  if (loader.joinable()) loader.join();
+  if (!s && pts_err != cudaSuccess) s = cuda_fail(pts_err, "run_host_mf: points");
+  if (!s && nump > 0) {
+    const cudaError_t e = cudaStreamWaitEvent(st, ev, 0);
+    if (e != cudaSuccess) s = cuda_fail(e, "run_host_mf: points");
+  }
   if (!s && nump > 0)
     s = ibem_e3d_field_form(IBEM_SOLVE_MIXED_IR, pts, nump, cen, rad, num, mat, kMfNu, x, nullptr, 0, nullptr, 0,
                             nullptr, nullptr, sig_inf, S, st);
   if (!s) {
     cudaError_t e = cudaMemcpyAsync(X, x, sizeof(double) * N, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess && nump > 0) e = cudaMemcpyAsync(stress, S, sizeof(double) * 6 * nump, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && nump > 0) e = cudaMemcpyAsync(g_stage, S, str_bytes, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess && nump > 0) std::memcpy(stress, g_stage, str_bytes);
     if (e != cudaSuccess) s = cuda_fail(e, "run_host_mf: results");
   }
+  if (st2) cudaStreamSynchronize(st2);
   if (st) cudaStreamSynchronize(st);
   free_async(cen, st);
   free_async(rad, st);
@@ -1286,6 +1336,8 @@ extern "C" ibem_status ibem_e3d_run_host_mf(const ibem_material* mat, int num, c
   free_async(x, st);
   free_async(S, st);
   free_async(prm, st);
+  if (ev) cudaEventDestroy(ev);
+  if (st2) cudaStreamDestroy(st2);
   if (st) cudaStreamDestroy(st);
   return s;
 }
