@@ -58,6 +58,13 @@ class MfReport(ctypes.Structure):
 
 
 PRECOND_BLOCK_JACOBI, PRECOND_LEARNED, PRECOND_NEUMANN = 0, 1, 2
+GEN_RSA, GEN_MC = 0, 1
+
+
+class GenParams(ctypes.Structure):
+    _fields_ = [("num", ctypes.c_int), ("r0", ctypes.c_double), ("rlo", ctypes.c_double), ("rhi", ctypes.c_double),
+                ("vf", ctypes.c_double), ("gap", ctypes.c_double), ("method", ctypes.c_int),
+                ("seed", ctypes.c_uint64), ("max_tries", ctypes.c_int64), ("sweeps", ctypes.c_int)]
 
 
 class IbemError(RuntimeError):
@@ -101,9 +108,15 @@ SIGNATURES = {
     "ibem_e3d_batch_farfield_rhs": (_int, [ctypes.POINTER(Batch), _c_dp, _vp, _vp]),
     "ibem_e3d_mf_tuning": (_int, [ctypes.POINTER(Batch), _c_ip, _c_ip, _vp]),
     "ibem_e3d_effective_modulus": (_int, [ctypes.POINTER(Batch), _vp, _c_dp, _c_dp, _c_dp, _c_dp, _vp]),
+    "ibem_e3d_batch_farfield_rhs_layout": (_int, [ctypes.POINTER(Batch), _int, _c_dp, _vp, _vp]),
+    "ibem_e3d_batch_dense_solve": (_int, [ctypes.POINTER(Batch), _int, _int, _vp, _vp, _dbl,
+                                          ctypes.POINTER(SolveReport), _vp]),
+    "ibem_e3d_effective_modulus_layout": (_int, [ctypes.POINTER(Batch), _int, _vp, _c_dp, _c_dp, _c_dp, _c_dp,
+                                                 _vp]),
     "ibem_e3d_run_host_mf": (_int, [ctypes.POINTER(Material), _int, _c_dp, _c_dp, _int, _c_dp, _c_dp, _int,
                                     ctypes.POINTER(ctypes.c_float), ctypes.POINTER(MfOptions), _c_dp, _c_dp,
                                     ctypes.POINTER(MfReport)]),
+    "ibem_e3d_generate_spheres": (_int, [ctypes.POINTER(GenParams), _c_dp, _c_dp, _c_dp]),
     "ibem_gnn_param_count": (_i64, []),
     "ibem_gnn_init_params": (_int, [_vp, ctypes.c_uint64, _vp]),
     "ibem_gnn_prepare": (_int, [ctypes.POINTER(Batch), _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

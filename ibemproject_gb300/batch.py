@@ -18,7 +18,7 @@ import ctypes
 import numpy as np
 
 from . import (Batch, IbemError, Material, MfOptions, MfReport, PRECOND_BLOCK_JACOBI, PRECOND_LEARNED,
-               PRECOND_NEUMANN, SOLVE_FP64, SolveReport, check, lib)
+               PRECOND_NEUMANN, SOLVE_FP64, SOLVE_MIXED_IR, SolveReport, check, lib)
 
 NU = 24
 KNN = 16
@@ -29,17 +29,26 @@ def _ptr(t) -> int:
     return t.data_ptr()
 
 
-class DeviceBatch:
-    """Realisations (each a cases.Case of the far-field kind) resident on `device`."""
+def _linear(batch) -> None:
+    if batch.layout != NU:
+        raise ValueError(f"the matrix-free solver and the learned preconditioner take layout {NU}, "
+                         f"not {batch.layout}")
 
-    def __init__(self, cases_list, device="cuda"):
+
+class DeviceBatch:
+    """Realisations (each a cases.Case of the far-field kind) resident on `device`, with
+    `layout` unknowns per particle (24: the matrix-free solver's; 60 or 78: quadratic
+    eigenstrain, solved by dense_batch_solve)."""
+
+    def __init__(self, cases_list, device="cuda", layout: int = NU):
         import torch
         self.cases = list(cases_list)
+        self.layout = int(layout)
         counts = [c.num for c in self.cases]
         self.seg_begin = np.zeros(len(counts) + 1, dtype=np.int32)
         self.seg_begin[1:] = np.cumsum(counts)
         self.num = int(self.seg_begin[-1])
-        self.N = NU * self.num
+        self.N = self.layout * self.num
         cen = np.concatenate([np.asarray(c.centers, dtype=np.float64).reshape(-1, 3) for c in self.cases])
         rad = np.concatenate([np.asarray(c.radius, dtype=np.float64) for c in self.cases])
         self.centers_host, self.radius_host = cen, rad
@@ -58,7 +67,7 @@ class DeviceBatch:
         return ctypes.byref(self.rec)
 
     def seg_rows(self, s: int) -> slice:
-        return slice(NU * int(self.seg_begin[s]), NU * int(self.seg_begin[s + 1]))
+        return slice(self.layout * int(self.seg_begin[s]), self.layout * int(self.seg_begin[s + 1]))
 
     def scalings(self):
         """(Dr, Dc) as host arrays of length N."""
@@ -90,12 +99,25 @@ def farfield_rhs(batch: DeviceBatch, sig_inf):
     import torch
     b = torch.zeros(batch.N, dtype=torch.float64, device=batch.device)
     sig = np.ascontiguousarray(sig_inf, dtype=np.float64)
-    check(lib().ibem_e3d_batch_farfield_rhs(batch.ref(), sig.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
-                                            _ptr(b), None))
+    check(lib().ibem_e3d_batch_farfield_rhs_layout(batch.ref(), batch.layout,
+                                                   sig.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), _ptr(b),
+                                                   None))
     return b
 
 
+def dense_batch_solve(batch: DeviceBatch, b, form: int = SOLVE_MIXED_IR, tol: float = 1e-10, x=None):
+    """Dense solves of every realisation (ibem_e3d_batch_dense_solve, the batch's layout):
+    returns (x, list of SolveReport)."""
+    import torch
+    if x is None:
+        x = torch.zeros_like(b)
+    reps = (SolveReport * batch.nseg)()
+    check(lib().ibem_e3d_batch_dense_solve(batch.ref(), batch.layout, form, _ptr(b), _ptr(x), tol, reps, None))
+    return x, list(reps)
+
+
 def matvec(batch: DeviceBatch, x, precision: int = 64):
+    _linear(batch)
     import torch
     y = torch.empty_like(x)
     check(lib().ibem_e3d_mf_matvec(batch.ref(), precision, _ptr(x), _ptr(y), None))
@@ -106,6 +128,7 @@ def matvec(batch: DeviceBatch, x, precision: int = 64):
 def solve(batch: DeviceBatch, b, precond: int = PRECOND_BLOCK_JACOBI, params=None, tol: float = 1e-10,
           inner_tol: float = 1e-5, restart: int = 50, max_outer: int = 8, max_cycles: int = 20, x=None):
     """Matrix-free solve of every realisation: returns (x, list of MfReport)."""
+    _linear(batch)
     import torch
     if x is None:
         x = torch.zeros_like(b)
@@ -119,6 +142,7 @@ def solve(batch: DeviceBatch, b, precond: int = PRECOND_BLOCK_JACOBI, params=Non
 def tuning(batch: DeviceBatch):
     """(source slices of the FP32 product, of the double-float / FP64 products) chosen by the
     library's autotuner for this batch's shape."""
+    _linear(batch)
     a, b = ctypes.c_int(0), ctypes.c_int(0)
     check(lib().ibem_e3d_mf_tuning(batch.ref(), ctypes.byref(a), ctypes.byref(b), None))
     return a.value, b.value
@@ -131,28 +155,29 @@ def effective_modulus(batch: DeviceBatch, x, sig_inf, volume=None):
     eps = np.zeros((batch.nseg, 6))
     e = np.zeros(batch.nseg)
     dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-    check(lib().ibem_e3d_effective_modulus(batch.ref(), _ptr(x), dp(volume), dp(sig), dp(eps), dp(e), None))
+    check(lib().ibem_e3d_effective_modulus_layout(batch.ref(), batch.layout, _ptr(x), dp(volume), dp(sig), dp(eps),
+                                                  dp(e), None))
     return e, eps
 
 
-def dense_system(case, device="cuda"):
-    """The layout-24 matrix of one realisation, assembled by ibem_e3d_pair_blocks (FP64,
-    column-major N x N, as a torch tensor whose transpose view is row-major)."""
+def dense_system(case, device="cuda", layout: int = NU):
+    """The matrix of one realisation, assembled by ibem_e3d_pair_blocks (FP64, column-major
+    N x N, as a torch tensor whose transpose view is row-major)."""
     import torch
-    n = NU * case.num
+    n = layout * case.num
     A = torch.zeros((n, n), dtype=torch.float64, device=device)  # column-major: A[c, r]
     cen = torch.from_numpy(np.ascontiguousarray(case.centers, dtype=np.float64)).to(device)
     rad = torch.from_numpy(np.ascontiguousarray(case.radius, dtype=np.float64)).to(device)
     m = Material(case.E0, case.nu0, case.E1, case.nu1)
-    check(lib().ibem_e3d_pair_blocks(_ptr(cen), _ptr(rad), case.num, ctypes.byref(m), NU, _ptr(A), n, 0, 0, None))
+    check(lib().ibem_e3d_pair_blocks(_ptr(cen), _ptr(rad), case.num, ctypes.byref(m), layout, _ptr(A), n, 0, 0, None))
     torch.cuda.synchronize()
     return A  # storage is column-major: element (r, c) is A[c, r]
 
 
-def dense_solve(case, b_seg, device="cuda"):
+def dense_solve(case, b_seg, device="cuda", layout: int = NU):
     """Plain FP64 LU solve (ibem_e3d_solve, IBEM_SOLVE_FP64) of one realisation."""
     import torch
-    A = dense_system(case, device)
+    A = dense_system(case, device, layout)
     n = A.shape[0]
     x = torch.zeros(n, dtype=torch.float64, device=device)
     rep = SolveReport()
@@ -165,6 +190,7 @@ def training_pairs(batch: DeviceBatch, nrhs: int, seed: int = 0):
     """Residual / correction pairs of the scaled system made by the plain FP64 solver:
     r_hat ~ N(0, 1) per entry, e_hat = As^-1 r_hat (solving A e = Dr^-1 r_hat with the
     FP64 LU, e_hat = Dc^-1 e).  Returns two (nrhs, N) FP64 device tensors."""
+    _linear(batch)
     import torch
     rng = np.random.default_rng(seed)
     dr, dc = batch.scalings()
@@ -193,6 +219,7 @@ def init_params(seed: int = 0, device="cuda"):
 
 def prepare(batch: DeviceBatch, r_hat=None, e_hat=None):
     """Graph, features and (with pairs) the training projections z, u; dict of tensors."""
+    _linear(batch)
     import torch
     dev = batch.device
     E = batch.num * KNN
@@ -242,12 +269,14 @@ def adamw(params, grad, m, v, step, lr, beta1=0.9, beta2=0.999, eps=1e-8, weight
 
 def train(batch: DeviceBatch, r_hat, e_hat, params, steps: int, lr: float = 2e-3, weight_decay: float = 0.0):
     """Full-batch training on the GPU (ibem_gnn_train); returns the loss history."""
+    _linear(batch)
     hist = np.zeros(steps + 1)
     check(lib().ibem_gnn_train(batch.ref(), int(r_hat.shape[0]), _ptr(r_hat), _ptr(e_hat), _ptr(params), steps, lr,
                                weight_decay, hist.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), None))
     return hist
 
 
-__all__ = ["DeviceBatch", "farfield_rhs", "matvec", "solve", "tuning", "effective_modulus", "dense_system", "dense_solve",
+__all__ = ["DeviceBatch", "farfield_rhs", "dense_batch_solve", "matvec", "solve", "tuning", "effective_modulus",
+           "dense_system", "dense_solve",
            "training_pairs", "param_count", "init_params", "prepare", "loss_grad", "edge_weights", "adamw", "train",
            "PRECOND_BLOCK_JACOBI", "PRECOND_LEARNED", "PRECOND_NEUMANN", "IbemError"]

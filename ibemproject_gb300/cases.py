@@ -263,3 +263,26 @@ def farfield_case(num: int = 2000, r0: float = 0.012, vf: float = 0.15, grid: in
     sig = np.array([0, 0, 0, 0, 0, sigma33], dtype=np.float64)
     return Case(E0, nu0, E1, nu1, np.zeros((0, 3)), np.zeros((0, 4), np.int32), np.zeros((0, 2)),
                 np.zeros((0, 24)), C, R, pts, sig, "farfield")
+
+
+def generated_case(num: int, r0: float, vf: float, seed: int, method: str = "mc", rlo: float = 0.8,
+                   rhi: float = 1.2, gap: float = 0.1, grid: int = 0, E0: float = 70e9, nu0: float = 0.3,
+                   E1: float = 400e9, nu1: float = 0.2, sigma33: float = 1.0) -> Case:
+    """Boundary-free far-field case whose spheres come from the library's native generator
+    (ibem_e3d_generate_spheres: "rsa" = random sequential addition inside the cube, "mc" =
+    hard-sphere Monte Carlo with compression, which reaches 30% volume fraction).  The
+    cube side L is returned in ``title`` as ``generated L=<side>``; stresses on grid^3."""
+    import ctypes
+
+    from . import GEN_MC, GEN_RSA, GenParams, check, lib
+    p = GenParams(int(num), r0, rlo, rhi, vf, gap, GEN_MC if method == "mc" else GEN_RSA, int(seed), 0, 0)
+    C = np.zeros((num, 3))
+    R = np.zeros(num)
+    side = ctypes.c_double(0.0)
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    check(lib().ibem_e3d_generate_spheres(ctypes.byref(p), dp(C), dp(R), ctypes.byref(side)))
+    L = side.value
+    pts = cell_grid(grid, 0.0, L) if grid else np.zeros((0, 3))
+    sig = np.array([0, 0, 0, 0, 0, sigma33], dtype=np.float64)
+    return Case(E0, nu0, E1, nu1, np.zeros((0, 3)), np.zeros((0, 4), np.int32), np.zeros((0, 2)),
+                np.zeros((0, 24)), C, R, pts, sig, f"generated L={L!r}")

@@ -576,13 +576,24 @@ __global__ void k_sub_f32(int64_t n, const float* __restrict__ a, const float* _
   if (i < n) out[i] = a[i] - b[i];
 }
 // mean order-0 eigenstrain weighted by volume: out[seg*6 + r] += V_p E_p[r]
-__global__ void k_vol_eigen(int num, const int* __restrict__ seg_of, const double* __restrict__ rad,
+// Volume integral of each particle's eigenstrain polynomial, summed per realisation.  Over a
+// sphere of radius a the linear terms average to zero and x_k x_l averages to a^2/5 delta_kl,
+// so the order-2 coefficients E_ijkk (diagonal (k, k) slots: 0, 3, 5 of the six p <= q of
+// layout 60; 0, 4, 8 of the nine (p, q) of layout 78) add a^2/5 each.
+__global__ void k_vol_eigen(int num, int nu, const int* __restrict__ seg_of, const double* __restrict__ rad,
                             const double* __restrict__ x, double* __restrict__ out) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= num) return;
   const double a = rad[p];
   const double vp = 4.0 / 3.0 * 3.141592653589793 * a * a * a;
-  for (int r = 0; r < 6; ++r) atomicAdd(out + 6 * seg_of[p] + r, vp * x[(int64_t)kMfNu * p + r]);
+  const double q = a * a / 5.0;
+  const double* e = x + (int64_t)nu * p;
+  for (int r = 0; r < 6; ++r) {
+    double v = e[r];
+    if (nu == 60) v += q * (e[24 + 6 * r] + e[24 + 6 * r + 3] + e[24 + 6 * r + 5]);
+    if (nu == 78) v += q * (e[24 + 9 * r] + e[24 + 9 * r + 4] + e[24 + 9 * r + 8]);
+    atomicAdd(out + 6 * seg_of[p] + r, vp * v);
+  }
 }
 
 inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
@@ -1184,22 +1195,71 @@ extern "C" ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const doub
   return s;
 }
 
-extern "C" ibem_status ibem_e3d_batch_farfield_rhs(const ibem_e3d_batch* batch, const double* sig_inf, double* b_dev,
-                                                   void* stream) {
-  if (!batch || !batch->seg_begin || !batch->mats || !sig_inf || !b_dev)
+extern "C" ibem_status ibem_e3d_batch_farfield_rhs_layout(const ibem_e3d_batch* batch, int layout,
+                                                          const double* sig_inf, double* b_dev, void* stream) {
+  const int nu = ibem_layout_size(layout);
+  if (!batch || !batch->seg_begin || !batch->mats || !sig_inf || !b_dev || nu < 0)
     return fail(IBEM_ERR_ARG, "batch_farfield_rhs: bad arguments");
   for (int s = 0; s < batch->nseg; ++s) {
     const int p0 = batch->seg_begin[s], n = batch->seg_begin[s + 1] - p0;
-    const ibem_status r = ibem_e3d_farfield_rhs(n, &batch->mats[s], 24, sig_inf, b_dev + (int64_t)kMfNu * p0, stream);
+    const ibem_status r = ibem_e3d_farfield_rhs(n, &batch->mats[s], layout, sig_inf, b_dev + (int64_t)nu * p0, stream);
     if (r) return r;
   }
   return IBEM_OK;
 }
 
+extern "C" ibem_status ibem_e3d_batch_farfield_rhs(const ibem_e3d_batch* batch, const double* sig_inf, double* b_dev,
+                                                   void* stream) {
+  return ibem_e3d_batch_farfield_rhs_layout(batch, 24, sig_inf, b_dev, stream);
+}
+
+extern "C" ibem_status ibem_e3d_batch_dense_solve(const ibem_e3d_batch* batch, int layout, ibem_solver_form form,
+                                                  const double* b_dev, double* x_dev, double tol,
+                                                  ibem_solve_report* reports, void* stream) {
+  const int nu = ibem_layout_size(layout);
+  if (!batch || !batch->seg_begin || !batch->mats || !batch->centers_dev || !batch->radius_dev || !b_dev || !x_dev ||
+      nu < 0 || batch->nseg < 0 || batch->seg_begin[0] != 0)
+    return fail(IBEM_ERR_ARG, "batch_dense_solve: bad arguments");
+  int64_t nmax = 0;
+  for (int s = 0; s < batch->nseg; ++s) {
+    const int n = batch->seg_begin[s + 1] - batch->seg_begin[s];
+    if (n < 0) return fail(IBEM_ERR_ARG, "batch_dense_solve: seg_begin must not decrease");
+    nmax = std::max<int64_t>(nmax, (int64_t)nu * n);
+  }
+  cudaStream_t st = as_stream(stream);
+  double* A = nullptr;  // the largest realisation's N x N matrix, reused by every realisation
+  ibem_status s = IBEM_OK;
+  if (nmax) {
+    const cudaError_t e = alloc_async((void**)&A, sizeof(double) * nmax * nmax, st);
+    if (e != cudaSuccess) s = cuda_fail(e, "batch_dense_solve: matrix");
+  }
+  for (int i = 0; i < batch->nseg && !s; ++i) {
+    const int p0 = batch->seg_begin[i], n = batch->seg_begin[i + 1] - p0;
+    const int64_t N = (int64_t)nu * n, off = (int64_t)nu * p0;
+    ibem_solve_report rep{};
+    if (n) {
+      s = ibem_e3d_pair_blocks(batch->centers_dev + 3 * (int64_t)p0, batch->radius_dev + p0, n, &batch->mats[i], layout,
+                               A, N, 0, 0, st);
+      if (!s) s = ibem_e3d_solve(form, N, A, N, b_dev + off, x_dev + off, tol, &rep, st);
+    }
+    if (reports) reports[i] = rep;
+  }
+  free_async(A, st);
+  return s;
+}
+
 extern "C" ibem_status ibem_e3d_effective_modulus(const ibem_e3d_batch* batch, const double* x_dev,
                                                   const double* volume, const double* sig_inf, double* mean_strain,
                                                   double* e_eff, void* stream) {
-  if (!batch || !x_dev || !volume || !sig_inf || !e_eff) return fail(IBEM_ERR_ARG, "effective_modulus: bad arguments");
+  return ibem_e3d_effective_modulus_layout(batch, 24, x_dev, volume, sig_inf, mean_strain, e_eff, stream);
+}
+
+extern "C" ibem_status ibem_e3d_effective_modulus_layout(const ibem_e3d_batch* batch, int layout, const double* x_dev,
+                                                         const double* volume, const double* sig_inf,
+                                                         double* mean_strain, double* e_eff, void* stream) {
+  const int nu = ibem_layout_size(layout);
+  if (!batch || !x_dev || !volume || !sig_inf || !e_eff || nu < 0)
+    return fail(IBEM_ERR_ARG, "effective_modulus: bad arguments");
   cudaStream_t st = as_stream(stream);
   MfBatch b;
   ibem_status s = mf_batch_init(b, *batch, st);
@@ -1212,7 +1272,7 @@ extern "C" ibem_status ibem_e3d_effective_modulus(const ibem_e3d_batch* batch, c
     if (e != cudaSuccess) s = cuda_fail(e, "effective_modulus");
   }
   if (!s) {
-    ::ibem::count_launch(), k_vol_eigen<<<nblk(b.num), 256, 0, st>>>(b.num, b.seg_of, b.rad, x_dev, acc);
+    ::ibem::count_launch(), k_vol_eigen<<<nblk(b.num), 256, 0, st>>>(b.num, nu, b.seg_of, b.rad, x_dev, acc);
     cudaMemcpyAsync(h.data(), acc, sizeof(double) * 6 * S, cudaMemcpyDeviceToHost, st);
     const cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) s = cuda_fail(e, "effective_modulus");

@@ -1,0 +1,241 @@
+// Seeded sphere microstructures for boundary-free far-field cases: the C ABI entry point
+// ibem_e3d_generate_spheres.  The reference reads centres and radii from position.txt
+// (configElastic3D.cpp:106-128) and ships no generator; this one makes the inputs of the
+// far-field workloads (thousands of spheres, hundreds of realisations) without text files.
+//
+// Two methods:
+//   RSA  random sequential addition: draw a centre uniformly in the box that keeps every
+//        sphere inside the cube, keep it when it clears every placed sphere, repeat;
+//        fast up to about 20% volume fraction, jams below 30% in small cubes.
+//   MC   hard-sphere Monte Carlo with box compression: spheres start on a simple cubic
+//        lattice in a cube large enough for the largest pair, every sweep moves each sphere
+//        by a random step (reflected at the faces, rejected if it would come closer than the
+//        minimum distance to a neighbour), then the cube and all centres are scaled down toward
+//        the target side as far as the closest pair allows; once the target is reached,
+//        further sweeps randomise the configuration.  Centres stay in [0, L]^3 (spheres may
+//        reach across the faces: the cube is a window of an unbounded particle cloud).
+// Pairs must keep a centre distance of at least r_i + r_j + gap * max(r_i, r_j).
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ibem_gb300.h"
+#include "../csrc/ibem_internal.h"
+
+namespace {
+
+// xoshiro256** seeded through splitmix64 (Blackman & Vigna, public-domain generators): the
+// same stream on every platform, so a seed names one microstructure.
+struct Rng {
+  uint64_t s[4];
+  explicit Rng(uint64_t seed) {
+    for (uint64_t& v : s) {
+      seed += 0x9e3779b97f4a7c15ULL;
+      uint64_t z = seed;
+      z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+      z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+      v = z ^ (z >> 31);
+    }
+  }
+  static uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+  uint64_t next() {
+    const uint64_t r = rotl(s[1] * 5, 7) * 9;
+    const uint64_t t = s[1] << 17;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = rotl(s[3], 45);
+    return r;
+  }
+  double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }  // [0, 1)
+  double uniform(double a, double b) { return a + (b - a) * uniform(); }
+};
+
+inline double min_dist(double ri, double rj, double gap) { return ri + rj + gap * std::max(ri, rj); }
+
+// Uniform cell grid over [0, L]^3 with cells no smaller than `h`, one vector of sphere
+// indices per cell.
+struct Cells {
+  int n = 1;
+  double inv = 0.0;
+  std::vector<std::vector<int>> cell;
+  std::vector<int> where;
+
+  void build(double L, double h, const std::vector<double>& c, int count) {
+    n = std::max(1, std::min(128, (int)std::floor(L / h)));
+    inv = n / L;
+    cell.assign((size_t)n * n * n, {});
+    where.assign(c.size() / 3, -1);
+    for (int k = 0; k < count; ++k) insert(k, &c[3 * k]);
+  }
+  int index(const double* x) const {
+    int i[3];
+    for (int d = 0; d < 3; ++d) i[d] = std::min(n - 1, std::max(0, (int)(x[d] * inv)));
+    return (i[2] * n + i[1]) * n + i[0];
+  }
+  void insert(int k, const double* x) {
+    const int id = index(x);
+    cell[id].push_back(k);
+    where[k] = id;
+  }
+  void remove(int k) {
+    std::vector<int>& v = cell[where[k]];
+    const auto it = std::find(v.begin(), v.end(), k);
+    *it = v.back();
+    v.pop_back();
+    where[k] = -1;
+  }
+  // Calls f(j) for every sphere j in the 27 cells around x.
+  template <class F>
+  bool any_near(const double* x, F&& f) const {
+    int i[3];
+    for (int d = 0; d < 3; ++d) i[d] = std::min(n - 1, std::max(0, (int)(x[d] * inv)));
+    for (int z = std::max(0, i[2] - 1); z <= std::min(n - 1, i[2] + 1); ++z)
+      for (int y = std::max(0, i[1] - 1); y <= std::min(n - 1, i[1] + 1); ++y)
+        for (int w = std::max(0, i[0] - 1); w <= std::min(n - 1, i[0] + 1); ++w)
+          for (int j : cell[(z * n + y) * n + w])
+            if (f(j)) return true;
+    return false;
+  }
+};
+
+bool clashes(const Cells& g, const std::vector<double>& c, const std::vector<double>& r, const double* x, double rx,
+             int self, double gap) {
+  return g.any_near(x, [&](int j) {
+    if (j == self) return false;
+    const double dx = x[0] - c[3 * j], dy = x[1] - c[3 * j + 1], dz = x[2] - c[3 * j + 2];
+    const double m = min_dist(rx, r[j], gap);
+    return dx * dx + dy * dy + dz * dz < m * m;
+  });
+}
+
+ibem_status rsa(const ibem_gen_params& p, double L, std::vector<double>& c, const std::vector<double>& r) {
+  const int num = p.num;
+  const double rmax = p.r0 * p.rhi, lo = rmax, hi = L - rmax;
+  if (hi <= lo) return ibem::fail(IBEM_ERR_ARG, "generate_spheres: cube smaller than one sphere");
+  Rng rng(p.seed);
+  Cells g;
+  g.build(L, min_dist(rmax, rmax, p.gap), c, 0);
+  const int64_t cap = p.max_tries > 0 ? p.max_tries : 200000000LL;
+  int64_t tries = 0;
+  for (int k = 0; k < num; ++k) {
+    double x[3];
+    do {
+      if (++tries > cap)
+        return ibem::fail(IBEM_ERR_ARG, "generate_spheres: random sequential addition stalled at " +
+                                            std::to_string(k) + " of " + std::to_string(num) + " spheres");
+      for (double& v : x) v = rng.uniform(lo, hi);
+    } while (clashes(g, c, r, x, r[k], -1, p.gap));
+    std::memcpy(&c[3 * k], x, sizeof x);
+    g.insert(k, x);
+  }
+  return IBEM_OK;
+}
+
+ibem_status mc(const ibem_gen_params& p, double L, std::vector<double>& c, const std::vector<double>& r) {
+  const int num = p.num;
+  const double rmax = *std::max_element(r.begin(), r.end());
+  const double h = min_dist(rmax, rmax, p.gap);
+  Rng rng(p.seed ^ 0x5bd1e995ULL);
+  // simple cubic start, spacing that clears the largest pair, sites in random order
+  int m = 1;
+  while ((int64_t)m * m * m < num) ++m;
+  const double s0 = h * (1.0 + 1e-9);
+  double Lc = std::max(L, m > 1 ? s0 * (m - 1) : L);
+  const double step0 = m > 1 ? Lc / (m - 1) : 0.0;
+  std::vector<int> site((size_t)m * m * m);
+  for (size_t i = 0; i < site.size(); ++i) site[i] = (int)i;
+  for (size_t i = site.size() - 1; i > 0; --i) std::swap(site[i], site[rng.next() % (i + 1)]);
+  for (int k = 0; k < num; ++k) {
+    const int q = site[k];
+    c[3 * k] = step0 * (q % m);
+    c[3 * k + 1] = step0 * ((q / m) % m);
+    c[3 * k + 2] = step0 * (q / (m * m));
+    if (m == 1)
+      for (int d = 0; d < 3; ++d) c[3 * k + d] = 0.5 * L;
+  }
+  // Cells of side >= h / kMinScale: a pair in non-adjacent cells is at least h / kMinScale
+  // apart, so after one shrink by a factor >= kMinScale it still clears h, the largest
+  // minimum distance; the closest pairs, which limit the shrink, are all in adjacent cells.
+  constexpr double kMinScale = 0.9;
+  const double hc = h / kMinScale;
+  Cells g;
+  double delta = 0.5 * h;
+  const int settle = p.sweeps > 0 ? p.sweeps : 100;
+  int after = 0, stalled = 0;
+  for (int sweep = 0; sweep < 100000; ++sweep) {
+    g.build(Lc, hc, c, num);
+    int accepted = 0;
+    for (int t = 0; t < num; ++t) {
+      const int k = (int)(rng.next() % (uint64_t)num);
+      double x[3];
+      for (int d = 0; d < 3; ++d) {  // steps that cross a face are reflected back into the cube
+        x[d] = c[3 * k + d] + rng.uniform(-delta, delta);
+        if (x[d] < 0.0) x[d] = -x[d];
+        if (x[d] > Lc) x[d] = 2.0 * Lc - x[d];
+        x[d] = std::min(std::max(x[d], 0.0), Lc);
+      }
+      if (clashes(g, c, r, x, r[k], k, p.gap)) continue;
+      g.remove(k);
+      std::memcpy(&c[3 * k], x, sizeof x);
+      g.insert(k, x);
+      ++accepted;
+    }
+    // keep about a third of the moves accepted
+    const double acc = (double)accepted / num;
+    delta *= acc > 0.35 ? 1.1 : 0.9;
+    delta = std::min(std::max(delta, 1e-6 * h), 0.5 * h);
+    if (Lc <= L) {
+      if (++after >= settle) return IBEM_OK;
+      continue;
+    }
+    // largest admissible shrink: the closest pair (relative to its minimum distance) may
+    // close half of its remaining room
+    double f = 0.0;
+    for (int k = 0; k < num; ++k)
+      g.any_near(&c[3 * k], [&](int j) {
+        if (j <= k) return false;
+        const double dx = c[3 * k] - c[3 * j], dy = c[3 * k + 1] - c[3 * j + 1], dz = c[3 * k + 2] - c[3 * j + 2];
+        f = std::max(f, min_dist(r[k], r[j], p.gap) / std::sqrt(dx * dx + dy * dy + dz * dz));
+        return false;
+      });
+    const double scale = std::max({L / Lc, kMinScale, 0.5 * (1.0 + f)});
+    stalled = scale > 1.0 - 1e-7 ? stalled + 1 : 0;
+    if (stalled > 2000) break;  // jammed: the closest pairs no longer open up
+    if (scale < 1.0) {
+      for (double& v : c) v *= scale;
+      Lc = std::max(L, Lc * scale);
+    }
+  }
+  return ibem::fail(IBEM_ERR_ARG, "generate_spheres: compression did not reach the volume fraction");
+}
+
+}  // namespace
+
+extern "C" ibem_status ibem_e3d_generate_spheres(const ibem_gen_params* p, double* centers, double* radius,
+                                                 double* side) {
+  if (!p || p->num < 1 || !centers || !radius || !(p->r0 > 0) || !(p->rlo > 0) || p->rhi < p->rlo ||
+      !(p->vf > 0 && p->vf < 0.6) || p->gap < 0 || (p->method != IBEM_GEN_RSA && p->method != IBEM_GEN_MC))
+    return ibem::fail(IBEM_ERR_ARG, "generate_spheres: bad parameters");
+  const int num = p->num;
+  std::vector<double> r(num), c(3 * (size_t)num, 0.0);
+  Rng rr(p->seed);
+  for (double& v : r) v = p->r0 * rr.uniform(p->rlo, p->rhi);
+  double vol = 0.0;
+  for (double v : r) vol += 4.0 / 3.0 * M_PI * v * v * v;
+  const double L = std::cbrt(vol / p->vf);
+  Rng rc(p->seed + 0x632be59bd9b4e019ULL);
+  ibem_gen_params q = *p;
+  q.seed = rc.next();
+  const ibem_status s = p->method == IBEM_GEN_RSA ? rsa(q, L, c, r) : mc(q, L, c, r);
+  if (s) return s;
+  std::memcpy(centers, c.data(), sizeof(double) * c.size());
+  std::memcpy(radius, r.data(), sizeof(double) * r.size());
+  if (side) *side = L;
+  return IBEM_OK;
+}

@@ -248,6 +248,22 @@ ibem_status ibem_e3d_mf_tuning(const ibem_e3d_batch* batch, int* slices_fp32, in
 ibem_status ibem_e3d_batch_farfield_rhs(const ibem_e3d_batch* batch, const double* sig_inf,
                                         double* b_dev, void* stream);
 
+/* The same for any layout (24, 60, 78): realisation s occupies entries
+ * layout * seg_begin[s] .. layout * seg_begin[s+1] - 1 of b_dev. */
+ibem_status ibem_e3d_batch_farfield_rhs_layout(const ibem_e3d_batch* batch, int layout,
+                                               const double* sig_inf, double* b_dev, void* stream);
+
+/* Dense solves of the realisations of a batch, one after another on the stream, for the
+ * layouts the matrix-free products do not cover (quadratic eigenstrain, layouts 60 and 78):
+ * per realisation its pair blocks (ibem_e3d_pair_blocks) into one N x N matrix sized for
+ * the largest realisation and allocated once, then ibem_e3d_solve(form, tol) (the mixed
+ * form: FP32 LU with split-BF16 tensor-core updates, FP64 GMRES-IR).  b_dev, x_dev: layout *
+ * seg_begin[nseg] doubles.  reports: host array of nseg (may be NULL).  Synchronous.
+ * The reference solves one microstructure per run (systemSolverElastic3D.h:44-60). */
+ibem_status ibem_e3d_batch_dense_solve(const ibem_e3d_batch* batch, int layout,
+                                       ibem_solver_form form, const double* b_dev, double* x_dev,
+                                       double tol, ibem_solve_report* reports, void* stream);
+
 /* Effective response of each realisation under the remote stress sig_inf (host, xx xy xz yy
  * yz zz) from its solution x: mean strain <e> = C0^-1 : sig_inf + sum_p (V_p / volume) E_p
  * (the eigenstrain's order-0 part, whose volume average over a sphere is E_p), written to
@@ -256,6 +272,13 @@ ibem_status ibem_e3d_batch_farfield_rhs(const ibem_e3d_batch* batch, const doubl
 ibem_status ibem_e3d_effective_modulus(const ibem_e3d_batch* batch, const double* x_dev,
                                        const double* volume, const double* sig_inf,
                                        double* mean_strain, double* e_eff, void* stream);
+
+/* The same for solutions of any layout: a layout-60/78 particle's eigenstrain
+ * E_ij + E_ijk x_k + E_ijkl x_k x_l averages to E_ij + (a^2 / 5) sum_k E_ijkk over its sphere. */
+ibem_status ibem_e3d_effective_modulus_layout(const ibem_e3d_batch* batch, int layout,
+                                              const double* x_dev, const double* volume,
+                                              const double* sig_inf, double* mean_strain,
+                                              double* e_eff, void* stream);
 
 /* The boundary-free far-field pipeline of one microstructure on host buffers, for FFI
  * callers (the matrix-free counterpart of ibem_e3d_run_host, layout 24): copies in,
@@ -268,6 +291,32 @@ ibem_status ibem_e3d_run_host_mf(const ibem_material* mat, int num, const double
                                  const double* sig_inf, ibem_precond pc, const float* gnn_params,
                                  const ibem_mf_options* opt, double* X, double* stress,
                                  ibem_mf_report* report);
+
+/* ---- microstructure generator (no reference counterpart) -------------------- */
+/* The reference reads centres and radii from position.txt (configElastic3D.cpp:106-128);
+ * this makes seeded far-field microstructures without text files. */
+typedef enum {
+  IBEM_GEN_RSA = 0, /* random sequential addition, every sphere inside the cube */
+  IBEM_GEN_MC = 1   /* hard-sphere Monte Carlo from a lattice with box compression, centres in
+                     * the cube; reaches volume fractions at which addition jams (30%) */
+} ibem_gen_method;
+
+typedef struct {
+  int num;            /* spheres */
+  double r0;          /* radius scale: radius_k = r0 * U[rlo, rhi] */
+  double rlo, rhi;
+  double vf;          /* volume fraction: cube side L = (sum of sphere volumes / vf)^(1/3) */
+  double gap;         /* centre distance >= r_i + r_j + gap * max(r_i, r_j) */
+  int method;         /* ibem_gen_method */
+  uint64_t seed;      /* the same seed gives the same microstructure on every platform */
+  int64_t max_tries;  /* RSA: candidate centres before giving up (0 = 2e8) */
+  int sweeps;         /* MC: sweeps after the target side is reached (0 = 100) */
+} ibem_gen_params;
+
+/* Host arrays: centers num x 3 (row-major), radius num; side (may be NULL) gets L.  Runs on
+ * the host only.  IBEM_ERR_ARG with a message when the packing cannot be reached. */
+ibem_status ibem_e3d_generate_spheres(const ibem_gen_params* p, double* centers, double* radius,
+                                      double* side);
 
 /* ---- learned preconditioner (no reference counterpart) --------------------- */
 /* On the graph of each particle's 16 nearest neighbours (edges e = (i <- j)), with B the

@@ -1,0 +1,79 @@
+"""The native microstructure generator (ibem_e3d_generate_spheres, host code of
+libibem_gb300.so; no GPU): every pair keeps its minimum distance, radii and centres stay in
+their ranges, the volume fraction is the one asked for, a seed names one microstructure, the
+Monte Carlo method reaches 30% (where addition jams) without leaving a lattice behind, and an
+unreachable packing is an error, not a hang."""
+import ctypes
+
+import numpy as np
+import pytest
+
+
+def gen(num, vf, seed=3, method="mc", r0=0.008):
+    from ibemproject_gb300 import cases
+    c = cases.generated_case(num, r0, vf, seed=seed, method=method)
+    return c, float(c.title.split("=")[1])
+
+
+def pair_ratio(C, R, gap=0.1):
+    d = np.sqrt(((C[:, None] - C[None]) ** 2).sum(-1))
+    m = R[:, None] + R[None] + gap * np.maximum(R[:, None], R[None])
+    np.fill_diagonal(d, np.inf)
+    return float((d / m).min())
+
+
+@pytest.mark.parametrize("method,num,vf", [("rsa", 1, 0.1), ("rsa", 200, 0.15), ("rsa", 2000, 0.15),
+                                           ("mc", 1, 0.2), ("mc", 50, 0.3), ("mc", 500, 0.3), ("mc", 1500, 0.25)])
+def test_spheres_clear_every_pair_and_fill_the_volume(method, num, vf):
+    r0 = 0.008
+    c, L = gen(num, vf, method=method, r0=r0)
+    C, R = c.centers, c.radius
+    assert C.shape == (num, 3) and R.shape == (num,)
+    assert R.min() >= 0.8 * r0 and R.max() <= 1.2 * r0
+    if num > 1:
+        assert pair_ratio(C, R) >= 1.0 - 1e-12
+    vol = float(np.sum(4.0 / 3.0 * np.pi * R ** 3))
+    assert abs(vol / L ** 3 - vf) <= 1e-12 * vf
+    if method == "rsa":   # every sphere inside the cube
+        assert (C - R[:, None]).min() >= 0 and (C + R[:, None]).max() <= L
+    else:                 # centres in the cube
+        assert C.min() >= 0 and C.max() <= L
+
+
+def test_seed_names_one_microstructure():
+    a, _ = gen(300, 0.25, seed=11)
+    b, _ = gen(300, 0.25, seed=11)
+    c, _ = gen(300, 0.25, seed=12)
+    assert np.array_equal(a.centers, b.centers) and np.array_equal(a.radius, b.radius)
+    assert not np.allclose(a.centers, c.centers)
+
+
+def test_monte_carlo_leaves_no_lattice_behind():
+    """Nearest-neighbour distances spread like a fluid's; no centre is left on a face."""
+    c, L = gen(1000, 0.3, seed=5)
+    C = c.centers
+    d = np.sqrt(((C[:, None] - C[None]) ** 2).sum(-1))
+    np.fill_diagonal(d, np.inf)
+    nn = d.min(1)
+    assert nn.std() / nn.mean() > 0.04
+    assert np.sum((C == 0) | (C == L)) == 0
+    # mean occupancy of the eight octants is uniform within sampling noise
+    oct_ = ((C > L / 2) * np.array([1, 2, 4])).sum(1)
+    counts = np.bincount(oct_, minlength=8)
+    assert counts.min() > 0.7 * 1000 / 8
+
+
+def test_unreachable_packing_is_an_error():
+    import ibemproject_gb300 as g
+    L = g.lib()
+    num = 400
+    C = np.zeros((num, 3))
+    R = np.zeros(num)
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    p = g.GenParams(num, 0.008, 0.8, 1.2, 0.45, 0.1, g.GEN_RSA, 1, 200000, 0)
+    assert L.ibem_e3d_generate_spheres(ctypes.byref(p), dp(C), dp(R), None) == 1
+    assert b"stalled" in L.ibem_last_error()
+    for bad in (g.GenParams(0, 0.008, 0.8, 1.2, 0.2, 0.1, g.GEN_MC, 1, 0, 0),
+                g.GenParams(10, 0.008, 1.2, 0.8, 0.2, 0.1, g.GEN_MC, 1, 0, 0),
+                g.GenParams(10, 0.008, 0.8, 1.2, 0.2, 0.1, 7, 1, 0, 0)):
+        assert L.ibem_e3d_generate_spheres(ctypes.byref(bad), dp(C), dp(R), None) == 1

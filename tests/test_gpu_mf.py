@@ -282,3 +282,49 @@ def test_autotuner_picks_valid_cached_shapes(B):
     rows = bt.seg_rows(0)
     xr = B.dense_solve(cs[0], b[rows]).cpu().numpy()
     assert scaled_err(x.cpu().numpy()[rows], xr) < 1e-8
+
+
+def test_quadratic_batch_dense_mixed_matches_fp64(B):
+    """Quadratic eigenstrain (layout 60) realisations of a ragged batch, solved one after
+    another by ibem_e3d_batch_dense_solve in the mixed form (FP32 LU with split-BF16
+    tensor-core updates, FP64 GMRES-IR), against the plain FP64 LU of each realisation, order
+    by order; the layout-aware effective modulus against a numpy restatement of the sphere
+    average E_ij + (a^2/5) E_ijkk; a lone sphere (uniform Eshelby eigenstrain: no quadratic
+    part) gives the layout-24 modulus."""
+    import ibemproject_gb300 as g
+    from ibemproject_gb300 import cases
+    nums = [1, 7, 40, 90]
+    cs = [cases.farfield_case(num=n, r0=0.012, vf=0.15, grid=0, seed=80 + k, E1=70e9 * (2.0 + 5.0 * k))
+          for k, n in enumerate(nums)]
+    bt = B.DeviceBatch(cs, layout=60)
+    sig = np.array([0.2, 0.0, 0.1, -0.3, 0.0, 1.0])
+    b = B.farfield_rhs(bt, sig)
+    assert b.numel() == 60 * sum(nums)
+    x, reps = B.dense_batch_solve(bt, b, g.SOLVE_MIXED_IR, tol=1e-12)
+    xh = x.cpu().numpy()
+    for s, c in enumerate(cs):
+        rows = bt.seg_rows(s)
+        xr = B.dense_solve(c, b[rows], layout=60).cpu().numpy().reshape(-1, 60)
+        xs = xh[rows].reshape(-1, 60)
+        for lo, hi in ((0, 6), (6, 24), (24, 60)):
+            assert scaled_err(xs[:, lo:hi], xr[:, lo:hi]) < 1e-8, (s, lo)
+        assert reps[s].backward_error <= 1e-12, s
+    # effective modulus: numpy restatement of the sphere average
+    vol = bt.volumes()
+    Eeff, eps = B.effective_modulus(bt, x, sig, volume=vol)
+    for s, c in enumerate(cs):
+        X = xh[bt.seg_rows(s)].reshape(-1, 60)
+        a = c.radius
+        avg = X[:, :6] + (a[:, None] ** 2 / 5) * (X[:, 24:60:6] + X[:, 27:60:6] + X[:, 29:60:6])
+        tr = sig[0] + sig[3] + sig[5]
+        e0 = ((1 + c.nu0) * sig - c.nu0 * tr * np.array([1, 0, 0, 1, 0, 1.0])) / c.E0
+        want = e0 + ((4 / 3 * np.pi * a ** 3)[:, None] * avg).sum(0) / vol[s]
+        np.testing.assert_allclose(eps[s], want, rtol=1e-12, atol=1e-12 * np.abs(want).max())
+        assert abs(Eeff[s] - sig[5] / want[5]) <= 1e-12 * abs(Eeff[s])
+    # the lone sphere: no quadratic part, same modulus as the linear layout
+    X0 = xh[bt.seg_rows(0)]
+    assert np.abs(X0[24:]).max() * cs[0].radius[0] ** 2 <= 1e-9 * np.abs(X0[:6]).max()
+    b1 = B.DeviceBatch(cs[:1])
+    x1, _ = B.solve(b1, B.farfield_rhs(b1, sig), B.PRECOND_BLOCK_JACOBI, tol=1e-12)
+    E1, _ = B.effective_modulus(b1, x1, sig, volume=vol[:1])
+    assert abs(E1[0] - Eeff[0]) <= 1e-9 * abs(E1[0])
