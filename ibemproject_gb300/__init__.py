@@ -117,6 +117,12 @@ SIGNATURES = {
                                     ctypes.POINTER(ctypes.c_float), ctypes.POINTER(MfOptions), _c_dp, _c_dp,
                                     ctypes.POINTER(MfReport)]),
     "ibem_e3d_generate_spheres": (_int, [ctypes.POINTER(GenParams), _c_dp, _c_dp, _c_dp]),
+    "ibem_e3d_sidecar_from_txt": (_int, [ctypes.c_char_p]),
+    "ibem_e3d_sidecar_write": (_int, [ctypes.c_char_p, ctypes.POINTER(Material), _int, _c_dp, _int, _c_ip, _c_dp,
+                                      _c_dp, _int, _c_dp, _c_dp, _int, _c_dp, _c_dp]),
+    "ibem_e3d_case_sizes": (_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]),
+    "ibem_e3d_read_case": (_int, [ctypes.c_char_p, ctypes.POINTER(Material), _c_dp, _c_ip, _c_dp, _c_dp, _c_dp,
+                                  _c_dp, _c_dp, _c_dp]),
     "ibem_gnn_param_count": (_i64, []),
     "ibem_gnn_init_params": (_int, [_vp, ctypes.c_uint64, _vp]),
     "ibem_gnn_prepare": (_int, [ctypes.POINTER(Batch), _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -213,6 +219,28 @@ def run_dir(path: str, layout: int = 78, form: int = SOLVE_FP64, tol: float = 1e
     rep = SolveReport()
     check(lib().ibem_e3d_run_dir(path.encode(), layout, form, tol, ctypes.byref(rep)))
     return rep
+
+
+def sidecar_from_txt(path: str) -> None:
+    """Write path/case.ibemb from the directory's text files (ibem_e3d_sidecar_from_txt)."""
+    check(lib().ibem_e3d_sidecar_from_txt(path.encode()))
+
+
+def read_case_native(path: str):
+    """The inputs of a case directory as the library reads them (the side-car when it is at
+    least as new as the text files): returns (cases.Case, read_from_side_car)."""
+    from . import cases
+    sz = (ctypes.c_int64 * 6)()
+    check(lib().ibem_e3d_case_sizes(path.encode(), sz))
+    NN, NE, num, nump, has_ff, from_sc = (int(v) for v in sz)
+    m = Material()
+    nodes, bc = np.zeros((NN, 3)), np.zeros((3 * NN, 2))
+    conn, tbc = np.zeros((NE, 4), np.int32), np.zeros((NE, 24))
+    cen, rad, pts, sig = np.zeros((num, 3)), np.zeros(num), np.zeros((nump, 3)), np.zeros(6)
+    check(lib().ibem_e3d_read_case(path.encode(), ctypes.byref(m), _dp(nodes), _ip(conn), _dp(bc), _dp(tbc),
+                                   _dp(cen), _dp(rad), _dp(pts), _dp(sig)))
+    c = cases.Case(m.E0, m.nu0, m.E1, m.nu1, nodes, conn, bc, tbc, cen, rad, pts, sig if has_ff else None)
+    return c, bool(from_sc)
 
 
 def bc_plan(case):

@@ -99,6 +99,11 @@ class configElastic3D_gb300 : public Config {
   int64_t n_unknowns() const { return 3 * (int64_t)NN + (int64_t)layout * num; }
   ibem_material material() const { return ibem_material{EE, XNU, E1, nu1}; }
 
+  // the text inputs, or the directory's binary side-car case.ibemb when it is at least as
+  // new as each of them (host/sidecar.cpp)
+  void setUp() override;
+  bool use_sidecar = true;
+  bool from_sidecar = false;
   void Readparticle_num() override;
   void Readpartical_info() override;
   void ReadBEM_num() override;

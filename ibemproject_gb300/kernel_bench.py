@@ -11,7 +11,8 @@
 --field NUM,G  the double-float stress sums (ibem_e3d_field_form, mixed form) of NUM spheres
                at G^3 grid points with random coefficients: NUM * G^3 pairs per launch.
 --solve NUM    the matrix-free solve of one far-field microstructure of NUM spheres (bench
-               distribution, N = 24 NUM) with block-Jacobi, Neumann and learned
+               distribution, N = 24 NUM; --vf sets the volume fraction, 0.15 by default,
+               Monte Carlo packing above 0.15) with block-Jacobi, Neumann and learned
                preconditioners (the network trained first on 12 microstructures of 100-150
                spheres): time, Arnoldi and refinement steps, phase times.
 --batch R      the batched measurement of bench.py (R realisations of U[50, 500] spheres,
@@ -151,7 +152,7 @@ def bench_field(num, grid, reps, dev):
             "ns_per_pair": ms * 1e6 / pairs if ms > 0 else None}
 
 
-def bench_solve(num, reps, dev):
+def bench_solve(num, reps, dev, vf=0.15):
     import numpy as np
     from . import batch as B
     from . import cases
@@ -163,10 +164,13 @@ def bench_solve(num, reps, dev):
     r, e = B.training_pairs(tb, nrhs=4, seed=5)
     params = B.init_params(seed=1, device=dev)
     hist = B.train(tb, r, e, params, steps=300, lr=3e-3)
-    c = cases.farfield_case(num=num, r0=0.012, vf=0.15, grid=0, seed=2024)
+    if vf <= 0.15:
+        c = cases.farfield_case(num=num, r0=0.012, vf=vf, grid=0, seed=2024)
+    else:   # random sequential addition jams near 25%: hard-sphere Monte Carlo packing
+        c = cases.generated_case(num, 0.012, vf, seed=2024, method="mc")
     bt = B.DeviceBatch([c], device=dev)
     b = B.farfield_rhs(bt, np.array([0, 0, 0, 0, 0, 1.0]))
-    out = {"kernel": "matrix-free solve", "spheres": num, "N": 24 * num, "reps": reps,
+    out = {"kernel": "matrix-free solve", "spheres": num, "N": 24 * num, "vf": vf, "reps": reps,
            "training_loss": [float(hist[0]), float(hist[-1])]}
     L = lib()
     for name, pc, pp in (("block_jacobi", B.PRECOND_BLOCK_JACOBI, None), ("neumann", B.PRECOND_NEUMANN, None),
@@ -227,6 +231,7 @@ def main(argv=None):
     ap.add_argument("--solve", type=int, action="append", default=[])
     ap.add_argument("--batch", type=int, action="append", default=[])
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--vf", type=float, default=0.15, help="volume fraction of --solve (above 0.15: Monte Carlo packing)")
     a = ap.parse_args(argv)
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
@@ -238,7 +243,7 @@ def main(argv=None):
     for n in a.mf:
         print(json.dumps(bench_mf(n, a.reps, dev)), flush=True)
     for n in a.solve:
-        print(json.dumps(bench_solve(n, a.reps, dev)), flush=True)
+        print(json.dumps(bench_solve(n, a.reps, dev, a.vf)), flush=True)
     for n in a.batch:
         print(json.dumps(bench_batch(n, a.reps, dev)), flush=True)
     for f in a.field:

@@ -292,6 +292,32 @@ ibem_status ibem_e3d_run_host_mf(const ibem_material* mat, int num, const double
                                  const ibem_mf_options* opt, double* X, double* stress,
                                  ibem_mf_report* report);
 
+/* ---- binary side-car of a case directory (no reference counterpart) --------- */
+/* case.ibemb holds what position.txt, BEM.txt, postprocess.txt (configElastic3D.cpp:32-197,
+ * configElastic3D.h:76-129) and farfield.txt hold, in binary (layout in host/sidecar.cpp);
+ * ibem_e3d_run_dir, ibem_e3d_case_sizes and ibem_e3d_read_case use it in place of the text
+ * files when it is at least as new as each of them.  All host-only and synchronous. */
+
+/* Parse the text files of `dir` and write dir/case.ibemb. */
+ibem_status ibem_e3d_sidecar_from_txt(const char* dir);
+
+/* Write a side-car at `path` from host arrays (the layouts of ibem_e3d_run_host;
+ * sig_inf may be NULL for a bounded case). */
+ibem_status ibem_e3d_sidecar_write(const char* path, const ibem_material* mat, int NN,
+                                   const double* nodes, int NE, const int* conn, const double* bc,
+                                   const double* tbc, int num, const double* centers,
+                                   const double* radius, int nump, const double* points,
+                                   const double* sig_inf);
+
+/* sizes[6] = NN, NE, num, nump, has_farfield, read_from_side_car. */
+ibem_status ibem_e3d_case_sizes(const char* dir, int64_t* sizes);
+
+/* The inputs of `dir` into host arrays sized by ibem_e3d_case_sizes (arrays of empty blocks
+ * may be NULL; sig_inf gets zeros when the case has a boundary). */
+ibem_status ibem_e3d_read_case(const char* dir, ibem_material* mat, double* nodes, int* conn,
+                               double* bc, double* tbc, double* centers, double* radius,
+                               double* points, double* sig_inf);
+
 /* ---- microstructure generator (no reference counterpart) -------------------- */
 /* The reference reads centres and radii from position.txt (configElastic3D.cpp:106-128);
  * this makes seeded far-field microstructures without text files. */
