@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--form", default="learned_gmres", choices=["learned_gmres", "mixed_ir"])
     ap.add_argument("--train-steps", type=int, default=300)
     ap.add_argument("--batch", type=int, default=256, help="realisations of the batched measurement (0: skip)")
+    ap.add_argument("--quad-form", default="bj", choices=["bj", "mixed"],
+                    help="solver form of the batch's quadratic realisations: block-Jacobi GMRES or FP32 LU + GMRES-IR")
     return ap.parse_args()
 
 
@@ -295,9 +297,10 @@ def run_batched(args, dev, params):
     U[2, 20], half with linear eigenstrain (24 unknowns per sphere) and half with quadratic
     (60), uniaxial remote stress.  One step = right-hand sides, the linear realisations in
     one batched matrix-free solve (learned preconditioner, FP64 refinement to relative
-    residual 1e-10), the quadratic ones by dense mixed-precision solves (FP32 LU with
-    split-BF16 tensor-core updates, FP64 GMRES-IR to scaled backward error 1e-12), and the
-    effective moduli of all.  Reports realisations per second."""
+    residual 1e-10), the quadratic ones assembled (FP64 pair blocks) and solved one after
+    another to scaled backward error 1e-12 (--quad-form bj: FP64 refinement of FP32-product
+    GMRES with per-sphere block-Jacobi; mixed: FP32 LU with split-BF16 tensor-core updates
+    and FP64 GMRES-IR), and the effective moduli of all.  Reports realisations per second."""
     import torch
     import ibemproject_gb300 as g
     from ibemproject_gb300 import batch as B
@@ -317,6 +320,7 @@ def run_batched(args, dev, params):
     bq = B.DeviceBatch([cs[i] for i in qi], device=dev, layout=60) if qi.size else None
     sig = np.array([0, 0, 0, 0, 0, 1.0])
     stream = torch.cuda.current_stream(dev)
+    qform = g.SOLVE_GMRES_BJ if args.quad_form == "bj" else g.SOLVE_MIXED_IR
 
     def step():
         out = {}
@@ -330,7 +334,7 @@ def run_batched(args, dev, params):
         ev[1].record(stream)
         if bq is not None:
             b = B.farfield_rhs(bq, sig)
-            x, reps = B.dense_batch_solve(bq, b, g.SOLVE_MIXED_IR, tol=1e-12)
+            x, reps = B.dense_batch_solve(bq, b, qform, tol=1e-12)
             e, _ = B.effective_modulus(bq, x, sig, volume=vol[qi])
             out["quad"] = (x, reps, e, b)
         ev[2].record(stream)
@@ -375,7 +379,10 @@ def run_batched(args, dev, params):
     quad_reps = out["quad"][1] if bq is not None else []
     return {"workload": (f"{args.batch} realisations, U[50,500] spheres r~U[0.8,1.2]*0.008, vf U[10%,30%], "
                          "E1/E0 U[2,20], half linear (24/sphere, matrix-free learned GMRES) and half quadratic "
-                         "(60/sphere, dense FP32-LU + BF16x3 + FP64 GMRES-IR) eigenstrain, far-field sigma33"),
+                         "(60/sphere, assembled; " + ("block-Jacobi FP32-product GMRES + FP64 refinement"
+                                                      if args.quad_form == "bj" else
+                                                      "FP32 LU + BF16x3 + FP64 GMRES-IR") +
+                         ") eigenstrain, far-field sigma33"),
             "value": args.batch / (ms / 1e3), "unit": "realisations/s", "ms_per_batch": ms,
             "ms_linear_part": ms_lin, "ms_quadratic_part": ms_quad,
             "realisations_linear": int(li.size), "realisations_quadratic": int(qi.size),

@@ -20,7 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libibem_gb300.so")
 
 IBEM_OK, IBEM_ERR_ARG, IBEM_ERR_CUDA, IBEM_ERR_NOCONV, IBEM_ERR_TIMEOUT, IBEM_ERR_SINGULAR, IBEM_ERR_IO = range(7)
-SOLVE_FP64, SOLVE_MIXED_IR = 0, 1
+SOLVE_FP64, SOLVE_MIXED_IR, SOLVE_GMRES_BJ = 0, 1, 2
 
 _c_dp = ctypes.POINTER(ctypes.c_double)
 _c_ip = ctypes.POINTER(ctypes.c_int)
@@ -92,6 +92,7 @@ SIGNATURES = {
     "ibem_e3d_get_ut": (_int, [_int, _int, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "ibem_e3d_farfield_rhs": (_int, [_int, ctypes.POINTER(Material), _int, _c_dp, _vp, _vp]),
     "ibem_e3d_solve": (_int, [_int, _i64, _vp, _i64, _vp, _vp, _dbl, ctypes.POINTER(SolveReport), _vp]),
+    "ibem_e3d_solve_bj": (_int, [_i64, _int, _vp, _i64, _vp, _vp, _dbl, ctypes.POINTER(SolveReport), _vp]),
     "ibem_gemm_sub_f32": (_int, [_i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp]),
     "ibem_e3d_solve_noalloc": (_int, [_i64, _vp, _i64, _vp, _vp, ctypes.POINTER(SolveReport), _vp]),
     "ibem_e3d_field": (_int, [_vp, _int, _vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _vp, _int, _vp,

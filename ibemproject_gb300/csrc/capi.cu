@@ -269,7 +269,15 @@ ibem_status ibem_e3d_farfield_rhs(int num, const ibem_material* mat, int layout,
 ibem_status ibem_e3d_solve(ibem_solver_form form, int64_t N, double* A_dev, int64_t lda,
                            const double* b_dev, double* x_dev, double tol,
                            ibem_solve_report* report, void* stream) {
+  if (form == IBEM_SOLVE_GMRES_BJ) return fail(IBEM_ERR_ARG, "solve: the block-Jacobi form is ibem_e3d_solve_bj");
   return solve_dense(form, N, A_dev, lda, b_dev, x_dev, tol, report, as_stream(stream));
+}
+
+ibem_status ibem_e3d_solve_bj(int64_t N, int block, const double* A_dev, int64_t lda, const double* b_dev,
+                              double* x_dev, double tol, ibem_solve_report* report, void* stream) {
+  // the block-Jacobi form reads A and never writes it
+  return solve_dense(IBEM_SOLVE_GMRES_BJ, N, const_cast<double*>(A_dev), lda, b_dev, x_dev, tol, report,
+                     as_stream(stream), block);
 }
 
 ibem_status ibem_gemm_sub_f32(int64_t m, int64_t n, int64_t k, const float* A_dev, int64_t lda,

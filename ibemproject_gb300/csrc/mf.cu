@@ -1240,7 +1240,9 @@ extern "C" ibem_status ibem_e3d_batch_dense_solve(const ibem_e3d_batch* batch, i
     if (n) {
       s = ibem_e3d_pair_blocks(batch->centers_dev + 3 * (int64_t)p0, batch->radius_dev + p0, n, &batch->mats[i], layout,
                                A, N, 0, 0, st);
-      if (!s) s = ibem_e3d_solve(form, N, A, N, b_dev + off, x_dev + off, tol, &rep, st);
+      if (!s)
+        s = form == IBEM_SOLVE_GMRES_BJ ? ibem_e3d_solve_bj(N, nu, A, N, b_dev + off, x_dev + off, tol, &rep, st)
+                                        : ibem_e3d_solve(form, N, A, N, b_dev + off, x_dev + off, tol, &rep, st);
     }
     if (reports) reports[i] = rep;
   }

@@ -9,6 +9,13 @@
 //                        cores with the split-BF16 "x3" scheme, FP32 accumulation), then
 //                        FP64 GMRES iterative refinement preconditioned by the FP32 factors;
 //                        FP64 is used for the residual b - A x and the GMRES arithmetic.
+//   IBEM_SOLVE_GMRES_BJ  no factorisation: iterative refinement whose corrections are GMRES
+//                        solves with an FP32 copy of the scaled matrix (products accumulated
+//                        in FP64), right-preconditioned by the inverses of its diagonal
+//                        blocks (one block per particle); FP64 residuals decide convergence.
+//                        Far cheaper than a factorisation for the small, well-conditioned
+//                        systems of far-field microstructures (a few thousand to 30,000
+//                        unknowns), whose LU is bound by launch latency.
 //
 // LU structure: recursive on column halves (Toledo), so most flops sit in a few large
 // GEMMs.  Leaves are panels of <= 32 columns factorised by one cooperative kernel that
@@ -25,6 +32,7 @@
 #include <cmath>
 #include <cstdio>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "ibem_internal.h"
@@ -52,6 +60,24 @@ __global__ void k_rowmax(int64_t n, const double* __restrict__ A, int64_t lda, d
   if (i >= n) return;
   double m = 0;
   for (int64_t j = 0; j < n; ++j) m = fmax(m, fabs(A[j * lda + i]));
+  r[i] = m > 0 ? 1.0 / m : 1.0;
+}
+
+// row max over a column chunk (grid.y = chunk): coalesced along columns, N x chunks threads
+__global__ void k_rowmax_part(int64_t n, const double* __restrict__ A, int64_t lda, int64_t chunk,
+                              double* __restrict__ part) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+  if (i >= n) return;
+  double m = 0;
+  for (int64_t j = j0; j < j1; ++j) m = fmax(m, fabs(A[j * lda + i]));
+  part[blockIdx.y * n + i] = m;
+}
+__global__ void k_rowmax_fin(int64_t n, int nparts, const double* __restrict__ part, double* __restrict__ r) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double m = 0;
+  for (int p = 0; p < nparts; ++p) m = fmax(m, part[p * n + i]);
   r[i] = m > 0 ? 1.0 / m : 1.0;
 }
 
@@ -1240,6 +1266,16 @@ __global__ void k_scaled_rowsum(int64_t n, const double* __restrict__ A, int64_t
   for (int64_t j = 0; j < n; ++j) s += fabs(A[j * lda + i]) * c[j];
   rs[i] = s * r[i];
 }
+// partial row sums of |A_ij| c_j over a column chunk (finished by k_scale_rows_of_parts)
+__global__ void k_abs_rowsum_part(int64_t n, const double* __restrict__ A, int64_t lda, const double* __restrict__ c,
+                                  int64_t chunk, double* __restrict__ part) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+  if (i >= n) return;
+  double s = 0;
+  for (int64_t j = j0; j < j1; ++j) s += fabs(A[j * lda + i]) * c[j];
+  part[blockIdx.y * n + i] = s;
+}
 // y = r .* (A (c .* v)) via the partial-sum GEMV; tmp is an N-vector
 __global__ void k_scale_rows_of_parts(int64_t n, int nparts, const double* __restrict__ part,
                                       const double* __restrict__ r, double* __restrict__ y) {
@@ -1247,7 +1283,123 @@ __global__ void k_scale_rows_of_parts(int64_t n, int nparts, const double* __res
   if (i >= n) return;
   double s = 0;
   for (int p = 0; p < nparts; ++p) s += part[p * n + i];
-  y[i] = r[i] * s;
+  y[i] = (r ? r[i] : 1.0) * s;
+}
+
+// Partial products of the FP32 scaled matrix with an FP64 vector over a column chunk,
+// accumulated in FP64 (finished by k_scale_rows_of_parts with r = nullptr).
+__global__ void k_gemv_part_f32(int64_t n, const float* __restrict__ W, int64_t ldw, const double* __restrict__ x,
+                                int64_t chunk, double* __restrict__ part) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+  if (i >= n) return;
+  double s0 = 0, s1 = 0;
+  int64_t j = j0;
+  for (; j + 1 < j1; j += 2) {
+    s0 += (double)W[j * ldw + i] * x[j];
+    s1 += (double)W[(j + 1) * ldw + i] * x[j + 1];
+  }
+  if (j < j1) s0 += (double)W[j * ldw + i] * x[j];
+  part[blockIdx.y * n + i] = s0 + s1;
+}
+
+// Inverse of diagonal block blockIdx.x (rows and columns g0 .. g0 + nb - 1, g0 = block *
+// blockIdx.x, nb = min(block, n - g0)) of As = R A C: Gauss-Jordan elimination in place with
+// partial pivoting, FP64 in dynamic shared memory (block x (block + 1) doubles, block <=
+// kBjMax), written in FP32, column-major, to P + blockIdx.x * block^2.  A zero pivot raises
+// *info (the block's first row + 1).
+constexpr int kBjMax = 80;
+constexpr int kBjThreads = 256;
+constexpr int kBjApplyThreads = 96;   // >= kBjMax, whole warps
+inline size_t bj_smem(int block) { return sizeof(double) * (size_t)block * (block + 1); }
+__global__ void __launch_bounds__(kBjThreads) k_bj_invert(int64_t n, int block, const double* __restrict__ A,
+                                                          int64_t lda, const double* __restrict__ r,
+                                                          const double* __restrict__ c, float* __restrict__ P,
+                                                          int* __restrict__ info) {
+  extern __shared__ double bj_mem[];
+  __shared__ double col[kBjMax];
+  __shared__ int piv[kBjMax];
+  __shared__ int sp;
+  const int ld = block + 1;
+  auto M = [&](int i) { return bj_mem + (size_t)i * ld; };   // row i
+  const int64_t g0 = (int64_t)block * blockIdx.x;
+  const int nb = (int)min((int64_t)block, n - g0);
+  const int t = threadIdx.x;
+  for (int e = t; e < nb * nb; e += kBjThreads) {
+    const int i = e % nb, j = e / nb;
+    M(i)[j] = r[g0 + i] * A[(g0 + j) * lda + g0 + i] * c[g0 + j];
+  }
+  __syncthreads();
+  for (int k = 0; k < nb; ++k) {
+    if (t < 32) {  // pivot: largest |M(i)[k]|, i >= k
+      double best = -1.0;
+      int bi = k;
+      for (int i = k + t; i < nb; i += 32) {
+        const double v = fabs(M(i)[k]);
+        if (v > best) best = v, bi = i;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_down_sync(0xffffffffu, best, o);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) best = ob, bi = oi;
+      }
+      if (t == 0) sp = bi, piv[k] = bi;
+    }
+    __syncthreads();
+    const int p = sp;
+    if (p != k)
+      for (int j = t; j < nb; j += kBjThreads) {
+        const double v = M(k)[j];
+        M(k)[j] = M(p)[j];
+        M(p)[j] = v;
+      }
+    __syncthreads();
+    const double d = M(k)[k];
+    if (d == 0.0) {
+      if (t == 0) atomicCAS(info, 0, (int)g0 + 1);
+      return;
+    }
+    for (int i = t; i < nb; i += kBjThreads) col[i] = M(i)[k];
+    __syncthreads();
+    if (t == 0) M(k)[k] = 1.0;
+    __syncthreads();
+    for (int j = t; j < nb; j += kBjThreads) M(k)[j] /= d;
+    __syncthreads();
+    for (int e = t; e < nb * nb; e += kBjThreads) {
+      const int i = e % nb, j = e / nb;
+      if (i != k) M(i)[j] = (j == k ? 0.0 : M(i)[j]) - col[i] * M(k)[j];
+    }
+    __syncthreads();
+  }
+  // undo the row exchanges as column exchanges of the inverse, last first
+  for (int k = nb - 1; k >= 0; --k) {
+    const int p = piv[k];
+    if (p != k)
+      for (int i = t; i < nb; i += kBjThreads) {
+        const double v = M(i)[k];
+        M(i)[k] = M(i)[p];
+        M(i)[p] = v;
+      }
+    __syncthreads();
+  }
+  float* out = P + (int64_t)blockIdx.x * block * block;
+  for (int e = t; e < nb * nb; e += kBjThreads) out[e] = (float)M(e % nb)[e / nb];
+}
+
+// z = P v blockwise (one CTA per diagonal block, thread i = row i of the block)
+__global__ void __launch_bounds__(kBjApplyThreads) k_bj_apply(int64_t n, int block, const float* __restrict__ P,
+                                                     const double* __restrict__ v, double* __restrict__ z) {
+  __shared__ double sv[kBjMax];
+  const int64_t g0 = (int64_t)block * blockIdx.x;
+  const int nb = (int)min((int64_t)block, n - g0);
+  const int i = threadIdx.x;
+  if (i < nb) sv[i] = v[g0 + i];
+  __syncthreads();
+  if (i >= nb) return;
+  const float* Pb = P + (int64_t)blockIdx.x * block * block;
+  double s = 0;
+  for (int j = 0; j < nb; ++j) s += (double)Pb[j * nb + i] * sv[j];
+  z[g0 + i] = s;
 }
 }  // namespace
 
@@ -1279,14 +1431,25 @@ static ibem_status scaled_backward_error(SolveCtx& cx, const double* A, int64_t 
   return IBEM_OK;
 }
 
+// Row scaling r (1 / row max) and column scaling c (1 / column max of R A): As = R A C.
+static ibem_status equilibrate(SolveCtx& cx, const double* A, int64_t lda) {
+  const int64_t N = cx.N;
+  const unsigned nb = (unsigned)((N + 255) / 256);
+  const int64_t chunk = (N + cx.nparts - 1) / cx.nparts;
+  ::ibem::count_launch(), k_rowmax_part<<<dim3(nb, (unsigned)cx.nparts), 256, 0, cx.st>>>(N, A, lda, chunk, cx.part);
+  ::ibem::count_launch(), k_rowmax_fin<<<nb, 256, 0, cx.st>>>(N, cx.nparts, cx.part, cx.r);
+  ::ibem::count_launch(), k_colmax<<<(unsigned)N, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c);
+  IBEM_LAUNCH_CHECK("equilibrate");
+  return IBEM_OK;
+}
+
 template <typename T>
 static ibem_status factor(SolveCtx& cx, const double* A, int64_t lda, T*& W, LuWork<T>& w, int& info) {
   const int64_t N = cx.N;
   IBEM_CUDA(cudaMalloc(&W, sizeof(T) * (size_t)N * N));
   {
     ProfScope ps(PROF_EQUIL, cx.st);
-    ::ibem::count_launch(), k_rowmax<<<(unsigned)((N + 255) / 256), 256, 0, cx.st>>>(N, A, lda, cx.r);
-    ::ibem::count_launch(), k_colmax<<<(unsigned)N, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c);
+    if (ibem_status q = equilibrate(cx, A, lda)) return q;
     dim3 g((unsigned)((N + 255) / 256), (unsigned)N);
     ::ibem::count_launch(), k_scale_copy<T><<<g, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c, W, N);
     IBEM_LAUNCH_CHECK("equilibrate");
@@ -1322,10 +1485,94 @@ static ibem_status factor(SolveCtx& cx, const double* A, int64_t lda, T*& W, LuW
   return IBEM_OK;
 }
 
+// One restart cycle of right-preconditioned GMRES on As d = rvec with FP64 vectors (V: N x
+// (m + 1), Z: N x m, hd: m + 1 doubles of device scratch): prec(v, z) writes z = M^-1 v and
+// op(z, w) writes w = As z.  Classical Gram-Schmidt applied twice, Givens rotations on the
+// host.  Stops after m steps or once the residual estimate |g_k+1| <= max(stop_abs,
+// stop_rel * beta); adds the correction Z y to ys.  steps: Arnoldi steps taken; est: the
+// final residual estimate; beta: ||rvec|| (0: nothing to do).
+template <class Prec, class Op>
+static ibem_status gmres_cycle(int64_t N, int m, const double* rvec, double* V, double* Z, double* hd, double* ys,
+                               double stop_abs, double stop_rel, Prec&& prec, Op&& op, int& steps, double& est,
+                               double& beta, cudaStream_t st) {
+  const unsigned nb = (unsigned)((N + 255) / 256);
+  steps = 0;
+  IBEM_CUDA(cudaMemsetAsync(hd, 0, sizeof(double), st));
+  ::ibem::count_launch(), k_dot_many<<<256, 256, 0, st>>>(N, 1, rvec, N, rvec, hd);
+  double b2 = 0;
+  IBEM_CUDA(cudaMemcpyAsync(&b2, hd, sizeof(double), cudaMemcpyDeviceToHost, st));
+  IBEM_CUDA(cudaStreamSynchronize(st));
+  beta = std::sqrt(std::max(b2, 0.0));
+  est = beta;
+  if (beta == 0) return IBEM_OK;
+  const double stop = std::max(stop_abs, stop_rel * beta);
+  ::ibem::count_launch(), k_axpby<<<nb, 256, 0, st>>>(N, 1.0 / beta, rvec, 0.0, V);
+  std::vector<double> H((m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0);
+  g[0] = beta;
+  int k = 0;
+  ibem_status s = IBEM_OK;
+  for (; k < m; ++k) {
+    double* vk = V + (size_t)k * N;
+    double* zk = Z + (size_t)k * N;
+    double* wv = V + (size_t)(k + 1) * N;
+    if ((s = prec(vk, zk))) return s;
+    if ((s = op(zk, wv))) return s;
+    // classical Gram-Schmidt, twice
+    std::vector<double> hk(k + 1, 0.0), h2(k + 1);
+    for (int pass = 0; pass < 2; ++pass) {
+      IBEM_CUDA(cudaMemsetAsync(hd, 0, sizeof(double) * (k + 1), st));
+      ::ibem::count_launch(), k_dot_many<<<256, 256, 0, st>>>(N, k + 1, V, N, wv, hd);
+      ::ibem::count_launch(), k_sub_Vh<<<nb, 256, 0, st>>>(N, k + 1, V, N, hd, wv);
+      IBEM_CUDA(cudaMemcpyAsync(h2.data(), hd, sizeof(double) * (k + 1), cudaMemcpyDeviceToHost, st));
+      IBEM_CUDA(cudaStreamSynchronize(st));
+      for (int i = 0; i <= k; ++i) hk[i] += h2[i];
+    }
+    IBEM_CUDA(cudaMemsetAsync(hd, 0, sizeof(double), st));
+    ::ibem::count_launch(), k_dot_many<<<256, 256, 0, st>>>(N, 1, wv, N, wv, hd);
+    double nrm2 = 0;
+    IBEM_CUDA(cudaMemcpyAsync(&nrm2, hd, sizeof(double), cudaMemcpyDeviceToHost, st));
+    IBEM_CUDA(cudaStreamSynchronize(st));
+    const double hn = std::sqrt(std::max(nrm2, 0.0));
+    if (hn > 0) ::ibem::count_launch(), k_axpby<<<nb, 256, 0, st>>>(N, 1.0 / hn, wv, 0.0, wv);
+    for (int i = 0; i <= k; ++i) H[i * m + k] = hk[i];
+    H[(k + 1) * m + k] = hn;
+    for (int i = 0; i < k; ++i) {  // previous Givens rotations
+      const double t = cs[i] * H[i * m + k] + sn[i] * H[(i + 1) * m + k];
+      H[(i + 1) * m + k] = -sn[i] * H[i * m + k] + cs[i] * H[(i + 1) * m + k];
+      H[i * m + k] = t;
+    }
+    const double den = std::hypot(H[k * m + k], H[(k + 1) * m + k]);
+    cs[k] = den > 0 ? H[k * m + k] / den : 1.0;
+    sn[k] = den > 0 ? H[(k + 1) * m + k] / den : 0.0;
+    H[k * m + k] = den;
+    H[(k + 1) * m + k] = 0;
+    g[k + 1] = -sn[k] * g[k];
+    g[k] = cs[k] * g[k];
+    ++steps;
+    est = std::fabs(g[k + 1]);
+    if (est <= stop || hn == 0) { ++k; break; }
+  }
+  std::vector<double> yv(k, 0.0);
+  for (int i = k - 1; i >= 0; --i) {
+    double t = g[i];
+    for (int j2 = i + 1; j2 < k; ++j2) t -= H[i * m + j2] * yv[j2];
+    yv[i] = t / H[i * m + i];
+  }
+  IBEM_CUDA(cudaMemcpyAsync(hd, yv.data(), sizeof(double) * k, cudaMemcpyHostToDevice, st));
+  ::ibem::count_launch(), k_axpby<<<nb, 256, 0, st>>>(N, -1.0, ys, 0.0, ys);  // ys = -ys
+  ::ibem::count_launch(), k_sub_Vh<<<nb, 256, 0, st>>>(N, k, Z, N, hd, ys);    // ys = -ys - Z y
+  ::ibem::count_launch(), k_axpby<<<nb, 256, 0, st>>>(N, -1.0, ys, 0.0, ys);  // ys = ys + Z y
+  IBEM_LAUNCH_CHECK("gmres update");
+  return IBEM_OK;
+}
+
 ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda, const double* b, double* x,
-                        double tol, ibem_solve_report* rep, cudaStream_t st) {
+                        double tol, ibem_solve_report* rep, cudaStream_t st, int block) {
   if (N <= 0 || !A || !b || !x || lda < N) return fail(IBEM_ERR_ARG, "solve: bad sizes or pointers");
-  if (form != IBEM_SOLVE_FP64 && form != IBEM_SOLVE_MIXED_IR) return fail(IBEM_ERR_ARG, "unknown solver form");
+  if (form != IBEM_SOLVE_FP64 && form != IBEM_SOLVE_MIXED_IR && form != IBEM_SOLVE_GMRES_BJ)
+    return fail(IBEM_ERR_ARG, "unknown solver form");
+  if (form == IBEM_SOLVE_GMRES_BJ && (block < 1 || block > kBjMax))
+    return fail(IBEM_ERR_ARG, "block-Jacobi form: block size must be 1.." + std::to_string(kBjMax));
   SolveCtx cx;
   ibem_status s = cx.alloc(N, st);
   if (s) return s;
@@ -1346,7 +1593,10 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
   cudaEventRecord(e0, st);
   double as_norm = 0;
   auto finish_norm = [&]() -> ibem_status {
-    ::ibem::count_launch(), k_scaled_rowsum<<<nb, 256, 0, st>>>(N, A, lda, cx.r, cx.c, cx.rs);
+    const int64_t chunk = (N + cx.nparts - 1) / cx.nparts;
+    ::ibem::count_launch(), k_abs_rowsum_part<<<dim3(nb, (unsigned)cx.nparts), 256, 0, st>>>(N, A, lda, cx.c, chunk,
+                                                                                              cx.part);
+    ::ibem::count_launch(), k_scale_rows_of_parts<<<nb, 256, 0, st>>>(N, cx.nparts, cx.part, cx.r, cx.rs);
     IBEM_LAUNCH_CHECK("scaled_rowsum");
     std::vector<double> h;
     ibem_status q = vec_to_host(cx.rs, N, h, st);
@@ -1371,6 +1621,86 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
     if (!s) s = scaled_backward_error(cx, A, lda, ys, bs, rvec, tmp, as_norm, R.backward_error);
     lu_free(w);
     cudaFree(W);
+  } else if (form == IBEM_SOLVE_GMRES_BJ) {
+    // As32 = FP32 copy of the scaled matrix, P = FP32 inverses of its block x block diagonal
+    // blocks; refinement: FP64 residual rs = bs - As ys, GMRES with As32 products (FP64
+    // accumulation) right-preconditioned by P reduces it by kInner, ys += correction.
+    constexpr int m = 60, max_outer = 30;
+    constexpr double kInner = 1e-6;  // about what an FP32 operator can resolve
+    const int64_t nblk = (N + block - 1) / block;
+    float *W = nullptr, *P = nullptr;
+    double *V = nullptr, *Z = nullptr, *hd = nullptr;
+    int* info_dev = nullptr;
+    cudaError_t ce = cudaMalloc(&W, sizeof(float) * (size_t)N * N);
+    if (ce == cudaSuccess) ce = cudaMalloc(&P, sizeof(float) * (size_t)nblk * block * block);
+    if (ce == cudaSuccess) ce = cudaMalloc(&V, sizeof(double) * (size_t)N * (m + 1));
+    if (ce == cudaSuccess) ce = cudaMalloc(&Z, sizeof(double) * (size_t)N * m);
+    if (ce == cudaSuccess) ce = cudaMalloc(&hd, sizeof(double) * (m + 1) * 2);
+    if (ce == cudaSuccess) ce = cudaMalloc(&info_dev, sizeof(int));
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(info_dev, 0, sizeof(int), st);
+    if (ce != cudaSuccess) s = cuda_fail(ce, "block-Jacobi workspace");
+    if (!s) {
+      ProfScope ps(PROF_EQUIL, st);
+      s = equilibrate(cx, A, lda);
+      if (!s) {
+        dim3 g((unsigned)((N + 255) / 256), (unsigned)N);
+        ::ibem::count_launch(), k_scale_copy<float><<<g, 256, 0, st>>>(N, A, lda, cx.r, cx.c, W, N);
+        if (bj_smem(block) > 48 * 1024)
+          cudaFuncSetAttribute(k_bj_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bj_smem(block));
+        ::ibem::count_launch(), k_bj_invert<<<(unsigned)nblk, kBjThreads, bj_smem(block), st>>>(N, block, A, lda, cx.r,
+                                                                                               cx.c, P, info_dev);
+        ::ibem::count_launch(), k_vmul<<<nb, 256, 0, st>>>(N, cx.r, b, bs);
+        IBEM_LAUNCH_CHECK("block-Jacobi setup");
+      }
+    }
+    int hinfo = 0;
+    if (!s) {
+      ce = cudaMemcpyAsync(&hinfo, info_dev, sizeof(int), cudaMemcpyDeviceToHost, st);
+      if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+      if (ce != cudaSuccess) s = cuda_fail(ce, "block-Jacobi setup");
+      if (!s && hinfo) {
+        R.info = hinfo;
+        s = fail(IBEM_ERR_SINGULAR, "singular diagonal block in the block-Jacobi form");
+      }
+    }
+    cudaEventRecord(e1, st);
+    if (!s) s = finish_norm();
+    if (!s) IBEM_CUDA(cudaMemsetAsync(ys, 0, sizeof(double) * N, st));
+    const int64_t chunk = (N + cx.nparts - 1) / cx.nparts;
+    auto prec = [&](const double* v, double* z) -> ibem_status {
+      ::ibem::count_launch(), k_bj_apply<<<(unsigned)nblk, kBjApplyThreads, 0, st>>>(N, block, P, v, z);
+      IBEM_LAUNCH_CHECK("block-Jacobi apply");
+      return IBEM_OK;
+    };
+    auto op32 = [&](const double* z, double* wv) -> ibem_status {
+      ProfScope ps(PROF_MATVEC, st, 2.0 * N * N);
+      ::ibem::count_launch(), k_gemv_part_f32<<<dim3(nb, (unsigned)cx.nparts), 256, 0, st>>>(N, W, N, z, chunk,
+                                                                                              cx.part);
+      ::ibem::count_launch(), k_scale_rows_of_parts<<<nb, 256, 0, st>>>(N, cx.nparts, cx.part, nullptr, wv);
+      IBEM_LAUNCH_CHECK("FP32 product");
+      return IBEM_OK;
+    };
+    int iters = 0;
+    for (int outer = 0; !s && outer < max_outer; ++outer) {
+      double be = 0;
+      if ((s = scaled_backward_error(cx, A, lda, ys, bs, rvec, tmp, as_norm, be))) break;
+      R.backward_error = be;
+      if (be <= tol) break;
+      int steps = 0;
+      double est = 0, beta = 0;
+      s = gmres_cycle(N, m, rvec, V, Z, hd, ys, 0.0, kInner, prec, op32, steps, est, beta, st);
+      iters += steps;
+      if (s || beta == 0) break;
+    }
+    cudaEventRecord(e2, st);
+    if (!s && R.backward_error > tol) s = fail(IBEM_ERR_NOCONV, "block-Jacobi GMRES did not reach the tolerance");
+    R.iterations = iters;
+    cudaFree(W);
+    cudaFree(P);
+    cudaFree(V);
+    cudaFree(Z);
+    cudaFree(hd);
+    cudaFree(info_dev);
   } else {
     float* W = nullptr;
     LuWork<float> w;
@@ -1401,71 +1731,17 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
       R.backward_error = be;
       if (be <= tol) break;
       // rvec holds rs = bs - As ys
-      IBEM_CUDA(cudaMemsetAsync(hd, 0, sizeof(double), st));
-      ::ibem::count_launch(), k_dot_many<<<256, 256, 0, st>>>(N, 1, rvec, N, rvec, hd);
-      double b2 = 0;
-      IBEM_CUDA(cudaMemcpyAsync(&b2, hd, sizeof(double), cudaMemcpyDeviceToHost, st));
-      IBEM_CUDA(cudaStreamSynchronize(st));
-      const double beta = std::sqrt(std::max(b2, 0.0));
-      if (beta == 0) break;
-      ::ibem::count_launch(), k_axpby<<<nb, 256, 0, st>>>(N, 1.0 / beta, rvec, 0.0, V);
-      std::vector<double> H((m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0);
-      g[0] = beta;
-      int k = 0;
-      for (; k < m; ++k) {
-        double* vk = V + (size_t)k * N;
-        double* zk = Z + (size_t)k * N;
-        double* wv = V + (size_t)(k + 1) * N;
-        IBEM_CUDA(cudaMemcpyAsync(zk, vk, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
-        if ((s = lu_apply<float>(W, N, N, w, zk, st))) break;
-        if ((s = scaled_matvec(cx, A, lda, zk, tmp, wv))) break;
-        // classical Gram-Schmidt, twice
-        std::vector<double> hk(k + 1, 0.0), h2(k + 1);
-        for (int pass = 0; pass < 2; ++pass) {
-          IBEM_CUDA(cudaMemsetAsync(hd, 0, sizeof(double) * (k + 1), st));
-          ::ibem::count_launch(), k_dot_many<<<256, 256, 0, st>>>(N, k + 1, V, N, wv, hd);
-          ::ibem::count_launch(), k_sub_Vh<<<nb, 256, 0, st>>>(N, k + 1, V, N, hd, wv);
-          IBEM_CUDA(cudaMemcpyAsync(h2.data(), hd, sizeof(double) * (k + 1), cudaMemcpyDeviceToHost, st));
-          IBEM_CUDA(cudaStreamSynchronize(st));
-          for (int i = 0; i <= k; ++i) hk[i] += h2[i];
-        }
-        IBEM_CUDA(cudaMemsetAsync(hd, 0, sizeof(double), st));
-        ::ibem::count_launch(), k_dot_many<<<256, 256, 0, st>>>(N, 1, wv, N, wv, hd);
-        double nrm2 = 0;
-        IBEM_CUDA(cudaMemcpyAsync(&nrm2, hd, sizeof(double), cudaMemcpyDeviceToHost, st));
-        IBEM_CUDA(cudaStreamSynchronize(st));
-        const double hn = std::sqrt(std::max(nrm2, 0.0));
-        if (hn > 0) ::ibem::count_launch(), k_axpby<<<nb, 256, 0, st>>>(N, 1.0 / hn, wv, 0.0, wv);
-        for (int i = 0; i <= k; ++i) H[i * m + k] = hk[i];
-        H[(k + 1) * m + k] = hn;
-        for (int i = 0; i < k; ++i) {  // previous Givens rotations
-          const double t = cs[i] * H[i * m + k] + sn[i] * H[(i + 1) * m + k];
-          H[(i + 1) * m + k] = -sn[i] * H[i * m + k] + cs[i] * H[(i + 1) * m + k];
-          H[i * m + k] = t;
-        }
-        const double den = std::hypot(H[k * m + k], H[(k + 1) * m + k]);
-        cs[k] = den > 0 ? H[k * m + k] / den : 1.0;
-        sn[k] = den > 0 ? H[(k + 1) * m + k] / den : 0.0;
-        H[k * m + k] = den;
-        H[(k + 1) * m + k] = 0;
-        g[k + 1] = -sn[k] * g[k];
-        g[k] = cs[k] * g[k];
-        ++iters;
-        // stop the inner cycle once the scaled residual estimate is well below tol
-        if (std::fabs(g[k + 1]) <= 1e-2 * tol * (as_norm + 1.0) || hn == 0) { ++k; break; }
-      }
-      if (s) break;
-      std::vector<double> yv(k, 0.0);
-      for (int i = k - 1; i >= 0; --i) {
-        double t = g[i];
-        for (int j2 = i + 1; j2 < k; ++j2) t -= H[i * m + j2] * yv[j2];
-        yv[i] = t / H[i * m + i];
-      }
-      IBEM_CUDA(cudaMemcpyAsync(hd, yv.data(), sizeof(double) * k, cudaMemcpyHostToDevice, st));
-      ::ibem::count_launch(), k_axpby<<<nb, 256, 0, st>>>(N, -1.0, ys, 0.0, ys);  // ys = -ys
-      ::ibem::count_launch(), k_sub_Vh<<<nb, 256, 0, st>>>(N, k, Z, N, hd, ys);    // ys = -ys - Z y
-      ::ibem::count_launch(), k_axpby<<<nb, 256, 0, st>>>(N, -1.0, ys, 0.0, ys);  // ys = ys + Z y
-      IBEM_LAUNCH_CHECK("gmres update");
+      int steps = 0;
+      double est = 0, beta = 0;
+      s = gmres_cycle(
+          N, m, rvec, V, Z, hd, ys, 1e-2 * tol * (as_norm + 1.0), 0.0,
+          [&](const double* v, double* z) -> ibem_status {
+            IBEM_CUDA(cudaMemcpyAsync(z, v, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+            return lu_apply<float>(W, N, N, w, z, st);
+          },
+          [&](const double* z, double* wv) { return scaled_matvec(cx, A, lda, z, tmp, wv); }, steps, est, beta, st);
+      iters += steps;
+      if (s || beta == 0) break;
     }
     cudaEventRecord(e2, st);
     if (!s) s = sticky_err(w, st);

@@ -17,6 +17,11 @@
                spheres): time, Arnoldi and refinement steps, phase times.
 --batch R      the batched measurement of bench.py (R realisations of U[50, 500] spheres,
                learned preconditioner, untrained network) with per-phase times.
+--quad R       R quadratic-eigenstrain realisations (layout 60, the batched measurement's
+               distribution) through ibem_e3d_batch_dense_solve (--quad-form bj: block-Jacobi
+               GMRES form, mixed: FP32 LU + GMRES-IR), with phases.
+--assemble NUM,LAYOUT  the pair blocks (ibem_e3d_pair_blocks, FP64) of NUM spheres in
+               layout 24, 60 or 78: achieved write bandwidth of the N^2 matrix.
 --mf NUM       the matrix-free products (ibem_e3d_mf_matvec: FP32, double-float, FP64) on a
                far-field microstructure of NUM spheres (bench distribution): NUM^2 pair
                products per launch, timed by the library's phase events.
@@ -32,7 +37,7 @@ import json
 
 import torch
 
-from . import lib, check, prof_report, SolveReport, SOLVE_FP64, SOLVE_MIXED_IR
+from . import lib, check, prof_report, SolveReport, SOLVE_FP64, SOLVE_GMRES_BJ, SOLVE_MIXED_IR
 
 
 def _p(t):
@@ -98,6 +103,35 @@ def bench_lu(n, form, reps, dev):
             "backward_error": rep.backward_error, "iterations": rep.iterations,
             "phases_ms": {k: round(v["ms"] / reps, 3) for k, v in prof.items()},
             "phase_launches": {k: v["launches"] / reps for k, v in prof.items()}}
+
+
+def bench_assemble(num, layout, reps, dev):
+    """ibem_e3d_pair_blocks of a far-field microstructure (bench distribution): the
+    (layout num)^2 FP64 matrix written once per call; algorithmic bytes = its 8 N^2 bytes."""
+    import numpy as np
+    from . import cases, material
+    c = cases.farfield_case(num=num, r0=0.012, vf=0.15, grid=0, seed=2024)
+    n = layout * num
+    A = torch.empty(n * n, dtype=torch.float64, device=dev)
+    cen = torch.from_numpy(np.ascontiguousarray(c.centers)).to(dev)
+    rad = torch.from_numpy(np.ascontiguousarray(c.radius)).to(dev)
+    m = material(c.E0, c.nu0, c.E1, c.nu1)
+    st = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(st.cuda_stream)
+    L = lib()
+    run = lambda: check(L.ibem_e3d_pair_blocks(_p(cen), _p(rad), num, ctypes.byref(m), layout, _p(A), n, 0, 0, sp))
+    run()   # warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        run()
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    return {"kernel": f"pair{layout} + self{layout} (assembly)", "spheres": num, "N": n, "reps": reps, "ms": ms,
+            "matrix_GB": 8.0 * n * n / 1e9, "GB_per_s": 8.0 * n * n / (ms * 1e-3) / 1e9,
+            "ns_per_pair": ms * 1e6 / (num * num)}
 
 
 def bench_mf(num, reps, dev):
@@ -221,6 +255,42 @@ def bench_batch(nreal, reps, dev):
             "phase_launches": {k: v["launches"] / reps for k, v in prof.items()}}
 
 
+def bench_quad(nreal, reps, dev, form="bj"):
+    """Quadratic-eigenstrain realisations of the batched measurement's distribution (U[50,
+    500] spheres, vf U[10%, 30%], E1/E0 U[2, 20], layout 60) through
+    ibem_e3d_batch_dense_solve (mixed form), with the per-phase profile."""
+    import numpy as np
+    from . import batch as B
+    from . import cases
+    rng = np.random.default_rng(4243)
+    nums = rng.integers(50, 501, size=nreal)
+    vfs = rng.uniform(0.10, 0.30, size=nreal)
+    con = rng.uniform(2.0, 20.0, size=nreal)
+    cs = [cases.generated_case(int(n), 0.008, float(v), seed=7500 + k, E1=70e9 * float(c))
+          for k, (n, v, c) in enumerate(zip(nums, vfs, con))]
+    bt = B.DeviceBatch(cs, device=dev, layout=60)
+    b = B.farfield_rhs(bt, np.array([0, 0, 0, 0, 0, 1.0]))
+    f = SOLVE_GMRES_BJ if form == "bj" else SOLVE_MIXED_IR
+    B.dense_batch_solve(bt, b, f, tol=1e-12)   # warm-up
+    torch.cuda.synchronize()
+    L = lib()
+    L.ibem_prof_enable(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        x, rep = B.dense_batch_solve(bt, b, f, tol=1e-12)
+    e1.record()
+    torch.cuda.synchronize()
+    prof = prof_report()
+    L.ibem_prof_enable(0)
+    return {"kernel": "batched dense solves, layout 60", "form": form, "realisations": nreal, "spheres": int(nums.sum()),
+            "unknowns": int(60 * nums.sum()), "ms": e0.elapsed_time(e1) / reps,
+            "factor_ms_sum": sum(r.t_factor_ms for r in rep), "solve_ms_sum": sum(r.t_solve_ms for r in rep),
+            "gmres_iterations_max": max(r.iterations for r in rep),
+            "phases_ms": {k: round(v["ms"] / reps, 3) for k, v in prof.items()},
+            "phase_launches": {k: v["launches"] / reps for k, v in prof.items()}}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gemm", action="append", default=[], help="M,N,K")
@@ -230,6 +300,9 @@ def main(argv=None):
     ap.add_argument("--field", action="append", default=[], help="NUM,GRID")
     ap.add_argument("--solve", type=int, action="append", default=[])
     ap.add_argument("--batch", type=int, action="append", default=[])
+    ap.add_argument("--assemble", action="append", default=[], help="NUM,LAYOUT")
+    ap.add_argument("--quad", type=int, action="append", default=[])
+    ap.add_argument("--quad-form", default="bj", choices=["bj", "mixed"])
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--vf", type=float, default=0.15, help="volume fraction of --solve (above 0.15: Monte Carlo packing)")
     a = ap.parse_args(argv)
@@ -240,8 +313,13 @@ def main(argv=None):
         print(json.dumps(bench_gemm(m, n, k, a.reps, dev)), flush=True)
     for n in a.lu:
         print(json.dumps(bench_lu(n, a.form, a.reps, dev)), flush=True)
+    for f in a.assemble:
+        num, lay = (int(v) for v in f.split(","))
+        print(json.dumps(bench_assemble(num, lay, a.reps, dev)), flush=True)
     for n in a.mf:
         print(json.dumps(bench_mf(n, a.reps, dev)), flush=True)
+    for n in a.quad:
+        print(json.dumps(bench_quad(n, a.reps, dev, a.quad_form)), flush=True)
     for n in a.solve:
         print(json.dumps(bench_solve(n, a.reps, dev, a.vf)), flush=True)
     for n in a.batch:

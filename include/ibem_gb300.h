@@ -134,7 +134,9 @@ ibem_status ibem_e3d_farfield_rhs(int num, const ibem_material* mat, int layout,
 
 typedef enum {
   IBEM_SOLVE_FP64 = 0,     /* equilibrated partial-pivot LU in FP64 (plain path) */
-  IBEM_SOLVE_MIXED_IR = 1  /* FP32 LU, split-BF16 tensor-core updates, FP64 GMRES-IR */
+  IBEM_SOLVE_MIXED_IR = 1, /* FP32 LU, split-BF16 tensor-core updates, FP64 GMRES-IR */
+  IBEM_SOLVE_GMRES_BJ = 2  /* no factorisation: FP64 refinement of FP32-product GMRES,
+                            * block-Jacobi preconditioned (ibem_e3d_solve_bj) */
 } ibem_solver_form;
 
 typedef struct {
@@ -153,6 +155,18 @@ typedef struct {
 ibem_status ibem_e3d_solve(ibem_solver_form form, int64_t N, double* A_dev, int64_t lda,
                            const double* b_dev, double* x_dev, double tol,
                            ibem_solve_report* report, void* stream);
+
+/* The block-Jacobi form (IBEM_SOLVE_GMRES_BJ), another form of systemSolverElastic3D::solve
+ * for the small far-field systems whose LU is bound by launch latency: A is equilibrated
+ * (As = R A C) and copied to FP32, the block x block diagonal blocks of As (block = unknowns
+ * per particle, 1..80) are inverted in FP64 and kept in FP32, and iterative refinement runs
+ * FP64 residuals bs - As ys, each followed by a GMRES(60) correction with the FP32 copy
+ * (products accumulated in FP64), right-preconditioned by the block inverses, until the
+ * scaled backward error (as in ibem_solve_report) is <= tol.  A_dev is left intact.
+ * report->iterations counts the Arnoldi steps.  Synchronous. */
+ibem_status ibem_e3d_solve_bj(int64_t N, int block, const double* A_dev, int64_t lda,
+                              const double* b_dev, double* x_dev, double tol,
+                              ibem_solve_report* report, void* stream);
 
 /* The trailing-update primitive of the mixed-precision factorisation, exposed for
  * testing and reuse: C (m x n) -= A (m x k) B (k x n), FP32 column-major storage,
@@ -257,7 +271,8 @@ ibem_status ibem_e3d_batch_farfield_rhs_layout(const ibem_e3d_batch* batch, int 
  * layouts the matrix-free products do not cover (quadratic eigenstrain, layouts 60 and 78):
  * per realisation its pair blocks (ibem_e3d_pair_blocks) into one N x N matrix sized for
  * the largest realisation and allocated once, then ibem_e3d_solve(form, tol) (the mixed
- * form: FP32 LU with split-BF16 tensor-core updates, FP64 GMRES-IR).  b_dev, x_dev: layout *
+ * form: FP32 LU with split-BF16 tensor-core updates, FP64 GMRES-IR; IBEM_SOLVE_GMRES_BJ:
+ * ibem_e3d_solve_bj with one block per particle).  b_dev, x_dev: layout *
  * seg_begin[nseg] doubles.  reports: host array of nseg (may be NULL).  Synchronous.
  * The reference solves one microstructure per run (systemSolverElastic3D.h:44-60). */
 ibem_status ibem_e3d_batch_dense_solve(const ibem_e3d_batch* batch, int layout,

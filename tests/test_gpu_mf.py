@@ -300,15 +300,17 @@ def test_quadratic_batch_dense_mixed_matches_fp64(B):
     sig = np.array([0.2, 0.0, 0.1, -0.3, 0.0, 1.0])
     b = B.farfield_rhs(bt, sig)
     assert b.numel() == 60 * sum(nums)
-    x, reps = B.dense_batch_solve(bt, b, g.SOLVE_MIXED_IR, tol=1e-12)
-    xh = x.cpu().numpy()
-    for s, c in enumerate(cs):
-        rows = bt.seg_rows(s)
-        xr = B.dense_solve(c, b[rows], layout=60).cpu().numpy().reshape(-1, 60)
-        xs = xh[rows].reshape(-1, 60)
-        for lo, hi in ((0, 6), (6, 24), (24, 60)):
-            assert scaled_err(xs[:, lo:hi], xr[:, lo:hi]) < 1e-8, (s, lo)
-        assert reps[s].backward_error <= 1e-12, s
+    refs = [B.dense_solve(c, b[bt.seg_rows(s)], layout=60).cpu().numpy().reshape(-1, 60) for s, c in enumerate(cs)]
+    for form in (g.SOLVE_GMRES_BJ, g.SOLVE_MIXED_IR):   # the mixed form's x is kept for the checks below
+        x, reps = B.dense_batch_solve(bt, b, form, tol=1e-12)
+        xh = x.cpu().numpy()
+        for s, c in enumerate(cs):
+            xs = xh[bt.seg_rows(s)].reshape(-1, 60)
+            for lo, hi in ((0, 6), (6, 24), (24, 60)):
+                assert scaled_err(xs[:, lo:hi], refs[s][:, lo:hi]) < 1e-8, (form, s, lo)
+            assert reps[s].backward_error <= 1e-12, (form, s)
+            if form == g.SOLVE_GMRES_BJ:
+                assert reps[s].iterations > 0
     # effective modulus: numpy restatement of the sphere average
     vol = bt.volumes()
     Eeff, eps = B.effective_modulus(bt, x, sig, volume=vol)
@@ -328,3 +330,35 @@ def test_quadratic_batch_dense_mixed_matches_fp64(B):
     x1, _ = B.solve(b1, B.farfield_rhs(b1, sig), B.PRECOND_BLOCK_JACOBI, tol=1e-12)
     E1, _ = B.effective_modulus(b1, x1, sig, volume=vol[:1])
     assert abs(E1[0] - Eeff[0]) <= 1e-9 * abs(E1[0])
+
+
+def test_block_jacobi_form_ragged_blocks_and_arguments(B):
+    """ibem_e3d_solve_bj with a block size that does not divide N (ragged last block) on a
+    linear far-field system, against the plain FP64 LU; A is left intact; the form is refused
+    by ibem_e3d_solve and block sizes outside 1..80 are refused."""
+    import ctypes
+
+    import torch
+
+    import ibemproject_gb300 as g
+    c = small_cases([7], seed=91)[0]
+    A = B.dense_system(c)
+    A0 = A.clone()
+    n = A.shape[0]
+    bt = B.DeviceBatch([c])
+    b = B.farfield_rhs(bt, np.array([0.1, 0.0, 0.0, 0.2, 0.0, 1.0]))
+    xr = B.dense_solve(c, b).cpu().numpy()
+    L = g.lib()
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    for block in (50, 24, 6):
+        x = torch.zeros(n, dtype=torch.float64, device=b.device)
+        rep = g.SolveReport()
+        g.check(L.ibem_e3d_solve_bj(n, block, P(A), n, P(b), P(x), 1e-12, ctypes.byref(rep), None))
+        assert scaled_err(x.cpu().numpy(), xr) < 1e-9, block
+        assert rep.backward_error <= 1e-12 and rep.iterations > 0
+    assert torch.equal(A, A0)
+    x = torch.zeros(n, dtype=torch.float64, device=b.device)
+    rep = g.SolveReport()
+    assert L.ibem_e3d_solve(g.SOLVE_GMRES_BJ, n, P(A), n, P(b), P(x), 1e-12, ctypes.byref(rep), None) == 1
+    for block in (0, 81):
+        assert L.ibem_e3d_solve_bj(n, block, P(A), n, P(b), P(x), 1e-12, ctypes.byref(rep), None) == 1
