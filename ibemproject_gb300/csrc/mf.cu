@@ -33,6 +33,7 @@
 #include "dfnum.cuh"
 #include "mf_contract.cuh"
 #include "prof.h"
+#include "solver.h"
 
 namespace ibem {
 namespace {
@@ -1226,11 +1227,17 @@ extern "C" ibem_status ibem_e3d_batch_dense_solve(const ibem_e3d_batch* batch, i
     if (n < 0) return fail(IBEM_ERR_ARG, "batch_dense_solve: seg_begin must not decrease");
     nmax = std::max<int64_t>(nmax, (int64_t)nu * n);
   }
+  if (form != IBEM_SOLVE_FP64 && form != IBEM_SOLVE_MIXED_IR && form != IBEM_SOLVE_GMRES_BJ)
+    return fail(IBEM_ERR_ARG, "batch_dense_solve: unknown solver form");
   cudaStream_t st = as_stream(stream);
-  double* A = nullptr;  // the largest realisation's N x N matrix, reused by every realisation
+  // the largest realisation's N x N matrix (and, for the block-Jacobi form, its FP32 copy),
+  // reused by every realisation
+  double* A = nullptr;
+  float* W = nullptr;
   ibem_status s = IBEM_OK;
   if (nmax) {
-    const cudaError_t e = alloc_async((void**)&A, sizeof(double) * nmax * nmax, st);
+    cudaError_t e = alloc_async((void**)&A, sizeof(double) * nmax * nmax, st);
+    if (e == cudaSuccess && form == IBEM_SOLVE_GMRES_BJ) e = alloc_async((void**)&W, sizeof(float) * nmax * nmax, st);
     if (e != cudaSuccess) s = cuda_fail(e, "batch_dense_solve: matrix");
   }
   for (int i = 0; i < batch->nseg && !s; ++i) {
@@ -1240,13 +1247,12 @@ extern "C" ibem_status ibem_e3d_batch_dense_solve(const ibem_e3d_batch* batch, i
     if (n) {
       s = ibem_e3d_pair_blocks(batch->centers_dev + 3 * (int64_t)p0, batch->radius_dev + p0, n, &batch->mats[i], layout,
                                A, N, 0, 0, st);
-      if (!s)
-        s = form == IBEM_SOLVE_GMRES_BJ ? ibem_e3d_solve_bj(N, nu, A, N, b_dev + off, x_dev + off, tol, &rep, st)
-                                        : ibem_e3d_solve(form, N, A, N, b_dev + off, x_dev + off, tol, &rep, st);
+      if (!s) s = solve_dense(form, N, A, N, b_dev + off, x_dev + off, tol, &rep, st, nu, W);
     }
     if (reports) reports[i] = rep;
   }
   free_async(A, st);
+  free_async(W, st);
   return s;
 }
 

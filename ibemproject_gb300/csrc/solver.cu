@@ -30,9 +30,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "ibem_internal.h"
@@ -696,6 +698,94 @@ __global__ void k_residual(int64_t n, int nparts, const double* __restrict__ par
   r[i] = b[i] - s;
 }
 
+// partial row sums of |A_ij| c_j over a column chunk (finished by k_scale_rows_of_parts)
+__global__ void k_abs_rowsum_part(int64_t n, const double* __restrict__ A, int64_t lda, const double* __restrict__ c,
+                                  int64_t chunk, double* __restrict__ part) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+  if (i >= n) return;
+  double s = 0;
+  for (int64_t j = j0; j < j1; ++j) s += fabs(A[j * lda + i]) * c[j];
+  part[blockIdx.y * n + i] = s;
+}
+// Partial products of the FP32 scaled matrix with an FP64 vector over a column chunk,
+// accumulated in FP64 (finished by k_scale_rows_of_parts with r = nullptr).
+__global__ void k_gemv_part_f32(int64_t n, const float* __restrict__ W, int64_t ldw, const double* __restrict__ x,
+                                int64_t chunk, double* __restrict__ part) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+  if (i >= n) return;
+  double s0 = 0, s1 = 0;
+  int64_t j = j0;
+  for (; j + 1 < j1; j += 2) {
+    s0 += (double)W[j * ldw + i] * x[j];
+    s1 += (double)W[(j + 1) * ldw + i] * x[j + 1];
+  }
+  if (j < j1) s0 += (double)W[j * ldw + i] * x[j];
+  part[blockIdx.y * n + i] = s0 + s1;
+}
+
+// Column-chunk reductions over a column-major matrix with 16-byte loads: thread t covers the
+// kV = 16 / sizeof(T) consecutive rows kV t .. kV t + kV - 1, eight columns per iteration,
+// FP64 accumulation; grid.y = chunk.  MODE 0: part = sum_j A_ij x_j; 1: part = max_j |A_ij|
+// (x unused); 2: part = sum_j |A_ij| x_j.  The caller checks that A is 16-byte aligned and
+// lda a multiple of kV; rows past a partial last vector are read one by one.
+template <typename T>
+__device__ __forceinline__ double vget(const float4& a, int v) {
+  return v == 0 ? a.x : v == 1 ? a.y : v == 2 ? a.z : a.w;
+}
+template <typename T>
+__device__ __forceinline__ double vget(const double2& a, int v) {
+  return v == 0 ? a.x : a.y;
+}
+template <int MODE>
+__device__ __forceinline__ void vacc(double& s, double a, double x) {
+  if (MODE == 0) s += a * x;
+  else if (MODE == 1) s = fmax(s, fabs(a));
+  else s += fabs(a) * x;
+}
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256) k_colreduce_v(int64_t n, const T* __restrict__ A, int64_t lda,
+                                                     const double* __restrict__ x, int64_t chunk,
+                                                     double* __restrict__ part) {
+  constexpr int kV = 16 / sizeof(T);
+  using VT = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  const int64_t i0 = kV * (blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+  if (i0 >= n) return;
+  const int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+  double s[kV];
+#pragma unroll
+  for (int v = 0; v < kV; ++v) s[v] = 0.0;
+  if (i0 + kV <= n) {
+    int64_t j = j0;
+    for (; j + 7 < j1; j += 8) {
+      VT a[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) a[u] = *reinterpret_cast<const VT*>(A + (j + u) * lda + i0);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const double xv = MODE == 1 ? 0.0 : x[j + u];
+#pragma unroll
+        for (int v = 0; v < kV; ++v) vacc<MODE>(s[v], vget<T>(a[u], v), xv);
+      }
+    }
+    for (; j < j1; ++j) {
+      const VT a = *reinterpret_cast<const VT*>(A + j * lda + i0);
+      const double xv = MODE == 1 ? 0.0 : x[j];
+#pragma unroll
+      for (int v = 0; v < kV; ++v) vacc<MODE>(s[v], vget<T>(a, v), xv);
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < kV; ++v)
+      if (i0 + v < n)
+        for (int64_t j = j0; j < j1; ++j) vacc<MODE>(s[v], (double)A[j * lda + i0 + v], MODE == 1 ? 0.0 : x[j]);
+  }
+#pragma unroll
+  for (int v = 0; v < kV; ++v)
+    if (i0 + v < n) part[blockIdx.y * n + i0 + v] = s[v];
+}
+
 // ---------------------------------------------------------------- triangular solves
 // Substitution with the factors in precision T (vectors FP64), blocks of kTrsvB rows.
 // After the factorisation, k_trsv_inv writes the inverse of every diagonal block of L
@@ -1175,11 +1265,36 @@ static ibem_status sticky_err(const LuWork<T>& w, cudaStream_t st) {
 }
 
 // r = b - A x  (FP64)
+// part (nparts x N) = column-chunk reductions of A (MODE as k_colreduce_v) with 16-byte
+// loads when A and lda allow them, else one element per load (dot products only).
+template <int MODE, typename T>
+static ibem_status colreduce(int64_t N, const T* A, int64_t lda, const double* x, int nparts, double* part,
+                             cudaStream_t st) {
+  constexpr int kV = 16 / sizeof(T);
+  const int64_t chunk = (N + nparts - 1) / nparts;
+  if (reinterpret_cast<uintptr_t>(A) % 16 == 0 && lda % kV == 0) {
+    const int64_t rows = (N + kV - 1) / kV;
+    ::ibem::count_launch(), k_colreduce_v<T, MODE><<<dim3((unsigned)((rows + 255) / 256), (unsigned)nparts), 256, 0,
+                                                    st>>>(N, A, lda, x, chunk, part);
+  } else {
+    static_assert(MODE == 0 || sizeof(T) == 8, "unaligned FP32 reductions are dot products only");
+    const dim3 grid((unsigned)((N + 255) / 256), (unsigned)nparts);
+    if constexpr (sizeof(T) == 4)
+      ::ibem::count_launch(), k_gemv_part_f32<<<grid, 256, 0, st>>>(N, A, lda, x, chunk, part);
+    else if constexpr (MODE == 0)
+      ::ibem::count_launch(), k_gemv_part<<<grid, 256, 0, st>>>(N, A, lda, x, chunk, part);
+    else if constexpr (MODE == 1)
+      ::ibem::count_launch(), k_rowmax_part<<<grid, 256, 0, st>>>(N, A, lda, chunk, part);
+    else
+      ::ibem::count_launch(), k_abs_rowsum_part<<<grid, 256, 0, st>>>(N, A, lda, x, chunk, part);
+  }
+  IBEM_LAUNCH_CHECK("column reduction");
+  return IBEM_OK;
+}
+
 static ibem_status residual(int64_t N, const double* A, int64_t lda, const double* x, const double* b, double* r,
                             double* part, int nparts, cudaStream_t st) {
-  const int64_t chunk = (N + nparts - 1) / nparts;
-  dim3 grid((unsigned)((N + 255) / 256), (unsigned)nparts);
-  ::ibem::count_launch(), k_gemv_part<<<grid, 256, 0, st>>>(N, A, lda, x, chunk, part);
+  if (ibem_status q = colreduce<0>(N, A, lda, x, nparts, part, st)) return q;
   ::ibem::count_launch(), k_residual<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, nparts, part, b, r);
   IBEM_LAUNCH_CHECK("residual");
   return IBEM_OK;
@@ -1188,21 +1303,35 @@ static ibem_status residual(int64_t N, const double* A, int64_t lda, const doubl
 
 // ------------------------------------------------------------------ device vectors
 namespace {
-__global__ void k_dot_many(int64_t n, int nv, const double* __restrict__ V, int64_t ldv, const double* __restrict__ w,
-                           double* __restrict__ out) {
-  // out[j] += sum_i V[i,j] w[i]  (grid-stride over rows, one atomic per block and vector)
-  __shared__ double red[256];
-  for (int j = 0; j < nv; ++j) {
-    double s = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-      s += V[j * ldv + i] * w[i];
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int t = blockDim.x / 2; t > 0; t >>= 1) {
-      if (threadIdx.x < t) red[threadIdx.x] += red[threadIdx.x + t];
-      __syncthreads();
+__global__ void __launch_bounds__(256) k_dot_many(int64_t n, int nv, const double* __restrict__ V, int64_t ldv,
+                                                  const double* __restrict__ w, double* __restrict__ out) {
+  // out[j] += sum_i V[i,j] w[i]: grid-stride over rows, eight vectors per pass accumulated
+  // in registers, warp shuffles, one shared-memory step and one atomic per block and vector
+  __shared__ double red[8][8];  // [warp][vector]; 256 threads
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int j0 = 0; j0 < nv; j0 += 8) {
+    const int nj = min(8, nv - j0);
+    double s[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s[u] = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+      const double wi = w[i];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (u < nj) s[u] += V[(j0 + u) * ldv + i] * wi;
     }
-    if (threadIdx.x == 0) atomicAdd(out + j, red[0]);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      double v = s[u];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp][u] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < nj) {
+      double t = 0;
+      for (int q = 0; q < 8; ++q) t += red[q][threadIdx.x];
+      atomicAdd(out + j0 + threadIdx.x, t);
+    }
     __syncthreads();
   }
 }
@@ -1266,16 +1395,6 @@ __global__ void k_scaled_rowsum(int64_t n, const double* __restrict__ A, int64_t
   for (int64_t j = 0; j < n; ++j) s += fabs(A[j * lda + i]) * c[j];
   rs[i] = s * r[i];
 }
-// partial row sums of |A_ij| c_j over a column chunk (finished by k_scale_rows_of_parts)
-__global__ void k_abs_rowsum_part(int64_t n, const double* __restrict__ A, int64_t lda, const double* __restrict__ c,
-                                  int64_t chunk, double* __restrict__ part) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
-  if (i >= n) return;
-  double s = 0;
-  for (int64_t j = j0; j < j1; ++j) s += fabs(A[j * lda + i]) * c[j];
-  part[blockIdx.y * n + i] = s;
-}
 // y = r .* (A (c .* v)) via the partial-sum GEMV; tmp is an N-vector
 __global__ void k_scale_rows_of_parts(int64_t n, int nparts, const double* __restrict__ part,
                                       const double* __restrict__ r, double* __restrict__ y) {
@@ -1284,23 +1403,6 @@ __global__ void k_scale_rows_of_parts(int64_t n, int nparts, const double* __res
   double s = 0;
   for (int p = 0; p < nparts; ++p) s += part[p * n + i];
   y[i] = (r ? r[i] : 1.0) * s;
-}
-
-// Partial products of the FP32 scaled matrix with an FP64 vector over a column chunk,
-// accumulated in FP64 (finished by k_scale_rows_of_parts with r = nullptr).
-__global__ void k_gemv_part_f32(int64_t n, const float* __restrict__ W, int64_t ldw, const double* __restrict__ x,
-                                int64_t chunk, double* __restrict__ part) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
-  if (i >= n) return;
-  double s0 = 0, s1 = 0;
-  int64_t j = j0;
-  for (; j + 1 < j1; j += 2) {
-    s0 += (double)W[j * ldw + i] * x[j];
-    s1 += (double)W[(j + 1) * ldw + i] * x[j + 1];
-  }
-  if (j < j1) s0 += (double)W[j * ldw + i] * x[j];
-  part[blockIdx.y * n + i] = s0 + s1;
 }
 
 // Inverse of diagonal block blockIdx.x (rows and columns g0 .. g0 + nb - 1, g0 = block *
@@ -1410,8 +1512,7 @@ static ibem_status scaled_matvec(SolveCtx& cx, const double* A, int64_t lda, con
   ProfScope ps(PROF_MATVEC, cx.st, 2.0 * N * N);
   const unsigned nb = (unsigned)((N + 255) / 256);
   ::ibem::count_launch(), k_vmul<<<nb, 256, 0, cx.st>>>(N, cx.c, v, tmp);
-  const int64_t chunk = (N + cx.nparts - 1) / cx.nparts;
-  ::ibem::count_launch(), k_gemv_part<<<dim3(nb, (unsigned)cx.nparts), 256, 0, cx.st>>>(N, A, lda, tmp, chunk, cx.part);
+  if (ibem_status q = colreduce<0>(N, A, lda, tmp, cx.nparts, cx.part, cx.st)) return q;
   ::ibem::count_launch(), k_scale_rows_of_parts<<<nb, 256, 0, cx.st>>>(N, cx.nparts, cx.part, cx.r, y);
   IBEM_LAUNCH_CHECK("scaled_matvec");
   return IBEM_OK;
@@ -1435,8 +1536,7 @@ static ibem_status scaled_backward_error(SolveCtx& cx, const double* A, int64_t 
 static ibem_status equilibrate(SolveCtx& cx, const double* A, int64_t lda) {
   const int64_t N = cx.N;
   const unsigned nb = (unsigned)((N + 255) / 256);
-  const int64_t chunk = (N + cx.nparts - 1) / cx.nparts;
-  ::ibem::count_launch(), k_rowmax_part<<<dim3(nb, (unsigned)cx.nparts), 256, 0, cx.st>>>(N, A, lda, chunk, cx.part);
+  if (ibem_status q = colreduce<1>(N, A, lda, (const double*)nullptr, cx.nparts, cx.part, cx.st)) return q;
   ::ibem::count_launch(), k_rowmax_fin<<<nb, 256, 0, cx.st>>>(N, cx.nparts, cx.part, cx.r);
   ::ibem::count_launch(), k_colmax<<<(unsigned)N, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c);
   IBEM_LAUNCH_CHECK("equilibrate");
@@ -1567,7 +1667,7 @@ static ibem_status gmres_cycle(int64_t N, int m, const double* rvec, double* V, 
 }
 
 ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda, const double* b, double* x,
-                        double tol, ibem_solve_report* rep, cudaStream_t st, int block) {
+                        double tol, ibem_solve_report* rep, cudaStream_t st, int block, float* ws32) {
   if (N <= 0 || !A || !b || !x || lda < N) return fail(IBEM_ERR_ARG, "solve: bad sizes or pointers");
   if (form != IBEM_SOLVE_FP64 && form != IBEM_SOLVE_MIXED_IR && form != IBEM_SOLVE_GMRES_BJ)
     return fail(IBEM_ERR_ARG, "unknown solver form");
@@ -1593,9 +1693,7 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
   cudaEventRecord(e0, st);
   double as_norm = 0;
   auto finish_norm = [&]() -> ibem_status {
-    const int64_t chunk = (N + cx.nparts - 1) / cx.nparts;
-    ::ibem::count_launch(), k_abs_rowsum_part<<<dim3(nb, (unsigned)cx.nparts), 256, 0, st>>>(N, A, lda, cx.c, chunk,
-                                                                                              cx.part);
+    if (ibem_status q = colreduce<2>(N, (const double*)A, lda, cx.c, cx.nparts, cx.part, st)) return q;
     ::ibem::count_launch(), k_scale_rows_of_parts<<<nb, 256, 0, st>>>(N, cx.nparts, cx.part, cx.r, cx.rs);
     IBEM_LAUNCH_CHECK("scaled_rowsum");
     std::vector<double> h;
@@ -1631,7 +1729,9 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
     float *W = nullptr, *P = nullptr;
     double *V = nullptr, *Z = nullptr, *hd = nullptr;
     int* info_dev = nullptr;
-    cudaError_t ce = cudaMalloc(&W, sizeof(float) * (size_t)N * N);
+    cudaError_t ce = ws32 ? cudaSuccess : cudaMalloc(&W, sizeof(float) * (size_t)N * N);
+    float* const Wown = W;
+    if (ws32) W = ws32;
     if (ce == cudaSuccess) ce = cudaMalloc(&P, sizeof(float) * (size_t)nblk * block * block);
     if (ce == cudaSuccess) ce = cudaMalloc(&V, sizeof(double) * (size_t)N * (m + 1));
     if (ce == cudaSuccess) ce = cudaMalloc(&Z, sizeof(double) * (size_t)N * m);
@@ -1666,7 +1766,6 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
     cudaEventRecord(e1, st);
     if (!s) s = finish_norm();
     if (!s) IBEM_CUDA(cudaMemsetAsync(ys, 0, sizeof(double) * N, st));
-    const int64_t chunk = (N + cx.nparts - 1) / cx.nparts;
     auto prec = [&](const double* v, double* z) -> ibem_status {
       ::ibem::count_launch(), k_bj_apply<<<(unsigned)nblk, kBjApplyThreads, 0, st>>>(N, block, P, v, z);
       IBEM_LAUNCH_CHECK("block-Jacobi apply");
@@ -1674,8 +1773,7 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
     };
     auto op32 = [&](const double* z, double* wv) -> ibem_status {
       ProfScope ps(PROF_MATVEC, st, 2.0 * N * N);
-      ::ibem::count_launch(), k_gemv_part_f32<<<dim3(nb, (unsigned)cx.nparts), 256, 0, st>>>(N, W, N, z, chunk,
-                                                                                              cx.part);
+      if (ibem_status q = colreduce<0>(N, (const float*)W, N, z, cx.nparts, cx.part, st)) return q;
       ::ibem::count_launch(), k_scale_rows_of_parts<<<nb, 256, 0, st>>>(N, cx.nparts, cx.part, nullptr, wv);
       IBEM_LAUNCH_CHECK("FP32 product");
       return IBEM_OK;
@@ -1695,7 +1793,7 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
     cudaEventRecord(e2, st);
     if (!s && R.backward_error > tol) s = fail(IBEM_ERR_NOCONV, "block-Jacobi GMRES did not reach the tolerance");
     R.iterations = iters;
-    cudaFree(W);
+    cudaFree(Wown);
     cudaFree(P);
     cudaFree(V);
     cudaFree(Z);

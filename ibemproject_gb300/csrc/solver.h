@@ -17,9 +17,11 @@ ibem_status gemm_sub_f32_tc(int64_t m, int64_t n, int64_t k, const float* A, int
                             cudaStream_t st);
 size_t gemm_tc_workspace_bytes(int64_t max_m, int64_t max_n);
 
-// block: diagonal block size of the IBEM_SOLVE_GMRES_BJ form (1..64; unknowns per particle)
+// block: diagonal block size of the IBEM_SOLVE_GMRES_BJ form (1..80; unknowns per particle);
+// ws32: optional N x N FP32 workspace of that form (allocated and freed inside when null).
 ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda, const double* b, double* x,
-                        double tol, ibem_solve_report* rep, cudaStream_t st, int block = 0);
+                        double tol, ibem_solve_report* rep, cudaStream_t st, int block = 0,
+                        float* ws32 = nullptr);
 
 // Allocation-free FP64 solve for N <= 1024 (workspace in a static device array).
 ibem_status solve_fp64_noalloc(int64_t N, const double* A, int64_t lda, const double* b, double* x,
