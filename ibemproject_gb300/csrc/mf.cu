@@ -1237,7 +1237,8 @@ extern "C" ibem_status ibem_e3d_batch_dense_solve(const ibem_e3d_batch* batch, i
   ibem_status s = IBEM_OK;
   if (nmax) {
     cudaError_t e = alloc_async((void**)&A, sizeof(double) * nmax * nmax, st);
-    if (e == cudaSuccess && form == IBEM_SOLVE_GMRES_BJ) e = alloc_async((void**)&W, sizeof(float) * nmax * nmax, st);
+    if (e == cudaSuccess && form == IBEM_SOLVE_GMRES_BJ)
+      e = alloc_async((void**)&W, sizeof(float) * ((nmax + 3) / 4 * 4) * nmax, st);
     if (e != cudaSuccess) s = cuda_fail(e, "batch_dense_solve: matrix");
   }
   for (int i = 0; i < batch->nseg && !s; ++i) {

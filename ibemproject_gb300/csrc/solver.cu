@@ -740,9 +740,14 @@ __device__ __forceinline__ double vget(const double2& a, int v) {
 }
 template <int MODE>
 __device__ __forceinline__ void vacc(double& s, double a, double x) {
-  if (MODE == 0) s += a * x;
-  else if (MODE == 1) s = fmax(s, fabs(a));
-  else s += fabs(a) * x;
+  if (MODE == 0) {
+    s += a * x;
+  } else if (MODE == 1) {  // max |a| on the bit patterns: integer instructions, not the FP64 pipe
+    const long long m = max(__double_as_longlong(s), __double_as_longlong(a) & 0x7fffffffffffffffLL);
+    s = __longlong_as_double(m);
+  } else {
+    s += fabs(a) * x;
+  }
 }
 template <typename T, int MODE>
 __global__ void __launch_bounds__(256) k_colreduce_v(int64_t n, const T* __restrict__ A, int64_t lda,
@@ -1405,6 +1410,52 @@ __global__ void k_scale_rows_of_parts(int64_t n, int nparts, const double* __res
   y[i] = (r ? r[i] : 1.0) * s;
 }
 
+// y-parts of the FP32 scaled matrix times an FP32 vector: float4 loads of four rows, eight
+// columns per iteration summed in FP32, those partial sums added in FP64 (GB300 runs FP64 at
+// a small fraction of its FP32 rate, so FP64 multiply-adds would bound this product).
+// Requires ldw % 4 == 0 and W 16-byte aligned.
+__global__ void __launch_bounds__(256) k_gemv_f32acc(int64_t n, const float* __restrict__ W, int64_t ldw,
+                                                     const float* __restrict__ x, int64_t chunk,
+                                                     double* __restrict__ part) {
+  const int64_t i0 = 4 * (blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+  if (i0 >= n) return;
+  const int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  int64_t j = j0;
+  for (; j + 7 < j1; j += 8) {
+    float4 a[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) a[u] = *reinterpret_cast<const float4*>(W + (j + u) * ldw + i0);
+    float t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const float xv = x[j + u];
+      t0 = fmaf(a[u].x, xv, t0);
+      t1 = fmaf(a[u].y, xv, t1);
+      t2 = fmaf(a[u].z, xv, t2);
+      t3 = fmaf(a[u].w, xv, t3);
+    }
+    s[0] += t0, s[1] += t1, s[2] += t2, s[3] += t3;
+  }
+  float t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f;
+  for (; j < j1; ++j) {
+    const float4 a = *reinterpret_cast<const float4*>(W + j * ldw + i0);
+    const float xv = x[j];
+    t0 = fmaf(a.x, xv, t0);
+    t1 = fmaf(a.y, xv, t1);
+    t2 = fmaf(a.z, xv, t2);
+    t3 = fmaf(a.w, xv, t3);
+  }
+  s[0] += t0, s[1] += t1, s[2] += t2, s[3] += t3;
+#pragma unroll
+  for (int v = 0; v < 4; ++v)
+    if (i0 + v < n) part[blockIdx.y * n + i0 + v] = s[v];
+}
+__global__ void k_d2f(int64_t n, const double* __restrict__ x, float* __restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = (float)x[i];
+}
+
 // Inverse of diagonal block blockIdx.x (rows and columns g0 .. g0 + nb - 1, g0 = block *
 // blockIdx.x, nb = min(block, n - g0)) of As = R A C: Gauss-Jordan elimination in place with
 // partial pivoting, FP64 in dynamic shared memory (block x (block + 1) doubles, block <=
@@ -1726,13 +1777,15 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
     constexpr int m = 60, max_outer = 30;
     constexpr double kInner = 1e-6;  // about what an FP32 operator can resolve
     const int64_t nblk = (N + block - 1) / block;
-    float *W = nullptr, *P = nullptr;
+    const int64_t ldw = (N + 3) / 4 * 4;   // float4 columns
+    float *W = nullptr, *P = nullptr, *zf = nullptr;
     double *V = nullptr, *Z = nullptr, *hd = nullptr;
     int* info_dev = nullptr;
-    cudaError_t ce = ws32 ? cudaSuccess : cudaMalloc(&W, sizeof(float) * (size_t)N * N);
+    cudaError_t ce = ws32 ? cudaSuccess : cudaMalloc(&W, sizeof(float) * (size_t)ldw * N);
     float* const Wown = W;
     if (ws32) W = ws32;
     if (ce == cudaSuccess) ce = cudaMalloc(&P, sizeof(float) * (size_t)nblk * block * block);
+    if (ce == cudaSuccess) ce = cudaMalloc(&zf, sizeof(float) * (size_t)N);
     if (ce == cudaSuccess) ce = cudaMalloc(&V, sizeof(double) * (size_t)N * (m + 1));
     if (ce == cudaSuccess) ce = cudaMalloc(&Z, sizeof(double) * (size_t)N * m);
     if (ce == cudaSuccess) ce = cudaMalloc(&hd, sizeof(double) * (m + 1) * 2);
@@ -1744,7 +1797,7 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
       s = equilibrate(cx, A, lda);
       if (!s) {
         dim3 g((unsigned)((N + 255) / 256), (unsigned)N);
-        ::ibem::count_launch(), k_scale_copy<float><<<g, 256, 0, st>>>(N, A, lda, cx.r, cx.c, W, N);
+        ::ibem::count_launch(), k_scale_copy<float><<<g, 256, 0, st>>>(N, A, lda, cx.r, cx.c, W, ldw);
         if (bj_smem(block) > 48 * 1024)
           cudaFuncSetAttribute(k_bj_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bj_smem(block));
         ::ibem::count_launch(), k_bj_invert<<<(unsigned)nblk, kBjThreads, bj_smem(block), st>>>(N, block, A, lda, cx.r,
@@ -1773,7 +1826,10 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
     };
     auto op32 = [&](const double* z, double* wv) -> ibem_status {
       ProfScope ps(PROF_MATVEC, st, 2.0 * N * N);
-      if (ibem_status q = colreduce<0>(N, (const float*)W, N, z, cx.nparts, cx.part, st)) return q;
+      const int64_t chunk = (N + cx.nparts - 1) / cx.nparts;
+      ::ibem::count_launch(), k_d2f<<<nb, 256, 0, st>>>(N, z, zf);
+      ::ibem::count_launch(), k_gemv_f32acc<<<dim3((unsigned)((N + 1023) / 1024), (unsigned)cx.nparts), 256, 0, st>>>(
+          N, W, ldw, zf, chunk, cx.part);
       ::ibem::count_launch(), k_scale_rows_of_parts<<<nb, 256, 0, st>>>(N, cx.nparts, cx.part, nullptr, wv);
       IBEM_LAUNCH_CHECK("FP32 product");
       return IBEM_OK;
@@ -1795,6 +1851,7 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
     R.iterations = iters;
     cudaFree(Wown);
     cudaFree(P);
+    cudaFree(zf);
     cudaFree(V);
     cudaFree(Z);
     cudaFree(hd);

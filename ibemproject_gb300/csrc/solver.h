@@ -18,7 +18,8 @@ ibem_status gemm_sub_f32_tc(int64_t m, int64_t n, int64_t k, const float* A, int
 size_t gemm_tc_workspace_bytes(int64_t max_m, int64_t max_n);
 
 // block: diagonal block size of the IBEM_SOLVE_GMRES_BJ form (1..80; unknowns per particle);
-// ws32: optional N x N FP32 workspace of that form (allocated and freed inside when null).
+// ws32: optional FP32 workspace of that form, ((N + 3) / 4 * 4) x N floats (allocated and
+// freed inside when null).
 ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda, const double* b, double* x,
                         double tol, ibem_solve_report* rep, cudaStream_t st, int block = 0,
                         float* ws32 = nullptr);
