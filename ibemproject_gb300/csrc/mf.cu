@@ -20,12 +20,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <map>
 #include <mutex>
 #include <thread>
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "gen_sphere24.cuh"
@@ -1230,31 +1232,79 @@ extern "C" ibem_status ibem_e3d_batch_dense_solve(const ibem_e3d_batch* batch, i
   if (form != IBEM_SOLVE_FP64 && form != IBEM_SOLVE_MIXED_IR && form != IBEM_SOLVE_GMRES_BJ)
     return fail(IBEM_ERR_ARG, "batch_dense_solve: unknown solver form");
   cudaStream_t st = as_stream(stream);
-  // the largest realisation's N x N matrix (and, for the block-Jacobi form, its FP32 copy),
-  // reused by every realisation
-  double* A = nullptr;
-  float* W = nullptr;
-  ibem_status s = IBEM_OK;
-  if (nmax) {
-    cudaError_t e = alloc_async((void**)&A, sizeof(double) * nmax * nmax, st);
-    if (e == cudaSuccess && form == IBEM_SOLVE_GMRES_BJ)
-      e = alloc_async((void**)&W, sizeof(float) * ((nmax + 3) / 4 * 4) * nmax, st);
-    if (e != cudaSuccess) s = cuda_fail(e, "batch_dense_solve: matrix");
+  // Workers: each owns a stream, the largest realisation's N x N matrix and (block-Jacobi
+  // form) its FP32 copy, and takes the next unsolved realisation until none is left.  The
+  // block-Jacobi form runs several workers at once, so that one realisation's
+  // latency-bound steps (host-driven GMRES, small kernels) overlap another's products; the
+  // factorising forms run one worker (their panel kernel needs every SM to itself).  As many
+  // workers as fit in a quarter of the free device memory, at most kDenseWorkers.
+  constexpr int kDenseWorkers = 4;
+  const size_t per_worker = sizeof(double) * nmax * nmax +
+                            (form == IBEM_SOLVE_GMRES_BJ ? sizeof(float) * ((nmax + 3) / 4 * 4) * nmax : 0);
+  int nwork = 1;
+  if (form == IBEM_SOLVE_GMRES_BJ && per_worker > 0) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+      nwork = (int)std::max<size_t>(1, std::min<size_t>({(size_t)kDenseWorkers, (size_t)batch->nseg,
+                                                         free_b / 4 / per_worker}));
   }
-  for (int i = 0; i < batch->nseg && !s; ++i) {
-    const int p0 = batch->seg_begin[i], n = batch->seg_begin[i + 1] - p0;
-    const int64_t N = (int64_t)nu * n, off = (int64_t)nu * p0;
-    ibem_solve_report rep{};
-    if (n) {
-      s = ibem_e3d_pair_blocks(batch->centers_dev + 3 * (int64_t)p0, batch->radius_dev + p0, n, &batch->mats[i], layout,
-                               A, N, 0, 0, st);
-      if (!s) s = solve_dense(form, N, A, N, b_dev + off, x_dev + off, tol, &rep, st, nu, W);
+  // b_dev is written on the caller's stream: let it land before the workers read it
+  cudaError_t e0 = cudaStreamSynchronize(st);
+  if (e0 != cudaSuccess) return cuda_fail(e0, "batch_dense_solve");
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::atomic<int> next{0};
+  std::atomic<bool> failed{false};
+  std::mutex err_mu;
+  ibem_status first = IBEM_OK;
+  std::string first_msg;
+  auto worker = [&](bool own_stream) {
+    cudaSetDevice(dev);
+    cudaStream_t ws = st;
+    ibem_status s = IBEM_OK;
+    if (own_stream) {
+      const cudaError_t e = cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking);
+      if (e != cudaSuccess) s = cuda_fail(e, "batch_dense_solve: stream");
     }
-    if (reports) reports[i] = rep;
+    double* A = nullptr;
+    float* W = nullptr;
+    if (!s && nmax) {
+      cudaError_t e = alloc_async((void**)&A, sizeof(double) * nmax * nmax, ws);
+      if (e == cudaSuccess && form == IBEM_SOLVE_GMRES_BJ)
+        e = alloc_async((void**)&W, sizeof(float) * ((nmax + 3) / 4 * 4) * nmax, ws);
+      if (e != cudaSuccess) s = cuda_fail(e, "batch_dense_solve: matrix");
+    }
+    while (!s && !failed.load()) {
+      const int i = next.fetch_add(1);
+      if (i >= batch->nseg) break;
+      const int p0 = batch->seg_begin[i], n = batch->seg_begin[i + 1] - p0;
+      const int64_t N = (int64_t)nu * n, off = (int64_t)nu * p0;
+      ibem_solve_report rep{};
+      if (n) {
+        s = ibem_e3d_pair_blocks(batch->centers_dev + 3 * (int64_t)p0, batch->radius_dev + p0, n, &batch->mats[i],
+                                 layout, A, N, 0, 0, ws);
+        if (!s) s = solve_dense(form, N, A, N, b_dev + off, x_dev + off, tol, &rep, ws, nu, W);
+      }
+      if (reports) reports[i] = rep;
+    }
+    free_async(A, ws);
+    free_async(W, ws);
+    cudaStreamSynchronize(ws);
+    if (own_stream && ws) cudaStreamDestroy(ws);
+    if (s) {
+      failed.store(true);
+      std::lock_guard<std::mutex> l(err_mu);
+      if (!first) first = s, first_msg = ibem_last_error();
+    }
+  };
+  if (nwork == 1) {
+    worker(false);
+  } else {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nwork; ++t) pool.emplace_back(worker, true);
+    for (auto& t : pool) t.join();
   }
-  free_async(A, st);
-  free_async(W, st);
-  return s;
+  return first ? fail(first, first_msg) : IBEM_OK;
 }
 
 extern "C" ibem_status ibem_e3d_effective_modulus(const ibem_e3d_batch* batch, const double* x_dev,
