@@ -13,11 +13,14 @@
 //                by blockIdx.z.
 //  bem_post      boundary part of the stress at sample points (post_stress_BEM,
 //                postProcessorElastic3D.cpp:224-365), contracted with U and T at every
-//                Gauss point; one thread per point, elements staged in shared memory.
+//                Gauss point: a per-call quadrature table (point, normal, weight x Jacobian,
+//                interpolated U and T per Gauss point) staged through shared memory, one
+//                thread per sample point.
 #include <cuda_runtime.h>
 
 #include "gen_bem.cuh"
 #include "ibem_internal.h"
+#include "prof.h"
 
 namespace {
 
@@ -285,53 +288,71 @@ __global__ void __launch_bounds__(128) bem_incl_kernel(
 }
 
 // ---- boundary part of the stress at sample points ----
-constexpr int kPostChunk = 32;
+// Everything at a Gauss point that does not depend on the sample point -- its position, unit
+// normal, weight x Jacobian, and U and T interpolated there -- is one record of the
+// quadrature table, formed once per call (one thread per (element, Gauss point)); the
+// per-point kernel then only evaluates the Kelvin stress kernels and contracts them.
+constexpr int kPostQ = 64;        // 8 x 8 Gauss points per element
+constexpr int kPostRec = 13;      // x y z, nx ny nz, w*J, u(3), t(3)
+constexpr int kPostStage = 128;   // table records per shared-memory stage (13 KB)
 
-__global__ void __launch_bounds__(128) bem_post_kernel(
-    const double* __restrict__ pts, int nump, const double* __restrict__ nodes, int NN,
-    const int* __restrict__ conn, int NE, BemMat bm, const double* __restrict__ U,
-    const double* __restrict__ T, double* __restrict__ stress) {
-  __shared__ double sel[kPostChunk][12];
-  __shared__ double sU[kPostChunk][12];
-  __shared__ double sT[kPostChunk][12];
+__global__ void bem_post_table(const double* __restrict__ nodes, int NN, const int* __restrict__ conn, int NE,
+                               const double* __restrict__ U, const double* __restrict__ T,
+                               double* __restrict__ tab) {
+  const int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (id >= (int64_t)NE * kPostQ) return;
+  const int e = (int)(id / kPostQ), q = (int)(id % kPostQ), mq = q / 8, kq = q % 8;
+  double c[12], u[12], t[12];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    int node = conn[4 * e + a] - 1;
+    if (node < 0 || node >= NN) node = 0;  // out-of-range connectivity: never index outside
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      c[3 * a + d] = nodes[3 * node + d];
+      u[3 * a + d] = U[3 * node + d];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 12; ++k) t[k] = T[12 * (int64_t)e + k];
+  double N[4], gc[3], nv[3], jac;
+  q4_point(c, kGP[mq], kGP[kq], N, gc, nv, jac);
+  double* r = tab + id * kPostRec;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    r[d] = gc[d];
+    r[3 + d] = nv[d];
+    r[7 + d] = N[0] * u[d] + N[1] * u[3 + d] + N[2] * u[6 + d] + N[3] * u[9 + d];
+    r[10 + d] = N[0] * t[d] + N[1] * t[3 + d] + N[2] * t[6 + d] + N[3] * t[9 + d];
+  }
+  r[6] = kGW[mq] * kGW[kq] * jac;
+}
+
+__global__ void __launch_bounds__(128) bem_post_kernel(const double* __restrict__ pts, int nump,
+                                                       const double* __restrict__ tab, int64_t nq, BemMat bm,
+                                                       double* __restrict__ stress) {
+  __shared__ double sq[kPostStage * kPostRec];
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   const bool act = s < nump;
   double P0 = 0, P1 = 0, P2 = 0;
   if (act) { P0 = pts[3 * s]; P1 = pts[3 * s + 1]; P2 = pts[3 * s + 2]; }
   double acc[6] = {0, 0, 0, 0, 0, 0};
-  for (int e0 = 0; e0 < NE; e0 += kPostChunk) {
-    const int ne = min(kPostChunk, NE - e0);
+  for (int64_t q0 = 0; q0 < nq; q0 += kPostStage) {
+    const int nqs = (int)min((int64_t)kPostStage, nq - q0);
     __syncthreads();
-    for (int idx = threadIdx.x; idx < ne * 12; idx += blockDim.x) {
-      const int ee = idx / 12, k = idx % 12, a = k / 3, d = k % 3;
-      int node = conn[4 * (e0 + ee) + a] - 1;
-      if (node < 0 || node >= NN) node = 0;  // out-of-range connectivity: never index outside
-      sel[ee][k] = nodes[3 * node + d];
-      sU[ee][k] = U[3 * node + d];
-      sT[ee][k] = T[12 * (int64_t)(e0 + ee) + k];
-    }
+    for (int idx = threadIdx.x; idx < nqs * kPostRec; idx += blockDim.x) sq[idx] = tab[q0 * kPostRec + idx];
     __syncthreads();
     if (!act) continue;
-    for (int ee = 0; ee < ne; ++ee)
-      for (int mq = 0; mq < 8; ++mq)
-        for (int kq = 0; kq < 8; ++kq) {
-          double N[4], gc[3], nv[3], jac;
-          q4_point(sel[ee], kGP[mq], kGP[kq], N, gc, nv, jac);
-          const double wj = kGW[mq] * kGW[kq] * jac;
-          double su[18], st[18];
-          bem_stress_post(gc[0] - P0, gc[1] - P1, gc[2] - P2, nv[0], nv[1], nv[2], bm, bm.lam0,
-                          bm.mu0, su, st);
-          double ub[3], tb[3];
+    for (int qq = 0; qq < nqs; ++qq) {
+      const double* r = sq + qq * kPostRec;
+      double su[18], st[18];
+      bem_stress_post(r[0] - P0, r[1] - P1, r[2] - P2, r[3], r[4], r[5], bm, bm.lam0, bm.mu0, su, st);
+      const double wj = r[6];
 #pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            ub[d] = N[0] * sU[ee][d] + N[1] * sU[ee][3 + d] + N[2] * sU[ee][6 + d] + N[3] * sU[ee][9 + d];
-            tb[d] = N[0] * sT[ee][d] + N[1] * sT[ee][3 + d] + N[2] * sT[ee][6 + d] + N[3] * sT[ee][9 + d];
-          }
-#pragma unroll
-          for (int t = 0; t < 6; ++t)
-            acc[t] += wj * (su[3 * t] * ub[0] + su[3 * t + 1] * ub[1] + su[3 * t + 2] * ub[2] +
-                            st[3 * t] * tb[0] + st[3 * t + 1] * tb[1] + st[3 * t + 2] * tb[2]);
-        }
+      for (int t = 0; t < 6; ++t)
+        acc[t] += wj * (su[3 * t] * r[7] + su[3 * t + 1] * r[8] + su[3 * t + 2] * r[9] + st[3 * t] * r[10] +
+                        st[3 * t + 1] * r[11] + st[3 * t + 2] * r[12]);
+    }
   }
   if (act)
 #pragma unroll
@@ -382,7 +403,14 @@ ibem_status bem_post(const double* pts, int nump, const double* nodes, int NN, c
                      int NE, const ibem_material& m, const double* U, const double* T,
                      double* stress, cudaStream_t st) {
   BemMat bm = bem_mat_init(m.E0, m.nu0, m.E1, m.nu1);
-  ::ibem::count_launch(), bem_post_kernel<<<(nump + 127) / 128, 128, 0, st>>>(pts, nump, nodes, NN, conn, NE, bm, U, T, stress);
+  ProfScope ps(PROF_BEM, st);
+  const int64_t nq = (int64_t)NE * kPostQ;
+  double* tab = nullptr;
+  IBEM_CUDA(cudaMallocAsync((void**)&tab, sizeof(double) * kPostRec * (nq > 0 ? nq : 1), st));
+  if (nq > 0)
+    ::ibem::count_launch(), bem_post_table<<<(unsigned)((nq + 127) / 128), 128, 0, st>>>(nodes, NN, conn, NE, U, T, tab);
+  ::ibem::count_launch(), bem_post_kernel<<<(nump + 127) / 128, 128, 0, st>>>(pts, nump, tab, nq, bm, stress);
+  cudaFreeAsync(tab, st);
   IBEM_LAUNCH_CHECK("bem_post");
   return IBEM_OK;
 }

@@ -20,6 +20,8 @@
 --quad R       R quadratic-eigenstrain realisations (layout 60, the batched measurement's
                distribution) through ibem_e3d_batch_dense_solve (--quad-form bj: block-Jacobi
                GMRES form, mixed: FP32 LU + GMRES-IR), with phases.
+--post G       ibem_e3d_field (FP64, layout 78) on the bounded-cube case (64 spheres, 600
+               boundary elements) at G^3 points: sphere sums and boundary part.
 --assemble NUM,LAYOUT  the pair blocks (ibem_e3d_pair_blocks, FP64) of NUM spheres in
                layout 24, 60 or 78: achieved write bandwidth of the N^2 matrix.
 --mf NUM       the matrix-free products (ibem_e3d_mf_matvec: FP32, double-float, FP64) on a
@@ -132,6 +134,43 @@ def bench_assemble(num, layout, reps, dev):
     return {"kernel": f"pair{layout} + self{layout} (assembly)", "spheres": num, "N": n, "reps": reps, "ms": ms,
             "matrix_GB": 8.0 * n * n / 1e9, "GB_per_s": 8.0 * n * n / (ms * 1e-3) / 1e9,
             "ns_per_pair": ms * 1e6 / (num * num)}
+
+
+def bench_post(grid, reps, dev):
+    """ibem_e3d_field (FP64) on the bounded-cube case of 64 spheres (radius 0.05, 600 Q4
+    boundary elements, layout 78) at grid^3 points with random coefficients: the sphere sums
+    and the boundary part (phase "bem": quadrature table + Kelvin kernels at 64 Gauss points
+    per element and point)."""
+    import numpy as np
+    from . import cases, material
+    c = cases.bounded_cube_case(n_face=10, num=64, radius=0.05, grid=grid, seed=12345)
+    rng = np.random.default_rng(5)
+    t = lambda a, dt=torch.float64: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dt)
+    pts, cen, rad, nodes = t(c.points), t(c.centers), t(c.radius), t(c.nodes)
+    conn = t(c.conn, torch.int32)
+    E = t(rng.standard_normal(78 * c.num) * 1e-3)
+    U = t(rng.standard_normal(3 * c.NN) * 1e-3)
+    T = t(rng.standard_normal(12 * c.NE))
+    S = torch.empty((c.nump, 6), dtype=torch.float64, device=dev)
+    m = material(c.E0, c.nu0, c.E1, c.nu1)
+    L = lib()
+    run = lambda: check(L.ibem_e3d_field(_p(pts), c.nump, _p(cen), _p(rad), c.num, ctypes.byref(m), 78, _p(E),
+                                         _p(nodes), c.NN, _p(conn), c.NE, _p(U), _p(T), None, _p(S), None))
+    run()
+    torch.cuda.synchronize()
+    L.ibem_prof_enable(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        run()
+    e1.record()
+    torch.cuda.synchronize()
+    prof = prof_report()
+    L.ibem_prof_enable(0)
+    return {"kernel": "field (FP64) with boundary part", "points": c.nump, "elements": c.NE, "spheres": c.num,
+            "reps": reps, "ms": e0.elapsed_time(e1) / reps,
+            "phases_ms": {k: round(v["ms"] / reps, 3) for k, v in prof.items()},
+            "ns_per_point_gauss_point": prof.get("bem", {}).get("ms", 0.0) / reps * 1e6 / (c.nump * c.NE * 64)}
 
 
 def bench_mf(num, reps, dev):
@@ -302,6 +341,7 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, action="append", default=[])
     ap.add_argument("--assemble", action="append", default=[], help="NUM,LAYOUT")
     ap.add_argument("--quad", type=int, action="append", default=[])
+    ap.add_argument("--post", type=int, action="append", default=[], help="grid of the bounded-cube field")
     ap.add_argument("--quad-form", default="bj", choices=["bj", "mixed"])
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--vf", type=float, default=0.15, help="volume fraction of --solve (above 0.15: Monte Carlo packing)")
@@ -318,6 +358,8 @@ def main(argv=None):
         print(json.dumps(bench_assemble(num, lay, a.reps, dev)), flush=True)
     for n in a.mf:
         print(json.dumps(bench_mf(n, a.reps, dev)), flush=True)
+    for gsz in a.post:
+        print(json.dumps(bench_post(gsz, a.reps, dev)), flush=True)
     for n in a.quad:
         print(json.dumps(bench_quad(n, a.reps, dev, a.quad_form)), flush=True)
     for n in a.solve:
