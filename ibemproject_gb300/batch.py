@@ -205,6 +205,25 @@ def training_pairs(batch: DeviceBatch, nrhs: int, seed: int = 0):
     return (torch.from_numpy(R).to(batch.device), torch.from_numpy(E).to(batch.device))
 
 
+def training_pairs_mf(batch: DeviceBatch, nrhs: int, seed: int = 0, tol: float = 1e-10):
+    """The pairs of training_pairs for microstructures too large for the dense LU (a
+    2,000-sphere system is 60 s in FP64): e_hat = As^-1 r_hat from the matrix-free solver
+    with block-Jacobi preconditioning and FP64 refinement to relative residual tol, i.e.
+    ||r_hat - As e_hat|| <= tol ||r_hat|| per realisation."""
+    import torch
+    _linear(batch)
+    rng = np.random.default_rng(seed)
+    dr, dc = batch.scalings()
+    R = torch.from_numpy(rng.standard_normal((nrhs, batch.N))).to(batch.device)
+    E = torch.empty_like(R)
+    drt = torch.from_numpy(dr).to(batch.device)
+    dct = torch.from_numpy(dc).to(batch.device)
+    for q in range(nrhs):
+        x, _ = solve(batch, (R[q] / drt).contiguous(), PRECOND_BLOCK_JACOBI, tol=tol)
+        E[q] = x / dct
+    return R, E
+
+
 # ------------------------------------------------------------------ learned preconditioner
 def param_count() -> int:
     return int(lib().ibem_gnn_param_count())
@@ -278,5 +297,5 @@ def train(batch: DeviceBatch, r_hat, e_hat, params, steps: int, lr: float = 2e-3
 
 __all__ = ["DeviceBatch", "farfield_rhs", "dense_batch_solve", "matvec", "solve", "tuning", "effective_modulus",
            "dense_system", "dense_solve",
-           "training_pairs", "param_count", "init_params", "prepare", "loss_grad", "edge_weights", "adamw", "train",
+           "training_pairs", "training_pairs_mf", "param_count", "init_params", "prepare", "loss_grad", "edge_weights", "adamw", "train",
            "PRECOND_BLOCK_JACOBI", "PRECOND_LEARNED", "PRECOND_NEUMANN", "IbemError"]

@@ -20,6 +20,9 @@
 --quad R       R quadratic-eigenstrain realisations (layout 60, the batched measurement's
                distribution) through ibem_e3d_batch_dense_solve (--quad-form bj: block-Jacobi
                GMRES form, mixed: FP32 LU + GMRES-IR), with phases.
+--train-full M the learned preconditioner trained on M microstructures of 500-2,000 spheres
+               (pairs from the matrix-free FP64-refined solver, mini-batches), evaluated
+               against the small training set, Neumann weights and block-Jacobi.
 --post G       ibem_e3d_field (FP64, layout 78) on the bounded-cube case (64 spheres, 600
                boundary elements) at G^3 points: sphere sums and boundary part.
 --assemble NUM,LAYOUT  the pair blocks (ibem_e3d_pair_blocks, FP64) of NUM spheres in
@@ -330,6 +333,94 @@ def bench_quad(nreal, reps, dev, form="bj"):
             "phase_launches": {k: v["launches"] / reps for k, v in prof.items()}}
 
 
+def _eval_preconditioners(c, variants, dev, reps=2):
+    """Matrix-free solve of one far-field microstructure with each (name, precond, params)."""
+    import time
+    import numpy as np
+    from . import batch as B
+    bt = B.DeviceBatch([c], device=dev)
+    b = B.farfield_rhs(bt, np.array([0, 0, 0, 0, 0, 1.0]))
+    out = {}
+    for name, pc, pp in variants:
+        B.solve(bt, b, pc, params=pp)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            _, rep = B.solve(bt, b, pc, params=pp)
+        torch.cuda.synchronize()
+        out[name] = {"s": (time.perf_counter() - t) / reps, "arnoldi_steps": rep[0].inner,
+                     "refinement_steps": rep[0].outer, "rel_residual": rep[0].rel_residual}
+    return out
+
+
+def bench_train_full(nmicro, steps, dev, groups=10, nrhs=2):
+    """The learned preconditioner trained on the full-size training set: nmicro seeded
+    microstructures of U[500, 2000] spheres (radius U[0.8, 1.2] x 0.012, Monte Carlo packing,
+    vf U[15%, 25%], E1/E0 U[2, 20]), nrhs residual / correction pairs each from the
+    matrix-free FP64-refined solver (relative residual 1e-10), mini-batches of nmicro / groups
+    microstructures cycled over `steps` AdamW steps; against the small set (12
+    microstructures of 100-150 spheres, dense FP64 pairs, full batch), the analytic Neumann
+    weights and block-Jacobi, on the 2,000-sphere bench microstructure and on 20,000 spheres
+    at vf 25%."""
+    import time
+    import numpy as np
+    from . import batch as B
+    from . import cases
+    rng = np.random.default_rng(31)
+    nums = rng.integers(500, 2001, size=nmicro)
+    vfs = rng.uniform(0.15, 0.25, size=nmicro)
+    con = rng.uniform(2.0, 20.0, size=nmicro)
+    t = time.perf_counter()
+    cs = [cases.generated_case(int(n), 0.012, float(v), seed=20000 + k, E1=70e9 * float(c0))
+          for k, (n, v, c0) in enumerate(zip(nums, vfs, con))]
+    t_gen = time.perf_counter() - t
+    t = time.perf_counter()
+    preps = []
+    per = (nmicro + groups - 1) // groups
+    for g0 in range(0, nmicro, per):
+        bt = B.DeviceBatch(cs[g0:g0 + per], device=dev)
+        r, e = B.training_pairs_mf(bt, nrhs, seed=g0)
+        preps.append((B.prepare(bt, r, e), bt.num))
+        del r, e
+    torch.cuda.synchronize()
+    t_pairs = time.perf_counter() - t
+    params = B.init_params(seed=1, device=dev)
+    m = torch.zeros_like(params)
+    v = torch.zeros_like(params)
+    first = [B.loss_grad(p, n, params)[0] for p, n in preps]
+    t = time.perf_counter()
+    for it in range(steps):
+        p, n = preps[it % len(preps)]
+        _, gr = B.loss_grad(p, n, params)
+        B.adamw(params, gr, m, v, it + 1, 3e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t
+    last = [B.loss_grad(p, n, params)[0] for p, n in preps]
+    del preps
+    # the small training set of bench.py
+    rs = np.random.default_rng(77)
+    sn = rs.integers(100, 151, size=12)
+    sv = rs.uniform(0.10, 0.20, size=12)
+    sc = rs.uniform(2.0, 20.0, size=12)
+    sc[:4] = 400.0 / 70.0
+    small = [cases.farfield_case(num=int(n), r0=0.012, vf=float(v0), grid=0, seed=9000 + k, E1=70e9 * float(c0))
+             for k, (n, v0, c0) in enumerate(zip(sn, sv, sc))]
+    sb = B.DeviceBatch(small, device=dev)
+    r, e = B.training_pairs(sb, nrhs=4, seed=5)
+    ps = B.init_params(seed=1, device=dev)
+    B.train(sb, r, e, ps, steps=300, lr=3e-3)
+    variants = [("block_jacobi", B.PRECOND_BLOCK_JACOBI, None), ("neumann", B.PRECOND_NEUMANN, None),
+                ("learned_small_set", B.PRECOND_LEARNED, ps), ("learned_full_set", B.PRECOND_LEARNED, params)]
+    ev = {"bench_2000_vf15": _eval_preconditioners(cases.farfield_case(num=2000, r0=0.012, vf=0.15, grid=0, seed=2024),
+                                                   variants, dev),
+          "spheres_20000_vf25": _eval_preconditioners(cases.generated_case(20000, 0.012, 0.25, seed=2024), variants,
+                                                      dev, reps=1)}
+    return {"kernel": "learned preconditioner, full training set", "microstructures": nmicro,
+            "spheres": int(nums.sum()), "pairs": nrhs * nmicro, "groups": len(first), "steps": steps,
+            "generation_s": t_gen, "pairs_and_graphs_s": t_pairs, "train_s": t_train,
+            "loss_first_mean": float(np.mean(first)), "loss_last_mean": float(np.mean(last)), "evaluation": ev}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gemm", action="append", default=[], help="M,N,K")
@@ -341,6 +432,8 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, action="append", default=[])
     ap.add_argument("--assemble", action="append", default=[], help="NUM,LAYOUT")
     ap.add_argument("--quad", type=int, action="append", default=[])
+    ap.add_argument("--train-full", type=int, default=0, help="microstructures of the full training set")
+    ap.add_argument("--train-steps", type=int, default=300)
     ap.add_argument("--post", type=int, action="append", default=[], help="grid of the bounded-cube field")
     ap.add_argument("--quad-form", default="bj", choices=["bj", "mixed"])
     ap.add_argument("--reps", type=int, default=3)
@@ -358,6 +451,8 @@ def main(argv=None):
         print(json.dumps(bench_assemble(num, lay, a.reps, dev)), flush=True)
     for n in a.mf:
         print(json.dumps(bench_mf(n, a.reps, dev)), flush=True)
+    if a.train_full:
+        print(json.dumps(bench_train_full(a.train_full, a.train_steps, dev)), flush=True)
     for gsz in a.post:
         print(json.dumps(bench_post(gsz, a.reps, dev)), flush=True)
     for n in a.quad:
