@@ -99,6 +99,8 @@ SIGNATURES = {
                               _int, _vp, _vp, _c_dp, _vp, _vp]),
     "ibem_e3d_field_form": (_int, [_int, _vp, _int, _vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _vp, _int,
                                    _vp, _int, _vp, _vp, _c_dp, _vp, _vp]),
+    "ibem_e3d_field_grid": (_int, [_int, _c_dp, _c_dp, _c_ip, _vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _vp,
+                                   _int, _vp, _int, _vp, _vp, _c_dp, _vp, _vp]),
     "ibem_e3d_run_host": (_int, [_int, _int, ctypes.POINTER(Material), _int, _c_dp, _int, _c_ip, _c_dp, _c_dp,
                                  _int, _c_dp, _c_dp, _int, _c_dp, _c_dp, _dbl, _c_dp, _c_dp,
                                  ctypes.POINTER(SolveReport)]),

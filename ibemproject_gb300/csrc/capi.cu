@@ -1,6 +1,8 @@
 // extern "C" entry points of libibem_gb300.so (declared in include/ibem_gb300.h).
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -105,10 +107,25 @@ __global__ void k_fill6(int nump, FarRhs f, double* __restrict__ s) {
   if (t < (int64_t)nump * 6) s[t] = f.v[t % 6];
 }
 
+struct GridSpec {
+  double lo[3], span[3];
+  int n[3];
+};
+// cell-centred grid points, x fastest: lo + ((i, j, k) + 1/2) / n * (hi - lo), the order of
+// operations of cases.cell_grid
+__global__ void k_grid_points(int64_t nump, GridSpec g, double* __restrict__ pts) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nump) return;
+  const int64_t idx[3] = {t % g.n[0], (t / g.n[0]) % g.n[1], t / ((int64_t)g.n[0] * g.n[1])};
+#pragma unroll
+  for (int d = 0; d < 3; ++d)  // rounded operation by operation (no fused multiply-add): a host grid matches
+    pts[3 * t + d] = __dadd_rn(g.lo[d], __dmul_rn(__ddiv_rn((double)idx[d] + 0.5, (double)g.n[d]), g.span[d]));
+}
 }  // namespace
 }  // namespace ibem
 
 using namespace ibem;
+
 
 extern "C" {
 
@@ -338,6 +355,32 @@ ibem_status ibem_e3d_field_form(ibem_solver_form form, const double* points_dev,
                                        : launch_field24(p, points_dev, nump, E_dev, stress_dev, st);
   if (layout == 60) return launch_field60(p, points_dev, nump, E_dev, stress_dev, st);
   return launch_field78(p, points_dev, nump, E_dev, stress_dev, st);
+}
+
+ibem_status ibem_e3d_field_grid(ibem_solver_form form, const double* lo, const double* hi, const int* n,
+                                const double* centers_dev, const double* radius_dev, int num,
+                                const ibem_material* mat, int layout, const double* E_dev,
+                                const double* nodes_dev, int NN, const int* conn_dev, int NE,
+                                const double* U_dev, const double* T_dev, const double* sig_inf,
+                                double* stress_dev, void* stream) {
+  if (!lo || !hi || !n || n[0] < 0 || n[1] < 0 || n[2] < 0) return fail(IBEM_ERR_ARG, "field_grid: bad grid");
+  const int64_t nump = (int64_t)n[0] * n[1] * n[2];
+  if (nump > INT32_MAX) return fail(IBEM_ERR_ARG, "field_grid: more than 2^31 - 1 points");
+  if (nump == 0) return IBEM_OK;
+  cudaStream_t st = as_stream(stream);
+  double* pts = nullptr;
+  IBEM_CUDA(cudaMallocAsync((void**)&pts, sizeof(double) * 3 * nump, st));
+  GridSpec g;
+  for (int d = 0; d < 3; ++d) g.lo[d] = lo[d], g.span[d] = hi[d] - lo[d], g.n[d] = n[d];
+  ::ibem::count_launch(), k_grid_points<<<(unsigned)((nump + 255) / 256), 256, 0, st>>>(nump, g, pts);
+  ibem_status s = IBEM_OK;
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) s = cuda_fail(e, "field_grid");
+  if (!s)
+    s = ibem_e3d_field_form(form, pts, (int)nump, centers_dev, radius_dev, num, mat, layout, E_dev, nodes_dev, NN,
+                            conn_dev, NE, U_dev, T_dev, sig_inf, stress_dev, stream);
+  cudaFreeAsync(pts, st);
+  return s;
 }
 
 ibem_status ibem_e3d_field(const double* points_dev, int nump, const double* centers_dev,

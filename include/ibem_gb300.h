@@ -431,12 +431,24 @@ ibem_status ibem_e3d_field(const double* points_dev, int nump, const double* cen
 /* ibem_e3d_field with a precision choice (no counterpart in the reference, which has one
  * precision).  IBEM_SOLVE_FP64 is ibem_e3d_field.  IBEM_SOLVE_MIXED_IR runs the sphere
  * sums of the 24-unknown layout in double-float arithmetic (pairs of FP32 numbers, about
- * 48 significant bits; agrees with the FP64 sums to ~1e-12 of the strain), which GB300
- * executes several times faster than FP64; the 60/78 layouts and the boundary part stay
- * FP64.  ibem_e3d_run_host / ibem_e3d_run_dir use the form given to them here too. */
+ * 48 significant bits) for spheres within 14 radii of a warp's points and in FP32 beyond
+ * (agrees with the FP64 sums to ~1e-9 of the strain), which GB300 executes several times
+ * faster than FP64; the 60/78 layouts and the boundary part stay FP64.
+ * ibem_e3d_run_host / ibem_e3d_run_dir use the form given to them here too. */
 ibem_status ibem_e3d_field_form(ibem_solver_form form, const double* points_dev, int nump,
                                 const double* centers_dev, const double* radius_dev, int num,
                                 const ibem_material* mat, int layout, const double* E_dev,
+                                const double* nodes_dev, int NN, const int* conn_dev, int NE,
+                                const double* U_dev, const double* T_dev, const double* sig_inf,
+                                double* stress_dev, void* stream);
+
+/* Grid service: ibem_e3d_field_form at the cell centres of an n[0] x n[1] x n[2] grid over
+ * the box [lo, hi] (host arrays of 3), generated on the device instead of read from a
+ * point list (postprocess.txt of a grid, configElastic3D.h:116-129): point (i, j, k) =
+ * lo + ((i, j, k) + 1/2) (hi - lo) / n, x fastest; stress_dev: n[0] n[1] n[2] x 6. */
+ibem_status ibem_e3d_field_grid(ibem_solver_form form, const double* lo, const double* hi,
+                                const int* n, const double* centers_dev, const double* radius_dev,
+                                int num, const ibem_material* mat, int layout, const double* E_dev,
                                 const double* nodes_dev, int NN, const int* conn_dev, int NE,
                                 const double* U_dev, const double* T_dev, const double* sig_inf,
                                 double* stress_dev, void* stream);

@@ -362,3 +362,47 @@ def test_block_jacobi_form_ragged_blocks_and_arguments(B):
     assert L.ibem_e3d_solve(g.SOLVE_GMRES_BJ, n, P(A), n, P(b), P(x), 1e-12, ctypes.byref(rep), None) == 1
     for block in (0, 81):
         assert L.ibem_e3d_solve_bj(n, block, P(A), n, P(b), P(x), 1e-12, ctypes.byref(rep), None) == 1
+
+
+def test_field_grid_service_matches_point_list(B):
+    """ibem_e3d_field_grid (points generated on the device) gives the stresses of
+    ibem_e3d_field_form at the cell-centred grid of cases.cell_grid, bit for bit, in both
+    forms, for a far-field case and a bounded cube with boundary elements."""
+    import ctypes
+
+    import torch
+
+    import ibemproject_gb300 as g
+    from ibemproject_gb300 import cases
+    dev = "cuda"
+    rng = np.random.default_rng(3)
+    for c, lo, hi, n in ((cases.farfield_case(num=40, r0=0.012, vf=0.15, grid=0, seed=5), None, None, (7, 5, 6)),
+                         (cases.bounded_cube_case(n_face=3, num=4, radius=0.05, grid=0, seed=2), 0.0, 1.0, (4, 4, 4))):
+        lo3 = np.full(3, lo if lo is not None else c.centers.min() - 0.01)
+        hi3 = np.full(3, hi if hi is not None else c.centers.max() + 0.01)
+        z, y, x = np.meshgrid((np.arange(n[2]) + 0.5) / n[2], (np.arange(n[1]) + 0.5) / n[1],
+                              (np.arange(n[0]) + 0.5) / n[0], indexing="ij")
+        pts = lo3 + np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1) * (hi3 - lo3)
+        T = lambda a, dt=torch.float64: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dt)
+        cen, rad, P = T(c.centers), T(c.radius), T(pts)
+        E = T(rng.standard_normal(24 * c.num) * 1e-3)
+        nodes = T(c.nodes if c.NN else np.zeros((1, 3)))
+        conn = T(c.conn if c.NE else np.zeros((1, 4)), torch.int32)
+        U = T(rng.standard_normal(max(3 * c.NN, 1)) * 1e-3)
+        Tt = T(rng.standard_normal(max(12 * c.NE, 1)))
+        sig = np.array([0.1, 0.0, 0.2, 0.0, 0.0, 1.0])
+        m = g.material(c.E0, c.nu0, c.E1, c.nu1)
+        dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        V = lambda t_: ctypes.c_void_p(t_.data_ptr())
+        npts = int(np.prod(n))
+        for form in (g.SOLVE_FP64, g.SOLVE_MIXED_IR):
+            S1 = torch.zeros((npts, 6), dtype=torch.float64, device=dev)
+            S2 = torch.zeros_like(S1)
+            g.check(g.lib().ibem_e3d_field_form(form, V(P), npts, V(cen), V(rad), c.num, ctypes.byref(m), 24, V(E),
+                                                V(nodes), c.NN, V(conn), c.NE, V(U), V(Tt), dp(sig), V(S1), None))
+            na = np.array(n, dtype=np.int32)
+            g.check(g.lib().ibem_e3d_field_grid(form, dp(lo3), dp(hi3), na.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                                V(cen), V(rad), c.num, ctypes.byref(m), 24, V(E), V(nodes), c.NN,
+                                                V(conn), c.NE, V(U), V(Tt), dp(sig), V(S2), None))
+            torch.cuda.synchronize()
+            assert torch.equal(S1, S2), form
