@@ -443,7 +443,7 @@ def run_ours(args, rank, world):
             if A is None:
                 A = torch.empty((N, N), dtype=torch.float64, device=dev)   # column-major N x N
             f = g.SOLVE_MIXED_IR if form == "mixed_ir" else g.SOLVE_FP64
-            g.check(L.ibem_e3d_pair_blocks_form(f, P(cen), P(rad), num, ctypes.byref(m), 24, P(A), N, 0, 0, sp))
+            g.check(L.ibem_e3d_pair_blocks(P(cen), P(rad), num, ctypes.byref(m), 24, P(A), N, 0, 0, sp))
             g.check(L.ibem_e3d_farfield_rhs(num, ctypes.byref(m), 24, sigp, P(b), sp))
             ev[1].record(stream)
             g.check(L.ibem_e3d_solve(f, N, P(A), N, P(b), P(xo), args.tol, ctypes.byref(rep), sp))

@@ -81,8 +81,6 @@ SIGNATURES = {
     "ibem_prof_enable": (None, [_int]),
     "ibem_prof_report": (_int, [ctypes.c_char_p, _int]),
     "ibem_e3d_pair_blocks": (_int, [_vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _i64, _i64, _i64, _vp]),
-    "ibem_e3d_pair_blocks_form": (_int, [_int, _vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _i64, _i64, _i64,
-                                         _vp]),
     "ibem_e3d_node_blocks": (_int, [_vp, _int, _vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _i64, _i64,
                                     _i64, _vp]),
     "ibem_e3d_bem_hg": (_int, [_vp, _int, _vp, _int, ctypes.POINTER(Material), _vp, _i64, _i64, _i64, _vp, _i64,

@@ -691,34 +691,6 @@ def to_f32(src: str, old_name: str, new_name: str) -> str:
     return out
 
 
-DF_HEAD = """// GENERATED by ibemproject_gb300/codegen.py -- do not edit by hand.
-// Double-float variant of the sphere pair blocks (the FP64 straight-line code of
-// gen_sphere{L}.cuh evaluated with the DF number type of dfnum.cuh: pairs of FP32 numbers,
-// ~48 significant bits, on the FP32 pipe).  Called in coordinates scaled by the source
-// radius (a = 1) with moduli divided by mu0, so every intermediate stays well inside FP32's
-// exponent range; the pair kernels multiply each block by mu0 a^(co - ro).
-#pragma once
-#include "gen_sphere_common.cuh"
-#include "dfnum.cuh"
-
-using ibem::DF;
-"""
-
-
-def to_df(src: str, old_name: str, new_name: str) -> str:
-    """Double-float copy of a generated block function: the same straight-line arithmetic
-    on DF values (division and square root of the sphere-integral prelude through the DF
-    reciprocal and inverse square root)."""
-    out = src.replace(old_name + "(", new_name + "(")
-    out = out.replace("const double irho2 = 1.0 / rho2;", "const DF irho2 = ibem::df_recip(rho2);")
-    out = out.replace("/ sqrt(rho2);", "* ibem::rsqrt_t(rho2);")
-    out = out.replace("Jv[m] = pw / (2 * m + 1); pw *= irho2;", "Jv[m] = pw * DF(1.0 / (2 * m + 1)); pw = pw * irho2;")
-    out = out.replace("const double", "const DF").replace("double Jv[", "DF Jv[").replace("double pw", "DF pw")
-    assert "sqrt(" not in out.replace("rsqrt_t(", "") and "pw / " not in out and "1.0 / rho2" not in out, \
-        "unconverted division or square root in " + new_name
-    return out
-
-
 def generate(out_dir: str | None = None) -> dict:
     out_dir = out_dir or os.path.join(HERE, "csrc")
     files = {}
@@ -742,12 +714,6 @@ def generate(out_dir: str | None = None) -> dict:
             fparts.append(to_f32(parts[1 + 2 * co + ro], nm, nm.replace("block24", "block24f")))
     fparts.append(to_f32(gen_self_function("sph_self24", 24), "sph_self24", "sph_self24f"))
     files["gen_sphere24_f32.cuh"] = "\n\n".join(fparts) + "\n"
-    dparts = [DF_HEAD.replace("{L}", "24")]
-    for co in range(2):
-        for ro in range(2):
-            nm = f"sph_block24_c{co}_r{ro}"
-            dparts.append(to_df(parts[1 + 2 * co + ro], nm, nm.replace("block24", "block24df")))
-    files["gen_sphere24_df.cuh"] = "\n\n".join(dparts) + "\n"
     for lay in (78, 60):
         U = units(lay)
         parts = [FILE_HEAD]

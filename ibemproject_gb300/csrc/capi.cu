@@ -150,22 +150,6 @@ ibem_status ibem_e3d_pair_blocks(const double* centers_dev, const double* radius
   return launch_pair78(p, A_dev, lda, row0, col0, st);
 }
 
-ibem_status ibem_e3d_pair_blocks_form(ibem_solver_form form, const double* centers_dev, const double* radius_dev,
-                                      int num, const ibem_material* mat, int layout, double* A_dev, int64_t lda,
-                                      int64_t row0, int64_t col0, void* stream) {
-  if (form == IBEM_SOLVE_FP64 || layout != 24)
-    return ibem_e3d_pair_blocks(centers_dev, radius_dev, num, mat, layout, A_dev, lda, row0, col0, stream);
-  if (form != IBEM_SOLVE_MIXED_IR && form != IBEM_SOLVE_GMRES_BJ) return fail(IBEM_ERR_ARG, "pair_blocks: unknown form");
-  if (!mat || !valid_layout(layout) || num < 0 || (num && (!centers_dev || !radius_dev || !A_dev)))
-    return fail(IBEM_ERR_ARG, "pair_blocks: bad arguments");
-  if (num > 65535) return fail(IBEM_ERR_ARG, "pair_blocks: at most 65535 particles per call");
-  if (lda < row0 + (int64_t)layout * num) return fail(IBEM_ERR_ARG, "pair_blocks: lda too small");
-  if (num == 0) return IBEM_OK;
-  SphLaunch p = sph(centers_dev, radius_dev, num, mat);
-  cudaStream_t st = as_stream(stream);
-  return launch_pair24_df(p, A_dev, lda, row0, col0, st);
-}
-
 ibem_status ibem_e3d_node_blocks(const double* nodes_dev, int NN, const double* centers_dev,
                                  const double* radius_dev, int num, const ibem_material* mat,
                                  int layout, double* H_dev, int64_t ldh, int64_t row0,

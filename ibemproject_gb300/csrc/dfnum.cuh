@@ -35,14 +35,6 @@ IBEM_HD inline DF rsqrt_t(DF x) {
   return DF(yd + yd * (t * 0.5f));
 }
 
-// 1 / x: FP32 estimate q0 and one double-float correction q0 + q0 (1 - x q0)
-IBEM_HD inline DF df_recip(DF x) {
-  const float q0 = 1.0f / x.v.hi;
-  const dfloat qd{q0, 0.0f};
-  const dfloat t = dfloat{1.0f, 0.0f} - x.v * qd;
-  return DF(qd + qd * t);
-}
-
 IBEM_HD inline double df_value(DF a) { return (double)a.v.hi + (double)a.v.lo; }
 
 }  // namespace ibem

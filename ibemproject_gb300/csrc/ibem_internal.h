@@ -38,8 +38,6 @@ struct SphLaunch {
   double E0, nu0, E1, nu1;
 };
 ibem_status launch_pair24(const SphLaunch& p, double* A, int64_t lda, int64_t row0, int64_t col0, cudaStream_t st);
-// the same blocks evaluated in double-float arithmetic (layout 24)
-ibem_status launch_pair24_df(const SphLaunch& p, double* A, int64_t lda, int64_t row0, int64_t col0, cudaStream_t st);
 ibem_status launch_pair60(const SphLaunch& p, double* A, int64_t lda, int64_t row0, int64_t col0, cudaStream_t st);
 ibem_status launch_pair78(const SphLaunch& p, double* A, int64_t lda, int64_t row0, int64_t col0, cudaStream_t st);
 ibem_status launch_node24(const SphLaunch& p, const double* nodes, int NN, double* H, int64_t ldh, int64_t row0, int64_t col0, cudaStream_t st);

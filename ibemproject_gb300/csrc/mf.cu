@@ -1281,8 +1281,8 @@ extern "C" ibem_status ibem_e3d_batch_dense_solve(const ibem_e3d_batch* batch, i
       const int64_t N = (int64_t)nu * n, off = (int64_t)nu * p0;
       ibem_solve_report rep{};
       if (n) {
-        s = ibem_e3d_pair_blocks_form(form, batch->centers_dev + 3 * (int64_t)p0, batch->radius_dev + p0, n,
-                                      &batch->mats[i], layout, A, N, 0, 0, ws);
+        s = ibem_e3d_pair_blocks(batch->centers_dev + 3 * (int64_t)p0, batch->radius_dev + p0, n, &batch->mats[i],
+                                 layout, A, N, 0, 0, ws);
         if (!s) s = solve_dense(form, N, A, N, b_dev + off, x_dev + off, tol, &rep, ws, nu, W);
       }
       if (reports) reports[i] = rep;

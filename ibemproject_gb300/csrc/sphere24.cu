@@ -1,7 +1,6 @@
 // Sphere kernels for the 24-unknown layout (eigenstrain orders 0 and 1).
 #include "field_contract.cuh"
 #include "gen_sphere24.cuh"
-#include "gen_sphere24_df.cuh"
 #include "prof.h"
 #include "sphere_kernels.cuh"
 
@@ -11,10 +10,6 @@ IBEM_PAIR_KERNEL(pair24_c0_r0, sph_block24_c0_r0, 24)
 IBEM_PAIR_KERNEL(pair24_c0_r1, sph_block24_c0_r1, 24)
 IBEM_PAIR_KERNEL(pair24_c1_r0, sph_block24_c1_r0, 24)
 IBEM_PAIR_KERNEL(pair24_c1_r1, sph_block24_c1_r1, 24)
-IBEM_PAIR_KERNEL_DF(pair24df_c0_r0, sph_block24df_c0_r0, 24, 0, 0)
-IBEM_PAIR_KERNEL_DF(pair24df_c0_r1, sph_block24df_c0_r1, 24, 0, 1)
-IBEM_PAIR_KERNEL_DF(pair24df_c1_r0, sph_block24df_c1_r0, 24, 1, 0)
-IBEM_PAIR_KERNEL_DF(pair24df_c1_r1, sph_block24df_c1_r1, 24, 1, 1)
 IBEM_SELF_KERNEL(self24, sph_self24, 24)
 IBEM_NODE_KERNEL(node24, sph_node24, 24)
 IBEM_FIELD_KERNEL(field24, sph_field24_contracted, 24)
@@ -172,22 +167,6 @@ ibem_status launch_pair24(const SphLaunch& p, double* A, int64_t lda, int64_t ro
   ::ibem::count_launch(), pair24_c1_r1<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, mc, base, lda);
   ::ibem::count_launch(), self24<<<(p.num + 127) / 128, 128, 0, st>>>(p.num, mc, base, lda);
   IBEM_LAUNCH_CHECK("pair24");
-  return IBEM_OK;
-}
-
-ibem_status launch_pair24_df(const SphLaunch& p, double* A, int64_t lda, int64_t row0, int64_t col0,
-                             cudaStream_t st) {
-  const SphMat mc = sph_mat_init(p.E0, p.nu0, p.E1, p.nu1);
-  const SphMat ms = sph_mat_scaled(mc);
-  ProfScope ps(PROF_PAIR, st);
-  double* base = A + col0 * lda + row0;
-  dim3 grid((p.num + kPairThreads - 1) / kPairThreads, p.num);
-  ::ibem::count_launch(), pair24df_c0_r0<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, ms, mc.mu0, base, lda);
-  ::ibem::count_launch(), pair24df_c0_r1<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, ms, mc.mu0, base, lda);
-  ::ibem::count_launch(), pair24df_c1_r0<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, ms, mc.mu0, base, lda);
-  ::ibem::count_launch(), pair24df_c1_r1<<<grid, kPairThreads, 0, st>>>(p.cen, p.rad, p.num, ms, mc.mu0, base, lda);
-  ::ibem::count_launch(), self24<<<(p.num + 127) / 128, 128, 0, st>>>(p.num, mc, base, lda);
-  IBEM_LAUNCH_CHECK("pair24 df");
   return IBEM_OK;
 }
 

@@ -14,7 +14,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "dfnum.cuh"
 #include "gen_sphere_common.cuh"
 #include "ibem_internal.h"
 
@@ -30,23 +29,6 @@ struct AddSink {
   int64_t lda;
   __device__ __forceinline__ void operator()(int r, int c, double v) const { A[c * lda + r] += v; }
 };
-
-// Stores a double-float block entry times a constant (the pair kernels' mu0 a^(co - ro)).
-template <class V>
-struct ScaledStoreSink {
-  double* A;
-  int64_t lda;
-  double scale;
-  __device__ __forceinline__ void operator()(int r, int c, V v) const { A[c * lda + r] = scale * df_value(v); }
-};
-
-// Contrast moduli divided by mu0, for the double-float blocks (O(1) numbers in FP32 range).
-inline SphMat sph_mat_scaled(const SphMat& mc) {
-  SphMat ms = mc;
-  ms.kmu /= mc.mu0;
-  ms.klam /= mc.mu0;
-  return ms;
-}
 
 constexpr int kPairThreads = 128;
 constexpr int kFieldThreads = 128;
@@ -67,28 +49,6 @@ constexpr int kFieldChunk = 64;
     const double x2 = cen[3 * s + 2] - cen[3 * h + 2];                                         \
     ibem::StoreSink sink{A + (int64_t)(NU) * h * lda + (int64_t)(NU) * s, lda};              \
     FN(x0, x1, x2, rad[h], mc, sink);                                                          \
-  }
-
-// The same block in double-float arithmetic (gen_sphere{NU}_df.cuh): evaluated in
-// coordinates scaled by the source radius a (a = 1) with the contrast moduli divided by mu0
-// (`ms`), then multiplied by mu0 a^(CO - RO) -- an entry of column order CO (eigenstrain
-// polynomial degree) and row order RO (derivatives at the target) scales as a^(CO - RO).
-#define IBEM_PAIR_KERNEL_DF(KNAME, FN, NU, CO, RO)                                               \
-  __global__ void __launch_bounds__(ibem::kPairThreads)                                        \
-      KNAME(const double* __restrict__ cen, const double* __restrict__ rad, int num, SphMat ms,  \
-            double mu0, double* __restrict__ A, int64_t lda) {                                 \
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;                                       \
-    const int h = blockIdx.y;                                                                  \
-    if (s >= num) return;                                                                      \
-    const double ia = 1.0 / rad[h];                                                            \
-    const double x0 = (cen[3 * s] - cen[3 * h]) * ia;                                          \
-    const double x1 = (cen[3 * s + 1] - cen[3 * h + 1]) * ia;                                  \
-    const double x2 = (cen[3 * s + 2] - cen[3 * h + 2]) * ia;                                  \
-    double sc = mu0;                                                                           \
-    for (int k = RO; k < CO; ++k) sc *= rad[h];                                                \
-    for (int k = CO; k < RO; ++k) sc *= ia;                                                    \
-    ibem::ScaledStoreSink<ibem::DF> sink{A + (int64_t)(NU) * h * lda + (int64_t)(NU) * s, lda, sc}; \
-    FN(x0, x1, x2, 1.0, ms, sink);                                                             \
   }
 
 #define IBEM_SELF_KERNEL(KNAME, FN, NU)                                              \

@@ -156,8 +156,7 @@ void integratorElastic3D_gb300::addFluxEquivalentInclusion(Config& c_) {
   auto& c = as_e3d(c_);
   const ibem_material m = c.material();
   const int64_t N = c.n_unknowns(), o = 3 * (int64_t)c.NN;
-  // the FP64 form assembles in FP64 (the reference's arithmetic); the mixed form in double-float
-  check(ibem_e3d_pair_blocks_form(c.form, c.d_cen.p, c.d_rad.p, c.num, &m, c.layout, c.HMAT.p, N, o, o, c.stream),
+  check(ibem_e3d_pair_blocks(c.d_cen.p, c.d_rad.p, c.num, &m, c.layout, c.HMAT.p, N, o, o, c.stream),
         "addFluxEquivalentInclusion");
 }
 void integratorElastic3D_gb300::addFluxEquivalentFirstOrderInclusion(Config& c_) { (void)as_e3d(c_); }

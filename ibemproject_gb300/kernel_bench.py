@@ -25,9 +25,8 @@
                against the small training set, Neumann weights and block-Jacobi.
 --post G       ibem_e3d_field (FP64, layout 78) on the bounded-cube case (64 spheres, 600
                boundary elements) at G^3 points: sphere sums and boundary part.
---assemble NUM,LAYOUT[,df]  the pair blocks (ibem_e3d_pair_blocks, FP64; ",df": the
-               double-float blocks of ibem_e3d_pair_blocks_form) of NUM spheres in layout 24,
-               60 or 78: achieved write bandwidth of the N^2 matrix.
+--assemble NUM,LAYOUT  the pair blocks (ibem_e3d_pair_blocks, FP64) of NUM spheres in
+               layout 24, 60 or 78: achieved write bandwidth of the N^2 matrix.
 --mf NUM       the matrix-free products (ibem_e3d_mf_matvec: FP32, double-float, FP64) on a
                far-field microstructure of NUM spheres (bench distribution): NUM^2 pair
                products per launch, timed by the library's phase events.
@@ -111,10 +110,9 @@ def bench_lu(n, form, reps, dev):
             "phase_launches": {k: v["launches"] / reps for k, v in prof.items()}}
 
 
-def bench_assemble(num, layout, reps, dev, df=False):
+def bench_assemble(num, layout, reps, dev):
     """ibem_e3d_pair_blocks of a far-field microstructure (bench distribution): the
-    (layout num)^2 FP64 matrix written once per call; algorithmic bytes = its 8 N^2 bytes.
-    df: the double-float blocks of ibem_e3d_pair_blocks_form (mixed form)."""
+    (layout num)^2 FP64 matrix written once per call; algorithmic bytes = its 8 N^2 bytes."""
     import numpy as np
     from . import cases, material
     c = cases.farfield_case(num=num, r0=0.012, vf=0.15, grid=0, seed=2024)
@@ -126,9 +124,7 @@ def bench_assemble(num, layout, reps, dev, df=False):
     st = torch.cuda.current_stream(dev)
     sp = ctypes.c_void_p(st.cuda_stream)
     L = lib()
-    f = SOLVE_MIXED_IR if df else SOLVE_FP64
-    run = lambda: check(L.ibem_e3d_pair_blocks_form(f, _p(cen), _p(rad), num, ctypes.byref(m), layout, _p(A), n, 0, 0,
-                                                    sp))
+    run = lambda: check(L.ibem_e3d_pair_blocks(_p(cen), _p(rad), num, ctypes.byref(m), layout, _p(A), n, 0, 0, sp))
     run()   # warm-up
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -138,7 +134,7 @@ def bench_assemble(num, layout, reps, dev, df=False):
     e1.record(st)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
-    return {"kernel": f"pair{layout}{'df' if df and layout == 24 else ''} + self{layout} (assembly)", "spheres": num, "N": n, "reps": reps, "ms": ms,
+    return {"kernel": f"pair{layout} + self{layout} (assembly)", "spheres": num, "N": n, "reps": reps, "ms": ms,
             "matrix_GB": 8.0 * n * n / 1e9, "GB_per_s": 8.0 * n * n / (ms * 1e-3) / 1e9,
             "ns_per_pair": ms * 1e6 / (num * num)}
 
@@ -451,9 +447,8 @@ def main(argv=None):
     for n in a.lu:
         print(json.dumps(bench_lu(n, a.form, a.reps, dev)), flush=True)
     for f in a.assemble:
-        parts = f.split(",")
-        print(json.dumps(bench_assemble(int(parts[0]), int(parts[1]), a.reps, dev, len(parts) > 2 and parts[2] == "df")),
-              flush=True)
+        num, lay = (int(v) for v in f.split(","))
+        print(json.dumps(bench_assemble(num, lay, a.reps, dev)), flush=True)
     for n in a.mf:
         print(json.dumps(bench_mf(n, a.reps, dev)), flush=True)
     if a.train_full:

@@ -148,18 +148,6 @@ typedef struct {
   double t_factor_ms, t_solve_ms;
 } ibem_solve_report;
 
-/* ibem_e3d_pair_blocks with a precision choice (no reference counterpart, which has one
- * precision): IBEM_SOLVE_FP64 is ibem_e3d_pair_blocks; IBEM_SOLVE_MIXED_IR and
- * IBEM_SOLVE_GMRES_BJ evaluate the layout-24 blocks in double-float arithmetic (pairs of
- * FP32 numbers, ~48 bits, entries within ~1e-13 of the FP64 ones) on the FP32 pipe, in
- * coordinates scaled by the source radius, and store them in FP64 (layouts 60 / 78 and the
- * self terms stay FP64: the double-float copy of their generated code would take ptxas
- * minutes to compile).  The forms whose residual is FP64 use these matrices. */
-ibem_status ibem_e3d_pair_blocks_form(ibem_solver_form form, const double* centers_dev,
-                                      const double* radius_dev, int num, const ibem_material* mat,
-                                      int layout, double* A_dev, int64_t lda, int64_t row0,
-                                      int64_t col0, void* stream);
-
 /* Solve A x = b in place of systemSolverElastic3D::solve (systemSolverElastic3D.h:44-60,
  * X = A.fullPivLu().solve(b)).  A_dev (N x N, column-major, lda) is overwritten by
  * factors (FP64 form) or left intact (mixed form); x_dev receives the solution.

@@ -2,7 +2,6 @@
 // oracle without a GPU (compiled by tests/test_codegen_host.py with the host compiler).
 #include <string.h>
 #include "gen_sphere24.cuh"
-#include "gen_sphere24_df.cuh"
 #include "gen_sphere60.cuh"
 #include "gen_sphere78.cuh"
 
@@ -41,34 +40,6 @@ extern "C" int hg_pair_block(int layout, const double* x, double a, double E0, d
   } else {
     return -1;
   }
-  return 0;
-}
-
-namespace {
-struct DfArrSink {
-  double* out;
-  int nu;
-  double scale;
-  void operator()(int r, int c, DF v) { out[r * nu + c] += scale * ibem::df_value(v); }
-};
-}  // namespace
-
-// The layout-24 pair block (no self term) the way the double-float pair kernels evaluate
-// it: coordinates divided by the source radius a, contrast moduli divided by mu0, each
-// (column order co, row order ro) sub-block times mu0 a^(co - ro).
-extern "C" int hg_pair_block24_df(const double* x, double a, double E0, double nu0, double E1, double nu1,
-                                  double* out) {
-  const SphMat mc = sph_mat_init(E0, nu0, E1, nu1);
-  SphMat ms = mc;
-  ms.kmu /= mc.mu0;
-  ms.klam /= mc.mu0;
-  memset(out, 0, sizeof(double) * 24 * 24);
-  const double y0 = x[0] / a, y1 = x[1] / a, y2 = x[2] / a;
-  DfArrSink s00{out, 24, mc.mu0}, s01{out, 24, mc.mu0 / a}, s10{out, 24, mc.mu0 * a}, s11{out, 24, mc.mu0};
-  sph_block24df_c0_r0(y0, y1, y2, 1.0, ms, s00);
-  sph_block24df_c0_r1(y0, y1, y2, 1.0, ms, s01);
-  sph_block24df_c1_r0(y0, y1, y2, 1.0, ms, s10);
-  sph_block24df_c1_r1(y0, y1, y2, 1.0, ms, s11);
   return 0;
 }
 

@@ -194,29 +194,3 @@ def test_field24_f32_far_pairs(hg):
         hg.hg_field24f32(d(cen + x), d(cen), ctypes.c_double(a), *_mat(), d(E), d(e2))
         worst = max(worst, scaled_err(e2, e1))
     assert worst < 3e-6, worst
-
-
-def test_double_float_pair_blocks_match_fp64(hg):
-    """The layout-24 blocks of the double-float pair kernels (radius-scaled coordinates,
-    moduli / mu0, sub-blocks times mu0 a^(co - ro)) against the FP64 generated blocks:
-    entry errors within 1e-12 of the block's largest entry, inside, near and far."""
-    import ctypes
-    hg.hg_pair_block24_df.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_double] + [ctypes.c_double] * 4 + \
-        [ctypes.POINTER(ctypes.c_double)]
-    rng = np.random.default_rng(11)
-    for dist in (0.3, 0.9, 1.05, 2.2, 6.0, 40.0):   # multiples of the radius (inside, touching, near, far)
-        for _ in range(4):
-            a = 0.012 * rng.uniform(0.8, 1.2)
-            v = rng.standard_normal(3)
-            x = v / np.linalg.norm(v) * dist * a
-            ref = np.zeros(24 * 24)
-            got = np.zeros(24 * 24)
-            mat = (70e9, 0.3, 70e9 * rng.uniform(2, 20), 0.2)
-            hg.hg_pair_block(24, d(x), ctypes.c_double(a), *[ctypes.c_double(v) for v in mat], 0, d(ref))
-            hg.hg_pair_block24_df(d(x), a, *mat, d(got))
-            ref = ref.reshape(24, 24)
-            got = got.reshape(24, 24)
-            for ro in (slice(0, 6), slice(6, 24)):
-                for co in (slice(0, 6), slice(6, 24)):
-                    r, g_ = ref[ro, co], got[ro, co]
-                    assert np.abs(g_ - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), (dist, ro, co)

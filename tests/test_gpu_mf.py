@@ -406,34 +406,3 @@ def test_field_grid_service_matches_point_list(B):
                                                 V(conn), c.NE, V(U), V(Tt), dp(sig), V(S2), None))
             torch.cuda.synchronize()
             assert torch.equal(S1, S2), form
-
-
-def test_double_float_pair_blocks_match_fp64(B):
-    """ibem_e3d_pair_blocks_form in the mixed form (double-float layout-24 blocks, stored in
-    FP64) against the FP64 blocks: every (particle pair, order pair) sub-block within 1e-12
-    of its largest entry; the self terms are the same FP64 code."""
-    import ctypes
-
-    import torch
-
-    import ibemproject_gb300 as g
-    c = small_cases([37], seed=13)[0]
-    n = 24 * c.num
-    cen = torch.from_numpy(np.ascontiguousarray(c.centers)).cuda()
-    rad = torch.from_numpy(np.ascontiguousarray(c.radius)).cuda()
-    m = g.material(c.E0, c.nu0, c.E1, c.nu1)
-    V = lambda t: ctypes.c_void_p(t.data_ptr())
-    A = {}
-    for form in (g.SOLVE_FP64, g.SOLVE_MIXED_IR):
-        A[form] = torch.zeros((n, n), dtype=torch.float64, device="cuda")
-        g.check(g.lib().ibem_e3d_pair_blocks_form(form, V(cen), V(rad), c.num, ctypes.byref(m), 24, V(A[form]), n, 0,
-                                                  0, None))
-    torch.cuda.synchronize()
-    ref = A[g.SOLVE_FP64].cpu().numpy().T.reshape(c.num, 24, c.num, 24)   # [s, row, h, col]
-    got = A[g.SOLVE_MIXED_IR].cpu().numpy().T.reshape(c.num, 24, c.num, 24)
-    for ro in (slice(0, 6), slice(6, 24)):
-        for co in (slice(0, 6), slice(6, 24)):
-            r = ref[:, ro][:, :, :, co]
-            e = np.abs(got[:, ro][:, :, :, co] - r).max(axis=(1, 3))
-            scale = np.abs(r).max(axis=(1, 3))
-            assert np.all(e <= 1e-12 * scale + 1e-300), (ro, co, float((e / np.maximum(scale, 1e-300)).max()))
