@@ -52,6 +52,24 @@ def test_run_dir_reads_reference_files(g):
     assert np.all(np.abs(S - z["stress"]) <= 1e-6 * np.abs(z["stress"]).max())
 
 
+def test_run_dir_from_side_car_matches_text(g):
+    """ibem_e3d_run_dir on the binary side-car (case.ibemb) writes the same stress.txt as on
+    the text files it was made from."""
+    from ibemproject_gb300 import cases
+    z = golden("tiny_reference.npz")
+    c = case_from_npz(z)
+    with tempfile.TemporaryDirectory() as d:
+        cases.write_case(d, c)
+        g.run_dir(d, layout=78)
+        text = open(os.path.join(d, "stress.txt")).read()
+        g.sidecar_from_txt(d)
+        for f in ("position.txt", "BEM.txt", "postprocess.txt"):
+            os.remove(os.path.join(d, f))
+        assert g.read_case_native(d)[1]
+        g.run_dir(d, layout=78)
+        assert open(os.path.join(d, "stress.txt")).read() == text
+
+
 @pytest.mark.parametrize("layout", [24, 60])
 def test_truncated_layouts_vs_oracle(g, oracle_mod, layout):
     """Layouts without a reference counterpart: the same entries, truncated (24) or with
