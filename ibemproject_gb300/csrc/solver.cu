@@ -1414,6 +1414,8 @@ __global__ void k_scale_rows_of_parts(int64_t n, int nparts, const double* __res
 // columns per iteration summed in FP32, those partial sums added in FP64 (GB300 runs FP64 at
 // a small fraction of its FP32 rate, so FP64 multiply-adds would bound this product).
 // Requires ldw % 4 == 0 and W 16-byte aligned.
+// ABS: row sums of |W| instead (x unused), for the norm of the backward error.
+template <bool ABS>
 __global__ void __launch_bounds__(256) k_gemv_f32acc(int64_t n, const float* __restrict__ W, int64_t ldw,
                                                      const float* __restrict__ x, int64_t chunk,
                                                      double* __restrict__ part) {
@@ -1429,22 +1431,30 @@ __global__ void __launch_bounds__(256) k_gemv_f32acc(int64_t n, const float* __r
     float t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f;
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
-      const float xv = x[j + u];
-      t0 = fmaf(a[u].x, xv, t0);
-      t1 = fmaf(a[u].y, xv, t1);
-      t2 = fmaf(a[u].z, xv, t2);
-      t3 = fmaf(a[u].w, xv, t3);
+      if (ABS) {
+        t0 += fabsf(a[u].x), t1 += fabsf(a[u].y), t2 += fabsf(a[u].z), t3 += fabsf(a[u].w);
+      } else {
+        const float xv = x[j + u];
+        t0 = fmaf(a[u].x, xv, t0);
+        t1 = fmaf(a[u].y, xv, t1);
+        t2 = fmaf(a[u].z, xv, t2);
+        t3 = fmaf(a[u].w, xv, t3);
+      }
     }
     s[0] += t0, s[1] += t1, s[2] += t2, s[3] += t3;
   }
   float t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f;
   for (; j < j1; ++j) {
     const float4 a = *reinterpret_cast<const float4*>(W + j * ldw + i0);
-    const float xv = x[j];
-    t0 = fmaf(a.x, xv, t0);
-    t1 = fmaf(a.y, xv, t1);
-    t2 = fmaf(a.z, xv, t2);
-    t3 = fmaf(a.w, xv, t3);
+    if (ABS) {
+      t0 += fabsf(a.x), t1 += fabsf(a.y), t2 += fabsf(a.z), t3 += fabsf(a.w);
+    } else {
+      const float xv = x[j];
+      t0 = fmaf(a.x, xv, t0);
+      t1 = fmaf(a.y, xv, t1);
+      t2 = fmaf(a.z, xv, t2);
+      t3 = fmaf(a.w, xv, t3);
+    }
   }
   s[0] += t0, s[1] += t1, s[2] += t2, s[3] += t3;
 #pragma unroll
@@ -1817,7 +1827,15 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
       }
     }
     cudaEventRecord(e1, st);
-    if (!s) s = finish_norm();
+    if (!s) {  // ||As||_inf from the FP32 copy: a denominator of the backward error, FP32 sums are ample
+      const int64_t chunk = (N + cx.nparts - 1) / cx.nparts;
+      ::ibem::count_launch(), k_gemv_f32acc<true><<<dim3((unsigned)((N + 1023) / 1024), (unsigned)cx.nparts), 256, 0,
+                                                     st>>>(N, W, ldw, nullptr, chunk, cx.part);
+      ::ibem::count_launch(), k_scale_rows_of_parts<<<nb, 256, 0, st>>>(N, cx.nparts, cx.part, nullptr, cx.rs);
+      std::vector<double> h;
+      s = vec_to_host(cx.rs, N, h, st);
+      as_norm = host_absmax(h);
+    }
     if (!s) IBEM_CUDA(cudaMemsetAsync(ys, 0, sizeof(double) * N, st));
     auto prec = [&](const double* v, double* z) -> ibem_status {
       ::ibem::count_launch(), k_bj_apply<<<(unsigned)nblk, kBjApplyThreads, 0, st>>>(N, block, P, v, z);
@@ -1828,8 +1846,8 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
       ProfScope ps(PROF_MATVEC, st, 2.0 * N * N);
       const int64_t chunk = (N + cx.nparts - 1) / cx.nparts;
       ::ibem::count_launch(), k_d2f<<<nb, 256, 0, st>>>(N, z, zf);
-      ::ibem::count_launch(), k_gemv_f32acc<<<dim3((unsigned)((N + 1023) / 1024), (unsigned)cx.nparts), 256, 0, st>>>(
-          N, W, ldw, zf, chunk, cx.part);
+      ::ibem::count_launch(), k_gemv_f32acc<false><<<dim3((unsigned)((N + 1023) / 1024), (unsigned)cx.nparts), 256, 0,
+                                                      st>>>(N, W, ldw, zf, chunk, cx.part);
       ::ibem::count_launch(), k_scale_rows_of_parts<<<nb, 256, 0, st>>>(N, cx.nparts, cx.part, nullptr, wv);
       IBEM_LAUNCH_CHECK("FP32 product");
       return IBEM_OK;
