@@ -77,3 +77,21 @@ def test_unreachable_packing_is_an_error():
                 g.GenParams(10, 0.008, 1.2, 0.8, 0.2, 0.1, g.GEN_MC, 1, 0, 0),
                 g.GenParams(10, 0.008, 0.8, 1.2, 0.2, 0.1, 7, 1, 0, 0)):
         assert L.ibem_e3d_generate_spheres(ctypes.byref(bad), dp(C), dp(R), None) == 1
+
+
+def test_matrix_free_helpers_refuse_quadratic_batches():
+    """The matrix-free solver and the learned preconditioner take layout 24 only: the Python
+    helpers refuse a layout-60 batch before any library call; its row ranges follow the
+    layout."""
+    import torch
+
+    from ibemproject_gb300 import batch as B
+    from ibemproject_gb300 import cases
+    cs = [cases.generated_case(n, 0.008, 0.2, seed=n) for n in (3, 5)]
+    bt = B.DeviceBatch(cs, device="cpu", layout=60)
+    assert bt.N == 60 * 8 and bt.seg_rows(1) == slice(180, 480)
+    b = torch.zeros(bt.N, dtype=torch.float64)
+    for call in (lambda: B.solve(bt, b), lambda: B.matvec(bt, b), lambda: B.tuning(bt),
+                 lambda: B.training_pairs(bt, 1), lambda: B.training_pairs_mf(bt, 1), lambda: B.prepare(bt)):
+        with pytest.raises(ValueError):
+            call()
