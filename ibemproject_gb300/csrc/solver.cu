@@ -708,22 +708,6 @@ __global__ void k_abs_rowsum_part(int64_t n, const double* __restrict__ A, int64
   for (int64_t j = j0; j < j1; ++j) s += fabs(A[j * lda + i]) * c[j];
   part[blockIdx.y * n + i] = s;
 }
-// Partial products of the FP32 scaled matrix with an FP64 vector over a column chunk,
-// accumulated in FP64 (finished by k_scale_rows_of_parts with r = nullptr).
-__global__ void k_gemv_part_f32(int64_t n, const float* __restrict__ W, int64_t ldw, const double* __restrict__ x,
-                                int64_t chunk, double* __restrict__ part) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
-  if (i >= n) return;
-  double s0 = 0, s1 = 0;
-  int64_t j = j0;
-  for (; j + 1 < j1; j += 2) {
-    s0 += (double)W[j * ldw + i] * x[j];
-    s1 += (double)W[(j + 1) * ldw + i] * x[j + 1];
-  }
-  if (j < j1) s0 += (double)W[j * ldw + i] * x[j];
-  part[blockIdx.y * n + i] = s0 + s1;
-}
 
 // Column-chunk reductions over a column-major matrix with 16-byte loads: thread t covers the
 // kV = 16 / sizeof(T) consecutive rows kV t .. kV t + kV - 1, eight columns per iteration,
@@ -1282,11 +1266,9 @@ static ibem_status colreduce(int64_t N, const T* A, int64_t lda, const double* x
     ::ibem::count_launch(), k_colreduce_v<T, MODE><<<dim3((unsigned)((rows + 255) / 256), (unsigned)nparts), 256, 0,
                                                     st>>>(N, A, lda, x, chunk, part);
   } else {
-    static_assert(MODE == 0 || sizeof(T) == 8, "unaligned FP32 reductions are dot products only");
+    static_assert(sizeof(T) == 8, "the one-element-per-load fallback reads FP64 matrices");
     const dim3 grid((unsigned)((N + 255) / 256), (unsigned)nparts);
-    if constexpr (sizeof(T) == 4)
-      ::ibem::count_launch(), k_gemv_part_f32<<<grid, 256, 0, st>>>(N, A, lda, x, chunk, part);
-    else if constexpr (MODE == 0)
+    if constexpr (MODE == 0)
       ::ibem::count_launch(), k_gemv_part<<<grid, 256, 0, st>>>(N, A, lda, x, chunk, part);
     else if constexpr (MODE == 1)
       ::ibem::count_launch(), k_rowmax_part<<<grid, 256, 0, st>>>(N, A, lda, chunk, part);
