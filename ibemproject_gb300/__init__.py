@@ -95,6 +95,7 @@ SIGNATURES = {
     "ibem_e3d_solve_bj": (_int, [_i64, _int, _vp, _i64, _vp, _vp, _dbl, ctypes.POINTER(SolveReport), _vp]),
     "ibem_gemm_sub_f32": (_int, [_i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp]),
     "ibem_e3d_solve_noalloc": (_int, [_i64, _vp, _i64, _vp, _vp, ctypes.POINTER(SolveReport), _vp]),
+    "ibem_selftest_bounded_wait": (_int, [_int, ctypes.c_longlong, _vp]),
     "ibem_e3d_field": (_int, [_vp, _int, _vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _vp, _int, _vp,
                               _int, _vp, _vp, _c_dp, _vp, _vp]),
     "ibem_e3d_field_form": (_int, [_int, _vp, _int, _vp, _vp, _int, ctypes.POINTER(Material), _int, _vp, _vp, _int,

@@ -60,11 +60,6 @@ class Case:
     def n_unknowns(self, layout: int) -> int:
         return 3 * self.NN + layout * self.num
 
-    def orc_mat(self):
-        """Material record for the oracle (test infrastructure)."""
-        import oracle  # noqa: WPS433 -- resolved from the repo root by the tests
-        return oracle.mat(self.E0, self.nu0, self.E1, self.nu1)
-
 
 def _lines(path: str) -> list[str]:
     with open(path, "rb") as f:

@@ -16,6 +16,7 @@
 //                Gauss point: a per-call quadrature table (point, normal, weight x Jacobian,
 //                interpolated U and T per Gauss point) staged through shared memory, one
 //                thread per sample point.
+#include <algorithm>
 #include <cuda_runtime.h>
 
 #include "gen_bem.cuh"
@@ -108,9 +109,12 @@ struct KelvinC {
 };
 
 // Integ3 for one (collocation node, element): dU, dT (3 x 12), BEMBuilderElastic3D.cpp:1169-1353
+// The traction part of this element is written to TG, laid out like G (column 12e + 3a + j,
+// row 3i + ii; zero for the singular corner); node_gather then sums the columns of the
+// elements that share a node in a fixed order, so H is the same bit for bit on every run.
 __global__ void __launch_bounds__(128) bem_hg_kernel(const double* __restrict__ nodes, int NN,
                                                      const int* __restrict__ conn, KelvinC kc,
-                                                     double* __restrict__ H, int64_t ldh,
+                                                     double* __restrict__ TG, int64_t ldt,
                                                      double* __restrict__ G, int64_t ldg) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int e = blockIdx.y;
@@ -160,20 +164,98 @@ __global__ void __launch_bounds__(128) bem_hg_kernel(const double* __restrict__ 
             }
           }
       }
-  // G columns of this element (overwrite); H node columns (accumulate)
+  // G columns of this element, and its traction columns for H (summed per node by node_gather)
 #pragma unroll
   for (int ii = 0; ii < 3; ++ii)
 #pragma unroll
-    for (int k = 0; k < 12; ++k) G[(12 * (int64_t)e + k) * ldg + 3 * i + ii] = dU[ii][k];
-#pragma unroll
-  for (int n = 0; n < 4; ++n)
-#pragma unroll
-    for (int jj = 0; jj < 3; ++jj) {
-      double* col = H + (3 * (int64_t)(sc[n] - 1) + jj) * ldh + 3 * i;
-#pragma unroll
-      for (int ii = 0; ii < 3; ++ii)
-        if (l_pi < 0 || n != l_pi) atomicAdd(col + ii, dT[ii][3 * n + jj]);
+    for (int k = 0; k < 12; ++k) {
+      G[(12 * (int64_t)e + k) * ldg + 3 * i + ii] = dU[ii][k];
+      TG[(12 * (int64_t)e + k) * ldt + 3 * i + ii] = (l_pi < 0 || k / 3 != l_pi) ? dT[ii][k] : 0.0;
     }
+}
+
+// ---- node incidence: the (element, corner) slots of every node, in increasing order ----
+// inc_start[c] .. inc_start[c + 1] - 1 index inc_slot, whose entries are 4e + a for the
+// corners a of elements e at node c.  Built with integer atomics, then each node's list is
+// sorted, so the order (and every sum over it) does not depend on scheduling.
+__global__ void k_inc_count(const int* __restrict__ conn, int NE, int NN, int* __restrict__ cnt) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= 4 * NE) return;
+  const int c = conn[id] - 1;
+  if (c >= 0 && c < NN) atomicAdd(cnt + c, 1);
+}
+
+// exclusive prefix sum of n counts into start[0..n] (one block, sequential chunks)
+__global__ void k_inc_scan(const int* __restrict__ cnt, int n, int* __restrict__ start) {
+  __shared__ int sh[1024];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < n; base += 1024) {
+    const int i = base + threadIdx.x;
+    const int v = i < n ? cnt[i] : 0;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+      const int t = threadIdx.x >= off ? sh[threadIdx.x - off] : 0;
+      __syncthreads();
+      sh[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < n) start[i] = carry + sh[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry += sh[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) start[n] = carry;
+}
+
+__global__ void k_inc_fill(const int* __restrict__ conn, int NE, int NN, const int* __restrict__ start,
+                           int* __restrict__ cursor, int* __restrict__ slot) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= 4 * NE) return;
+  const int c = conn[id] - 1;
+  if (c < 0 || c >= NN) return;
+  slot[start[c] + atomicAdd(cursor + c, 1)] = id;
+}
+
+__global__ void k_inc_sort(int NN, const int* __restrict__ start, int* __restrict__ slot) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= NN) return;
+  for (int i = start[c] + 1; i < start[c + 1]; ++i) {
+    const int v = slot[i];
+    int j = i - 1;
+    while (j >= start[c] && slot[j] > v) { slot[j + 1] = slot[j]; --j; }
+    slot[j + 1] = v;
+  }
+}
+
+// H[(3c + d) ldh + r] (+)= sum over node c's slots 4e + a, in order, of S[(12e + 3a + d) lds + r]
+// for rows r < nrows; the element columns of S are laid out like G.
+__global__ void __launch_bounds__(256) k_node_gather(int64_t nrows, int NN, const int* __restrict__ start,
+                                                     const int* __restrict__ slot, const double* __restrict__ S,
+                                                     int64_t lds, double* __restrict__ H, int64_t ldh, int accumulate) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  for (int c = blockIdx.y; c < NN; c += gridDim.y) {
+    double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
+    for (int q = start[c]; q < start[c + 1]; ++q) {
+      const int64_t col = 3 * (int64_t)slot[q];   // 12e + 3a
+      acc0 += S[col * lds + r];
+      acc1 += S[(col + 1) * lds + r];
+      acc2 += S[(col + 2) * lds + r];
+    }
+    double* h = H + 3 * (int64_t)c * ldh + r;
+    if (accumulate) {
+      h[0] += acc0;
+      h[ldh] += acc1;
+      h[2 * ldh] += acc2;
+    } else {
+      h[0] = acc0;
+      h[ldh] = acc1;
+      h[2 * ldh] = acc2;
+    }
+  }
 }
 
 // Rigid-body diagonal (:1478-1501): H(r, 3i+l) = -sum_c H(r, c) over columns c with c%3 == l.
@@ -234,10 +316,12 @@ __device__ __forceinline__ void stress_dispatch(int f, double x0, double x1, dou
 
 // blockIdx.z = W index * 3 + dof.  Rows of the layout: order 0 -> t; order 1 -> 6 + 3t + w;
 // order 2 -> 24 + 9t + 3w + z (layout 78) or 24 + 6t + pairidx(w<=z) (layout 60).
+// The displacement part (the H rows) is written per element into UG, laid out like G;
+// node_gather sums it per node in a fixed element order (no atomics on matrix entries).
 template <int ORDER>
 __global__ void __launch_bounds__(128) bem_incl_kernel(
     const double* __restrict__ nodes, int NN, const int* __restrict__ conn, const double* __restrict__ cen,
-    int num, BemMat bm, int nu, int compact, double* __restrict__ H, int64_t ldh,
+    int num, BemMat bm, int nu, int compact, double* __restrict__ UG, int64_t ldu,
     double* __restrict__ G, int64_t ldg) {
   const int K = blockIdx.x * blockDim.x + threadIdx.x;
   const int e = blockIdx.y;
@@ -281,7 +365,7 @@ __global__ void __launch_bounds__(128) bem_incl_kernel(
     const int64_t row = (int64_t)nu * K + r;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-      atomicAdd(H + (3 * (int64_t)(sc[a] - 1) + n) * ldh + row, -fac * au[t][a]);
+      UG[(12 * (int64_t)e + 3 * a + n) * ldu + row] = -fac * au[t][a];   // summed per node by node_gather
       G[(12 * (int64_t)e + 3 * a + n) * ldg + row] = fac * at[t][a];
     }
   }
@@ -363,12 +447,46 @@ __global__ void __launch_bounds__(128) bem_post_kernel(const double* __restrict_
 
 namespace ibem {
 
+// Node incidence lists of the mesh (see k_inc_*), in stream-ordered memory freed by the caller
+// with cudaFreeAsync: *start (NN + 1 ints) then the slots (4 NE ints) in one allocation.
+static ibem_status node_incidence(const int* conn, int NN, int NE, int** start, int** slot, cudaStream_t st) {
+  int* buf = nullptr;
+  const size_t n = (size_t)(NN + 1) + 2 * (size_t)NN + 4 * (size_t)NE;
+  IBEM_CUDA(cudaMallocAsync((void**)&buf, sizeof(int) * n, st));
+  int* s0 = buf;
+  int* cnt = s0 + NN + 1;
+  int* cur = cnt + NN;
+  int* sl = cur + NN;
+  IBEM_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * 2 * (size_t)NN, st));
+  const unsigned g4 = (unsigned)((4 * (int64_t)NE + 255) / 256);
+  if (NE > 0) ::ibem::count_launch(), k_inc_count<<<g4, 256, 0, st>>>(conn, NE, NN, cnt);
+  ::ibem::count_launch(), k_inc_scan<<<1, 1024, 0, st>>>(cnt, NN, s0);
+  if (NE > 0) ::ibem::count_launch(), k_inc_fill<<<g4, 256, 0, st>>>(conn, NE, NN, s0, cur, sl);
+  ::ibem::count_launch(), k_inc_sort<<<(NN + 255) / 256, 256, 0, st>>>(NN, s0, sl);
+  IBEM_LAUNCH_CHECK("node incidence");
+  *start = s0;
+  *slot = sl;
+  return IBEM_OK;
+}
+
+static dim3 gather_grid(int64_t nrows, int NN) {
+  return dim3((unsigned)((nrows + 255) / 256), (unsigned)std::min(NN, 65535));
+}
+
 ibem_status bem_hg(const double* nodes, int NN, const int* conn, int NE, const ibem_material& m,
                    double* H, int64_t ldh, int64_t hrow0, int64_t hcol0, double* G, int64_t ldg,
                    int64_t grow0, int64_t gcol0, cudaStream_t st) {
   double* Hb = H + hcol0 * ldh + hrow0;
   double* Gb = G + gcol0 * ldg + grow0;
-  IBEM_CUDA(cudaMemset2DAsync(Hb, ldh * sizeof(double), 0, 3 * (size_t)NN * sizeof(double), 3 * (size_t)NN, st));
+  if (NN <= 0) return IBEM_OK;
+  const int64_t ldt = 3 * (int64_t)NN;
+  double* TG = nullptr;
+  const size_t tg_bytes = sizeof(double) * ldt * 12 * (size_t)(NE > 0 ? NE : 1);
+  IBEM_CUDA(cudaMallocAsync((void**)&TG, tg_bytes, st));
+  IBEM_CUDA(cudaMemsetAsync(TG, 0, tg_bytes, st));   // an element with bad connectivity adds nothing
+  int *start = nullptr, *slot = nullptr;
+  ibem_status s = node_incidence(conn, NN, NE, &start, &slot, st);
+  if (s) { cudaFreeAsync(TG, st); return s; }
   const double mu = m.E0 / (2 * (1 + m.nu0));
   KelvinC kc;
   kc.cu = 1.0 / (16 * IBEM_PI * mu * (1 - m.nu0));
@@ -376,8 +494,11 @@ ibem_status bem_hg(const double* nodes, int NN, const int* conn, int NE, const i
   kc.ct = 1.0 / (8 * IBEM_PI * (1 - m.nu0));
   kc.c3 = 1 - 2 * m.nu0;
   dim3 grid((NN + 127) / 128, NE);
-  ::ibem::count_launch(), bem_hg_kernel<<<grid, 128, 0, st>>>(nodes, NN, conn, kc, Hb, ldh, Gb, ldg);
+  if (NE > 0) ::ibem::count_launch(), bem_hg_kernel<<<grid, 128, 0, st>>>(nodes, NN, conn, kc, TG, ldt, Gb, ldg);
+  ::ibem::count_launch(), k_node_gather<<<gather_grid(ldt, NN), 256, 0, st>>>(ldt, NN, start, slot, TG, ldt, Hb, ldh, 0);
   ::ibem::count_launch(), bem_diag_kernel<<<(3 * NN + 127) / 128, 128, 0, st>>>(NN, Hb, ldh);
+  cudaFreeAsync(start, st);
+  cudaFreeAsync(TG, st);
   IBEM_LAUNCH_CHECK("bem_hg");
   return IBEM_OK;
 }
@@ -390,11 +511,23 @@ ibem_status bem_to_incl(const double* nodes, int NN, const int* conn, int NE, co
   double* Hb = H + hcol0 * ldh + row0;
   double* Gb = G + gcol0 * ldg + row0;
   const int compact = layout == 60;
+  if (NN <= 0 || NE <= 0 || num <= 0) return IBEM_OK;
+  const int64_t rows = (int64_t)layout * num;
+  double* UG = nullptr;
+  const size_t ug_bytes = sizeof(double) * rows * 12 * (size_t)NE;
+  IBEM_CUDA(cudaMallocAsync((void**)&UG, ug_bytes, st));
+  IBEM_CUDA(cudaMemsetAsync(UG, 0, ug_bytes, st));   // an element with bad connectivity adds nothing
+  int *start = nullptr, *slot = nullptr;
+  ibem_status s = node_incidence(conn, NN, NE, &start, &slot, st);
+  if (s) { cudaFreeAsync(UG, st); return s; }
   dim3 g0((num + 127) / 128, NE, 3), g1((num + 127) / 128, NE, 9), g2((num + 127) / 128, NE, 27);
-  ::ibem::count_launch(), bem_incl_kernel<0><<<g0, 128, 0, st>>>(nodes, NN, conn, cen, num, bm, layout, compact, Hb, ldh, Gb, ldg);
-  ::ibem::count_launch(), bem_incl_kernel<1><<<g1, 128, 0, st>>>(nodes, NN, conn, cen, num, bm, layout, compact, Hb, ldh, Gb, ldg);
+  ::ibem::count_launch(), bem_incl_kernel<0><<<g0, 128, 0, st>>>(nodes, NN, conn, cen, num, bm, layout, compact, UG, rows, Gb, ldg);
+  ::ibem::count_launch(), bem_incl_kernel<1><<<g1, 128, 0, st>>>(nodes, NN, conn, cen, num, bm, layout, compact, UG, rows, Gb, ldg);
   if (layout != 24)
-    ::ibem::count_launch(), bem_incl_kernel<2><<<g2, 128, 0, st>>>(nodes, NN, conn, cen, num, bm, layout, compact, Hb, ldh, Gb, ldg);
+    ::ibem::count_launch(), bem_incl_kernel<2><<<g2, 128, 0, st>>>(nodes, NN, conn, cen, num, bm, layout, compact, UG, rows, Gb, ldg);
+  ::ibem::count_launch(), k_node_gather<<<gather_grid(rows, NN), 256, 0, st>>>(rows, NN, start, slot, UG, rows, Hb, ldh, 1);
+  cudaFreeAsync(start, st);
+  cudaFreeAsync(UG, st);
   IBEM_LAUNCH_CHECK("bem_to_incl");
   return IBEM_OK;
 }

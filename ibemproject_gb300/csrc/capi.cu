@@ -324,6 +324,12 @@ ibem_status ibem_gemm_sub_f32(int64_t m, int64_t n, int64_t k, const float* A_de
   return s;
 }
 
+ibem_status ibem_selftest_bounded_wait(int which, long long limit, void* stream) {
+  if (which == 0) return selftest_flag_wait(limit, as_stream(stream));
+  if (which == 1) return selftest_mbar_wait(limit, as_stream(stream));
+  return fail(IBEM_ERR_ARG, "selftest_bounded_wait: which must be 0 (panel flag) or 1 (GEMM mbarrier)");
+}
+
 ibem_status ibem_e3d_solve_noalloc(int64_t N, const double* A_dev, int64_t lda, const double* b_dev,
                                    double* x_dev, ibem_solve_report* report, void* stream) {
   return solve_fp64_noalloc(N, A_dev, lda, b_dev, x_dev, report, as_stream(stream));

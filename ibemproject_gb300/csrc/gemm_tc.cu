@@ -100,8 +100,8 @@ __device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
   return done != 0;
 }
 // bounded wait; false (and the error flag raised) on time-out or when another thread failed
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
-  for (long long it = 0; it < kWaitLimit; ++it) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, long long limit = kWaitLimit) {
+  for (long long it = 0; it < limit; ++it) {
     if (mbar_test(bar, parity)) return true;
     if ((it & 255) == 255 && *reinterpret_cast<volatile int*>(err) != 0) return false;
   }
@@ -315,7 +315,37 @@ ibem_status encode_map(CUtensorMap* map, const __nv_bfloat16* ptr, int64_t rows,
   return IBEM_OK;
 }
 
+// Self-test of the bounded mbarrier wait: one thread waits, with the same mbar_wait, on a
+// freshly initialised barrier that nobody arrives at; the wait must give up and raise err.
+__global__ void k_selftest_mbar_wait(int* err, long long limit) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  const uint32_t b = smem_u32(&bar);
+  mbar_init(b, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  mbar_wait(b, 0, err, limit);
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(b) : "memory");
+}
+
 }  // namespace
+
+ibem_status selftest_mbar_wait(long long limit, cudaStream_t st) {
+  if (limit < 1 || limit > kWaitLimit) return fail(IBEM_ERR_ARG, "selftest_mbar_wait: limit outside 1..2^22 polls");
+  int* err = nullptr;
+  IBEM_CUDA(cudaMalloc(&err, sizeof(int)));
+  int h = 0;
+  cudaError_t ce = cudaMemsetAsync(err, 0, sizeof(int), st);
+  if (ce == cudaSuccess) {
+    ::ibem::count_launch(), k_selftest_mbar_wait<<<1, 32, 0, st>>>(err, limit);
+    ce = cudaGetLastError();
+  }
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+  cudaFree(err);
+  if (ce != cudaSuccess) return cuda_fail(ce, "selftest_mbar_wait");
+  if (h) return fail(IBEM_ERR_TIMEOUT, "selftest_mbar_wait: the bounded wait gave up (expected)");
+  return IBEM_OK;
+}
 
 size_t gemm_tc_workspace_bytes(int64_t max_m, int64_t max_n) {
   const int64_t kp = kMaxKChunk;

@@ -241,12 +241,13 @@ __device__ __forceinline__ void calu_elim(T (&a)[R][kLeaf], bool (&live)[R], int
   __syncthreads();
 }
 
-// one polling thread per flag: threads t < n wait for flags[t] == tag (bounded)
-__device__ __forceinline__ void calu_wait(const int* flags, int n, int tag, GridSync* gs, int* s_fail) {
+// one polling thread per flag: threads t < n wait for flags[t] == tag (bounded by limit polls)
+__device__ __forceinline__ void calu_wait(const int* flags, int n, int tag, GridSync* gs, int* s_fail,
+                                          long long limit = kSpinLimit) {
   if ((int)threadIdx.x < n) {
     long long it = 0;
     while (ld_acquire_s32(flags + threadIdx.x) != tag) {
-      if (++it > kSpinLimit || *reinterpret_cast<volatile int*>(&gs->err) != 0) {
+      if (++it > limit || *reinterpret_cast<volatile int*>(&gs->err) != 0) {
         atomicExch(&gs->err, 1);
         *s_fail = 1;
         break;
@@ -1943,10 +1944,13 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
 // panel kernel's candidate rows and grid barrier, residual scratch) lives in one
 // file-scope static __device__ array of kNoAllocBytes, so N is limited to kNoAllocMaxN.
 // The array is held by every GPU that loads the library until the process exits.
-// Its device address is looked up once per device, on that device's first call
-// (cudaGetSymbolAddress); make that first call before any stream capture.  All calls
-// share the array and it keeps the last call's contents: calls that overlap on the GPU
-// (other host threads, other streams) race and must be serialised by the caller.
+// The first call on a device sets that device up (launch shapes from occupancy
+// queries); make that first call before any stream capture.  The array's device
+// address is looked up on every call (cudaGetSymbolAddress, which allocates nothing),
+// so it stays valid after the module is reloaded.  The call waits for its stream before
+// it returns, because it reads the solve's status back to the host.  All calls share
+// the array and it keeps the last call's contents: calls that overlap on the GPU (other
+// host threads, other streams) race and must be serialised by the caller.
 // ===================================================================================
 namespace {
 constexpr int64_t kNoAllocMaxN = 1024;
@@ -1970,7 +1974,7 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
-unsigned char* g_noalloc_base[kNoAllocMaxDevices] = {};
+bool g_noalloc_ready[kNoAllocMaxDevices] = {};
 int g_noalloc_ncta[kNoAllocMaxDevices] = {};
 int g_noalloc_trsv_grid[kNoAllocMaxDevices] = {};
 
@@ -2012,9 +2016,10 @@ __global__ void k_absmax4(int64_t n, const double* __restrict__ a, const double*
 static ibem_status noalloc_setup(int dev, unsigned char** base, int* ncta, int* trsv_grid) {
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(IBEM_ERR_ARG, "solve_noalloc: device index out of range");
-  if (!g_noalloc_base[dev]) {
-    void* p = nullptr;
-    IBEM_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+  void* p = nullptr;
+  IBEM_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+  if (!p) return fail(IBEM_ERR_CUDA, "solve_noalloc: no device address for the static workspace");
+  if (!g_noalloc_ready[dev]) {
     int nsm = 0;
     IBEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     IBEM_CUDA(set_solver_smem_attrs<double>());
@@ -2027,9 +2032,9 @@ static ibem_status noalloc_setup(int dev, unsigned char** base, int* ncta, int* 
     if (per_tr < 1) return fail(IBEM_ERR_CUDA, "solve_noalloc: triangular-solve kernel cannot be resident");
     g_noalloc_trsv_grid[dev] = per_tr * nsm;
     g_noalloc_ncta[dev] = std::min(nsm, kCaluMaxCta);
-    g_noalloc_base[dev] = static_cast<unsigned char*>(p);
+    g_noalloc_ready[dev] = true;
   }
-  *base = g_noalloc_base[dev];
+  *base = static_cast<unsigned char*>(p);
   *ncta = g_noalloc_ncta[dev];
   *trsv_grid = g_noalloc_trsv_grid[dev];
   return IBEM_OK;
@@ -2112,6 +2117,42 @@ ibem_status solve_fp64_noalloc(int64_t N, const double* A, int64_t lda, const do
   }
   if (hgs.err) return fail(IBEM_ERR_TIMEOUT, "solve_noalloc: a bounded wait of the panel or triangular-solve kernel gave up");
   if (hinfo) return fail(IBEM_ERR_SINGULAR, "solve_noalloc: zero pivot");
+  return IBEM_OK;
+}
+
+// ===================================================================================
+// Self-test of the panel kernel's bounded flag wait: one CTA waits, with the same
+// calu_wait, for a flag that nothing sets.  The wait must give up after `limit` polls,
+// raise the sticky error flag and return, so the host sees IBEM_ERR_TIMEOUT and the
+// context stays usable.
+// ===================================================================================
+namespace {
+__global__ void k_selftest_flag_wait(const int* flags, GridSync* gs, long long limit, int* s_out) {
+  __shared__ int s_fail;
+  if (threadIdx.x == 0) s_fail = 0;
+  __syncthreads();
+  calu_wait(flags, 1, 1, gs, &s_fail, limit);
+  if (threadIdx.x == 0) *s_out = s_fail;
+}
+}  // namespace
+
+ibem_status selftest_flag_wait(long long limit, cudaStream_t st) {
+  if (limit < 1 || limit > kSpinLimit) return fail(IBEM_ERR_ARG, "selftest_flag_wait: limit outside 1..2^22 polls");
+  int* d = nullptr;   // [0] the flag nothing sets, [1] GridSync, [2] the CTA's failure record
+  IBEM_CUDA(cudaMalloc(&d, 4 * sizeof(int)));
+  ibem_status s = IBEM_OK;
+  int h[4] = {0, 0, 0, 0};
+  cudaError_t ce = cudaMemsetAsync(d, 0, 4 * sizeof(int), st);
+  if (ce == cudaSuccess) {
+    ::ibem::count_launch(), k_selftest_flag_wait<<<1, 32, 0, st>>>(d, reinterpret_cast<GridSync*>(d + 1), limit, d + 2);
+    ce = cudaGetLastError();
+  }
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost, st);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+  if (ce != cudaSuccess) s = cuda_fail(ce, "selftest_flag_wait");
+  cudaFree(d);
+  if (s) return s;
+  if (h[1] && h[2]) return fail(IBEM_ERR_TIMEOUT, "selftest_flag_wait: the bounded wait gave up (expected)");
   return IBEM_OK;
 }
 

@@ -28,4 +28,9 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
 ibem_status solve_fp64_noalloc(int64_t N, const double* A, int64_t lda, const double* b, double* x,
                                ibem_solve_report* rep, cudaStream_t st);
 
+// Self-tests of the bounded device-side waits (a wait on a flag / an mbarrier that nothing
+// completes, given up after `limit` polls): IBEM_ERR_TIMEOUT when the wait gave up.
+ibem_status selftest_flag_wait(long long limit, cudaStream_t st);
+ibem_status selftest_mbar_wait(long long limit, cudaStream_t st);
+
 }  // namespace ibem

@@ -183,11 +183,21 @@ ibem_status ibem_gemm_sub_f32(int64_t m, int64_t n, int64_t k, const float* A_de
  * cudaMalloc/cudaFree can stall the device.  The caller owns A_dev (left intact), b_dev
  * and x_dev; the rest of the workspace is one static device array of about 11 MB inside
  * the library, held by every GPU that loads it until the process exits, which limits N
- * to 1024 (larger N returns IBEM_ERR_ARG).  The first call on a device looks the array's
- * address up (setup), so make it before any stream capture.  Every call reuses the same
- * array: calls that overlap on the GPU (from several host threads or streams) race and
- * must be serialised by the caller.  Synchronous; report gets the scaled backward error
- * and info as for ibem_e3d_solve (timings are left 0). */
+ * to 1024 (larger N returns IBEM_ERR_ARG).  The first call on a device sets that device
+ * up (launch shapes), so make it before any stream capture; every call looks the array's
+ * device address up again (no allocation).  Every call reuses the same array: calls that
+ * overlap on the GPU (from several host threads or streams) race and must be serialised
+ * by the caller.  The call waits for its stream before it returns (it reads the solve's
+ * status back); report gets the scaled backward error and info as for ibem_e3d_solve
+ * (timings are left 0). */
+/* Self-test of the bounded device-side waits (no reference counterpart; the reference
+ * has no device code).  which = 0: one CTA waits, with the panel kernel's flag wait, for a
+ * flag that nothing sets; which = 1: one thread waits, with the tensor-core GEMM's mbarrier
+ * wait, on a barrier nobody arrives at.  Each wait gives up after `limit` polls
+ * (1 .. 2^22, the production limit), raises the kernel's error flag and returns, so the
+ * call returns IBEM_ERR_TIMEOUT and the context stays usable.  Synchronous. */
+ibem_status ibem_selftest_bounded_wait(int which, long long limit, void* stream);
+
 ibem_status ibem_e3d_solve_noalloc(int64_t N, const double* A_dev, int64_t lda, const double* b_dev,
                                    double* x_dev, ibem_solve_report* report, void* stream);
 

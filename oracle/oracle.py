@@ -34,10 +34,20 @@ def build(quiet: bool = True) -> str:
     return LIB_PATH
 
 
+def reference_dir() -> str | None:
+    """The reference checkout: IBEM_REFERENCE_DIR, else a directory named ``reference``
+    beside the repository; None when neither holds the reference's sources."""
+    cands = [os.environ.get("IBEM_REFERENCE_DIR"), os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")]
+    for d in cands:
+        if d and os.path.isfile(os.path.join(d, "integratorElastic3DHelper.cpp")):
+            return d
+    return None
+
+
 def build_ref() -> str | None:
     """Compile the reference harness when the reference sources are present."""
-    ref = os.environ.get("IBEM_REFERENCE_DIR", "/root/reference")
-    if not os.path.isdir(ref):
+    ref = reference_dir()
+    if ref is None:
         return None
     out = subprocess.run(["make", "-C", HERE, "ref", f"REF={ref}"], capture_output=True, text=True)
     if out.returncode != 0:
@@ -93,6 +103,11 @@ def mat(E0, nu0, E1, nu1):
     return OrcMat(E0, nu0, E1, nu1)
 
 
+def case_mat(case):
+    """Material record of a case (anything with E0, nu0, E1, nu1)."""
+    return OrcMat(case.E0, case.nu0, case.E1, case.nu1)
+
+
 def layout_size(layout: int) -> int:
     return lib().orc_layout_size(layout)
 
@@ -132,7 +147,7 @@ def pair_blocks(centers, radius, m, layout):
 def assemble(case, layout, m=None):
     """Full HMAT / GMAT of a bounded case (addBEM, addFieldToBEM, inclusion and
     BEM->inclusion blocks), in the reference's order and layout."""
-    m = m or case.orc_mat()
+    m = m or case_mat(case)
     L = lib()
     nu = layout_size(layout)
     NN, NE, num = case.NN, case.NE, case.num
@@ -188,7 +203,7 @@ def get_ut(case, tcol, X):
 
 
 def post(case, layout, E, Ub=None, Tb=None, sig_inf=None, points=None, m=None):
-    m = m or case.orc_mat()
+    m = m or case_mat(case)
     pts = np.ascontiguousarray(case.points if points is None else points, dtype=np.float64)
     nump = len(pts)
     out = np.zeros((nump, 6))

@@ -9,10 +9,11 @@
 // Nothing in the product links, loads or runs this file or its binary.
 //
 // Usage:
-//   ibem_ref run <workdir> [--no-solve] [--no-post]
+//   ibem_ref run <workdir> [--no-solve] [--no-post] [--no-matrices]
 //       reads position.txt / BEM.txt / postprocess.txt from <workdir> (the reference
 //       opens them by fixed relative names, configElastic3D.h:54-56), writes
-//       HMAT.npy GMAT.npy A.npy b.npy X.npy U.npy T.npy stress.npy timings.txt there.
+//       HMAT.npy GMAT.npy A.npy b.npy X.npy U.npy T.npy stress.npy timings.txt there
+//       (--no-matrices: no HMAT / GMAT / A, which are N x N and N x 12NE doubles).
 //   ibem_ref kat <workdir>
 //       reads kat_in.npy (rows: x0 x1 x2 a) and kat_mat.npy (E0 nu0 E1 nu1) and
 //       writes the reference's D_xy / IGreen / Green values to kat_*.npy.
@@ -101,7 +102,7 @@ static void dump_vec(const std::string& name, const VectorXd& v) {
   write_npy(name, v.data(), {(long)v.size()}, false);
 }
 
-static int cmd_run(const char* dir, bool solve, bool post) {
+static int cmd_run(const char* dir, bool solve, bool post, bool matrices) {
   if (chdir(dir) != 0) { std::perror(dir); return 2; }
   configElastic3D cfg;
   FILE* tf = std::fopen("timings.txt", "w");
@@ -130,10 +131,12 @@ static int cmd_run(const char* dir, bool solve, bool post) {
   timed("addFluxEquivalentBEM", [&] { B.addFluxEquivalentBEM(cfg); });
   timed("addFluxEquivalentFirstOrderBEM", [&] { B.addFluxEquivalentFirstOrderBEM(cfg); });
   timed("addFluxEquivalentSecondOrderBEM", [&] { B.addFluxEquivalentSecondOrderBEM(cfg); });
-  dump_mat("HMAT.npy", cfg.HMAT);
-  dump_mat("GMAT.npy", cfg.GMAT);
+  if (matrices) {
+    dump_mat("HMAT.npy", cfg.HMAT);
+    dump_mat("GMAT.npy", cfg.GMAT);
+  }
   timed("ApplyBC", [&] { B.ApplyBC(cfg); });
-  dump_mat("A.npy", cfg.A);
+  if (matrices) dump_mat("A.npy", cfg.A);
   dump_vec("b.npy", cfg.b);
   if (solve) {
     systemSolverElastic3D solver;
@@ -233,14 +236,15 @@ static int cmd_kat(const char* dir) {
 
 int main(int argc, char** argv) {
   if (argc >= 3 && std::strcmp(argv[1], "run") == 0) {
-    bool solve = true, post = true;
+    bool solve = true, post = true, matrices = true;
     for (int i = 3; i < argc; ++i) {
       if (std::strcmp(argv[i], "--no-solve") == 0) solve = false;
       if (std::strcmp(argv[i], "--no-post") == 0) post = false;
+      if (std::strcmp(argv[i], "--no-matrices") == 0) matrices = false;
     }
-    return cmd_run(argv[2], solve, post);
+    return cmd_run(argv[2], solve, post, matrices);
   }
   if (argc >= 3 && std::strcmp(argv[1], "kat") == 0) return cmd_kat(argv[2]);
-  std::fprintf(stderr, "usage: ibem_ref run <dir> [--no-solve] [--no-post] | kat <dir>\n");
+  std::fprintf(stderr, "usage: ibem_ref run <dir> [--no-solve] [--no-post] [--no-matrices] | kat <dir>\n");
   return 2;
 }

@@ -70,3 +70,9 @@ def test_bc_plan_rejects_non_square(g):
     c.bc[j, 0] = 0.0   # one more prescribed displacement without a matching traction unknown
     with pytest.raises(g.IbemError):
         g.bc_plan(c)
+
+
+def test_selftest_bounded_wait_checks_arguments_on_the_host(g):
+    assert g.lib().ibem_selftest_bounded_wait(2, 100, None) == g.IBEM_ERR_ARG
+    assert g.lib().ibem_selftest_bounded_wait(0, 0, None) == g.IBEM_ERR_ARG
+    assert g.lib().ibem_selftest_bounded_wait(1, 1 << 23, None) == g.IBEM_ERR_ARG

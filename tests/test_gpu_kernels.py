@@ -121,6 +121,30 @@ def test_assembly_vs_reference_matrices(g):
     assert scaled_err(G[n3:], z["GMAT"][n3:]) < 1e-11
 
 
+def test_assembly_is_bit_reproducible(g):
+    """H sums element contributions per node in a fixed order (no atomics on matrix
+    entries): two assemblies of a mesh whose nodes are shared by up to four elements give
+    the same matrices bit for bit."""
+    from ibemproject_gb300 import cases
+    c = cases.bounded_cube_case(n_face=4, num=3, radius=0.1, grid=0, seed=11)
+    mats = []
+    for _ in range(2):
+        m = g.material(c.E0, c.nu0, c.E1, c.nu1)
+        N = 3 * c.NN + 24 * c.num
+        Ht = torch.zeros((N, N), dtype=torch.float64, device="cuda")
+        Gt = torch.zeros((12 * c.NE, N), dtype=torch.float64, device="cuda")
+        nodes, conn, cen = dev(c.nodes), dev(c.conn.astype(np.int32)), dev(c.centers)
+        L = g.lib()
+        g.check(L.ibem_e3d_bem_hg(P(nodes), c.NN, P(conn), c.NE, ctypes.byref(m), P(Ht), N, 0, 0, P(Gt), N, 0, 0,
+                                  None))
+        g.check(L.ibem_e3d_bem_to_incl(P(nodes), c.NN, P(conn), c.NE, P(cen), c.num, ctypes.byref(m), 24, P(Ht),
+                                       N, 0, P(Gt), N, 0, 3 * c.NN, None))
+        torch.cuda.synchronize()
+        mats.append((Ht.cpu(), Gt.cpu()))
+    assert torch.equal(mats[0][0], mats[1][0]) and torch.equal(mats[0][1], mats[1][1])
+    assert mats[0][0].abs().max() > 0
+
+
 def test_apply_bc_and_get_ut(g, oracle_mod):
     z, c, Ht, Gt = _tiny_device_matrices(g)
     N = Ht.shape[0]

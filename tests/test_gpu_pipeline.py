@@ -92,7 +92,7 @@ def test_farfield_case_vs_oracle(g, oracle_mod, form):
     from ibemproject_gb300 import cases
     c = cases.farfield_case(num=60, r0=0.05, vf=0.12, grid=5, seed=9)
     X, S, rep = g.run_host(c, layout=24, form=form, tol=1e-14)
-    m = c.orc_mat()
+    m = oracle_mod.case_mat(c)
     A = oracle_mod.pair_blocks(c.centers, c.radius, m, 24)
     b = oracle_mod.farfield_rhs(c.num, m, 24, c.sig_inf)
     Xo = np.linalg.solve(A, b)

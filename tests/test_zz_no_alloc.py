@@ -24,7 +24,7 @@ def _systems(oracle_mod):
     c = case_from_npz(z)
     A1, b1, _, _ = oracle_mod.apply_bc(c, z["HMAT"], z["GMAT"])          # bounded cube, N = 234
     f = cases.farfield_case(num=30, r0=0.05, vf=0.1, grid=0, seed=4)
-    m = f.orc_mat()
+    m = oracle_mod.case_mat(f)
     A2 = oracle_mod.pair_blocks(f.centers, f.radius, m, 24)               # 30 spheres, N = 720
     b2 = oracle_mod.farfield_rhs(f.num, m, 24, f.sig_inf)
     return [(np.asfortranarray(A1), b1), (np.asfortranarray(A2), b2)]
@@ -56,6 +56,27 @@ def test_noalloc_solve_matches_allocating_solve_twice(oracle_mod):
         x_na, rep = _solve(g, "noalloc", A, b)
         assert scaled_err(x_na, x_ref) < 1e-9
         assert rep.info == 0 and rep.backward_error < 1e-13
+
+
+def test_noalloc_solve_leaves_free_device_memory_unchanged(oracle_mod):
+    """Two calls after a warm-up call leave the device's free memory as it was: the entry
+    point itself allocates nothing (its inputs are allocated before the first reading)."""
+    import ibemproject_gb300 as g
+    g.lib()
+    (A, b), _ = _systems(oracle_mod)
+    N = len(b)
+    At = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()
+    bt = torch.from_numpy(np.ascontiguousarray(b)).cuda()
+    xt = torch.zeros(N, dtype=torch.float64, device="cuda")
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    call = lambda: g.check(g.lib().ibem_e3d_solve_noalloc(N, P(At), N, P(bt), P(xt), None, None))
+    call()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    call()
+    call()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
 
 
 def test_noalloc_rejects_sizes_beyond_its_workspace():
