@@ -1,0 +1,654 @@
+// Exterior and interior Eshelby fields of an ellipsoidal inclusion with a linear
+// (Taylor order 0 + 1) eigenstrain, host and device, in any real type T (double, float).
+//
+// The reference's spherical integrator (integratorElastic3DHelper.cpp:41-664, 2394-2554)
+// writes the disturbance strain of an inclusion as derivatives of two potentials of its
+// eigenstrain density rho,
+//     phi_rho(x) = int rho(x') / |x - x'| dV',   psi_rho(x) = int rho(x') |x - x'| dV',
+//     D_ijkl = [psi_,klij - 2 nu d_kl phi_,ij - (1 - nu)(d_il phi_,kj + d_jl phi_,ki
+//               + d_ik phi_,lj + d_jk phi_,li)] / (8 pi (1 - nu))          (:2394-2554)
+// with rho = 1 (uniform part) or x'_p (linear part).  The same tensor is evaluated here
+// for an ellipsoid sum_m y_m^2 / a_m^2 <= 1 in its principal frame y = Q^T (x - c):
+//
+//  * psi from phi: psi_rho,k = x_k phi_rho - phi_{rho x'_k}, so only Newtonian potentials
+//    of the densities 1, y'_m and y'_m y'_n are needed;
+//  * those are Ferrers / Dyson integrals over the confocal parameter s >= lambda,
+//        phi_1     = C int U ds / Delta
+//        phi_m     = C a_m^2 y_m int U t_m ds / Delta
+//        phi_mn    = C [ a_m^2/4 d_mn int U^2 ds/Delta + a_m^2 a_n^2 y_m y_n int U t_m t_n ds/Delta
+//                        - a_m^2 a_n^2/4 d_mn int U^2 t_n ds/Delta ]
+//    with C = pi a1 a2 a3, t_m = 1 / (a_m^2 + s), U = 1 - sum y_m^2 t_m,
+//    Delta = sqrt(prod (a_m^2 + s)); lambda = 0 inside, else the largest root of the cubic
+//    sum y_m^2 / (a_m^2 + lambda) = 1 (obtained from x'_m rho_n = -a_m^2/(2(n+1)) d'_m of
+//    (1 - |y'|_a^2)^(n+1) and integration by parts);
+//  * expanding U, every potential is a polynomial in y times the integrals
+//        I_k(lambda) = int_lambda^inf prod_m t_m^(k_m) ds / Delta,   |k| <= 3;
+//  * I_k are third-order parameter derivatives of Carlson's R_F (I_0 = 2 R_F(a^2 + lambda)),
+//    evaluated by Carlson's duplication algorithm (B. C. Carlson, "Numerical computation
+//    of real or complex elliptic integrals", Numer. Algorithms 10, 1995) run in truncated
+//    Taylor arithmetic in the three arguments -- exact in the sphere and spheroid limits,
+//    where partial-fraction recurrences between the I_k break down;
+//  * derivatives in x come from truncated multivariate Taylor series ("jets") in the
+//    global displacement h of the target point: lambda(x + h) by Newton iteration on jets,
+//    I_k(lambda0 + delta) from the closed-form lambda-derivatives dI_k/dlambda = -prod
+//    x_m^-(k_m + 1/2), then products with the polynomial factors.
+// For a1 = a2 = a3 everything reduces to the sphere formulas of the reference.
+#pragma once
+#include <math.h>
+
+#include "gen_sphere_common.cuh"
+
+namespace ibem {
+namespace ell {
+
+// ------------------------------------------------------------------ jets
+// Monomials h1^a h2^b h3^c of total degree d <= K in graded order; inside one degree a
+// descending, then b descending.
+IBEM_HD constexpr int nmono(int K) { return (K + 1) * (K + 2) * (K + 3) / 6; }
+IBEM_HD constexpr int midx(int a, int b, int c) {
+  return (a + b + c) * (a + b + c + 1) * (a + b + c + 2) / 6 + (b + c) * (b + c + 1) / 2 + c;
+}
+
+template <typename T, int K>
+struct Jet {
+  static constexpr int N = nmono(K);
+  T c[N];
+};
+
+template <typename T, int K>
+IBEM_HD IBEM_INLINE void jzero(Jet<T, K>& o) {
+#pragma unroll
+  for (int i = 0; i < Jet<T, K>::N; ++i) o.c[i] = T(0);
+}
+
+// o = a * b (o must not alias a or b)
+template <typename T, int K>
+IBEM_HD IBEM_INLINE void jmul(const Jet<T, K>& a, const Jet<T, K>& b, Jet<T, K>& o) {
+#pragma unroll
+  for (int g1 = 0; g1 <= K; ++g1)
+#pragma unroll
+    for (int g2 = 0; g2 <= K - g1; ++g2)
+#pragma unroll
+      for (int g3 = 0; g3 <= K - g1 - g2; ++g3) {
+        T s = T(0);
+#pragma unroll
+        for (int a1 = 0; a1 <= g1; ++a1)
+#pragma unroll
+          for (int a2 = 0; a2 <= g2; ++a2)
+#pragma unroll
+            for (int a3 = 0; a3 <= g3; ++a3) s += a.c[midx(a1, a2, a3)] * b.c[midx(g1 - a1, g2 - a2, g3 - a3)];
+        o.c[midx(g1, g2, g3)] = s;
+      }
+}
+
+// o += w * a * b
+template <typename T, int K>
+IBEM_HD IBEM_INLINE void jfma(T w, const Jet<T, K>& a, const Jet<T, K>& b, Jet<T, K>& o) {
+#pragma unroll
+  for (int g1 = 0; g1 <= K; ++g1)
+#pragma unroll
+    for (int g2 = 0; g2 <= K - g1; ++g2)
+#pragma unroll
+      for (int g3 = 0; g3 <= K - g1 - g2; ++g3) {
+        T s = T(0);
+#pragma unroll
+        for (int a1 = 0; a1 <= g1; ++a1)
+#pragma unroll
+          for (int a2 = 0; a2 <= g2; ++a2)
+#pragma unroll
+            for (int a3 = 0; a3 <= g3; ++a3) s += a.c[midx(a1, a2, a3)] * b.c[midx(g1 - a1, g2 - a2, g3 - a3)];
+        o.c[midx(g1, g2, g3)] += w * s;
+      }
+}
+
+// o = (l0 + l1 h1 + l2 h2 + l3 h3) * a   (o must not alias a)
+template <typename T, int K>
+IBEM_HD IBEM_INLINE void jmul_lin(T l0, T l1, T l2, T l3, const Jet<T, K>& a, Jet<T, K>& o) {
+#pragma unroll
+  for (int g1 = 0; g1 <= K; ++g1)
+#pragma unroll
+    for (int g2 = 0; g2 <= K - g1; ++g2)
+#pragma unroll
+      for (int g3 = 0; g3 <= K - g1 - g2; ++g3) {
+        T s = l0 * a.c[midx(g1, g2, g3)];
+        if (g1 > 0) s += l1 * a.c[midx(g1 - 1, g2, g3)];
+        if (g2 > 0) s += l2 * a.c[midx(g1, g2 - 1, g3)];
+        if (g3 > 0) s += l3 * a.c[midx(g1, g2, g3 - 1)];
+        o.c[midx(g1, g2, g3)] = s;
+      }
+}
+
+// o += w * a
+template <typename T, int K>
+IBEM_HD IBEM_INLINE void jaxpy(T w, const Jet<T, K>& a, Jet<T, K>& o) {
+#pragma unroll
+  for (int i = 0; i < Jet<T, K>::N; ++i) o.c[i] += w * a.c[i];
+}
+
+// f(a) for a jet a with constant term a0 and f given by its Taylor coefficients at a0:
+// o = sum_n f_n (a - a0)^n, f_n = f^(n)(a0)/n!
+template <typename T, int K>
+IBEM_HD IBEM_INLINE void jcompose(const Jet<T, K>& a, const T* f, Jet<T, K>& o) {
+  Jet<T, K> u = a, p, t;
+  u.c[0] = T(0);
+  jzero(o);
+  o.c[0] = f[0];
+  p = u;
+#pragma unroll
+  for (int n = 1; n <= K; ++n) {
+    jaxpy(f[n], p, o);
+    if (n < K) {
+      jmul(p, u, t);
+      p = t;
+    }
+  }
+}
+
+// a^(q) for real q (a0 > 0)
+template <typename T, int K>
+IBEM_HD IBEM_INLINE void jpow(const Jet<T, K>& a, T q, Jet<T, K>& o) {
+  T f[K + 1];
+  const T a0 = a.c[0];
+  f[0] = pow(a0, q);
+  T coef = T(1);
+#pragma unroll
+  for (int n = 1; n <= K; ++n) {
+    coef *= (q - T(n - 1)) / T(n);
+    f[n] = f[0] * coef / pow(a0, T(n));
+  }
+  jcompose(a, f, o);
+}
+
+// ------------------------------------------------------------------ Carlson R_F jets
+// I_k(lambda) for all |k| <= 3 at x_m = a_m^2 + lambda: third-order Taylor coefficients of
+// 2 R_F(x1, x2, x3) in its arguments (duplication algorithm, Carlson 1995), scaled by
+// d/dx_m of int prod (x + tau)^-(k_m + 1/2) = -(k_m + 1/2) I_{k + e_m}:
+//     I_k = 2 c_k(R_F) prod_m w(k_m),  w = 1, -2, 8/3, -16/5.
+// Output ik[midx(k1, k2, k3)] (20 values).
+template <typename T>
+IBEM_HD inline void carlson_ik(const T x[3], T* ik) {
+  using J = Jet<T, 3>;
+  J X[3], A, A0;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    jzero(X[m]);
+    X[m].c[0] = x[m];
+  }
+  X[0].c[midx(1, 0, 0)] = T(1);
+  X[1].c[midx(0, 1, 0)] = T(1);
+  X[2].c[midx(0, 0, 1)] = T(1);
+#pragma unroll
+  for (int i = 0; i < J::N; ++i) A0.c[i] = (X[0].c[i] + X[1].c[i] + X[2].c[i]) / T(3);
+  A = A0;
+  // iteration count from the values (Carlson 1995, eq. 2.2-2.4 with r the unit roundoff)
+  const T r = sizeof(T) == sizeof(double) ? T(1.1102230246251565e-16) : T(5.9604645e-08);
+  const T Qv = pow(T(3) * r, T(-1.0 / 6.0)) *
+               fmax(fabs(A0.c[0] - x[0]), fmax(fabs(A0.c[0] - x[1]), fabs(A0.c[0] - x[2])));
+  T pow4 = T(1);
+  J s[3], lam, t;
+#pragma unroll 1
+  for (int it = 0; it < 40 && pow4 * Qv >= fabs(A.c[0]); ++it) {
+#pragma unroll
+    for (int m = 0; m < 3; ++m) jpow(X[m], T(0.5), s[m]);
+    jmul(s[0], s[1], lam);
+    jfma(T(1), s[0], s[2], lam);
+    jfma(T(1), s[1], s[2], lam);
+#pragma unroll
+    for (int i = 0; i < J::N; ++i) {
+      A.c[i] = (A.c[i] + lam.c[i]) * T(0.25);
+#pragma unroll
+      for (int m = 0; m < 3; ++m) X[m].c[i] = (X[m].c[i] + lam.c[i]) * T(0.25);
+    }
+    pow4 *= T(0.25);
+  }
+  // X = (A0 - x) / (4^m A), Y likewise, Z = -X - Y
+  J invA, Xs, Ys, Zs;
+  jpow(A, T(-1), invA);
+  J d0 = A0, d1 = A0;
+  d0.c[0] -= x[0];
+  d0.c[midx(1, 0, 0)] -= T(1);
+  d1.c[0] -= x[1];
+  d1.c[midx(0, 1, 0)] -= T(1);
+  jmul(d0, invA, Xs);
+  jmul(d1, invA, Ys);
+#pragma unroll
+  for (int i = 0; i < J::N; ++i) {
+    Xs.c[i] *= pow4;
+    Ys.c[i] *= pow4;
+    Zs.c[i] = -Xs.c[i] - Ys.c[i];
+  }
+  J E2, E3, E22, E23;
+  jmul(Xs, Ys, E2);
+  jmul(Zs, Zs, t);
+#pragma unroll
+  for (int i = 0; i < J::N; ++i) E2.c[i] -= t.c[i];
+  jmul(Xs, Ys, t);
+  jmul(t, Zs, E3);
+  jmul(E2, E2, E22);
+  jmul(E2, E3, E23);
+  J ser;
+#pragma unroll
+  for (int i = 0; i < J::N; ++i)
+    ser.c[i] = -E2.c[i] / T(10) + E3.c[i] / T(14) + E22.c[i] / T(24) - T(3) * E23.c[i] / T(44);
+  ser.c[0] += T(1);
+  J rsA, rf;
+  jpow(A, T(-0.5), rsA);
+  jmul(rsA, ser, rf);
+  const T w[4] = {T(1), T(-2), T(8.0 / 3.0), T(-16.0 / 5.0)};
+#pragma unroll
+  for (int k1 = 0; k1 <= 3; ++k1)
+#pragma unroll
+    for (int k2 = 0; k2 <= 3 - k1; ++k2)
+#pragma unroll
+      for (int k3 = 0; k3 <= 3 - k1 - k2; ++k3)
+        ik[midx(k1, k2, k3)] = T(2) * rf.c[midx(k1, k2, k3)] * w[k1] * w[k2] * w[k3];
+}
+
+// ------------------------------------------------------------------ lambda
+// Largest root of sum y_m^2 / (a2_m + lambda) = 1 for an exterior point (the cubic
+// prod (a2 + lambda) - sum y_m^2 prod_{n != m} (a2_n + lambda) = 0), by Newton on the
+// convex decreasing rational form from the left, where each step stays below the root;
+// 0 for a point inside or on the surface.
+template <typename T>
+IBEM_HD inline T ell_lambda(const T y[3], const T a2[3]) {
+  const T q = y[0] * y[0] / a2[0] + y[1] * y[1] / a2[1] + y[2] * y[2] / a2[2];
+  if (q <= T(1)) return T(0);
+  const T r2 = y[0] * y[0] + y[1] * y[1] + y[2] * y[2];
+  const T amax = fmax(a2[0], fmax(a2[1], a2[2]));
+  T lam = fmax(T(0), r2 - amax);
+#pragma unroll 1
+  for (int it = 0; it < 100; ++it) {
+    T f = T(-1), df = T(0);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const T t = T(1) / (a2[m] + lam);
+      f += y[m] * y[m] * t;
+      df -= y[m] * y[m] * t * t;
+    }
+    const T step = -f / df;
+    lam += step;
+    if (!(step > T(4) * (sizeof(T) == sizeof(double) ? T(1.1102230246251565e-16) : T(5.9604645e-08)) * lam))
+      break;
+  }
+  return lam;
+}
+
+// ------------------------------------------------------------------ potentials
+// Jets (order K in the global displacement h of the evaluation point) of the Newtonian
+// potentials of the densities 1, x'_p and x'_p x'_q (global components, relative to the
+// centre), for an ellipsoid with semi-axes a and rotation Q (Q[3 i + m]: global component
+// i of principal axis m), at the point c + d.
+template <typename T, int K>
+struct EllPot {
+  Jet<T, K> f0;      // phi_1
+  Jet<T, K> f1[3];   // phi_{x'_p}
+  Jet<T, K> f2[6];   // phi_{x'_p x'_q}, pairs 00 01 02 11 12 22
+  T d[3];            // x - c
+  bool inside;
+};
+
+IBEM_HD constexpr int sym_pair(int p, int q) {
+  return p <= q ? (p == 0 ? q : (p == 1 ? 2 + q : 5)) : (q == 0 ? p : (q == 1 ? 2 + p : 5));
+}
+
+template <typename T, int K>
+IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], EllPot<T, K>& P) {
+  using J = Jet<T, K>;
+  T y[3], a2[3];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    y[m] = Q[m] * d[0] + Q[3 + m] * d[1] + Q[6 + m] * d[2];
+    a2[m] = a[m] * a[m];
+    P.d[m] = d[m];
+  }
+  const T lam0 = ell_lambda(y, a2);
+  const T qin = y[0] * y[0] / a2[0] + y[1] * y[1] / a2[1] + y[2] * y[2] / a2[2];
+  P.inside = qin <= T(1);
+  T x[3];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) x[m] = a2[m] + lam0;
+  // l_m(h) = y_m + (Q^T h)_m and sq_m = l_m^2
+  J sq[3];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    jzero(sq[m]);
+    const T l1 = Q[m], l2 = Q[3 + m], l3 = Q[6 + m];
+    sq[m].c[0] = y[m] * y[m];
+    if (K >= 1) {
+      sq[m].c[midx(1, 0, 0)] = T(2) * y[m] * l1;
+      sq[m].c[midx(0, 1, 0)] = T(2) * y[m] * l2;
+      sq[m].c[midx(0, 0, 1)] = T(2) * y[m] * l3;
+    }
+    if (K >= 2) {
+      sq[m].c[midx(2, 0, 0)] = l1 * l1;
+      sq[m].c[midx(0, 2, 0)] = l2 * l2;
+      sq[m].c[midx(0, 0, 2)] = l3 * l3;
+      sq[m].c[midx(1, 1, 0)] = T(2) * l1 * l2;
+      sq[m].c[midx(1, 0, 1)] = T(2) * l1 * l3;
+      sq[m].c[midx(0, 1, 1)] = T(2) * l2 * l3;
+    }
+  }
+  // powers of delta(h) = lambda(c + d + h) - lambda0 (zero inside)
+  J dp[K + 1];
+#pragma unroll
+  for (int n = 0; n <= K; ++n) jzero(dp[n]);
+  dp[0].c[0] = T(1);
+  if (!P.inside) {
+    T gp = T(0);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) gp -= y[m] * y[m] / (x[m] * x[m]);
+    J del, G, inv, t;
+    jzero(del);
+#pragma unroll 1
+    for (int it = 0; it < K; ++it) {
+      dp[1] = del;
+#pragma unroll
+      for (int n = 2; n <= K; ++n) jmul(dp[n - 1], del, dp[n]);
+      jzero(G);
+      G.c[0] = T(-1);
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        jzero(inv);
+        T xm = T(1) / x[m], s = xm;
+#pragma unroll
+        for (int n = 0; n <= K; ++n) {
+          jaxpy(s, dp[n], inv);
+          s *= -xm;
+        }
+        jfma(T(1), sq[m], inv, G);
+      }
+      G.c[0] = T(0);   // lambda0 is the root: the constant term vanishes (to rounding)
+      jaxpy(-T(1) / gp, G, del);
+    }
+    dp[1] = del;
+#pragma unroll
+    for (int n = 2; n <= K; ++n) jmul(dp[n - 1], del, dp[n]);
+  }
+  // I_k(lambda0) and their jets
+  T ik[20];
+  carlson_ik(x, ik);
+  J I[20];
+#pragma unroll
+  for (int k1 = 0; k1 <= 3; ++k1)
+#pragma unroll
+    for (int k2 = 0; k2 <= 3 - k1; ++k2)
+#pragma unroll
+      for (int k3 = 0; k3 <= 3 - k1 - k2; ++k3) {
+        const int id = midx(k1, k2, k3);
+        J& o = I[id];
+        jzero(o);
+        o.c[0] = ik[id];
+        if (!P.inside) {
+          // dI/dlambda = -f(lambda), f(lambda0 + delta) = f0 prod_m (1 + delta/x_m)^-(k_m + 1/2)
+          const int kk[3] = {k1, k2, k3};
+          T b[K + 1];
+          b[0] = T(1);
+#pragma unroll
+          for (int n = 1; n <= K; ++n) b[n] = T(0);
+          T f0 = T(1);
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            const T qm = T(kk[m]) + T(0.5);
+            f0 *= pow(x[m], -qm);
+            T bm[K + 1], coef = T(1);
+            bm[0] = T(1);
+#pragma unroll
+            for (int n = 1; n <= K; ++n) {
+              coef *= (-qm - T(n - 1)) / T(n);
+              bm[n] = coef / pow(x[m], T(n));
+            }
+            T nb[K + 1];
+#pragma unroll
+            for (int n = 0; n <= K; ++n) {
+              T s = T(0);
+#pragma unroll
+              for (int j = 0; j <= n; ++j) s += b[j] * bm[n - j];
+              nb[n] = s;
+            }
+#pragma unroll
+            for (int n = 0; n <= K; ++n) b[n] = nb[n];
+          }
+#pragma unroll
+          for (int n = 0; n < K; ++n) jaxpy(-f0 * b[n] / T(n + 1), dp[n + 1], o);
+        }
+      }
+  // F1_j = int U prod t^j ds/Delta = I_j - sum_m sq_m I_{j+e_m}
+  // F2_j = int U^2 prod t^j ds/Delta = I_j - 2 sum_m sq_m I_{j+e_m} + sum_{m,n} sq_m sq_n I_{j+e_m+e_n}
+  const T C = T(IBEM_PI) * a[0] * a[1] * a[2];
+  J t, u;
+  auto e = [](int m, int k1, int k2, int k3) { return midx(k1 + (m == 0), k2 + (m == 1), k3 + (m == 2)); };
+  // phi_1 = C F1_0
+  J F;
+  F = I[0];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) jfma(-T(1), sq[m], I[e(m, 0, 0, 0)], F);
+#pragma unroll
+  for (int i = 0; i < J::N; ++i) P.f0.c[i] = C * F.c[i];
+  // phi_{y'_m} = C a_m^2 l_m F1_{e_m}, rotated to global densities
+  J p1[3];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    const int km[3] = {m == 0, m == 1, m == 2};
+    F = I[midx(km[0], km[1], km[2])];
+#pragma unroll
+    for (int n = 0; n < 3; ++n) jfma(-T(1), sq[n], I[e(n, km[0], km[1], km[2])], F);
+    jmul_lin(C * a2[m] * y[m], C * a2[m] * Q[m], C * a2[m] * Q[3 + m], C * a2[m] * Q[6 + m], F, p1[m]);
+  }
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    jzero(P.f1[p]);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) jaxpy(Q[3 * p + m], p1[m], P.f1[p]);
+  }
+  // phi_{y'_m y'_n}
+  J F20;   // F2_0
+  F20 = I[0];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) jfma(-T(2), sq[m], I[e(m, 0, 0, 0)], F20);
+#pragma unroll
+  for (int m = 0; m < 3; ++m)
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+      jmul(sq[m], sq[n], u);
+      jfma(T(1), u, I[midx((m == 0) + (n == 0), (m == 1) + (n == 1), (m == 2) + (n == 2))], F20);
+    }
+  J p2[6];
+#pragma unroll
+  for (int m = 0; m < 3; ++m)
+#pragma unroll
+    for (int n = m; n < 3; ++n) {
+      const int km[3] = {(m == 0) + (n == 0), (m == 1) + (n == 1), (m == 2) + (n == 2)};
+      // F1_{e_m + e_n}, times a_m^2 a_n^2 l_m l_n
+      F = I[midx(km[0], km[1], km[2])];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) jfma(-T(1), sq[r], I[e(r, km[0], km[1], km[2])], F);
+      jmul_lin(y[m], Q[m], Q[3 + m], Q[6 + m], F, t);
+      J& o = p2[sym_pair(m, n)];
+      jmul_lin(C * a2[m] * a2[n] * y[n], C * a2[m] * a2[n] * Q[n], C * a2[m] * a2[n] * Q[3 + n],
+               C * a2[m] * a2[n] * Q[6 + n], t, o);
+      if (m == n) {
+        // + C a_m^2/4 F2_0 - C a_m^4/4 F2_{e_m}
+        jaxpy(C * a2[m] / T(4), F20, o);
+        const int em[3] = {m == 0, m == 1, m == 2};
+        F = I[midx(em[0], em[1], em[2])];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) jfma(-T(2), sq[r], I[e(r, em[0], em[1], em[2])], F);
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int s = 0; s < 3; ++s) {
+            jmul(sq[r], sq[s], u);
+            jfma(T(1), u,
+                 I[midx(em[0] + (r == 0) + (s == 0), em[1] + (r == 1) + (s == 1), em[2] + (r == 2) + (s == 2))], F);
+          }
+        jaxpy(-C * a2[m] * a2[m] / T(4), F, o);
+      }
+    }
+  // global densities x'_p x'_q = sum_mn Q_pm Q_qn y'_m y'_n
+#pragma unroll
+  for (int p = 0; p < 3; ++p)
+#pragma unroll
+    for (int q = p; q < 3; ++q) {
+      J& o = P.f2[sym_pair(p, q)];
+      jzero(o);
+#pragma unroll
+      for (int m = 0; m < 3; ++m)
+#pragma unroll
+        for (int n = 0; n < 3; ++n) jaxpy(Q[3 * p + m] * Q[3 * q + n], p2[sym_pair(m, n)], o);
+    }
+}
+
+// ------------------------------------------------------------------ derivatives
+IBEM_HD constexpr int fact(int n) { return n <= 1 ? 1 : n * fact(n - 1); }
+
+// d^alpha f at h = 0 from the jet coefficient (alpha given by index counts)
+template <typename T, int K>
+IBEM_HD IBEM_INLINE T jder(const Jet<T, K>& f, int a1, int a2, int a3) {
+  return T(fact(a1) * fact(a2) * fact(a3)) * f.c[midx(a1, a2, a3)];
+}
+
+// counts of an index list
+IBEM_HD IBEM_INLINE void counts(const int* idx, int n, int* c) {
+  c[0] = c[1] = c[2] = 0;
+  for (int s = 0; s < n; ++s) ++c[idx[s]];
+}
+
+// phi_rho,idx  (rho: -1 uniform, p = 0..2 the linear density x'_p)
+template <typename T, int K>
+IBEM_HD inline T phi_d(const EllPot<T, K>& P, int rho, const int* idx, int n) {
+  int c[3];
+  counts(idx, n, c);
+  return jder(rho < 0 ? P.f0 : P.f1[rho], c[0], c[1], c[2]);
+}
+
+// psi_rho,k idx = d^idx (x_k phi_rho - phi_{rho x'_k}) at the point
+template <typename T, int K>
+IBEM_HD inline T psi_d(const EllPot<T, K>& P, int rho, int k, const int* idx, int n) {
+  int c[3];
+  counts(idx, n, c);
+  const Jet<T, K>& f = rho < 0 ? P.f0 : P.f1[rho];
+  const Jet<T, K>& g = rho < 0 ? P.f1[k] : P.f2[sym_pair(rho, k)];
+  T v = P.d[k] * jder(f, c[0], c[1], c[2]) - jder(g, c[0], c[1], c[2]);
+  if (c[k] > 0) {   // d^idx of h_k phi: c_k d^(idx - e_k) phi
+    c[k] -= 1;
+    v += T(c[k] + 1) * jder(f, c[0], c[1], c[2]);
+  }
+  return v;
+}
+
+// D(i,j,k,l [,p]; R) of the reference (strain ij, eigenstrain kl of density rho), without
+// the factor 1 / (8 pi (1 - nu)): psi_,klijR - 2 nu d_kl phi_,ijR - (1 - nu)(...)
+template <typename T, int K>
+IBEM_HD inline T Dsum(const EllPot<T, K>& P, T nu, int rho, int i, int j, int k, int l, const int* R, int nR) {
+  int idx[8];
+  int n = 0;
+  idx[n++] = l;
+  idx[n++] = i;
+  idx[n++] = j;
+  for (int s = 0; s < nR; ++s) idx[n++] = R[s];
+  T v = psi_d(P, rho, k, idx, n);
+  int id2[6];
+  auto ph = [&](int x1, int x2) {
+    id2[0] = x1;
+    id2[1] = x2;
+    for (int s = 0; s < nR; ++s) id2[2 + s] = R[s];
+    return phi_d(P, rho, id2, 2 + nR);
+  };
+  if (k == l) v -= T(2) * nu * ph(i, j);
+  T s4 = T(0);
+  if (i == l) s4 += ph(k, j);
+  if (j == l) s4 += ph(k, i);
+  if (i == k) s4 += ph(l, j);
+  if (j == k) s4 += ph(l, i);
+  return v - (T(1) - nu) * s4;
+}
+
+// ------------------------------------------------------------------ blocks and sums
+// layout-24 unknown u: order 0 (u < 6): symmetric pair t = u; order 1: t = (u - 6) / 3,
+// moment p = (u - 6) % 3.  Pairs t: 00 01 02 11 12 22.
+IBEM_HD constexpr int pair_i(int t) { return t < 3 ? 0 : (t < 5 ? 1 : 2); }
+IBEM_HD constexpr int pair_j(int t) { return t < 3 ? t : (t < 5 ? t - 2 : 2); }
+
+// One (s, h) block of the layout-24 equivalent-inclusion system for an ellipsoidal source
+// h (integratorElastic3D.cpp:341-567 with the sphere's potentials replaced): rows (s, ij[,r]),
+// columns (h, mn[,p]):
+//   map[m][n] (-sum_kl (C0 - C1)_ijkl D(k,l,m,n[,p]; [r]) + [self] C0_ijmn delta),
+// d = centre of s - centre of h.  out[row * 24 + col].
+template <typename T>
+IBEM_HD inline void ell_block24(const T d[3], const T Q[9], const T a[3], const SphMat& mc, bool self, T* out) {
+  EllPot<T, 4> P;
+  ell_potentials<T, 4>(d, Q, a, P);
+  const T nu = T(mc.tn2) / T(2);
+  const T kd = T(mc.kd);
+  for (int rr = 0; rr < 24; ++rr) {
+    const int ro = rr < 6 ? 0 : 1;
+    const int rt = ro ? (rr - 6) / 3 : rr;
+    const int R[1] = {ro ? (rr - 6) % 3 : 0};
+    const int i = pair_i(rt), j = pair_j(rt);
+    for (int cc = 0; cc < 24; ++cc) {
+      const int co = cc < 6 ? 0 : 1;
+      const int ct = co ? (cc - 6) / 3 : cc;
+      const int rho = co ? (cc - 6) % 3 : -1;
+      const int m = pair_i(ct), n = pair_j(ct);
+      // sum_kl (C0 - C1)_ijkl D_kl = dlam d_ij D_kk + 2 dmu D_ij
+      T acc = T(2) * T(mc.dmu) * Dsum(P, nu, rho, i, j, m, n, R, ro);
+      if (i == j) {
+        T tr = T(0);
+        for (int k = 0; k < 3; ++k) tr += Dsum(P, nu, rho, k, k, m, n, R, ro);
+        acc += T(mc.dlam) * tr;
+      }
+      T v = -kd * acc;
+      if (self && ro == co && (ro == 0 || R[0] == rho)) {
+        // C0_ijmn
+        T c0 = T(mc.mu0) * (T((i == m) * (j == n)) + T((i == n) * (j == m)));
+        if (i == j && m == n) c0 += T(mc.lam0);
+        v += c0;
+      }
+      out[rr * 24 + cc] = (m == n ? T(1) : T(2)) * v;
+    }
+  }
+}
+
+// Strain (6: xx xy xz yy yz zz) at c + d due to the layout-24 eigenstrain E of an
+// ellipsoidal source (postProcessorElastic3D.cpp:367-470 with the ellipsoid's potentials),
+// accumulated into e.  Returns true if the point lies inside (or on) the ellipsoid.
+template <typename T>
+IBEM_HD inline bool ell_strain24(const T d[3], const T Q[9], const T a[3], const SphMat& mc, const T* E, T* e) {
+  EllPot<T, 3> P;
+  ell_potentials<T, 3>(d, Q, a, P);
+  const T nu = T(mc.tn2) / T(2);
+  const T kd = T(mc.kd);
+  for (int rt = 0; rt < 6; ++rt) {
+    const int i = pair_i(rt), j = pair_j(rt);
+    T s = T(0);
+    for (int cc = 0; cc < 24; ++cc) {
+      const int co = cc < 6 ? 0 : 1;
+      const int ct = co ? (cc - 6) / 3 : cc;
+      const int rho = co ? (cc - 6) % 3 : -1;
+      const int m = pair_i(ct), n = pair_j(ct);
+      s += (m == n ? T(1) : T(2)) * Dsum(P, nu, rho, i, j, m, n, nullptr, 0) * E[cc];
+    }
+    e[rt] += kd * s;
+  }
+  return P.inside;
+}
+
+// Rotation matrix (Q[3 i + m]: global component i of principal axis m) of a unit quaternion
+// (w, x, y, z); the quaternion is normalised first.
+template <typename T>
+IBEM_HD inline void quat_to_rot(const T* q, T* Q) {
+  const T n = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  const T w = q[0] / n, x = q[1] / n, y = q[2] / n, z = q[3] / n;
+  Q[0] = T(1) - T(2) * (y * y + z * z);
+  Q[1] = T(2) * (x * y - w * z);
+  Q[2] = T(2) * (x * z + w * y);
+  Q[3] = T(2) * (x * y + w * z);
+  Q[4] = T(1) - T(2) * (x * x + z * z);
+  Q[5] = T(2) * (y * z - w * x);
+  Q[6] = T(2) * (x * z - w * y);
+  Q[7] = T(2) * (y * z + w * x);
+  Q[8] = T(1) - T(2) * (x * x + y * y);
+}
+
+}  // namespace ell
+}  // namespace ibem

@@ -87,6 +87,15 @@ def lib():
         L.orc_stress_kernel.argtypes = [_dp, _dp, ctypes.POINTER(OrcMat), ctypes.c_double,
                                         ctypes.c_double, ctypes.c_int, _dp, _dp]
         L.orc_farfield_rhs.argtypes = [ctypes.c_int, ctypes.POINTER(OrcMat), ctypes.c_int, _dp, _dp]
+        L.orc_ell_D_quad.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int, _dp]
+        L.orc_ell_I.argtypes = [_ip, _dp, ctypes.c_double, ctypes.c_int]
+        L.orc_ell_I.restype = ctypes.c_double
+        for f in (L.orc_carlson_rf, L.orc_carlson_rd):
+            f.argtypes = [ctypes.c_double] * 3
+            f.restype = ctypes.c_double
+        L.orc_ell_lambda.argtypes = [_dp, _dp]
+        L.orc_ell_lambda.restype = ctypes.c_double
         _lib = L
     return _lib
 
@@ -236,3 +245,33 @@ def stress_kernel(x, nv, m, dlam, dmu, nder):
                             _d(np.ascontiguousarray(nv, dtype=np.float64)), ctypes.byref(m),
                             float(dlam), float(dmu), nder, _d(Dsu), _d(Dst))
     return Dsu.reshape(nrow, 3), Dst.reshape(nrow, 3)
+
+
+# ---------------------------------------------------------------- ellipsoids (ell_oracle.c)
+def ell_D_quad(order, nder, x, a, Q, nu, n=(32, 32, 64)):
+    """D tensor of an ellipsoid (semi-axes a, rotation Q: Q[i, m] = global component i of
+    principal axis m) at the exterior point x (relative to the centre), by volume quadrature
+    of the differentiated kernels; digit order as D_tensor."""
+    out = np.zeros(3 ** (4 + order + nder))
+    lib().orc_ell_D_quad(order, nder, _d(np.ascontiguousarray(x, dtype=np.float64)),
+                         _d(np.ascontiguousarray(a, dtype=np.float64)),
+                         _d(np.ascontiguousarray(Q, dtype=np.float64).ravel()), float(nu), n[0], n[1], n[2], _d(out))
+    return out.reshape((3,) * (4 + order + nder))
+
+
+def ell_I(k, a, lam, n=64):
+    return lib().orc_ell_I(_i(np.ascontiguousarray(k, dtype=np.int32)), _d(np.ascontiguousarray(a, dtype=np.float64)),
+                           float(lam), int(n))
+
+
+def carlson_rf(x, y, z):
+    return lib().orc_carlson_rf(x, y, z)
+
+
+def carlson_rd(x, y, z):
+    return lib().orc_carlson_rd(x, y, z)
+
+
+def ell_lambda(y, a):
+    return lib().orc_ell_lambda(_d(np.ascontiguousarray(y, dtype=np.float64)),
+                                _d(np.ascontiguousarray(a, dtype=np.float64)))
