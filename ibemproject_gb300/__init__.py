@@ -67,6 +67,12 @@ class GenParams(ctypes.Structure):
                 ("seed", ctypes.c_uint64), ("max_tries", ctypes.c_int64), ("sweeps", ctypes.c_int)]
 
 
+class EllGenParams(ctypes.Structure):
+    _fields_ = [("num", ctypes.c_int), ("a1", ctypes.c_double), ("a2lo", ctypes.c_double), ("a2hi", ctypes.c_double),
+                ("a3lo", ctypes.c_double), ("a3hi", ctypes.c_double), ("vf", ctypes.c_double),
+                ("gap", ctypes.c_double), ("seed", ctypes.c_uint64), ("max_tries", ctypes.c_int64)]
+
+
 class IbemError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"ibem status {status}: {msg}")
@@ -106,6 +112,11 @@ SIGNATURES = {
                                  _int, _c_dp, _c_dp, _int, _c_dp, _c_dp, _dbl, _c_dp, _c_dp,
                                  ctypes.POINTER(SolveReport)]),
     "ibem_e3d_run_dir": (_int, [ctypes.c_char_p, _int, _int, _dbl, ctypes.POINTER(SolveReport)]),
+    "ibem_e3d_ell_pair_blocks": (_int, [_vp, _vp, _vp, _int, ctypes.POINTER(Material), _vp, _i64, _i64, _i64, _vp]),
+    "ibem_e3d_ell_field": (_int, [_int, _vp, _int, _vp, _vp, _vp, _int, ctypes.POINTER(Material), _vp, _c_dp, _vp,
+                                  _vp]),
+    "ibem_e3d_run_host_ell": (_int, [_int, ctypes.POINTER(Material), _int, _c_dp, _c_dp, _c_dp, _int, _c_dp, _c_dp,
+                                     _dbl, _c_dp, _c_dp, ctypes.POINTER(SolveReport)]),
     "ibem_e3d_mf_matvec": (_int, [ctypes.POINTER(Batch), _int, _vp, _vp, _vp]),
     "ibem_e3d_mf_solve": (_int, [ctypes.POINTER(Batch), _vp, _vp, _int, _vp, ctypes.POINTER(MfOptions),
                                  ctypes.POINTER(MfReport), _vp]),
@@ -121,6 +132,7 @@ SIGNATURES = {
                                     ctypes.POINTER(ctypes.c_float), ctypes.POINTER(MfOptions), _c_dp, _c_dp,
                                     ctypes.POINTER(MfReport)]),
     "ibem_e3d_generate_spheres": (_int, [ctypes.POINTER(GenParams), _c_dp, _c_dp, _c_dp]),
+    "ibem_e3d_generate_ellipsoids": (_int, [ctypes.POINTER(EllGenParams), _c_dp, _c_dp, _c_dp, _c_dp]),
     "ibem_e3d_sidecar_from_txt": (_int, [ctypes.c_char_p]),
     "ibem_e3d_sidecar_write": (_int, [ctypes.c_char_p, ctypes.POINTER(Material), _int, _c_dp, _int, _c_ip, _c_dp,
                                       _c_dp, _int, _c_dp, _c_dp, _int, _c_dp, _c_dp]),
@@ -217,6 +229,23 @@ def run_host_mf(case, precond: int = PRECOND_LEARNED, params=None, tol: float = 
     check(lib().ibem_e3d_run_host_mf(ctypes.byref(m), case.num, _dp(cen), _dp(rad), case.nump, _dp(pts), _dp(sig),
                                      precond, prm, ctypes.byref(opt), _dp(X), _dp(S), ctypes.byref(rep)))
     return X, S, rep
+
+
+def run_host_ell(case, form: int = SOLVE_FP64, tol: float = 1e-12):
+    """Boundary-free ellipsoid pipeline (case.axes, case.quats set) through the host-buffer
+    C ABI: returns (X, stress, report)."""
+    m = material(case.E0, case.nu0, case.E1, case.nu1)
+    N = 24 * case.num
+    X = np.zeros(N)
+    S = np.zeros((max(case.nump, 1), 6))
+    rep = SolveReport()
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    cen, ax, qt = f64(case.centers), f64(case.axes), f64(case.quats)
+    pts = f64(case.points if case.nump else np.zeros((1, 3)))
+    sig = f64(case.sig_inf)
+    check(lib().ibem_e3d_run_host_ell(form, ctypes.byref(m), case.num, _dp(cen), _dp(ax), _dp(qt), case.nump, _dp(pts),
+                                      _dp(sig), tol, _dp(X), _dp(S), ctypes.byref(rep)))
+    return X, S[:case.nump], rep
 
 
 def run_dir(path: str, layout: int = 78, form: int = SOLVE_FP64, tol: float = 1e-12) -> SolveReport:

@@ -40,6 +40,8 @@ class Case:
     points: np.ndarray         # nump x 3
     sig_inf: np.ndarray | None = None   # far-field stress (6) for boundary-free cases
     title: str = "ibem_case"
+    axes: np.ndarray | None = None      # ellipsoids: num x 3 semi-axes (None: spheres of `radius`)
+    quats: np.ndarray | None = None     # ellipsoids: num x 4 unit quaternions (w, x, y, z)
 
     @property
     def NN(self) -> int:
@@ -281,3 +283,26 @@ def generated_case(num: int, r0: float, vf: float, seed: int, method: str = "mc"
     sig = np.array([0, 0, 0, 0, 0, sigma33], dtype=np.float64)
     return Case(E0, nu0, E1, nu1, np.zeros((0, 3)), np.zeros((0, 4), np.int32), np.zeros((0, 2)),
                 np.zeros((0, 24)), C, R, pts, sig, f"generated L={L!r}")
+
+
+def ellipsoid_case(num: int, a1: float = 0.008, vf: float = 0.15, seed: int = 31, grid: int = 0,
+                   a2=(0.5, 1.0), a3=(0.25, 1.0), gap: float = 0.2, E0: float = 70e9, nu0: float = 0.3,
+                   E1: float = 400e9, nu1: float = 0.2, sigma33: float = 1.0, max_tries: int = 0) -> Case:
+    """Boundary-free far-field case of `num` ellipsoids from the library's generator
+    (ibem_e3d_generate_ellipsoids): semi-axes a1, a1 U[a2], a1 U[a3], Haar-uniform
+    orientations, random sequential addition with the surfaces kept about gap * a3 apart,
+    cube side from the volume fraction `vf`; stresses on a cell-centred grid^3.  `radius`
+    holds the longest semi-axis (a bounding radius)."""
+    import ctypes
+
+    from . import EllGenParams, check, lib
+    p = EllGenParams(int(num), a1, a2[0], a2[1], a3[0], a3[1], vf, gap, int(seed), int(max_tries))
+    C, A, Q = np.zeros((num, 3)), np.zeros((num, 3)), np.zeros((num, 4))
+    side = ctypes.c_double(0.0)
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    check(lib().ibem_e3d_generate_ellipsoids(ctypes.byref(p), dp(C), dp(A), dp(Q), ctypes.byref(side)))
+    L = side.value
+    pts = cell_grid(grid, 0.0, L) if grid else np.zeros((0, 3))
+    sig = np.array([0, 0, 0, 0, 0, sigma33], dtype=np.float64)
+    return Case(E0, nu0, E1, nu1, np.zeros((0, 3)), np.zeros((0, 4), np.int32), np.zeros((0, 2)),
+                np.zeros((0, 24)), C, A.max(axis=1), pts, sig, f"ellipsoids L={L!r}", A, Q)

@@ -61,54 +61,90 @@ IBEM_HD IBEM_INLINE void jzero(Jet<T, K>& o) {
   for (int i = 0; i < Jet<T, K>::N; ++i) o.c[i] = T(0);
 }
 
+// Product tables: the (alpha, beta) decompositions of every output monomial gamma,
+// grouped by gamma; `last` marks the final term of a group.  Built at compile time; the
+// device reads them from constant memory (every thread of a warp reads the same entry).
+template <int K>
+struct MulTab {
+  static constexpr int NT = K == 3 ? 84 : (K == 4 ? 210 : 1);
+  unsigned char a[NT], b[NT], g[NT], last[NT];
+};
+
+template <int K>
+constexpr MulTab<K> make_multab() {
+  MulTab<K> t{};
+  int n = 0;
+  for (int d = 0; d <= K; ++d)
+    for (int g1 = d; g1 >= 0; --g1)
+      for (int g2 = d - g1; g2 >= 0; --g2) {
+        const int g3 = d - g1 - g2;
+        for (int a1 = 0; a1 <= g1; ++a1)
+          for (int a2 = 0; a2 <= g2; ++a2)
+            for (int a3 = 0; a3 <= g3; ++a3) {
+              t.a[n] = (unsigned char)midx(a1, a2, a3);
+              t.b[n] = (unsigned char)midx(g1 - a1, g2 - a2, g3 - a3);
+              t.g[n] = (unsigned char)midx(g1, g2, g3);
+              t.last[n] = 0;
+              ++n;
+            }
+        t.last[n - 1] = 1;
+      }
+  return t;
+}
+
+constexpr MulTab<3> kMulTab3 = make_multab<3>();
+constexpr MulTab<4> kMulTab4 = make_multab<4>();
+#ifdef __CUDACC__
+static __constant__ MulTab<3> kMulTab3Dev = make_multab<3>();
+static __constant__ MulTab<4> kMulTab4Dev = make_multab<4>();
+#endif
+
+template <int K>
+IBEM_HD IBEM_INLINE const MulTab<K>& multab() {
+#ifdef __CUDA_ARCH__
+  if constexpr (K == 3) return kMulTab3Dev; else return kMulTab4Dev;
+#else
+  if constexpr (K == 3) return kMulTab3; else return kMulTab4;
+#endif
+}
+
+// o = w_old * o + w * a * b  (o must not alias a or b)
+template <typename T, int K>
+IBEM_HD inline void jmul_acc(T keep, T w, const Jet<T, K>& a, const Jet<T, K>& b, Jet<T, K>& o) {
+  static_assert(K == 3 || K == 4, "jets of order 3 or 4");
+  const MulTab<K>& tb = multab<K>();
+  T acc = T(0);
+#pragma unroll 1
+  for (int t = 0; t < MulTab<K>::NT; ++t) {
+    acc += a.c[tb.a[t]] * b.c[tb.b[t]];
+    if (tb.last[t]) {
+      o.c[tb.g[t]] = keep * o.c[tb.g[t]] + w * acc;
+      acc = T(0);
+    }
+  }
+}
+
 // o = a * b (o must not alias a or b)
 template <typename T, int K>
 IBEM_HD IBEM_INLINE void jmul(const Jet<T, K>& a, const Jet<T, K>& b, Jet<T, K>& o) {
-#pragma unroll
-  for (int g1 = 0; g1 <= K; ++g1)
-#pragma unroll
-    for (int g2 = 0; g2 <= K - g1; ++g2)
-#pragma unroll
-      for (int g3 = 0; g3 <= K - g1 - g2; ++g3) {
-        T s = T(0);
-#pragma unroll
-        for (int a1 = 0; a1 <= g1; ++a1)
-#pragma unroll
-          for (int a2 = 0; a2 <= g2; ++a2)
-#pragma unroll
-            for (int a3 = 0; a3 <= g3; ++a3) s += a.c[midx(a1, a2, a3)] * b.c[midx(g1 - a1, g2 - a2, g3 - a3)];
-        o.c[midx(g1, g2, g3)] = s;
-      }
+  jzero(o);
+  jmul_acc(T(1), T(1), a, b, o);
 }
 
 // o += w * a * b
 template <typename T, int K>
 IBEM_HD IBEM_INLINE void jfma(T w, const Jet<T, K>& a, const Jet<T, K>& b, Jet<T, K>& o) {
-#pragma unroll
-  for (int g1 = 0; g1 <= K; ++g1)
-#pragma unroll
-    for (int g2 = 0; g2 <= K - g1; ++g2)
-#pragma unroll
-      for (int g3 = 0; g3 <= K - g1 - g2; ++g3) {
-        T s = T(0);
-#pragma unroll
-        for (int a1 = 0; a1 <= g1; ++a1)
-#pragma unroll
-          for (int a2 = 0; a2 <= g2; ++a2)
-#pragma unroll
-            for (int a3 = 0; a3 <= g3; ++a3) s += a.c[midx(a1, a2, a3)] * b.c[midx(g1 - a1, g2 - a2, g3 - a3)];
-        o.c[midx(g1, g2, g3)] += w * s;
-      }
+  jmul_acc(T(1), w, a, b, o);
 }
 
 // o = (l0 + l1 h1 + l2 h2 + l3 h3) * a   (o must not alias a)
 template <typename T, int K>
-IBEM_HD IBEM_INLINE void jmul_lin(T l0, T l1, T l2, T l3, const Jet<T, K>& a, Jet<T, K>& o) {
-#pragma unroll
+IBEM_HD inline void jmul_lin(T l0, T l1, T l2, T l3, const Jet<T, K>& a, Jet<T, K>& o) {
+#pragma unroll 1
   for (int g1 = 0; g1 <= K; ++g1)
-#pragma unroll
+#pragma unroll 1
     for (int g2 = 0; g2 <= K - g1; ++g2)
-#pragma unroll
+#pragma unroll 1
       for (int g3 = 0; g3 <= K - g1 - g2; ++g3) {
         T s = l0 * a.c[midx(g1, g2, g3)];
         if (g1 > 0) s += l1 * a.c[midx(g1 - 1, g2, g3)];
@@ -169,7 +205,7 @@ template <typename T>
 IBEM_HD inline void carlson_ik(const T x[3], T* ik) {
   using J = Jet<T, 3>;
   J X[3], A, A0;
-#pragma unroll
+#pragma unroll 1
   for (int m = 0; m < 3; ++m) {
     jzero(X[m]);
     X[m].c[0] = x[m];
@@ -177,7 +213,7 @@ IBEM_HD inline void carlson_ik(const T x[3], T* ik) {
   X[0].c[midx(1, 0, 0)] = T(1);
   X[1].c[midx(0, 1, 0)] = T(1);
   X[2].c[midx(0, 0, 1)] = T(1);
-#pragma unroll
+#pragma unroll 1
   for (int i = 0; i < J::N; ++i) A0.c[i] = (X[0].c[i] + X[1].c[i] + X[2].c[i]) / T(3);
   A = A0;
   // iteration count from the values (Carlson 1995, eq. 2.2-2.4 with r the unit roundoff)
@@ -188,15 +224,15 @@ IBEM_HD inline void carlson_ik(const T x[3], T* ik) {
   J s[3], lam, t;
 #pragma unroll 1
   for (int it = 0; it < 40 && pow4 * Qv >= fabs(A.c[0]); ++it) {
-#pragma unroll
+#pragma unroll 1
     for (int m = 0; m < 3; ++m) jpow(X[m], T(0.5), s[m]);
     jmul(s[0], s[1], lam);
     jfma(T(1), s[0], s[2], lam);
     jfma(T(1), s[1], s[2], lam);
-#pragma unroll
+#pragma unroll 1
     for (int i = 0; i < J::N; ++i) {
       A.c[i] = (A.c[i] + lam.c[i]) * T(0.25);
-#pragma unroll
+#pragma unroll 1
       for (int m = 0; m < 3; ++m) X[m].c[i] = (X[m].c[i] + lam.c[i]) * T(0.25);
     }
     pow4 *= T(0.25);
@@ -211,7 +247,7 @@ IBEM_HD inline void carlson_ik(const T x[3], T* ik) {
   d1.c[midx(0, 1, 0)] -= T(1);
   jmul(d0, invA, Xs);
   jmul(d1, invA, Ys);
-#pragma unroll
+#pragma unroll 1
   for (int i = 0; i < J::N; ++i) {
     Xs.c[i] *= pow4;
     Ys.c[i] *= pow4;
@@ -220,14 +256,14 @@ IBEM_HD inline void carlson_ik(const T x[3], T* ik) {
   J E2, E3, E22, E23;
   jmul(Xs, Ys, E2);
   jmul(Zs, Zs, t);
-#pragma unroll
+#pragma unroll 1
   for (int i = 0; i < J::N; ++i) E2.c[i] -= t.c[i];
   jmul(Xs, Ys, t);
   jmul(t, Zs, E3);
   jmul(E2, E2, E22);
   jmul(E2, E3, E23);
   J ser;
-#pragma unroll
+#pragma unroll 1
   for (int i = 0; i < J::N; ++i)
     ser.c[i] = -E2.c[i] / T(10) + E3.c[i] / T(14) + E22.c[i] / T(24) - T(3) * E23.c[i] / T(44);
   ser.c[0] += T(1);
@@ -235,11 +271,11 @@ IBEM_HD inline void carlson_ik(const T x[3], T* ik) {
   jpow(A, T(-0.5), rsA);
   jmul(rsA, ser, rf);
   const T w[4] = {T(1), T(-2), T(8.0 / 3.0), T(-16.0 / 5.0)};
-#pragma unroll
+#pragma unroll 1
   for (int k1 = 0; k1 <= 3; ++k1)
-#pragma unroll
+#pragma unroll 1
     for (int k2 = 0; k2 <= 3 - k1; ++k2)
-#pragma unroll
+#pragma unroll 1
       for (int k3 = 0; k3 <= 3 - k1 - k2; ++k3)
         ik[midx(k1, k2, k3)] = T(2) * rf.c[midx(k1, k2, k3)] * w[k1] * w[k2] * w[k3];
 }
@@ -259,7 +295,7 @@ IBEM_HD inline T ell_lambda(const T y[3], const T a2[3]) {
 #pragma unroll 1
   for (int it = 0; it < 100; ++it) {
     T f = T(-1), df = T(0);
-#pragma unroll
+#pragma unroll 1
     for (int m = 0; m < 3; ++m) {
       const T t = T(1) / (a2[m] + lam);
       f += y[m] * y[m] * t;
@@ -295,7 +331,7 @@ template <typename T, int K>
 IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], EllPot<T, K>& P) {
   using J = Jet<T, K>;
   T y[3], a2[3];
-#pragma unroll
+#pragma unroll 1
   for (int m = 0; m < 3; ++m) {
     y[m] = Q[m] * d[0] + Q[3 + m] * d[1] + Q[6 + m] * d[2];
     a2[m] = a[m] * a[m];
@@ -305,11 +341,11 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
   const T qin = y[0] * y[0] / a2[0] + y[1] * y[1] / a2[1] + y[2] * y[2] / a2[2];
   P.inside = qin <= T(1);
   T x[3];
-#pragma unroll
+#pragma unroll 1
   for (int m = 0; m < 3; ++m) x[m] = a2[m] + lam0;
   // l_m(h) = y_m + (Q^T h)_m and sq_m = l_m^2
   J sq[3];
-#pragma unroll
+#pragma unroll 1
   for (int m = 0; m < 3; ++m) {
     jzero(sq[m]);
     const T l1 = Q[m], l2 = Q[3 + m], l3 = Q[6 + m];
@@ -330,27 +366,27 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
   }
   // powers of delta(h) = lambda(c + d + h) - lambda0 (zero inside)
   J dp[K + 1];
-#pragma unroll
+#pragma unroll 1
   for (int n = 0; n <= K; ++n) jzero(dp[n]);
   dp[0].c[0] = T(1);
   if (!P.inside) {
     T gp = T(0);
-#pragma unroll
+#pragma unroll 1
     for (int m = 0; m < 3; ++m) gp -= y[m] * y[m] / (x[m] * x[m]);
     J del, G, inv, t;
     jzero(del);
 #pragma unroll 1
     for (int it = 0; it < K; ++it) {
       dp[1] = del;
-#pragma unroll
+#pragma unroll 1
       for (int n = 2; n <= K; ++n) jmul(dp[n - 1], del, dp[n]);
       jzero(G);
       G.c[0] = T(-1);
-#pragma unroll
+#pragma unroll 1
       for (int m = 0; m < 3; ++m) {
         jzero(inv);
         T xm = T(1) / x[m], s = xm;
-#pragma unroll
+#pragma unroll 1
         for (int n = 0; n <= K; ++n) {
           jaxpy(s, dp[n], inv);
           s *= -xm;
@@ -361,18 +397,18 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
       jaxpy(-T(1) / gp, G, del);
     }
     dp[1] = del;
-#pragma unroll
+#pragma unroll 1
     for (int n = 2; n <= K; ++n) jmul(dp[n - 1], del, dp[n]);
   }
   // I_k(lambda0) and their jets
   T ik[20];
   carlson_ik(x, ik);
   J I[20];
-#pragma unroll
+#pragma unroll 1
   for (int k1 = 0; k1 <= 3; ++k1)
-#pragma unroll
+#pragma unroll 1
     for (int k2 = 0; k2 <= 3 - k1; ++k2)
-#pragma unroll
+#pragma unroll 1
       for (int k3 = 0; k3 <= 3 - k1 - k2; ++k3) {
         const int id = midx(k1, k2, k3);
         J& o = I[id];
@@ -383,32 +419,32 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
           const int kk[3] = {k1, k2, k3};
           T b[K + 1];
           b[0] = T(1);
-#pragma unroll
+#pragma unroll 1
           for (int n = 1; n <= K; ++n) b[n] = T(0);
           T f0 = T(1);
-#pragma unroll
+#pragma unroll 1
           for (int m = 0; m < 3; ++m) {
             const T qm = T(kk[m]) + T(0.5);
             f0 *= pow(x[m], -qm);
             T bm[K + 1], coef = T(1);
             bm[0] = T(1);
-#pragma unroll
+#pragma unroll 1
             for (int n = 1; n <= K; ++n) {
               coef *= (-qm - T(n - 1)) / T(n);
               bm[n] = coef / pow(x[m], T(n));
             }
             T nb[K + 1];
-#pragma unroll
+#pragma unroll 1
             for (int n = 0; n <= K; ++n) {
               T s = T(0);
-#pragma unroll
+#pragma unroll 1
               for (int j = 0; j <= n; ++j) s += b[j] * bm[n - j];
               nb[n] = s;
             }
-#pragma unroll
+#pragma unroll 1
             for (int n = 0; n <= K; ++n) b[n] = nb[n];
           }
-#pragma unroll
+#pragma unroll 1
           for (int n = 0; n < K; ++n) jaxpy(-f0 * b[n] / T(n + 1), dp[n + 1], o);
         }
       }
@@ -420,47 +456,47 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
   // phi_1 = C F1_0
   J F;
   F = I[0];
-#pragma unroll
+#pragma unroll 1
   for (int m = 0; m < 3; ++m) jfma(-T(1), sq[m], I[e(m, 0, 0, 0)], F);
-#pragma unroll
+#pragma unroll 1
   for (int i = 0; i < J::N; ++i) P.f0.c[i] = C * F.c[i];
   // phi_{y'_m} = C a_m^2 l_m F1_{e_m}, rotated to global densities
   J p1[3];
-#pragma unroll
+#pragma unroll 1
   for (int m = 0; m < 3; ++m) {
     const int km[3] = {m == 0, m == 1, m == 2};
     F = I[midx(km[0], km[1], km[2])];
-#pragma unroll
+#pragma unroll 1
     for (int n = 0; n < 3; ++n) jfma(-T(1), sq[n], I[e(n, km[0], km[1], km[2])], F);
     jmul_lin(C * a2[m] * y[m], C * a2[m] * Q[m], C * a2[m] * Q[3 + m], C * a2[m] * Q[6 + m], F, p1[m]);
   }
-#pragma unroll
+#pragma unroll 1
   for (int p = 0; p < 3; ++p) {
     jzero(P.f1[p]);
-#pragma unroll
+#pragma unroll 1
     for (int m = 0; m < 3; ++m) jaxpy(Q[3 * p + m], p1[m], P.f1[p]);
   }
   // phi_{y'_m y'_n}
   J F20;   // F2_0
   F20 = I[0];
-#pragma unroll
+#pragma unroll 1
   for (int m = 0; m < 3; ++m) jfma(-T(2), sq[m], I[e(m, 0, 0, 0)], F20);
-#pragma unroll
+#pragma unroll 1
   for (int m = 0; m < 3; ++m)
-#pragma unroll
+#pragma unroll 1
     for (int n = 0; n < 3; ++n) {
       jmul(sq[m], sq[n], u);
       jfma(T(1), u, I[midx((m == 0) + (n == 0), (m == 1) + (n == 1), (m == 2) + (n == 2))], F20);
     }
   J p2[6];
-#pragma unroll
+#pragma unroll 1
   for (int m = 0; m < 3; ++m)
-#pragma unroll
+#pragma unroll 1
     for (int n = m; n < 3; ++n) {
       const int km[3] = {(m == 0) + (n == 0), (m == 1) + (n == 1), (m == 2) + (n == 2)};
       // F1_{e_m + e_n}, times a_m^2 a_n^2 l_m l_n
       F = I[midx(km[0], km[1], km[2])];
-#pragma unroll
+#pragma unroll 1
       for (int r = 0; r < 3; ++r) jfma(-T(1), sq[r], I[e(r, km[0], km[1], km[2])], F);
       jmul_lin(y[m], Q[m], Q[3 + m], Q[6 + m], F, t);
       J& o = p2[sym_pair(m, n)];
@@ -471,11 +507,11 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
         jaxpy(C * a2[m] / T(4), F20, o);
         const int em[3] = {m == 0, m == 1, m == 2};
         F = I[midx(em[0], em[1], em[2])];
-#pragma unroll
+#pragma unroll 1
         for (int r = 0; r < 3; ++r) jfma(-T(2), sq[r], I[e(r, em[0], em[1], em[2])], F);
-#pragma unroll
+#pragma unroll 1
         for (int r = 0; r < 3; ++r)
-#pragma unroll
+#pragma unroll 1
           for (int s = 0; s < 3; ++s) {
             jmul(sq[r], sq[s], u);
             jfma(T(1), u,
@@ -485,15 +521,15 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
       }
     }
   // global densities x'_p x'_q = sum_mn Q_pm Q_qn y'_m y'_n
-#pragma unroll
+#pragma unroll 1
   for (int p = 0; p < 3; ++p)
-#pragma unroll
+#pragma unroll 1
     for (int q = p; q < 3; ++q) {
       J& o = P.f2[sym_pair(p, q)];
       jzero(o);
-#pragma unroll
+#pragma unroll 1
       for (int m = 0; m < 3; ++m)
-#pragma unroll
+#pragma unroll 1
         for (int n = 0; n < 3; ++n) jaxpy(Q[3 * p + m] * Q[3 * q + n], p2[sym_pair(m, n)], o);
     }
 }

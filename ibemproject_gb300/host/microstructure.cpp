@@ -57,6 +57,13 @@ struct Rng {
 };
 
 inline double min_dist(double ri, double rj, double gap) { return ri + rj + gap * std::max(ri, rj); }
+}  // namespace
+
+namespace ibem {
+void ell_quat_to_rot_host(const double* q, double* Q);
+}
+
+namespace {
 
 // Uniform cell grid over [0, L]^3 with cells no smaller than `h`, one vector of sphere
 // indices per cell.
@@ -215,7 +222,143 @@ ibem_status mc(const ibem_gen_params& p, double L, std::vector<double>& c, const
   return ibem::fail(IBEM_ERR_ARG, "generate_spheres: compression did not reach the volume fraction");
 }
 
+// ---------------------------------------------------------------- ellipsoids
+// Perram-Wertheim contact function of two ellipsoids x^T M_A x <= 1 and x^T M_B x <= 1
+// (M = Q diag(a^-2) Q^T) whose centres differ by r:
+//   F(lam) = lam (1 - lam) r^T [(1 - lam) M_A^-1 + lam M_B^-1]^-1 r,  0 <= lam <= 1;
+// F is concave and the bodies are disjoint exactly when max F > 1 (J. W. Perram and
+// M. S. Wertheim, J. Comput. Phys. 58 (1985) 409).  Scaling r by s scales F by s^2.
+struct Ell {
+  double P[9];   // M^-1 = Q diag(a^2) Q^T
+  double rb;     // bounding radius (longest semi-axis)
+  double ri;     // inscribed radius (shortest semi-axis)
+};
+
+Ell make_ell(const double* a, const double* q, double inflate) {
+  Ell e;
+  double Q[9];
+  ibem::ell_quat_to_rot_host(q, Q);
+  double s[3];
+  for (int m = 0; m < 3; ++m) s[m] = (a[m] + inflate) * (a[m] + inflate);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double v = 0.0;
+      for (int m = 0; m < 3; ++m) v += Q[3 * i + m] * s[m] * Q[3 * j + m];
+      e.P[3 * i + j] = v;
+    }
+  e.rb = std::max(a[0], std::max(a[1], a[2])) + inflate;
+  e.ri = std::min(a[0], std::min(a[1], a[2])) + inflate;
+  return e;
+}
+
+double pw_value(const Ell& A, const Ell& B, const double* r, double lam) {
+  double G[9];
+  for (int i = 0; i < 9; ++i) G[i] = (1.0 - lam) * A.P[i] + lam * B.P[i];
+  // r^T G^-1 r by Cramer's rule (G symmetric positive definite)
+  const double c00 = G[4] * G[8] - G[5] * G[7], c01 = G[5] * G[6] - G[3] * G[8], c02 = G[3] * G[7] - G[4] * G[6];
+  const double det = G[0] * c00 + G[1] * c01 + G[2] * c02;
+  const double c11 = G[0] * G[8] - G[2] * G[6], c12 = G[2] * G[3] - G[0] * G[5], c22 = G[0] * G[4] - G[1] * G[3];
+  const double q = r[0] * r[0] * c00 + r[1] * r[1] * c11 + r[2] * r[2] * c22 +
+                   2.0 * (r[0] * r[1] * c01 + r[0] * r[2] * c02 + r[1] * r[2] * c12);
+  return lam * (1.0 - lam) * q / det;
+}
+
+// max_lam F by golden-section search (F is concave on [0, 1])
+double pw_max(const Ell& A, const Ell& B, const double* r) {
+  const double g = 0.6180339887498949;
+  double lo = 0.0, hi = 1.0, x1 = hi - g * (hi - lo), x2 = lo + g * (hi - lo);
+  double f1 = pw_value(A, B, r, x1), f2 = pw_value(A, B, r, x2);
+  for (int it = 0; it < 40; ++it) {
+    if (f1 < f2) { lo = x1; x1 = x2; f1 = f2; x2 = lo + g * (hi - lo); f2 = pw_value(A, B, r, x2); }
+    else { hi = x2; x2 = x1; f2 = f1; x1 = hi - g * (hi - lo); f1 = pw_value(A, B, r, x1); }
+  }
+  return std::max(f1, f2);
+}
+
+// true when the (inflated) ellipsoids overlap
+bool ell_overlap(const Ell& A, const Ell& B, const double* r) {
+  const double d2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+  if (d2 >= (A.rb + B.rb) * (A.rb + B.rb)) return false;
+  if (d2 < (A.ri + B.ri) * (A.ri + B.ri)) return true;
+  return pw_max(A, B, r) <= 1.0;
+}
+
+// Haar-uniform unit quaternion (w, x, y, z) from three uniforms (K. Shoemake, Graphics Gems III, 1992)
+void uniform_quat(Rng& g, double* q) {
+  const double u1 = g.uniform(), u2 = 2.0 * M_PI * g.uniform(), u3 = 2.0 * M_PI * g.uniform();
+  const double s1 = std::sqrt(1.0 - u1), s2 = std::sqrt(u1);
+  q[0] = s2 * std::cos(u3);
+  q[1] = s1 * std::sin(u2);
+  q[2] = s1 * std::cos(u2);
+  q[3] = s2 * std::sin(u3);
+}
+
 }  // namespace
+
+namespace ibem {
+void ell_quat_to_rot_host(const double* q, double* Q) {
+  const double n = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  const double w = q[0] / n, x = q[1] / n, y = q[2] / n, z = q[3] / n;
+  Q[0] = 1 - 2 * (y * y + z * z); Q[1] = 2 * (x * y - w * z); Q[2] = 2 * (x * z + w * y);
+  Q[3] = 2 * (x * y + w * z); Q[4] = 1 - 2 * (x * x + z * z); Q[5] = 2 * (y * z - w * x);
+  Q[6] = 2 * (x * z - w * y); Q[7] = 2 * (y * z + w * x); Q[8] = 1 - 2 * (x * x + y * y);
+}
+}  // namespace ibem
+
+extern "C" ibem_status ibem_e3d_generate_ellipsoids(const ibem_ell_gen_params* p, double* centers, double* axes,
+                                                    double* quats, double* side) {
+  if (!p || p->num < 1 || !centers || !axes || !quats || !(p->a1 > 0) || !(p->a2lo > 0) || p->a2hi < p->a2lo ||
+      !(p->a3lo > 0) || p->a3hi < p->a3lo || p->a2hi > 1 || p->a3hi > 1 || !(p->vf > 0 && p->vf < 0.5) ||
+      p->gap < 0)
+    return ibem::fail(IBEM_ERR_ARG, "generate_ellipsoids: bad parameters");
+  const int num = p->num;
+  Rng rs(p->seed);
+  std::vector<double> a(3 * (size_t)num), q(4 * (size_t)num), c(3 * (size_t)num, 0.0);
+  double vol = 0.0;
+  for (int k = 0; k < num; ++k) {
+    a[3 * k] = p->a1;
+    a[3 * k + 1] = p->a1 * rs.uniform(p->a2lo, p->a2hi);
+    a[3 * k + 2] = p->a1 * rs.uniform(p->a3lo, p->a3hi);
+    uniform_quat(rs, &q[4 * k]);
+    vol += 4.0 / 3.0 * M_PI * a[3 * k] * a[3 * k + 1] * a[3 * k + 2];
+  }
+  const double L = std::cbrt(vol / p->vf);
+  // surfaces kept apart by inflating every semi-axis by gap * a3 / 2 during the tests
+  std::vector<Ell> e(num);
+  double rbmax = 0.0;
+  for (int k = 0; k < num; ++k) {
+    e[k] = make_ell(&a[3 * k], &q[4 * k], 0.5 * p->gap * a[3 * k + 2]);
+    rbmax = std::max(rbmax, e[k].rb);
+  }
+  const double lo = p->a1, hi = L - p->a1;
+  if (hi <= lo) return ibem::fail(IBEM_ERR_ARG, "generate_ellipsoids: cube smaller than one ellipsoid");
+  Rng rng(p->seed + 0x632be59bd9b4e019ULL);
+  Cells g;
+  g.build(L, 2.0 * rbmax, c, 0);
+  const int64_t cap = p->max_tries > 0 ? p->max_tries : 200000000LL;
+  int64_t tries = 0;
+  for (int k = 0; k < num; ++k) {
+    double x[3];
+    bool bad;
+    do {
+      if (++tries > cap)
+        return ibem::fail(IBEM_ERR_ARG, "generate_ellipsoids: random sequential addition stalled at " +
+                                            std::to_string(k) + " of " + std::to_string(num));
+      for (double& v : x) v = rng.uniform(lo, hi);
+      bad = g.any_near(x, [&](int j) {
+        const double r[3] = {c[3 * j] - x[0], c[3 * j + 1] - x[1], c[3 * j + 2] - x[2]};
+        return ell_overlap(e[k], e[j], r);
+      });
+    } while (bad);
+    std::memcpy(&c[3 * k], x, sizeof x);
+    g.insert(k, x);
+  }
+  std::memcpy(centers, c.data(), sizeof(double) * c.size());
+  std::memcpy(axes, a.data(), sizeof(double) * a.size());
+  std::memcpy(quats, q.data(), sizeof(double) * q.size());
+  if (side) *side = L;
+  return IBEM_OK;
+}
 
 extern "C" ibem_status ibem_e3d_generate_spheres(const ibem_gen_params* p, double* centers, double* radius,
                                                  double* side) {

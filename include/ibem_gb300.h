@@ -369,6 +369,26 @@ typedef struct {
 ibem_status ibem_e3d_generate_spheres(const ibem_gen_params* p, double* centers, double* radius,
                                       double* side);
 
+/* Seeded ellipsoid microstructures: semi-axes a1, a2 = a1 U[a2lo, a2hi], a3 = a1 U[a3lo, a3hi]
+ * (a3 is then the shortest only if a3hi <= a2lo), orientations uniform on SO(3) (Haar,
+ * quaternions from three uniforms), centres by random sequential addition inside the cube
+ * [a1, L - a1]^3 of side L = (sum of volumes / vf)^(1/3).  Two ellipsoids are kept apart
+ * by testing them with every semi-axis inflated by gap * a3 / 2 (Perram-Wertheim contact
+ * function).  Host outputs: centers n x 3, axes n x 3 (a1 a2 a3 along the principal
+ * axes), quats n x 4 (w, x, y, z), side (may be NULL).  Host only. */
+typedef struct {
+  int num;
+  double a1;
+  double a2lo, a2hi, a3lo, a3hi;
+  double vf;
+  double gap;
+  uint64_t seed;
+  int64_t max_tries;  /* candidate centres before giving up (0 = 2e8) */
+} ibem_ell_gen_params;
+
+ibem_status ibem_e3d_generate_ellipsoids(const ibem_ell_gen_params* p, double* centers, double* axes,
+                                         double* quats, double* side);
+
 /* ---- learned preconditioner (no reference counterpart) --------------------- */
 /* On the graph of each particle's 16 nearest neighbours (edges e = (i <- j)), with B the
  * block-Jacobi inverses and As the scaled pair blocks, the Neumann series of As^-1 gives
@@ -462,6 +482,40 @@ ibem_status ibem_e3d_field_grid(ibem_solver_form form, const double* lo, const d
                                 const double* nodes_dev, int NN, const int* conn_dev, int NE,
                                 const double* U_dev, const double* T_dev, const double* sig_inf,
                                 double* stress_dev, void* stream);
+
+/* ---- ellipsoidal inclusions (layout 24, boundary-free cases) ---------------- */
+
+/* No reference counterpart: the reference's elastic integrator treats spheres only
+ * (integratorElastic3DHelper.cpp:41-664).  An ellipsoid h has a centre (centers_dev, n x 3),
+ * semi-axes a1, a2, a3 (axes_dev, n x 3) along its principal axes, and an orientation
+ * (quats_dev, n x 4: unit quaternion w, x, y, z taking the principal frame to the global
+ * one; normalised on use).  Unknowns per particle: the 24 of layout 24 (E_ij, E_ijp) in
+ * global coordinates about the centre.  For a1 = a2 = a3 every result equals the sphere
+ * entry point's.  Device pointers; up to 65535 ellipsoids per call. */
+
+/* Pair blocks of the equivalent-inclusion rows (the ellipsoid counterpart of
+ * ibem_e3d_pair_blocks with layout 24; integratorElastic3D.cpp:341-567): the (24 num)^2
+ * block at A[row0.., col0..] (column-major, lda), FP64. */
+ibem_status ibem_e3d_ell_pair_blocks(const double* centers_dev, const double* axes_dev, const double* quats_dev,
+                                     int num, const ibem_material* mat, double* A_dev, int64_t lda, int64_t row0,
+                                     int64_t col0, void* stream);
+
+/* Stresses at sample points under the remote stress sig_inf (host, 6) from the layout-24
+ * eigenstrain E_dev (postProcessorElastic3D.cpp:367-522 with ellipsoids): stress_dev is
+ * overwritten (nump x 6, xx xy xz yy yz zz).  form IBEM_SOLVE_FP64: FP64 throughout;
+ * IBEM_SOLVE_MIXED_IR: an ellipsoid farther than 14 of its longest semi-axes from all 32
+ * points of a warp is evaluated in FP32. */
+ibem_status ibem_e3d_ell_field(ibem_solver_form form, const double* points_dev, int nump, const double* centers_dev,
+                               const double* axes_dev, const double* quats_dev, int num, const ibem_material* mat,
+                               const double* E_dev, const double* sig_inf, double* stress_dev, void* stream);
+
+/* Whole boundary-free ellipsoid pipeline on host arrays (pair blocks, far-field right-hand
+ * side, dense solve in `form` (IBEM_SOLVE_FP64 or IBEM_SOLVE_MIXED_IR), stresses), all
+ * copies inside: X (24 num) and stress (nump x 6) are host outputs.  Synchronous. */
+ibem_status ibem_e3d_run_host_ell(ibem_solver_form form, const ibem_material* mat, int num, const double* centers,
+                                  const double* axes, const double* quats, int nump, const double* points,
+                                  const double* sig_inf, double tol, double* X, double* stress,
+                                  ibem_solve_report* report);
 
 /* ---- whole pipeline on host buffers --------------------------------------- */
 
