@@ -3,6 +3,7 @@
 
 #include <cstdint>
 
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -52,10 +53,11 @@ namespace {
 __global__ void k_bc_ucols(int64_t N, int n3, const int* __restrict__ ucol, const double* __restrict__ H,
                            int64_t ldh, double* __restrict__ A, int64_t lda) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
-  if (i >= N || j >= n3) return;
-  const int c = ucol[j];
-  if (c >= 0) A[(int64_t)c * lda + i] = H[(int64_t)j * ldh + i];
+  if (i >= N) return;
+  for (int j = blockIdx.y; j < n3; j += gridDim.y) {
+    const int c = ucol[j];
+    if (c >= 0) A[(int64_t)c * lda + i] = H[(int64_t)j * ldh + i];
+  }
 }
 __global__ void k_bc_tcols(int64_t N, int nt, const int* __restrict__ tcol, const double* __restrict__ G,
                            int64_t ldg, double* __restrict__ A, int64_t lda) {
@@ -234,7 +236,7 @@ ibem_status ibem_e3d_apply_bc(int NN, int NE, int64_t N, const int* ucol_dev, co
   cudaStream_t st = as_stream(stream);
   IBEM_CUDA(cudaMemset2DAsync(A_dev, lda * sizeof(double), 0, N * sizeof(double), n3, st));
   const unsigned gx = (unsigned)((N + 255) / 256);
-  ::ibem::count_launch(), k_bc_ucols<<<dim3(gx, n3), 256, 0, st>>>(N, n3, ucol_dev, H_dev, ldh, A_dev, lda);
+  ::ibem::count_launch(), k_bc_ucols<<<dim3(gx, std::min(n3, 65535)), 256, 0, st>>>(N, n3, ucol_dev, H_dev, ldh, A_dev, lda);
   for (int k0 = 0; k0 < nt; k0 += 65535) {
     const int cnt = std::min(65535, nt - k0);
     ::ibem::count_launch(), k_bc_tcols<<<dim3(gx, cnt), 256, 0, st>>>(N, cnt, tcol_dev + k0, G_dev + (int64_t)k0 * ldg, ldg, A_dev, lda);

@@ -92,6 +92,42 @@ constexpr MulTab<K> make_multab() {
   return t;
 }
 
+// Shift tables: for every monomial gamma (midx order) the index of gamma - e_i (255: none).
+template <int K>
+struct ShiftTab {
+  unsigned char s[nmono(K)][3];
+};
+
+template <int K>
+constexpr ShiftTab<K> make_shifttab() {
+  ShiftTab<K> t{};
+  for (int d = 0; d <= K; ++d)
+    for (int g1 = d; g1 >= 0; --g1)
+      for (int g2 = d - g1; g2 >= 0; --g2) {
+        const int g3 = d - g1 - g2, id = midx(g1, g2, g3);
+        t.s[id][0] = (unsigned char)(g1 > 0 ? midx(g1 - 1, g2, g3) : 255);
+        t.s[id][1] = (unsigned char)(g2 > 0 ? midx(g1, g2 - 1, g3) : 255);
+        t.s[id][2] = (unsigned char)(g3 > 0 ? midx(g1, g2, g3 - 1) : 255);
+      }
+  return t;
+}
+
+constexpr ShiftTab<3> kShiftTab3 = make_shifttab<3>();
+constexpr ShiftTab<4> kShiftTab4 = make_shifttab<4>();
+#ifdef __CUDACC__
+static __constant__ ShiftTab<3> kShiftTab3Dev = make_shifttab<3>();
+static __constant__ ShiftTab<4> kShiftTab4Dev = make_shifttab<4>();
+#endif
+
+template <int K>
+IBEM_HD IBEM_INLINE const ShiftTab<K>& shifttab() {
+#ifdef __CUDA_ARCH__
+  if constexpr (K == 3) return kShiftTab3Dev; else return kShiftTab4Dev;
+#else
+  if constexpr (K == 3) return kShiftTab3; else return kShiftTab4;
+#endif
+}
+
 constexpr MulTab<3> kMulTab3 = make_multab<3>();
 constexpr MulTab<4> kMulTab4 = make_multab<4>();
 #ifdef __CUDACC__
@@ -140,18 +176,15 @@ IBEM_HD IBEM_INLINE void jfma(T w, const Jet<T, K>& a, const Jet<T, K>& b, Jet<T
 // o = (l0 + l1 h1 + l2 h2 + l3 h3) * a   (o must not alias a)
 template <typename T, int K>
 IBEM_HD inline void jmul_lin(T l0, T l1, T l2, T l3, const Jet<T, K>& a, Jet<T, K>& o) {
+  const ShiftTab<K>& sh = shifttab<K>();
 #pragma unroll 1
-  for (int g1 = 0; g1 <= K; ++g1)
-#pragma unroll 1
-    for (int g2 = 0; g2 <= K - g1; ++g2)
-#pragma unroll 1
-      for (int g3 = 0; g3 <= K - g1 - g2; ++g3) {
-        T s = l0 * a.c[midx(g1, g2, g3)];
-        if (g1 > 0) s += l1 * a.c[midx(g1 - 1, g2, g3)];
-        if (g2 > 0) s += l2 * a.c[midx(g1, g2 - 1, g3)];
-        if (g3 > 0) s += l3 * a.c[midx(g1, g2, g3 - 1)];
-        o.c[midx(g1, g2, g3)] = s;
-      }
+  for (int g = 0; g < Jet<T, K>::N; ++g) {
+    T v = l0 * a.c[g];
+    if (sh.s[g][0] != 255) v += l1 * a.c[sh.s[g][0]];
+    if (sh.s[g][1] != 255) v += l2 * a.c[sh.s[g][1]];
+    if (sh.s[g][2] != 255) v += l3 * a.c[sh.s[g][2]];
+    o.c[g] = v;
+  }
 }
 
 // o += w * a
@@ -180,18 +213,15 @@ IBEM_HD IBEM_INLINE void jcompose(const Jet<T, K>& a, const T* f, Jet<T, K>& o) 
   }
 }
 
-// a^(q) for real q (a0 > 0)
+// a^q for q in {1/2, -1/2, -1} (a0 > 0): f_0 = a0^q from sqrt / reciprocal, then the
+// Taylor coefficients f_n = f_(n-1) (q - n + 1) / (n a0)
 template <typename T, int K>
-IBEM_HD IBEM_INLINE void jpow(const Jet<T, K>& a, T q, Jet<T, K>& o) {
+IBEM_HD IBEM_INLINE void jpow(const Jet<T, K>& a, int twice_q, Jet<T, K>& o) {
   T f[K + 1];
-  const T a0 = a.c[0];
-  f[0] = pow(a0, q);
-  T coef = T(1);
+  const T a0 = a.c[0], ia = T(1) / a0, q = T(twice_q) / T(2);
+  f[0] = twice_q == 1 ? sqrt(a0) : (twice_q == -1 ? T(1) / sqrt(a0) : ia);
 #pragma unroll
-  for (int n = 1; n <= K; ++n) {
-    coef *= (q - T(n - 1)) / T(n);
-    f[n] = f[0] * coef / pow(a0, T(n));
-  }
+  for (int n = 1; n <= K; ++n) f[n] = f[n - 1] * (q - T(n - 1)) / T(n) * ia;
   jcompose(a, f, o);
 }
 
@@ -217,15 +247,15 @@ IBEM_HD inline void carlson_ik(const T x[3], T* ik) {
   for (int i = 0; i < J::N; ++i) A0.c[i] = (X[0].c[i] + X[1].c[i] + X[2].c[i]) / T(3);
   A = A0;
   // iteration count from the values (Carlson 1995, eq. 2.2-2.4 with r the unit roundoff)
-  const T r = sizeof(T) == sizeof(double) ? T(1.1102230246251565e-16) : T(5.9604645e-08);
-  const T Qv = pow(T(3) * r, T(-1.0 / 6.0)) *
+  // (3 r)^(-1/6)
+  const T Qv = (sizeof(T) == sizeof(double) ? T(379.82022430228585) : T(13.322930834122156)) *
                fmax(fabs(A0.c[0] - x[0]), fmax(fabs(A0.c[0] - x[1]), fabs(A0.c[0] - x[2])));
   T pow4 = T(1);
   J s[3], lam, t;
 #pragma unroll 1
   for (int it = 0; it < 40 && pow4 * Qv >= fabs(A.c[0]); ++it) {
 #pragma unroll 1
-    for (int m = 0; m < 3; ++m) jpow(X[m], T(0.5), s[m]);
+    for (int m = 0; m < 3; ++m) jpow(X[m], 1, s[m]);
     jmul(s[0], s[1], lam);
     jfma(T(1), s[0], s[2], lam);
     jfma(T(1), s[1], s[2], lam);
@@ -239,7 +269,7 @@ IBEM_HD inline void carlson_ik(const T x[3], T* ik) {
   }
   // X = (A0 - x) / (4^m A), Y likewise, Z = -X - Y
   J invA, Xs, Ys, Zs;
-  jpow(A, T(-1), invA);
+  jpow(A, -2, invA);
   J d0 = A0, d1 = A0;
   d0.c[0] -= x[0];
   d0.c[midx(1, 0, 0)] -= T(1);
@@ -268,7 +298,7 @@ IBEM_HD inline void carlson_ik(const T x[3], T* ik) {
     ser.c[i] = -E2.c[i] / T(10) + E3.c[i] / T(14) + E22.c[i] / T(24) - T(3) * E23.c[i] / T(44);
   ser.c[0] += T(1);
   J rsA, rf;
-  jpow(A, T(-0.5), rsA);
+  jpow(A, -1, rsA);
   jmul(rsA, ser, rf);
   const T w[4] = {T(1), T(-2), T(8.0 / 3.0), T(-16.0 / 5.0)};
 #pragma unroll 1
@@ -403,6 +433,13 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
   // I_k(lambda0) and their jets
   T ik[20];
   carlson_ik(x, ik);
+  // 1 / x_m, 1 / sqrt(x_m) for the lambda-derivatives
+  T ix[3], rx[3];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    ix[m] = T(1) / x[m];
+    rx[m] = sqrt(ix[m]);
+  }
   J I[20];
 #pragma unroll 1
   for (int k1 = 0; k1 <= 3; ++k1)
@@ -419,39 +456,43 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
           const int kk[3] = {k1, k2, k3};
           T b[K + 1];
           b[0] = T(1);
-#pragma unroll 1
+#pragma unroll
           for (int n = 1; n <= K; ++n) b[n] = T(0);
           T f0 = T(1);
 #pragma unroll 1
           for (int m = 0; m < 3; ++m) {
             const T qm = T(kk[m]) + T(0.5);
-            f0 *= pow(x[m], -qm);
+            f0 *= rx[m];
+            for (int j = 0; j < kk[m]; ++j) f0 *= ix[m];
             T bm[K + 1], coef = T(1);
             bm[0] = T(1);
-#pragma unroll 1
+#pragma unroll
             for (int n = 1; n <= K; ++n) {
-              coef *= (-qm - T(n - 1)) / T(n);
-              bm[n] = coef / pow(x[m], T(n));
+              coef *= (-qm - T(n - 1)) / T(n) * ix[m];
+              bm[n] = coef;
             }
-            T nb[K + 1];
-#pragma unroll 1
-            for (int n = 0; n <= K; ++n) {
+#pragma unroll
+            for (int n = K; n >= 1; --n) {
               T s = T(0);
-#pragma unroll 1
+#pragma unroll
               for (int j = 0; j <= n; ++j) s += b[j] * bm[n - j];
-              nb[n] = s;
+              b[n] = s;
             }
-#pragma unroll 1
-            for (int n = 0; n <= K; ++n) b[n] = nb[n];
           }
 #pragma unroll 1
           for (int n = 0; n < K; ++n) jaxpy(-f0 * b[n] / T(n + 1), dp[n + 1], o);
         }
       }
+  // the six products sq_m sq_n (pairs 00 01 02 11 12 22)
+  J sq2[6];
+#pragma unroll 1
+  for (int m = 0; m < 3; ++m)
+#pragma unroll 1
+    for (int n = m; n < 3; ++n) jmul(sq[m], sq[n], sq2[sym_pair(m, n)]);
   // F1_j = int U prod t^j ds/Delta = I_j - sum_m sq_m I_{j+e_m}
   // F2_j = int U^2 prod t^j ds/Delta = I_j - 2 sum_m sq_m I_{j+e_m} + sum_{m,n} sq_m sq_n I_{j+e_m+e_n}
   const T C = T(IBEM_PI) * a[0] * a[1] * a[2];
-  J t, u;
+  J t;
   auto e = [](int m, int k1, int k2, int k3) { return midx(k1 + (m == 0), k2 + (m == 1), k3 + (m == 2)); };
   // phi_1 = C F1_0
   J F;
@@ -484,10 +525,9 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
 #pragma unroll 1
   for (int m = 0; m < 3; ++m)
 #pragma unroll 1
-    for (int n = 0; n < 3; ++n) {
-      jmul(sq[m], sq[n], u);
-      jfma(T(1), u, I[midx((m == 0) + (n == 0), (m == 1) + (n == 1), (m == 2) + (n == 2))], F20);
-    }
+    for (int n = m; n < 3; ++n)
+      jfma(m == n ? T(1) : T(2), sq2[sym_pair(m, n)], I[midx((m == 0) + (n == 0), (m == 1) + (n == 1), (m == 2) + (n == 2))],
+           F20);
   J p2[6];
 #pragma unroll 1
   for (int m = 0; m < 3; ++m)
@@ -512,11 +552,9 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
 #pragma unroll 1
         for (int r = 0; r < 3; ++r)
 #pragma unroll 1
-          for (int s = 0; s < 3; ++s) {
-            jmul(sq[r], sq[s], u);
-            jfma(T(1), u,
+          for (int s = r; s < 3; ++s)
+            jfma(r == s ? T(1) : T(2), sq2[sym_pair(r, s)],
                  I[midx(em[0] + (r == 0) + (s == 0), em[1] + (r == 1) + (s == 1), em[2] + (r == 2) + (s == 2))], F);
-          }
         jaxpy(-C * a2[m] * a2[m] / T(4), F, o);
       }
     }
@@ -535,60 +573,73 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
 }
 
 // ------------------------------------------------------------------ derivatives
-IBEM_HD constexpr int fact(int n) { return n <= 1 ? 1 : n * fact(n - 1); }
-
-// d^alpha f at h = 0 from the jet coefficient (alpha given by index counts)
+// Derivative tables of one evaluation: phi[r][midx(alpha)] = d^alpha phi_rho for |alpha| <= K
+// and psi[r][midx(beta)] = d^beta psi_rho for 4 <= |beta| <= K + 1, with r = 0 the uniform
+// density and r = 1 + p the density x'_p.  d^beta psi = d^(beta - e_k) (x_k phi_rho -
+// phi_{rho x'_k}) for any k with beta_k > 0; d^alpha (h_k f) = alpha! c_(alpha - e_k)(f).
 template <typename T, int K>
-IBEM_HD IBEM_INLINE T jder(const Jet<T, K>& f, int a1, int a2, int a3) {
-  return T(fact(a1) * fact(a2) * fact(a3)) * f.c[midx(a1, a2, a3)];
-}
+struct EllDer {
+  T phi[4][nmono(K)];
+  T psi[4][nmono(K + 1)];
+  bool inside;
+};
 
-// counts of an index list
-IBEM_HD IBEM_INLINE void counts(const int* idx, int n, int* c) {
-  c[0] = c[1] = c[2] = 0;
-  for (int s = 0; s < n; ++s) ++c[idx[s]];
-}
+IBEM_HD IBEM_INLINE int fact_small(int n) { return n <= 1 ? 1 : (n == 2 ? 2 : (n == 3 ? 6 : (n == 4 ? 24 : 120))); }
 
-// phi_rho,idx  (rho: -1 uniform, p = 0..2 the linear density x'_p)
 template <typename T, int K>
-IBEM_HD inline T phi_d(const EllPot<T, K>& P, int rho, const int* idx, int n) {
-  int c[3];
-  counts(idx, n, c);
-  return jder(rho < 0 ? P.f0 : P.f1[rho], c[0], c[1], c[2]);
-}
-
-// psi_rho,k idx = d^idx (x_k phi_rho - phi_{rho x'_k}) at the point
-template <typename T, int K>
-IBEM_HD inline T psi_d(const EllPot<T, K>& P, int rho, int k, const int* idx, int n) {
-  int c[3];
-  counts(idx, n, c);
-  const Jet<T, K>& f = rho < 0 ? P.f0 : P.f1[rho];
-  const Jet<T, K>& g = rho < 0 ? P.f1[k] : P.f2[sym_pair(rho, k)];
-  T v = P.d[k] * jder(f, c[0], c[1], c[2]) - jder(g, c[0], c[1], c[2]);
-  if (c[k] > 0) {   // d^idx of h_k phi: c_k d^(idx - e_k) phi
-    c[k] -= 1;
-    v += T(c[k] + 1) * jder(f, c[0], c[1], c[2]);
+IBEM_HD inline void ell_derivs(const EllPot<T, K>& P, EllDer<T, K>& D) {
+  D.inside = P.inside;
+#pragma unroll 1
+  for (int r = 0; r < 4; ++r) {
+    const Jet<T, K>& f = r == 0 ? P.f0 : P.f1[r - 1];
+#pragma unroll 1
+    for (int a1 = 0; a1 <= K; ++a1)
+#pragma unroll 1
+      for (int a2 = 0; a2 <= K - a1; ++a2)
+#pragma unroll 1
+        for (int a3 = 0; a3 <= K - a1 - a2; ++a3) {
+          const int id = midx(a1, a2, a3);
+          D.phi[r][id] = T(fact_small(a1) * fact_small(a2) * fact_small(a3)) * f.c[id];
+        }
+#pragma unroll 1
+    for (int b1 = 0; b1 <= K + 1; ++b1)
+#pragma unroll 1
+      for (int b2 = 0; b2 <= K + 1 - b1; ++b2)
+#pragma unroll 1
+        for (int b3 = 0; b3 <= K + 1 - b1 - b2; ++b3) {
+          const int deg = b1 + b2 + b3;
+          if (deg < 4) continue;
+          const int k = b1 > 0 ? 0 : (b2 > 0 ? 1 : 2);
+          const int a[3] = {b1 - (k == 0), b2 - (k == 1), b3 - (k == 2)};
+          const Jet<T, K>& g = r == 0 ? P.f1[k] : P.f2[sym_pair(r - 1, k)];
+          const int ia = midx(a[0], a[1], a[2]);
+          const T af = T(fact_small(a[0]) * fact_small(a[1]) * fact_small(a[2]));
+          T v = P.d[k] * f.c[ia] - g.c[ia];
+          if (a[k] > 0) v += f.c[midx(a[0] - (k == 0), a[1] - (k == 1), a[2] - (k == 2))];
+          D.psi[r][midx(b1, b2, b3)] = af * v;
+        }
   }
-  return v;
 }
 
-// D(i,j,k,l [,p]; R) of the reference (strain ij, eigenstrain kl of density rho), without
-// the factor 1 / (8 pi (1 - nu)): psi_,klijR - 2 nu d_kl phi_,ijR - (1 - nu)(...)
+// D(i,j,k,l [,p]; R) of the reference (strain ij, eigenstrain kl of density rho = -1
+// (uniform) or p), without the factor 1 / (8 pi (1 - nu)):
+//   psi_,klijR - 2 nu d_kl phi_,ijR - (1 - nu)(d_il phi_,kjR + d_jl phi_,kiR + d_ik phi_,ljR + d_jk phi_,liR)
 template <typename T, int K>
-IBEM_HD inline T Dsum(const EllPot<T, K>& P, T nu, int rho, int i, int j, int k, int l, const int* R, int nR) {
-  int idx[8];
-  int n = 0;
-  idx[n++] = l;
-  idx[n++] = i;
-  idx[n++] = j;
-  for (int s = 0; s < nR; ++s) idx[n++] = R[s];
-  T v = psi_d(P, rho, k, idx, n);
-  int id2[6];
+IBEM_HD inline T Dsum(const EllDer<T, K>& D, T nu, int rho, int i, int j, int k, int l, const int* R, int nR) {
+  const int r = rho + 1;
+  int c[3] = {0, 0, 0};
+  for (int s = 0; s < nR; ++s) ++c[R[s]];
+  int cp[3] = {c[0], c[1], c[2]};
+  ++cp[k];
+  ++cp[l];
+  ++cp[i];
+  ++cp[j];
+  T v = D.psi[r][midx(cp[0], cp[1], cp[2])];
   auto ph = [&](int x1, int x2) {
-    id2[0] = x1;
-    id2[1] = x2;
-    for (int s = 0; s < nR; ++s) id2[2 + s] = R[s];
-    return phi_d(P, rho, id2, 2 + nR);
+    int q[3] = {c[0], c[1], c[2]};
+    ++q[x1];
+    ++q[x2];
+    return D.phi[r][midx(q[0], q[1], q[2])];
   };
   if (k == l) v -= T(2) * nu * ph(i, j);
   T s4 = T(0);
@@ -612,29 +663,45 @@ IBEM_HD constexpr int pair_j(int t) { return t < 3 ? t : (t < 5 ? t - 2 : 2); }
 // d = centre of s - centre of h.  out[row * 24 + col].
 template <typename T>
 IBEM_HD inline void ell_block24(const T d[3], const T Q[9], const T a[3], const SphMat& mc, bool self, T* out) {
-  EllPot<T, 4> P;
-  ell_potentials<T, 4>(d, Q, a, P);
+  EllDer<T, 4> P;
+  {
+    EllPot<T, 4> pot;
+    ell_potentials<T, 4>(d, Q, a, pot);
+    ell_derivs(pot, P);
+  }
   const T nu = T(mc.tn2) / T(2);
   const T kd = T(mc.kd);
+  // Dt[r][rho][t][u] = D(pair t, pair u [, rho]; R) with r = 0: no collocation derivative,
+  // 1 + R: the derivative R; rho = 0 uniform, 1 + p linear.  576 values, one Dsum each.
+  T Dt[4][4][6][6];
+#pragma unroll 1
+  for (int r = 0; r < 4; ++r) {
+    const int R[1] = {r - 1};
+#pragma unroll 1
+    for (int rho = 0; rho < 4; ++rho)
+#pragma unroll 1
+      for (int t = 0; t < 6; ++t)
+#pragma unroll 1
+        for (int u = 0; u < 6; ++u)
+          Dt[r][rho][t][u] = Dsum(P, nu, rho - 1, pair_i(t), pair_j(t), pair_i(u), pair_j(u), R, r > 0 ? 1 : 0);
+  }
+#pragma unroll 1
   for (int rr = 0; rr < 24; ++rr) {
     const int ro = rr < 6 ? 0 : 1;
     const int rt = ro ? (rr - 6) / 3 : rr;
-    const int R[1] = {ro ? (rr - 6) % 3 : 0};
+    const int r = ro ? 1 + (rr - 6) % 3 : 0;
     const int i = pair_i(rt), j = pair_j(rt);
+#pragma unroll 1
     for (int cc = 0; cc < 24; ++cc) {
       const int co = cc < 6 ? 0 : 1;
       const int ct = co ? (cc - 6) / 3 : cc;
-      const int rho = co ? (cc - 6) % 3 : -1;
+      const int rho = co ? 1 + (cc - 6) % 3 : 0;
       const int m = pair_i(ct), n = pair_j(ct);
       // sum_kl (C0 - C1)_ijkl D_kl = dlam d_ij D_kk + 2 dmu D_ij
-      T acc = T(2) * T(mc.dmu) * Dsum(P, nu, rho, i, j, m, n, R, ro);
-      if (i == j) {
-        T tr = T(0);
-        for (int k = 0; k < 3; ++k) tr += Dsum(P, nu, rho, k, k, m, n, R, ro);
-        acc += T(mc.dlam) * tr;
-      }
+      T acc = T(2) * T(mc.dmu) * Dt[r][rho][rt][ct];
+      if (i == j) acc += T(mc.dlam) * (Dt[r][rho][0][ct] + Dt[r][rho][3][ct] + Dt[r][rho][5][ct]);
       T v = -kd * acc;
-      if (self && ro == co && (ro == 0 || R[0] == rho)) {
+      if (self && ro == co && (ro == 0 || r == rho)) {
         // C0_ijmn
         T c0 = T(mc.mu0) * (T((i == m) * (j == n)) + T((i == n) * (j == m)));
         if (i == j && m == n) c0 += T(mc.lam0);
@@ -650,8 +717,12 @@ IBEM_HD inline void ell_block24(const T d[3], const T Q[9], const T a[3], const 
 // accumulated into e.  Returns true if the point lies inside (or on) the ellipsoid.
 template <typename T>
 IBEM_HD inline bool ell_strain24(const T d[3], const T Q[9], const T a[3], const SphMat& mc, const T* E, T* e) {
-  EllPot<T, 3> P;
-  ell_potentials<T, 3>(d, Q, a, P);
+  EllDer<T, 3> P;
+  {
+    EllPot<T, 3> pot;
+    ell_potentials<T, 3>(d, Q, a, pot);
+    ell_derivs(pot, P);
+  }
   const T nu = T(mc.tn2) / T(2);
   const T kd = T(mc.kd);
   for (int rt = 0; rt < 6; ++rt) {

@@ -69,12 +69,13 @@ __global__ void k_split_a(int64_t m, int64_t k, const float* __restrict__ A, int
 __global__ void k_split_b(int64_t k, int64_t n, const float* __restrict__ B, int64_t ldb, int64_t kp,
                           __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
   const int64_t kk = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t j = blockIdx.y;
-  if (kk >= kp || j >= n) return;
-  const float v = kk < k ? B[j * ldb + kk] : 0.0f;
-  const __nv_bfloat16 h = __float2bfloat16_rn(v);
-  hi[j * kp + kk] = h;
-  lo[j * kp + kk] = __float2bfloat16_rn(v - __bfloat162float(h));
+  if (kk >= kp) return;
+  for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+    const float v = kk < k ? B[j * ldb + kk] : 0.0f;
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    hi[j * kp + kk] = h;
+    lo[j * kp + kk] = __float2bfloat16_rn(v - __bfloat162float(h));
+  }
 }
 
 // ---------------------------------------------------------------- PTX helpers
@@ -380,7 +381,7 @@ ibem_status gemm_sub_f32_tc(int64_t m, int64_t n, int64_t k, const float* A, int
       ProfScope psplit(PROF_GEMM_SPLIT, st);
     ::ibem::count_launch(), k_split_a<<<dim3((unsigned)((m + 31) / 32), (unsigned)(kp / 32)), dim3(32, 8), 0, st>>>(
         m, kc, A + k0 * lda, lda, kp, ahi, alo);
-    ::ibem::count_launch(), k_split_b<<<dim3((unsigned)((kp + 255) / 256), (unsigned)n), 256, 0, st>>>(
+    ::ibem::count_launch(), k_split_b<<<dim3((unsigned)((kp + 255) / 256), (unsigned)std::min<int64_t>(n, 65535)), 256, 0, st>>>(
         kc, n, B + k0, ldb, kp, bhi, blo);
       IBEM_LAUNCH_CHECK("gemm_tc split");
     }

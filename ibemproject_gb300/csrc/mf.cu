@@ -631,7 +631,10 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
   }
   b.ntiles = (int)tiles.size();
   // slices of the source range: about 4 CTAs per SM in total, at least 32 sources per slice
-  const int want = 152 * 4;
+  int dev = 0, nsm = 0;
+  IBEM_CUDA(cudaGetDevice(&dev));
+  IBEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int want = std::max(1, nsm) * 4;
   b.hsplit = std::max(1, std::min((want + b.ntiles - 1) / b.ntiles, (b.max_seg + 31) / 32));
   b.hsplit_wide = b.hsplit;
   std::vector<SphMat> md(in.nseg), ms(in.nseg);

@@ -104,9 +104,8 @@ template <typename T>
 __global__ void k_scale_copy(int64_t n, const double* __restrict__ A, int64_t lda, const double* __restrict__ r,
                              const double* __restrict__ c, T* __restrict__ W, int64_t ldw) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t j = blockIdx.y;
   if (i >= n) return;
-  W[j * ldw + i] = (T)(r[i] * A[j * lda + i] * c[j]);
+  for (int64_t j = blockIdx.y; j < n; j += gridDim.y) W[j * ldw + i] = (T)(r[i] * A[j * lda + i] * c[j]);
 }
 
 // ---------------------------------------------------------------- panel error flag
@@ -1594,7 +1593,7 @@ static ibem_status factor(SolveCtx& cx, const double* A, int64_t lda, T*& W, LuW
   {
     ProfScope ps(PROF_EQUIL, cx.st);
     if (ibem_status q = equilibrate(cx, A, lda)) return q;
-    dim3 g((unsigned)((N + 255) / 256), (unsigned)N);
+    dim3 g((unsigned)((N + 255) / 256), (unsigned)std::min<int64_t>(N, 65535));
     ::ibem::count_launch(), k_scale_copy<T><<<g, 256, 0, cx.st>>>(N, A, lda, cx.r, cx.c, W, N);
     IBEM_LAUNCH_CHECK("equilibrate");
   }
@@ -1789,7 +1788,7 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
       ProfScope ps(PROF_EQUIL, st);
       s = equilibrate(cx, A, lda);
       if (!s) {
-        dim3 g((unsigned)((N + 255) / 256), (unsigned)N);
+        dim3 g((unsigned)((N + 255) / 256), (unsigned)std::min<int64_t>(N, 65535));
         ::ibem::count_launch(), k_scale_copy<float><<<g, 256, 0, st>>>(N, A, lda, cx.r, cx.c, W, ldw);
         if (bj_smem(block) > 48 * 1024)
           cudaFuncSetAttribute(k_bj_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bj_smem(block));

@@ -61,8 +61,10 @@ extern "C" int he_D(int order, int nder, const double* d, const double* quat, co
                     double* out) {
   double Q[9];
   quat_to_rot(quat, Q);
-  EllPot<double, 4> P;
-  ell_potentials<double, 4>(d, Q, a, P);
+  EllPot<double, 4> pot;
+  ell_potentials<double, 4>(d, Q, a, pot);
+  EllDer<double, 4> P;
+  ell_derivs(pot, P);
   const int total = 4 + order + nder;
   int lim = 1;
   for (int t = 0; t < total; ++t) lim *= 3;

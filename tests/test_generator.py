@@ -95,3 +95,51 @@ def test_matrix_free_helpers_refuse_quadratic_batches():
                  lambda: B.training_pairs(bt, 1), lambda: B.training_pairs_mf(bt, 1), lambda: B.prepare(bt)):
         with pytest.raises(ValueError):
             call()
+
+
+def _pw_max(PA, PB, r):
+    """max over lam of the Perram-Wertheim contact function (numpy restatement, grid + refine)."""
+    lam = np.linspace(1e-4, 1 - 1e-4, 201)
+    best = 0.0
+    for _ in range(3):
+        vals = [l * (1 - l) * r @ np.linalg.solve((1 - l) * PA + l * PB, r) for l in lam]
+        k = int(np.argmax(vals))
+        best = max(best, vals[k])
+        lo, hi = lam[max(k - 1, 0)], lam[min(k + 1, len(lam) - 1)]
+        lam = np.linspace(lo, hi, 41)
+    return best
+
+
+def test_ellipsoid_generator_keeps_bodies_apart_and_is_seeded():
+    """ibem_e3d_generate_ellipsoids: semi-axes in range, unit quaternions, centres in the
+    cube, the same microstructure for the same seed, and no two ellipsoids overlapping
+    (Perram-Wertheim contact function > 1, checked here by a grid search in numpy)."""
+    from ibemproject_gb300 import cases
+    c = cases.ellipsoid_case(150, a1=0.008, vf=0.15, seed=2)
+    c2 = cases.ellipsoid_case(150, a1=0.008, vf=0.15, seed=2)
+    assert np.array_equal(c.centers, c2.centers) and np.array_equal(c.quats, c2.quats)
+    assert not np.array_equal(c.centers, cases.ellipsoid_case(150, a1=0.008, vf=0.15, seed=3).centers)
+    A = c.axes
+    assert np.all(A[:, 0] == 0.008)
+    assert np.all((A[:, 1] >= 0.004) & (A[:, 1] <= 0.008)) and np.all((A[:, 2] >= 0.002) & (A[:, 2] <= 0.008))
+    assert np.allclose(np.linalg.norm(c.quats, axis=1), 1.0)
+    L = float(c.title.split("=")[1])
+    assert np.all(c.centers >= 0.008) and np.all(c.centers <= L - 0.008)
+    vol = (4 / 3 * np.pi * A.prod(axis=1)).sum()
+    assert abs(vol / L ** 3 - 0.15) < 1e-9
+
+    def rot(q):
+        w, x, y, z = q / np.linalg.norm(q)
+        return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                         [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                         [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+    Ps = [rot(q) @ np.diag(a ** 2) @ rot(q).T for q, a in zip(c.quats, A)]
+    checked = 0
+    for i in range(c.num):
+        for j in range(i + 1, c.num):
+            r = c.centers[j] - c.centers[i]
+            if np.linalg.norm(r) >= A[i, 0] + A[j, 0]:
+                continue
+            checked += 1
+            assert _pw_max(Ps[i], Ps[j], r) > 1.0, (i, j)
+    assert checked > 0

@@ -68,7 +68,7 @@ def host_block(he, c, s, h):
 
 def test_pair_blocks_match_host_evaluator(g, he):
     from ibemproject_gb300 import cases
-    c = cases.ellipsoid_case(37, vf=0.2, seed=3)   # 37: a ragged last warp of targets
+    c = cases.ellipsoid_case(37, vf=0.1, seed=3)   # 37: a ragged last warp of targets
     A = ell_matrix(g, c)
     rng = np.random.default_rng(0)
     pairs = [(s, s) for s in range(3)] + [tuple(rng.integers(0, c.num, 2)) for _ in range(40)] + [(36, 0), (0, 36)]
@@ -103,7 +103,7 @@ def test_pipeline_against_host_assembled_solve(g, he, form, tol):
     """run_host_ell (assembly, right-hand side, dense solve, stresses) against a numpy solve
     of the system assembled by the host evaluator, and stresses summed by it."""
     from ibemproject_gb300 import cases
-    c = cases.ellipsoid_case(24, vf=0.18, seed=7, grid=3)
+    c = cases.ellipsoid_case(24, vf=0.1, seed=7, grid=3)
     X, S, rep = g.run_host_ell(c, form=form, tol=1e-14)
     N = 24 * c.num
     A = np.zeros((N, N))
@@ -142,7 +142,7 @@ def test_mixed_field_matches_fp64_field_far_and_near(g):
     """The mixed form's FP32 far path: a grid over a cube much wider than the
     microstructure, so that both paths run, against the FP64 sums."""
     from ibemproject_gb300 import cases
-    c = cases.ellipsoid_case(60, vf=0.15, seed=11)
+    c = cases.ellipsoid_case(60, vf=0.1, seed=11)
     L = float(c.title.split("=")[1])
     pts = cases.cell_grid(12, -2.0 * L, 3.0 * L)
     rng = np.random.default_rng(2)
