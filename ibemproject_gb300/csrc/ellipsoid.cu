@@ -12,10 +12,12 @@
 //   block in FP64 (the FP64 pipe bounds the kernel); the warp then writes the blocks one
 //   column at a time through shared memory, so that every store instruction covers
 //   consecutive rows (the 32 blocks of a warp are 768 consecutive rows of each column).
-// stress sums: one thread per sample point, sources staged through shared memory in
+// stress sums: one thread per sample point and source slice (blockIdx.y; enough slices
+//   to fill the GPU when there are few points), sources staged through shared memory in
 //   chunks; the mixed form evaluates a source in FP32 (coordinates scaled by its longest
 //   semi-axis) when it lies beyond kEllFarAxes of those axes from all 32 points of the
-//   warp, in FP64 otherwise.
+//   warp, in FP64 otherwise.  The slices' partial sums are added in slice order by a
+//   second kernel (no atomics: the same stresses on every run).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -78,23 +80,29 @@ struct EllRec {
   double c[3], a[3], Q[9], E[24];
 };
 
+// Partial strain sums of the ellipsoids of one source slice (blockIdx.y) at every point:
+// part[(slice * nump + t) * 6 + k], and the last ellipsoid of the slice that holds the point
+// (or -1) in inside_part[slice * nump + t].
 __global__ void __launch_bounds__(kEllFieldThreads) k_ell_field24(const double* __restrict__ pts, int nump,
                                                                   const double* __restrict__ cen,
                                                                   const double* __restrict__ axes,
                                                                   const double* __restrict__ Qall, int num, SphMat mc,
                                                                   const double* __restrict__ E, int mixed,
-                                                                  double* __restrict__ stress) {
+                                                                  double* __restrict__ part,
+                                                                  int* __restrict__ inside_part) {
   __shared__ EllRec sr[kEllChunk];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const bool act = t < nump;
+  const int per = (num + gridDim.y - 1) / gridDim.y;
+  const int hb = blockIdx.y * per, he = min(num, hb + per);
   double p[3] = {0, 0, 0};
   if (act)
 #pragma unroll
     for (int i = 0; i < 3; ++i) p[i] = pts[3 * (int64_t)t + i];
   double e[6] = {0, 0, 0, 0, 0, 0};
   int inside = -1;
-  for (int h0 = 0; h0 < num; h0 += kEllChunk) {
-    const int nh = min(kEllChunk, num - h0);
+  for (int h0 = hb; h0 < he; h0 += kEllChunk) {
+    const int nh = min(kEllChunk, he - h0);
     __syncthreads();
     for (int i = threadIdx.x; i < nh * 39; i += blockDim.x) {
       const int hh = i / 39, f = i % 39;
@@ -137,11 +145,33 @@ __global__ void __launch_bounds__(kEllFieldThreads) k_ell_field24(const double* 
     }
   }
   if (!act) return;
+  const int64_t o = (int64_t)blockIdx.y * nump + t;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) part[6 * o + k] = e[k];
+  inside_part[o] = inside;
+}
+
+// Sum of the slices in slice order (the same on every run), the local eigenstrain of the
+// last ellipsoid holding the point (postProcessorElastic3D.cpp:383-433), stress += C0 : e.
+__global__ void k_ell_field_reduce(int nump, int nsl, const double* __restrict__ part,
+                                   const int* __restrict__ inside_part, const double* __restrict__ pts,
+                                   const double* __restrict__ cen, const double* __restrict__ E, SphMat mc,
+                                   double* __restrict__ stress) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nump) return;
+  double e[6] = {0, 0, 0, 0, 0, 0};
+  int inside = -1;
+  for (int sl = 0; sl < nsl; ++sl) {
+    const int64_t o = (int64_t)sl * nump + t;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) e[k] += part[6 * o + k];
+    inside = max(inside, inside_part[o]);
+  }
   if (inside >= 0) {
-    // local eigenstrain polynomial of the inclusion that holds the point (postProcessorElastic3D.cpp:409-433)
     const double* Ei = E + 24 * (int64_t)inside;
-    const double d[3] = {p[0] - cen[3 * (int64_t)inside], p[1] - cen[3 * (int64_t)inside + 1],
-                         p[2] - cen[3 * (int64_t)inside + 2]};
+    const double d[3] = {pts[3 * (int64_t)t] - cen[3 * (int64_t)inside],
+                         pts[3 * (int64_t)t + 1] - cen[3 * (int64_t)inside + 1],
+                         pts[3 * (int64_t)t + 2] - cen[3 * (int64_t)inside + 2]};
     for (int r = 0; r < 6; ++r) e[r] -= Ei[r] + Ei[6 + 3 * r] * d[0] + Ei[7 + 3 * r] * d[1] + Ei[8 + 3 * r] * d[2];
   }
   const double tr = e[0] + e[3] + e[5];
@@ -231,11 +261,24 @@ ibem_status ibem_e3d_ell_field(ibem_solver_form form, const double* points_dev, 
   if (!s) {
     const SphMat mc = sph_mat_init(mat->E0, mat->nu0, mat->E1, mat->nu1);
     ProfScope ps(PROF_FIELD, st);
-    ::ibem::count_launch(), k_ell_field24<<<(unsigned)((nump + kEllFieldThreads - 1) / kEllFieldThreads),
-                                            kEllFieldThreads, 0, st>>>(points_dev, nump, centers_dev, axes_dev, Q,
-                                                                       num, mc, E_dev,
-                                                                       form == IBEM_SOLVE_MIXED_IR ? 1 : 0, stress_dev);
-    cudaError_t e = cudaGetLastError();
+    // source slices: about 8 CTAs per SM in total, at least one chunk of sources per slice
+    int dev = 0, nsm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int gx = (nump + kEllFieldThreads - 1) / kEllFieldThreads;
+    const int nsl = std::max(1, std::min((8 * nsm + gx - 1) / gx, (num + kEllChunk - 1) / kEllChunk));
+    double* part = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&part, (sizeof(double) * 6 + sizeof(int)) * (size_t)nsl * nump, st);
+    if (e == cudaSuccess) {
+      int* inside = reinterpret_cast<int*>(part + 6 * (size_t)nsl * nump);
+      ::ibem::count_launch(), k_ell_field24<<<dim3((unsigned)gx, (unsigned)nsl), kEllFieldThreads, 0, st>>>(
+          points_dev, nump, centers_dev, axes_dev, Q, num, mc, E_dev, form == IBEM_SOLVE_MIXED_IR ? 1 : 0, part,
+          inside);
+      ::ibem::count_launch(), k_ell_field_reduce<<<(unsigned)((nump + 255) / 256), 256, 0, st>>>(
+          nump, nsl, part, inside, points_dev, centers_dev, E_dev, mc, stress_dev);
+      e = cudaGetLastError();
+      cudaFreeAsync(part, st);
+    }
     if (e != cudaSuccess) s = cuda_fail(e, "ell_field");
   }
   cudaFreeAsync(Q, st);

@@ -27,6 +27,9 @@
                boundary elements) at G^3 points: sphere sums and boundary part.
 --assemble NUM,LAYOUT  the pair blocks (ibem_e3d_pair_blocks, FP64) of NUM spheres in
                layout 24, 60 or 78: achieved write bandwidth of the N^2 matrix.
+--field-far NUM,G  the same with the grid moved far from every sphere (FP32 path only).
+--ell NUM,G    ellipsoid pair blocks (FP64) and stress sums (FP64 and mixed) of NUM
+               ellipsoids (a1 0.008, a2 a1 U[0.5,1], a3 a1 U[0.25,1], vf 15%) at G^3 points.
 --mf NUM       the matrix-free products (ibem_e3d_mf_matvec: FP32, double-float, FP64) on a
                far-field microstructure of NUM spheres (bench distribution): NUM^2 pair
                products per launch, timed by the library's phase events.
@@ -198,10 +201,14 @@ def bench_mf(num, reps, dev):
     return out
 
 
-def bench_field(num, grid, reps, dev):
+def bench_field(num, grid, reps, dev, far=False):
+    """far: the grid is moved 20 cube sides away, so that every sphere is far from every
+    warp's points and only the FP32 path runs (its flop count per pair)."""
     import numpy as np
     from . import Material, batch as B, cases
     c = cases.farfield_case(num=num, r0=0.012, vf=0.15, grid=grid, seed=2024)
+    if far:
+        c.points = c.points + np.array([20.0 * c.points.max(), 0.0, 0.0])
     L = lib()
     m = Material(c.E0, c.nu0, c.E1, c.nu1)
     g = torch.Generator(device="cpu").manual_seed(5)
@@ -224,8 +231,51 @@ def bench_field(num, grid, reps, dev):
     L.ibem_prof_enable(0)
     ms = prof.get("field", {}).get("ms", 0.0) / reps
     pairs = num * c.nump
-    return {"kernel": "field24_df", "spheres": num, "points": c.nump, "pairs": pairs, "reps": reps, "ms": ms,
+    return {"kernel": "field24_df" + (" (all far: FP32 path)" if far else ""), "spheres": num, "points": c.nump,
+            "pairs": pairs, "reps": reps, "ms": ms,
             "ns_per_pair": ms * 1e6 / pairs if ms > 0 else None}
+
+
+def bench_ell(num, grid, reps, dev):
+    """Ellipsoid pair blocks (ibem_e3d_ell_pair_blocks, FP64) and stress sums
+    (ibem_e3d_ell_field, FP64 and mixed) of `num` ellipsoids of the config-3 distribution
+    (vf 15%) on a grid^3 of points; event-timed per call."""
+    import numpy as np
+    from . import Material, SOLVE_FP64, SOLVE_MIXED_IR, cases
+    c = cases.ellipsoid_case(num, vf=0.15, seed=3, grid=grid)
+    L = lib()
+    m = Material(c.E0, c.nu0, c.E1, c.nu1)
+    N = 24 * num
+    dv = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(dev)
+    cen, ax, qt, pts = dv(c.centers), dv(c.axes), dv(c.quats), dv(c.points)
+    A = torch.empty((N, N), dtype=torch.float64, device=dev)
+    E = (torch.randn(N, dtype=torch.float64, generator=torch.Generator().manual_seed(3)) * 1e-9).to(dev)
+    S = torch.empty((max(1, c.nump), 6), dtype=torch.float64, device=dev)
+    sig = np.ascontiguousarray(c.sig_inf)
+    sigp = sig.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    out = {"kernel": "ellipsoids", "num": num, "points": c.nump, "pairs": num * num}
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    out["pair_blocks_ms"] = timed(lambda: check(L.ibem_e3d_ell_pair_blocks(_p(cen), _p(ax), _p(qt), num,
+                                                                            ctypes.byref(m), _p(A), N, 0, 0, None)))
+    for name, form in (("field_fp64_ms", SOLVE_FP64), ("field_mixed_ms", SOLVE_MIXED_IR)):
+        if c.nump:
+            out[name] = timed(lambda: check(L.ibem_e3d_ell_field(form, _p(pts), c.nump, _p(cen), _p(ax), _p(qt), num,
+                                                                 ctypes.byref(m), _p(E), sigp, _p(S), None)))
+    out["ns_per_block"] = out["pair_blocks_ms"] * 1e6 / (num * num)
+    if c.nump:
+        out["ns_per_field_pair_fp64"] = out["field_fp64_ms"] * 1e6 / (num * c.nump)
+    return out
 
 
 def bench_solve(num, reps, dev, vf=0.15):
@@ -428,6 +478,8 @@ def main(argv=None):
     ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--mf", type=int, action="append", default=[])
     ap.add_argument("--field", action="append", default=[], help="NUM,GRID")
+    ap.add_argument("--field-far", action="append", default=[], help="NUM,GRID with every sphere far from the points")
+    ap.add_argument("--ell", action="append", default=[], help="NUM,GRID: ellipsoid pair blocks and stress sums")
     ap.add_argument("--solve", type=int, action="append", default=[])
     ap.add_argument("--batch", type=int, action="append", default=[])
     ap.add_argument("--assemble", action="append", default=[], help="NUM,LAYOUT")
@@ -464,6 +516,12 @@ def main(argv=None):
     for f in a.field:
         num, grid = (int(v) for v in f.split(","))
         print(json.dumps(bench_field(num, grid, a.reps, dev)), flush=True)
+    for f in a.ell:
+        num, grid = (int(v) for v in f.split(","))
+        print(json.dumps(bench_ell(num, grid, a.reps, dev)), flush=True)
+    for f in a.field_far:
+        num, grid = (int(v) for v in f.split(","))
+        print(json.dumps(bench_field(num, grid, a.reps, dev, far=True)), flush=True)
     return 0
 
 
