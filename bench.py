@@ -241,14 +241,15 @@ def roofline_chosen(prof, case):
             "traffic_source": FIELD_DF_SOURCE, "flops_source": FIELD_DF_SOURCE}
 
 
-# Algorithmic FP32 flops of one (point, sphere) pair of the contracted stress sum (the FP32
-# path of field24_df, counted by ncu on an all-far launch).
-FIELD_ALG_FLOPS_PER_PAIR = 420.0
-# Executed FP32 flops per pair on this workload (FADD + FMUL + 2 FFMA thread instructions of
-# one full-size launch counted by ncu: double-float within 14 radii of a warp's points, FP32
-# beyond) and the launch's DRAM bytes (read + write), from the same capture.
-FIELD_DF_FLOPS_PER_PAIR = 888.8
-FIELD_DF_TRAFFIC_PER_LAUNCH = 21.10e6
+# Algorithmic FP32 flops of one (point, sphere) pair of the contracted stress sum: the FP32
+# path of field24_df alone (FADD + FMUL + 2 FFMA thread instructions counted by ncu on a launch
+# whose points are far from every sphere, 2.641e10 flops / 6.554e7 pairs).
+FIELD_ALG_FLOPS_PER_PAIR = 403.0
+# Executed FP32 flops per pair on this workload (the same count over one full-size launch:
+# double-float within 14 radii of a warp's points, FP32 beyond; 4.663e11 / 5.243e8) and the
+# launch's DRAM bytes (read + write) from the same capture.
+FIELD_DF_FLOPS_PER_PAIR = 889.4
+FIELD_DF_TRAFFIC_PER_LAUNCH = 21.00e6
 FIELD_DF_SOURCE = "profiles/field24_df_bench2000.md"
 
 

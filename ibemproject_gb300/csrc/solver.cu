@@ -1913,7 +1913,8 @@ ibem_status solve_dense(ibem_solver_form form, int64_t N, double* A, int64_t lda
     lu_free(w);
     cudaFree(W);
   }
-  if (!s) ::ibem::count_launch(), k_vmul<<<nb, 256, 0, st>>>(N, cx.c, ys, x);  // x = C ys
+  // x = C ys; also when the tolerance was missed, so that the caller gets the iterate reached
+  if (!s || s == IBEM_ERR_NOCONV) ::ibem::count_launch(), k_vmul<<<nb, 256, 0, st>>>(N, cx.c, ys, x);
   cudaStreamSynchronize(st);
   float t1 = 0, t2 = 0;
   cudaEventElapsedTime(&t1, e0, e1);

@@ -32,7 +32,7 @@ typedef enum {
   IBEM_OK = 0,
   IBEM_ERR_ARG = 1,      /* invalid argument (sizes, layout, null pointer) */
   IBEM_ERR_CUDA = 2,     /* a CUDA runtime call or kernel launch failed */
-  IBEM_ERR_NOCONV = 3,   /* iterative refinement did not reach the tolerance */
+  IBEM_ERR_NOCONV = 3,   /* iterative refinement did not reach the tolerance (x holds the iterate reached) */
   IBEM_ERR_TIMEOUT = 4,  /* a device-side wait gave up (kernel returned early) */
   IBEM_ERR_SINGULAR = 5, /* a zero pivot was met */
   IBEM_ERR_IO = 6        /* an input file could not be read or parsed */

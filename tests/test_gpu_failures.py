@@ -6,7 +6,8 @@
   returns IBEM_ERR_TIMEOUT and a normal solve right after it still works.
 * Non-convergence: the iterative forms (mixed FP32 LU + GMRES-IR, block-Jacobi GMRES, the
   matrix-free solve) asked for a tolerance below rounding, with their iteration limits,
-  return IBEM_ERR_NOCONV and still report the backward error / residual they reached.
+  return IBEM_ERR_NOCONV, still report the backward error / residual they reached and
+  leave the iterate reached in x.
 """
 import ctypes
 
@@ -76,6 +77,7 @@ def test_block_jacobi_form_reports_noconv(g, oracle_mod):
     st, x, rep = _dense(g, g.SOLVE_GMRES_BJ, A, b, 1e-30, bj_block=24)
     assert st == g.IBEM_ERR_NOCONV
     assert 0 < rep.backward_error < 1e-12
+    assert scaled_err(x, np.linalg.solve(A, b)) < 1e-9   # the iterate reached is returned
 
 
 def test_matrix_free_solve_reports_noconv(g):
