@@ -4,7 +4,10 @@
 // orders 0 and 1) are never formed: their products with the coefficients are evaluated
 // as the contracted strain and its gradient (mf_contract.cuh):
 //   k_mf_apply_f32  As x in FP32 on the scaled system (mf.h), the GMRES operator;
-//   k_mf_apply_f64  As x in FP64, the refinement residual Dr b - As xs.
+//   k_mf_apply_f64  As x in FP64, the refinement residual Dr b - As xs; for the residual
+//                   that decides convergence it takes only the source chunks near each
+//                   warp's targets and k_mf_apply_df the far ones (both visit particles in
+//                   the Morton order of their centres, so warps and chunks are compact).
 // One thread per target particle s, 128 consecutive targets of one realisation per CTA;
 // the CTA's source particles h (a slice of the realisation, gridDim.y slices) are staged
 // through shared memory in chunks with their coefficients, and every thread sums the
@@ -13,7 +16,7 @@
 // Solver: iterative refinement x += Dc d; each correction d solves As d = Dr r with a
 // restarted FP32 GMRES right-preconditioned by a block-sparse P (block-Jacobi, Neumann or
 // learned); the residual that drives the next correction is a double-float product
-// (k_mf_apply_df, ~48 bits) and the one that decides convergence the FP64 product.  All
+// (k_mf_apply_df, ~48 bits) and the one that decides convergence the split product.  All
 // realisations of a batch run in lock step (per-realisation Arnoldi: segmented dot
 // products, Hessenberg updates and Givens rotations on the device, one thread per
 // realisation), stopping each realisation on its own residual estimate.
@@ -42,6 +45,7 @@ namespace {
 
 constexpr int kMfThreads = 128;
 constexpr int kMfChunk = 32;
+constexpr double kMfFarRadii = 8.0;   // near / far split of the deciding residual
 
 // sink of a generated block: acc[r] += v * x[c] (r, c compile-time constants after inlining)
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
@@ -109,11 +113,51 @@ __global__ void __launch_bounds__(kMfThreads)
 
 // FP64 product of the scaled system (the refinement residual): the same evaluation as the
 // FP32 kernel in double precision, offsets from FP64 centres.
+// Split products (the deciding residual): particles are visited in the Morton order of
+// their centres within each realisation (perm: position -> particle), so the 32 targets of a
+// warp and the 32 sources of a chunk are compact clusters.  mode 0: every pair; 1: only the
+// chunks near the warp's targets (box distance <= kMfFarRadii radii of the chunk's largest
+// sphere), and the self term; 2: only the far chunks, no self term.
+__device__ __forceinline__ void warp_box(bool act, double x, double y, double z, double* lo, double* hi) {
+  double v[3] = {x, y, z};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    double a = act ? v[d] : 1e300, b = act ? v[d] : -1e300;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a = fmin(a, __shfl_xor_sync(0xffffffffu, a, o));
+      b = fmax(b, __shfl_xor_sync(0xffffffffu, b, o));
+    }
+    lo[d] = a;
+    hi[d] = b;
+  }
+}
+
+// chunk box of the staged sources (lane i reads source i) and the largest radius
+__device__ __forceinline__ bool chunk_is_far(const double* wlo, const double* whi, int nh, double cx, double cy,
+                                             double cz, double r) {
+  const int lane = threadIdx.x & 31;
+  const bool a = lane < nh;
+  double lo[3], hi[3];
+  warp_box(a, cx, cy, cz, lo, hi);
+  double rm = a ? r : 0.0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) rm = fmax(rm, __shfl_xor_sync(0xffffffffu, rm, o));
+  double d2 = 0.0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double g = fmax(0.0, fmax(lo[d] - whi[d], wlo[d] - hi[d]));
+    d2 += g * g;
+  }
+  return d2 > kMfFarRadii * kMfFarRadii * rm * rm;
+}
+
 __global__ void __launch_bounds__(kMfThreads)
     k_mf_apply_f64(const MfTile* __restrict__ tiles, const int* __restrict__ seg_begin,
                    const int* __restrict__ mask, int mask_on,
                    const double* __restrict__ cen, const double* __restrict__ rad,
-                   const SphMat* __restrict__ mats, const double* __restrict__ x, double* __restrict__ y) {
+                   const SphMat* __restrict__ mats, const double* __restrict__ x, double* __restrict__ y,
+                   const int* __restrict__ perm, int mode) {
   __shared__ double sc[kMfChunk * 4];
   __shared__ double sx[kMfChunk * kMfNu];
   const MfTile t = tiles[blockIdx.x];
@@ -122,8 +166,9 @@ __global__ void __launch_bounds__(kMfThreads)
   const int per = (he0 - hb0 + gridDim.y - 1) / gridDim.y;
   const int hb = hb0 + blockIdx.y * per, he = min(he0, hb + per);
   if (hb >= he) return;
-  const int s = t.s0 + threadIdx.x;
+  const int pos = t.s0 + threadIdx.x;
   const bool act = threadIdx.x < t.ns;
+  const int s = act ? perm[pos] : 0;
   const SphMat mc = mats[t.seg];   // moduli divided by mu0 (scaled system)
   double p0 = 0, p1 = 0, p2 = 0, as = 1;
   if (act) {
@@ -132,6 +177,8 @@ __global__ void __launch_bounds__(kMfThreads)
     p2 = cen[3 * (int64_t)s + 2];
     as = rad[s];
   }
+  double wlo[3], whi[3];
+  warp_box(act, p0, p1, p2, wlo, whi);
   double acc[kMfNu];
 #pragma unroll
   for (int r = 0; r < kMfNu; ++r) acc[r] = 0.0;
@@ -139,13 +186,21 @@ __global__ void __launch_bounds__(kMfThreads)
     const int nh = min(kMfChunk, he - h0);
     __syncthreads();
     for (int i = threadIdx.x; i < nh; i += blockDim.x) {
-      sc[4 * i] = cen[3 * (int64_t)(h0 + i)];
-      sc[4 * i + 1] = cen[3 * (int64_t)(h0 + i) + 1];
-      sc[4 * i + 2] = cen[3 * (int64_t)(h0 + i) + 2];
-      sc[4 * i + 3] = 1.0 / rad[h0 + i];
+      const int h = perm[h0 + i];
+      sc[4 * i] = cen[3 * (int64_t)h];
+      sc[4 * i + 1] = cen[3 * (int64_t)h + 1];
+      sc[4 * i + 2] = cen[3 * (int64_t)h + 2];
+      sc[4 * i + 3] = 1.0 / rad[h];
     }
-    for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x) sx[i] = x[(int64_t)kMfNu * h0 + i];
+    for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x)
+      sx[i] = x[(int64_t)kMfNu * perm[h0 + i / kMfNu] + i % kMfNu];
     __syncthreads();
+    if (mode) {
+      const int l = threadIdx.x & 31;
+      const bool far = chunk_is_far(wlo, whi, nh, l < nh ? sc[4 * l] : 0.0, l < nh ? sc[4 * l + 1] : 0.0,
+                                    l < nh ? sc[4 * l + 2] : 0.0, l < nh ? 1.0 / sc[4 * l + 3] : 0.0);
+      if (far != (mode == 2)) continue;
+    }
     if (!act) continue;
 #pragma unroll 1
     for (int hh = 0; hh < nh; ++hh) {
@@ -157,7 +212,7 @@ __global__ void __launch_bounds__(kMfThreads)
   if (!act) return;
   double yv[kMfNu];
   sph_pair_map24<double>(acc, mc.kmu, mc.klam, yv);
-  if (s >= hb && s < he) {
+  if (pos >= hb && pos < he && mode != 2) {
     MvSink<double> sk{yv, x + (int64_t)kMfNu * s};
     sph_self24(mc, sk);
   }
@@ -179,38 +234,59 @@ __global__ void __launch_bounds__(kMfThreads)
     k_mf_apply_df(const MfTile* __restrict__ tiles, const int* __restrict__ seg_begin,
                    const int* __restrict__ mask, int mask_on,
                   const double* __restrict__ cen, const double* __restrict__ rad,
-                  const SphMat* __restrict__ mats, const double* __restrict__ x, double* __restrict__ y) {
+                  const SphMat* __restrict__ mats, const double* __restrict__ x, double* __restrict__ y,
+                  const int* __restrict__ perm, int mode) {
   __shared__ DF sc[kMfChunk * 4];
   __shared__ DF sx[kMfChunk * kMfNu];
+  __shared__ double sr[kMfChunk * 4];   // FP64 centres and radii of the chunk (near / far test)
   const MfTile t = tiles[blockIdx.x];
   if (mask && mask[t.seg] != mask_on) return;  // realisation left out of this product
   const int hb0 = seg_begin[t.seg], he0 = seg_begin[t.seg + 1];
   const int per = (he0 - hb0 + gridDim.y - 1) / gridDim.y;
   const int hb = hb0 + blockIdx.y * per, he = min(he0, hb + per);
   if (hb >= he) return;
-  const int s = t.s0 + threadIdx.x;
+  const int pos = t.s0 + threadIdx.x;
   const bool act = threadIdx.x < t.ns;
+  const int s = act ? perm[pos] : 0;
   const SphMat mc = mats[t.seg];   // moduli divided by mu0 (scaled system)
   DF p0, p1, p2, as(1.0);
+  double q0 = 0, q1 = 0, q2 = 0;
   if (act) {
-    p0 = DF(cen[3 * (int64_t)s]);
-    p1 = DF(cen[3 * (int64_t)s + 1]);
-    p2 = DF(cen[3 * (int64_t)s + 2]);
+    q0 = cen[3 * (int64_t)s];
+    q1 = cen[3 * (int64_t)s + 1];
+    q2 = cen[3 * (int64_t)s + 2];
+    p0 = DF(q0);
+    p1 = DF(q1);
+    p2 = DF(q2);
     as = DF(rad[s]);
   }
+  double wlo[3], whi[3];
+  warp_box(act, q0, q1, q2, wlo, whi);
   const DF tn1(mc.tn1), tn2(mc.tn2);
   DF acc[kMfNu];
   for (int h0 = hb; h0 < he; h0 += kMfChunk) {
     const int nh = min(kMfChunk, he - h0);
     __syncthreads();
     for (int i = threadIdx.x; i < nh; i += blockDim.x) {
-      sc[4 * i] = DF(cen[3 * (int64_t)(h0 + i)]);
-      sc[4 * i + 1] = DF(cen[3 * (int64_t)(h0 + i) + 1]);
-      sc[4 * i + 2] = DF(cen[3 * (int64_t)(h0 + i) + 2]);
-      sc[4 * i + 3] = DF(1.0 / rad[h0 + i]);
+      const int h = perm[h0 + i];
+      sr[4 * i] = cen[3 * (int64_t)h];
+      sr[4 * i + 1] = cen[3 * (int64_t)h + 1];
+      sr[4 * i + 2] = cen[3 * (int64_t)h + 2];
+      sr[4 * i + 3] = rad[h];
+      sc[4 * i] = DF(sr[4 * i]);
+      sc[4 * i + 1] = DF(sr[4 * i + 1]);
+      sc[4 * i + 2] = DF(sr[4 * i + 2]);
+      sc[4 * i + 3] = DF(1.0 / sr[4 * i + 3]);
     }
-    for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x) sx[i] = DF(x[(int64_t)kMfNu * h0 + i]);
+    for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x)
+      sx[i] = DF(x[(int64_t)kMfNu * perm[h0 + i / kMfNu] + i % kMfNu]);
     __syncthreads();
+    if (mode) {
+      const int l = threadIdx.x & 31;
+      const bool far = chunk_is_far(wlo, whi, nh, l < nh ? sr[4 * l] : 0.0, l < nh ? sr[4 * l + 1] : 0.0,
+                                    l < nh ? sr[4 * l + 2] : 0.0, l < nh ? sr[4 * l + 3] : 0.0);
+      if (far != (mode == 2)) continue;
+    }
     if (!act) continue;
 #pragma unroll 1
     for (int hh = 0; hh < nh; ++hh) {
@@ -222,7 +298,7 @@ __global__ void __launch_bounds__(kMfThreads)
   if (!act) return;
   DF yv[kMfNu];
   sph_pair_map24<DF>(acc, DF(mc.kmu), DF(mc.klam), yv);
-  if (s >= hb && s < he) {
+  if (pos >= hb && pos < he && mode != 2) {
     DfSink sk{yv, x + (int64_t)kMfNu * s};
     sph_self24(mc, sk);
   }
@@ -661,6 +737,44 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
   IBEM_CUDA(alloc_async((void**)&b.dr, sizeof(double) * b.N, st));
   IBEM_CUDA(alloc_async((void**)&b.dc, sizeof(double) * b.N, st));
   IBEM_CUDA(alloc_async((void**)&b.tiles, sizeof(MfTile) * b.ntiles, st));
+  // Morton order of the centres within each realisation (10 bits per axis of its bounding box)
+  std::vector<int> perm(b.num);
+  {
+    std::vector<double> ch(3 * (size_t)b.num);
+    IBEM_CUDA(cudaMemcpyAsync(ch.data(), in.centers_dev, sizeof(double) * ch.size(), cudaMemcpyDeviceToHost, st));
+    IBEM_CUDA(cudaStreamSynchronize(st));
+    auto spread = [](uint32_t v) {
+      v &= 0x3ffu;
+      v = (v | (v << 16)) & 0x030000ffu;
+      v = (v | (v << 8)) & 0x0300f00fu;
+      v = (v | (v << 4)) & 0x030c30c3u;
+      v = (v | (v << 2)) & 0x09249249u;
+      return v;
+    };
+    std::vector<std::pair<uint32_t, int>> key;
+    for (int s = 0; s < in.nseg; ++s) {
+      const int p0 = b.seg_begin_h[s], p1 = b.seg_begin_h[s + 1];
+      double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+      for (int p = p0; p < p1; ++p)
+        for (int d = 0; d < 3; ++d) {
+          lo[d] = std::min(lo[d], ch[3 * (size_t)p + d]);
+          hi[d] = std::max(hi[d], ch[3 * (size_t)p + d]);
+        }
+      key.clear();
+      for (int p = p0; p < p1; ++p) {
+        uint32_t q[3];
+        for (int d = 0; d < 3; ++d) {
+          const double w = hi[d] > lo[d] ? (ch[3 * (size_t)p + d] - lo[d]) / (hi[d] - lo[d]) : 0.0;
+          q[d] = (uint32_t)std::min(1023.0, std::max(0.0, std::floor(w * 1024.0)));
+        }
+        key.push_back({spread(q[0]) | (spread(q[1]) << 1) | (spread(q[2]) << 2), p});
+      }
+      std::sort(key.begin(), key.end());
+      for (int i = 0; i < p1 - p0; ++i) perm[p0 + i] = key[i].second;
+    }
+  }
+  IBEM_CUDA(alloc_async((void**)&b.perm, sizeof(int) * b.num, st));
+  IBEM_CUDA(cudaMemcpyAsync(b.perm, perm.data(), sizeof(int) * b.num, cudaMemcpyHostToDevice, st));
   IBEM_CUDA(cudaMemcpyAsync(b.seg_begin, b.seg_begin_h.data(), sizeof(int) * (in.nseg + 1), cudaMemcpyHostToDevice, st));
   IBEM_CUDA(cudaMemcpyAsync(b.seg_of, seg_of.data(), sizeof(int) * b.num, cudaMemcpyHostToDevice, st));
   IBEM_CUDA(cudaMemcpyAsync(b.matd, md.data(), sizeof(SphMat) * in.nseg, cudaMemcpyHostToDevice, st));
@@ -687,6 +801,7 @@ void mf_batch_free(MfBatch& b) {
   free_async(b.dr, st);
   free_async(b.dc, st);
   free_async(b.tiles, st);
+  free_async(b.perm, st);
   b = MfBatch();
 }
 
@@ -802,17 +917,31 @@ ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_
 ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st, const int* mask, int mask_on) {
   ProfScope ps(PROF_MF_F64, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
-  ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, mask, mask_on,
-                                                                                              b.cen, b.rad, b.mats, x, y);
+  // near chunks in FP64, far chunks (beyond kMfFarRadii radii of the warp's targets) in
+  // double-float: their contributions are at most kMfFarRadii^-3 of a near one, so the
+  // double-float rounding (~2^-44 per operation) stays far below FP64 level in the sum
+  ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
+      b.tiles, b.seg_begin, mask, mask_on, b.cen, b.rad, b.mats, x, y, b.perm, 1);
+  ::ibem::count_launch(), k_mf_apply_df<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
+      b.tiles, b.seg_begin, mask, mask_on, b.cen, b.rad, b.mats, x, y, b.perm, 2);
   IBEM_LAUNCH_CHECK("mf apply f64");
+  return IBEM_OK;
+}
+
+ibem_status mf_apply_f64_all(const MfBatch& b, const double* x, double* y, cudaStream_t st) {
+  ProfScope ps(PROF_MF_F64, st, 0.0);
+  IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
+  ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
+      b.tiles, b.seg_begin, nullptr, 1, b.cen, b.rad, b.mats, x, y, b.perm, 0);
+  IBEM_LAUNCH_CHECK("mf apply f64 (all pairs)");
   return IBEM_OK;
 }
 
 ibem_status mf_apply_df(const MfBatch& b, const double* x, double* y, cudaStream_t st, const int* mask, int mask_on) {
   ProfScope ps(PROF_MF_DF, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
-  ::ibem::count_launch(), k_mf_apply_df<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, mask, mask_on,
-                                                                                             b.cen, b.rad, b.mats, x, y);
+  ::ibem::count_launch(), k_mf_apply_df<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
+      b.tiles, b.seg_begin, mask, mask_on, b.cen, b.rad, b.mats, x, y, b.perm, 0);
   IBEM_LAUNCH_CHECK("mf apply df");
   return IBEM_OK;
 }
@@ -1099,7 +1228,7 @@ using namespace ibem;
 
 extern "C" ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int precision, const double* x_dev,
                                           double* y_dev, void* stream) {
-  if (!batch || !x_dev || !y_dev || (precision != 32 && precision != 48 && precision != 64))
+  if (!batch || !x_dev || !y_dev || (precision != 32 && precision != 48 && precision != 64 && precision != 65))
     return fail(IBEM_ERR_ARG, "mf_matvec: bad arguments");
   cudaStream_t st = as_stream(stream);
   MfBatch b;
@@ -1112,7 +1241,8 @@ extern "C" ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int preci
       if (e != cudaSuccess) s = cuda_fail(e, "mf_matvec workspace");
       if (!s) {
         ::ibem::count_launch(), k_div64<<<nblk(b.N), 256, 0, st>>>(b.N, x_dev, b.dc, xs);  // xs = x / Dc
-        s = precision == 64 ? mf_apply_f64(b, xs, ys, st) : mf_apply_df(b, xs, ys, st);
+        s = precision == 64 ? mf_apply_f64(b, xs, ys, st)
+                            : precision == 65 ? mf_apply_f64_all(b, xs, ys, st) : mf_apply_df(b, xs, ys, st);
         if (!s) ::ibem::count_launch(), k_div64<<<nblk(b.N), 256, 0, st>>>(b.N, ys, b.dr, y_dev);  // y = ys / Dr
       }
       if (!s) {

@@ -60,6 +60,8 @@ struct MfBatch {
   double* dc = nullptr;       // N: column scaling
   MfTile* tiles = nullptr;
   int ntiles = 0;
+  int* perm = nullptr;        // num: particles of each realisation in the Morton order of their
+                              // centres (position -> particle), used by the split FP64 product
   int hsplit = 1;      // source slices per target tile, FP32 product (autotuned)
   int hsplit_wide = 1; // the same for the double-float and FP64 products (~255 registers)
 };
@@ -82,9 +84,13 @@ struct MfPrecond {
   float* Q = nullptr;    // num*kKnn x 24 x 24 off-diagonal blocks, or nullptr (block-diagonal)
   int* nbr = nullptr;    // num*kKnn neighbour indices (-1: empty slot)
 };
-// y = As x (FP64, scaled system); y is overwritten
+// y = As x (scaled system, the deciding residual); y is overwritten.  Pairs whose source lies
+// within 8 radii (of the chunk's largest sphere) of the warp's targets are evaluated in FP64,
+// the others in double-float; targets and sources are visited in Morton order.
 ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st, const int* mask = nullptr,
                          int mask_on = 1);
+// the same with every pair in FP64 (the reference for the split)
+ibem_status mf_apply_f64_all(const MfBatch& b, const double* x, double* y, cudaStream_t st);
 // y = As x in double-float arithmetic (~48 bits, FP32 pipe); y is overwritten
 ibem_status mf_apply_df(const MfBatch& b, const double* x, double* y, cudaStream_t st, const int* mask = nullptr,
                         int mask_on = 1);

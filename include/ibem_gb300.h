@@ -242,9 +242,10 @@ typedef struct {
 /* y = A x for the sphere systems of a batch (the matrix ibem_e3d_pair_blocks would
  * assemble for each realisation, layout 24), without storing A: every 24 x 24 pair block is
  * evaluated inside the product, on the scaled system (x and y are converted on the way in
- * and out).  precision 64: FP64; 48: double-float (FP32 pairs, ~48 bits, several times
- * faster on GB300); 32: FP32, about 1e-6 relative.  x_dev, y_dev: 24 * seg_begin[nseg]
- * doubles. */
+ * and out).  precision 64: the product that decides the solver's convergence (FP64 for the
+ * sources within 8 radii of a warp's 32 targets, double-float beyond; within 1e-12 of FP64);
+ * 65: every pair in FP64; 48: double-float (FP32 pairs, ~48 bits, several times faster on
+ * GB300); 32: FP32, about 1e-6 relative.  x_dev, y_dev: 24 * seg_begin[nseg] doubles. */
 ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int precision, const double* x_dev,
                                double* y_dev, void* stream);
 

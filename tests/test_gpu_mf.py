@@ -58,6 +58,25 @@ def test_mf_matvec_matches_assembled_matrix(B):
         assert rel(dr[rows] * y32[rows], dr[rows] * ref) < 2e-5
 
 
+def test_split_deciding_product_matches_fp64(B):
+    """The deciding residual's product (FP64 for source chunks within 8 radii of a warp's
+    targets, double-float beyond; Morton order) against every pair in FP64, on a batch of
+    three realisations large enough to have far chunks: 1e-12 relative, row by row."""
+    import torch
+    from ibemproject_gb300 import cases
+    cs = [cases.farfield_case(num=n, r0=0.012, vf=0.2, grid=0, seed=40 + n) for n in (1500, 700, 33)]
+    bt = B.DeviceBatch(cs)
+    rng = np.random.default_rng(8)
+    dr, dc = bt.scalings()
+    x = torch.from_numpy(rng.standard_normal(bt.N) * dc).cuda()
+    y_split = B.matvec(bt, x, 64).cpu().numpy()
+    y_all = B.matvec(bt, x, 65).cpu().numpy()
+    for s in range(len(cs)):
+        rows = bt.seg_rows(s)
+        assert rel(dr[rows] * y_split[rows], dr[rows] * y_all[rows]) < 1e-12
+        assert scaled_err(y_split[rows], y_all[rows]) < 1e-12
+
+
 def test_block_jacobi_solve_matches_dense_lu(B):
     cs = small_cases([120, 45], seed=5, contrast=[5.7, 15.0])
     bt = B.DeviceBatch(cs)
