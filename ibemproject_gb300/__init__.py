@@ -70,7 +70,8 @@ class GenParams(ctypes.Structure):
 class EllGenParams(ctypes.Structure):
     _fields_ = [("num", ctypes.c_int), ("a1", ctypes.c_double), ("a2lo", ctypes.c_double), ("a2hi", ctypes.c_double),
                 ("a3lo", ctypes.c_double), ("a3hi", ctypes.c_double), ("vf", ctypes.c_double),
-                ("gap", ctypes.c_double), ("seed", ctypes.c_uint64), ("max_tries", ctypes.c_int64)]
+                ("gap", ctypes.c_double), ("seed", ctypes.c_uint64), ("max_tries", ctypes.c_int64),
+                ("method", ctypes.c_int), ("sweeps", ctypes.c_int)]
 
 
 class IbemError(RuntimeError):

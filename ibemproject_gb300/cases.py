@@ -287,16 +287,19 @@ def generated_case(num: int, r0: float, vf: float, seed: int, method: str = "mc"
 
 def ellipsoid_case(num: int, a1: float = 0.008, vf: float = 0.15, seed: int = 31, grid: int = 0,
                    a2=(0.5, 1.0), a3=(0.25, 1.0), gap: float = 0.2, E0: float = 70e9, nu0: float = 0.3,
-                   E1: float = 400e9, nu1: float = 0.2, sigma33: float = 1.0, max_tries: int = 0) -> Case:
+                   E1: float = 400e9, nu1: float = 0.2, sigma33: float = 1.0, max_tries: int = 0,
+                   method: str = "rsa") -> Case:
     """Boundary-free far-field case of `num` ellipsoids from the library's generator
     (ibem_e3d_generate_ellipsoids): semi-axes a1, a1 U[a2], a1 U[a3], Haar-uniform
-    orientations, random sequential addition with the surfaces kept about gap * a3 apart,
-    cube side from the volume fraction `vf`; stresses on a cell-centred grid^3.  `radius`
-    holds the longest semi-axis (a bounding radius)."""
+    orientations, random sequential addition ("rsa") or hard-ellipsoid Monte Carlo with
+    compression ("mc", for volume fractions above ~20%) with the surfaces kept about
+    gap * a3 apart, cube side from the volume fraction `vf`; stresses on a cell-centred
+    grid^3.  `radius` holds the longest semi-axis (a bounding radius)."""
     import ctypes
 
-    from . import EllGenParams, check, lib
-    p = EllGenParams(int(num), a1, a2[0], a2[1], a3[0], a3[1], vf, gap, int(seed), int(max_tries))
+    from . import GEN_MC, GEN_RSA, EllGenParams, check, lib
+    p = EllGenParams(int(num), a1, a2[0], a2[1], a3[0], a3[1], vf, gap, int(seed), int(max_tries),
+                     GEN_MC if method == "mc" else GEN_RSA, 0)
     C, A, Q = np.zeros((num, 3)), np.zeros((num, 3)), np.zeros((num, 4))
     side = ctypes.c_double(0.0)
     dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))

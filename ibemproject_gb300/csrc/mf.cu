@@ -46,6 +46,7 @@ namespace {
 constexpr int kMfThreads = 128;
 constexpr int kMfChunk = 32;
 constexpr double kMfFarRadii = 8.0;   // near / far split of the deciding residual
+constexpr int kMfSplitMin = 4096;     // smallest realisation (particles) that uses the split
 
 // sink of a generated block: acc[r] += v * x[c] (r, c compile-time constants after inlining)
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
@@ -920,10 +921,14 @@ ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStrea
   // near chunks in FP64, far chunks (beyond kMfFarRadii radii of the warp's targets) in
   // double-float: their contributions are at most kMfFarRadii^-3 of a near one, so the
   // double-float rounding (~2^-44 per operation) stays far below FP64 level in the sum
+  // in realisations below kMfSplitMin particles most (warp, chunk) pairs are near, and one
+  // FP64 launch over every pair is faster than the two passes
+  const bool split = b.max_seg >= kMfSplitMin;
   ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
-      b.tiles, b.seg_begin, mask, mask_on, b.cen, b.rad, b.mats, x, y, b.perm, 1);
-  ::ibem::count_launch(), k_mf_apply_df<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
-      b.tiles, b.seg_begin, mask, mask_on, b.cen, b.rad, b.mats, x, y, b.perm, 2);
+      b.tiles, b.seg_begin, mask, mask_on, b.cen, b.rad, b.mats, x, y, b.perm, split ? 1 : 0);
+  if (split)
+    ::ibem::count_launch(), k_mf_apply_df<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
+        b.tiles, b.seg_begin, mask, mask_on, b.cen, b.rad, b.mats, x, y, b.perm, 2);
   IBEM_LAUNCH_CHECK("mf apply f64");
   return IBEM_OK;
 }

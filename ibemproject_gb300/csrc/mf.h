@@ -84,9 +84,10 @@ struct MfPrecond {
   float* Q = nullptr;    // num*kKnn x 24 x 24 off-diagonal blocks, or nullptr (block-diagonal)
   int* nbr = nullptr;    // num*kKnn neighbour indices (-1: empty slot)
 };
-// y = As x (scaled system, the deciding residual); y is overwritten.  Pairs whose source lies
-// within 8 radii (of the chunk's largest sphere) of the warp's targets are evaluated in FP64,
-// the others in double-float; targets and sources are visited in Morton order.
+// y = As x (scaled system, the deciding residual); y is overwritten.  In batches whose largest
+// realisation has 4,096 particles or more, pairs whose source lies within 8 radii (of the
+// chunk's largest sphere) of the warp's targets are evaluated in FP64 and the others in
+// double-float; below that, every pair in FP64.  Targets and sources in Morton order.
 ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st, const int* mask = nullptr,
                          int mask_on = 1);
 // the same with every pair in FP64 (the reference for the split)

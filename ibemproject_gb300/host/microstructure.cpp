@@ -305,11 +305,157 @@ void ell_quat_to_rot_host(const double* q, double* Q) {
 }
 }  // namespace ibem
 
+namespace {
+
+// random sequential addition inside [a1, L - a1]^3
+ibem_status ell_rsa(const ibem_ell_gen_params& p, double L, double rbmax, const std::vector<Ell>& e,
+                    std::vector<double>& c) {
+  const int num = p.num;
+  const double lo = p.a1, hi = L - p.a1;
+  if (hi <= lo) return ibem::fail(IBEM_ERR_ARG, "generate_ellipsoids: cube smaller than one ellipsoid");
+  Rng rng(p.seed + 0x632be59bd9b4e019ULL);
+  Cells g;
+  g.build(L, 2.0 * rbmax, c, 0);
+  const int64_t cap = p.max_tries > 0 ? p.max_tries : 200000000LL;
+  int64_t tries = 0;
+  for (int k = 0; k < num; ++k) {
+    double x[3];
+    bool bad;
+    do {
+      if (++tries > cap)
+        return ibem::fail(IBEM_ERR_ARG, "generate_ellipsoids: random sequential addition stalled at " +
+                                            std::to_string(k) + " of " + std::to_string(num));
+      for (double& v : x) v = rng.uniform(lo, hi);
+      bad = g.any_near(x, [&](int j) {
+        const double r[3] = {c[3 * j] - x[0], c[3 * j + 1] - x[1], c[3 * j + 2] - x[2]};
+        return ell_overlap(e[k], e[j], r);
+      });
+    } while (bad);
+    std::memcpy(&c[3 * k], x, sizeof x);
+    g.insert(k, x);
+  }
+  return IBEM_OK;
+}
+
+// q <- q * (rotation by a small random angle about a uniform axis), normalised
+void jiggle_quat(Rng& g, double maxang, const double* q, double* out) {
+  double ax[3], n2;
+  do {
+    for (double& v : ax) v = g.uniform(-1.0, 1.0);
+    n2 = ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2];
+  } while (n2 > 1.0 || n2 < 1e-12);
+  const double ang = g.uniform(-maxang, maxang), sh = std::sin(0.5 * ang) / std::sqrt(n2);
+  const double r[4] = {std::cos(0.5 * ang), ax[0] * sh, ax[1] * sh, ax[2] * sh};
+  double o[4] = {q[0] * r[0] - q[1] * r[1] - q[2] * r[2] - q[3] * r[3],
+                 q[0] * r[1] + q[1] * r[0] + q[2] * r[3] - q[3] * r[2],
+                 q[0] * r[2] - q[1] * r[3] + q[2] * r[0] + q[3] * r[1],
+                 q[0] * r[3] + q[1] * r[2] - q[2] * r[1] + q[3] * r[0]};
+  const double n = std::sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2] + o[3] * o[3]);
+  for (int i = 0; i < 4; ++i) out[i] = o[i] / n;
+}
+
+// Hard-ellipsoid Monte Carlo with box compression (the ellipsoid counterpart of `mc` above):
+// a simple cubic start that clears the largest bounding spheres, sweeps of random
+// translations (reflected at the faces) and small rotations rejected on overlap, and after
+// each sweep a uniform scaling of the centres toward the target side as far as the closest
+// pair allows (scaling a pair's offset by s scales its contact function by s^2, so the pair
+// touches at s = F_max^-1/2; the scale closes half of the remaining room).  Centres stay in
+// [0, L]^3; orientations change with the moves.
+ibem_status ell_mc(const ibem_ell_gen_params& p, double L, double rbmax, const std::vector<double>& a,
+                   std::vector<double>& q, std::vector<Ell>& e, std::vector<double>& c) {
+  const int num = p.num;
+  Rng rng(p.seed ^ 0x5bd1e995ULL);
+  int m = 1;
+  while ((int64_t)m * m * m < num) ++m;
+  const double s0 = 2.0 * rbmax * (1.0 + 1e-9);
+  double Lc = std::max(L, m > 1 ? s0 * (m - 1) : L);
+  const double step0 = m > 1 ? Lc / (m - 1) : 0.0;
+  std::vector<int> site((size_t)m * m * m);
+  for (size_t i = 0; i < site.size(); ++i) site[i] = (int)i;
+  for (size_t i = site.size() - 1; i > 0; --i) std::swap(site[i], site[rng.next() % (i + 1)]);
+  for (int k = 0; k < num; ++k) {
+    const int t = site[k];
+    c[3 * k] = step0 * (t % m);
+    c[3 * k + 1] = step0 * ((t / m) % m);
+    c[3 * k + 2] = step0 * (t / (m * m));
+    if (m == 1)
+      for (int d = 0; d < 3; ++d) c[3 * k + d] = 0.5 * L;
+  }
+  constexpr double kMinScale = 0.9;
+  const double h = 2.0 * rbmax;
+  const double hc = h / kMinScale;
+  const double infl = 0.5 * p.gap;
+  Cells g;
+  double delta = 0.25 * h, rot = 0.3;
+  const int settle = p.sweeps > 0 ? p.sweeps : 50;
+  int after = 0, stalled = 0;
+  for (int sweep = 0; sweep < 20000; ++sweep) {
+    g.build(Lc, hc, c, num);
+    int accepted = 0;
+    for (int t = 0; t < num; ++t) {
+      const int k = (int)(rng.next() % (uint64_t)num);
+      double x[3], qn[4];
+      for (int d = 0; d < 3; ++d) {
+        x[d] = c[3 * k + d] + rng.uniform(-delta, delta);
+        if (x[d] < 0.0) x[d] = -x[d];
+        if (x[d] > Lc) x[d] = 2.0 * Lc - x[d];
+        x[d] = std::min(std::max(x[d], 0.0), Lc);
+      }
+      jiggle_quat(rng, rot, &q[4 * k], qn);
+      const Ell en = make_ell(&a[3 * k], qn, infl * a[3 * k + 2]);
+      const bool bad = g.any_near(x, [&](int j) {
+        if (j == k) return false;
+        const double r[3] = {c[3 * j] - x[0], c[3 * j + 1] - x[1], c[3 * j + 2] - x[2]};
+        return ell_overlap(en, e[j], r);
+      });
+      if (bad) continue;
+      g.remove(k);
+      std::memcpy(&c[3 * k], x, sizeof x);
+      std::memcpy(&q[4 * k], qn, sizeof qn);
+      e[k] = en;
+      g.insert(k, x);
+      ++accepted;
+    }
+    const double acc = (double)accepted / num;
+    delta *= acc > 0.35 ? 1.1 : 0.9;
+    delta = std::min(std::max(delta, 1e-6 * h), 0.5 * h);
+    rot = std::min(std::max(rot * (acc > 0.35 ? 1.1 : 0.9), 1e-4), 1.0);
+    if (Lc <= L) {
+      if (++after >= settle) return IBEM_OK;
+      continue;
+    }
+    // largest admissible shrink from the closest pair (bounding spheres overlapping)
+    double f = 0.0;
+    for (int k = 0; k < num; ++k)
+      g.any_near(&c[3 * k], [&](int j) {
+        if (j <= k) return false;
+        const double r[3] = {c[3 * j] - c[3 * k], c[3 * j + 1] - c[3 * k + 1], c[3 * j + 2] - c[3 * k + 2]};
+        const double d2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        if (d2 >= (e[k].rb + e[j].rb) * (e[k].rb + e[j].rb)) {
+          f = std::max(f, (e[k].rb + e[j].rb) / std::sqrt(d2));
+          return false;
+        }
+        f = std::max(f, 1.0 / std::sqrt(pw_max(e[k], e[j], r)));
+        return false;
+      });
+    const double scale = std::max({L / Lc, kMinScale, 0.5 * (1.0 + f)});
+    stalled = scale > 1.0 - 1e-7 ? stalled + 1 : 0;
+    if (stalled > 500) break;
+    if (scale < 1.0) {
+      for (double& v : c) v *= scale;
+      Lc = std::max(L, Lc * scale);
+    }
+  }
+  return ibem::fail(IBEM_ERR_ARG, "generate_ellipsoids: compression did not reach the volume fraction");
+}
+
+}  // namespace
+
 extern "C" ibem_status ibem_e3d_generate_ellipsoids(const ibem_ell_gen_params* p, double* centers, double* axes,
                                                     double* quats, double* side) {
   if (!p || p->num < 1 || !centers || !axes || !quats || !(p->a1 > 0) || !(p->a2lo > 0) || p->a2hi < p->a2lo ||
       !(p->a3lo > 0) || p->a3hi < p->a3lo || p->a2hi > 1 || p->a3hi > 1 || !(p->vf > 0 && p->vf < 0.5) ||
-      p->gap < 0)
+      p->gap < 0 || (p->method != IBEM_GEN_RSA && p->method != IBEM_GEN_MC))
     return ibem::fail(IBEM_ERR_ARG, "generate_ellipsoids: bad parameters");
   const int num = p->num;
   Rng rs(p->seed);
@@ -330,29 +476,8 @@ extern "C" ibem_status ibem_e3d_generate_ellipsoids(const ibem_ell_gen_params* p
     e[k] = make_ell(&a[3 * k], &q[4 * k], 0.5 * p->gap * a[3 * k + 2]);
     rbmax = std::max(rbmax, e[k].rb);
   }
-  const double lo = p->a1, hi = L - p->a1;
-  if (hi <= lo) return ibem::fail(IBEM_ERR_ARG, "generate_ellipsoids: cube smaller than one ellipsoid");
-  Rng rng(p->seed + 0x632be59bd9b4e019ULL);
-  Cells g;
-  g.build(L, 2.0 * rbmax, c, 0);
-  const int64_t cap = p->max_tries > 0 ? p->max_tries : 200000000LL;
-  int64_t tries = 0;
-  for (int k = 0; k < num; ++k) {
-    double x[3];
-    bool bad;
-    do {
-      if (++tries > cap)
-        return ibem::fail(IBEM_ERR_ARG, "generate_ellipsoids: random sequential addition stalled at " +
-                                            std::to_string(k) + " of " + std::to_string(num));
-      for (double& v : x) v = rng.uniform(lo, hi);
-      bad = g.any_near(x, [&](int j) {
-        const double r[3] = {c[3 * j] - x[0], c[3 * j + 1] - x[1], c[3 * j + 2] - x[2]};
-        return ell_overlap(e[k], e[j], r);
-      });
-    } while (bad);
-    std::memcpy(&c[3 * k], x, sizeof x);
-    g.insert(k, x);
-  }
+  ibem_status st = p->method == IBEM_GEN_MC ? ell_mc(*p, L, rbmax, a, q, e, c) : ell_rsa(*p, L, rbmax, e, c);
+  if (st) return st;
   std::memcpy(centers, c.data(), sizeof(double) * c.size());
   std::memcpy(axes, a.data(), sizeof(double) * a.size());
   std::memcpy(quats, q.data(), sizeof(double) * q.size());

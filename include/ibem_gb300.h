@@ -242,8 +242,9 @@ typedef struct {
 /* y = A x for the sphere systems of a batch (the matrix ibem_e3d_pair_blocks would
  * assemble for each realisation, layout 24), without storing A: every 24 x 24 pair block is
  * evaluated inside the product, on the scaled system (x and y are converted on the way in
- * and out).  precision 64: the product that decides the solver's convergence (FP64 for the
- * sources within 8 radii of a warp's 32 targets, double-float beyond; within 1e-12 of FP64);
+ * and out).  precision 64: the product that decides the solver's convergence (in
+ * realisations of 4,096 particles or more FP64 for the sources within 8 radii of a warp's
+ * 32 targets and double-float beyond, within 1e-12 of FP64; FP64 throughout below that);
  * 65: every pair in FP64; 48: double-float (FP32 pairs, ~48 bits, several times faster on
  * GB300); 32: FP32, about 1e-6 relative.  x_dev, y_dev: 24 * seg_begin[nseg] doubles. */
 ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int precision, const double* x_dev,
@@ -372,11 +373,14 @@ ibem_status ibem_e3d_generate_spheres(const ibem_gen_params* p, double* centers,
 
 /* Seeded ellipsoid microstructures: semi-axes a1, a2 = a1 U[a2lo, a2hi], a3 = a1 U[a3lo, a3hi]
  * (a3 is then the shortest only if a3hi <= a2lo), orientations uniform on SO(3) (Haar,
- * quaternions from three uniforms), centres by random sequential addition inside the cube
- * [a1, L - a1]^3 of side L = (sum of volumes / vf)^(1/3).  Two ellipsoids are kept apart
- * by testing them with every semi-axis inflated by gap * a3 / 2 (Perram-Wertheim contact
- * function).  Host outputs: centers n x 3, axes n x 3 (a1 a2 a3 along the principal
- * axes), quats n x 4 (w, x, y, z), side (may be NULL).  Host only. */
+ * quaternions from three uniforms), cube side L = (sum of volumes / vf)^(1/3).  Two
+ * ellipsoids are kept apart by testing them with every semi-axis inflated by gap * a3 / 2
+ * (Perram-Wertheim contact function).  method IBEM_GEN_RSA: random sequential addition of
+ * centres inside [a1, L - a1]^3 (jams near 20% for the default shapes); IBEM_GEN_MC:
+ * hard-ellipsoid Monte Carlo (translations and rotations) with box compression, centres in
+ * [0, L]^3, orientations moved from their Haar draws.  Host outputs: centers n x 3, axes
+ * n x 3 (a1 a2 a3 along the principal axes), quats n x 4 (w, x, y, z), side (may be NULL).
+ * Host only. */
 typedef struct {
   int num;
   double a1;
@@ -384,7 +388,9 @@ typedef struct {
   double vf;
   double gap;
   uint64_t seed;
-  int64_t max_tries;  /* candidate centres before giving up (0 = 2e8) */
+  int64_t max_tries;  /* RSA: candidate centres before giving up (0 = 2e8) */
+  int method;         /* ibem_gen_method */
+  int sweeps;         /* MC: sweeps after the target side is reached (0 = 50) */
 } ibem_ell_gen_params;
 
 ibem_status ibem_e3d_generate_ellipsoids(const ibem_ell_gen_params* p, double* centers, double* axes,
