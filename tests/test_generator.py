@@ -110,23 +110,27 @@ def _pw_max(PA, PB, r):
     return best
 
 
-def test_ellipsoid_generator_keeps_bodies_apart_and_is_seeded():
+@pytest.mark.parametrize("method,vf", [("rsa", 0.15), ("mc", 0.27)])
+def test_ellipsoid_generator_keeps_bodies_apart_and_is_seeded(method, vf):
     """ibem_e3d_generate_ellipsoids: semi-axes in range, unit quaternions, centres in the
     cube, the same microstructure for the same seed, and no two ellipsoids overlapping
-    (Perram-Wertheim contact function > 1, checked here by a grid search in numpy)."""
+    (Perram-Wertheim contact function > 1, checked here by a grid search in numpy); random
+    sequential addition and Monte Carlo compression (which reaches the fill fractions where
+    addition jams)."""
     from ibemproject_gb300 import cases
-    c = cases.ellipsoid_case(150, a1=0.008, vf=0.15, seed=2)
-    c2 = cases.ellipsoid_case(150, a1=0.008, vf=0.15, seed=2)
+    c = cases.ellipsoid_case(150, a1=0.008, vf=vf, seed=2, method=method)
+    c2 = cases.ellipsoid_case(150, a1=0.008, vf=vf, seed=2, method=method)
     assert np.array_equal(c.centers, c2.centers) and np.array_equal(c.quats, c2.quats)
-    assert not np.array_equal(c.centers, cases.ellipsoid_case(150, a1=0.008, vf=0.15, seed=3).centers)
+    assert not np.array_equal(c.centers, cases.ellipsoid_case(150, a1=0.008, vf=vf, seed=3, method=method).centers)
     A = c.axes
     assert np.all(A[:, 0] == 0.008)
     assert np.all((A[:, 1] >= 0.004) & (A[:, 1] <= 0.008)) and np.all((A[:, 2] >= 0.002) & (A[:, 2] <= 0.008))
     assert np.allclose(np.linalg.norm(c.quats, axis=1), 1.0)
     L = float(c.title.split("=")[1])
-    assert np.all(c.centers >= 0.008) and np.all(c.centers <= L - 0.008)
+    lo = 0.008 if method == "rsa" else 0.0
+    assert np.all(c.centers >= lo) and np.all(c.centers <= L - lo)
     vol = (4 / 3 * np.pi * A.prod(axis=1)).sum()
-    assert abs(vol / L ** 3 - 0.15) < 1e-9
+    assert abs(vol / L ** 3 - vf) < 1e-9
 
     def rot(q):
         w, x, y, z = q / np.linalg.norm(q)
