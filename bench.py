@@ -342,16 +342,19 @@ def train_preconditioner(args, rank, dev):
 
 
 def run_batched(args, dev, params):
-    """Batched realisations (config 5's shape, with spheres): args.batch microstructures of
-    U[50, 500] spheres (radius U[0.8, 1.2] x 0.008, min gap 0.1 r, hard-sphere Monte Carlo
-    packing from the library's generator), volume fraction U[10%, 30%], contrast E1/E0
-    U[2, 20], half with linear eigenstrain (24 unknowns per sphere) and half with quadratic
-    (60), uniaxial remote stress.  One step = right-hand sides, the linear realisations in
-    one batched matrix-free solve (learned preconditioner, FP64 refinement to relative
-    residual 1e-10), the quadratic ones assembled (FP64 pair blocks) and solved one after
-    another to scaled backward error 1e-12 (--quad-form bj: FP64 refinement of FP32-product
-    GMRES with per-sphere block-Jacobi; mixed: FP32 LU with split-BF16 tensor-core updates
-    and FP64 GMRES-IR), and the effective moduli of all.  Reports realisations per second."""
+    """Batched realisations (config 5): args.batch microstructures of U[50, 500] particles,
+    spheres or ellipsoids 50/50 (spheres: radius U[0.8, 1.2] x 0.008, min gap 0.1 r;
+    ellipsoids: a1 = 0.008, a2 = a1 U[0.5, 1], a3 = a1 U[0.25, 1], Haar orientations, gap
+    ~0.2 a3; both packed by the library's hard-particle Monte Carlo generators), volume
+    fraction U[10%, 30%], contrast E1/E0 U[2, 20]; spheres half with linear eigenstrain (24
+    unknowns per sphere) and half with quadratic (60), ellipsoids linear; uniaxial remote
+    stress.  One step = right-hand sides, the linear sphere realisations in one batched
+    matrix-free solve (learned preconditioner, FP64 refinement to relative residual 1e-10),
+    the quadratic sphere and the ellipsoid realisations assembled (FP64 pair blocks) and
+    solved one after another to scaled backward error 1e-12 (--quad-form bj: FP64 refinement
+    of FP32-product GMRES with per-particle block-Jacobi; mixed: FP32 LU with split-BF16
+    tensor-core updates and FP64 GMRES-IR), and the effective moduli of all.  Reports
+    realisations per second."""
     import torch
     import ibemproject_gb300 as g
     from ibemproject_gb300 import batch as B
@@ -360,22 +363,25 @@ def run_batched(args, dev, params):
     nums = rng.integers(50, 501, size=args.batch)
     vfs = rng.uniform(0.10, 0.30, size=args.batch)
     contrast = rng.uniform(2.0, 20.0, size=args.batch)
-    quad = rng.random(args.batch) < 0.5
+    ell = rng.random(args.batch) < 0.5
+    quad = (rng.random(args.batch) < 0.5) & ~ell
     t = time.perf_counter()
-    cs = [cases.generated_case(int(n), 0.008, float(v), seed=7000 + k, E1=70e9 * float(c))
-          for k, (n, v, c) in enumerate(zip(nums, vfs, contrast))]
+    cs = [cases.ellipsoid_case(int(n), a1=0.008, vf=float(v), seed=7000 + k, E1=70e9 * float(c), method="mc")
+          if e else cases.generated_case(int(n), 0.008, float(v), seed=7000 + k, E1=70e9 * float(c))
+          for k, (n, v, c, e) in enumerate(zip(nums, vfs, contrast, ell))]
     t_gen = time.perf_counter() - t
     vol = np.array([float(c.title.split("=")[1]) ** 3 for c in cs])   # cube of side L
-    li, qi = np.flatnonzero(~quad), np.flatnonzero(quad)
+    li, qi, ei = np.flatnonzero(~quad & ~ell), np.flatnonzero(quad), np.flatnonzero(ell)
     bl = B.DeviceBatch([cs[i] for i in li], device=dev) if li.size else None
     bq = B.DeviceBatch([cs[i] for i in qi], device=dev, layout=60) if qi.size else None
+    be = B.DeviceBatch([cs[i] for i in ei], device=dev) if ei.size else None
     sig = np.array([0, 0, 0, 0, 0, 1.0])
     stream = torch.cuda.current_stream(dev)
     qform = g.SOLVE_GMRES_BJ if args.quad_form == "bj" else g.SOLVE_MIXED_IR
 
     def step():
         out = {}
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         ev[0].record(stream)
         if bl is not None:
             b = B.farfield_rhs(bl, sig)
@@ -383,12 +389,13 @@ def run_batched(args, dev, params):
             e, _ = B.effective_modulus(bl, x, sig, volume=vol[li])
             out["lin"] = (x, reps, e, b)
         ev[1].record(stream)
-        if bq is not None:
-            b = B.farfield_rhs(bq, sig)
-            x, reps = B.dense_batch_solve(bq, b, qform, tol=1e-12)
-            e, _ = B.effective_modulus(bq, x, sig, volume=vol[qi])
-            out["quad"] = (x, reps, e, b)
-        ev[2].record(stream)
+        for key, bt, idx in (("quad", bq, qi), ("ell", be, ei)):
+            if bt is not None:
+                b = B.farfield_rhs(bt, sig)
+                x, reps = B.dense_batch_solve(bt, b, qform, tol=1e-12)
+                e, _ = B.effective_modulus(bt, x, sig, volume=vol[idx])
+                out[key] = (x, reps, e, b)
+            ev[2 if key == "quad" else 3].record(stream)
         return out, ev
 
     step()   # warm-up
@@ -405,45 +412,51 @@ def run_batched(args, dev, params):
     ms = t0.elapsed_time(t1) / k
     ms_lin = statistics.median(e[0].elapsed_time(e[1]) for e in evs)
     ms_quad = statistics.median(e[1].elapsed_time(e[2]) for e in evs)
+    ms_ell = statistics.median(e[2].elapsed_time(e[3]) for e in evs)
     # realisations of each kind against the plain FP64 LU of their own layout
-    errs = {"linear": [], "quadratic": []}
-    for kind, bt, idx, lay in (("linear", bl, li, 24), ("quadratic", bq, qi, 60)):
+    errs = {"linear_spheres": [], "quadratic_spheres": [], "linear_ellipsoids": []}
+    for kind, key, bt, idx, lay in (("linear_spheres", "lin", bl, li, 24), ("quadratic_spheres", "quad", bq, qi, 60),
+                                    ("linear_ellipsoids", "ell", be, ei, 24)):
         if bt is None:
             continue
-        x, _, _, b = out["lin" if lay == 24 else "quad"]
+        x, _, _, b = out[key]
         sub = nums[idx]
-        picks = {int(np.argmin(sub)), int(np.argmin(np.abs(sub - 200)))}
-        if lay == 24:
-            picks.add(int(np.argmax(sub)))
+        picks = {int(np.argmin(sub)), int(np.argmin(np.abs(sub - 200))), int(np.argmax(sub))}
         for s_ in sorted(picks):
             rows = bt.seg_rows(s_)
-            xd = B.dense_solve(cs[idx[s_]], b[rows], device=dev, layout=lay)
-            errs[kind].append(float((x[rows] - xd).abs().max() / xd.abs().max()))
+            if key == "ell":
+                c = cs[idx[s_]]
+                c0 = cases.Case(c.E0, c.nu0, c.E1, c.nu1, c.nodes, c.conn, c.bc, c.tbc, c.centers, c.radius,
+                                np.zeros((0, 3)), c.sig_inf, c.title, c.axes, c.quats)
+                xd = torch.from_numpy(g.run_host_ell(c0, form=g.SOLVE_FP64)[0])
+                errs[kind].append(float((x[rows].cpu() - xd).abs().max() / xd.abs().max()))
+            else:
+                xd = B.dense_solve(cs[idx[s_]], b[rows], device=dev, layout=lay)
+                errs[kind].append(float((x[rows] - xd).abs().max() / xd.abs().max()))
     E0 = np.array([c.E0 for c in cs])
     e_all = np.zeros(args.batch)
-    if bl is not None:
-        e_all[li] = out["lin"][2]
-    if bq is not None:
-        e_all[qi] = out["quad"][2]
+    for key, idx in (("lin", li), ("quad", qi), ("ell", ei)):
+        if key in out:
+            e_all[idx] = out[key][2]
     ratio = e_all / E0
     lin_reps = out["lin"][1] if bl is not None else []
-    quad_reps = out["quad"][1] if bq is not None else []
-    return {"workload": (f"{args.batch} realisations, U[50,500] spheres r~U[0.8,1.2]*0.008, vf U[10%,30%], "
-                         "E1/E0 U[2,20], half linear (24/sphere, matrix-free learned GMRES) and half quadratic "
-                         "(60/sphere, assembled; " + ("block-Jacobi FP32-product GMRES + FP64 refinement"
-                                                      if args.quad_form == "bj" else
-                                                      "FP32 LU + BF16x3 + FP64 GMRES-IR") +
-                         ") eigenstrain, far-field sigma33"),
+    dense_reps = (out["quad"][1] if bq is not None else []) + (out["ell"][1] if be is not None else [])
+    return {"workload": (f"{args.batch} realisations, U[50,500] particles, spheres (r~U[0.8,1.2]*0.008) or ellipsoids "
+                         "(a1=0.008, a2=a1 U[0.5,1], a3=a1 U[0.25,1]) 50/50, vf U[10%,30%], E1/E0 U[2,20]; spheres half "
+                         "linear (24/sphere, matrix-free learned GMRES) and half quadratic (60/sphere), ellipsoids "
+                         "linear; quadratic and ellipsoid realisations assembled and solved by " +
+                         ("block-Jacobi FP32-product GMRES + FP64 refinement" if args.quad_form == "bj" else
+                          "FP32 LU + BF16x3 + FP64 GMRES-IR") + ", far-field sigma33"),
             "value": args.batch / (ms / 1e3), "unit": "realisations/s", "ms_per_batch": ms,
-            "ms_linear_part": ms_lin, "ms_quadratic_part": ms_quad,
-            "realisations_linear": int(li.size), "realisations_quadratic": int(qi.size),
-            "spheres": int(nums.sum()), "unknowns": int(24 * nums[li].sum() + 60 * nums[qi].sum()),
-            "pair_products_per_matvec_linear": int(np.sum(nums[li].astype(np.int64) ** 2)),
+            "ms_linear_spheres": ms_lin, "ms_quadratic_spheres": ms_quad, "ms_ellipsoids": ms_ell,
+            "realisations_linear_spheres": int(li.size), "realisations_quadratic_spheres": int(qi.size),
+            "realisations_ellipsoids": int(ei.size),
+            "particles": int(nums.sum()), "unknowns": int(24 * nums[li].sum() + 60 * nums[qi].sum() + 24 * nums[ei].sum()),
             "arnoldi_steps_max": max((r.inner for r in lin_reps), default=0),
             "refinement_steps_max": max((r.outer for r in lin_reps), default=0),
             "rel_residual_max": max((r.rel_residual for r in lin_reps), default=0.0),
-            "quadratic_backward_error_max": max((r.backward_error for r in quad_reps), default=0.0),
-            "quadratic_gmres_iterations_max": max((r.iterations for r in quad_reps), default=0),
+            "dense_backward_error_max": max((r.backward_error for r in dense_reps), default=0.0),
+            "dense_gmres_iterations_max": max((r.iterations for r in dense_reps), default=0),
             "rel_err_vs_plain_fp64": errs,
             "effective_modulus_over_E0": {"mean": float(ratio.mean()), "min": float(ratio.min()),
                                           "max": float(ratio.max())},

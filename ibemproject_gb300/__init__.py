@@ -44,7 +44,7 @@ class SolveReport(ctypes.Structure):
 class Batch(ctypes.Structure):
     _fields_ = [("nseg", ctypes.c_int), ("seg_begin", ctypes.POINTER(ctypes.c_int)),
                 ("centers_dev", ctypes.c_void_p), ("radius_dev", ctypes.c_void_p),
-                ("mats", ctypes.POINTER(Material))]
+                ("mats", ctypes.POINTER(Material)), ("axes_dev", ctypes.c_void_p), ("quats_dev", ctypes.c_void_p)]
 
 
 class MfOptions(ctypes.Structure):

@@ -30,6 +30,9 @@ def _ptr(t) -> int:
 
 
 def _linear(batch) -> None:
+    if getattr(batch, "ellipsoids", False):
+        raise ValueError("the matrix-free solver and the learned preconditioner take spheres; "
+                         "solve ellipsoid batches with dense_batch_solve")
     if batch.layout != NU:
         raise ValueError(f"the matrix-free solver and the learned preconditioner take layout {NU}, "
                          f"not {batch.layout}")
@@ -55,8 +58,18 @@ class DeviceBatch:
         self.centers = torch.from_numpy(cen.copy()).to(device)
         self.radius = torch.from_numpy(rad.copy()).to(device)
         self.mats = (Material * len(self.cases))(*[Material(c.E0, c.nu0, c.E1, c.nu1) for c in self.cases])
+        # ellipsoids: every realisation carries semi-axes and quaternions (a batch is all
+        # spheres or all ellipsoids)
+        self.ellipsoids = all(getattr(c, "axes", None) is not None for c in self.cases) and bool(self.cases)
+        self.axes = self.quats = None
+        if self.ellipsoids:
+            self.axes = torch.from_numpy(np.concatenate([np.asarray(c.axes, dtype=np.float64) for c in self.cases])).to(
+                device)
+            self.quats = torch.from_numpy(np.concatenate([np.asarray(c.quats, dtype=np.float64)
+                                                          for c in self.cases])).to(device)
         self.rec = Batch(len(self.cases), self.seg_begin.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
-                         _ptr(self.centers), _ptr(self.radius), self.mats)
+                         _ptr(self.centers), _ptr(self.radius), self.mats,
+                         _ptr(self.axes) if self.ellipsoids else None, _ptr(self.quats) if self.ellipsoids else None)
         self.device = device
 
     @property

@@ -938,6 +938,7 @@ extern "C" ibem_status ibem_gnn_init_params(float* params_dev, uint64_t seed, vo
 extern "C" ibem_status ibem_gnn_prepare(const ibem_e3d_batch* batch, int nrhs, const double* r_hat_dev,
                                         const double* e_hat_dev, int* nbr_dev, float* node_feat_dev,
                                         float* edge_feat_dev, float* z_dev, float* u_dev, void* stream) {
+  if (batch && batch->axes_dev) return fail(IBEM_ERR_ARG, "matrix-free products and the learned preconditioner take spheres; solve ellipsoid batches with ibem_e3d_batch_dense_solve");
   if (!batch || !nbr_dev || !node_feat_dev || !edge_feat_dev || nrhs < 0) return fail(IBEM_ERR_ARG, "gnn_prepare: bad arguments");
   if (nrhs > 0 && (!r_hat_dev || !e_hat_dev || !z_dev || !u_dev)) return fail(IBEM_ERR_ARG, "gnn_prepare: samples");
   cudaStream_t st = as_stream(stream);
@@ -1000,6 +1001,7 @@ extern "C" ibem_status ibem_gnn_adamw(int64_t n, float* params_dev, const float*
 extern "C" ibem_status ibem_gnn_train(const ibem_e3d_batch* batch, int nrhs, const double* r_hat_dev,
                                       const double* e_hat_dev, float* params_dev, int steps, float lr,
                                       float weight_decay, double* loss_hist, void* stream) {
+  if (batch && batch->axes_dev) return fail(IBEM_ERR_ARG, "matrix-free products and the learned preconditioner take spheres; solve ellipsoid batches with ibem_e3d_batch_dense_solve");
   if (!batch || nrhs <= 0 || !r_hat_dev || !e_hat_dev || !params_dev || steps < 0 || !loss_hist)
     return fail(IBEM_ERR_ARG, "gnn_train: bad arguments");
   cudaStream_t st = as_stream(stream);

@@ -661,11 +661,13 @@ __global__ void k_sub_f32(int64_t n, const float* __restrict__ a, const float* _
 // so the order-2 coefficients E_ijkk (diagonal (k, k) slots: 0, 3, 5 of the six p <= q of
 // layout 60; 0, 4, 8 of the nine (p, q) of layout 78) add a^2/5 each.
 __global__ void k_vol_eigen(int num, int nu, const int* __restrict__ seg_of, const double* __restrict__ rad,
-                            const double* __restrict__ x, double* __restrict__ out) {
+                            const double* __restrict__ axes, const double* __restrict__ x, double* __restrict__ out) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= num) return;
   const double a = rad[p];
-  const double vp = 4.0 / 3.0 * 3.141592653589793 * a * a * a;
+  // particle volume (an ellipsoid's linear eigenstrain averages to its uniform part)
+  const double vp = 4.0 / 3.0 * 3.141592653589793 *
+                    (axes ? axes[3 * (int64_t)p] * axes[3 * (int64_t)p + 1] * axes[3 * (int64_t)p + 2] : a * a * a);
   const double q = a * a / 5.0;
   const double* e = x + (int64_t)nu * p;
   for (int r = 0; r < 6; ++r) {
@@ -699,6 +701,7 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
   b.N = (int64_t)kMfNu * b.num;
   b.cen = in.centers_dev;
   b.rad = in.radius_dev;
+  b.axes = in.axes_dev;
   std::vector<int> seg_of(b.num);
   std::vector<MfTile> tiles;
   for (int s = 0; s < in.nseg; ++s) {
@@ -1233,6 +1236,7 @@ using namespace ibem;
 
 extern "C" ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int precision, const double* x_dev,
                                           double* y_dev, void* stream) {
+  if (batch && batch->axes_dev) return fail(IBEM_ERR_ARG, "matrix-free products and the learned preconditioner take spheres; solve ellipsoid batches with ibem_e3d_batch_dense_solve");
   if (!batch || !x_dev || !y_dev || (precision != 32 && precision != 48 && precision != 64 && precision != 65))
     return fail(IBEM_ERR_ARG, "mf_matvec: bad arguments");
   cudaStream_t st = as_stream(stream);
@@ -1285,6 +1289,7 @@ extern "C" ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int preci
 extern "C" ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const double* b_dev, double* x_dev,
                                          ibem_precond pc, const float* gnn_params_dev, const ibem_mf_options* opt,
                                          ibem_mf_report* reports, void* stream) {
+  if (batch && batch->axes_dev) return fail(IBEM_ERR_ARG, "matrix-free products and the learned preconditioner take spheres; solve ellipsoid batches with ibem_e3d_batch_dense_solve");
   if (!batch || !b_dev || !x_dev || !reports) return fail(IBEM_ERR_ARG, "mf_solve: bad arguments");
   if (pc != IBEM_PRECOND_BLOCK_JACOBI && pc != IBEM_PRECOND_LEARNED && pc != IBEM_PRECOND_NEUMANN)
     return fail(IBEM_ERR_ARG, "mf_solve: preconditioner");
@@ -1369,6 +1374,8 @@ extern "C" ibem_status ibem_e3d_batch_dense_solve(const ibem_e3d_batch* batch, i
   }
   if (form != IBEM_SOLVE_FP64 && form != IBEM_SOLVE_MIXED_IR && form != IBEM_SOLVE_GMRES_BJ)
     return fail(IBEM_ERR_ARG, "batch_dense_solve: unknown solver form");
+  if (batch->axes_dev && (layout != 24 || !batch->quats_dev))
+    return fail(IBEM_ERR_ARG, "batch_dense_solve: ellipsoids take layout 24 and need quaternions");
   cudaStream_t st = as_stream(stream);
   // Workers: each owns a stream, the largest realisation's N x N matrix and (block-Jacobi
   // form) its FP32 copy, and takes the next unsolved realisation until none is left.  The
@@ -1419,8 +1426,11 @@ extern "C" ibem_status ibem_e3d_batch_dense_solve(const ibem_e3d_batch* batch, i
       const int64_t N = (int64_t)nu * n, off = (int64_t)nu * p0;
       ibem_solve_report rep{};
       if (n) {
-        s = ibem_e3d_pair_blocks(batch->centers_dev + 3 * (int64_t)p0, batch->radius_dev + p0, n, &batch->mats[i],
-                                 layout, A, N, 0, 0, ws);
+        s = batch->axes_dev
+                ? ibem_e3d_ell_pair_blocks(batch->centers_dev + 3 * (int64_t)p0, batch->axes_dev + 3 * (int64_t)p0,
+                                           batch->quats_dev + 4 * (int64_t)p0, n, &batch->mats[i], A, N, 0, 0, ws)
+                : ibem_e3d_pair_blocks(batch->centers_dev + 3 * (int64_t)p0, batch->radius_dev + p0, n,
+                                       &batch->mats[i], layout, A, N, 0, 0, ws);
         if (!s) s = solve_dense(form, N, A, N, b_dev + off, x_dev + off, tol, &rep, ws, nu, W);
       }
       if (reports) reports[i] = rep;
@@ -1457,6 +1467,7 @@ extern "C" ibem_status ibem_e3d_effective_modulus_layout(const ibem_e3d_batch* b
   const int nu = ibem_layout_size(layout);
   if (!batch || !x_dev || !volume || !sig_inf || !e_eff || nu < 0)
     return fail(IBEM_ERR_ARG, "effective_modulus: bad arguments");
+  if (batch->axes_dev && layout != 24) return fail(IBEM_ERR_ARG, "effective_modulus: ellipsoids take layout 24");
   cudaStream_t st = as_stream(stream);
   MfBatch b;
   ibem_status s = mf_batch_init(b, *batch, st);
@@ -1469,7 +1480,7 @@ extern "C" ibem_status ibem_e3d_effective_modulus_layout(const ibem_e3d_batch* b
     if (e != cudaSuccess) s = cuda_fail(e, "effective_modulus");
   }
   if (!s) {
-    ::ibem::count_launch(), k_vol_eigen<<<nblk(b.num), 256, 0, st>>>(b.num, nu, b.seg_of, b.rad, x_dev, acc);
+    ::ibem::count_launch(), k_vol_eigen<<<nblk(b.num), 256, 0, st>>>(b.num, nu, b.seg_of, b.rad, b.axes, x_dev, acc);
     cudaMemcpyAsync(h.data(), acc, sizeof(double) * 6 * S, cudaMemcpyDeviceToHost, st);
     const cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) s = cuda_fail(e, "effective_modulus");
@@ -1601,6 +1612,7 @@ extern "C" ibem_status ibem_e3d_run_host_mf(const ibem_material* mat, int num, c
 
 extern "C" ibem_status ibem_e3d_mf_tuning(const ibem_e3d_batch* batch, int* slices_fp32, int* slices_wide,
                                           void* stream) {
+  if (batch && batch->axes_dev) return fail(IBEM_ERR_ARG, "matrix-free products and the learned preconditioner take spheres; solve ellipsoid batches with ibem_e3d_batch_dense_solve");
   if (!batch || !slices_fp32 || !slices_wide) return fail(IBEM_ERR_ARG, "mf_tuning: bad arguments");
   cudaStream_t st = as_stream(stream);
   MfBatch b;

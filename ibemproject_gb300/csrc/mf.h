@@ -51,6 +51,7 @@ struct MfBatch {
   int* seg_of = nullptr;      // num
   const double* cen = nullptr;  // caller's, num x 3
   const double* rad = nullptr;  // caller's, num
+  const double* axes = nullptr; // caller's, num x 3 (ellipsoids), or nullptr (spheres)
   float4* gh = nullptr;       // centre (high float parts), radius
   float4* gl = nullptr;       // centre (low float parts), 1 / radius
   SphMat* matd = nullptr;     // per segment, physical units

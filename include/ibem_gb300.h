@@ -208,13 +208,18 @@ ibem_status ibem_e3d_solve_noalloc(int64_t N, const double* A_dev, int64_t lda, 
  * only with each other; unknowns of particle p are entries 24p .. 24p+23 of b and x (the
  * layout-24 order of a single-realisation system).  No reference counterpart: the
  * reference solves one microstructure per run (systemSolverElastic3D.h:44-60) with
- * the matrix stored. */
+ * the matrix stored.  A batch of ellipsoids (axes_dev and quats_dev set, radius_dev their
+ * longest semi-axes) is solved by ibem_e3d_batch_dense_solve with layout 24 (the
+ * matrix-free products take spheres only); ibem_e3d_effective_modulus* uses the ellipsoid
+ * volumes. */
 typedef struct {
   int nseg;
   const int* seg_begin;          /* host, nseg + 1 offsets, seg_begin[0] = 0 */
   const double* centers_dev;     /* seg_begin[nseg] x 3, row-major */
   const double* radius_dev;      /* seg_begin[nseg] */
   const ibem_material* mats;     /* host, one per realisation */
+  const double* axes_dev;        /* ellipsoids: seg_begin[nseg] x 3 semi-axes, or NULL (spheres) */
+  const double* quats_dev;       /* ellipsoids: seg_begin[nseg] x 4 unit quaternions (w, x, y, z) */
 } ibem_e3d_batch;
 
 typedef enum {

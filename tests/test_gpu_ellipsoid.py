@@ -184,3 +184,35 @@ def test_ellipsoid_entry_points_check_arguments(g):
         g.IBEM_ERR_ARG
     assert g.lib().ibem_e3d_ell_field(7, None, 1, None, None, None, 0, ctypes.byref(m), None, None, None, None) == \
         g.IBEM_ERR_ARG
+
+
+@pytest.mark.parametrize("form", ["bj", "mixed"])
+def test_ellipsoid_batches_dense_solve_and_effective_modulus(g, form):
+    """A ragged batch of ellipsoid realisations (different materials) through
+    ibem_e3d_batch_dense_solve (block-Jacobi GMRES and the mixed LU form) against the plain
+    FP64 pipeline of each realisation, and the effective moduli against their definition:
+    <e> = C0^-1 : sigma + sum_p (V_p / V) E_p, V_p = 4/3 pi a1 a2 a3."""
+    from ibemproject_gb300 import batch as B
+    from ibemproject_gb300 import cases
+    cs = [cases.ellipsoid_case(n, vf=v, seed=20 + n, E1=70e9 * c, method="mc")
+          for n, v, c in ((7, 0.2, 3.0), (40, 0.27, 12.0), (1, 0.05, 5.7))]
+    bt = B.DeviceBatch(cs)
+    assert bt.ellipsoids
+    sig = np.array([0, 0, 0, 0, 0, 1.0])
+    b = B.farfield_rhs(bt, sig)
+    f = g.SOLVE_GMRES_BJ if form == "bj" else g.SOLVE_MIXED_IR
+    x, reps = B.dense_batch_solve(bt, b, f, tol=1e-12)
+    vols = np.array([float(c.title.split("=")[1]) ** 3 for c in cs])
+    e_eff, eps = B.effective_modulus(bt, x, sig, volume=vols)
+    x = x.cpu().numpy()
+    for s, c in enumerate(cs):
+        rows = bt.seg_rows(s)
+        xd, _, _ = g.run_host_ell(c, form=g.SOLVE_FP64)
+        assert scaled_err(x[rows], xd) < 1e-8
+        E = xd.reshape(-1, 24)[:, :6]
+        vp = 4 / 3 * np.pi * c.axes.prod(axis=1)
+        mean_star = (vp[:, None] * E).sum(axis=0) / vols[s]
+        e33 = sig[5] / c.E0 + mean_star[5]   # remote strain of sigma33 alone: sigma33 / E0
+        assert abs(e_eff[s] - sig[5] / e33) <= 1e-9 * abs(e_eff[s])
+    with pytest.raises(ValueError):
+        B.solve(bt, b)
