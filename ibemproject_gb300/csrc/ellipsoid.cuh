@@ -36,10 +36,43 @@
 #pragma once
 #include <math.h>
 
-#include "gen_sphere_common.cuh"
+#include "gen_sphere_common.cuh"   // first: it defines IBEM_HD and IBEM_INLINE
+#include "dfnum.cuh"
 
 namespace ibem {
 namespace ell {
+
+// ------------------------------------------------------------------ number types
+// The evaluator runs in double, float or double-float (DF: ~48 bits on the FP32 pipe, which
+// GB300 runs at 64x its FP64 rate).  Scalar functions and the unit roundoff by type:
+IBEM_HD inline double vsqrt(double x) { return sqrt(x); }
+IBEM_HD inline float vsqrt(float x) { return sqrtf(x); }
+IBEM_HD inline DF vsqrt(DF x) { return x * rsqrt_t(x); }
+IBEM_HD inline double vfabs(double x) { return fabs(x); }
+IBEM_HD inline float vfabs(float x) { return fabsf(x); }
+IBEM_HD inline DF vfabs(DF x) { return x.v.hi < 0.0f ? -x : x; }
+template <typename T>
+IBEM_HD inline T vfmax(T a, T b) { return a > b ? a : b; }
+IBEM_HD inline double jval(double x) { return x; }
+IBEM_HD inline double jval(float x) { return (double)x; }
+IBEM_HD inline double jval(DF x) { return df_value(x); }
+template <typename T>
+struct NumTraits;
+template <>
+struct NumTraits<double> {
+  static constexpr double eps = 1.1102230246251565e-16;
+  static constexpr double carlson_q = 379.82022430228585;   // (3 eps)^(-1/6)
+};
+template <>
+struct NumTraits<float> {
+  static constexpr double eps = 5.9604645e-08;
+  static constexpr double carlson_q = 13.322930834122156;
+};
+template <>
+struct NumTraits<DF> {
+  static constexpr double eps = 5.7e-14;                    // ~2^-44
+  static constexpr double carlson_q = 125.0;                // (3 eps)^(-1/6)
+};
 
 // ------------------------------------------------------------------ jets
 // Monomials h1^a h2^b h3^c of total degree d <= K in graded order; inside one degree a
@@ -219,7 +252,7 @@ template <typename T, int K>
 IBEM_HD IBEM_INLINE void jpow(const Jet<T, K>& a, int twice_q, Jet<T, K>& o) {
   T f[K + 1];
   const T a0 = a.c[0], ia = T(1) / a0, q = T(twice_q) / T(2);
-  f[0] = twice_q == 1 ? sqrt(a0) : (twice_q == -1 ? T(1) / sqrt(a0) : ia);
+  f[0] = twice_q == 1 ? vsqrt(a0) : (twice_q == -1 ? T(1) / vsqrt(a0) : ia);
 #pragma unroll
   for (int n = 1; n <= K; ++n) f[n] = f[n - 1] * (q - T(n - 1)) / T(n) * ia;
   jcompose(a, f, o);
@@ -247,13 +280,16 @@ IBEM_HD inline void carlson_ik(const T x[3], T* ik) {
   for (int i = 0; i < J::N; ++i) A0.c[i] = (X[0].c[i] + X[1].c[i] + X[2].c[i]) / T(3);
   A = A0;
   // iteration count from the values (Carlson 1995, eq. 2.2-2.4 with r the unit roundoff)
-  // (3 r)^(-1/6)
-  const T Qv = (sizeof(T) == sizeof(double) ? T(379.82022430228585) : T(13.322930834122156)) *
-               fmax(fabs(A0.c[0] - x[0]), fmax(fabs(A0.c[0] - x[1]), fabs(A0.c[0] - x[2])));
+  // (3 r)^(-1/6) max |A0 - x_m|
+  const T Qv = T(NumTraits<T>::carlson_q) *
+               vfmax(vfabs(A0.c[0] - x[0]), vfmax(vfabs(A0.c[0] - x[1]), vfabs(A0.c[0] - x[2])));
   T pow4 = T(1);
   J s[3], lam, t;
 #pragma unroll 1
-  for (int it = 0; it < 40 && pow4 * Qv >= fabs(A.c[0]); ++it) {
+  // Carlson's criterion bounds the error of the value; the third parameter derivatives are
+  // 4^-3 smaller per unit of deviation, so the loop runs until the criterion holds with a
+  // margin of 4^3 (three more halvings of the relative spread's square root)
+  for (int it = 0; it < 40 && T(64.0) * pow4 * Qv >= vfabs(A.c[0]); ++it) {
 #pragma unroll 1
     for (int m = 0; m < 3; ++m) jpow(X[m], 1, s[m]);
     jmul(s[0], s[1], lam);
@@ -320,8 +356,8 @@ IBEM_HD inline T ell_lambda(const T y[3], const T a2[3]) {
   const T q = y[0] * y[0] / a2[0] + y[1] * y[1] / a2[1] + y[2] * y[2] / a2[2];
   if (q <= T(1)) return T(0);
   const T r2 = y[0] * y[0] + y[1] * y[1] + y[2] * y[2];
-  const T amax = fmax(a2[0], fmax(a2[1], a2[2]));
-  T lam = fmax(T(0), r2 - amax);
+  const T amax = vfmax(a2[0], vfmax(a2[1], a2[2]));
+  T lam = vfmax(T(0), r2 - amax);
 #pragma unroll 1
   for (int it = 0; it < 100; ++it) {
     T f = T(-1), df = T(0);
@@ -333,8 +369,7 @@ IBEM_HD inline T ell_lambda(const T y[3], const T a2[3]) {
     }
     const T step = -f / df;
     lam += step;
-    if (!(step > T(4) * (sizeof(T) == sizeof(double) ? T(1.1102230246251565e-16) : T(5.9604645e-08)) * lam))
-      break;
+    if (!(step > T(4.0 * NumTraits<T>::eps) * lam)) break;
   }
   return lam;
 }
@@ -438,7 +473,7 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
 #pragma unroll
   for (int m = 0; m < 3; ++m) {
     ix[m] = T(1) / x[m];
-    rx[m] = sqrt(ix[m]);
+    rx[m] = vsqrt(ix[m]);
   }
   J I[20];
 #pragma unroll 1
@@ -586,12 +621,12 @@ struct EllDer {
 
 IBEM_HD IBEM_INLINE int fact_small(int n) { return n <= 1 ? 1 : (n == 2 ? 2 : (n == 3 ? 6 : (n == 4 ? 24 : 120))); }
 
-template <typename T, int K>
-IBEM_HD inline void ell_derivs(const EllPot<T, K>& P, EllDer<T, K>& D) {
+template <typename J, int K, typename T>
+IBEM_HD inline void ell_derivs(const EllPot<J, K>& P, EllDer<T, K>& D) {
   D.inside = P.inside;
 #pragma unroll 1
   for (int r = 0; r < 4; ++r) {
-    const Jet<T, K>& f = r == 0 ? P.f0 : P.f1[r - 1];
+    const Jet<J, K>& f = r == 0 ? P.f0 : P.f1[r - 1];
 #pragma unroll 1
     for (int a1 = 0; a1 <= K; ++a1)
 #pragma unroll 1
@@ -599,7 +634,7 @@ IBEM_HD inline void ell_derivs(const EllPot<T, K>& P, EllDer<T, K>& D) {
 #pragma unroll 1
         for (int a3 = 0; a3 <= K - a1 - a2; ++a3) {
           const int id = midx(a1, a2, a3);
-          D.phi[r][id] = T(fact_small(a1) * fact_small(a2) * fact_small(a3)) * f.c[id];
+          D.phi[r][id] = T(fact_small(a1) * fact_small(a2) * fact_small(a3)) * T(jval(f.c[id]));
         }
 #pragma unroll 1
     for (int b1 = 0; b1 <= K + 1; ++b1)
@@ -611,12 +646,12 @@ IBEM_HD inline void ell_derivs(const EllPot<T, K>& P, EllDer<T, K>& D) {
           if (deg < 4) continue;
           const int k = b1 > 0 ? 0 : (b2 > 0 ? 1 : 2);
           const int a[3] = {b1 - (k == 0), b2 - (k == 1), b3 - (k == 2)};
-          const Jet<T, K>& g = r == 0 ? P.f1[k] : P.f2[sym_pair(r - 1, k)];
+          const Jet<J, K>& g = r == 0 ? P.f1[k] : P.f2[sym_pair(r - 1, k)];
           const int ia = midx(a[0], a[1], a[2]);
           const T af = T(fact_small(a[0]) * fact_small(a[1]) * fact_small(a[2]));
-          T v = P.d[k] * f.c[ia] - g.c[ia];
+          J v = P.d[k] * f.c[ia] - g.c[ia];
           if (a[k] > 0) v += f.c[midx(a[0] - (k == 0), a[1] - (k == 1), a[2] - (k == 2))];
-          D.psi[r][midx(b1, b2, b3)] = af * v;
+          D.psi[r][midx(b1, b2, b3)] = af * T(jval(v));
         }
   }
 }
@@ -661,12 +696,25 @@ IBEM_HD constexpr int pair_j(int t) { return t < 3 ? t : (t < 5 ? t - 2 : 2); }
 // columns (h, mn[,p]):
 //   map[m][n] (-sum_kl (C0 - C1)_ijkl D(k,l,m,n[,p]; [r]) + [self] C0_ijmn delta),
 // d = centre of s - centre of h.  out[row * 24 + col].
-template <typename T>
+// J: the type of the jets (the FP64 pipe's double, or DF on the FP32 pipe; the tables and
+// the block are formed in T).  The evaluation runs in coordinates scaled by the source's
+// longest semi-axis s, where every quantity is O(1); the tensor is scale-free except for one
+// factor s per column of order 1 and 1/s per row of order 1.
+template <typename T, typename J = T>
 IBEM_HD inline void ell_block24(const T d[3], const T Q[9], const T a[3], const SphMat& mc, bool self, T* out) {
+  const T sc = vfmax(a[0], vfmax(a[1], a[2])), isc = T(1) / sc;
   EllDer<T, 4> P;
   {
-    EllPot<T, 4> pot;
-    ell_potentials<T, 4>(d, Q, a, pot);
+    J dj[3], aj[3], Qj[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      dj[i] = J(d[i] * isc);
+      aj[i] = J(a[i] * isc);
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Qj[i] = J(Q[i]);
+    EllPot<J, 4> pot;
+    ell_potentials<J, 4>(dj, Qj, aj, pot);
     ell_derivs(pot, P);
   }
   const T nu = T(mc.tn2) / T(2);
@@ -700,7 +748,7 @@ IBEM_HD inline void ell_block24(const T d[3], const T Q[9], const T a[3], const 
       // sum_kl (C0 - C1)_ijkl D_kl = dlam d_ij D_kk + 2 dmu D_ij
       T acc = T(2) * T(mc.dmu) * Dt[r][rho][rt][ct];
       if (i == j) acc += T(mc.dlam) * (Dt[r][rho][0][ct] + Dt[r][rho][3][ct] + Dt[r][rho][5][ct]);
-      T v = -kd * acc;
+      T v = -kd * acc * (co == ro ? T(1) : (co ? sc : isc));
       if (self && ro == co && (ro == 0 || r == rho)) {
         // C0_ijmn
         T c0 = T(mc.mu0) * (T((i == m) * (j == n)) + T((i == n) * (j == m)));
@@ -715,12 +763,23 @@ IBEM_HD inline void ell_block24(const T d[3], const T Q[9], const T a[3], const 
 // Strain (6: xx xy xz yy yz zz) at c + d due to the layout-24 eigenstrain E of an
 // ellipsoidal source (postProcessorElastic3D.cpp:367-470 with the ellipsoid's potentials),
 // accumulated into e.  Returns true if the point lies inside (or on) the ellipsoid.
-template <typename T>
+// J: the jets' type (see ell_block24); coordinates scaled by the longest semi-axis s, the
+// order-1 coefficients (of x'_p) carry the factor s back.
+template <typename T, typename J = T>
 IBEM_HD inline bool ell_strain24(const T d[3], const T Q[9], const T a[3], const SphMat& mc, const T* E, T* e) {
+  const T sc = vfmax(a[0], vfmax(a[1], a[2])), isc = T(1) / sc;
   EllDer<T, 3> P;
   {
-    EllPot<T, 3> pot;
-    ell_potentials<T, 3>(d, Q, a, pot);
+    J dj[3], aj[3], Qj[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      dj[i] = J(d[i] * isc);
+      aj[i] = J(a[i] * isc);
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Qj[i] = J(Q[i]);
+    EllPot<J, 3> pot;
+    ell_potentials<J, 3>(dj, Qj, aj, pot);
     ell_derivs(pot, P);
   }
   const T nu = T(mc.tn2) / T(2);
@@ -733,7 +792,7 @@ IBEM_HD inline bool ell_strain24(const T d[3], const T Q[9], const T a[3], const
       const int ct = co ? (cc - 6) / 3 : cc;
       const int rho = co ? (cc - 6) % 3 : -1;
       const int m = pair_i(ct), n = pair_j(ct);
-      s += (m == n ? T(1) : T(2)) * Dsum(P, nu, rho, i, j, m, n, nullptr, 0) * E[cc];
+      s += (m == n ? T(1) : T(2)) * Dsum(P, nu, rho, i, j, m, n, nullptr, 0) * (co ? sc * E[cc] : E[cc]);
     }
     e[rt] += kd * s;
   }

@@ -197,7 +197,11 @@ def test_adamw_matches_oracle(B):
 
 
 def test_learned_preconditioner_beats_block_jacobi(B):
-    """Train on 8 microstructures, then solve 3 held-out ones with both preconditioners."""
+    """Train on 8 microstructures, then solve 3 held-out ones with block-Jacobi (the
+    untrained network), the learned weights and the analytic Neumann weights (all 1).  The
+    network must cut block-Jacobi's Arnoldi steps by 20% and stay within 10% of Neumann's
+    (with two weights per edge on fixed Neumann blocks it reaches Neumann's step count; it
+    does not beat it -- measured 32 vs 33 held out)."""
     import torch
     train_cs = small_cases([90, 120, 100, 80, 110, 95, 130, 85], seed=100, vf=0.2)
     bt = B.DeviceBatch(train_cs)
@@ -215,6 +219,9 @@ def test_learned_preconditioner_beats_block_jacobi(B):
     print(f"training loss {hist[0]:.4f} -> {hist[-1]:.4f}; Arnoldi steps: block-Jacobi {it0}, "
           f"learned {it1}, Neumann weights 1 {it2}")
     assert it1 < 0.8 * it0, (it0, it1)
+    # against the method without the network's weights (every weight 1: the analytic
+    # Neumann terms): the trained network must do at least as well, within 10%
+    assert it1 <= 1.1 * it2, (it1, it2)
     x0, x1 = x0.cpu().numpy(), x1.cpu().numpy()
     for s, c in enumerate(test_cs):
         rows = tb.seg_rows(s)
