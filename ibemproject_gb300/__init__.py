@@ -114,8 +114,6 @@ SIGNATURES = {
                                  ctypes.POINTER(SolveReport)]),
     "ibem_e3d_run_dir": (_int, [ctypes.c_char_p, _int, _int, _dbl, ctypes.POINTER(SolveReport)]),
     "ibem_e3d_ell_pair_blocks": (_int, [_vp, _vp, _vp, _int, ctypes.POINTER(Material), _vp, _i64, _i64, _i64, _vp]),
-    "ibem_e3d_ell_pair_blocks_form": (_int, [_int, _vp, _vp, _vp, _int, ctypes.POINTER(Material), _vp, _i64, _i64,
-                                             _i64, _vp]),
     "ibem_e3d_ell_field": (_int, [_int, _vp, _int, _vp, _vp, _vp, _int, ctypes.POINTER(Material), _vp, _c_dp, _vp,
                                   _vp]),
     "ibem_e3d_run_host_ell": (_int, [_int, ctypes.POINTER(Material), _int, _c_dp, _c_dp, _c_dp, _int, _c_dp, _c_dp,

@@ -37,25 +37,4 @@ IBEM_HD inline DF rsqrt_t(DF x) {
 
 IBEM_HD inline double df_value(DF a) { return (double)a.v.hi + (double)a.v.lo; }
 
-IBEM_HD inline bool operator<(DF a, DF b) { return b > a; }
-IBEM_HD inline bool operator<=(DF a, DF b) { return !(a > b); }
-IBEM_HD inline bool operator>=(DF a, DF b) { return !(b > a); }
-
-// 1 / x: FP32 estimate and one double-float Newton step (relative error ~2^-44)
-IBEM_HD inline DF recip_t(DF x) {
-  const float y0 = 1.0f / x.v.hi;
-  const dfloat yd{y0, 0.0f};
-  const dfloat t = dfloat{1.0f, 0.0f} - x.v * yd;
-  return DF(yd + yd * t);
-}
-IBEM_HD inline DF operator/(DF a, DF b) { return a * recip_t(b); }
-IBEM_HD inline DF& operator-=(DF& a, DF b) {
-  a.v = a.v - b.v;
-  return a;
-}
-IBEM_HD inline DF& operator*=(DF& a, DF b) {
-  a.v = a.v * b.v;
-  return a;
-}
-
 }  // namespace ibem

@@ -12,15 +12,12 @@
 //   block in FP64 (the FP64 pipe bounds the kernel); the warp then writes the blocks one
 //   column at a time through shared memory, so that every store instruction covers
 //   consecutive rows (the 32 blocks of a warp are 768 consecutive rows of each column).
-// The FP64 pipe is GB300's scarce unit (1/64 of the FP32 rate): the mixed and block-Jacobi
-//   forms assemble with double-float jets (~48-bit arithmetic on the FP32 pipe, entries
-//   within 1e-11 of the FP64 ones), the plain FP64 form with FP64 jets.
 // stress sums: one thread per sample point and source slice (blockIdx.y; enough slices
 //   to fill the GPU when there are few points), sources staged through shared memory in
 //   chunks; the mixed form evaluates a source in FP32 (coordinates scaled by its longest
 //   semi-axis) when it lies beyond kEllFarAxes of those axes from all 32 points of the
-//   warp and in double-float otherwise, the FP64 form in FP64.  The slices' partial sums are added in slice order by a
-//   second kernel (no atomics: the same stresses on every run).
+//   warp and in FP64 otherwise, the FP64 form in FP64 throughout.  The slices' partial sums
+//   are added in slice order by a second kernel (no atomics: the same stresses on every run).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -44,7 +41,6 @@ __global__ void k_ell_rot(int num, const double* __restrict__ quat, double* __re
   if (h < num) ell::quat_to_rot(quat + 4 * (int64_t)h, Q + 9 * (int64_t)h);
 }
 
-template <typename J>
 __global__ void __launch_bounds__(kEllPairThreads) k_ell_pair24(const double* __restrict__ cen,
                                                                 const double* __restrict__ axes,
                                                                 const double* __restrict__ Qall, int num, SphMat mc,
@@ -67,7 +63,7 @@ __global__ void __launch_bounds__(kEllPairThreads) k_ell_pair24(const double* __
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) Q[i] = Qall[9 * (int64_t)h + i];
-    ell::ell_block24<double, J>(d, Q, a, mc, s == h, blk);
+    ell::ell_block24<double>(d, Q, a, mc, s == h, blk);
   }
   double* base = A + 24 * (int64_t)h * lda + 24 * (int64_t)s0;
   for (int c = 0; c < 24; ++c) {
@@ -144,10 +140,7 @@ __global__ void __launch_bounds__(kEllFieldThreads) k_ell_field24(const double* 
           for (int i = 0; i < 6; ++i) e[i] += (double)ef[i];
         }
       } else if (act) {
-        // near: FP64 jets, or double-float jets in the mixed form
-        const bool in = mixed ? ell::ell_strain24<double, DF>(d, r.Q, r.a, mc, r.E, e)
-                              : ell::ell_strain24<double>(d, r.Q, r.a, mc, r.E, e);
-        if (in) inside = h0 + hh;
+        if (ell::ell_strain24<double>(d, r.Q, r.a, mc, r.E, e)) inside = h0 + hh;
       }
     }
   }
@@ -223,15 +216,6 @@ extern "C" {
 ibem_status ibem_e3d_ell_pair_blocks(const double* centers_dev, const double* axes_dev, const double* quats_dev,
                                      int num, const ibem_material* mat, double* A_dev, int64_t lda, int64_t row0,
                                      int64_t col0, void* stream) {
-  return ibem_e3d_ell_pair_blocks_form(IBEM_SOLVE_FP64, centers_dev, axes_dev, quats_dev, num, mat, A_dev, lda, row0,
-                                       col0, stream);
-}
-
-ibem_status ibem_e3d_ell_pair_blocks_form(ibem_solver_form form, const double* centers_dev, const double* axes_dev,
-                                          const double* quats_dev, int num, const ibem_material* mat, double* A_dev,
-                                          int64_t lda, int64_t row0, int64_t col0, void* stream) {
-  if (form != IBEM_SOLVE_FP64 && form != IBEM_SOLVE_MIXED_IR && form != IBEM_SOLVE_GMRES_BJ)
-    return fail(IBEM_ERR_ARG, "ell_pair_blocks: unknown form");
   ibem_status s = check_geometry(centers_dev, axes_dev, quats_dev, num, "ell_pair_blocks");
   if (s) return s;
   if (!mat || (num && !A_dev) || row0 < 0 || col0 < 0) return fail(IBEM_ERR_ARG, "ell_pair_blocks: bad arguments");
@@ -245,12 +229,8 @@ ibem_status ibem_e3d_ell_pair_blocks_form(ibem_solver_form form, const double* c
     const SphMat mc = sph_mat_init(mat->E0, mat->nu0, mat->E1, mat->nu1);
     ProfScope ps(PROF_PAIR, st);
     dim3 grid((unsigned)((num + kEllPairThreads - 1) / kEllPairThreads), (unsigned)num);
-    if (form == IBEM_SOLVE_FP64)
-      ::ibem::count_launch(), k_ell_pair24<double><<<grid, kEllPairThreads, 0, st>>>(centers_dev, axes_dev, Q, num, mc,
-                                                                                     A_dev + col0 * lda + row0, lda);
-    else
-      ::ibem::count_launch(), k_ell_pair24<DF><<<grid, kEllPairThreads, 0, st>>>(centers_dev, axes_dev, Q, num, mc,
-                                                                                 A_dev + col0 * lda + row0, lda);
+    ::ibem::count_launch(), k_ell_pair24<<<grid, kEllPairThreads, 0, st>>>(centers_dev, axes_dev, Q, num, mc,
+                                                                           A_dev + col0 * lda + row0, lda);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) s = cuda_fail(e, "ell_pair_blocks");
   }
@@ -332,7 +312,7 @@ ibem_status ibem_e3d_run_host_ell(ibem_solver_form form, const ibem_material* ma
       e = cudaMemcpyAsync(p, points, sizeof(double) * 3 * nump, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) s = cuda_fail(e, "run_host_ell: upload");
   }
-  if (!s) s = ibem_e3d_ell_pair_blocks_form(form, c, a, q, num, mat, A, N, 0, 0, st);
+  if (!s) s = ibem_e3d_ell_pair_blocks(c, a, q, num, mat, A, N, 0, 0, st);
   if (!s) s = ibem_e3d_farfield_rhs(num, mat, 24, sig_inf, b, st);
   if (!s) s = solve_dense(form, N, A, N, b, x, tol, &rep, st);
   if (!s && nump) s = ibem_e3d_ell_field(form, p, nump, c, a, q, num, mat, x, sig_inf, S, st);

@@ -36,26 +36,19 @@
 #pragma once
 #include <math.h>
 
-#include "gen_sphere_common.cuh"   // first: it defines IBEM_HD and IBEM_INLINE
-#include "dfnum.cuh"
+#include "gen_sphere_common.cuh"
 
 namespace ibem {
 namespace ell {
 
 // ------------------------------------------------------------------ number types
-// The evaluator runs in double, float or double-float (DF: ~48 bits on the FP32 pipe, which
-// GB300 runs at 64x its FP64 rate).  Scalar functions and the unit roundoff by type:
+// The evaluator runs in double or float.  Scalar functions and the unit roundoff by type:
 IBEM_HD inline double vsqrt(double x) { return sqrt(x); }
 IBEM_HD inline float vsqrt(float x) { return sqrtf(x); }
-IBEM_HD inline DF vsqrt(DF x) { return x * rsqrt_t(x); }
 IBEM_HD inline double vfabs(double x) { return fabs(x); }
 IBEM_HD inline float vfabs(float x) { return fabsf(x); }
-IBEM_HD inline DF vfabs(DF x) { return x.v.hi < 0.0f ? -x : x; }
 template <typename T>
 IBEM_HD inline T vfmax(T a, T b) { return a > b ? a : b; }
-IBEM_HD inline double jval(double x) { return x; }
-IBEM_HD inline double jval(float x) { return (double)x; }
-IBEM_HD inline double jval(DF x) { return df_value(x); }
 template <typename T>
 struct NumTraits;
 template <>
@@ -67,11 +60,6 @@ template <>
 struct NumTraits<float> {
   static constexpr double eps = 5.9604645e-08;
   static constexpr double carlson_q = 13.322930834122156;
-};
-template <>
-struct NumTraits<DF> {
-  static constexpr double eps = 5.7e-14;                    // ~2^-44
-  static constexpr double carlson_q = 125.0;                // (3 eps)^(-1/6)
 };
 
 // ------------------------------------------------------------------ jets
@@ -621,12 +609,12 @@ struct EllDer {
 
 IBEM_HD IBEM_INLINE int fact_small(int n) { return n <= 1 ? 1 : (n == 2 ? 2 : (n == 3 ? 6 : (n == 4 ? 24 : 120))); }
 
-template <typename J, int K, typename T>
-IBEM_HD inline void ell_derivs(const EllPot<J, K>& P, EllDer<T, K>& D) {
+template <typename T, int K>
+IBEM_HD inline void ell_derivs(const EllPot<T, K>& P, EllDer<T, K>& D) {
   D.inside = P.inside;
 #pragma unroll 1
   for (int r = 0; r < 4; ++r) {
-    const Jet<J, K>& f = r == 0 ? P.f0 : P.f1[r - 1];
+    const Jet<T, K>& f = r == 0 ? P.f0 : P.f1[r - 1];
 #pragma unroll 1
     for (int a1 = 0; a1 <= K; ++a1)
 #pragma unroll 1
@@ -634,7 +622,7 @@ IBEM_HD inline void ell_derivs(const EllPot<J, K>& P, EllDer<T, K>& D) {
 #pragma unroll 1
         for (int a3 = 0; a3 <= K - a1 - a2; ++a3) {
           const int id = midx(a1, a2, a3);
-          D.phi[r][id] = T(fact_small(a1) * fact_small(a2) * fact_small(a3)) * T(jval(f.c[id]));
+          D.phi[r][id] = T(fact_small(a1) * fact_small(a2) * fact_small(a3)) * f.c[id];
         }
 #pragma unroll 1
     for (int b1 = 0; b1 <= K + 1; ++b1)
@@ -646,12 +634,12 @@ IBEM_HD inline void ell_derivs(const EllPot<J, K>& P, EllDer<T, K>& D) {
           if (deg < 4) continue;
           const int k = b1 > 0 ? 0 : (b2 > 0 ? 1 : 2);
           const int a[3] = {b1 - (k == 0), b2 - (k == 1), b3 - (k == 2)};
-          const Jet<J, K>& g = r == 0 ? P.f1[k] : P.f2[sym_pair(r - 1, k)];
+          const Jet<T, K>& g = r == 0 ? P.f1[k] : P.f2[sym_pair(r - 1, k)];
           const int ia = midx(a[0], a[1], a[2]);
           const T af = T(fact_small(a[0]) * fact_small(a[1]) * fact_small(a[2]));
-          J v = P.d[k] * f.c[ia] - g.c[ia];
+          T v = P.d[k] * f.c[ia] - g.c[ia];
           if (a[k] > 0) v += f.c[midx(a[0] - (k == 0), a[1] - (k == 1), a[2] - (k == 2))];
-          D.psi[r][midx(b1, b2, b3)] = af * T(jval(v));
+          D.psi[r][midx(b1, b2, b3)] = af * v;
         }
   }
 }
@@ -696,25 +684,22 @@ IBEM_HD constexpr int pair_j(int t) { return t < 3 ? t : (t < 5 ? t - 2 : 2); }
 // columns (h, mn[,p]):
 //   map[m][n] (-sum_kl (C0 - C1)_ijkl D(k,l,m,n[,p]; [r]) + [self] C0_ijmn delta),
 // d = centre of s - centre of h.  out[row * 24 + col].
-// J: the type of the jets (the FP64 pipe's double, or DF on the FP32 pipe; the tables and
-// the block are formed in T).  The evaluation runs in coordinates scaled by the source's
-// longest semi-axis s, where every quantity is O(1); the tensor is scale-free except for one
-// factor s per column of order 1 and 1/s per row of order 1.
-template <typename T, typename J = T>
+// The evaluation runs in coordinates scaled by the source's longest semi-axis s, where every
+// quantity is O(1); the tensor is scale-free except for one factor s per column of order 1
+// and 1/s per row of order 1.
+template <typename T>
 IBEM_HD inline void ell_block24(const T d[3], const T Q[9], const T a[3], const SphMat& mc, bool self, T* out) {
   const T sc = vfmax(a[0], vfmax(a[1], a[2])), isc = T(1) / sc;
   EllDer<T, 4> P;
   {
-    J dj[3], aj[3], Qj[9];
+    T ds[3], as[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      dj[i] = J(d[i] * isc);
-      aj[i] = J(a[i] * isc);
+      ds[i] = d[i] * isc;
+      as[i] = a[i] * isc;
     }
-#pragma unroll
-    for (int i = 0; i < 9; ++i) Qj[i] = J(Q[i]);
-    EllPot<J, 4> pot;
-    ell_potentials<J, 4>(dj, Qj, aj, pot);
+    EllPot<T, 4> pot;
+    ell_potentials<T, 4>(ds, Q, as, pot);
     ell_derivs(pot, P);
   }
   const T nu = T(mc.tn2) / T(2);
@@ -763,23 +748,21 @@ IBEM_HD inline void ell_block24(const T d[3], const T Q[9], const T a[3], const 
 // Strain (6: xx xy xz yy yz zz) at c + d due to the layout-24 eigenstrain E of an
 // ellipsoidal source (postProcessorElastic3D.cpp:367-470 with the ellipsoid's potentials),
 // accumulated into e.  Returns true if the point lies inside (or on) the ellipsoid.
-// J: the jets' type (see ell_block24); coordinates scaled by the longest semi-axis s, the
-// order-1 coefficients (of x'_p) carry the factor s back.
-template <typename T, typename J = T>
+// Coordinates scaled by the longest semi-axis s; the order-1 coefficients (of x'_p) carry
+// the factor s back.
+template <typename T>
 IBEM_HD inline bool ell_strain24(const T d[3], const T Q[9], const T a[3], const SphMat& mc, const T* E, T* e) {
   const T sc = vfmax(a[0], vfmax(a[1], a[2])), isc = T(1) / sc;
   EllDer<T, 3> P;
   {
-    J dj[3], aj[3], Qj[9];
+    T ds[3], as[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      dj[i] = J(d[i] * isc);
-      aj[i] = J(a[i] * isc);
+      ds[i] = d[i] * isc;
+      as[i] = a[i] * isc;
     }
-#pragma unroll
-    for (int i = 0; i < 9; ++i) Qj[i] = J(Q[i]);
-    EllPot<J, 3> pot;
-    ell_potentials<J, 3>(dj, Qj, aj, pot);
+    EllPot<T, 3> pot;
+    ell_potentials<T, 3>(ds, Q, as, pot);
     ell_derivs(pot, P);
   }
   const T nu = T(mc.tn2) / T(2);

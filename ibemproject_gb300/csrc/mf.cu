@@ -1427,9 +1427,8 @@ extern "C" ibem_status ibem_e3d_batch_dense_solve(const ibem_e3d_batch* batch, i
       ibem_solve_report rep{};
       if (n) {
         s = batch->axes_dev
-                ? ibem_e3d_ell_pair_blocks_form(form, batch->centers_dev + 3 * (int64_t)p0,
-                                                batch->axes_dev + 3 * (int64_t)p0, batch->quats_dev + 4 * (int64_t)p0,
-                                                n, &batch->mats[i], A, N, 0, 0, ws)
+                ? ibem_e3d_ell_pair_blocks(batch->centers_dev + 3 * (int64_t)p0, batch->axes_dev + 3 * (int64_t)p0,
+                                           batch->quats_dev + 4 * (int64_t)p0, n, &batch->mats[i], A, N, 0, 0, ws)
                 : ibem_e3d_pair_blocks(batch->centers_dev + 3 * (int64_t)p0, batch->radius_dev + p0, n,
                                        &batch->mats[i], layout, A, N, 0, 0, ws);
         if (!s) s = solve_dense(form, N, A, N, b_dev + off, x_dev + off, tol, &rep, ws, nu, W);

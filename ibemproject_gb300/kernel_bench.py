@@ -28,7 +28,7 @@
 --assemble NUM,LAYOUT  the pair blocks (ibem_e3d_pair_blocks, FP64) of NUM spheres in
                layout 24, 60 or 78: achieved write bandwidth of the N^2 matrix.
 --field-far NUM,G  the same with the grid moved far from every sphere (FP32 path only).
---ell NUM,G    ellipsoid pair blocks (FP64 and double-float) and stress sums (FP64 and mixed) of NUM
+--ell NUM,G    ellipsoid pair blocks (FP64) and stress sums (FP64 and mixed) of NUM
                ellipsoids (a1 0.008, a2 a1 U[0.5,1], a3 a1 U[0.25,1], vf 15%) at G^3 points.
 --mf NUM       the matrix-free products (ibem_e3d_mf_matvec: FP32, double-float, FP64) on a
                far-field microstructure of NUM spheres (bench distribution): NUM^2 pair
@@ -268,8 +268,6 @@ def bench_ell(num, grid, reps, dev):
 
     out["pair_blocks_ms"] = timed(lambda: check(L.ibem_e3d_ell_pair_blocks(_p(cen), _p(ax), _p(qt), num,
                                                                             ctypes.byref(m), _p(A), N, 0, 0, None)))
-    out["pair_blocks_double_float_ms"] = timed(lambda: check(L.ibem_e3d_ell_pair_blocks_form(
-        SOLVE_MIXED_IR, _p(cen), _p(ax), _p(qt), num, ctypes.byref(m), _p(A), N, 0, 0, None)))
     for name, form in (("field_fp64_ms", SOLVE_FP64), ("field_mixed_ms", SOLVE_MIXED_IR)):
         if c.nump:
             out[name] = timed(lambda: check(L.ibem_e3d_ell_field(form, _p(pts), c.nump, _p(cen), _p(ax), _p(qt), num,

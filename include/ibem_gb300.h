@@ -512,19 +512,11 @@ ibem_status ibem_e3d_ell_pair_blocks(const double* centers_dev, const double* ax
                                      int num, const ibem_material* mat, double* A_dev, int64_t lda, int64_t row0,
                                      int64_t col0, void* stream);
 
-/* The same blocks for a solver form: IBEM_SOLVE_FP64 as above; IBEM_SOLVE_MIXED_IR and
- * IBEM_SOLVE_GMRES_BJ with the derivative series in double-float arithmetic (~48 bits on
- * the FP32 pipe, several times faster on GB300; entries within 1e-11 of the FP64 ones,
- * below what those forms' FP64 refinement resolves). */
-ibem_status ibem_e3d_ell_pair_blocks_form(ibem_solver_form form, const double* centers_dev, const double* axes_dev,
-                                          const double* quats_dev, int num, const ibem_material* mat, double* A_dev,
-                                          int64_t lda, int64_t row0, int64_t col0, void* stream);
-
 /* Stresses at sample points under the remote stress sig_inf (host, 6) from the layout-24
  * eigenstrain E_dev (postProcessorElastic3D.cpp:367-522 with ellipsoids): stress_dev is
  * overwritten (nump x 6, xx xy xz yy yz zz).  form IBEM_SOLVE_FP64: FP64 throughout;
  * IBEM_SOLVE_MIXED_IR: an ellipsoid farther than 14 of its longest semi-axes from all 32
- * points of a warp is evaluated in FP32, the others in double-float. */
+ * points of a warp is evaluated in FP32, the others in FP64. */
 ibem_status ibem_e3d_ell_field(ibem_solver_form form, const double* points_dev, int nump, const double* centers_dev,
                                const double* axes_dev, const double* quats_dev, int num, const ibem_material* mat,
                                const double* E_dev, const double* sig_inf, double* stress_dev, void* stream);

@@ -79,21 +79,3 @@ extern "C" int he_D(int order, int nder, const double* d, const double* quat, co
 }
 
 extern "C" void he_rot(const double* quat, double* Q) { quat_to_rot(quat, Q); }
-
-// the block with double-float jets (the mixed and block-Jacobi forms' assembly)
-extern "C" int he_block24_df(const double* d, const double* quat, const double* a, double E0, double nu0,
-                             double E1, double nu1, int self, double* out) {
-  double Q[9];
-  quat_to_rot(quat, Q);
-  SphMat mc = sph_mat_init(E0, nu0, E1, nu1);
-  ell_block24<double, ibem::DF>(d, Q, a, mc, self != 0, out);
-  return 0;
-}
-
-extern "C" int he_strain24_df(const double* d, const double* quat, const double* a, double E0, double nu0,
-                              double E1, double nu1, const double* E, double* e) {
-  double Q[9];
-  quat_to_rot(quat, Q);
-  SphMat mc = sph_mat_init(E0, nu0, E1, nu1);
-  return ell_strain24<double, ibem::DF>(d, Q, a, mc, E, e) ? 1 : 0;
-}

@@ -211,34 +211,3 @@ def test_single_precision_blocks(he):
     he.he_block24(*args[:-1], 0, d(o64))
     he.he_block24_f32(*args[:-1], 0, d(o32))
     assert scaled_err(o32, o64) < 1e-5
-
-
-def test_double_float_jets_match_fp64(he):
-    """The double-float instantiation of the jets (the assembly and near-field sums of the
-    mixed and block-Jacobi forms, on the FP32 pipe) against FP64: every order sub-block of
-    the pair block within 1e-11 of its largest entry, strains within 1e-11, from the centre
-    of the source to 25 longest semi-axes away, random shapes and orientations."""
-    rng = np.random.default_rng(0)
-    worst_b = worst_e = 0.0
-    for t in range(60):
-        a = np.array([0.008, 0.008 * rng.uniform(0.5, 1), 0.008 * rng.uniform(0.25, 1)])
-        q = rng.normal(size=4)
-        x = rng.normal(size=3)
-        x = x / np.linalg.norm(x) * 0.008 * (0.0 if t % 10 == 0 else rng.uniform(0.2, 25.0))
-        o64, odf = np.zeros(576), np.zeros(576)
-        args = (d(x), d(q), d(a), *[ctypes.c_double(v) for v in MAT], int(t % 10 == 0))
-        he.he_block24(*args, d(o64))
-        he.he_block24_df(*args, d(odf))
-        B64, Bdf = o64.reshape(24, 24), odf.reshape(24, 24)
-        for rs in (slice(0, 6), slice(6, 24)):
-            for cs in (slice(0, 6), slice(6, 24)):
-                m = np.abs(B64[rs, cs]).max()
-                if m > 0:
-                    worst_b = max(worst_b, np.abs(Bdf[rs, cs] - B64[rs, cs]).max() / m)
-        E = rng.normal(size=24)
-        E[6:] /= 0.008
-        e64, edf = np.zeros(6), np.zeros(6)
-        he.he_strain24(d(x), d(q), d(a), *[ctypes.c_double(v) for v in MAT], d(E), d(e64))
-        he.he_strain24_df(d(x), d(q), d(a), *[ctypes.c_double(v) for v in MAT], d(E), d(edf))
-        worst_e = max(worst_e, np.abs(edf - e64).max() / np.abs(e64).max())
-    assert worst_b < 1e-11 and worst_e < 1e-11, (worst_b, worst_e)

@@ -78,30 +78,6 @@ def test_pair_blocks_match_host_evaluator(g, he):
         assert scaled_err(got, want) < 1e-12, (s, h)
 
 
-def test_double_float_blocks_match_fp64_blocks(g):
-    """ibem_e3d_ell_pair_blocks_form with the mixed form (double-float jets) against the FP64
-    blocks, every order sub-block within 1e-11 of its largest entry."""
-    from ibemproject_gb300 import cases
-    c = cases.ellipsoid_case(45, vf=0.1, seed=13)
-    A64 = ell_matrix(g, c)
-    N = 24 * c.num
-    At = torch.zeros((N, N), dtype=torch.float64, device="cuda")
-    m = g.material(c.E0, c.nu0, c.E1, c.nu1)
-    cen, ax, qt = dev(c.centers), dev(c.axes), dev(c.quats)
-    g.check(g.lib().ibem_e3d_ell_pair_blocks_form(g.SOLVE_MIXED_IR, P(cen), P(ax), P(qt), c.num, ctypes.byref(m),
-                                                  P(At), N, 0, 0, None))
-    torch.cuda.synchronize()
-    Adf = At.cpu().numpy().T
-    for s in range(c.num):
-        for h in range(c.num):
-            for r0, r1 in ((0, 6), (6, 24)):
-                for c0, c1 in ((0, 6), (6, 24)):
-                    blk = A64[24 * s + r0:24 * s + r1, 24 * h + c0:24 * h + c1]
-                    got = Adf[24 * s + r0:24 * s + r1, 24 * h + c0:24 * h + c1]
-                    if np.abs(blk).max() > 0:
-                        assert scaled_err(got, blk) < 1e-11, (s, h)
-
-
 def test_sphere_limit_matches_sphere_blocks(g):
     from ibemproject_gb300 import cases
     c = cases.farfield_case(num=30, r0=0.05, vf=0.12, grid=0, seed=9)
