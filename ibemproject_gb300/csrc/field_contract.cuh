@@ -156,14 +156,52 @@ IBEM_HD inline SphDF sph_df_make(const double* cen, double a, const double* Eu) 
   return s;
 }
 
-// e[6] += strain / c at the point (px, py, pz) (double-float, point already converted);
-// returns whether the point lies inside or on the sphere.  The caller multiplies by
-// c = 1 / (8 pi (1 - nu)) once, after the sum.
-IBEM_HD IBEM_INLINE bool sph_field24_df(const dfloat* p, const SphDF& sp, dfloat tn1, dfloat tn2, dfloat* e) {
+// Compensated sums (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci.
+// Comput. 26, 2005, algorithm Dot2) over double-float operands: s is the FP32 running sum of
+// the leading products, c the FP32 sum of every rounding error (TwoSum of each addition,
+// FMA residual and cross terms of each product).  The value s + c carries about twice
+// FP32's precision like a double-float sum, at 12 instead of 18 FP32 instructions per
+// multiply-add (no renormalisation after each term).
+struct dacc {
+  float s, c;
+};
+IBEM_HD IBEM_INLINE dacc dacc_of(dfloat x) { return {x.hi, x.lo}; }
+IBEM_HD IBEM_INLINE dacc dacc_prod(dfloat x, dfloat y) {
+  const float p = x.hi * y.hi;
+  return {p, df_fmaf(x.hi, y.lo, df_fmaf(x.lo, y.hi, df_fmaf(x.hi, y.hi, -p)))};
+}
+// a += x * y
+IBEM_HD IBEM_INLINE void dacc_fma(dacc& a, dfloat x, dfloat y) {
+  const float p = x.hi * y.hi;
+  const float e = df_fmaf(x.hi, y.lo, df_fmaf(x.lo, y.hi, df_fmaf(x.hi, y.hi, -p)));
+  const float s = a.s + p;
+  const float bb = s - a.s;
+  a.c += ((a.s - (s - bb)) + (p - bb)) + e;
+  a.s = s;
+}
+// a += x
+IBEM_HD IBEM_INLINE void dacc_add(dacc& a, dfloat x) {
+  const float s = a.s + x.hi;
+  const float bb = s - a.s;
+  a.c += ((a.s - (s - bb)) + (x.hi - bb)) + x.lo;
+  a.s = s;
+}
+IBEM_HD IBEM_INLINE dfloat dacc_val(dacc a) { return df_fast_two_sum(a.s, a.c); }
+IBEM_HD IBEM_INLINE dfloat dot3(const dfloat* u, const dfloat* x) {
+  dacc a = dacc_prod(u[0], x[0]);
+  dacc_fma(a, u[1], x[1]);
+  dacc_fma(a, u[2], x[2]);
+  return dacc_val(a);
+}
+
+// e[6] += strain / c at the point p (double-float, point already converted), each e[t] a
+// compensated sum over the spheres; returns whether the point lies inside or on the sphere.
+// The caller multiplies by c = 1 / (8 pi (1 - nu)) once, after the sum.
+IBEM_HD IBEM_INLINE bool sph_field24_df(const dfloat* p, const SphDF& sp, dfloat tn1, dfloat tn2, dacc* e) {
   dfloat x[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) x[i] = (p[i] - sp.c[i]) * sp.ia;
-  const dfloat r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+  const dfloat r2 = dot3(x, x);
   const bool ext = r2.hi > 1.0f || (r2.hi == 1.0f && r2.lo > 0.0f);
   const float fe = ext ? 1.0f : 0.0f;
   const dfloat rho2 = ext ? r2 : dfloat{1.0f, 0.0f};
@@ -193,44 +231,86 @@ IBEM_HD IBEM_INLINE bool sph_field24_df(const dfloat* p, const SphDF& sp, dfloat
   const int ti[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};  // (m, n) -> symmetric pair
   dfloat Ex[3], Ep[6], Epx[3], Gx[3][3], s[3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i) Ex[i] = sp.E[ti[i][0]] * x[0] + sp.E[ti[i][1]] * x[1] + sp.E[ti[i][2]] * x[2];
+  for (int i = 0; i < 3; ++i) {
+    const dfloat u[3] = {sp.E[ti[i][0]], sp.E[ti[i][1]], sp.E[ti[i][2]]};
+    Ex[i] = dot3(u, x);
+  }
 #pragma unroll
-  for (int t = 0; t < 6; ++t) Ep[t] = sp.F[3 * t] * x[0] + sp.F[3 * t + 1] * x[1] + sp.F[3 * t + 2] * x[2];
+  for (int t2 = 0; t2 < 6; ++t2) Ep[t2] = dot3(sp.F + 3 * t2, x);
 #pragma unroll
-  for (int n = 0; n < 3; ++n) Epx[n] = Ep[ti[n][0]] * x[0] + Ep[ti[n][1]] * x[1] + Ep[ti[n][2]] * x[2];
+  for (int n = 0; n < 3; ++n) {
+    const dfloat u[3] = {Ep[ti[n][0]], Ep[ti[n][1]], Ep[ti[n][2]]};
+    Epx[n] = dot3(u, x);
+  }
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
 #pragma unroll
-    for (int j = 0; j < 3; ++j)
-      Gx[i][j] = sp.F[3 * ti[j][0] + i] * x[0] + sp.F[3 * ti[j][1] + i] * x[1] + sp.F[3 * ti[j][2] + i] * x[2];
-    s[i] = Gx[i][0] * x[0] + Gx[i][1] * x[1] + Gx[i][2] * x[2];
+    for (int j = 0; j < 3; ++j) {
+      const dfloat u[3] = {sp.F[3 * ti[j][0] + i], sp.F[3 * ti[j][1] + i], sp.F[3 * ti[j][2] + i]};
+      Gx[i][j] = dot3(u, x);
+    }
+    s[i] = dot3(Gx[i], x);
   }
-  const dfloat q = Ex[0] * x[0] + Ex[1] * x[1] + Ex[2] * x[2];
-  const dfloat qp = Epx[0] * x[0] + Epx[1] * x[1] + Epx[2] * x[2];
-  const dfloat tEp = Ep[0] + Ep[3] + Ep[5];
-  const dfloat vx = sp.v[0] * x[0] + sp.v[1] * x[1] + sp.v[2] * x[2];
-  const dfloat wx = sp.w[0] * x[0] + sp.w[1] * x[1] + sp.w[2] * x[2];
+  const dfloat q = dot3(Ex, x), qp = dot3(Epx, x), vx = dot3(sp.v, x), wx = dot3(sp.w, x);
   const dfloat tE = sp.tE;
-  const dfloat tv = tEp + vx * 2.0f;
-  const dfloat A = Ps4 * q + Ps3 * tE - tE * Ph2 * tn2 + (Q4 * qp + Q3 * tv - wx * V1_2 * tn2);
-  const dfloat B = Ps3 * q + Ps2 * tE - tE * Ph1 * tn2 + (Q3 * qp + Q2 * tv - wx * V1_1 * tn2);
+  dacc ta = dacc_of(Ep[0]);
+  dacc_add(ta, Ep[3]);
+  dacc_add(ta, Ep[5]);
+  dacc_add(ta, vx * 2.0f);
+  const dfloat tv = dacc_val(ta);
+  const dfloat Ph2t = Ph2 * tn2, Ph1t = Ph1 * tn2, V12t = V1_2 * tn2, V11t = V1_1 * tn2;
+  dacc aA = dacc_prod(Ps4, q);
+  dacc_fma(aA, Ps3 - Ph2t, tE);
+  dacc_fma(aA, Q4, qp);
+  dacc_fma(aA, Q3, tv);
+  dacc_fma(aA, -V12t, wx);
+  const dfloat A = dacc_val(aA);
+  dacc aB = dacc_prod(Ps3, q);
+  dacc_fma(aB, Ps2 - Ph1t, tE);
+  dacc_fma(aB, Q3, qp);
+  dacc_fma(aB, Q2, tv);
+  dacc_fma(aB, -V11t, wx);
+  const dfloat B = dacc_val(aB);
   const dfloat tn1x2 = tn1 * 2.0f, tn1x4 = tn1 * 4.0f;
-  const dfloat cE = Ps3 * 2.0f - Ph2 * tn1x2;
-  const dfloat cEp = Q3 * 2.0f - V1_2 * tn1x2, cv = Q2 * 2.0f - V1_1 * tn1x2;
-  const dfloat cs = Q3, cgw = Q2 - V1_1 * tn2;  // g == w: the two terms share a coefficient
+  dacc c;
+  c = dacc_of(Ps3 * 2.0f); dacc_fma(c, -tn1x2, Ph2); const dfloat cE = dacc_val(c);
+  c = dacc_of(Q3 * 2.0f); dacc_fma(c, -tn1x2, V1_2); const dfloat cEp = dacc_val(c);
+  c = dacc_of(Q2 * 2.0f); dacc_fma(c, -tn1x2, V1_1); const dfloat cv = dacc_val(c);
+  const dfloat cs = Q3, cgw = Q2 - V11t;  // g == w: the two terms share a coefficient
+  c = dacc_of(Ps2 * 2.0f); dacc_fma(c, -tn1x4, Ph1); const dfloat C0 = dacc_val(c);
+  c = dacc_of(Q2 * 2.0f); dacc_fma(c, -tn1x4, V1_1); const dfloat C1 = dacc_val(c);
+  const dfloat C2 = cv;   // 2 Q2 - 2 tn1 V1_1
   dfloat W[3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i) W[i] = cE * Ex[i] + cEp * Epx[i] + cv * sp.v[i] + cs * s[i] + cgw * sp.w[i];
-  const dfloat C0 = Ps2 * 2.0f - Ph1 * tn1x4;
-  const dfloat C1 = Q2 * 2.0f - V1_1 * tn1x4;
-  const dfloat C2 = Q2 * 2.0f - V1_1 * tn1x2;
+  for (int i = 0; i < 3; ++i) {
+    dacc w = dacc_prod(cE, Ex[i]);
+    dacc_fma(w, cEp, Epx[i]);
+    dacc_fma(w, cv, sp.v[i]);
+    dacc_fma(w, cs, s[i]);
+    dacc_fma(w, cgw, sp.w[i]);
+    W[i] = dacc_val(w);
+  }
+  dfloat Ax[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) Ax[i] = A * x[i];
   const int pi[6] = {0, 0, 0, 1, 1, 2}, pj[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
-  for (int t = 0; t < 6; ++t) {
-    const int i = pi[t], j = pj[t];
-    dfloat r = A * x[i] * x[j] + W[i] * x[j] + W[j] * x[i] + C0 * sp.E[t] + C1 * Ep[t] + C2 * (Gx[i][j] + Gx[j][i]);
-    if (i == j) r += B;
-    e[t] += r;
+  for (int t2 = 0; t2 < 6; ++t2) {
+    const int i = pi[t2], j = pj[t2];
+    dacc& o = e[t2];
+    dacc_fma(o, Ax[i], x[j]);
+    if (i == j) {
+      dacc_fma(o, W[i] * 2.0f, x[i]);
+      dacc_add(o, B);
+      dacc_fma(o, C2 * 2.0f, Gx[i][i]);
+    } else {
+      dacc_fma(o, W[i], x[j]);
+      dacc_fma(o, W[j], x[i]);
+      dacc_fma(o, C2, Gx[i][j]);
+      dacc_fma(o, C2, Gx[j][i]);
+    }
+    dacc_fma(o, C0, sp.E[t2]);
+    dacc_fma(o, C1, Ep[t2]);
   }
   return !ext;
 }

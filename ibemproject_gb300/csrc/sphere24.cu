@@ -18,11 +18,19 @@ IBEM_FIELD_KERNEL(field24, sph_field24_contracted, 24)
 // (field_contract.cuh), split by distance.  Points are processed in Morton order (a stable
 // radix sort of 30-bit keys inside the point cloud's bounding box), so the 32 points of a
 // warp form a compact cluster; a sphere that lies beyond kFarRadii radii from all 32 of them
-// is summed in FP32 (sph_field24_f32, warp-uniform branch), every other one in double-float.
-// The loading threads turn each chunk of spheres into SphDF constants (scaled coordinates);
-// every thread keeps its six strain sums in double-float, and the inside test, the local
-// eigenstrain and C0 run in FP64 at the end.
-// per-sphere double-float constants, computed once per call (FP64 arithmetic, one thread each)
+// is summed in FP32 (sph_field24_f32), every other one in double-float.  Two kernels, one
+// code path each (a single loop over both paths stalled on instruction fetch, and the
+// double-float path's registers limited the FP32 path's occupancy):
+//   field24_far   every (warp, sphere) pair: the distance test, the FP32 sum of the far
+//                 spheres (Kahan-compensated per chunk of 64 spheres, then added to
+//                 double-float accumulators: as accurate as a double-float sum of every
+//                 term, at 4 instead of ~10 FP32 adds), and per (warp, chunk) a 64-bit
+//                 mask of the near spheres;
+//   field24_near  per warp, the spheres of its masks in double-float (compensated dot
+//                 products; each warp stages one sphere's constants at a time in its own
+//                 shared slot: no block barriers), then the inside test, the local
+//                 eigenstrain and C0 in FP64.
+// Per-sphere double-float constants (SphDF, scaled coordinates) are made once per call.
 __global__ void k_sph_df(int num, const double* __restrict__ cen, const double* __restrict__ rad,
                          const double* __restrict__ E, ibem::SphDF* __restrict__ out) {
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
@@ -30,23 +38,22 @@ __global__ void k_sph_df(int num, const double* __restrict__ cen, const double* 
 }
 
 __global__ void __launch_bounds__(ibem::kFieldThreads)
-    field24_df(const double* __restrict__ pts, const int* __restrict__ order, int nump,
-               const double* __restrict__ cen, const ibem::SphDF* __restrict__ sph, int num, SphMat mc,
-               const double* __restrict__ E, double* __restrict__ stress) {
+    field24_far(const double* __restrict__ pts, const int* __restrict__ order, int nump,
+                const ibem::SphDF* __restrict__ sph, int num, float tn1, float tn2,
+                unsigned long long* __restrict__ nmask, int nchunk, ibem::dfloat* __restrict__ accbuf) {
   static_assert(sizeof(ibem::SphDF) == 18 * sizeof(float4), "SphDF is copied as 18 float4");
-  static_assert(ibem::kFieldChunk <= 64, "the near-sphere mask of a chunk is 64 bits");
-  __shared__ ibem::SphDF ss[ibem::kFieldChunk];
+  static_assert(ibem::kFieldChunk == 64, "the near-sphere mask of a chunk is 64 bits");
+  __shared__ __align__(16) ibem::SphDF ss[ibem::kFieldChunk];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const bool act = t < nump;
+  const bool warp_act = (t & ~31) < nump;
   const int s = act ? order[t] : 0;
-  double p0 = 0, p1 = 0, p2 = 0;
-  if (act) { p0 = pts[3 * (int64_t)s]; p1 = pts[3 * (int64_t)s + 1]; p2 = pts[3 * (int64_t)s + 2]; }
-  const ibem::dfloat pd[3] = {ibem::df_make(p0), ibem::df_make(p1), ibem::df_make(p2)};
-  const ibem::dfloat tn1 = ibem::df_make(mc.tn1), tn2 = ibem::df_make(mc.tn2);
+  ibem::dfloat pd[3] = {};
+  if (act)
+    for (int k = 0; k < 3; ++k) pd[k] = ibem::df_make(pts[3 * (int64_t)s + k]);
   const float far2 = ibem::kFarRadii * ibem::kFarRadii;
   ibem::dfloat acc[6] = {};
-  int inside = -1;
-  for (int h0 = 0; h0 < num; h0 += ibem::kFieldChunk) {
+  for (int h0 = 0, c = 0; h0 < num; h0 += ibem::kFieldChunk, ++c) {
     const int nh = min(ibem::kFieldChunk, num - h0);
     __syncthreads();
     {
@@ -55,10 +62,8 @@ __global__ void __launch_bounds__(ibem::kFieldThreads)
       for (int i = threadIdx.x; i < nh * 18; i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
-    // pass 1: the spheres far from every point of the warp, in FP32; the others are noted
-    // in a warp-uniform mask and summed in double-float in pass 2, so that each pass runs
-    // one of the two code paths
     unsigned long long near = 0;
+    float sum[6] = {}, comp[6] = {};   // Kahan sums of the chunk's far spheres
 #pragma unroll 1
     for (int hh = 0; hh < nh; ++hh) {
       const ibem::SphDF& sp = ss[hh];
@@ -68,24 +73,68 @@ __global__ void __launch_bounds__(ibem::kFieldThreads)
       if (__all_sync(0xffffffffu, far)) {
         if (act) {
           float r[6];
-          ibem::sph_field24_f32(pd, sp, tn1.hi, tn2.hi, r);
+          ibem::sph_field24_f32(pd, sp, tn1, tn2, r);
 #pragma unroll
-          for (int k = 0; k < 6; ++k) ibem::df_add_f(acc[k], r[k]);
+          for (int k = 0; k < 6; ++k) {
+            const float y = r[k] - comp[k], u = sum[k] + y;
+            comp[k] = (u - sum[k]) - y;
+            sum[k] = u;
+          }
         }
       } else {
         near |= 1ull << hh;
       }
     }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      ibem::df_add_f(acc[k], sum[k]);
+      ibem::df_add_f(acc[k], -comp[k]);
+    }
+    if (warp_act && (threadIdx.x & 31) == 0) nmask[(int64_t)(t >> 5) * nchunk + c] = near;
+  }
+  if (act)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) accbuf[6 * (int64_t)t + k] = acc[k];
+}
+
+__global__ void __launch_bounds__(ibem::kFieldThreads)
+    field24_near(const double* __restrict__ pts, const int* __restrict__ order, int nump,
+                 const double* __restrict__ cen, const ibem::SphDF* __restrict__ sph, SphMat mc,
+                 const double* __restrict__ E, const unsigned long long* __restrict__ nmask, int nchunk,
+                 const ibem::dfloat* __restrict__ accbuf, double* __restrict__ stress) {
+  __shared__ __align__(16) ibem::SphDF ss[ibem::kFieldThreads / 32];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  if ((t & ~31) >= nump) return;   // whole warp past the end (no block barriers below)
+  const bool act = t < nump;
+  const int s = act ? order[t] : 0;
+  double p0 = 0, p1 = 0, p2 = 0;
+  if (act) { p0 = pts[3 * (int64_t)s]; p1 = pts[3 * (int64_t)s + 1]; p2 = pts[3 * (int64_t)s + 2]; }
+  const ibem::dfloat pd[3] = {ibem::df_make(p0), ibem::df_make(p1), ibem::df_make(p2)};
+  const ibem::dfloat tn1 = ibem::df_make(mc.tn1), tn2 = ibem::df_make(mc.tn2);
+  ibem::dacc acc[6] = {};
+  if (act)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) acc[k] = ibem::dacc_of(accbuf[6 * (int64_t)t + k]);
+  ibem::SphDF& sp = ss[threadIdx.x >> 5];
+  const unsigned long long* wm = nmask + (int64_t)(t >> 5) * nchunk;
+  int inside = -1;
+#pragma unroll 1
+  for (int c = 0; c < nchunk; ++c) {
+    unsigned long long near = wm[c];
 #pragma unroll 1
     while (near) {
-      const int hh = __ffsll((long long)near) - 1;
+      const int h = c * ibem::kFieldChunk + __ffsll((long long)near) - 1;
       near &= near - 1;
-      if (act && ibem::sph_field24_df(pd, ss[hh], tn1, tn2, acc)) inside = h0 + hh;
+      __syncwarp();
+      if (lane < 18) reinterpret_cast<float4*>(&sp)[lane] = reinterpret_cast<const float4*>(sph + h)[lane];
+      __syncwarp();
+      if (act && ibem::sph_field24_df(pd, sp, tn1, tn2, acc)) inside = h;
     }
   }
   if (!act) return;
   double e[6];
-  for (int r = 0; r < 6; ++r) e[r] = mc.kd * ibem::df_double(acc[r]);
+  for (int r = 0; r < 6; ++r) e[r] = mc.kd * ((double)acc[r].s + (double)acc[r].c);
   if (inside >= 0) {
     const double* Ei = E + 24 * (int64_t)inside;
     const double x0 = p0 - cen[3 * inside], x1 = p1 - cen[3 * inside + 1], x2 = p2 - cen[3 * inside + 2];
@@ -194,23 +243,36 @@ ibem_status launch_field24_df(const SphLaunch& p, const double* pts, int nump, c
   if (nump <= 0) return IBEM_OK;
   SphMat mc = sph_mat_init(p.E0, p.nu0, p.E1, p.nu1);
   ProfScope ps(PROF_FIELD, st);
-  // Morton order of the points (stream-ordered scratch: keys, indices, sort workspace)
+  // stream-ordered scratch: Morton keys and indices, sort workspace, sphere constants, the
+  // near masks (one 64-bit word per warp and chunk of spheres) and the far sums
   const unsigned nb = (unsigned)((nump + 255) / 256);
   size_t sort_bytes = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, (const unsigned*)nullptr, (unsigned*)nullptr,
                                   (const int*)nullptr, (int*)nullptr, nump, 0, 30, st);
-  const size_t n4 = ((size_t)nump * 4 + 255) / 256 * 256;
-  const size_t nsph = ((size_t)p.num * sizeof(SphDF) + 255) / 256 * 256;
-  const size_t bytes = 64 + 4 * n4 + nsph + sort_bytes;
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  const int nchunk = (p.num + kFieldChunk - 1) / kFieldChunk;
+  const int64_t nwarp = (nump + 31) / 32;
+  const size_t n4 = up((size_t)nump * 4);
+  const size_t nsph = up((size_t)p.num * sizeof(SphDF));
+  const size_t nmsk = up((size_t)nwarp * (size_t)nchunk * 8);
+  const size_t nacc = up((size_t)nump * 6 * sizeof(dfloat));
+  const size_t bytes = 256 + 4 * n4 + nsph + nmsk + nacc + sort_bytes;
   char* buf = nullptr;
   IBEM_CUDA(cudaMallocAsync((void**)&buf, bytes, st));
   unsigned long long* box = reinterpret_cast<unsigned long long*>(buf);
-  unsigned* k0 = reinterpret_cast<unsigned*>(buf + 64);
-  unsigned* k1 = reinterpret_cast<unsigned*>(buf + 64 + n4);
-  int* i0 = reinterpret_cast<int*>(buf + 64 + 2 * n4);
-  int* i1 = reinterpret_cast<int*>(buf + 64 + 3 * n4);
-  SphDF* sph = reinterpret_cast<SphDF*>(buf + 64 + 4 * n4);
-  void* tmp = buf + 64 + 4 * n4 + nsph;
+  char* q = buf + 256;
+  unsigned* k0 = reinterpret_cast<unsigned*>(q);
+  unsigned* k1 = reinterpret_cast<unsigned*>(q + n4);
+  int* i0 = reinterpret_cast<int*>(q + 2 * n4);
+  int* i1 = reinterpret_cast<int*>(q + 3 * n4);
+  q += 4 * n4;
+  SphDF* sph = reinterpret_cast<SphDF*>(q);
+  q += nsph;
+  unsigned long long* nmask = reinterpret_cast<unsigned long long*>(q);
+  q += nmsk;
+  dfloat* accbuf = reinterpret_cast<dfloat*>(q);
+  q += nacc;
+  void* tmp = q;
   ibem_status s = IBEM_OK;
   // box = (min, min, min, max, max, max) starts at (all ones, zeros) in the ordered-integer image
   cudaError_t e = cudaMemsetAsync(box, 0xff, 3 * sizeof(unsigned long long), st);
@@ -222,8 +284,11 @@ ibem_status launch_field24_df(const SphLaunch& p, const double* pts, int nump, c
     e = cub::DeviceRadixSort::SortPairs(tmp, sort_bytes, k0, k1, i0, i1, nump, 0, 30, st);
   }
   if (e == cudaSuccess) {
-    ::ibem::count_launch(), field24_df<<<(nump + kFieldThreads - 1) / kFieldThreads, kFieldThreads, 0, st>>>(
-        pts, i1, nump, p.cen, sph, p.num, mc, E, stress);
+    const unsigned grid = (unsigned)((nump + kFieldThreads - 1) / kFieldThreads);
+    ::ibem::count_launch(), field24_far<<<grid, kFieldThreads, 0, st>>>(
+        pts, i1, nump, sph, p.num, (float)mc.tn1, (float)mc.tn2, nmask, nchunk, accbuf);
+    ::ibem::count_launch(), field24_near<<<grid, kFieldThreads, 0, st>>>(pts, i1, nump, p.cen, sph, mc, E, nmask,
+                                                                        nchunk, accbuf, stress);
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) s = cuda_fail(e, "field24_df");

@@ -131,9 +131,9 @@ extern "C" int hg_field24df(const double* p, const double* cen, double a, double
   SphMat mc = sph_mat_init(E0, nu0, E1, nu1);
   const ibem::SphDF sp = ibem::sph_df_make(cen, a, E);
   const ibem::dfloat pd[3] = {ibem::df_make(p[0]), ibem::df_make(p[1]), ibem::df_make(p[2])};
-  ibem::dfloat acc[6] = {};
+  ibem::dacc acc[6] = {};
   ibem::sph_field24_df(pd, sp, ibem::df_make(mc.tn1), ibem::df_make(mc.tn2), acc);
-  for (int t = 0; t < 6; ++t) e[t] = mc.kd * ibem::df_double(acc[t]);
+  for (int t = 0; t < 6; ++t) e[t] = mc.kd * ((double)acc[t].s + (double)acc[t].c);
   return 0;
 }
 
