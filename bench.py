@@ -208,13 +208,15 @@ def sm_count():
 
 
 def roofline_chosen(prof, case):
-    """Roofline of the largest kernel of the matrix-free step, the split stress sums
-    (field24_df): FP32-pipe bound.  Algorithmic work = FIELD_ALG_FLOPS_PER_PAIR, the FP32
-    flops of the contracted strain of one (point, sphere) pair, x the pairs of one launch,
-    over its event-timed duration; the executed-flop fraction (ncu's FP32 instruction count
-    of the launch, double-float emulation near the points included) is reported beside it.
-    Peak = the nominal FP32 FMA rate (SMs of this device x 128 lanes x 2 flops) at the
-    measured maximum SM clock; MEASURED_PEAKS.json holds no FP32 figure."""
+    """Roofline of the largest stage of the matrix-free step, the split stress sums
+    (field24_far, FP32 beyond 14 radii of a warp's points, and field24_near, double-float
+    within): FP32-pipe bound.  Algorithmic work = FIELD_ALG_FLOPS_PER_PAIR, the FP32 flops of
+    the contracted strain of one (point, sphere) pair, x the pairs of one call, over the
+    event-timed duration of the call (the two kernels plus the Morton sort of the points);
+    the executed-flop fraction (ncu's FP32 instruction count of both kernels, double-float
+    arithmetic near the points included) is reported beside it.  Peak = the nominal FP32 FMA
+    rate (SMs of this device x 128 lanes x 2 flops) at the measured maximum SM clock;
+    MEASURED_PEAKS.json holds no FP32 figure."""
     f = prof.get("field")
     if not f or f["ms"] <= 0:
         return None
@@ -229,28 +231,28 @@ def roofline_chosen(prof, case):
     launch_s = f["ms"] / f["launches"] * 1e-3
     achieved = FIELD_ALG_FLOPS_PER_PAIR * pairs / launch_s / 1e12
     executed = FIELD_DF_FLOPS_PER_PAIR * pairs / launch_s / 1e12
-    return {"kernel": "field24_df (stress sums, double-float near / FP32 far)", "bound": "fp32", "achieved": achieved,
-            "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+    return {"kernel": "field24_far + field24_near (stress sums, FP32 far / double-float near)", "bound": "fp32",
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
             "peak_source": f"nominal FP32 FMA rate, {nsm} SMs at sm_max_mhz {mhz:g} (no measured FP32 peak)",
             "sm_count": nsm, "flops_per_pair": FIELD_ALG_FLOPS_PER_PAIR,
             "flops_per_pair_note": "algorithmic: the FP32 contraction of one (point, sphere) pair",
             "executed_flops_per_pair": FIELD_DF_FLOPS_PER_PAIR, "executed_achieved": executed,
             "frac_executed": executed / peak, "pairs_per_launch": pairs,
             "avg_launch_ms": f["ms"] / f["launches"], "traffic": FIELD_DF_TRAFFIC_PER_LAUNCH,
-            "traffic_unit": "bytes per launch (ncu dram read+write)",
+            "traffic_unit": "bytes per call (ncu dram read+write of both kernels)",
             "traffic_source": FIELD_DF_SOURCE, "flops_source": FIELD_DF_SOURCE}
 
 
 # Algorithmic FP32 flops of one (point, sphere) pair of the contracted stress sum: the FP32
-# path of field24_df alone (FADD + FMUL + 2 FFMA thread instructions counted by ncu on a launch
-# whose points are far from every sphere, 2.641e10 flops / 6.554e7 pairs).
-FIELD_ALG_FLOPS_PER_PAIR = 403.0
-# Executed FP32 flops per pair on this workload (the same count over one full-size launch:
-# double-float within 14 radii of a warp's points, FP32 beyond; 4.663e11 / 5.243e8) and the
-# launch's DRAM bytes (read + write) from the same capture.
-FIELD_DF_FLOPS_PER_PAIR = 889.4
-FIELD_DF_TRAFFIC_PER_LAUNCH = 21.00e6
-FIELD_DF_SOURCE = "profiles/field24_df_bench2000.md"
+# path alone (FADD + FMUL + 2 FFMA thread instructions counted by ncu on a field24_far launch
+# whose points are far from every sphere, 2.431e10 flops / 6.554e7 pairs).
+FIELD_ALG_FLOPS_PER_PAIR = 370.9
+# Executed FP32 flops per pair on this workload (the same count over both kernels of one
+# full-size call: 1.640e11 far + 2.271e11 near = 3.911e11 / 5.243e8 pairs) and the call's
+# DRAM bytes (read + write of both kernels) from the same capture.
+FIELD_DF_FLOPS_PER_PAIR = 745.9
+FIELD_DF_TRAFFIC_PER_LAUNCH = 43.59e6
+FIELD_DF_SOURCE = "profiles/field24_far_near_bench2000.md"
 
 
 # ------------------------------------------------------------------ clocks

@@ -231,7 +231,7 @@ def bench_field(num, grid, reps, dev, far=False):
     L.ibem_prof_enable(0)
     ms = prof.get("field", {}).get("ms", 0.0) / reps
     pairs = num * c.nump
-    return {"kernel": "field24_df" + (" (all far: FP32 path)" if far else ""), "spheres": num, "points": c.nump,
+    return {"kernel": "field24_far + field24_near" + (" (all far: FP32 path)" if far else ""), "spheres": num, "points": c.nump,
             "pairs": pairs, "reps": reps, "ms": ms,
             "ns_per_pair": ms * 1e6 / pairs if ms > 0 else None}
 
