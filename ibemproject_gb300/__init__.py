@@ -49,7 +49,7 @@ class Batch(ctypes.Structure):
 
 class MfOptions(ctypes.Structure):
     _fields_ = [("restart", ctypes.c_int), ("max_cycles", ctypes.c_int), ("max_outer", ctypes.c_int),
-                ("tol", ctypes.c_double), ("inner_tol", ctypes.c_double)]
+                ("tol", ctypes.c_double), ("inner_tol", ctypes.c_double), ("stepwise", ctypes.c_int)]
 
 
 class MfReport(ctypes.Structure):
@@ -123,6 +123,7 @@ SIGNATURES = {
                                  ctypes.POINTER(MfReport), _vp]),
     "ibem_e3d_batch_farfield_rhs": (_int, [ctypes.POINTER(Batch), _c_dp, _vp, _vp]),
     "ibem_e3d_mf_tuning": (_int, [ctypes.POINTER(Batch), _c_ip, _c_ip, _vp]),
+    "ibem_e3d_mf_tile_shape": (_int, [ctypes.POINTER(Batch), _c_ip, _c_ip, _c_ip, _vp]),
     "ibem_e3d_effective_modulus": (_int, [ctypes.POINTER(Batch), _vp, _c_dp, _c_dp, _c_dp, _c_dp, _vp]),
     "ibem_e3d_batch_farfield_rhs_layout": (_int, [ctypes.POINTER(Batch), _int, _c_dp, _vp, _vp]),
     "ibem_e3d_batch_dense_solve": (_int, [ctypes.POINTER(Batch), _int, _int, _vp, _vp, _dbl,

@@ -139,14 +139,16 @@ def matvec(batch: DeviceBatch, x, precision: int = 64):
 
 
 def solve(batch: DeviceBatch, b, precond: int = PRECOND_BLOCK_JACOBI, params=None, tol: float = 1e-10,
-          inner_tol: float = 1e-5, restart: int = 50, max_outer: int = 8, max_cycles: int = 20, x=None):
-    """Matrix-free solve of every realisation: returns (x, list of MfReport)."""
+          inner_tol: float = 1e-5, restart: int = 50, max_outer: int = 8, max_cycles: int = 20, x=None,
+          stepwise: bool = False):
+    """Matrix-free solve of every realisation: returns (x, list of MfReport).  stepwise: launch
+    each Arnoldi step from the host instead of one captured CUDA graph per GMRES cycle."""
     _linear(batch)
     import torch
     if x is None:
         x = torch.zeros_like(b)
     reps = (MfReport * batch.nseg)()
-    opt = MfOptions(restart, max_cycles, max_outer, tol, inner_tol)
+    opt = MfOptions(restart, max_cycles, max_outer, tol, inner_tol, int(stepwise))
     check(lib().ibem_e3d_mf_solve(batch.ref(), _ptr(b), _ptr(x), precond,
                                   _ptr(params) if params is not None else None, ctypes.byref(opt), reps, None))
     return x, list(reps)
@@ -159,6 +161,15 @@ def tuning(batch: DeviceBatch):
     a, b = ctypes.c_int(0), ctypes.c_int(0)
     check(lib().ibem_e3d_mf_tuning(batch.ref(), ctypes.byref(a), ctypes.byref(b), None))
     return a.value, b.value
+
+
+def tile_shape(batch: DeviceBatch):
+    """(targets per CTA, persistent launch 0/1, source slices) of the FP32 product chosen by
+    the library's autotuner for this batch's shape."""
+    _linear(batch)
+    t, p, h = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+    check(lib().ibem_e3d_mf_tile_shape(batch.ref(), ctypes.byref(t), ctypes.byref(p), ctypes.byref(h), None))
+    return t.value, p.value, h.value
 
 
 def effective_modulus(batch: DeviceBatch, x, sig_inf, volume=None):

@@ -22,6 +22,8 @@ int count_launch() {
   g_launches.fetch_add(1, std::memory_order_relaxed);
   return 0;
 }
+void add_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launches_so_far() { return g_launches.load(); }
 
 ibem_status fail(ibem_status st, const std::string& msg) {
   g_last_error = msg;

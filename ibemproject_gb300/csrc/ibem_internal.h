@@ -29,6 +29,10 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 // Counts kernel launches of this library (read through ibem_kernel_launches); every
 // launch site is written `::ibem::count_launch(), kernel<<<...>>>(...)`.
 int count_launch();
+// Adds n launches to the count (kernels that ran as nodes of a replayed CUDA graph; n < 0
+// takes back launches counted while a graph was captured, when nothing ran).
+void add_launches(long long n);
+long long launches_so_far();
 
 // ---- sphere kernels (sphere24.cu / sphere60.cu / sphere78.cu) ----
 struct SphLaunch {

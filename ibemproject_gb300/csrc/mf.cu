@@ -29,6 +29,8 @@
 #include <mutex>
 #include <thread>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -58,18 +60,18 @@ struct MvSink {
   __device__ __forceinline__ void operator()(int r, int c, T v) const { acc[r] = fma_t(v, xs[c], acc[r]); }
 };
 
-__global__ void __launch_bounds__(kMfThreads)
-    k_mf_apply_f32(const MfTile* __restrict__ tiles, const int* __restrict__ seg_begin,
-                   const int* __restrict__ mask, int mask_on,
-                   const float4* __restrict__ gh, const float4* __restrict__ gl,
-                   const SphMatF* __restrict__ mats, const float* __restrict__ x, float* __restrict__ y) {
-  __shared__ float4 sgh[kMfChunk], sgl[kMfChunk];
-  __shared__ float sx[kMfChunk * kMfNu];
-  const MfTile t = tiles[blockIdx.x];
+// One work item of the FP32 product: the TT targets of a tile against source slice `slice`
+// of `nslice` of its realisation (TT = blockDim.x, the tile shape the autotuner picks).
+template <int TT>
+__device__ __forceinline__ void mf_f32_item(const MfTile t, int slice, int nslice, const int* __restrict__ seg_begin,
+                                            const int* __restrict__ mask, int mask_on,
+                                            const float4* __restrict__ gh, const float4* __restrict__ gl,
+                                            const SphMatF* __restrict__ mats, const float* __restrict__ x,
+                                            float* __restrict__ y, float4* sgh, float4* sgl, float* sx) {
   if (mask && mask[t.seg] != mask_on) return;  // realisation left out of this product
   const int hb0 = seg_begin[t.seg], he0 = seg_begin[t.seg + 1];
-  const int per = (he0 - hb0 + gridDim.y - 1) / gridDim.y;
-  const int hb = hb0 + blockIdx.y * per, he = min(he0, hb + per);
+  const int per = (he0 - hb0 + nslice - 1) / nslice;
+  const int hb = hb0 + slice * per, he = min(he0, hb + per);
   if (hb >= he) return;
   const int s = t.s0 + threadIdx.x;
   const bool act = threadIdx.x < t.ns;
@@ -82,11 +84,11 @@ __global__ void __launch_bounds__(kMfThreads)
   for (int h0 = hb; h0 < he; h0 += kMfChunk) {
     const int nh = min(kMfChunk, he - h0);
     __syncthreads();
-    for (int i = threadIdx.x; i < nh; i += blockDim.x) {
+    for (int i = threadIdx.x; i < nh; i += TT) {
       sgh[i] = gh[h0 + i];
       sgl[i] = gl[h0 + i];
     }
-    for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x) sx[i] = x[(int64_t)kMfNu * h0 + i];
+    for (int i = threadIdx.x; i < nh * kMfNu; i += TT) sx[i] = x[(int64_t)kMfNu * h0 + i];
     __syncthreads();
     if (!act) continue;
 #pragma unroll 1
@@ -110,6 +112,37 @@ __global__ void __launch_bounds__(kMfThreads)
   float* o = y + (int64_t)kMfNu * s;
 #pragma unroll
   for (int r = 0; r < kMfNu; ++r) atomicAdd(o + r, yv[r]);
+}
+
+// one CTA per (tile, slice): grid (ntiles, nslice)
+template <int TT>
+__global__ void __launch_bounds__(TT)
+    k_mf_apply_f32(const MfTile* __restrict__ tiles, const int* __restrict__ seg_begin,
+                   const int* __restrict__ mask, int mask_on,
+                   const float4* __restrict__ gh, const float4* __restrict__ gl,
+                   const SphMatF* __restrict__ mats, const float* __restrict__ x, float* __restrict__ y) {
+  __shared__ float4 sgh[kMfChunk], sgl[kMfChunk];
+  __shared__ float sx[kMfChunk * kMfNu];
+  mf_f32_item<TT>(tiles[blockIdx.x], blockIdx.y, gridDim.y, seg_begin, mask, mask_on, gh, gl, mats, x, y, sgh, sgl,
+                  sx);
+}
+
+// persistent form: as many CTAs as fit on the GPU at once walk a work list of (tile,
+// slice) pairs sorted by decreasing cost (sources x targets), CTA c taking items c,
+// c + gridDim.x, ... (the longest first, so that the realisations of a ragged batch finish
+// together)
+template <int TT>
+__global__ void __launch_bounds__(TT)
+    k_mf_apply_f32_persist(const MfTile* __restrict__ tiles, const int2* __restrict__ work, int nwork, int nslice,
+                           const int* __restrict__ seg_begin, const int* __restrict__ mask, int mask_on,
+                           const float4* __restrict__ gh, const float4* __restrict__ gl,
+                           const SphMatF* __restrict__ mats, const float* __restrict__ x, float* __restrict__ y) {
+  __shared__ float4 sgh[kMfChunk], sgl[kMfChunk];
+  __shared__ float sx[kMfChunk * kMfNu];
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const int2 it = work[w];
+    mf_f32_item<TT>(tiles[it.x], it.y, nslice, seg_begin, mask, mask_on, gh, gl, mats, x, y, sgh, sgl, sx);
+  }
 }
 
 // FP64 product of the scaled system (the refinement residual): the same evaluation as the
@@ -419,10 +452,13 @@ __device__ __forceinline__ float dot24(const float* __restrict__ a, const float*
   }
   return s;
 }
+// kdev (graph-captured Arnoldi steps): v is column *kdev of a basis with column stride vstride
 __global__ void k_precond_apply(int num, const float* __restrict__ D, const float* __restrict__ Q,
-                                const int* __restrict__ nbr, const float* __restrict__ v, float* __restrict__ z) {
+                                const int* __restrict__ nbr, const float* __restrict__ v, float* __restrict__ z,
+                                const int* __restrict__ kdev = nullptr, int64_t vstride = 0) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= (int64_t)num * kMfNu) return;
+  if (kdev) v += (int64_t)(*kdev) * vstride;
   const int64_t p = t / kMfNu;
   const int r = (int)(t % kMfNu);
   float s = dot24(D + t * kMfNu, v + p * kMfNu);
@@ -435,13 +471,14 @@ __global__ void k_precond_apply(int num, const float* __restrict__ D, const floa
   z[t] = s;
 }
 
-// out[seg * ldo + j] += sum over the segment's rows of V_j[row] * w[row], j < nv.
+// out[seg * ldo + j] += sum over the segment's rows of V_j[row] * w[row], j < nv (+ *kdev).
 // grid (nseg, splits); a CTA of 256 threads holds up to 8 rows per thread in registers.
 constexpr int kDotRows = 8, kDotThreads = 256;
 template <class TV>
 __global__ void __launch_bounds__(kDotThreads)
     k_seg_dots(const int* __restrict__ seg_begin, int nv, const TV* __restrict__ V, int64_t ldv,
-               const TV* __restrict__ w, double* __restrict__ out, int ldo) {
+               const TV* __restrict__ w, double* __restrict__ out, int ldo, const int* __restrict__ kdev = nullptr) {
+  if (kdev) nv += *kdev;
   const int seg = blockIdx.x;
   const int64_t r0 = (int64_t)kMfNu * seg_begin[seg], r1 = (int64_t)kMfNu * seg_begin[seg + 1];
   const int64_t base = r0 + (int64_t)blockIdx.y * kDotThreads * kDotRows;
@@ -473,23 +510,28 @@ __global__ void __launch_bounds__(kDotThreads)
   }
 }
 
-// w[row] -= sum_j h[seg(row) * ldh + j] V_j[row]
+// w[row] -= sum_j h[seg(row) * ldh + j] V_j[row], j < nv (+ *kdev)
 __global__ void k_seg_sub(int64_t N, const int* __restrict__ seg_of, int nv, const float* __restrict__ V, int64_t ldv,
-                          const double* __restrict__ h, int ldh, float* __restrict__ w) {
+                          const double* __restrict__ h, int ldh, float* __restrict__ w,
+                          const int* __restrict__ kdev = nullptr) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= N) return;
+  if (kdev) nv += *kdev;
   const double* hs = h + (int64_t)seg_of[r / kMfNu] * ldh;
   float s = w[r];
   for (int j = 0; j < nv; ++j) s -= (float)hs[j] * V[(int64_t)j * ldv + r];
   w[r] = s;
 }
 
-// y[row] (+)= scale[seg(row)] * x[row] (FP32 <- FP64 / FP32)
+// y[row] (+)= scale[seg(row)] * x[row] (FP32 <- FP64 / FP32); with kdev, y is column
+// *kdev + 1 of a basis with column stride ystride
 template <class TX, class TY>
 __global__ void k_seg_scale(int64_t N, const int* __restrict__ seg_of, const double* __restrict__ scale,
-                            const TX* __restrict__ x, TY* __restrict__ y, int add) {
+                            const TX* __restrict__ x, TY* __restrict__ y, int add, const int* __restrict__ kdev = nullptr,
+                            int64_t ystride = 0) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= N) return;
+  if (kdev) y += (int64_t)(*kdev + 1) * ystride;
   const double v = scale[seg_of[r / kMfNu]] * (double)x[r];
   y[r] = add ? (TY)((double)y[r] + v) : (TY)v;
 }
@@ -516,9 +558,10 @@ struct Krylov {
   int* nactive;   // 1
 };
 
-__global__ void k_arnoldi_update(int nseg, int m, int k, Krylov K) {
+__global__ void k_arnoldi_update(int nseg, int m, int k, Krylov K, const int* __restrict__ kdev = nullptr) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nseg) return;
+  if (kdev) k = *kdev;
   if (!K.active[s]) {
     K.inv[s] = 0.0;
     return;
@@ -592,16 +635,30 @@ __global__ void k_cycle_start(int nseg, int m, Krylov K, const int* __restrict__
   if (a) atomicAdd(K.nactive, 1);
 }
 
-// x[row] += sum_j y[seg][j] V_j[row]
+// x[row] += sum_j y[seg][j] V_j[row], j < nv (+ *kdev)
 __global__ void k_seg_combine(int64_t N, const int* __restrict__ seg_of, int nv, const float* __restrict__ V,
-                              int64_t ldv, const double* __restrict__ y, int ldy, float* __restrict__ x) {
+                              int64_t ldv, const double* __restrict__ y, int ldy, float* __restrict__ x,
+                              const int* __restrict__ kdev = nullptr) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= N) return;
+  if (kdev) nv += *kdev;
   const double* ys = y + (int64_t)seg_of[r / kMfNu] * ldy;
   double s = 0;
   for (int j = 0; j < nv; ++j) s += ys[j] * (double)V[(int64_t)j * ldv + r];
   x[r] += (float)s;
 }
+
+// end of a graph-captured Arnoldi step: k += 1; the cycle's while loop goes on while
+// k < m and some realisation is still active
+__global__ void k_step_ctl(int* __restrict__ kdev, const int* __restrict__ nactive, int m,
+                           cudaGraphConditionalHandle h) {
+  const int k = *kdev + 1;
+  *kdev = k;
+  cudaGraphSetConditional(h, (k < m && *nactive > 0) ? 1u : 0u);
+}
+
+// steps taken by a captured cycle, added up for the launch count
+__global__ void k_add_steps(const int* __restrict__ kdev, int* __restrict__ total) { *total += *kdev; }
 
 template <class T>
 __global__ void k_fill(T* p, int64_t n, T v) {
@@ -710,6 +767,14 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
       tiles.push_back({s, p, std::min(kMfThreads, b.seg_begin_h[s + 1] - p), 0});
   }
   b.ntiles = (int)tiles.size();
+  std::vector<MfTile> tiles_s[3];
+  for (int k = 0; k < 3; ++k) {
+    const int tt = 64 << k;
+    for (int s = 0; s < in.nseg; ++s)
+      for (int p = b.seg_begin_h[s]; p < b.seg_begin_h[s + 1]; p += tt)
+        tiles_s[k].push_back({s, p, std::min(tt, b.seg_begin_h[s + 1] - p), 0});
+    b.ntiles_s[k] = (int)tiles_s[k].size();
+  }
   // slices of the source range: about 4 CTAs per SM in total, at least 32 sources per slice
   int dev = 0, nsm = 0;
   IBEM_CUDA(cudaGetDevice(&dev));
@@ -741,6 +806,7 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
   IBEM_CUDA(alloc_async((void**)&b.dr, sizeof(double) * b.N, st));
   IBEM_CUDA(alloc_async((void**)&b.dc, sizeof(double) * b.N, st));
   IBEM_CUDA(alloc_async((void**)&b.tiles, sizeof(MfTile) * b.ntiles, st));
+  for (int k = 0; k < 3; ++k) IBEM_CUDA(alloc_async((void**)&b.tiles_s[k], sizeof(MfTile) * b.ntiles_s[k], st));
   // Morton order of the centres within each realisation (10 bits per axis of its bounding box)
   std::vector<int> perm(b.num);
   {
@@ -785,6 +851,10 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
   IBEM_CUDA(cudaMemcpyAsync(b.matf, mf.data(), sizeof(SphMatF) * in.nseg, cudaMemcpyHostToDevice, st));
   IBEM_CUDA(cudaMemcpyAsync(b.mats, ms.data(), sizeof(SphMat) * in.nseg, cudaMemcpyHostToDevice, st));
   IBEM_CUDA(cudaMemcpyAsync(b.tiles, tiles.data(), sizeof(MfTile) * b.ntiles, cudaMemcpyHostToDevice, st));
+  for (int k = 0; k < 3; ++k)
+    IBEM_CUDA(cudaMemcpyAsync(b.tiles_s[k], tiles_s[k].data(), sizeof(MfTile) * b.ntiles_s[k], cudaMemcpyHostToDevice,
+                              st));
+  b.tshape = 1;   // 128 targets per CTA until the autotuner says otherwise
   ::ibem::count_launch(), k_mf_prep<<<nblk(b.num), 256, 0, st>>>(b.num, b.cen, b.rad, b.seg_of, b.matd, b.gh, b.gl,
                                                                  b.dr, b.dc);
   IBEM_LAUNCH_CHECK("mf prep");
@@ -805,19 +875,68 @@ void mf_batch_free(MfBatch& b) {
   free_async(b.dr, st);
   free_async(b.dc, st);
   free_async(b.tiles, st);
+  for (int k = 0; k < 3; ++k) free_async(b.tiles_s[k], st);
+  free_async(b.work, st);
   free_async(b.perm, st);
   b = MfBatch();
 }
 
+ibem_status mf_set_f32_shape(MfBatch& b, int tshape, int hsplit, int persist, cudaStream_t st) {
+  b.tshape = tshape;
+  b.hsplit = hsplit;
+  b.persist = persist;
+  if (!persist) return IBEM_OK;
+  // work list: every (tile, slice) with sources, by decreasing targets x sources
+  std::vector<MfTile> tiles(b.ntiles_s[tshape]);
+  {
+    // tiles of this shape, rebuilt on the host from the segment table (as at batch init)
+    const int tt = 64 << tshape;
+    int n = 0;
+    for (int s = 0; s < b.nseg; ++s)
+      for (int p = b.seg_begin_h[s]; p < b.seg_begin_h[s + 1]; p += tt)
+        tiles[n++] = {s, p, std::min(tt, b.seg_begin_h[s + 1] - p), 0};
+  }
+  std::vector<std::pair<int64_t, int2>> items;
+  for (int t = 0; t < (int)tiles.size(); ++t) {
+    const int hb0 = b.seg_begin_h[tiles[t].seg], he0 = b.seg_begin_h[tiles[t].seg + 1];
+    const int per = (he0 - hb0 + hsplit - 1) / hsplit;
+    for (int j = 0; j < hsplit; ++j) {
+      const int len = std::min(he0, hb0 + (j + 1) * per) - (hb0 + j * per);
+      if (len > 0) items.push_back({(int64_t)len * tiles[t].ns, make_int2(t, j)});
+    }
+  }
+  std::stable_sort(items.begin(), items.end(), [](const auto& a, const auto& c) { return a.first > c.first; });
+  std::vector<int2> w(items.size());
+  for (size_t i = 0; i < items.size(); ++i) w[i] = items[i].second;
+  free_async(b.work, st);
+  b.work = nullptr;
+  b.nwork = (int)w.size();
+  IBEM_CUDA(alloc_async((void**)&b.work, sizeof(int2) * std::max<size_t>(1, w.size()), st));
+  IBEM_CUDA(cudaMemcpyAsync(b.work, w.data(), sizeof(int2) * w.size(), cudaMemcpyHostToDevice, st));
+  IBEM_CUDA(cudaStreamSynchronize(st));   // w must outlive the copy
+  int dev = 0, sms = 0, per_sm = 0;
+  IBEM_CUDA(cudaGetDevice(&dev));
+  IBEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int tt = 64 << tshape;
+  cudaError_t e = tshape == 0   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mf_apply_f32_persist<64>, tt, 0)
+                  : tshape == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mf_apply_f32_persist<128>, tt, 0)
+                                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mf_apply_f32_persist<256>, tt, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "mf persistent occupancy");
+  b.persist_ctas = std::max(1, std::min(b.nwork, std::max(1, per_sm) * sms));
+  return IBEM_OK;
+}
+
 // ------------------------------------------------------------------ autotuner
 // The products' launch shape is (target tiles) x (source slices); the slice count trades
-// parallelism and tail effects against the atomic adds of the partial sums.  For a shape
-// class (log2 buckets of the tile count and of the largest realisation, and the number of
-// SMs) the tuner times each candidate count once with CUDA events (one launch each, inputs
-// of zeros, the same work as any input) and keeps the fastest; the table lives for the
-// process.  The FP32 kernel (128 registers) and the double-float / FP64 kernels (~255
-// registers, half the resident CTAs) are tuned separately (the double-float kernel stands
-// for both wide ones).
+// parallelism and tail effects against the atomic adds of the partial sums.  For the FP32
+// product (the GMRES operator, launched once per Arnoldi step) the tuner also picks the
+// tile shape (64, 128 or 256 targets per CTA) and the launch form: one CTA per (tile,
+// slice), or persistent CTAs (as many as fit on the GPU) over a list of (tile, slice) items
+// sorted by decreasing cost.  For a shape class (log2 buckets of the tile count and of the
+// largest realisation, and the number of SMs) every candidate is run once to warm up and
+// once timed with CUDA events (inputs of zeros: the same work as any input); the fastest is
+// kept for the process.  The double-float / FP64 kernels (~255 registers) keep 128-target
+// tiles and get their own slice count.
 namespace {
 struct TuneKey {
   int tiles_b, seg_b, sms;
@@ -825,13 +944,26 @@ struct TuneKey {
     return tiles_b != o.tiles_b ? tiles_b < o.tiles_b : seg_b != o.seg_b ? seg_b < o.seg_b : sms < o.sms;
   }
 };
+struct TuneVal {
+  int hsplit, hsplit_wide, tshape, persist;
+};
 std::mutex g_tune_mu;
-std::map<TuneKey, std::pair<int, int>> g_tune;
+std::map<TuneKey, TuneVal> g_tune;
 
 int log2_bucket(int v) {
   int b = 0;
   while ((1 << b) < v) ++b;
   return b;
+}
+// slice counts that give 1, 2, 4 and 8 CTAs per SM in total (at least 32 sources a slice)
+std::vector<int> slice_candidates(int ntiles, int max_seg, int sms) {
+  const int cap = std::max(1, (max_seg + 31) / 32);
+  std::vector<int> cand;
+  for (int per_sm : {1, 2, 4, 8}) {
+    const int h = std::max(1, std::min(cap, (sms * per_sm + ntiles - 1) / ntiles));
+    if (std::find(cand.begin(), cand.end(), h) == cand.end()) cand.push_back(h);
+  }
+  return cand;
 }
 }  // namespace
 
@@ -840,23 +972,30 @@ ibem_status mf_tune(MfBatch& b, cudaStream_t st) {
   IBEM_CUDA(cudaGetDevice(&dev));
   IBEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const TuneKey key{log2_bucket(b.ntiles), log2_bucket(b.max_seg), sms};
-  {
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    auto it = g_tune.find(key);
-    if (it != g_tune.end()) {
-      const int cap = std::max(1, (b.max_seg + 31) / 32);
-      b.hsplit = std::min(it->second.first, cap);
-      b.hsplit_wide = std::min(it->second.second, cap);
-      return IBEM_OK;
-    }
-  }
-  // candidates: CTA totals of 1, 2, 4 and 8 per SM (and the slice count that gives one
-  // slice per 32 sources at most)
   const int cap = std::max(1, (b.max_seg + 31) / 32);
-  std::vector<int> cand;
-  for (int per_sm : {1, 2, 4, 8}) {
-    const int h = std::max(1, std::min(cap, (sms * per_sm + b.ntiles - 1) / b.ntiles));
-    if (std::find(cand.begin(), cand.end(), h) == cand.end()) cand.push_back(h);
+  // IBEM_MF_F32_SHAPE="shape,persistent,slices" fixes the FP32 product's launch (tests and
+  // measurements of every shape); the wide products keep the batch's initial slice count
+  if (const char* f = std::getenv("IBEM_MF_F32_SHAPE")) {
+    int ts = 1, pers = 0, h = 1;
+    if (std::sscanf(f, "%d,%d,%d", &ts, &pers, &h) == 3 && ts >= 0 && ts < 3 && (pers == 0 || pers == 1) && h >= 1)
+      return mf_set_f32_shape(b, ts, std::min(h, cap), pers, st);
+    return fail(IBEM_ERR_ARG, "IBEM_MF_F32_SHAPE: expected shape (0-2),persistent (0/1),slices (>= 1)");
+  }
+  {
+    bool hit = false;
+    TuneVal v{};
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto it = g_tune.find(key);
+      if (it != g_tune.end()) {
+        hit = true;
+        v = it->second;
+      }
+    }
+    if (hit) {
+      b.hsplit_wide = std::min(v.hsplit_wide, cap);
+      return mf_set_f32_shape(b, v.tshape, std::min(v.hsplit, cap), v.persist, st);
+    }
   }
   float* xf = nullptr;
   float* yf = nullptr;
@@ -875,45 +1014,78 @@ ibem_status mf_tune(MfBatch& b, cudaStream_t st) {
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
     if (e != cudaSuccess) s = cuda_fail(e, "mf tune");
   }
-  int best_f = b.hsplit, best_w = b.hsplit_wide;
-  for (int wide = 0; wide < 2 && !s; ++wide) {
-    float best_ms = 1e30f;
-    for (int h : cand) {
-      if (wide) b.hsplit_wide = h; else b.hsplit = h;
+  // runs the product twice (warm-up, then timed) and returns the timed milliseconds
+  auto time_it = [&](bool wide, float& ms) -> ibem_status {
+    for (int rep = 0; rep < 2; ++rep) {
       cudaEventRecord(e0, st);
-      s = wide ? mf_apply_df(b, xd, yd, st) : mf_apply_f32(b, xf, yf, st);
+      ibem_status r = wide ? mf_apply_df(b, xd, yd, st) : mf_apply_f32(b, xf, yf, st);
       cudaEventRecord(e1, st);
-      if (s) break;
-      const cudaError_t e = cudaEventSynchronize(e1);
-      if (e != cudaSuccess) { s = cuda_fail(e, "mf tune"); break; }
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      if (ms < best_ms) {
-        best_ms = ms;
-        (wide ? best_w : best_f) = h;
+      if (r) return r;
+    }
+    const cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) return cuda_fail(e, "mf tune");
+    cudaEventElapsedTime(&ms, e0, e1);
+    return IBEM_OK;
+  };
+  TuneVal best{b.hsplit, b.hsplit_wide, b.tshape, 0};
+  float best_ms = 1e30f;
+  for (int ts = 0; ts < 3 && !s; ++ts)
+    for (int h : slice_candidates(b.ntiles_s[ts], b.max_seg, sms)) {
+      for (int pers = 0; pers < 2 && !s; ++pers) {
+        if ((s = mf_set_f32_shape(b, ts, h, pers, st))) break;
+        float ms = 0.f;
+        if ((s = time_it(false, ms))) break;
+        if (ms < best_ms) {
+          best_ms = ms;
+          best.tshape = ts;
+          best.hsplit = h;
+          best.persist = pers;
+        }
       }
+      if (s) break;
+    }
+  best_ms = 1e30f;
+  for (int h : slice_candidates(b.ntiles, b.max_seg, sms)) {
+    if (s) break;
+    b.hsplit_wide = h;
+    float ms = 0.f;
+    if ((s = time_it(true, ms))) break;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best.hsplit_wide = h;
     }
   }
-  b.hsplit = best_f;
-  b.hsplit_wide = best_w;
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   free_async(xf, st);
   free_async(yf, st);
   free_async(xd, st);
   free_async(yd, st);
-  if (!s) {
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune[key] = {best_f, best_w};
-  }
-  return s;
+  if (s) return s;
+  b.hsplit_wide = best.hsplit_wide;
+  if ((s = mf_set_f32_shape(b, best.tshape, best.hsplit, best.persist, st))) return s;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = best;
+  return IBEM_OK;
+}
+
+template <int TT>
+void launch_f32(const MfBatch& b, const float* x, float* y, cudaStream_t st, const int* mask, int mask_on) {
+  const MfTile* tiles = b.tiles_s[TT == 64 ? 0 : (TT == 128 ? 1 : 2)];
+  if (b.persist)
+    ::ibem::count_launch(), k_mf_apply_f32_persist<TT><<<b.persist_ctas, TT, 0, st>>>(
+        tiles, b.work, b.nwork, b.hsplit, b.seg_begin, mask, mask_on, b.gh, b.gl, b.matf, x, y);
+  else
+    ::ibem::count_launch(), k_mf_apply_f32<TT><<<dim3(b.ntiles_s[TT == 64 ? 0 : (TT == 128 ? 1 : 2)], b.hsplit), TT, 0,
+                                                 st>>>(tiles, b.seg_begin, mask, mask_on, b.gh, b.gl, b.matf, x, y);
 }
 
 ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_t st, const int* mask, int mask_on) {
   ProfScope ps(PROF_MF_F32, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(float) * b.N, st));
-  ::ibem::count_launch(), k_mf_apply_f32<<<dim3(b.ntiles, b.hsplit), kMfThreads, 0, st>>>(b.tiles, b.seg_begin, mask, mask_on,
-                                                                                         b.gh, b.gl, b.matf, x, y);
+  if (b.tshape == 0) launch_f32<64>(b, x, y, st, mask, mask_on);
+  else if (b.tshape == 2) launch_f32<256>(b, x, y, st, mask, mask_on);
+  else launch_f32<128>(b, x, y, st, mask, mask_on);
   IBEM_LAUNCH_CHECK("mf apply f32");
   return IBEM_OK;
 }
@@ -975,19 +1147,30 @@ struct MfSolver {
   int64_t N;
   float* V = nullptr;    // (m+1) x N Krylov basis
   float* z = nullptr;    // N
-  float* w = nullptr;    // N
+  float* w = nullptr;    // N   new Arnoldi vector before normalisation (and scratch)
   float* d = nullptr;    // N   correction of the current refinement step
   float* rin = nullptr;  // N   right-hand side of the current GMRES solve
   float* r32 = nullptr;  // N   residual of a restarted cycle
   int* done = nullptr;   // nseg
   double* tolv = nullptr;  // nseg: residual reduction asked of this GMRES solve
+  int* kdev = nullptr;     // Arnoldi step index of the graph-captured cycle
+  int* steps_dev = nullptr;  // Arnoldi steps run by the captured cycles (launch count)
   Krylov K{};
   void* kmem = nullptr;
   int splits = 1;
-  MfSolver(const MfBatch& bb, cudaStream_t s, int mm) : b(bb), st(s), m(mm), N(bb.N) {
+  // one GMRES cycle's Arnoldi steps as a CUDA graph: a while node whose body is one step
+  // (captured once per solver; the buffers it uses live as long as the solver)
+  bool use_graph = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  long long step_kernels = 0;   // kernels in one captured step
+  const MfPrecond* graph_pc = nullptr;
+  MfSolver(const MfBatch& bb, cudaStream_t s, int mm, bool graphs) : b(bb), st(s), m(mm), N(bb.N), use_graph(graphs) {
     splits = (int)((kMfNu * (int64_t)b.max_seg + kDotThreads * kDotRows - 1) / (kDotThreads * kDotRows));
   }
   ~MfSolver() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
     free_async(V, st);
     free_async(z, st);
     free_async(w, st);
@@ -1009,7 +1192,8 @@ struct MfSolver {
     IBEM_CUDA(alloc_async((void**)&tolv, sizeof(double) * b.nseg, st));
     const size_t S = b.nseg;
     const size_t nd = S * ((size_t)(m + 1) * m + (m + 1) + 2 * (size_t)m + 5 + 2 * (size_t)(m + 1) + m);
-    IBEM_CUDA(alloc_async((void**)&kmem, nd * sizeof(double) + sizeof(int) * (3 * S + 1), st));
+    const size_t ni = 3 * S + 3;
+    IBEM_CUDA(alloc_async((void**)&kmem, nd * sizeof(double) + sizeof(int) * ni, st));
     double* p = (double*)kmem;
     K.H = p; p += S * (m + 1) * m;
     K.g = p; p += S * (m + 1);
@@ -1027,17 +1211,21 @@ struct MfSolver {
     K.kc = ip; ip += S;
     K.active = ip; ip += S;
     K.nsteps = ip; ip += S;
-    K.nactive = ip;
-    IBEM_CUDA(cudaMemsetAsync(kmem, 0, nd * sizeof(double) + sizeof(int) * (3 * S + 1), st));
+    K.nactive = ip; ip += 1;
+    kdev = ip; ip += 1;
+    steps_dev = ip;
+    IBEM_CUDA(cudaMemsetAsync(kmem, 0, nd * sizeof(double) + sizeof(int) * ni, st));
     return IBEM_OK;
   }
   template <class T>
-  ibem_status seg_norm2(const T* v, double* n2) {
-    IBEM_CUDA(cudaMemsetAsync(n2, 0, sizeof(double) * b.nseg, st));
-    ::ibem::count_launch(), k_seg_dots<T><<<dim3(b.nseg, splits), kDotThreads, 0, st>>>(b.seg_begin, 1, v, 0, v, n2, 1);
+  ibem_status seg_norm2(const T* v, double* n2, cudaStream_t s) {
+    IBEM_CUDA(cudaMemsetAsync(n2, 0, sizeof(double) * b.nseg, s));
+    ::ibem::count_launch(), k_seg_dots<T><<<dim3(b.nseg, splits), kDotThreads, 0, s>>>(b.seg_begin, 1, v, 0, v, n2, 1);
     IBEM_LAUNCH_CHECK("seg norm");
     return IBEM_OK;
   }
+  template <class T>
+  ibem_status seg_norm2(const T* v, double* n2) { return seg_norm2(v, n2, st); }
   int read_nactive(ibem_status& s) {
     int h = 0;
     cudaError_t e = cudaMemcpyAsync(&h, K.nactive, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -1045,12 +1233,77 @@ struct MfSolver {
     if (e != cudaSuccess) s = cuda_fail(e, "gmres: read active count");
     return h;
   }
+  // Arnoldi step k on stream s: w = As P v_k, two Gram-Schmidt passes against v_0..v_k,
+  // the per-realisation Hessenberg update, v_(k+1) = w / ||w||.  With kd (graph capture) the
+  // kernels read k from *kd instead.
+  ibem_status arnoldi_step(const MfPrecond& P, int k, const int* kd, cudaStream_t s) {
+    const int S = b.nseg;
+    const float* vk = kd ? V : V + (int64_t)k * N;
+    const int nv = kd ? 1 : k + 1;   // k_seg_dots / k_seg_sub add *kd
+    ::ibem::count_launch(), k_precond_apply<<<nblk(N), 256, 0, s>>>(b.num, P.D, P.Q, P.nbr, vk, z, kd, kd ? N : 0);
+    ibem_status r = mf_apply_f32(b, z, w, s, K.active, 1);   // converged realisations sit out
+    if (r) return r;
+    ProfScope pg(PROF_GMRES_OTHER, s);
+    IBEM_CUDA(cudaMemsetAsync(K.d1, 0, sizeof(double) * 2 * (size_t)S * (m + 1), s));
+    ::ibem::count_launch(), k_seg_dots<float><<<dim3(S, splits), kDotThreads, 0, s>>>(b.seg_begin, nv, V, N, w, K.d1, m + 1, kd);
+    ::ibem::count_launch(), k_seg_sub<<<nblk(N), 256, 0, s>>>(N, b.seg_of, nv, V, N, K.d1, m + 1, w, kd);
+    ::ibem::count_launch(), k_seg_dots<float><<<dim3(S, splits), kDotThreads, 0, s>>>(b.seg_begin, nv, V, N, w, K.d2, m + 1, kd);
+    ::ibem::count_launch(), k_seg_sub<<<nblk(N), 256, 0, s>>>(N, b.seg_of, nv, V, N, K.d2, m + 1, w, kd);
+    if ((r = seg_norm2(w, K.n2, s))) return r;
+    IBEM_CUDA(cudaMemsetAsync(K.nactive, 0, sizeof(int), s));
+    ::ibem::count_launch(), k_arnoldi_update<<<nblk(S, 128), 128, 0, s>>>(S, m, k, K, kd);
+    float* vnext = kd ? V : V + (int64_t)(k + 1) * N;
+    ::ibem::count_launch(), k_seg_scale<float, float><<<nblk(N), 256, 0, s>>>(N, b.seg_of, K.inv, w, vnext, 0, kd,
+                                                                               kd ? N : 0);
+    IBEM_LAUNCH_CHECK("arnoldi step");
+    return IBEM_OK;
+  }
+  // The cycle graph: while (k < m and a realisation is active) { Arnoldi step *kdev; k += 1 }.
+  // Captured on a private stream (capture only records; the graph runs on st).
+  ibem_status build_graph(const MfPrecond& P) {
+    cudaStream_t cs = nullptr;
+    cudaGraphConditionalHandle h;
+    cudaGraphNodeParams cp{};
+    cudaGraphNode_t node;
+    IBEM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaError_t e = cudaGraphCreate(&graph, 0);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) {
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = h;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp);
+    }
+    ibem_status r = IBEM_OK;
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(cs, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                            cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      const long long before = launches_so_far();
+      r = arnoldi_step(P, 0, kdev, cs);
+      if (!r) ::ibem::count_launch(), k_step_ctl<<<1, 1, 0, cs>>>(kdev, K.nactive, m, h);
+      step_kernels = launches_so_far() - before;
+      add_launches(-step_kernels);   // captured, not run
+      cudaGraph_t body = nullptr;
+      const cudaError_t e2 = cudaStreamEndCapture(cs, &body);
+      if (e2 != cudaSuccess && !r) e = e2;
+    }
+    if (e == cudaSuccess && !r) e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaStreamDestroy(cs);
+    if (r) return r;
+    if (e != cudaSuccess) return cuda_fail(e, "gmres: cycle graph");
+    graph_pc = &P;
+    return IBEM_OK;
+  }
   // FP32 GMRES(m) with restarts on As d = rin, right-preconditioned by P; d overwritten.
   // Realisations flagged in `done` take no step.  Stops each realisation once
   // ||rin - As d|| <= inner_tol ||rin|| (Arnoldi estimate).
   ibem_status gmres(const MfPrecond& P, int max_cycles) {
     const int S = b.nseg;
     ibem_status s = IBEM_OK;
+    // the phase profiler records events, which a graph's while loop cannot hold
+    const bool graphed = use_graph && !prof_on();
+    if (graphed && (!exec || graph_pc != &P) && (s = build_graph(P))) return s;
     IBEM_CUDA(cudaMemsetAsync(d, 0, sizeof(float) * N, st));
     for (int cyc = 0; cyc < max_cycles && !s; ++cyc) {
       const float* r = rin;
@@ -1067,37 +1320,36 @@ struct MfSolver {
       const int na = read_nactive(s);
       if (s || na == 0) break;
       int k = 0;
-      while (k < m) {
-        float* vk = V + (int64_t)k * N;
-        float* wv = V + (int64_t)(k + 1) * N;
-        ::ibem::count_launch(), k_precond_apply<<<nblk(N), 256, 0, st>>>(b.num, P.D, P.Q, P.nbr, vk, z);
-        if ((s = mf_apply_f32(b, z, wv, st, K.active, 1))) break;   // converged realisations sit out
-        {
-          ProfScope pg(PROF_GMRES_OTHER, st);
-          IBEM_CUDA(cudaMemsetAsync(K.d1, 0, sizeof(double) * 2 * (size_t)S * (m + 1), st));
-          ::ibem::count_launch(), k_seg_dots<float><<<dim3(S, splits), kDotThreads, 0, st>>>(b.seg_begin, k + 1, V, N, wv, K.d1, m + 1);
-          ::ibem::count_launch(), k_seg_sub<<<nblk(N), 256, 0, st>>>(N, b.seg_of, k + 1, V, N, K.d1, m + 1, wv);
-          ::ibem::count_launch(), k_seg_dots<float><<<dim3(S, splits), kDotThreads, 0, st>>>(b.seg_begin, k + 1, V, N, wv, K.d2, m + 1);
-          ::ibem::count_launch(), k_seg_sub<<<nblk(N), 256, 0, st>>>(N, b.seg_of, k + 1, V, N, K.d2, m + 1, wv);
-          if ((s = seg_norm2(wv, K.n2))) break;
-          IBEM_CUDA(cudaMemsetAsync(K.nactive, 0, sizeof(int), st));
-          ::ibem::count_launch(), k_arnoldi_update<<<nblk(S, 128), 128, 0, st>>>(S, m, k, K);
-          ::ibem::count_launch(), k_seg_scale<float, float><<<nblk(N), 256, 0, st>>>(N, b.seg_of, K.inv, wv, wv, 0);
-          IBEM_LAUNCH_CHECK("arnoldi step");
+      if (graphed) {
+        IBEM_CUDA(cudaMemsetAsync(kdev, 0, sizeof(int), st));
+        IBEM_CUDA(cudaGraphLaunch(exec, st));
+        ::ibem::count_launch(), k_add_steps<<<1, 1, 0, st>>>(kdev, steps_dev);
+        IBEM_LAUNCH_CHECK("gmres cycle graph");
+      } else {
+        while (k < m) {
+          if ((s = arnoldi_step(P, k, nullptr, st))) break;
+          ++k;
+          if (read_nactive(s) == 0 || s) break;
         }
-        ++k;
-        if (read_nactive(s) == 0 || s) break;
       }
       if (s) break;
       // d += P V y
       ::ibem::count_launch(), k_hess_solve<<<nblk(S, 128), 128, 0, st>>>(S, m, K);
       IBEM_CUDA(cudaMemsetAsync(w, 0, sizeof(float) * N, st));
-      ::ibem::count_launch(), k_seg_combine<<<nblk(N), 256, 0, st>>>(N, b.seg_of, k, V, N, K.yv, m, w);
+      ::ibem::count_launch(), k_seg_combine<<<nblk(N), 256, 0, st>>>(N, b.seg_of, graphed ? 0 : k, V, N, K.yv, m, w,
+                                                                    graphed ? kdev : nullptr);
       ::ibem::count_launch(), k_precond_apply<<<nblk(N), 256, 0, st>>>(b.num, P.D, P.Q, P.nbr, w, z);
       ::ibem::count_launch(), k_add_f32<<<nblk(N), 256, 0, st>>>(N, z, d);
       IBEM_LAUNCH_CHECK("gmres update");
     }
     return s;
+  }
+  // kernels the captured cycles ran (read once, when the solve has synchronised)
+  long long graph_launches() {
+    if (!exec) return 0;
+    int h = 0;
+    if (cudaMemcpy(&h, steps_dev, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+    return (long long)h * step_kernels;
   }
 };
 
@@ -1107,7 +1359,7 @@ ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPr
                      ibem_mf_report* rep, cudaStream_t st) {
   const int S = b.nseg;
   const int64_t N = b.N;
-  MfSolver g(b, st, o.restart);
+  MfSolver g(b, st, o.restart, o.stepwise == 0);
   ibem_status s = g.alloc();
   double *xs = nullptr, *rs = nullptr, *y = nullptr, *bs = nullptr, *bn2 = nullptr;
   if (!s) {
@@ -1218,6 +1470,7 @@ ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPr
       rep[i].outer = outer_of[i];
       rep[i].inner = steps[i];
     }
+    if (!s) add_launches(g.graph_launches());
     for (int i = 0; i < S && !s; ++i)
       if (!(rep[i].rel_residual <= o.tol)) s = fail(IBEM_ERR_NOCONV, "mf solve: a realisation missed the tolerance");
   }
@@ -1262,8 +1515,9 @@ extern "C" ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int preci
       free_async(ys, st);
     } else {
       float *xf = nullptr, *yf = nullptr;
-      cudaError_t e = alloc_async((void**)&xf, sizeof(float) * b.N, st);
-      if (e == cudaSuccess) e = alloc_async((void**)&yf, sizeof(float) * b.N, st);
+      s = mf_tune(b, st);   // the tile shape the solver's GMRES uses
+      cudaError_t e = s ? cudaSuccess : alloc_async((void**)&xf, sizeof(float) * b.N, st);
+      if (e == cudaSuccess && !s) e = alloc_async((void**)&yf, sizeof(float) * b.N, st);
       if (e != cudaSuccess) s = cuda_fail(e, "mf_matvec workspace");
       if (!s) {
         ::ibem::count_launch(), k_div_to_f32<<<nblk(b.N), 256, 0, st>>>(b.N, x_dev, b.dc, xf);  // xs = x / Dc
@@ -1623,6 +1877,25 @@ extern "C" ibem_status ibem_e3d_mf_tuning(const ibem_e3d_batch* batch, int* slic
     *slices_wide = b.hsplit_wide;
     const cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) s = cuda_fail(e, "mf_tuning");
+  }
+  mf_batch_free(b);
+  return s;
+}
+
+extern "C" ibem_status ibem_e3d_mf_tile_shape(const ibem_e3d_batch* batch, int* targets_per_cta, int* persistent,
+                                              int* slices, void* stream) {
+  if (batch && batch->axes_dev) return fail(IBEM_ERR_ARG, "matrix-free products and the learned preconditioner take spheres; solve ellipsoid batches with ibem_e3d_batch_dense_solve");
+  if (!batch || !targets_per_cta || !persistent || !slices) return fail(IBEM_ERR_ARG, "mf_tile_shape: bad arguments");
+  cudaStream_t st = as_stream(stream);
+  MfBatch b;
+  ibem_status s = mf_batch_init(b, *batch, st);
+  if (!s) s = mf_tune(b, st);
+  if (!s) {
+    *targets_per_cta = 64 << b.tshape;
+    *persistent = b.persist;
+    *slices = b.hsplit;
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) s = cuda_fail(e, "mf_tile_shape");
   }
   mf_batch_free(b);
   return s;

@@ -65,7 +65,18 @@ struct MfBatch {
                               // centres (position -> particle), used by the split FP64 product
   int hsplit = 1;      // source slices per target tile, FP32 product (autotuned)
   int hsplit_wide = 1; // the same for the double-float and FP64 products (~255 registers)
+  // FP32 product (the GMRES operator): tile shape and launch form, picked by the autotuner
+  MfTile* tiles_s[3] = {nullptr, nullptr, nullptr};   // tiles of 64, 128 and 256 targets
+  int ntiles_s[3] = {0, 0, 0};
+  int tshape = 1;             // index of the tile shape (64 << tshape targets per CTA)
+  int persist = 0;            // 1: persistent CTAs over a cost-sorted list of (tile, slice)
+  int2* work = nullptr;       // that list (persist only)
+  int nwork = 0, persist_ctas = 0;
 };
+
+// Sets the FP32 product's tile shape (0, 1, 2: 64, 128, 256 targets per CTA), source slices
+// and launch form; builds the persistent form's work list.
+ibem_status mf_set_f32_shape(MfBatch& b, int tshape, int hsplit, int persist, cudaStream_t st);
 
 ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st);
 // Source-slice counts of the products for this batch's shape, from the autotuner's table

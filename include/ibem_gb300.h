@@ -234,6 +234,10 @@ typedef struct {
   int max_outer;      /* FP64 refinement steps (0 = 8) */
   double tol;         /* target rel_residual (0 = 1e-10) */
   double inner_tol;   /* residual reduction asked of each FP32 GMRES solve (0 = 1e-5) */
+  int stepwise;       /* 0: the Arnoldi steps of each GMRES cycle run as one launch of a
+                       * captured CUDA graph (a device-side while loop: no host round trip
+                       * per step); 1: each step launched from the host, which reads the
+                       * count of still-active realisations after it */
 } ibem_mf_options;
 
 typedef struct {
@@ -251,7 +255,8 @@ typedef struct {
  * realisations of 4,096 particles or more FP64 for the sources within 8 radii of a warp's
  * 32 targets and double-float beyond, within 1e-12 of FP64; FP64 throughout below that);
  * 65: every pair in FP64; 48: double-float (FP32 pairs, ~48 bits, several times faster on
- * GB300); 32: FP32, about 1e-6 relative.  x_dev, y_dev: 24 * seg_begin[nseg] doubles. */
+ * GB300); 32: FP32, about 1e-6 relative, in the tile shape the autotuner picks for the
+ * solver (ibem_e3d_mf_tile_shape).  x_dev, y_dev: 24 * seg_begin[nseg] doubles. */
 ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int precision, const double* x_dev,
                                double* y_dev, void* stream);
 
@@ -274,6 +279,14 @@ ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const double* b_dev, 
  * No reference counterpart.  Synchronous. */
 ibem_status ibem_e3d_mf_tuning(const ibem_e3d_batch* batch, int* slices_fp32, int* slices_wide,
                                void* stream);
+
+/* The FP32 product's tile shape the same autotuner picks (it times every candidate of the
+ * shape class once): targets per CTA (64, 128 or 256), launch form (0: one CTA per (tile,
+ * source slice); 1: persistent CTAs, as many as fit on the GPU, over the (tile, slice)
+ * items sorted by decreasing cost) and source slices.  No reference counterpart.
+ * Synchronous. */
+ibem_status ibem_e3d_mf_tile_shape(const ibem_e3d_batch* batch, int* targets_per_cta, int* persistent,
+                                   int* slices, void* stream);
 
 /* Far-field right-hand sides of a batch (ibem_e3d_farfield_rhs per realisation, layout 24). */
 ibem_status ibem_e3d_batch_farfield_rhs(const ibem_e3d_batch* batch, const double* sig_inf,

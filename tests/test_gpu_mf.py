@@ -295,6 +295,64 @@ def test_batched_edge_cases_all_preconditioners(B):
             assert reps[s].rel_residual <= 1e-11
 
 
+def test_graph_cycles_match_stepwise_launches(B):
+    """GMRES cycles as one captured CUDA graph launch each (a device-side while loop over
+    the Arnoldi steps) against the same solve launched step by step from the host: the same
+    iterates up to the products' atomic summation order (solutions within 1e-9, Arnoldi step
+    counts within one), on a ragged batch with every preconditioner, restarts included
+    (restart 8), and the launch count includes the kernels the graphs ran."""
+    import ibemproject_gb300 as g
+    from ibemproject_gb300 import cases
+    nums = [1, 17, 60, 130, 210]
+    cs = [cases.farfield_case(num=n, r0=0.012, vf=0.12, grid=0, seed=90 + k, E1=70e9 * (3.0 + 2.0 * k))
+          for k, n in enumerate(nums)]
+    bt = B.DeviceBatch(cs)
+    b = B.farfield_rhs(bt, np.array([0.3, 0.1, 0.0, -0.2, 0.05, 1.0]))
+    params = B.init_params(seed=4)
+    L = g.lib()
+    for pc, pp in ((B.PRECOND_BLOCK_JACOBI, None), (B.PRECOND_LEARNED, params)):
+        for restart in (50, 8):
+            xs, rs = B.solve(bt, b, pc, params=pp, tol=1e-11, restart=restart, stepwise=True)
+            n0 = L.ibem_kernel_launches()
+            xg, rg = B.solve(bt, b, pc, params=pp, tol=1e-11, restart=restart)
+            n1 = L.ibem_kernel_launches()
+            xs, xg = xs.cpu().numpy(), xg.cpu().numpy()
+            steps = sum(r.inner for r in rg)
+            assert n1 - n0 >= steps, (n1 - n0, steps)   # at least one kernel per Arnoldi step
+            for s in range(len(cs)):
+                rows = bt.seg_rows(s)
+                assert scaled_err(xg[rows], xs[rows]) < 1e-9, (pc, restart, s)
+                assert rg[s].rel_residual <= 1e-11 and rs[s].rel_residual <= 1e-11
+                assert abs(rg[s].inner - rs[s].inner) <= 1, (pc, restart, s, rg[s].inner, rs[s].inner)
+
+
+@pytest.mark.parametrize("shape", ["0,0,1", "0,1,3", "1,0,2", "1,1,1", "2,0,1", "2,1,4"])
+def test_fp32_product_every_tile_shape(B, shape, monkeypatch):
+    """The FP32 product in every tile shape and launch form the autotuner chooses from (64,
+    128 and 256 targets per CTA; one CTA per (tile, slice) or persistent CTAs over the
+    cost-sorted work list; several source slices) against the assembled matrix, on a ragged
+    batch (realisations of 1, 70 and 300 spheres, partly filled tiles), with a solve."""
+    import torch
+    monkeypatch.setenv("IBEM_MF_F32_SHAPE", shape)
+    cs = small_cases([1, 70, 300], seed=17, contrast=[4.0, 9.0, 14.0])
+    bt = B.DeviceBatch(cs)
+    assert B.tile_shape(bt) == (64 << int(shape[0]), int(shape[2]), min(int(shape[4]), (300 + 31) // 32))
+    rng = np.random.default_rng(8)
+    dr, dc = bt.scalings()
+    x = torch.from_numpy(rng.standard_normal(bt.N) * dc).cuda()
+    y32 = B.matvec(bt, x, 32).cpu().numpy()
+    for s, c in enumerate(cs):
+        rows = bt.seg_rows(s)
+        A = B.dense_system(c).cpu().numpy().T
+        ref = A @ x.cpu().numpy()[rows]
+        assert rel(dr[rows] * y32[rows], dr[rows] * ref) < 2e-5, (shape, s)
+    b = B.farfield_rhs(bt, np.array([0, 0, 0, 0, 0, 1.0]))
+    xs, reps = B.solve(bt, b, B.PRECOND_BLOCK_JACOBI, tol=1e-11)
+    xr = B.dense_solve(cs[2], b[bt.seg_rows(2)]).cpu().numpy()
+    assert scaled_err(xs.cpu().numpy()[bt.seg_rows(2)], xr) < 1e-8
+    assert all(r.rel_residual <= 1e-11 for r in reps)
+
+
 def test_autotuner_picks_valid_cached_shapes(B):
     """The launch-shape autotuner: slice counts within [1, sources / 32], the same on a
     second call (cached per shape class), and solves with the tuned shapes stay exact."""
@@ -304,6 +362,9 @@ def test_autotuner_picks_valid_cached_shapes(B):
     cap = max(1, (300 + 31) // 32)
     assert 1 <= f <= cap and 1 <= w <= cap
     assert B.tuning(bt) == (f, w)
+    t, p, h = B.tile_shape(bt)
+    assert t in (64, 128, 256) and p in (0, 1) and 1 <= h <= cap
+    assert B.tile_shape(bt) == (t, p, h)
     b = B.farfield_rhs(bt, np.array([0, 0, 0, 0, 0, 1.0]))
     x, reps = B.solve(bt, b, B.PRECOND_BLOCK_JACOBI, tol=1e-11)
     rows = bt.seg_rows(0)
