@@ -83,8 +83,8 @@ IBEM_HD IBEM_INLINE void jzero(Jet<T, K>& o) {
 }
 
 // Product tables: the (alpha, beta) decompositions of every output monomial gamma,
-// grouped by gamma; `last` marks the final term of a group.  Built at compile time; the
-// device reads them from constant memory (every thread of a warp reads the same entry).
+// grouped by gamma; `last` marks the final term of a group.  Built at compile time (the
+// unrolled products below index their operands with its entries as constants).
 template <int K>
 struct MulTab {
   static constexpr int NT = K == 3 ? 84 : (K == 4 ? 210 : 1);
@@ -92,7 +92,7 @@ struct MulTab {
 };
 
 template <int K>
-constexpr MulTab<K> make_multab() {
+IBEM_HD constexpr MulTab<K> make_multab() {
   MulTab<K> t{};
   int n = 0;
   for (int d = 0; d <= K; ++d)
@@ -149,36 +149,40 @@ IBEM_HD IBEM_INLINE const ShiftTab<K>& shifttab() {
 #endif
 }
 
-constexpr MulTab<3> kMulTab3 = make_multab<3>();
-constexpr MulTab<4> kMulTab4 = make_multab<4>();
+// o = w_old * o + w * a * b  (o must not alias a or b).  One out-of-line copy per type and
+// order, fully unrolled over the product table (a compile-time constant): both operands are
+// read once into registers and every term indexes them with constant indices, instead of
+// two loads per term from the caller's local memory.
 #ifdef __CUDACC__
-static __constant__ MulTab<3> kMulTab3Dev = make_multab<3>();
-static __constant__ MulTab<4> kMulTab4Dev = make_multab<4>();
-#endif
-
-template <int K>
-IBEM_HD IBEM_INLINE const MulTab<K>& multab() {
-#ifdef __CUDA_ARCH__
-  if constexpr (K == 3) return kMulTab3Dev; else return kMulTab4Dev;
+#define IBEM_NOINLINE __noinline__
 #else
-  if constexpr (K == 3) return kMulTab3; else return kMulTab4;
+#define IBEM_NOINLINE __attribute__((noinline))
 #endif
-}
-
-// o = w_old * o + w * a * b  (o must not alias a or b)
 template <typename T, int K>
-IBEM_HD inline void jmul_acc(T keep, T w, const Jet<T, K>& a, const Jet<T, K>& b, Jet<T, K>& o) {
+IBEM_HD IBEM_NOINLINE void jmul_acc_ptr(T keep, T w, const T* __restrict__ a, const T* __restrict__ b,
+                                        T* __restrict__ o) {
   static_assert(K == 3 || K == 4, "jets of order 3 or 4");
-  const MulTab<K>& tb = multab<K>();
+  constexpr MulTab<K> tb = make_multab<K>();
+  constexpr int N = nmono(K);
+  T av[N], bv[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    av[i] = a[i];
+    bv[i] = b[i];
+  }
   T acc = T(0);
-#pragma unroll 1
+#pragma unroll
   for (int t = 0; t < MulTab<K>::NT; ++t) {
-    acc += a.c[tb.a[t]] * b.c[tb.b[t]];
+    acc += av[tb.a[t]] * bv[tb.b[t]];
     if (tb.last[t]) {
-      o.c[tb.g[t]] = keep * o.c[tb.g[t]] + w * acc;
+      o[tb.g[t]] = keep * o[tb.g[t]] + w * acc;
       acc = T(0);
     }
   }
+}
+template <typename T, int K>
+IBEM_HD IBEM_INLINE void jmul_acc(T keep, T w, const Jet<T, K>& a, const Jet<T, K>& b, Jet<T, K>& o) {
+  jmul_acc_ptr<T, K>(keep, w, a.c, b.c, o.c);
 }
 
 // o = a * b (o must not alias a or b)
