@@ -66,8 +66,9 @@ def parse():
     ap.add_argument("--ellipsoids", type=int, default=4000, help="ellipsoids of the mixed-form measurement (0: skip)")
     ap.add_argument("--ell-plain", type=int, default=1000,
                     help="ellipsoids of the plain-FP64 vs mixed comparison (0: skip)")
-    ap.add_argument("--quad-form", default="bj", choices=["bj", "mixed"],
-                    help="solver form of the batch's quadratic realisations: block-Jacobi GMRES or FP32 LU + GMRES-IR")
+    ap.add_argument("--quad-form", default="mf", choices=["mf", "bj", "mixed"],
+                    help="solver of the batch's quadratic realisations: matrix-free block-Jacobi GMRES (layout 60, "
+                         "no matrices), or dense: block-Jacobi GMRES or FP32 LU + GMRES-IR")
     return ap.parse_args()
 
 
@@ -352,11 +353,12 @@ def run_batched(args, dev, params):
     unknowns per sphere) and half with quadratic (60), ellipsoids linear; uniaxial remote
     stress.  One step = right-hand sides, the linear sphere realisations in one batched
     matrix-free solve (learned preconditioner, FP64 refinement to relative residual 1e-10),
-    the quadratic sphere and the ellipsoid realisations assembled (FP64 pair blocks) and
-    solved one after another to scaled backward error 1e-12 (--quad-form bj: FP64 refinement
-    of FP32-product GMRES with per-particle block-Jacobi; mixed: FP32 LU with split-BF16
-    tensor-core updates and FP64 GMRES-IR), and the effective moduli of all.  Reports
-    realisations per second."""
+    the quadratic sphere realisations in one batched matrix-free solve of layout 60
+    (block-Jacobi, the same refinement; --quad-form bj / mixed: assembled and solved densely
+    like the ellipsoids), the ellipsoid realisations assembled (FP64 pair blocks) and solved
+    one after another to scaled backward error 1e-12 (FP64 refinement of FP32-product GMRES
+    with per-particle block-Jacobi), and the effective moduli of all.  Reports realisations per
+    second."""
     import torch
     import ibemproject_gb300 as g
     from ibemproject_gb300 import batch as B
@@ -379,7 +381,7 @@ def run_batched(args, dev, params):
     be = B.DeviceBatch([cs[i] for i in ei], device=dev) if ei.size else None
     sig = np.array([0, 0, 0, 0, 0, 1.0])
     stream = torch.cuda.current_stream(dev)
-    qform = g.SOLVE_GMRES_BJ if args.quad_form == "bj" else g.SOLVE_MIXED_IR
+    qform = g.SOLVE_MIXED_IR if args.quad_form == "mixed" else g.SOLVE_GMRES_BJ
 
     def step():
         out = {}
@@ -394,7 +396,10 @@ def run_batched(args, dev, params):
         for key, bt, idx in (("quad", bq, qi), ("ell", be, ei)):
             if bt is not None:
                 b = B.farfield_rhs(bt, sig)
-                x, reps = B.dense_batch_solve(bt, b, qform, tol=1e-12)
+                if key == "quad" and args.quad_form == "mf":
+                    x, reps = B.solve(bt, b, B.PRECOND_BLOCK_JACOBI)
+                else:
+                    x, reps = B.dense_batch_solve(bt, b, g.SOLVE_GMRES_BJ if key == "ell" else qform, tol=1e-12)
                 e, _ = B.effective_modulus(bt, x, sig, volume=vol[idx])
                 out[key] = (x, reps, e, b)
             ev[2 if key == "quad" else 3].record(stream)
@@ -441,14 +446,18 @@ def run_batched(args, dev, params):
         if key in out:
             e_all[idx] = out[key][2]
     ratio = e_all / E0
+    quad_mf = args.quad_form == "mf"
     lin_reps = out["lin"][1] if bl is not None else []
-    dense_reps = (out["quad"][1] if bq is not None else []) + (out["ell"][1] if be is not None else [])
+    quad_reps = out["quad"][1] if bq is not None else []
+    dense_reps = ([] if quad_mf else quad_reps) + (out["ell"][1] if be is not None else [])
     return {"workload": (f"{args.batch} realisations, U[50,500] particles, spheres (r~U[0.8,1.2]*0.008) or ellipsoids "
                          "(a1=0.008, a2=a1 U[0.5,1], a3=a1 U[0.25,1]) 50/50, vf U[10%,30%], E1/E0 U[2,20]; spheres half "
-                         "linear (24/sphere, matrix-free learned GMRES) and half quadratic (60/sphere), ellipsoids "
-                         "linear; quadratic and ellipsoid realisations assembled and solved by " +
-                         ("block-Jacobi FP32-product GMRES + FP64 refinement" if args.quad_form == "bj" else
-                          "FP32 LU + BF16x3 + FP64 GMRES-IR") + ", far-field sigma33"),
+                         "linear (24/sphere, matrix-free learned GMRES) and half quadratic (60/sphere, " +
+                         ("matrix-free block-Jacobi GMRES" if quad_mf else
+                          "assembled, block-Jacobi FP32-product GMRES + FP64 refinement" if args.quad_form == "bj" else
+                          "assembled, FP32 LU + BF16x3 + FP64 GMRES-IR") +
+                         "), ellipsoids linear (assembled, block-Jacobi FP32-product GMRES + FP64 refinement), "
+                         "far-field sigma33"),
             "value": args.batch / (ms / 1e3), "unit": "realisations/s", "ms_per_batch": ms,
             "ms_linear_spheres": ms_lin, "ms_quadratic_spheres": ms_quad, "ms_ellipsoids": ms_ell,
             "realisations_linear_spheres": int(li.size), "realisations_quadratic_spheres": int(qi.size),
@@ -457,6 +466,9 @@ def run_batched(args, dev, params):
             "arnoldi_steps_max": max((r.inner for r in lin_reps), default=0),
             "refinement_steps_max": max((r.outer for r in lin_reps), default=0),
             "rel_residual_max": max((r.rel_residual for r in lin_reps), default=0.0),
+            "quadratic_matrix_free": quad_mf,
+            "quadratic_arnoldi_steps_max": max((r.inner for r in quad_reps), default=0) if quad_mf else None,
+            "quadratic_rel_residual_max": max((r.rel_residual for r in quad_reps), default=0.0) if quad_mf else None,
             "dense_backward_error_max": max((r.backward_error for r in dense_reps), default=0.0),
             "dense_gmres_iterations_max": max((r.iterations for r in dense_reps), default=0),
             "rel_err_vs_plain_fp64": errs,

@@ -124,6 +124,9 @@ SIGNATURES = {
     "ibem_e3d_batch_farfield_rhs": (_int, [ctypes.POINTER(Batch), _c_dp, _vp, _vp]),
     "ibem_e3d_mf_tuning": (_int, [ctypes.POINTER(Batch), _c_ip, _c_ip, _vp]),
     "ibem_e3d_mf_tile_shape": (_int, [ctypes.POINTER(Batch), _c_ip, _c_ip, _c_ip, _vp]),
+    "ibem_e3d_mf_solve_layout": (_int, [ctypes.POINTER(Batch), _int, _vp, _vp, _int, _vp, ctypes.POINTER(MfOptions),
+                                        ctypes.POINTER(MfReport), _vp]),
+    "ibem_e3d_mf_matvec_layout": (_int, [ctypes.POINTER(Batch), _int, _int, _vp, _vp, _vp]),
     "ibem_e3d_effective_modulus": (_int, [ctypes.POINTER(Batch), _vp, _c_dp, _c_dp, _c_dp, _c_dp, _vp]),
     "ibem_e3d_batch_farfield_rhs_layout": (_int, [ctypes.POINTER(Batch), _int, _c_dp, _vp, _vp]),
     "ibem_e3d_batch_dense_solve": (_int, [ctypes.POINTER(Batch), _int, _int, _vp, _vp, _dbl,

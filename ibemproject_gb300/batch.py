@@ -29,12 +29,12 @@ def _ptr(t) -> int:
     return t.data_ptr()
 
 
-def _linear(batch) -> None:
+def _linear(batch, layouts=(NU,)) -> None:
     if getattr(batch, "ellipsoids", False):
         raise ValueError("the matrix-free solver and the learned preconditioner take spheres; "
                          "solve ellipsoid batches with dense_batch_solve")
-    if batch.layout != NU:
-        raise ValueError(f"the matrix-free solver and the learned preconditioner take layout {NU}, "
+    if batch.layout not in layouts:
+        raise ValueError(f"this matrix-free call takes layout {' or '.join(str(v) for v in layouts)}, "
                          f"not {batch.layout}")
 
 
@@ -85,8 +85,9 @@ class DeviceBatch:
     def scalings(self):
         """(Dr, Dc) as host arrays of length N."""
         mu0 = np.repeat([c.E0 / (2 * (1 + c.nu0)) for c in self.cases], np.diff(self.seg_begin))
-        o = np.zeros(NU)
+        o = np.zeros(self.layout)   # eigenstrain order of each unknown
         o[6:] = 1.0
+        o[24:] = 2.0
         a = self.radius_host[:, None]
         dr = (a ** o) / mu0[:, None]
         dc = a ** (-o)
@@ -130,10 +131,11 @@ def dense_batch_solve(batch: DeviceBatch, b, form: int = SOLVE_MIXED_IR, tol: fl
 
 
 def matvec(batch: DeviceBatch, x, precision: int = 64):
-    _linear(batch)
+    """y = A x without storing A (ibem_e3d_mf_matvec_layout, the batch's layout 24 or 60)."""
+    _linear(batch, (NU, 60))
     import torch
     y = torch.empty_like(x)
-    check(lib().ibem_e3d_mf_matvec(batch.ref(), precision, _ptr(x), _ptr(y), None))
+    check(lib().ibem_e3d_mf_matvec_layout(batch.ref(), batch.layout, precision, _ptr(x), _ptr(y), None))
     torch.cuda.synchronize()
     return y
 
@@ -141,16 +143,18 @@ def matvec(batch: DeviceBatch, x, precision: int = 64):
 def solve(batch: DeviceBatch, b, precond: int = PRECOND_BLOCK_JACOBI, params=None, tol: float = 1e-10,
           inner_tol: float = 1e-5, restart: int = 50, max_outer: int = 8, max_cycles: int = 20, x=None,
           stepwise: bool = False):
-    """Matrix-free solve of every realisation: returns (x, list of MfReport).  stepwise: launch
-    each Arnoldi step from the host instead of one captured CUDA graph per GMRES cycle."""
-    _linear(batch)
+    """Matrix-free solve of every realisation (the batch's layout: 24, or 60 with the
+    block-Jacobi preconditioner): returns (x, list of MfReport).  stepwise: launch each Arnoldi
+    step from the host instead of one captured CUDA graph per GMRES cycle."""
+    _linear(batch, (NU, 60))
     import torch
     if x is None:
         x = torch.zeros_like(b)
     reps = (MfReport * batch.nseg)()
     opt = MfOptions(restart, max_cycles, max_outer, tol, inner_tol, int(stepwise))
-    check(lib().ibem_e3d_mf_solve(batch.ref(), _ptr(b), _ptr(x), precond,
-                                  _ptr(params) if params is not None else None, ctypes.byref(opt), reps, None))
+    check(lib().ibem_e3d_mf_solve_layout(batch.ref(), batch.layout, _ptr(b), _ptr(x), precond,
+                                         _ptr(params) if params is not None else None, ctypes.byref(opt), reps,
+                                         None))
     return x, list(reps)
 
 

@@ -19,7 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = [
     "csrc/sphere24.cu", "csrc/sphere60.cu", "csrc/sphere78.cu", "csrc/bem.cu",
     "csrc/solver.cu", "csrc/gemm_tc.cu", "csrc/capi.cu", "csrc/prof.cu", "csrc/mf.cu", "csrc/gnn.cu",
-    "csrc/ellipsoid.cu",
+    "csrc/ellipsoid.cu", "csrc/mf60.cu",
     "host/ibem_plugins.cpp", "host/microstructure.cpp", "host/sidecar.cpp",
 ]
 

@@ -679,6 +679,15 @@ IBEM_HD inline SphMatF sph_matf_init(const SphMat& m) {
 """
 
 
+F60_HEAD = """// GENERATED by ibemproject_gb300/codegen.py -- do not edit by hand.
+// FP32 variant of the layout-60 sphere blocks for the matrix-free solver of quadratic
+// realisations, called in coordinates scaled by the source radius (a = 1).  Same derivation
+// as gen_sphere60.cuh.
+#pragma once
+#include "gen_sphere24_f32.cuh"   // SphMatF
+"""
+
+
 def to_f32(src: str, old_name: str, new_name: str) -> str:
     """Single-precision copy of a generated block function: the same straight-line
     arithmetic with float operands and literals."""
@@ -722,10 +731,35 @@ def generate(out_dir: str | None = None) -> dict:
             for ro in range(3):
                 rows = [r for r in range(len(U)) if U[r][0] == ro]
                 parts.append(gen_block_function(f"sph_block{lay}_c{co}_r{ro}", lay, rows, cols))
+        nblk = len(parts) - 1
         parts.append(gen_field_function(f"sph_field{lay}", lay))
         parts.append(gen_node_function(f"sph_node{lay}", lay))
         parts.append(gen_self_function(f"sph_self{lay}", lay))
         files[f"gen_sphere{lay}.cuh"] = "\n\n".join(parts) + "\n"
+        if lay == 60:
+            # FP32 blocks of the layout-60 matrix-free products (scaled coordinates, a = 1): the
+            # large sub-blocks split into groups of 6 columns (one symmetric pair (m, n) each),
+            # so that each kernel's straight-line code keeps its values in registers: the
+            # order-1 columns of the order-2 rows in 3 groups, the order-2 columns of the
+            # order-1 and order-2 rows in 6
+            fparts = [F60_HEAD]
+            def add(name, ro, cols):
+                src = gen_block_function(name, 60, [r for r in range(len(U)) if U[r][0] == ro], cols)
+                fparts.append(to_f32(src, name, name.replace("block60", "block60f")))
+            for ro in range(3):
+                for co in range(3):
+                    cols = [c for c in range(len(U)) if U[c][0] == co]
+                    if co == 2 and ro >= 1:
+                        for g, pr in enumerate(SYM_PAIRS):
+                            add(f"sph_block60_c2g{g}_r{ro}", ro, [c for c in cols if (U[c][1], U[c][2]) == pr])
+                    elif co == 1 and ro == 2:
+                        for g in range(3):
+                            prs = SYM_PAIRS[2 * g:2 * g + 2]
+                            add(f"sph_block60_c1g{g}_r2", ro, [c for c in cols if (U[c][1], U[c][2]) in prs])
+                    else:
+                        add(f"sph_block60m_c{co}_r{ro}", ro, cols)
+            fparts.append(to_f32(gen_self_function("sph_self60", 60), "sph_self60", "sph_self60f"))
+            files["gen_sphere60_f32.cuh"] = "\n\n".join(fparts) + "\n"
     # boundary stress kernels: one function per (order, W tuple, dof) and the
     # post-processing variant (order 0, all dofs)
     parts = [FILE_HEAD]

@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(kMfThreads)
 }
 
 // Geometry in the FP32 layout, scalings, segment of every particle.
-__global__ void k_mf_prep(int num, const double* __restrict__ cen, const double* __restrict__ rad,
+__global__ void k_mf_prep(int nu, int num, const double* __restrict__ cen, const double* __restrict__ rad,
                           const int* __restrict__ seg_of, const SphMat* __restrict__ mats, float4* __restrict__ gh,
                           float4* __restrict__ gl, double* __restrict__ dr, double* __restrict__ dc) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -357,9 +357,12 @@ __global__ void k_mf_prep(int num, const double* __restrict__ cen, const double*
   gh[p] = make_float4(hi[0], hi[1], hi[2], (float)a);
   gl[p] = make_float4(lo[0], lo[1], lo[2], (float)(1.0 / a));
   const double imu = 1.0 / mats[seg_of[p]].mu0;
-  for (int r = 0; r < kMfNu; ++r) {
-    dr[(int64_t)kMfNu * p + r] = (r >= 6 ? a : 1.0) * imu;
-    dc[(int64_t)kMfNu * p + r] = r >= 6 ? 1.0 / a : 1.0;
+  // rows / columns of eigenstrain order o (0: 6, 1: 18, 2: 36 unknowns): a^o / mu0, a^-o
+  for (int r = 0; r < nu; ++r) {
+    const int o = r < 6 ? 0 : (r < 24 ? 1 : 2);
+    const double ao = o == 0 ? 1.0 : (o == 1 ? a : a * a);
+    dr[(int64_t)nu * p + r] = ao * imu;
+    dc[(int64_t)nu * p + r] = 1.0 / ao;
   }
 }
 
@@ -476,11 +479,11 @@ __global__ void k_precond_apply(int num, const float* __restrict__ D, const floa
 constexpr int kDotRows = 8, kDotThreads = 256;
 template <class TV>
 __global__ void __launch_bounds__(kDotThreads)
-    k_seg_dots(const int* __restrict__ seg_begin, int nv, const TV* __restrict__ V, int64_t ldv,
+    k_seg_dots(int nu, const int* __restrict__ seg_begin, int nv, const TV* __restrict__ V, int64_t ldv,
                const TV* __restrict__ w, double* __restrict__ out, int ldo, const int* __restrict__ kdev = nullptr) {
   if (kdev) nv += *kdev;
   const int seg = blockIdx.x;
-  const int64_t r0 = (int64_t)kMfNu * seg_begin[seg], r1 = (int64_t)kMfNu * seg_begin[seg + 1];
+  const int64_t r0 = (int64_t)nu * seg_begin[seg], r1 = (int64_t)nu * seg_begin[seg + 1];
   const int64_t base = r0 + (int64_t)blockIdx.y * kDotThreads * kDotRows;
   if (base >= r1) return;
   TV wr[kDotRows];
@@ -511,13 +514,13 @@ __global__ void __launch_bounds__(kDotThreads)
 }
 
 // w[row] -= sum_j h[seg(row) * ldh + j] V_j[row], j < nv (+ *kdev)
-__global__ void k_seg_sub(int64_t N, const int* __restrict__ seg_of, int nv, const float* __restrict__ V, int64_t ldv,
+__global__ void k_seg_sub(int nu, int64_t N, const int* __restrict__ seg_of, int nv, const float* __restrict__ V, int64_t ldv,
                           const double* __restrict__ h, int ldh, float* __restrict__ w,
                           const int* __restrict__ kdev = nullptr) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= N) return;
   if (kdev) nv += *kdev;
-  const double* hs = h + (int64_t)seg_of[r / kMfNu] * ldh;
+  const double* hs = h + (int64_t)seg_of[r / nu] * ldh;
   float s = w[r];
   for (int j = 0; j < nv; ++j) s -= (float)hs[j] * V[(int64_t)j * ldv + r];
   w[r] = s;
@@ -526,13 +529,13 @@ __global__ void k_seg_sub(int64_t N, const int* __restrict__ seg_of, int nv, con
 // y[row] (+)= scale[seg(row)] * x[row] (FP32 <- FP64 / FP32); with kdev, y is column
 // *kdev + 1 of a basis with column stride ystride
 template <class TX, class TY>
-__global__ void k_seg_scale(int64_t N, const int* __restrict__ seg_of, const double* __restrict__ scale,
+__global__ void k_seg_scale(int nu, int64_t N, const int* __restrict__ seg_of, const double* __restrict__ scale,
                             const TX* __restrict__ x, TY* __restrict__ y, int add, const int* __restrict__ kdev = nullptr,
                             int64_t ystride = 0) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= N) return;
   if (kdev) y += (int64_t)(*kdev + 1) * ystride;
-  const double v = scale[seg_of[r / kMfNu]] * (double)x[r];
+  const double v = scale[seg_of[r / nu]] * (double)x[r];
   y[r] = add ? (TY)((double)y[r] + v) : (TY)v;
 }
 
@@ -636,13 +639,13 @@ __global__ void k_cycle_start(int nseg, int m, Krylov K, const int* __restrict__
 }
 
 // x[row] += sum_j y[seg][j] V_j[row], j < nv (+ *kdev)
-__global__ void k_seg_combine(int64_t N, const int* __restrict__ seg_of, int nv, const float* __restrict__ V,
+__global__ void k_seg_combine(int nu, int64_t N, const int* __restrict__ seg_of, int nv, const float* __restrict__ V,
                               int64_t ldv, const double* __restrict__ y, int ldy, float* __restrict__ x,
                               const int* __restrict__ kdev = nullptr) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= N) return;
   if (kdev) nv += *kdev;
-  const double* ys = y + (int64_t)seg_of[r / kMfNu] * ldy;
+  const double* ys = y + (int64_t)seg_of[r / nu] * ldy;
   double s = 0;
   for (int j = 0; j < nv; ++j) s += ys[j] * (double)V[(int64_t)j * ldv + r];
   x[r] += (float)s;
@@ -683,10 +686,10 @@ __global__ void k_sub64(int64_t n, const double* __restrict__ a, const double* _
   if (i < n) out[i] = a[i] - b[i];
 }
 // out = a - b (FP64) on the rows of realisations with done == 0
-__global__ void k_sub64_masked(int64_t n, const int* __restrict__ seg_of, const int* __restrict__ done,
+__global__ void k_sub64_masked(int nu, int64_t n, const int* __restrict__ seg_of, const int* __restrict__ done,
                                const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n && !done[seg_of[i / kMfNu]]) out[i] = a[i] - b[i];
+  if (i < n && !done[seg_of[i / nu]]) out[i] = a[i] - b[i];
 }
 // y = x / d (FP64)
 __global__ void k_div64(int64_t n, const double* __restrict__ x, const double* __restrict__ d, double* __restrict__ y) {
@@ -740,7 +743,9 @@ inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t
 }  // namespace
 
 // ------------------------------------------------------------------ batch set-up
-ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st) {
+ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st, int layout) {
+  if (layout != 24 && layout != 60) return fail(IBEM_ERR_ARG, "mf: layout 24 or 60");
+  b.nu = layout;
   if (in.nseg <= 0 || !in.seg_begin || !in.centers_dev || !in.radius_dev || !in.mats)
     return fail(IBEM_ERR_ARG, "mf: bad batch");
   b.st = st;
@@ -755,7 +760,7 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
     b.max_seg = std::max(b.max_seg, n);
   }
   b.num = b.seg_begin_h[in.nseg];
-  b.N = (int64_t)kMfNu * b.num;
+  b.N = (int64_t)b.nu * b.num;
   b.cen = in.centers_dev;
   b.rad = in.radius_dev;
   b.axes = in.axes_dev;
@@ -855,7 +860,7 @@ ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st)
     IBEM_CUDA(cudaMemcpyAsync(b.tiles_s[k], tiles_s[k].data(), sizeof(MfTile) * b.ntiles_s[k], cudaMemcpyHostToDevice,
                               st));
   b.tshape = 1;   // 128 targets per CTA until the autotuner says otherwise
-  ::ibem::count_launch(), k_mf_prep<<<nblk(b.num), 256, 0, st>>>(b.num, b.cen, b.rad, b.seg_of, b.matd, b.gh, b.gl,
+  ::ibem::count_launch(), k_mf_prep<<<nblk(b.num), 256, 0, st>>>(b.nu, b.num, b.cen, b.rad, b.seg_of, b.matd, b.gh, b.gl,
                                                                  b.dr, b.dc);
   IBEM_LAUNCH_CHECK("mf prep");
   // the host vectors above must outlive the copies
@@ -971,11 +976,11 @@ ibem_status mf_tune(MfBatch& b, cudaStream_t st) {
   int dev = 0, sms = 0;
   IBEM_CUDA(cudaGetDevice(&dev));
   IBEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const TuneKey key{log2_bucket(b.ntiles), log2_bucket(b.max_seg), sms};
+  const TuneKey key{log2_bucket(b.ntiles), log2_bucket(b.max_seg), sms * 100 + b.nu};
   const int cap = std::max(1, (b.max_seg + 31) / 32);
   // IBEM_MF_F32_SHAPE="shape,persistent,slices" fixes the FP32 product's launch (tests and
   // measurements of every shape); the wide products keep the batch's initial slice count
-  if (const char* f = std::getenv("IBEM_MF_F32_SHAPE")) {
+  if (const char* f = b.nu == 24 ? std::getenv("IBEM_MF_F32_SHAPE") : nullptr) {
     int ts = 1, pers = 0, h = 1;
     if (std::sscanf(f, "%d,%d,%d", &ts, &pers, &h) == 3 && ts >= 0 && ts < 3 && (pers == 0 || pers == 1) && h >= 1)
       return mf_set_f32_shape(b, ts, std::min(h, cap), pers, st);
@@ -1031,7 +1036,8 @@ ibem_status mf_tune(MfBatch& b, cudaStream_t st) {
   float best_ms = 1e30f;
   for (int ts = 0; ts < 3 && !s; ++ts)
     for (int h : slice_candidates(b.ntiles_s[ts], b.max_seg, sms)) {
-      for (int pers = 0; pers < 2 && !s; ++pers) {
+      if (b.nu == 60 && ts != 1) break;   // the layout-60 products have 128-target tiles only
+      for (int pers = 0; pers < (b.nu == 60 ? 1 : 2) && !s; ++pers) {
         if ((s = mf_set_f32_shape(b, ts, h, pers, st))) break;
         float ms = 0.f;
         if ((s = time_it(false, ms))) break;
@@ -1083,6 +1089,7 @@ void launch_f32(const MfBatch& b, const float* x, float* y, cudaStream_t st, con
 ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_t st, const int* mask, int mask_on) {
   ProfScope ps(PROF_MF_F32, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(float) * b.N, st));
+  if (b.nu == 60) return mf60_apply_f32(b, x, y, st, mask, mask_on);
   if (b.tshape == 0) launch_f32<64>(b, x, y, st, mask, mask_on);
   else if (b.tshape == 2) launch_f32<256>(b, x, y, st, mask, mask_on);
   else launch_f32<128>(b, x, y, st, mask, mask_on);
@@ -1093,6 +1100,7 @@ ibem_status mf_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_
 ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st, const int* mask, int mask_on) {
   ProfScope ps(PROF_MF_F64, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
+  if (b.nu == 60) return mf60_apply_f64(b, x, y, st, mask, mask_on);
   // near chunks in FP64, far chunks (beyond kMfFarRadii radii of the warp's targets) in
   // double-float: their contributions are at most kMfFarRadii^-3 of a near one, so the
   // double-float rounding (~2^-44 per operation) stays far below FP64 level in the sum
@@ -1111,6 +1119,7 @@ ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStrea
 ibem_status mf_apply_f64_all(const MfBatch& b, const double* x, double* y, cudaStream_t st) {
   ProfScope ps(PROF_MF_F64, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
+  if (b.nu == 60) return mf60_apply_f64(b, x, y, st, nullptr, 1);
   ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
       b.tiles, b.seg_begin, nullptr, 1, b.cen, b.rad, b.mats, x, y, b.perm, 0);
   IBEM_LAUNCH_CHECK("mf apply f64 (all pairs)");
@@ -1120,6 +1129,7 @@ ibem_status mf_apply_f64_all(const MfBatch& b, const double* x, double* y, cudaS
 ibem_status mf_apply_df(const MfBatch& b, const double* x, double* y, cudaStream_t st, const int* mask, int mask_on) {
   ProfScope ps(PROF_MF_DF, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
+  if (b.nu == 60) return mf60_apply_f64(b, x, y, st, mask, mask_on);   // no double-float form of layout 60
   ::ibem::count_launch(), k_mf_apply_df<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
       b.tiles, b.seg_begin, mask, mask_on, b.cen, b.rad, b.mats, x, y, b.perm, 0);
   IBEM_LAUNCH_CHECK("mf apply df");
@@ -1166,7 +1176,7 @@ struct MfSolver {
   long long step_kernels = 0;   // kernels in one captured step
   const MfPrecond* graph_pc = nullptr;
   MfSolver(const MfBatch& bb, cudaStream_t s, int mm, bool graphs) : b(bb), st(s), m(mm), N(bb.N), use_graph(graphs) {
-    splits = (int)((kMfNu * (int64_t)b.max_seg + kDotThreads * kDotRows - 1) / (kDotThreads * kDotRows));
+    splits = (int)((b.nu * (int64_t)b.max_seg + kDotThreads * kDotRows - 1) / (kDotThreads * kDotRows));
   }
   ~MfSolver() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -1220,7 +1230,7 @@ struct MfSolver {
   template <class T>
   ibem_status seg_norm2(const T* v, double* n2, cudaStream_t s) {
     IBEM_CUDA(cudaMemsetAsync(n2, 0, sizeof(double) * b.nseg, s));
-    ::ibem::count_launch(), k_seg_dots<T><<<dim3(b.nseg, splits), kDotThreads, 0, s>>>(b.seg_begin, 1, v, 0, v, n2, 1);
+    ::ibem::count_launch(), k_seg_dots<T><<<dim3(b.nseg, splits), kDotThreads, 0, s>>>(b.nu, b.seg_begin, 1, v, 0, v, n2, 1);
     IBEM_LAUNCH_CHECK("seg norm");
     return IBEM_OK;
   }
@@ -1233,6 +1243,14 @@ struct MfSolver {
     if (e != cudaSuccess) s = cuda_fail(e, "gmres: read active count");
     return h;
   }
+  // z = P v (layout 24: the block-sparse preconditioner; layout 60: the realisation's
+  // block-Jacobi block, P.D holding one 60 x 60 block per realisation)
+  ibem_status precond(const MfPrecond& P, const float* v, float* z, const int* kd, int64_t vstride, cudaStream_t s) {
+    if (b.nu == 60) return mf60_precond_apply(b, P.D, v, z, kd, vstride, s);
+    ::ibem::count_launch(), k_precond_apply<<<nblk(N), 256, 0, s>>>(b.num, P.D, P.Q, P.nbr, v, z, kd, vstride);
+    IBEM_LAUNCH_CHECK("preconditioner");
+    return IBEM_OK;
+  }
   // Arnoldi step k on stream s: w = As P v_k, two Gram-Schmidt passes against v_0..v_k,
   // the per-realisation Hessenberg update, v_(k+1) = w / ||w||.  With kd (graph capture) the
   // kernels read k from *kd instead.
@@ -1240,20 +1258,21 @@ struct MfSolver {
     const int S = b.nseg;
     const float* vk = kd ? V : V + (int64_t)k * N;
     const int nv = kd ? 1 : k + 1;   // k_seg_dots / k_seg_sub add *kd
-    ::ibem::count_launch(), k_precond_apply<<<nblk(N), 256, 0, s>>>(b.num, P.D, P.Q, P.nbr, vk, z, kd, kd ? N : 0);
-    ibem_status r = mf_apply_f32(b, z, w, s, K.active, 1);   // converged realisations sit out
+    ibem_status r = precond(P, vk, z, kd, kd ? N : 0, s);
+    if (r) return r;
+    r = mf_apply_f32(b, z, w, s, K.active, 1);   // converged realisations sit out
     if (r) return r;
     ProfScope pg(PROF_GMRES_OTHER, s);
     IBEM_CUDA(cudaMemsetAsync(K.d1, 0, sizeof(double) * 2 * (size_t)S * (m + 1), s));
-    ::ibem::count_launch(), k_seg_dots<float><<<dim3(S, splits), kDotThreads, 0, s>>>(b.seg_begin, nv, V, N, w, K.d1, m + 1, kd);
-    ::ibem::count_launch(), k_seg_sub<<<nblk(N), 256, 0, s>>>(N, b.seg_of, nv, V, N, K.d1, m + 1, w, kd);
-    ::ibem::count_launch(), k_seg_dots<float><<<dim3(S, splits), kDotThreads, 0, s>>>(b.seg_begin, nv, V, N, w, K.d2, m + 1, kd);
-    ::ibem::count_launch(), k_seg_sub<<<nblk(N), 256, 0, s>>>(N, b.seg_of, nv, V, N, K.d2, m + 1, w, kd);
+    ::ibem::count_launch(), k_seg_dots<float><<<dim3(S, splits), kDotThreads, 0, s>>>(b.nu, b.seg_begin, nv, V, N, w, K.d1, m + 1, kd);
+    ::ibem::count_launch(), k_seg_sub<<<nblk(N), 256, 0, s>>>(b.nu, N, b.seg_of, nv, V, N, K.d1, m + 1, w, kd);
+    ::ibem::count_launch(), k_seg_dots<float><<<dim3(S, splits), kDotThreads, 0, s>>>(b.nu, b.seg_begin, nv, V, N, w, K.d2, m + 1, kd);
+    ::ibem::count_launch(), k_seg_sub<<<nblk(N), 256, 0, s>>>(b.nu, N, b.seg_of, nv, V, N, K.d2, m + 1, w, kd);
     if ((r = seg_norm2(w, K.n2, s))) return r;
     IBEM_CUDA(cudaMemsetAsync(K.nactive, 0, sizeof(int), s));
     ::ibem::count_launch(), k_arnoldi_update<<<nblk(S, 128), 128, 0, s>>>(S, m, k, K, kd);
     float* vnext = kd ? V : V + (int64_t)(k + 1) * N;
-    ::ibem::count_launch(), k_seg_scale<float, float><<<nblk(N), 256, 0, s>>>(N, b.seg_of, K.inv, w, vnext, 0, kd,
+    ::ibem::count_launch(), k_seg_scale<float, float><<<nblk(N), 256, 0, s>>>(b.nu, N, b.seg_of, K.inv, w, vnext, 0, kd,
                                                                                kd ? N : 0);
     IBEM_LAUNCH_CHECK("arnoldi step");
     return IBEM_OK;
@@ -1315,7 +1334,7 @@ struct MfSolver {
       if ((s = seg_norm2(r, K.n2))) break;
       IBEM_CUDA(cudaMemsetAsync(K.nactive, 0, sizeof(int), st));
       ::ibem::count_launch(), k_cycle_start<<<nblk(S, 128), 128, 0, st>>>(S, m, K, done, cyc == 0, tolv);
-      ::ibem::count_launch(), k_seg_scale<float, float><<<nblk(N), 256, 0, st>>>(N, b.seg_of, K.inv, r, V, 0);
+      ::ibem::count_launch(), k_seg_scale<float, float><<<nblk(N), 256, 0, st>>>(b.nu, N, b.seg_of, K.inv, r, V, 0);
       IBEM_LAUNCH_CHECK("gmres cycle start");
       const int na = read_nactive(s);
       if (s || na == 0) break;
@@ -1336,9 +1355,9 @@ struct MfSolver {
       // d += P V y
       ::ibem::count_launch(), k_hess_solve<<<nblk(S, 128), 128, 0, st>>>(S, m, K);
       IBEM_CUDA(cudaMemsetAsync(w, 0, sizeof(float) * N, st));
-      ::ibem::count_launch(), k_seg_combine<<<nblk(N), 256, 0, st>>>(N, b.seg_of, graphed ? 0 : k, V, N, K.yv, m, w,
+      ::ibem::count_launch(), k_seg_combine<<<nblk(N), 256, 0, st>>>(b.nu, N, b.seg_of, graphed ? 0 : k, V, N, K.yv, m, w,
                                                                     graphed ? kdev : nullptr);
-      ::ibem::count_launch(), k_precond_apply<<<nblk(N), 256, 0, st>>>(b.num, P.D, P.Q, P.nbr, w, z);
+      if ((s = precond(P, w, z, nullptr, 0, st))) break;
       ::ibem::count_launch(), k_add_f32<<<nblk(N), 256, 0, st>>>(N, z, d);
       IBEM_LAUNCH_CHECK("gmres update");
     }
@@ -1455,7 +1474,7 @@ ibem_status mf_solve(const MfBatch& b, const double* bvec, double* x, const MfPr
       continue;
     }
     if ((s = mf_apply_df(b, xs, y, st, g.done, 0))) break;   // done realisations keep their residual
-    ::ibem::count_launch(), k_sub64_masked<<<nblk(N), 256, 0, st>>>(N, b.seg_of, g.done, bs, y, rs);
+    ::ibem::count_launch(), k_sub64_masked<<<nblk(N), 256, 0, st>>>(b.nu, N, b.seg_of, g.done, bs, y, rs);
     IBEM_LAUNCH_CHECK("mf refinement");
     exact = false;
     if ((s = read_rel())) break;
@@ -1489,12 +1508,18 @@ using namespace ibem;
 
 extern "C" ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int precision, const double* x_dev,
                                           double* y_dev, void* stream) {
+  return ibem_e3d_mf_matvec_layout(batch, 24, precision, x_dev, y_dev, stream);
+}
+
+extern "C" ibem_status ibem_e3d_mf_matvec_layout(const ibem_e3d_batch* batch, int layout, int precision,
+                                                 const double* x_dev, double* y_dev, void* stream) {
   if (batch && batch->axes_dev) return fail(IBEM_ERR_ARG, "matrix-free products and the learned preconditioner take spheres; solve ellipsoid batches with ibem_e3d_batch_dense_solve");
   if (!batch || !x_dev || !y_dev || (precision != 32 && precision != 48 && precision != 64 && precision != 65))
     return fail(IBEM_ERR_ARG, "mf_matvec: bad arguments");
+  if (layout != 24 && layout != 60) return fail(IBEM_ERR_ARG, "mf_matvec: layout 24 or 60");
   cudaStream_t st = as_stream(stream);
   MfBatch b;
-  ibem_status s = mf_batch_init(b, *batch, st);
+  ibem_status s = mf_batch_init(b, *batch, st, layout);
   if (!s) {
     if (precision != 32) {
       double *xs = nullptr, *ys = nullptr;
@@ -1543,6 +1568,15 @@ extern "C" ibem_status ibem_e3d_mf_matvec(const ibem_e3d_batch* batch, int preci
 extern "C" ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const double* b_dev, double* x_dev,
                                          ibem_precond pc, const float* gnn_params_dev, const ibem_mf_options* opt,
                                          ibem_mf_report* reports, void* stream) {
+  return ibem_e3d_mf_solve_layout(batch, 24, b_dev, x_dev, pc, gnn_params_dev, opt, reports, stream);
+}
+
+extern "C" ibem_status ibem_e3d_mf_solve_layout(const ibem_e3d_batch* batch, int layout, const double* b_dev,
+                                                double* x_dev, ibem_precond pc, const float* gnn_params_dev,
+                                                const ibem_mf_options* opt, ibem_mf_report* reports, void* stream) {
+  if (layout != 24 && layout != 60) return fail(IBEM_ERR_ARG, "mf_solve: layout 24 or 60");
+  if (layout == 60 && pc != IBEM_PRECOND_BLOCK_JACOBI)
+    return fail(IBEM_ERR_ARG, "mf_solve: layout 60 takes the block-Jacobi preconditioner");
   if (batch && batch->axes_dev) return fail(IBEM_ERR_ARG, "matrix-free products and the learned preconditioner take spheres; solve ellipsoid batches with ibem_e3d_batch_dense_solve");
   if (!batch || !b_dev || !x_dev || !reports) return fail(IBEM_ERR_ARG, "mf_solve: bad arguments");
   if (pc != IBEM_PRECOND_BLOCK_JACOBI && pc != IBEM_PRECOND_LEARNED && pc != IBEM_PRECOND_NEUMANN)
@@ -1561,16 +1595,19 @@ extern "C" ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const doub
   for (auto& e : ev) IBEM_CUDA(cudaEventCreate(&e));
   IBEM_CUDA(cudaEventRecord(ev[0], st));
   MfBatch b;
-  ibem_status s = mf_batch_init(b, *batch, st);
+  ibem_status s = mf_batch_init(b, *batch, st, layout);
   if (!s) s = mf_tune(b, st);
   MfPrecond P;
   if (!s) {
-    const cudaError_t e = alloc_async((void**)&P.D, sizeof(float) * kMfNu * kMfNu * (size_t)b.num, st);
+    // layout 24: one 24 x 24 block per particle (the learned and Neumann forms change them);
+    // layout 60: one 60 x 60 block per realisation
+    const size_t nblocks = layout == 60 ? (size_t)b.nseg : (size_t)b.num;
+    const cudaError_t e = alloc_async((void**)&P.D, sizeof(float) * layout * layout * nblocks, st);
     if (e != cudaSuccess) s = cuda_fail(e, "mf_solve: preconditioner blocks");
   }
   {
     ProfScope pp(PROF_PRECOND, st);
-    if (!s) s = mf_block_jacobi(b, P.D, st);
+    if (!s) s = layout == 60 ? mf60_block_jacobi(b, P.D, st) : mf_block_jacobi(b, P.D, st);
     if (!s && pc != IBEM_PRECOND_BLOCK_JACOBI)
       s = mf_neighbour_precond(b, pc == IBEM_PRECOND_LEARNED ? gnn_params_dev : nullptr, P, st);
   }

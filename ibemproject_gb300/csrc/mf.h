@@ -43,6 +43,7 @@ inline void free_async(void* p, cudaStream_t st) {
 
 struct MfBatch {
   cudaStream_t st = nullptr;   // stream of the call that owns the batch's buffers
+  int nu = 24;                 // unknowns per particle: 24 or 60
   int nseg = 0, num = 0, max_seg = 0;
   int64_t N = 0;
   std::vector<int> seg_begin_h;
@@ -74,11 +75,22 @@ struct MfBatch {
   int nwork = 0, persist_ctas = 0;
 };
 
+// layout-60 products (mf60.cu): FP32 and FP64 (the double-float entry points fall back to
+// FP64 there), the realisations' block-Jacobi inverses (Pseg: nseg x 60 x 60) and their
+// application
+ibem_status mf60_apply_f32(const MfBatch& b, const float* x, float* y, cudaStream_t st, const int* mask, int mask_on);
+ibem_status mf60_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st, const int* mask,
+                           int mask_on);
+ibem_status mf60_block_jacobi(const MfBatch& b, float* Pseg, cudaStream_t st);
+ibem_status mf60_precond_apply(const MfBatch& b, const float* Pseg, const float* v, float* z, const int* kdev,
+                               int64_t vstride, cudaStream_t st);
+
 // Sets the FP32 product's tile shape (0, 1, 2: 64, 128, 256 targets per CTA), source slices
 // and launch form; builds the persistent form's work list.
 ibem_status mf_set_f32_shape(MfBatch& b, int tshape, int hsplit, int persist, cudaStream_t st);
 
-ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st);
+// layout 24 (orders 0 and 1) or 60 (orders 0 to 2: block-Jacobi preconditioner only)
+ibem_status mf_batch_init(MfBatch& b, const ibem_e3d_batch& in, cudaStream_t st, int layout = 24);
 // Source-slice counts of the products for this batch's shape, from the autotuner's table
 // (timed on first use of a shape class, then cached for the process).
 ibem_status mf_tune(MfBatch& b, cudaStream_t st);

@@ -272,6 +272,21 @@ ibem_status ibem_e3d_mf_solve(const ibem_e3d_batch* batch, const double* b_dev, 
                               ibem_precond pc, const float* gnn_params_dev,
                               const ibem_mf_options* opt, ibem_mf_report* reports, void* stream);
 
+/* The same for quadratic eigenstrain (layout 60: orders 0, 1 and 2, 60 unknowns per sphere,
+ * integratorElastic3D.cpp:341-682) or layout 24: every 60 x 60 pair block is evaluated
+ * inside the products from the same generated code as ibem_e3d_pair_blocks(layout 60), in
+ * FP32 for the GMRES products and in FP64 for the refinement residuals (both of them; there
+ * is no double-float form of layout 60).  Layout 60 takes IBEM_PRECOND_BLOCK_JACOBI only (the
+ * realisation's own 60 x 60 block, the same for all its spheres in the scaled system).
+ * b_dev, x_dev: layout * seg_begin[nseg] doubles. */
+ibem_status ibem_e3d_mf_solve_layout(const ibem_e3d_batch* batch, int layout, const double* b_dev,
+                                     double* x_dev, ibem_precond pc, const float* gnn_params_dev,
+                                     const ibem_mf_options* opt, ibem_mf_report* reports, void* stream);
+
+/* ibem_e3d_mf_matvec for layout 24 or 60 (layout 60: precision 32 or FP64 for 48, 64, 65). */
+ibem_status ibem_e3d_mf_matvec_layout(const ibem_e3d_batch* batch, int layout, int precision,
+                                      const double* x_dev, double* y_dev, void* stream);
+
 /* Launch shape the autotuner picks for this batch's products: source slices per target tile
  * of the FP32 product and of the double-float / FP64 products.  The first call for a shape
  * class (log2 buckets of the tile count and of the largest realisation) times the

@@ -80,9 +80,10 @@ def test_unreachable_packing_is_an_error():
 
 
 def test_matrix_free_helpers_refuse_quadratic_batches():
-    """The matrix-free solver and the learned preconditioner take layout 24 only: the Python
-    helpers refuse a layout-60 batch before any library call; its row ranges follow the
-    layout."""
+    """The learned preconditioner, its training data and the autotuner queries take layout 24
+    only (the matrix-free solve and products also take layout 60): the Python helpers refuse
+    a layout-60 batch before any library call; its row ranges and scalings follow the layout
+    (orders 0, 1, 2: a^o / mu0 and a^-o)."""
     import torch
 
     from ibemproject_gb300 import batch as B
@@ -90,9 +91,13 @@ def test_matrix_free_helpers_refuse_quadratic_batches():
     cs = [cases.generated_case(n, 0.008, 0.2, seed=n) for n in (3, 5)]
     bt = B.DeviceBatch(cs, device="cpu", layout=60)
     assert bt.N == 60 * 8 and bt.seg_rows(1) == slice(180, 480)
-    b = torch.zeros(bt.N, dtype=torch.float64)
-    for call in (lambda: B.solve(bt, b), lambda: B.matvec(bt, b), lambda: B.tuning(bt),
-                 lambda: B.training_pairs(bt, 1), lambda: B.training_pairs_mf(bt, 1), lambda: B.prepare(bt)):
+    dr, dc = bt.scalings()
+    a = bt.radius_host[0]
+    mu0 = cs[0].E0 / (2 * (1 + cs[0].nu0))
+    assert np.allclose(dr[:60] * mu0, [1.0] * 6 + [a] * 18 + [a * a] * 36)
+    assert np.allclose(dc[:60], [1.0] * 6 + [1 / a] * 18 + [1 / a ** 2] * 36)
+    for call in (lambda: B.tuning(bt), lambda: B.tile_shape(bt), lambda: B.training_pairs(bt, 1),
+                 lambda: B.training_pairs_mf(bt, 1), lambda: B.prepare(bt)):
         with pytest.raises(ValueError):
             call()
 
