@@ -66,6 +66,7 @@ extern "C" int hg_field(int layout, const double* x, double a, double E0, double
 }
 
 #include "gen_bem.cuh"
+#include "bem_contract.cuh"
 
 // Dsu/Dst of all rows of one order (rows (k<=l) x W, W last), dofs fastest.
 extern "C" int hg_bem_stress(int order, const double* x, const double* nv, double E0, double nu0,
@@ -112,6 +113,22 @@ extern "C" int hg_bem_stress_post(const double* x, const double* nv, double E0, 
                                   double E1, double nu1, double* Dsu, double* Dst) {
   BemMat bm = bem_mat_init(E0, nu0, E1, nu1);
   bem_stress_post(x[0], x[1], x[2], nv[0], nv[1], nv[2], bm, bm.lam0, bm.mu0, Dsu, Dst);
+  return 0;
+}
+
+// the same stress contracted with boundary values u and t (bem_contract.cuh), and the
+// generated kernels contracted with them afterwards
+extern "C" int hg_bem_post_pair(const double* x, const double* nv, const double* u, const double* t, double E0,
+                                double nu0, double E1, double nu1, double* s_contracted, double* s_generated) {
+  BemMat bm = bem_mat_init(E0, nu0, E1, nu1);
+  double Dsu[18], Dst[18];
+  bem_stress_post(x[0], x[1], x[2], nv[0], nv[1], nv[2], bm, bm.lam0, bm.mu0, Dsu, Dst);
+  for (int q = 0; q < 6; ++q) {
+    s_generated[q] = 0.0;
+    for (int n = 0; n < 3; ++n) s_generated[q] += Dsu[3 * q + n] * u[n] + Dst[3 * q + n] * t[n];
+  }
+  bem_post_contracted(x[0], x[1], x[2], nv[0], nv[1], nv[2], u[0], u[1], u[2], t[0], t[1], t[2], bem_post_coef(bm),
+                      s_contracted);
   return 0;
 }
 
