@@ -11,8 +11,9 @@
 //         + [cu1 (n.u) / R^5 + cu3 (x.n)(x.u) / R^7 + ct1 (x.t) / R^5] x x
 //         + cu4 / R^3 (n u + u n) + cu5 / R^5 [(x.u)(n x + x n) + (x.n)(u x + x u)]
 //         + ct2 / R^3 (t x + x t)
-// with the material coefficients below (their values were matched exactly, symbolically in
-// A, B, lambda0, mu0, against the generated kernels; the host tests compare the two to 1e-13).
+// with the material coefficients below (matched exactly, symbolically in A, B, lambda0, mu0,
+// against the generated kernels by ibemproject_gb300/bem_contract_derivation.py; the host
+// tests compare the two to 1e-13).
 // About 115 FP64 operations per (point, Gauss point) against ~700 for forming Dsu and Dst.
 #pragma once
 #include "gen_sphere_common.cuh"
