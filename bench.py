@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--no-cube64", action="store_true", help="skip the bounded-cube (64 spheres) measurement")
     ap.add_argument("--no-cube64-cpu", action="store_true", help="skip the oracle timing of the bounded cube")
     ap.add_argument("--ellipsoids", type=int, default=4000, help="ellipsoids of the mixed-form measurement (0: skip)")
+    ap.add_argument("--large", type=int, default=20000,
+                    help="spheres of the vf-25%% learned vs block-Jacobi measurement at config 4's size (0: skip)")
     ap.add_argument("--ell-plain", type=int, default=1000,
                     help="ellipsoids of the plain-FP64 vs mixed comparison (0: skip)")
     ap.add_argument("--quad-form", default="mf", choices=["mf", "bj", "mixed"],
@@ -477,6 +479,43 @@ def run_batched(args, dev, params):
             "generation_s": t_gen}
 
 
+def run_large(args, dev, params):
+    """The learned preconditioner at BASELINE config 4's size, with spheres (the matrix-free
+    products take spheres): args.large spheres of radius U[0.8, 1.2] x 0.008 packed by the
+    library's hard-sphere Monte Carlo generator to vf 25% (N = 24 x args.large), uniaxial
+    remote stress; matrix-free FP32 GMRES(50) with FP64 refinement to relative residual 1e-10,
+    preconditioned by the network trained for the headline (never trained on this size), by
+    the same blocks with every weight 1 (analytic Neumann) and by block-Jacobi.  One warm-up
+    and one timed solve each (CUDA events, inputs in HBM)."""
+    import torch
+    from ibemproject_gb300 import batch as B
+    from ibemproject_gb300 import cases
+    t = time.perf_counter()
+    c = cases.generated_case(args.large, 0.008, 0.25, seed=515, method="mc")
+    t_gen = time.perf_counter() - t
+    bt = B.DeviceBatch([c], device=dev)
+    b = B.farfield_rhs(bt, np.array([0, 0, 0, 0, 0, 1.0]))
+    out = {"workload": f"{args.large} spheres r~U[0.8,1.2]*0.008, hard-sphere Monte Carlo to vf 25%, linear eigenstrain "
+                       f"(N={24 * args.large}), far-field sigma33; matrix-free GMRES(50) + FP64 refinement to 1e-10",
+           "generation_s": t_gen}
+    xs = {}
+    for key, pc, pp in (("learned", B.PRECOND_LEARNED, params), ("neumann", B.PRECOND_NEUMANN, None),
+                        ("block_jacobi", B.PRECOND_BLOCK_JACOBI, None)):
+        B.solve(bt, b, pc, params=pp)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        x, reps = B.solve(bt, b, pc, params=pp)
+        e1.record()
+        torch.cuda.synchronize()
+        xs[key] = x
+        out[key] = {"s": e0.elapsed_time(e1) / 1e3, "arnoldi_steps": reps[0].inner, "refinement_steps": reps[0].outer,
+                    "rel_residual": reps[0].rel_residual}
+    ref = xs["block_jacobi"]
+    out["rel_diff_learned_vs_block_jacobi"] = float((xs["learned"] - ref).abs().max() / ref.abs().max())
+    return out
+
+
 def run_cube64(args, dev):
     """The bounded-cube workload (unit cube, 6 x 10 x 10 Q4 elements, 64 spheres of radius
     0.05 by random sequential addition, seed 12345, stresses on the 32^3 cell-centred grid)
@@ -731,6 +770,12 @@ def run_ours(args, rank, world):
             extra["bounded_cube_64_spheres"] = run_cube64(args, dev)
         except Exception as ex:   # reported in the JSON line; the headline measurement stands
             extra["bounded_cube_64_spheres"] = {"error": f"{type(ex).__name__}: {ex}"}
+        torch.cuda.empty_cache()
+    if rank == 0 and args.large > 0 and params is not None:
+        try:
+            extra["learned_vs_block_jacobi_large"] = run_large(args, dev, params)
+        except Exception as ex:
+            extra["learned_vs_block_jacobi_large"] = {"error": f"{type(ex).__name__}: {ex}"}
         torch.cuda.empty_cache()
     if rank == 0 and args.ellipsoids > 0:
         try:
