@@ -445,6 +445,45 @@ __global__ void __launch_bounds__(128) bem_post_kernel(const double* __restrict_
     for (int t = 0; t < 6; ++t) stress[6 * (int64_t)s + t] = acc[t];
 }
 
+// double-float records of the Gauss points (one thread each)
+__global__ void k_post_df_table(const double* __restrict__ tab, int64_t nq, BemPostCoef cf,
+                                ibem::BemPostDF* __restrict__ out) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q < nq) out[q] = ibem::bem_post_df_record(tab + q * kPostRec, cf);
+}
+
+// the mixed form's boundary sums: double-float contraction (bem_contract.cuh), the records
+// staged in shared memory 64 at a time, compensated sums per component
+constexpr int kPostStageDF = 64;
+__global__ void __launch_bounds__(128) bem_post_kernel_df(const double* __restrict__ pts, int nump,
+                                                          const ibem::BemPostDF* __restrict__ tab, int64_t nq,
+                                                          ibem::BemPostCoefDF cf, double* __restrict__ stress) {
+  static_assert(sizeof(ibem::BemPostDF) == 11 * sizeof(float4), "BemPostDF is copied as 11 float4");
+  __shared__ __align__(16) ibem::BemPostDF sq[kPostStageDF];
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool act = s < nump;
+  ibem::dfloat p[3] = {};
+  if (act)
+    for (int k = 0; k < 3; ++k) p[k] = ibem::df_make(pts[3 * (int64_t)s + k]);
+  ibem::dacc acc[6] = {};
+  for (int64_t q0 = 0; q0 < nq; q0 += kPostStageDF) {
+    const int nqs = (int)min((int64_t)kPostStageDF, nq - q0);
+    __syncthreads();
+    {
+      const float4* src = reinterpret_cast<const float4*>(tab + q0);
+      float4* dst = reinterpret_cast<float4*>(sq);
+      for (int i = threadIdx.x; i < nqs * 11; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    if (!act) continue;
+#pragma unroll 1
+    for (int qq = 0; qq < nqs; ++qq) ibem::bem_post_contracted_df(p, sq[qq], cf, acc);
+  }
+  if (act)
+#pragma unroll
+    for (int t = 0; t < 6; ++t) stress[6 * (int64_t)s + t] = (double)acc[t].s + (double)acc[t].c;
+}
+
 }  // namespace
 
 namespace ibem {
@@ -536,16 +575,26 @@ ibem_status bem_to_incl(const double* nodes, int NN, const int* conn, int NE, co
 
 ibem_status bem_post(const double* pts, int nump, const double* nodes, int NN, const int* conn,
                      int NE, const ibem_material& m, const double* U, const double* T,
-                     double* stress, cudaStream_t st) {
+                     double* stress, cudaStream_t st, bool mixed) {
   BemMat bm = bem_mat_init(m.E0, m.nu0, m.E1, m.nu1);
+  const BemPostCoef cf = bem_post_coef(bm);
   ProfScope ps(PROF_BEM, st);
   const int64_t nq = (int64_t)NE * kPostQ;
   double* tab = nullptr;
-  IBEM_CUDA(cudaMallocAsync((void**)&tab, sizeof(double) * kPostRec * (nq > 0 ? nq : 1), st));
+  const size_t tab_bytes = sizeof(double) * kPostRec * (nq > 0 ? nq : 1);
+  const size_t df_bytes = mixed ? sizeof(BemPostDF) * (nq > 0 ? nq : 1) : 0;
+  IBEM_CUDA(cudaMallocAsync((void**)&tab, tab_bytes + df_bytes, st));
+  BemPostDF* tdf = mixed ? reinterpret_cast<BemPostDF*>(reinterpret_cast<char*>(tab) + tab_bytes) : nullptr;
+  const unsigned gq = (unsigned)((nq + 127) / 128);
   if (nq > 0)
-    ::ibem::count_launch(), bem_post_table<<<(unsigned)((nq + 127) / 128), 128, 0, st>>>(nodes, NN, conn, NE, U, T, tab);
-  ::ibem::count_launch(), bem_post_kernel<<<(nump + 127) / 128, 128, 0, st>>>(pts, nump, tab, nq, bem_post_coef(bm),
-                                                                               stress);
+    ::ibem::count_launch(), bem_post_table<<<gq, 128, 0, st>>>(nodes, NN, conn, NE, U, T, tab);
+  if (mixed) {
+    if (nq > 0) ::ibem::count_launch(), k_post_df_table<<<gq, 128, 0, st>>>(tab, nq, cf, tdf);
+    ::ibem::count_launch(), bem_post_kernel_df<<<(nump + 127) / 128, 128, 0, st>>>(pts, nump, tdf, nq,
+                                                                                  bem_post_coef_df(cf), stress);
+  } else {
+    ::ibem::count_launch(), bem_post_kernel<<<(nump + 127) / 128, 128, 0, st>>>(pts, nump, tab, nq, cf, stress);
+  }
   cudaFreeAsync(tab, st);
   IBEM_LAUNCH_CHECK("bem_post");
   return IBEM_OK;

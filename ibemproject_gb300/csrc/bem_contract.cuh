@@ -41,12 +41,12 @@ IBEM_HD IBEM_INLINE void bem_post_contracted(double x0, double x1, double x2, do
                                              double u0, double u1, double u2, double t0, double t1, double t2,
                                              const BemPostCoef& c, double* s) {
   const double r2 = x0 * x0 + x1 * x1 + x2 * x2;
-  const double ir2 = 1.0 / r2;
 #ifdef __CUDA_ARCH__
   const double ir = rsqrt(r2);
 #else
   const double ir = 1.0 / sqrt(r2);
 #endif
+  const double ir2 = ir * ir;   // no separate FP64 division
   const double ir3 = ir * ir2, ir5 = ir3 * ir2, ir7 = ir5 * ir2;
   const double xn = x0 * n0 + x1 * n1 + x2 * n2, xu = x0 * u0 + x1 * u1 + x2 * u2;
   const double nu = n0 * u0 + n1 * u1 + n2 * u2, xt = x0 * t0 + x1 * t1 + x2 * t2;
@@ -68,3 +68,104 @@ IBEM_HD IBEM_INLINE void bem_post_contracted(double x0, double x1, double x2, do
     s[q] = v;
   }
 }
+
+// ---------------------------------------------------------------------------------------
+// The same contraction in double-float arithmetic (dfloat.cuh: ~48 bits on the FP32 pipe,
+// which GB300 runs at 64x its FP64 rate), for the mixed form's stresses.  Everything that
+// depends on the Gauss point only is converted once per call into a BemPostDF record,
+// including n.u and n_k u_l + n_l u_k times their material coefficients; per (point, Gauss
+// point) pair the kernel forms x, the powers of 1/R and four dot products, and adds the six
+// components, weighted by the quadrature weight, to compensated sums (dacc).
+#include "dfloat.cuh"
+
+namespace ibem {
+
+struct BemPostDF {
+  dfloat y[3], n[3], u[3], t[3];
+  dfloat w;        // quadrature weight x Jacobian
+  dfloat nu0, nu1; // cu0 (n.u), cu1 (n.u)
+  dfloat nuk[6];   // cu4 (n_k u_l + n_l u_k), pairs xx xy xz yy yz zz
+  dfloat pad;      // 176 bytes: 11 float4
+};
+
+struct BemPostCoefDF {
+  dfloat cu1, cu3, cu5, ct0, ct1, ct2;
+};
+
+IBEM_HD inline BemPostCoefDF bem_post_coef_df(const BemPostCoef& c) {
+  return {df_make(c.cu1), df_make(c.cu3), df_make(c.cu5), df_make(c.ct0), df_make(c.ct1), df_make(c.ct2)};
+}
+
+// r: y, n, w, u, t of one Gauss point (the FP64 quadrature-table record layout: y 0-2, n 3-5,
+// w 6, u 7-9, t 10-12)
+IBEM_HD inline BemPostDF bem_post_df_record(const double* r, const BemPostCoef& c) {
+  BemPostDF o;
+  for (int k = 0; k < 3; ++k) {
+    o.y[k] = df_make(r[k]);
+    o.n[k] = df_make(r[3 + k]);
+    o.u[k] = df_make(r[7 + k]);
+    o.t[k] = df_make(r[10 + k]);
+  }
+  o.w = df_make(r[6]);
+  const double nu = r[3] * r[7] + r[4] * r[8] + r[5] * r[9];
+  o.nu0 = df_make(c.cu0 * nu);
+  o.nu1 = df_make(c.cu1 * nu);
+  const int pi[6] = {0, 0, 0, 1, 1, 2}, pj[6] = {0, 1, 2, 1, 2, 2};
+  for (int q = 0; q < 6; ++q)
+    o.nuk[q] = df_make(c.cu4 * (r[3 + pi[q]] * r[7 + pj[q]] + r[3 + pj[q]] * r[7 + pi[q]]));
+  o.pad = dfloat{0.0f, 0.0f};
+  return o;
+}
+
+// acc[6] += w sigma (compensated sums) for the sample point p (double-float)
+IBEM_HD IBEM_INLINE void bem_post_contracted_df(const dfloat* p, const BemPostDF& g, const BemPostCoefDF& c,
+                                                dacc* acc) {
+  dfloat x[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) x[k] = g.y[k] - p[k];
+  const dfloat r2 = dot3(x, x);
+  // 1 / R: FP32 estimate, one double-float Newton step
+  float y0;
+#ifdef __CUDA_ARCH__
+  y0 = rsqrtf(r2.hi);
+#else
+  y0 = 1.0f / std::sqrt(r2.hi);
+#endif
+  const dfloat yd{y0, 0.0f};
+  const dfloat ir = yd + yd * ((dfloat{1.0f, 0.0f} - r2 * (yd * yd)) * 0.5f);
+  const dfloat ir2 = ir * ir;
+  const dfloat W3 = g.w * (ir * ir2), W5 = W3 * ir2, W7 = W5 * ir2;
+  const dfloat xn = dot3(x, g.n), xu = dot3(x, g.u), xt = dot3(x, g.t);
+  const dfloat xnxu = xn * xu;
+  dacc aa = dacc_of(g.nu0);
+  dacc_fma(aa, c.ct0, xt);
+  dacc ab = dacc_of(g.nu1);
+  dacc_fma(ab, c.ct1, xt);
+  dacc a = dacc_prod(W3, dacc_val(aa));
+  dacc_fma(a, W5 * c.cu1, xnxu);
+  dacc b = dacc_prod(W5, dacc_val(ab));
+  dacc_fma(b, W7 * c.cu3, xnxu);
+  const dfloat av = dacc_val(a), bv = dacc_val(b);
+  const dfloat d = (W5 * c.cu5) * xu, e = (W5 * c.cu5) * xn, f = W3 * c.ct2;
+  dfloat w[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    dacc s = dacc_prod(d, g.n[k]);
+    dacc_fma(s, e, g.u[k]);
+    dacc_fma(s, f, g.t[k]);
+    w[k] = dacc_val(s);
+  }
+  const int pi[6] = {0, 0, 0, 1, 1, 2}, pj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const int k = pi[q], l = pj[q];
+    dacc& o = acc[q];
+    dacc_fma(o, bv * x[k], x[l]);
+    dacc_fma(o, W3, g.nuk[q]);
+    dacc_fma(o, w[k], x[l]);
+    dacc_fma(o, w[l], x[k]);
+    if (k == l) dacc_add(o, av);
+  }
+}
+
+}  // namespace ibem

@@ -350,7 +350,8 @@ ibem_status ibem_e3d_field_form(ibem_solver_form form, const double* points_dev,
   if (nump == 0) return IBEM_OK;
   cudaStream_t st = as_stream(stream);
   if (NE > 0) {
-    ibem_status s = bem_post(points_dev, nump, nodes_dev, NN, conn_dev, NE, *mat, U_dev, T_dev, stress_dev, st);
+    ibem_status s = bem_post(points_dev, nump, nodes_dev, NN, conn_dev, NE, *mat, U_dev, T_dev, stress_dev, st,
+                             form == IBEM_SOLVE_MIXED_IR);
     if (s) return s;
   } else {
     FarRhs f;

@@ -156,44 +156,6 @@ IBEM_HD inline SphDF sph_df_make(const double* cen, double a, const double* Eu) 
   return s;
 }
 
-// Compensated sums (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci.
-// Comput. 26, 2005, algorithm Dot2) over double-float operands: s is the FP32 running sum of
-// the leading products, c the FP32 sum of every rounding error (TwoSum of each addition,
-// FMA residual and cross terms of each product).  The value s + c carries about twice
-// FP32's precision like a double-float sum, at 12 instead of 18 FP32 instructions per
-// multiply-add (no renormalisation after each term).
-struct dacc {
-  float s, c;
-};
-IBEM_HD IBEM_INLINE dacc dacc_of(dfloat x) { return {x.hi, x.lo}; }
-IBEM_HD IBEM_INLINE dacc dacc_prod(dfloat x, dfloat y) {
-  const float p = x.hi * y.hi;
-  return {p, df_fmaf(x.hi, y.lo, df_fmaf(x.lo, y.hi, df_fmaf(x.hi, y.hi, -p)))};
-}
-// a += x * y
-IBEM_HD IBEM_INLINE void dacc_fma(dacc& a, dfloat x, dfloat y) {
-  const float p = x.hi * y.hi;
-  const float e = df_fmaf(x.hi, y.lo, df_fmaf(x.lo, y.hi, df_fmaf(x.hi, y.hi, -p)));
-  const float s = a.s + p;
-  const float bb = s - a.s;
-  a.c += ((a.s - (s - bb)) + (p - bb)) + e;
-  a.s = s;
-}
-// a += x
-IBEM_HD IBEM_INLINE void dacc_add(dacc& a, dfloat x) {
-  const float s = a.s + x.hi;
-  const float bb = s - a.s;
-  a.c += ((a.s - (s - bb)) + (x.hi - bb)) + x.lo;
-  a.s = s;
-}
-IBEM_HD IBEM_INLINE dfloat dacc_val(dacc a) { return df_fast_two_sum(a.s, a.c); }
-IBEM_HD IBEM_INLINE dfloat dot3(const dfloat* u, const dfloat* x) {
-  dacc a = dacc_prod(u[0], x[0]);
-  dacc_fma(a, u[1], x[1]);
-  dacc_fma(a, u[2], x[2]);
-  return dacc_val(a);
-}
-
 // e[6] += strain / c at the point p (double-float, point already converted), each e[t] a
 // compensated sum over the spheres; returns whether the point lies inside or on the sphere.
 // The caller multiplies by c = 1 / (8 pi (1 - nu)) once, after the sum.

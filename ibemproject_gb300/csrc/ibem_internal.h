@@ -65,6 +65,6 @@ ibem_status bem_to_incl(const double* nodes, int NN, const int* conn, int NE, co
                         cudaStream_t st);
 ibem_status bem_post(const double* pts, int nump, const double* nodes, int NN, const int* conn,
                      int NE, const ibem_material& m, const double* U, const double* T,
-                     double* stress, cudaStream_t st);
+                     double* stress, cudaStream_t st, bool mixed = false);
 
 }  // namespace ibem

@@ -132,6 +132,26 @@ extern "C" int hg_bem_post_pair(const double* x, const double* nv, const double*
   return 0;
 }
 
+// the mixed form's double-float contraction of one Gauss point record r (y, n, w, u, t) at
+// the sample point p, and the FP64 contraction times the weight
+extern "C" int hg_bem_post_pair_df(const double* p, const double* r, double E0, double nu0, double E1, double nu1,
+                                   double* s_df, double* s_fp64) {
+  BemMat bm = bem_mat_init(E0, nu0, E1, nu1);
+  const BemPostCoef cf = bem_post_coef(bm);
+  const ibem::BemPostDF g = ibem::bem_post_df_record(r, cf);
+  const ibem::dfloat pd[3] = {ibem::df_make(p[0]), ibem::df_make(p[1]), ibem::df_make(p[2])};
+  ibem::dacc acc[6] = {};
+  ibem::bem_post_contracted_df(pd, g, ibem::bem_post_coef_df(cf), acc);
+  double s[6];
+  bem_post_contracted(r[0] - p[0], r[1] - p[1], r[2] - p[2], r[3], r[4], r[5], r[7], r[8], r[9], r[10], r[11], r[12], cf,
+                      s);
+  for (int q = 0; q < 6; ++q) {
+    s_df[q] = (double)acc[q].s + (double)acc[q].c;
+    s_fp64[q] = r[6] * s[q];
+  }
+  return 0;
+}
+
 #include "field_contract.cuh"
 
 extern "C" int hg_field24c(const double* x, double a, double E0, double nu0, double E1, double nu1,
