@@ -415,17 +415,26 @@ __global__ void bem_post_table(const double* __restrict__ nodes, int NN, const i
 
 // sums over the staged Gauss points of the stress contracted with their boundary values
 // (bem_contract.cuh: ~115 FP64 operations per pair instead of forming the 2 x 18 Kelvin kernels)
+// Gauss points [q_begin, q_end) of slice blockIdx.y of gridDim.y (a multiple of kPostStage)
+__device__ __forceinline__ void post_slice(int64_t nq, int64_t& qb, int64_t& qe) {
+  const int64_t per = ((nq + gridDim.y - 1) / gridDim.y + kPostStage - 1) / kPostStage * kPostStage;
+  qb = min(nq, (int64_t)blockIdx.y * per);
+  qe = min(nq, qb + per);
+}
+
 __global__ void __launch_bounds__(128) bem_post_kernel(const double* __restrict__ pts, int nump,
                                                        const double* __restrict__ tab, int64_t nq, BemPostCoef cf,
-                                                       double* __restrict__ stress) {
+                                                       double* __restrict__ part) {
   __shared__ double sq[kPostStage * kPostRec];
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   const bool act = s < nump;
   double P0 = 0, P1 = 0, P2 = 0;
   if (act) { P0 = pts[3 * s]; P1 = pts[3 * s + 1]; P2 = pts[3 * s + 2]; }
   double acc[6] = {0, 0, 0, 0, 0, 0};
-  for (int64_t q0 = 0; q0 < nq; q0 += kPostStage) {
-    const int nqs = (int)min((int64_t)kPostStage, nq - q0);
+  int64_t qb, qe;
+  post_slice(nq, qb, qe);
+  for (int64_t q0 = qb; q0 < qe; q0 += kPostStage) {
+    const int nqs = (int)min((int64_t)kPostStage, qe - q0);
     __syncthreads();
     for (int idx = threadIdx.x; idx < nqs * kPostRec; idx += blockDim.x) sq[idx] = tab[q0 * kPostRec + idx];
     __syncthreads();
@@ -442,7 +451,16 @@ __global__ void __launch_bounds__(128) bem_post_kernel(const double* __restrict_
   }
   if (act)
 #pragma unroll
-    for (int t = 0; t < 6; ++t) stress[6 * (int64_t)s + t] = acc[t];
+    for (int t = 0; t < 6; ++t) part[6 * ((int64_t)blockIdx.y * nump + s) + t] = acc[t];
+}
+
+// stress = sum of the slices' partial sums, in slice order (the same result on every run)
+__global__ void k_post_reduce(int nump, int nslice, const double* __restrict__ part, double* __restrict__ stress) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= 6 * (int64_t)nump) return;
+  double v = 0.0;
+  for (int k = 0; k < nslice; ++k) v += part[(int64_t)k * 6 * nump + i];
+  stress[i] = v;
 }
 
 // double-float records of the Gauss points (one thread each)
@@ -457,7 +475,7 @@ __global__ void k_post_df_table(const double* __restrict__ tab, int64_t nq, BemP
 constexpr int kPostStageDF = 64;
 __global__ void __launch_bounds__(128) bem_post_kernel_df(const double* __restrict__ pts, int nump,
                                                           const ibem::BemPostDF* __restrict__ tab, int64_t nq,
-                                                          ibem::BemPostCoefDF cf, double* __restrict__ stress) {
+                                                          ibem::BemPostCoefDF cf, double* __restrict__ part) {
   static_assert(sizeof(ibem::BemPostDF) == 11 * sizeof(float4), "BemPostDF is copied as 11 float4");
   __shared__ __align__(16) ibem::BemPostDF sq[kPostStageDF];
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -466,8 +484,10 @@ __global__ void __launch_bounds__(128) bem_post_kernel_df(const double* __restri
   if (act)
     for (int k = 0; k < 3; ++k) p[k] = ibem::df_make(pts[3 * (int64_t)s + k]);
   ibem::dacc acc[6] = {};
-  for (int64_t q0 = 0; q0 < nq; q0 += kPostStageDF) {
-    const int nqs = (int)min((int64_t)kPostStageDF, nq - q0);
+  int64_t qb, qe;
+  post_slice(nq, qb, qe);   // slice boundaries are multiples of kPostStage, hence of kPostStageDF
+  for (int64_t q0 = qb; q0 < qe; q0 += kPostStageDF) {
+    const int nqs = (int)min((int64_t)kPostStageDF, qe - q0);
     __syncthreads();
     {
       const float4* src = reinterpret_cast<const float4*>(tab + q0);
@@ -481,7 +501,7 @@ __global__ void __launch_bounds__(128) bem_post_kernel_df(const double* __restri
   }
   if (act)
 #pragma unroll
-    for (int t = 0; t < 6; ++t) stress[6 * (int64_t)s + t] = (double)acc[t].s + (double)acc[t].c;
+    for (int t = 0; t < 6; ++t) part[6 * ((int64_t)blockIdx.y * nump + s) + t] = (double)acc[t].s + (double)acc[t].c;
 }
 
 }  // namespace
@@ -581,20 +601,32 @@ ibem_status bem_post(const double* pts, int nump, const double* nodes, int NN, c
   ProfScope ps(PROF_BEM, st);
   const int64_t nq = (int64_t)NE * kPostQ;
   double* tab = nullptr;
-  const size_t tab_bytes = sizeof(double) * kPostRec * (nq > 0 ? nq : 1);
-  const size_t df_bytes = mixed ? sizeof(BemPostDF) * (nq > 0 ? nq : 1) : 0;
-  IBEM_CUDA(cudaMallocAsync((void**)&tab, tab_bytes + df_bytes, st));
+  // source slices of the Gauss points: about 8 CTAs per SM in total, at least one staged
+  // chunk each (few sample points would otherwise leave most SMs idle)
+  int dev = 0, nsm = 0;
+  IBEM_CUDA(cudaGetDevice(&dev));
+  IBEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int gx = (nump + 127) / 128;
+  const int64_t chunks = (nq + kPostStage - 1) / kPostStage;
+  const int nslice = (int)std::max<int64_t>(1, std::min<int64_t>((8 * (int64_t)nsm + gx - 1) / gx, chunks));
+  const size_t tab_bytes = (sizeof(double) * kPostRec * (nq > 0 ? nq : 1) + 255) / 256 * 256;
+  const size_t df_bytes = mixed ? (sizeof(BemPostDF) * (nq > 0 ? nq : 1) + 255) / 256 * 256 : 0;
+  const size_t part_bytes = sizeof(double) * 6 * (size_t)nslice * (size_t)nump;
+  IBEM_CUDA(cudaMallocAsync((void**)&tab, tab_bytes + df_bytes + part_bytes, st));
   BemPostDF* tdf = mixed ? reinterpret_cast<BemPostDF*>(reinterpret_cast<char*>(tab) + tab_bytes) : nullptr;
+  double* part = reinterpret_cast<double*>(reinterpret_cast<char*>(tab) + tab_bytes + df_bytes);
   const unsigned gq = (unsigned)((nq + 127) / 128);
+  const dim3 grid((unsigned)gx, (unsigned)nslice);
   if (nq > 0)
     ::ibem::count_launch(), bem_post_table<<<gq, 128, 0, st>>>(nodes, NN, conn, NE, U, T, tab);
   if (mixed) {
     if (nq > 0) ::ibem::count_launch(), k_post_df_table<<<gq, 128, 0, st>>>(tab, nq, cf, tdf);
-    ::ibem::count_launch(), bem_post_kernel_df<<<(nump + 127) / 128, 128, 0, st>>>(pts, nump, tdf, nq,
-                                                                                  bem_post_coef_df(cf), stress);
+    ::ibem::count_launch(), bem_post_kernel_df<<<grid, 128, 0, st>>>(pts, nump, tdf, nq, bem_post_coef_df(cf), part);
   } else {
-    ::ibem::count_launch(), bem_post_kernel<<<(nump + 127) / 128, 128, 0, st>>>(pts, nump, tab, nq, cf, stress);
+    ::ibem::count_launch(), bem_post_kernel<<<grid, 128, 0, st>>>(pts, nump, tab, nq, cf, part);
   }
+  ::ibem::count_launch(), k_post_reduce<<<(unsigned)((6 * (int64_t)nump + 255) / 256), 256, 0, st>>>(nump, nslice,
+                                                                                                   part, stress);
   cudaFreeAsync(tab, st);
   IBEM_LAUNCH_CHECK("bem_post");
   return IBEM_OK;
