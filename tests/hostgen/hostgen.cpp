@@ -3,6 +3,7 @@
 #include <string.h>
 #include "gen_sphere24.cuh"
 #include "gen_sphere60.cuh"
+#include "gen_sphere60_f32.cuh"
 #include "gen_sphere78.cuh"
 
 namespace {
@@ -175,6 +176,43 @@ extern "C" int hg_field24df(const double* p, const double* cen, double a, double
 }
 
 #include "mf_contract.cuh"
+
+// The layout-60 pair block at offset x of a unit source sphere: out64 from the FP64 functions
+// (all nine sub-blocks), out32 from the FP32 column groups the matrix-free solver calls
+// (moduli / mu0, multiplied back by mu0 here); out[r * 60 + c]
+struct Put60 {
+  double* M;
+  double scale;
+  template <class T>
+  void operator()(int r, int c, T v) { M[r * 60 + c] += scale * (double)v; }
+};
+extern "C" int hg_block60_groups(const double* x, double E0, double nu0, double E1, double nu1, double* out64,
+                                 double* out32) {
+  SphMat mc = sph_mat_init(E0, nu0, E1, nu1);
+  const SphMatF mf = sph_matf_init(mc);
+  for (int i = 0; i < 3600; ++i) out64[i] = out32[i] = 0.0;
+  Put60 p64{out64, 1.0}, p32{out32, mc.mu0};
+  const double a = 1.0;
+  sph_block60_c0_r0(x[0], x[1], x[2], a, mc, p64); sph_block60_c1_r0(x[0], x[1], x[2], a, mc, p64);
+  sph_block60_c2_r0(x[0], x[1], x[2], a, mc, p64); sph_block60_c0_r1(x[0], x[1], x[2], a, mc, p64);
+  sph_block60_c1_r1(x[0], x[1], x[2], a, mc, p64); sph_block60_c2_r1(x[0], x[1], x[2], a, mc, p64);
+  sph_block60_c0_r2(x[0], x[1], x[2], a, mc, p64); sph_block60_c1_r2(x[0], x[1], x[2], a, mc, p64);
+  sph_block60_c2_r2(x[0], x[1], x[2], a, mc, p64);
+  const float f0 = (float)x[0], f1 = (float)x[1], f2 = (float)x[2], one = 1.0f;
+  sph_block60fm_c0_r0(f0, f1, f2, one, mf, p32); sph_block60fm_c1_r0(f0, f1, f2, one, mf, p32);
+  sph_block60fm_c2_r0(f0, f1, f2, one, mf, p32); sph_block60fm_c0_r1(f0, f1, f2, one, mf, p32);
+  sph_block60fm_c1_r1(f0, f1, f2, one, mf, p32);
+  sph_block60f_c2g0_r1(f0, f1, f2, one, mf, p32); sph_block60f_c2g1_r1(f0, f1, f2, one, mf, p32);
+  sph_block60f_c2g2_r1(f0, f1, f2, one, mf, p32); sph_block60f_c2g3_r1(f0, f1, f2, one, mf, p32);
+  sph_block60f_c2g4_r1(f0, f1, f2, one, mf, p32); sph_block60f_c2g5_r1(f0, f1, f2, one, mf, p32);
+  sph_block60fm_c0_r2(f0, f1, f2, one, mf, p32);
+  sph_block60f_c1g0_r2(f0, f1, f2, one, mf, p32); sph_block60f_c1g1_r2(f0, f1, f2, one, mf, p32);
+  sph_block60f_c1g2_r2(f0, f1, f2, one, mf, p32);
+  sph_block60f_c2g0_r2(f0, f1, f2, one, mf, p32); sph_block60f_c2g1_r2(f0, f1, f2, one, mf, p32);
+  sph_block60f_c2g2_r2(f0, f1, f2, one, mf, p32); sph_block60f_c2g3_r2(f0, f1, f2, one, mf, p32);
+  sph_block60f_c2g4_r2(f0, f1, f2, one, mf, p32); sph_block60f_c2g5_r2(f0, f1, f2, one, mf, p32);
+  return 0;
+}
 
 // Product of one layout-24 pair block with a coefficient vector as the matrix-free solver
 // evaluates it (contracted strain and its gradient), in FP64 or FP32.

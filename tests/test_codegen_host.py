@@ -131,6 +131,29 @@ def test_contracted_field_matches_generated(hg):
         assert scaled_err(e2, e1) < 1e-13, (t, x, e1, e2)
 
 
+def test_layout60_fp32_column_groups_match_fp64_blocks(hg):
+    """The FP32 column groups of the layout-60 blocks (the matrix-free solver's GMRES product,
+    gen_sphere60_f32.cuh) cover every entry of the FP64 pair block exactly once: each
+    (row order, column order) sub-block within 2e-5 of its largest entry, outside and inside
+    the unit source sphere."""
+    rng = np.random.default_rng(41)
+    for k in range(12):
+        x = rng.normal(size=3)
+        x *= (0.5 if k % 4 == 0 else rng.uniform(2.1, 12.0)) / np.linalg.norm(x)
+        o64, o32 = np.zeros(3600), np.zeros(3600)
+        hg.hg_block60_groups(d(x), *_mat(), d(o64), d(o32))
+        B64, B32 = o64.reshape(60, 60), o32.reshape(60, 60)
+        edges = (0, 6, 24, 60)
+        for ro in range(3):
+            for co in range(3):
+                rs, cs = slice(edges[ro], edges[ro + 1]), slice(edges[co], edges[co + 1])
+                m = np.abs(B64[rs, cs]).max()
+                if m == 0.0:   # some sub-blocks vanish inside the sphere
+                    assert np.abs(B32[rs, cs]).max() <= 1e-6 * np.abs(B64).max(), (k, ro, co)
+                    continue
+                assert np.abs(B32[rs, cs] - B64[rs, cs]).max() <= 2e-5 * m, (k, ro, co)
+
+
 def test_bem_post_contracted_matches_generated(hg):
     """The boundary part of the stresses contracted with the boundary displacement and traction
     before forming any tensor (bem_contract.cuh) against the generated Kelvin kernels
