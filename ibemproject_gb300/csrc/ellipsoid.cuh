@@ -83,17 +83,33 @@ IBEM_HD IBEM_INLINE void jzero(Jet<T, K>& o) {
 }
 
 // Product tables: the (alpha, beta) decompositions of every output monomial gamma,
-// grouped by gamma; `last` marks the final term of a group.  Built at compile time (the
-// unrolled products below index their operands with its entries as constants).
-template <int K>
+// grouped by gamma; `last` marks the final term of a group.  AMAX bounds the degree of alpha:
+// K for general products, 2 when the left operand is a quadratic polynomial (the squared
+// offsets l_m^2, whose coefficients of degree 3 and more are zero; 155 instead of 210 terms
+// at order 4).  Built at compile time (the unrolled products below index their operands with
+// its entries as constants).
+template <int K, int AMAX>
+IBEM_HD constexpr int multab_count() {
+  int n = 0;
+  for (int d = 0; d <= K; ++d)
+    for (int g1 = d; g1 >= 0; --g1)
+      for (int g2 = d - g1; g2 >= 0; --g2)
+        for (int a1 = 0; a1 <= g1; ++a1)
+          for (int a2 = 0; a2 <= g2; ++a2)
+            for (int a3 = 0; a3 <= d - g1 - g2; ++a3)
+              if (a1 + a2 + a3 <= AMAX) ++n;
+  return n;
+}
+
+template <int K, int AMAX = K>
 struct MulTab {
-  static constexpr int NT = K == 3 ? 84 : (K == 4 ? 210 : 1);
+  static constexpr int NT = multab_count<K, AMAX>();
   unsigned char a[NT], b[NT], g[NT], last[NT];
 };
 
-template <int K>
-IBEM_HD constexpr MulTab<K> make_multab() {
-  MulTab<K> t{};
+template <int K, int AMAX = K>
+IBEM_HD constexpr MulTab<K, AMAX> make_multab() {
+  MulTab<K, AMAX> t{};
   int n = 0;
   for (int d = 0; d <= K; ++d)
     for (int g1 = d; g1 >= 0; --g1)
@@ -102,6 +118,7 @@ IBEM_HD constexpr MulTab<K> make_multab() {
         for (int a1 = 0; a1 <= g1; ++a1)
           for (int a2 = 0; a2 <= g2; ++a2)
             for (int a3 = 0; a3 <= g3; ++a3) {
+              if (a1 + a2 + a3 > AMAX) continue;
               t.a[n] = (unsigned char)midx(a1, a2, a3);
               t.b[n] = (unsigned char)midx(g1 - a1, g2 - a2, g3 - a3);
               t.g[n] = (unsigned char)midx(g1, g2, g3);
@@ -158,21 +175,20 @@ IBEM_HD IBEM_INLINE const ShiftTab<K>& shifttab() {
 #else
 #define IBEM_NOINLINE __attribute__((noinline))
 #endif
-template <typename T, int K>
+template <typename T, int K, int AMAX = K>
 IBEM_HD IBEM_NOINLINE void jmul_acc_ptr(T keep, T w, const T* __restrict__ a, const T* __restrict__ b,
                                         T* __restrict__ o) {
   static_assert(K == 3 || K == 4, "jets of order 3 or 4");
-  constexpr MulTab<K> tb = make_multab<K>();
-  constexpr int N = nmono(K);
-  T av[N], bv[N];
+  constexpr MulTab<K, AMAX> tb = make_multab<K, AMAX>();
+  constexpr int N = nmono(K), NA = nmono(AMAX);
+  T av[NA], bv[N];
 #pragma unroll
-  for (int i = 0; i < N; ++i) {
-    av[i] = a[i];
-    bv[i] = b[i];
-  }
+  for (int i = 0; i < NA; ++i) av[i] = a[i];
+#pragma unroll
+  for (int i = 0; i < N; ++i) bv[i] = b[i];
   T acc = T(0);
 #pragma unroll
-  for (int t = 0; t < MulTab<K>::NT; ++t) {
+  for (int t = 0; t < MulTab<K, AMAX>::NT; ++t) {
     acc += av[tb.a[t]] * bv[tb.b[t]];
     if (tb.last[t]) {
       o[tb.g[t]] = keep * o[tb.g[t]] + w * acc;
@@ -196,6 +212,17 @@ IBEM_HD IBEM_INLINE void jmul(const Jet<T, K>& a, const Jet<T, K>& b, Jet<T, K>&
 template <typename T, int K>
 IBEM_HD IBEM_INLINE void jfma(T w, const Jet<T, K>& a, const Jet<T, K>& b, Jet<T, K>& o) {
   jmul_acc(T(1), w, a, b, o);
+}
+
+// the same with a quadratic left operand (coefficients of degree 3 and more zero)
+template <typename T, int K>
+IBEM_HD IBEM_INLINE void jfma_q(T w, const Jet<T, K>& a, const Jet<T, K>& b, Jet<T, K>& o) {
+  jmul_acc_ptr<T, K, 2>(T(1), w, a.c, b.c, o.c);
+}
+template <typename T, int K>
+IBEM_HD IBEM_INLINE void jmul_q(const Jet<T, K>& a, const Jet<T, K>& b, Jet<T, K>& o) {
+  jzero(o);
+  jmul_acc_ptr<T, K, 2>(T(1), T(1), a.c, b.c, o.c);
 }
 
 // o = (l0 + l1 h1 + l2 h2 + l3 h3) * a   (o must not alias a)
@@ -448,7 +475,7 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
           jaxpy(s, dp[n], inv);
           s *= -xm;
         }
-        jfma(T(1), sq[m], inv, G);
+        jfma_q(T(1), sq[m], inv, G);
       }
       G.c[0] = T(0);   // lambda0 is the root: the constant term vanishes (to rounding)
       jaxpy(-T(1) / gp, G, del);
@@ -515,7 +542,7 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
 #pragma unroll 1
   for (int m = 0; m < 3; ++m)
 #pragma unroll 1
-    for (int n = m; n < 3; ++n) jmul(sq[m], sq[n], sq2[sym_pair(m, n)]);
+    for (int n = m; n < 3; ++n) jmul_q(sq[m], sq[n], sq2[sym_pair(m, n)]);
   // F1_j = int U prod t^j ds/Delta = I_j - sum_m sq_m I_{j+e_m}
   // F2_j = int U^2 prod t^j ds/Delta = I_j - 2 sum_m sq_m I_{j+e_m} + sum_{m,n} sq_m sq_n I_{j+e_m+e_n}
   const T C = T(IBEM_PI) * a[0] * a[1] * a[2];
@@ -525,7 +552,7 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
   J F;
   F = I[0];
 #pragma unroll 1
-  for (int m = 0; m < 3; ++m) jfma(-T(1), sq[m], I[e(m, 0, 0, 0)], F);
+  for (int m = 0; m < 3; ++m) jfma_q(-T(1), sq[m], I[e(m, 0, 0, 0)], F);
 #pragma unroll 1
   for (int i = 0; i < J::N; ++i) P.f0.c[i] = C * F.c[i];
   // phi_{y'_m} = C a_m^2 l_m F1_{e_m}, rotated to global densities
@@ -535,7 +562,7 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
     const int km[3] = {m == 0, m == 1, m == 2};
     F = I[midx(km[0], km[1], km[2])];
 #pragma unroll 1
-    for (int n = 0; n < 3; ++n) jfma(-T(1), sq[n], I[e(n, km[0], km[1], km[2])], F);
+    for (int n = 0; n < 3; ++n) jfma_q(-T(1), sq[n], I[e(n, km[0], km[1], km[2])], F);
     jmul_lin(C * a2[m] * y[m], C * a2[m] * Q[m], C * a2[m] * Q[3 + m], C * a2[m] * Q[6 + m], F, p1[m]);
   }
 #pragma unroll 1
@@ -548,7 +575,7 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
   J F20;   // F2_0
   F20 = I[0];
 #pragma unroll 1
-  for (int m = 0; m < 3; ++m) jfma(-T(2), sq[m], I[e(m, 0, 0, 0)], F20);
+  for (int m = 0; m < 3; ++m) jfma_q(-T(2), sq[m], I[e(m, 0, 0, 0)], F20);
 #pragma unroll 1
   for (int m = 0; m < 3; ++m)
 #pragma unroll 1
@@ -564,7 +591,7 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
       // F1_{e_m + e_n}, times a_m^2 a_n^2 l_m l_n
       F = I[midx(km[0], km[1], km[2])];
 #pragma unroll 1
-      for (int r = 0; r < 3; ++r) jfma(-T(1), sq[r], I[e(r, km[0], km[1], km[2])], F);
+      for (int r = 0; r < 3; ++r) jfma_q(-T(1), sq[r], I[e(r, km[0], km[1], km[2])], F);
       jmul_lin(y[m], Q[m], Q[3 + m], Q[6 + m], F, t);
       J& o = p2[sym_pair(m, n)];
       jmul_lin(C * a2[m] * a2[n] * y[n], C * a2[m] * a2[n] * Q[n], C * a2[m] * a2[n] * Q[3 + n],
@@ -575,7 +602,7 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
         const int em[3] = {m == 0, m == 1, m == 2};
         F = I[midx(em[0], em[1], em[2])];
 #pragma unroll 1
-        for (int r = 0; r < 3; ++r) jfma(-T(2), sq[r], I[e(r, em[0], em[1], em[2])], F);
+        for (int r = 0; r < 3; ++r) jfma_q(-T(2), sq[r], I[e(r, em[0], em[1], em[2])], F);
 #pragma unroll 1
         for (int r = 0; r < 3; ++r)
 #pragma unroll 1
