@@ -463,7 +463,7 @@ IBEM_HD inline void ell_potentials(const T d[3], const T Q[9], const T a[3], Ell
     for (int it = 0; it < K; ++it) {
       dp[1] = del;
 #pragma unroll 1
-      for (int n = 2; n <= K; ++n) jmul(dp[n - 1], del, dp[n]);
+      for (int n = 2; n <= K && it > 0; ++n) jmul(dp[n - 1], del, dp[n]);   // del = 0 on the first pass
       jzero(G);
       G.c[0] = T(-1);
 #pragma unroll 1

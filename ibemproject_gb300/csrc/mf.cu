@@ -149,9 +149,10 @@ __global__ void __launch_bounds__(TT)
 // FP32 kernel in double precision, offsets from FP64 centres.
 // Split products (the deciding residual): particles are visited in the Morton order of
 // their centres within each realisation (perm: position -> particle), so the 32 targets of a
-// warp and the 32 sources of a chunk are compact clusters.  mode 0: every pair; 1: only the
-// chunks near the warp's targets (box distance <= kMfFarRadii radii of the chunk's largest
-// sphere), and the self term; 2: only the far chunks, no self term.
+// warp form a compact cluster.  mode 0: every pair; 1: only the sources near the warp's
+// targets (within kMfFarRadii of their radius of the targets' bounding box), and the self
+// term; 2: only the far sources, no self term.  The test is per (warp, source) and
+// warp-uniform.
 __device__ __forceinline__ void warp_box(bool act, double x, double y, double z, double* lo, double* hi) {
   double v[3] = {x, y, z};
 #pragma unroll
@@ -167,23 +168,20 @@ __device__ __forceinline__ void warp_box(bool act, double x, double y, double z,
   }
 }
 
-// chunk box of the staged sources (lane i reads source i) and the largest radius
-__device__ __forceinline__ bool chunk_is_far(const double* wlo, const double* whi, int nh, double cx, double cy,
-                                             double cz, double r) {
-  const int lane = threadIdx.x & 31;
-  const bool a = lane < nh;
-  double lo[3], hi[3];
-  warp_box(a, cx, cy, cz, lo, hi);
-  double rm = a ? r : 0.0;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) rm = fmax(rm, __shfl_xor_sync(0xffffffffu, rm, o));
+// whether a source sphere (c, r) lies beyond kMfFarRadii of its radius from the box of the
+// warp's targets: the same for every lane; rounded operations without contraction, so that
+// the FP64 and double-float kernels of a split product classify every pair the same way
+__device__ __forceinline__ bool source_is_far(const double* wlo, const double* whi, double cx, double cy, double cz,
+                                              double r) {
+  const double c[3] = {cx, cy, cz};
   double d2 = 0.0;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const double g = fmax(0.0, fmax(lo[d] - whi[d], wlo[d] - hi[d]));
-    d2 += g * g;
+    const double g = fmax(0.0, fmax(__dadd_rn(wlo[d], -c[d]), __dadd_rn(c[d], -whi[d])));
+    d2 = __dadd_rn(d2, __dmul_rn(g, g));
   }
-  return d2 > kMfFarRadii * kMfFarRadii * rm * rm;
+  const double lim = __dmul_rn(kMfFarRadii, r);
+  return d2 > __dmul_rn(lim, lim);
 }
 
 __global__ void __launch_bounds__(kMfThreads)
@@ -193,6 +191,7 @@ __global__ void __launch_bounds__(kMfThreads)
                    const SphMat* __restrict__ mats, const double* __restrict__ x, double* __restrict__ y,
                    const int* __restrict__ perm, int mode) {
   __shared__ double sc[kMfChunk * 4];
+  __shared__ double srad[kMfChunk];
   __shared__ double sx[kMfChunk * kMfNu];
   const MfTile t = tiles[blockIdx.x];
   if (mask && mask[t.seg] != mask_on) return;  // realisation left out of this product
@@ -225,19 +224,17 @@ __global__ void __launch_bounds__(kMfThreads)
       sc[4 * i + 1] = cen[3 * (int64_t)h + 1];
       sc[4 * i + 2] = cen[3 * (int64_t)h + 2];
       sc[4 * i + 3] = 1.0 / rad[h];
+      srad[i] = rad[h];
     }
     for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x)
       sx[i] = x[(int64_t)kMfNu * perm[h0 + i / kMfNu] + i % kMfNu];
     __syncthreads();
-    if (mode) {
-      const int l = threadIdx.x & 31;
-      const bool far = chunk_is_far(wlo, whi, nh, l < nh ? sc[4 * l] : 0.0, l < nh ? sc[4 * l + 1] : 0.0,
-                                    l < nh ? sc[4 * l + 2] : 0.0, l < nh ? 1.0 / sc[4 * l + 3] : 0.0);
-      if (far != (mode == 2)) continue;
-    }
     if (!act) continue;
 #pragma unroll 1
     for (int hh = 0; hh < nh; ++hh) {
+      // mode 1: only the sources near the warp's targets; 2: only the far ones (warp-uniform)
+      if (mode && source_is_far(wlo, whi, sc[4 * hh], sc[4 * hh + 1], sc[4 * hh + 2], srad[hh]) != (mode == 2))
+        continue;
       const double ia = sc[4 * hh + 3];
       const double x0 = (p0 - sc[4 * hh]) * ia, x1 = (p1 - sc[4 * hh + 1]) * ia, x2 = (p2 - sc[4 * hh + 2]) * ia;
       sph_pair_apply24<double, true>(x0, x1, x2, 1.0, 0.0, 0.0, mc.tn1, mc.tn2, sx + kMfNu * hh, as * ia, acc);
@@ -315,15 +312,11 @@ __global__ void __launch_bounds__(kMfThreads)
     for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x)
       sx[i] = DF(x[(int64_t)kMfNu * perm[h0 + i / kMfNu] + i % kMfNu]);
     __syncthreads();
-    if (mode) {
-      const int l = threadIdx.x & 31;
-      const bool far = chunk_is_far(wlo, whi, nh, l < nh ? sr[4 * l] : 0.0, l < nh ? sr[4 * l + 1] : 0.0,
-                                    l < nh ? sr[4 * l + 2] : 0.0, l < nh ? sr[4 * l + 3] : 0.0);
-      if (far != (mode == 2)) continue;
-    }
     if (!act) continue;
 #pragma unroll 1
     for (int hh = 0; hh < nh; ++hh) {
+      if (mode && source_is_far(wlo, whi, sr[4 * hh], sr[4 * hh + 1], sr[4 * hh + 2], sr[4 * hh + 3]) != (mode == 2))
+        continue;
       const DF ia = sc[4 * hh + 3];
       const DF x0 = (p0 - sc[4 * hh]) * ia, x1 = (p1 - sc[4 * hh + 1]) * ia, x2 = (p2 - sc[4 * hh + 2]) * ia;
       sph_pair_apply24<DF, true>(x0, x1, x2, DF(1.0), DF(), DF(), tn1, tn2, sx + kMfNu * hh, as * ia, acc);
@@ -1101,11 +1094,11 @@ ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStrea
   ProfScope ps(PROF_MF_F64, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
   if (b.nu == 60) return mf60_apply_f64(b, x, y, st, mask, mask_on);
-  // near chunks in FP64, far chunks (beyond kMfFarRadii radii of the warp's targets) in
-  // double-float: their contributions are at most kMfFarRadii^-3 of a near one, so the
-  // double-float rounding (~2^-44 per operation) stays far below FP64 level in the sum
-  // in realisations below kMfSplitMin particles most (warp, chunk) pairs are near, and one
-  // FP64 launch over every pair is faster than the two passes
+  // near sources in FP64, far sources (beyond kMfFarRadii of their radius from the box of
+  // the warp's targets) in double-float: their contributions are at most kMfFarRadii^-3 of a
+  // near one, so the double-float rounding (~2^-44 per operation) stays far below FP64 level
+  // in the sum.  In realisations below kMfSplitMin particles most (warp, source) pairs are
+  // near, and one FP64 launch over every pair is faster than the two passes
   const bool split = b.max_seg >= kMfSplitMin;
   ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
       b.tiles, b.seg_begin, mask, mask_on, b.cen, b.rad, b.mats, x, y, b.perm, split ? 1 : 0);
