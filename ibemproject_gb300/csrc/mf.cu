@@ -48,7 +48,8 @@ namespace {
 constexpr int kMfThreads = 128;
 constexpr int kMfChunk = 32;
 constexpr double kMfFarRadii = 8.0;   // near / far split of the deciding residual
-constexpr int kMfSplitMin = 4096;     // smallest realisation (particles) that uses the split
+constexpr int kMfSplitMin = 1280;     // smallest realisation (particles) that uses the split
+constexpr int kMfSkipMin = 5000;      // from here the far pass skips near sources (256-thread CTAs)
 
 // sink of a generated block: acc[r] += v * x[c] (r, c compile-time constants after inlining)
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
@@ -151,8 +152,14 @@ __global__ void __launch_bounds__(TT)
 // their centres within each realisation (perm: position -> particle), so the 32 targets of a
 // warp form a compact cluster.  mode 0: every pair; 1: only the sources near the warp's
 // targets (within kMfFarRadii of their radius of the targets' bounding box), and the self
-// term; 2: only the far sources, no self term.  The test is per (warp, source) and
-// warp-uniform.
+// term; 2 and 3: only the far sources, no self term.  The test is per (warp, source) and
+// warp-uniform.  The double-float pair code is longer than the instruction cache: warps of
+// an SM that run it at different places each fetch their own instructions, and issue fell
+// to half when the far pass let every warp skip its own near sources.  So the far pass
+// keeps them together: mode 2 (two 128-thread CTAs per SM) evaluates every source of the
+// chunk, a warp's near ones against zero coefficients, so every CTA does the same work;
+// mode 3 (one 256-thread CTA per SM) skips them, the barrier at each chunk realigning the
+// warps of the SM.
 __device__ __forceinline__ void warp_box(bool act, double x, double y, double z, double* lo, double* hi) {
   double v[3] = {x, y, z};
 #pragma unroll
@@ -183,6 +190,43 @@ __device__ __forceinline__ bool source_is_far(const double* wlo, const double* w
   const double lim = __dmul_rn(kMfFarRadii, r);
   return d2 > __dmul_rn(lim, lim);
 }
+// The sources of one CTA (blockIdx.y of gridDim.y slices), in chunks of kMfChunk: chunk j
+// starts at first + j * step and ends at end at the latest.  The full product (mode 0) takes
+// a contiguous range of the realisation; the split ones take every gridDim.y-th chunk from
+// blockIdx.y.  In Morton order the near sources of a tile sit in a few neighbouring chunks:
+// dealt out in turn, every CTA gets about the average share of them.
+struct MfSlice {
+  int first, step, end;
+  __device__ __forceinline__ bool holds(int p) const {
+    return p >= first && p < end && (p - first) % step < kMfChunk;
+  }
+};
+__device__ __forceinline__ MfSlice mf_slice(int hb0, int he0, int mode) {
+  const int k = blockIdx.y, ns = gridDim.y;
+  if (mode) return {hb0 + kMfChunk * k, kMfChunk * ns, he0};
+  const int per = (he0 - hb0 + ns - 1) / ns;
+  const int hb = hb0 + k * per;
+  return {hb, kMfChunk, min(he0, hb + per)};
+}
+
+// Sources of the chunk at h0 (nh of them) that this warp evaluates, as a bit mask (bit i:
+// source h0 + i); the same for every lane.  Lane i classifies source i.  Evaluating the
+// selected sources in turn keeps the warps of a CTA at the same place in the long
+// straight-line pair code (instruction fetches shared), which skipping inside the loop
+// would not.
+__device__ __forceinline__ unsigned chunk_mask(int mode, bool warp_on, const double* wlo, const double* whi, int h0,
+                                               int nh, const int* __restrict__ perm, const double* __restrict__ cen,
+                                               const double* __restrict__ rad) {
+  const int lane = threadIdx.x & 31;
+  bool take = lane < nh;
+  if (mode && take) {
+    const int h = perm[h0 + lane];
+    take = source_is_far(wlo, whi, cen[3 * (int64_t)h], cen[3 * (int64_t)h + 1], cen[3 * (int64_t)h + 2], rad[h]) ==
+           (mode >= 2);
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, take);
+  return warp_on ? m : 0u;
+}
 
 __global__ void __launch_bounds__(kMfThreads)
     k_mf_apply_f64(const MfTile* __restrict__ tiles, const int* __restrict__ seg_begin,
@@ -191,14 +235,11 @@ __global__ void __launch_bounds__(kMfThreads)
                    const SphMat* __restrict__ mats, const double* __restrict__ x, double* __restrict__ y,
                    const int* __restrict__ perm, int mode) {
   __shared__ double sc[kMfChunk * 4];
-  __shared__ double srad[kMfChunk];
   __shared__ double sx[kMfChunk * kMfNu];
   const MfTile t = tiles[blockIdx.x];
   if (mask && mask[t.seg] != mask_on) return;  // realisation left out of this product
-  const int hb0 = seg_begin[t.seg], he0 = seg_begin[t.seg + 1];
-  const int per = (he0 - hb0 + gridDim.y - 1) / gridDim.y;
-  const int hb = hb0 + blockIdx.y * per, he = min(he0, hb + per);
-  if (hb >= he) return;
+  const MfSlice sl = mf_slice(seg_begin[t.seg], seg_begin[t.seg + 1], mode);
+  if (sl.first >= sl.end) return;
   const int pos = t.s0 + threadIdx.x;
   const bool act = threadIdx.x < t.ns;
   const int s = act ? perm[pos] : 0;
@@ -215,26 +256,26 @@ __global__ void __launch_bounds__(kMfThreads)
   double acc[kMfNu];
 #pragma unroll
   for (int r = 0; r < kMfNu; ++r) acc[r] = 0.0;
-  for (int h0 = hb; h0 < he; h0 += kMfChunk) {
-    const int nh = min(kMfChunk, he - h0);
-    __syncthreads();
+  const bool warp_on = __any_sync(0xffffffffu, act);
+  for (int h0 = sl.first; h0 < sl.end; h0 += sl.step) {
+    const int nh = min(kMfChunk, sl.end - h0);
+    // mode 1: the sources near the warp's targets; 2: the far ones; 0: all
+    unsigned m = chunk_mask(mode, warp_on, wlo, whi, h0, nh, perm, cen, rad);
+    if (!__syncthreads_or(m != 0u)) continue;   // no warp of the CTA needs this chunk
     for (int i = threadIdx.x; i < nh; i += blockDim.x) {
       const int h = perm[h0 + i];
       sc[4 * i] = cen[3 * (int64_t)h];
       sc[4 * i + 1] = cen[3 * (int64_t)h + 1];
       sc[4 * i + 2] = cen[3 * (int64_t)h + 2];
       sc[4 * i + 3] = 1.0 / rad[h];
-      srad[i] = rad[h];
     }
     for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x)
       sx[i] = x[(int64_t)kMfNu * perm[h0 + i / kMfNu] + i % kMfNu];
     __syncthreads();
     if (!act) continue;
 #pragma unroll 1
-    for (int hh = 0; hh < nh; ++hh) {
-      // mode 1: only the sources near the warp's targets; 2: only the far ones (warp-uniform)
-      if (mode && source_is_far(wlo, whi, sc[4 * hh], sc[4 * hh + 1], sc[4 * hh + 2], srad[hh]) != (mode == 2))
-        continue;
+    for (; m; m &= m - 1u) {
+      const int hh = __ffs(m) - 1;
       const double ia = sc[4 * hh + 3];
       const double x0 = (p0 - sc[4 * hh]) * ia, x1 = (p1 - sc[4 * hh + 1]) * ia, x2 = (p2 - sc[4 * hh + 2]) * ia;
       sph_pair_apply24<double, true>(x0, x1, x2, 1.0, 0.0, 0.0, mc.tn1, mc.tn2, sx + kMfNu * hh, as * ia, acc);
@@ -243,7 +284,7 @@ __global__ void __launch_bounds__(kMfThreads)
   if (!act) return;
   double yv[kMfNu];
   sph_pair_map24<double>(acc, mc.kmu, mc.klam, yv);
-  if (pos >= hb && pos < he && mode != 2) {
+  if (sl.holds(pos) && mode < 2) {
     MvSink<double> sk{yv, x + (int64_t)kMfNu * s};
     sph_self24(mc, sk);
   }
@@ -261,7 +302,8 @@ struct DfSink {
   __device__ __forceinline__ void operator()(int r, int c, double v) const { acc[r] += DF(v) * DF(xs[c]); }
 };
 
-__global__ void __launch_bounds__(kMfThreads)
+template <int TT>
+__global__ void __launch_bounds__(TT)
     k_mf_apply_df(const MfTile* __restrict__ tiles, const int* __restrict__ seg_begin,
                    const int* __restrict__ mask, int mask_on,
                   const double* __restrict__ cen, const double* __restrict__ rad,
@@ -269,13 +311,12 @@ __global__ void __launch_bounds__(kMfThreads)
                   const int* __restrict__ perm, int mode) {
   __shared__ DF sc[kMfChunk * 4];
   __shared__ DF sx[kMfChunk * kMfNu];
-  __shared__ double sr[kMfChunk * 4];   // FP64 centres and radii of the chunk (near / far test)
+  __shared__ DF szero[kMfNu];   // the coefficients of a skipped source in mode 2
+  if (threadIdx.x < kMfNu) szero[threadIdx.x] = DF();
   const MfTile t = tiles[blockIdx.x];
   if (mask && mask[t.seg] != mask_on) return;  // realisation left out of this product
-  const int hb0 = seg_begin[t.seg], he0 = seg_begin[t.seg + 1];
-  const int per = (he0 - hb0 + gridDim.y - 1) / gridDim.y;
-  const int hb = hb0 + blockIdx.y * per, he = min(he0, hb + per);
-  if (hb >= he) return;
+  const MfSlice sl = mf_slice(seg_begin[t.seg], seg_begin[t.seg + 1], mode);
+  if (sl.first >= sl.end) return;
   const int pos = t.s0 + threadIdx.x;
   const bool act = threadIdx.x < t.ns;
   const int s = act ? perm[pos] : 0;
@@ -295,37 +336,36 @@ __global__ void __launch_bounds__(kMfThreads)
   warp_box(act, q0, q1, q2, wlo, whi);
   const DF tn1(mc.tn1), tn2(mc.tn2);
   DF acc[kMfNu];
-  for (int h0 = hb; h0 < he; h0 += kMfChunk) {
-    const int nh = min(kMfChunk, he - h0);
-    __syncthreads();
+  const bool warp_on = __any_sync(0xffffffffu, act);
+  for (int h0 = sl.first; h0 < sl.end; h0 += sl.step) {
+    const int nh = min(kMfChunk, sl.end - h0);
+    unsigned m = chunk_mask(mode, warp_on, wlo, whi, h0, nh, perm, cen, rad);
+    if (!__syncthreads_or(m != 0u)) continue;   // no warp of the CTA needs this chunk
     for (int i = threadIdx.x; i < nh; i += blockDim.x) {
       const int h = perm[h0 + i];
-      sr[4 * i] = cen[3 * (int64_t)h];
-      sr[4 * i + 1] = cen[3 * (int64_t)h + 1];
-      sr[4 * i + 2] = cen[3 * (int64_t)h + 2];
-      sr[4 * i + 3] = rad[h];
-      sc[4 * i] = DF(sr[4 * i]);
-      sc[4 * i + 1] = DF(sr[4 * i + 1]);
-      sc[4 * i + 2] = DF(sr[4 * i + 2]);
-      sc[4 * i + 3] = DF(1.0 / sr[4 * i + 3]);
+      sc[4 * i] = DF(cen[3 * (int64_t)h]);
+      sc[4 * i + 1] = DF(cen[3 * (int64_t)h + 1]);
+      sc[4 * i + 2] = DF(cen[3 * (int64_t)h + 2]);
+      sc[4 * i + 3] = DF(1.0 / rad[h]);
     }
     for (int i = threadIdx.x; i < nh * kMfNu; i += blockDim.x)
       sx[i] = DF(x[(int64_t)kMfNu * perm[h0 + i / kMfNu] + i % kMfNu]);
     __syncthreads();
     if (!act) continue;
+    const unsigned all = nh >= 32 ? 0xffffffffu : (1u << nh) - 1u;
 #pragma unroll 1
-    for (int hh = 0; hh < nh; ++hh) {
-      if (mode && source_is_far(wlo, whi, sr[4 * hh], sr[4 * hh + 1], sr[4 * hh + 2], sr[4 * hh + 3]) != (mode == 2))
-        continue;
+    for (unsigned k = mode == 2 ? all : m; k; k &= k - 1u) {
+      const int hh = __ffs(k) - 1;
+      const DF* xs = (m >> hh) & 1u ? sx + kMfNu * hh : szero;
       const DF ia = sc[4 * hh + 3];
       const DF x0 = (p0 - sc[4 * hh]) * ia, x1 = (p1 - sc[4 * hh + 1]) * ia, x2 = (p2 - sc[4 * hh + 2]) * ia;
-      sph_pair_apply24<DF, true>(x0, x1, x2, DF(1.0), DF(), DF(), tn1, tn2, sx + kMfNu * hh, as * ia, acc);
+      sph_pair_apply24<DF, true>(x0, x1, x2, DF(1.0), DF(), DF(), tn1, tn2, xs, as * ia, acc);
     }
   }
   if (!act) return;
   DF yv[kMfNu];
   sph_pair_map24<DF>(acc, DF(mc.kmu), DF(mc.klam), yv);
-  if (pos >= hb && pos < he && mode != 2) {
+  if (sl.holds(pos) && mode < 2) {
     DfSink sk{yv, x + (int64_t)kMfNu * s};
     sph_self24(mc, sk);
   }
@@ -1102,9 +1142,14 @@ ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStrea
   const bool split = b.max_seg >= kMfSplitMin;
   ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
       b.tiles, b.seg_begin, mask, mask_on, b.cen, b.rad, b.mats, x, y, b.perm, split ? 1 : 0);
-  if (split)
-    ::ibem::count_launch(), k_mf_apply_df<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
+  if (split && b.max_seg < kMfSkipMin)
+    ::ibem::count_launch(), k_mf_apply_df<kMfThreads><<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
         b.tiles, b.seg_begin, mask, mask_on, b.cen, b.rad, b.mats, x, y, b.perm, 2);
+  else if (split)   // the same number of warps per SM, one CTA of 256 targets (tiles_s[2])
+    ::ibem::count_launch(),
+        k_mf_apply_df<2 * kMfThreads><<<dim3(b.ntiles_s[2], std::min((b.max_seg + 31) / 32, 2 * b.hsplit_wide)),
+                                         2 * kMfThreads, 0, st>>>(b.tiles_s[2], b.seg_begin, mask, mask_on, b.cen,
+                                                                  b.rad, b.mats, x, y, b.perm, 3);
   IBEM_LAUNCH_CHECK("mf apply f64");
   return IBEM_OK;
 }
@@ -1123,7 +1168,7 @@ ibem_status mf_apply_df(const MfBatch& b, const double* x, double* y, cudaStream
   ProfScope ps(PROF_MF_DF, st, 0.0);
   IBEM_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * b.N, st));
   if (b.nu == 60) return mf60_apply_f64(b, x, y, st, mask, mask_on);   // no double-float form of layout 60
-  ::ibem::count_launch(), k_mf_apply_df<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
+  ::ibem::count_launch(), k_mf_apply_df<kMfThreads><<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
       b.tiles, b.seg_begin, mask, mask_on, b.cen, b.rad, b.mats, x, y, b.perm, 0);
   IBEM_LAUNCH_CHECK("mf apply df");
   return IBEM_OK;
