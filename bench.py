@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--grid", type=int, default=64)
     ap.add_argument("--tol", type=float, default=1e-12)
     ap.add_argument("--no-plain", action="store_true", help="skip the one plain-FP64 comparison solve")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--form", default="learned_gmres", choices=["learned_gmres", "mixed_ir"])
     ap.add_argument("--train-steps", type=int, default=300)
     ap.add_argument("--batch", type=int, default=256, help="realisations of the batched measurement (0: skip)")
