@@ -47,7 +47,7 @@ namespace {
 
 constexpr int kMfThreads = 128;
 constexpr int kMfChunk = 32;
-constexpr double kMfFarRadii = 8.0;   // near / far split of the deciding residual
+constexpr double kMfFarRadii = 4.0;   // near / far split of the deciding residual
 constexpr int kMfSplitMin = 1280;     // smallest realisation (particles) that uses the split
 constexpr int kMfSkipMin = 5000;      // from here the far pass skips near sources (256-thread CTAs)
 
@@ -1136,9 +1136,11 @@ ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStrea
   if (b.nu == 60) return mf60_apply_f64(b, x, y, st, mask, mask_on);
   // near sources in FP64, far sources (beyond kMfFarRadii of their radius from the box of
   // the warp's targets) in double-float: their contributions are at most kMfFarRadii^-3 of a
-  // near one, so the double-float rounding (~2^-44 per operation) stays far below FP64 level
-  // in the sum.  In realisations below kMfSplitMin particles most (warp, source) pairs are
-  // near, and one FP64 launch over every pair is faster than the two passes
+  // touching one, so the double-float rounding (~2^-44 per operation, times 4^-3) is ~1e-15
+  // of the largest term, the level of the FP64 rounding of the near pairs (measured: split
+  // against all pairs in FP64 6.6e-16 relative, 5.2e-16 with 8 radii, 1.7e-14 for
+  // double-float everywhere).  In realisations below kMfSplitMin particles most (warp,
+  // source) pairs are near, and one FP64 launch over every pair is faster than the two passes
   const bool split = b.max_seg >= kMfSplitMin;
   ::ibem::count_launch(), k_mf_apply_f64<<<dim3(b.ntiles, b.hsplit_wide), kMfThreads, 0, st>>>(
       b.tiles, b.seg_begin, mask, mask_on, b.cen, b.rad, b.mats, x, y, b.perm, split ? 1 : 0);

@@ -58,14 +58,16 @@ def test_mf_matvec_matches_assembled_matrix(B):
         assert rel(dr[rows] * y32[rows], dr[rows] * ref) < 2e-5
 
 
-def test_split_deciding_product_matches_fp64(B):
-    """The deciding residual's product (FP64 for source chunks within 8 radii of a warp's
-    targets, double-float beyond; Morton order) against every pair in FP64, on a batch of
-    three realisations, the largest above the 4,096 particles that switch the split on and
-    large enough to have far chunks: 1e-12 relative, row by row."""
+@pytest.mark.parametrize("sizes", [(4500, 700, 33), (5200, 33)])
+def test_split_deciding_product_matches_fp64(B, sizes):
+    """The deciding residual's product (FP64 for sources near a warp's targets, double-float
+    beyond; Morton order) against every pair in FP64, row by row at 1e-12 relative.  The
+    largest realisation sets the form for the whole batch: 4,500 particles give the far pass
+    that evaluates every source (near ones against zero coefficients), 5,200 the one that
+    skips them in 256-thread CTAs."""
     import torch
     from ibemproject_gb300 import cases
-    cs = [cases.farfield_case(num=n, r0=0.012, vf=0.2, grid=0, seed=40 + n) for n in (4500, 700, 33)]
+    cs = [cases.farfield_case(num=n, r0=0.012, vf=0.2, grid=0, seed=40 + n) for n in sizes]
     bt = B.DeviceBatch(cs)
     rng = np.random.default_rng(8)
     dr, dc = bt.scalings()
