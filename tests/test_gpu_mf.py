@@ -58,7 +58,7 @@ def test_mf_matvec_matches_assembled_matrix(B):
         assert rel(dr[rows] * y32[rows], dr[rows] * ref) < 2e-5
 
 
-@pytest.mark.parametrize("sizes", [(4500, 700, 33), (5200, 33)])
+@pytest.mark.parametrize("sizes", [(4500, 700, 33, 1), (5200, 33, 1)])
 def test_split_deciding_product_matches_fp64(B, sizes):
     """The deciding residual's product (FP64 for sources near a warp's targets, double-float
     beyond; Morton order) against every pair in FP64, row by row at 1e-12 relative.  The
