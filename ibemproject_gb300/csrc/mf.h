@@ -109,9 +109,9 @@ struct MfPrecond {
   int* nbr = nullptr;    // num*kKnn neighbour indices (-1: empty slot)
 };
 // y = As x (scaled system, the deciding residual); y is overwritten.  In batches whose largest
-// realisation has 4,096 particles or more, pairs whose source lies within 8 radii (of the
-// chunk's largest sphere) of the warp's targets are evaluated in FP64 and the others in
-// double-float; below that, every pair in FP64.  Targets and sources in Morton order.
+// realisation has 1,280 particles or more, pairs whose source lies within 4 of its radii of
+// the box of the warp's targets are evaluated in FP64 and the others in double-float; below
+// that, every pair in FP64.  Targets and sources in Morton order.
 ibem_status mf_apply_f64(const MfBatch& b, const double* x, double* y, cudaStream_t st, const int* mask = nullptr,
                          int mask_on = 1);
 // the same with every pair in FP64 (the reference for the split)

@@ -252,8 +252,9 @@ typedef struct {
  * assemble for each realisation, layout 24), without storing A: every 24 x 24 pair block is
  * evaluated inside the product, on the scaled system (x and y are converted on the way in
  * and out).  precision 64: the product that decides the solver's convergence (in
- * realisations of 4,096 particles or more FP64 for the sources within 8 radii of a warp's
- * 32 targets and double-float beyond, within 1e-12 of FP64; FP64 throughout below that);
+ * batches whose largest realisation has 1,280 particles or more, FP64 for the sources within
+ * 4 of their radii of a warp's 32 targets and double-float beyond: measured within 1e-15
+ * norm-wise of every pair in FP64; FP64 throughout below that);
  * 65: every pair in FP64; 48: double-float (FP32 pairs, ~48 bits, several times faster on
  * GB300); 32: FP32, about 1e-6 relative, in the tile shape the autotuner picks for the
  * solver (ibem_e3d_mf_tile_shape).  x_dev, y_dev: 24 * seg_begin[nseg] doubles. */
