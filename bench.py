@@ -212,7 +212,7 @@ def sm_count():
 
 def roofline_chosen(prof, case):
     """Roofline of the largest stage of the matrix-free step, the split stress sums
-    (field24_far, FP32 beyond 14 radii of a warp's points, and field24_near, double-float
+    (field24_far, FP32 beyond 12 radii of a warp's points, and field24_near, double-float
     within): FP32-pipe bound.  Algorithmic work = FIELD_ALG_FLOPS_PER_PAIR, the FP32 flops of
     the contracted strain of one (point, sphere) pair, x the pairs of one call, over the
     event-timed duration of the call (the two kernels plus the Morton sort of the points);
@@ -251,9 +251,9 @@ def roofline_chosen(prof, case):
 # whose points are far from every sphere, 2.431e10 flops / 6.554e7 pairs).
 FIELD_ALG_FLOPS_PER_PAIR = 370.9
 # Executed FP32 flops per pair on this workload (the same count over both kernels of one
-# full-size call: 1.640e11 far + 2.271e11 near = 3.911e11 / 5.243e8 pairs) and the call's
-# DRAM bytes (read + write of both kernels) from the same capture.
-FIELD_DF_FLOPS_PER_PAIR = 745.9
+# full-size call, double-float within 12 radii: 1.731e11 far + 1.592e11 near = 3.323e11 /
+# 5.243e8 pairs) and the call's DRAM bytes (read + write of both kernels) from the same capture.
+FIELD_DF_FLOPS_PER_PAIR = 633.8
 FIELD_DF_TRAFFIC_PER_LAUNCH = 43.59e6
 FIELD_DF_SOURCE = "profiles/field24_far_near_bench2000.md"
 

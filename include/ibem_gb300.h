@@ -502,7 +502,7 @@ ibem_status ibem_e3d_field(const double* points_dev, int nump, const double* cen
 /* ibem_e3d_field with a precision choice (no counterpart in the reference, which has one
  * precision).  IBEM_SOLVE_FP64 is ibem_e3d_field.  IBEM_SOLVE_MIXED_IR runs the sphere
  * sums of the 24-unknown layout in double-float arithmetic (pairs of FP32 numbers, about
- * 48 significant bits) for spheres within 14 radii of a warp's points and in FP32 beyond
+ * 48 significant bits) for spheres within 12 radii of a warp's points and in FP32 beyond
  * (agrees with the FP64 sums to ~1e-9 of the strain), which GB300 executes several times
  * faster than FP64; the 60/78 layouts and the boundary part stay FP64.
  * ibem_e3d_run_host / ibem_e3d_run_dir use the form given to them here too. */

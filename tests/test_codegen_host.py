@@ -235,16 +235,17 @@ def test_pair_apply_matches_generated_block(hg, fp32):
 
 def test_field24_f32_far_pairs(hg):
     """The FP32 far-pair contraction of the mixed stress sums against the FP64 contraction:
-    beyond 14 radii its relative error stays at the FP32 rounding level (< 3e-6 of the
-    largest strain component), and its size relative to a contact-distance sphere is below
-    (1/14)^3, which is what bounds its share of the summed error."""
+    beyond 12 radii (the split's threshold) its relative error stays at the FP32 rounding
+    level (< 3e-6 of the largest strain component), and its size relative to a
+    contact-distance sphere is below (1/12)^3, which is what bounds its share of the summed
+    error."""
     rng = np.random.default_rng(21)
     worst = 0.0
     for t in range(200):
         a = 0.012 * (0.8 + 0.4 * rng.random())
         cen = rng.random(3) * 0.4
         x = rng.normal(size=3)
-        x *= a * (14.0 + 30.0 * rng.random()) / np.linalg.norm(x)
+        x *= a * (12.0 + 30.0 * rng.random()) / np.linalg.norm(x)
         E = rng.normal(size=24) * 1e-3
         E[6:] /= a
         e1, e2 = np.zeros(6), np.zeros(6)

@@ -223,7 +223,7 @@ def test_tensor_core_gemm(g, m, n, k):
 @pytest.mark.gpu
 def test_field_double_float_vs_fp64_and_oracle(g, oracle_mod):
     """Stresses of the 24-unknown layout: the FP64 sums match the oracle to 1e-11 and the
-    split sums of the mixed form (ibem_e3d_field_form: double-float for spheres within 14
+    split sums of the mixed form (ibem_e3d_field_form: double-float for spheres within 12
     radii of a warp's points, FP32 beyond) to 1e-9 (scaled), with points inside, near and
     far from the spheres.  The FP32 share is designed for ~1e-9 of the strain (random-sign
     coefficients, as here, are its worst case); the solution target is 1e-8."""

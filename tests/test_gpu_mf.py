@@ -581,7 +581,7 @@ def test_full_size_2000_spheres_matrix_free_matches_dense_mixed(B):
 
 def test_full_size_2000_spheres_split_stress_sums(B):
     """The headline workload's stresses at full size (2,000 spheres x 64^3 = 262,144 points)
-    from its matrix-free solution: the split sums of the mixed form (double-float within 14
+    from its matrix-free solution: the split sums of the mixed form (double-float within 12
     radii of a warp's points, FP32 beyond, Morton-ordered points) against the FP64 sums,
     within the 1e-8 the solution is measured at (max-norm, scaled by the largest stress)."""
     import ctypes
